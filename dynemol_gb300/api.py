@@ -1,0 +1,270 @@
+"""Python mirror of the C ABI of libelhlprop.so (include/elhl_prop.h).
+
+Two layers, matching the library:
+
+* the drop-in symbols with the reference's by-reference calling convention:
+  ``propagationelhl_gpucaller`` (Taylor_gpu.cpp:634-736) and
+  ``propagation_gpucaller`` (Taylor_gpu.cpp:295-330), plus ``gpu_init`` /
+  ``gpu_finalize`` / ``gpu_pin`` / ``gpu_unpin`` (GPU_Interface.cpp:226-302);
+* :class:`Trajectory`, the device-resident electron-hole trajectory whose
+  ``step`` is one or more calls of ElHl_Chebyshev (ElHl_Chebyshev.f:148-291).
+
+The library must be built (``dynemol_gb300.build.build()``); loading fails
+loudly otherwise -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libelhlprop.so")
+
+# status codes (elhl_prop.h)
+OK, ERR_BAD_ARG, ERR_NO_CONVERGENCE, ERR_TIMEOUT, ERR_OOM, ERR_CUDA, ERR_NOT_PD, ERR_NO_DEVICE, ERR_UNSUPPORTED = range(9)
+METHOD_TAYLOR_REF, METHOD_CHEBYSHEV = 0, 1
+PREC_FP64, PREC_FP32, PREC_BF16X3 = 0, 1, 2
+
+EXPORTED_SYMBOLS = (
+    "gpu_init_", "gpu_finalize_", "gpu_pin_", "gpu_unpin_", "propagation_gpucaller_",
+    "propagationelhl_gpucaller_", "elhl_last_status", "elhl_status_string", "elhl_traj_config_default",
+    "elhl_traj_create", "elhl_traj_destroy", "elhl_traj_init_fmo", "elhl_traj_set_psi", "elhl_traj_get_psi", "elhl_traj_step",
+    "elhl_traj_step_device", "elhl_traj_get_matrices", "elhl_traj_get_stats", "elhl_device_count",
+    "elhl_sm_count", "elhl_set_stream",
+)
+
+
+class ElhlError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        self.status = status
+        super().__init__(f"{where}: {status_string(status)} (status {status})")
+
+
+class BasisDesc(ctypes.Structure):
+    _fields_ = [("natoms", ctypes.c_int), ("nao", ctypes.c_int)] + [
+        (n, ctypes.c_void_p) for n in ("atom_ao0", "atom_nao", "ao_n", "ao_l", "ao_m", "ao_nzeta", "ao_zeta",
+                                       "ao_coef", "ao_ip", "ao_kwh", "ao_vshift", "ao_frag")] + [("nfrag", ctypes.c_int)]
+
+
+class TrajConfig(ctypes.Structure):
+    _fields_ = [("method", ctypes.c_int), ("precision", ctypes.c_int), ("dt", ctypes.c_double),
+                ("frame_step", ctypes.c_int), ("tol", ctypes.c_double), ("norm_tol", ctypes.c_double),
+                ("cheb_tol", ctypes.c_double), ("cutoff", ctypes.c_double), ("max_conv_calls", ctypes.c_int),
+                ("ncols", ctypes.c_int)]
+
+
+class TrajStats(ctypes.Structure):
+    _fields_ = [("orders", ctypes.c_longlong), ("conv_calls", ctypes.c_longlong), ("substeps", ctypes.c_longlong),
+                ("save_tau", ctypes.c_double * 2), ("t", ctypes.c_double), ("it", ctypes.c_int),
+                ("status", ctypes.c_int), ("prop_ms", ctypes.c_double), ("rebuild_ms", ctypes.c_double),
+                ("prop_launches", ctypes.c_int), ("rebuild_count", ctypes.c_int)]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libelhlprop.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: run dynemol_gb300.build.build() (no CPU fallback exists)")
+    L = ctypes.CDLL(path)
+    vp, ip, dp, ci = ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double), ctypes.c_int
+    L.gpu_init_.argtypes = [ip, ip]
+    L.gpu_init_.restype = None
+    L.gpu_finalize_.argtypes = []
+    L.gpu_finalize_.restype = None
+    L.gpu_pin_.argtypes = [vp, ip]
+    L.gpu_pin_.restype = None
+    L.gpu_unpin_.argtypes = [vp]
+    L.gpu_unpin_.restype = None
+    L.propagation_gpucaller_.argtypes = [ip, dp, dp, dp, dp, vp, vp, vp]
+    L.propagation_gpucaller_.restype = None
+    L.propagationelhl_gpucaller_.argtypes = [ip, vp, vp, vp, vp, vp, vp, vp, dp, dp, dp, dp]
+    L.propagationelhl_gpucaller_.restype = None
+    L.elhl_last_status.restype = ci
+    L.elhl_status_string.argtypes = [ci]
+    L.elhl_status_string.restype = ctypes.c_char_p
+    L.elhl_traj_config_default.argtypes = [ctypes.POINTER(TrajConfig)]
+    L.elhl_traj_config_default.restype = None
+    L.elhl_traj_create.argtypes = [ctypes.POINTER(BasisDesc), vp, ctypes.POINTER(TrajConfig), ctypes.POINTER(vp)]
+    L.elhl_traj_destroy.argtypes = [vp]
+    L.elhl_traj_init_fmo.argtypes = [vp, ci, vp, ci, ci, vp, ci]
+    L.elhl_traj_set_psi.argtypes = [vp, vp, vp]
+    L.elhl_traj_get_psi.argtypes = [vp, vp, vp]
+    L.elhl_traj_step.argtypes = [vp, vp, ci, vp]
+    L.elhl_traj_step_device.argtypes = [vp, vp, ci, vp]
+    L.elhl_traj_get_matrices.argtypes = [vp, vp, vp, vp]
+    L.elhl_traj_get_stats.argtypes = [vp, ctypes.POINTER(TrajStats)]
+    L.elhl_device_count.restype = ci
+    L.elhl_sm_count.restype = ci
+    L.elhl_set_stream.argtypes = [vp]
+    for s in EXPORTED_SYMBOLS:
+        getattr(L, s)
+    _lib = L
+    return L
+
+
+def status_string(status: int) -> str:
+    return load().elhl_status_string(int(status)).decode()
+
+
+def _p(a):
+    return None if a is None else ctypes.c_void_p(a.ctypes.data)
+
+
+def _check(rc: int, where: str):
+    if rc != OK:
+        raise ElhlError(rc, where)
+
+
+# ---------------------------------------------------------------- drop-in
+def gpu_init(myid: int = 0, procs_per_dev: int = 1):
+    L = load()
+    L.gpu_init_(ctypes.byref(ctypes.c_int(myid)), ctypes.byref(ctypes.c_int(procs_per_dev)))
+    _check(L.elhl_last_status(), "gpu_init_")
+
+
+def gpu_finalize():
+    load().gpu_finalize_()
+
+
+def gpu_pin(arr: np.ndarray):
+    L = load()
+    L.gpu_pin_(_p(arr), ctypes.byref(ctypes.c_int(arr.nbytes)))
+    _check(L.elhl_last_status(), "gpu_pin_")
+
+
+def gpu_unpin(arr: np.ndarray):
+    L = load()
+    L.gpu_unpin_(_p(arr))
+    _check(L.elhl_last_status(), "gpu_unpin_")
+
+
+def propagationelhl_gpucaller(S, h, psi_bra, psi_ket, t_init, t_max, tau):
+    """One particle, one nuclear step, reference semantics.
+
+    Returns (H', AO_bra, psi_bra, psi_ket, save_tau); psi arrays are updated in place."""
+    L = load()
+    N = S.shape[0]
+    S = np.asfortranarray(S, np.float64)
+    h = np.asfortranarray(h, np.float64)
+    Hp = np.zeros((N, N), order="F")
+    ao_bra = np.zeros(N, np.complex128)
+    ao_ket = np.zeros(N, np.complex128)
+    assert psi_bra.dtype == np.complex128 and psi_bra.flags.c_contiguous
+    assert psi_ket.dtype == np.complex128 and psi_ket.flags.c_contiguous
+    tau_c, st = ctypes.c_double(tau), ctypes.c_double(0.0)
+    L.propagationelhl_gpucaller_(ctypes.byref(ctypes.c_int(N)), _p(S), _p(h), _p(Hp), _p(ao_bra), _p(ao_ket),
+                                 _p(psi_bra), _p(psi_ket), ctypes.byref(ctypes.c_double(t_init)),
+                                 ctypes.byref(ctypes.c_double(t_max)), ctypes.byref(tau_c), ctypes.byref(st))
+    _check(L.elhl_last_status(), "propagationelhl_gpucaller_")
+    return Hp, ao_bra, psi_bra, psi_ket, st.value
+
+
+def propagation_gpucaller(Hp, psi_bra, psi_ket, t_init, t_max, tau):
+    L = load()
+    N = Hp.shape[0]
+    Hp = np.asfortranarray(Hp, np.float64)
+    tau_c, st = ctypes.c_double(tau), ctypes.c_double(0.0)
+    L.propagation_gpucaller_(ctypes.byref(ctypes.c_int(N)), ctypes.byref(tau_c), ctypes.byref(st),
+                             ctypes.byref(ctypes.c_double(t_init)), ctypes.byref(ctypes.c_double(t_max)),
+                             _p(psi_bra), _p(psi_ket), _p(Hp))
+    _check(L.elhl_last_status(), "propagation_gpucaller_")
+    return psi_bra, psi_ket, st.value
+
+
+# ---------------------------------------------------------------- trajectories
+def default_config(**kw) -> TrajConfig:
+    c = TrajConfig()
+    load().elhl_traj_config_default(ctypes.byref(c))
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+class Trajectory:
+    """Device-resident electron-hole trajectory (S, h, H', Psi live in HBM)."""
+
+    def __init__(self, system, coords=None, config: TrajConfig | None = None, **cfg_kw):
+        L = load()
+        self.sys = system
+        self._keep = [system.atom_ao0, system.atom_nao, system.ao_n, system.ao_l, system.ao_m, system.ao_nzeta,
+                      system.ao_zeta, system.ao_coef, system.ao_ip, system.ao_kwh, system.ao_vshift, system.ao_frag]
+        self.desc = BasisDesc(system.natoms, system.nao, *[_p(a) for a in self._keep], system.nfrag)
+        self.config = config if config is not None else default_config(**cfg_kw)
+        c = np.ascontiguousarray(system.coords if coords is None else coords, np.float64)
+        h = ctypes.c_void_p()
+        _check(L.elhl_traj_create(ctypes.byref(self.desc), _p(c), ctypes.byref(self.config), ctypes.byref(h)),
+               "elhl_traj_create")
+        self.handle = h
+        self.N = system.nao
+        self.P = 2
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().elhl_traj_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init_fmo(self, electron_state: int, hole_state: int):
+        """Initial electron / hole states from the El / Hl fragment MOs (1-based)."""
+        el = np.ascontiguousarray(self.sys.fragment_atoms("E"), np.int32)
+        hl = np.ascontiguousarray(self.sys.fragment_atoms("H"), np.int32)
+        _check(load().elhl_traj_init_fmo(self.handle, len(el), _p(el), electron_state, len(hl), _p(hl), hole_state),
+               "elhl_traj_init_fmo")
+
+    def set_psi(self, psi_bra, psi_ket):
+        b = np.asfortranarray(psi_bra, np.complex128)
+        k = np.asfortranarray(psi_ket, np.complex128)
+        _check(load().elhl_traj_set_psi(self.handle, _p(b), _p(k)), "elhl_traj_set_psi")
+
+    def get_psi(self):
+        b = np.zeros((self.N, self.P), np.complex128, order="F")
+        k = np.zeros((self.N, self.P), np.complex128, order="F")
+        _check(load().elhl_traj_get_psi(self.handle, _p(b), _p(k)), "elhl_traj_get_psi")
+        return b, k
+
+    def step(self, coords=None, nsteps: int = 1, want_pops: bool = True):
+        """nsteps nuclear steps; coords None = fixed nuclei, else (nsteps, natoms, 3).
+        Returns populations (nsteps, P, nfrag+1) or None."""
+        pops = np.zeros((nsteps, self.P, self.sys.nfrag + 1)) if want_pops else None
+        c = None if coords is None else np.ascontiguousarray(coords, np.float64)
+        if c is not None and c.size != nsteps * self.sys.natoms * 3:
+            raise ValueError("coords must hold nsteps * natoms * 3 values")
+        _check(load().elhl_traj_step(self.handle, _p(c), nsteps, _p(pops)), "elhl_traj_step")
+        return pops
+
+    def step_device(self, d_coords_ptr: int, nsteps: int, d_pops_ptr: int):
+        """Device-pointer variant (pointers as integers)."""
+        _check(load().elhl_traj_step_device(self.handle, ctypes.c_void_p(d_coords_ptr), nsteps,
+                                            ctypes.c_void_p(d_pops_ptr)), "elhl_traj_step_device")
+
+    def matrices(self):
+        N = self.N
+        S, h, Hp = (np.zeros((N, N), order="F") for _ in range(3))
+        _check(load().elhl_traj_get_matrices(self.handle, _p(S), _p(h), _p(Hp)), "elhl_traj_get_matrices")
+        return S, h, Hp
+
+    def stats(self) -> TrajStats:
+        st = TrajStats()
+        _check(load().elhl_traj_get_stats(self.handle, ctypes.byref(st)), "elhl_traj_get_stats")
+        return st
+
+
+def set_stream(stream_handle: int | None):
+    """Route library work to a caller stream (integer cudaStream_t) or back to its own (None)."""
+    _check(load().elhl_set_stream(ctypes.c_void_p(stream_handle) if stream_handle else None), "elhl_set_stream")
+
+
+def device_count() -> int:
+    return int(load().elhl_device_count())

@@ -1,0 +1,299 @@
+// Device build of the STO overlap S and the extended-Hueckel h for one
+// nuclear configuration.
+//
+// One thread per atom pair (ia >= ib).  Each thread writes its whole AO
+// block of S and h and the transposed block, so every element of the two
+// N x N matrices is written exactly once (no memset, no atomics).
+//
+//   lined-up overlaps ... SOLAP (overlap_D.f:701-962): Fernandez-Rico 1F1
+//                         expansion of <n00|n'00>, then recurrences in l, l', m
+//   rotation ............ ROTAR for l <= 1 (overlap_D.f:983-1027), gamma = 0
+//   normalisation ....... GET_ANOR / GET_ANOR_DIVISOR (overlap_D.f:464-517)
+//   assembly ............ BUILD_OVERLAP_MATRIX (overlap_D.f:228-291), diag 1
+//   Hueckel ............. h_ij = X_ij S_ij, weighted Wolfsberg-Helmholz
+//                         (hamiltonians.f:33-63, ElHl_Chebyshev.f:313-321)
+//
+// Supported basis: n <= 3, l <= 1, one or two zetas (the H/C/O EHT basis of
+// the workloads).  Table values re(i)=i and reali(i)=1/i are evaluated
+// inline; they are the same IEEE values the reference tabulates.
+#include "elhl_internal.cuh"
+
+namespace elhl {
+namespace {
+
+constexpr int kMaxN = 3;
+constexpr int kMaxL = 1;
+constexpr int kNT = kMaxN + 3 * kMaxL + 1;  // n index bound: na + la + 2 lb <= 6 -> 7 entries
+constexpr int kHR = kNT + 2;                // 1F1 rows (alpha up to namax + 1)
+constexpr int kHC = 2 * kNT + 2;            // 1F1 columns (gamma up to ngmax)
+
+__device__ __forceinline__ double rcp_int(int i) { return i == 0 ? 0.0 : 1.0 / (double)i; }
+
+__device__ double dfact(int n) {
+    double f = 1.0;
+    for (int i = 1; i <= n; ++i) f = f * (double)i;
+    return f;
+}
+
+// <na la m | nb lb m>, m = 0..min(la, lb), lined-up frame.  Returns false on
+// quantum numbers outside the supported range.
+__device__ bool lined_up_overlap(int na, int la, double za, int nb, int lb, double zb, double R,
+                                 double *sol) {
+    if (na < 1 || nb < 1 || na > kMaxN || nb > kMaxN || la > kMaxL || lb > kMaxL) return false;
+    double h1f1[kHR][kHC];
+    double smat[kNT][kNT], saux_l[kNT][kNT], sbase[kNT][kNT];
+
+    const bool a_big = (za >= zb);
+    int nmin, nmax, npmin, npmax;
+    double z, zp;
+    if (a_big) {
+        nmin = na - la; nmax = na + la + 2 * lb; npmin = nb - lb; npmax = nb + lb + 2 * la;
+        z = za; zp = zb;
+    } else {
+        nmin = nb - lb; nmax = nb + lb + 2 * la; npmin = na - la; npmax = na + la + 2 * lb;
+        z = zb; zp = za;
+    }
+    const double expzR = exp(-z * R);
+    const int ngmax = nmax + npmax + 2;
+    const int namax = npmax + 1;
+    const double arg = (z - zp) * R;
+    int ia = (ngmax - (int)z) / 2;
+    if (ia < 1) ia = 1;
+    if (ia >= namax) ia = namax - 1;
+
+    // 1F1[ia, ngmax, arg] and 1F1[ia+1, ngmax, arg] by their series
+    double ta = arg * (double)ia * rcp_int(ngmax), fa = 1.0;
+    double tb = arg * (double)(ia + 1) * rcp_int(ngmax), fb = 1.0;
+    const int imax = 1000 - ngmax - 1;
+    for (int i = 1; i <= imax; ++i) {
+        fa = fa + ta;
+        fb = fb + tb;
+        ta = ta * (double)(ia + i) * arg * rcp_int(ngmax + i) * rcp_int(i + 1);
+        tb = tb * (double)(ia + i + 1) * arg * rcp_int(ngmax + i) * rcp_int(i + 1);
+        if (tb < 1.0e-35 * fb) break;
+    }
+    h1f1[ia][ngmax] = fa;
+    h1f1[ia + 1][ngmax] = fb;
+    double aux = arg - (double)ngmax;
+    for (int i = ia + 1; i <= namax - 1; ++i)
+        h1f1[i + 1][ngmax] = ((aux + (double)(i + i)) * h1f1[i][ngmax] + (double)(ngmax - i) * h1f1[i - 1][ngmax]) * rcp_int(i);
+    for (int i = ia; i >= 2; --i)
+        h1f1[i - 1][ngmax] = ((double)i * h1f1[i + 1][ngmax] - (aux + (double)(i + i)) * h1f1[i][ngmax]) * rcp_int(ngmax - i);
+    for (int j = ngmax - 1; j >= 2; --j) {
+        h1f1[1][j] = (h1f1[2][j + 1] + (double)(j - 1) * h1f1[1][j + 1]) * rcp_int(j);
+        aux = arg * rcp_int(j);
+        const int itop = min(namax - 1, j - 2);
+        for (int i = 1; i <= itop; ++i) h1f1[i + 1][j] = aux * h1f1[i + 1][j + 1] + h1f1[i][j];
+    }
+
+    // basic integrals <N00|N'00>
+    {
+        const double pi4 = 12.566370614359172953850573533118012;
+        const double zzpR = (z + zp) * R;
+        const double zzpi = 1.0 / (z + zp);
+        double zzpin = 1.0;
+        for (int e = 0; e < nmin + npmin + 1; ++e) zzpin *= zzpi;
+        for (int n = nmin; n <= nmax; ++n) {
+            double zzpinp = zzpin;
+            for (int np = npmin; np <= npmax - n + nmin; ++np) {
+                double auxk = dfact(n + np) * zzpinp;
+                double sumk = 0.0;
+                for (int k = 0; k <= n + np; ++k) {
+                    double sumj = 0.0;
+                    for (int j = max(0, k - n); j <= min(k, np); ++j)
+                        sumj = sumj + h1f1[j + 1][k + 2] * (1.0 / dfact(n + j - k)) * (1.0 / dfact(np - j));
+                    sumk = sumk + sumj * auxk;
+                    auxk = auxk * zzpR * rcp_int(n + np - k) * rcp_int(k + 2);
+                }
+                const double v = pi4 * expzR * dfact(n) * dfact(np) * sumk;
+                const int r0 = a_big ? n : np, r1 = a_big ? np : n;
+                smat[r0][r1] = v;
+                saux_l[r0][r1] = v;
+                sbase[r0][r1] = v;
+                zzpinp = zzpinp * zzpi;
+            }
+            zzpin = zzpin * zzpi;
+        }
+    }
+
+    nmin = na - la; nmax = na + la + 2 * lb; npmin = nb - lb; npmax = nb + lb + 2 * la;
+    const double Rinv = 1.0 / R, R2 = R * R, R4 = R2 * R2;
+    double m0 = 0.5;
+    const int mtop = min(la, lb);
+    for (int m = 0; m <= mtop; ++m) {
+        if (la > m) {  // raise l on A (l = m -> m+1; l <= 1 so no second rung)
+            for (int np = npmin; np <= npmax - 2; ++np) {
+                double prev = smat[nmin][np];
+                for (int n = nmin + 1; n <= nmax - 1 - np + npmin; ++n) {
+                    const double v = (double)(m + m + 1) * 0.5 * Rinv * (smat[n + 1][np] + R2 * prev - smat[n - 1][np + 2]);
+                    prev = smat[n][np];
+                    saux_l[n][np] = prev;
+                    smat[n][np] = v;
+                }
+            }
+        }
+        if (lb > m) {  // raise l' on B
+            for (int n = nmin + la - m; n <= nmax - la + m - 2; ++n) {
+                double prev = smat[n][npmin];
+                for (int np = npmin + 1; np <= npmax - 2 * (la - m) - n + nmin + la - m - 1; ++np) {
+                    const double v = -(double)(m + m + 1) * 0.5 * Rinv * (smat[n][np + 1] + R2 * prev - smat[n + 2][np - 1]);
+                    prev = smat[n][np];
+                    saux_l[n][np] = prev;
+                    smat[n][np] = v;
+                }
+            }
+        }
+        sol[m] = smat[na][nb];
+        if (m == mtop) break;
+        nmin += 1; nmax -= 3; npmin += 1; npmax -= 3;
+        aux = m0 * 0.25 * (double)(m + m + 1) * (double)(m + m + 1) * Rinv * Rinv;
+        for (int n = nmin; n <= nmax; ++n)
+            for (int np = npmin; np <= npmax - n + nmin; ++np)
+                saux_l[n][np] = aux * (2.0 * (sbase[n + 1][np + 1] + R2 * (sbase[n + 1][np - 1] + sbase[n - 1][np + 1])) -
+                                       sbase[n + 3][np - 1] - sbase[n - 1][np + 3] - R4 * sbase[n - 1][np - 1]);
+        for (int n = nmin; n <= nmax; ++n)
+            for (int np = npmin; np <= npmax - n + nmin; ++np) {
+                smat[n][np] = saux_l[n][np];
+                sbase[n][np] = saux_l[n][np];
+            }
+        m0 = 1.0;
+    }
+    return true;
+}
+
+__device__ __forceinline__ double anor(double ea, double eb, int na, int nb, int la, int lb, double aux) {
+    double a = 1.0;
+    for (int e = 0; e < 2 * na + 1; ++e) a *= ea * 2.0;
+    double b = 1.0;
+    for (int e = 0; e < 2 * nb + 1; ++e) b *= eb * 2.0;
+    double v = a * b;
+    v = v * (la * 2 + 1.0);
+    v = v * (lb * 2 + 1.0);
+    v = v * aux;
+    const double PI = 4.0 * atan(1.0);
+    return sqrt(v) / (4.0 * PI);
+}
+
+__device__ __forceinline__ double x_ij(double ipi, double ipj, double vi, double vj, double ki, double kj) {
+    const double c1 = ipi - ipj, c2 = ipi + ipj;
+    const double c3 = (c1 / c2) * (c1 / c2);
+    const double c4 = (vi + vj) * 0.5;
+    const double k = (ki + kj) * 0.5;
+    const double keff = k + c3 + c3 * c3 * (1.0 - k);
+    return keff * c2 * 0.5 + c4;
+}
+
+__global__ void build_sh_kernel(DevBasis b, const double *__restrict__ coords, double cutoff,
+                                double *__restrict__ S, double *__restrict__ h, int ld) {
+    const int ia = blockIdx.y * blockDim.y + threadIdx.y;
+    const int ib = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ia >= b.natoms || ib >= b.natoms || ib > ia) return;
+    const int a0 = b.atom_ao0[ia], na_ao = b.atom_nao[ia];
+    const int b0 = b.atom_ao0[ib], nb_ao = b.atom_nao[ib];
+
+    if (ia == ib) {  // diagonal block: S = 1, h = IP + V_shift; same-atom off-diagonals 0
+        for (int jb = 0; jb < nb_ao; ++jb)
+            for (int ja = 0; ja < na_ao; ++ja) {
+                const int r = a0 + ja, c = b0 + jb;
+                const size_t o = (size_t)c * ld + r;
+                S[o] = (r == c) ? 1.0 : 0.0;
+                h[o] = (r == c) ? b.ao_ip[r] + b.ao_vshift[r] : 0.0;
+            }
+        return;
+    }
+
+    // B - A vector, lined-up frame (ROTATIONOVERLAP, overlap_D.f:558-574)
+    const double xab = coords[3 * ib] - coords[3 * ia];
+    const double yab = coords[3 * ib + 1] - coords[3 * ia + 1];
+    const double zab = coords[3 * ib + 2] - coords[3 * ia + 2];
+    const double xy = sqrt(xab * xab + yab * yab);
+    double sinal = 0.0, cosal = 1.0;
+    if (xy > 1.0e-10) {
+        sinal = yab / xy;
+        cosal = xab / xy;
+    }
+    const double R = sqrt(xab * xab + yab * yab + zab * zab);
+    const bool inside = !(R > cutoff);
+
+    // rotation matrices r(m, m'; l) for l = 0, 1: rot[l][m+1][m'+1]
+    double rot[2][3][3];
+    if (inside) {
+        const double sinbet = xy / R, cosbet = zab / R;
+        const double root2 = 1.414213562373095;  // literal used by ROTAR
+        const double d11 = (1.0 + cosbet) * 0.5, d10 = -sinbet / root2, d1m = (1.0 - cosbet) * 0.5;
+        const double d01 = -d10, d00 = d11 - d1m;
+        for (int l = 0; l < 2; ++l)
+            for (int i = 0; i < 3; ++i)
+                for (int j = 0; j < 3; ++j) rot[l][i][j] = 0.0;
+        rot[0][1][1] = 1.0;
+        rot[1][1][1] = d00;
+        rot[1][2][1] = root2 * d01 * cosal;
+        rot[1][0][1] = root2 * d01 * sinal;
+        rot[1][1][2] = root2 * d10;
+        rot[1][1][0] = -root2 * d10 * 0.0;
+        rot[1][2][2] = d11 * cosal - d1m * cosal;
+        rot[1][2][0] = -d11 * sinal - d1m * sinal;
+        rot[1][0][2] = d11 * sinal - d1m * sinal;
+        rot[1][0][0] = d11 * cosal + d1m * cosal;
+    }
+
+    for (int jb = 0; jb < nb_ao; ++jb) {
+        const int bb = b0 + jb;
+        for (int ja = 0; ja < na_ao; ++ja) {
+            const int aa = a0 + ja;
+            double s = 0.0;
+            if (inside) {
+                const int na = b.ao_n[aa], la = b.ao_l[aa], ma = b.ao_m[aa];
+                const int nb = b.ao_n[bb], lb = b.ao_l[bb], mb = b.ao_m[bb];
+                const double aux = 1.0 / (dfact(na + na) * dfact(nb + nb));
+                const int msup = min(la, lb);
+                double solnorm[kMaxL + 1] = {0.0, 0.0};
+                for (int j = 0; j < b.ao_nzeta[bb]; ++j) {
+                    for (int i = 0; i < b.ao_nzeta[aa]; ++i) {
+                        const double eb = b.ao_zeta[2 * bb + j], ea = b.ao_zeta[2 * aa + i];
+                        double sol[kMaxL + 1];
+                        if (!lined_up_overlap(na, la, ea, nb, lb, eb, R, sol)) {
+                            sol[0] = sol[1] = __longlong_as_double(0x7ff8000000000000ULL);  // NaN marks unsupported
+                        }
+                        double an = anor(ea, eb, na, nb, la, lb, aux);
+                        double part[kMaxL + 1];
+                        for (int m = 0; m <= msup - 1; ++m) {
+                            part[m] = sol[m] * an;
+                            an = an / sqrt((la + m + 1.0) * (la - m) * (lb + m + 1.0) * (lb - m));
+                            if (m == 0) an = an + an;
+                        }
+                        part[msup] = sol[msup] * an;
+                        const double cc = b.ao_coef[2 * aa + i] * b.ao_coef[2 * bb + j];
+                        for (int k = 0; k <= msup; ++k) solnorm[k] = solnorm[k] + cc * part[k];
+                    }
+                }
+                double sux0 = solnorm[0] * rot[la][ma + 1][1] * rot[lb][mb + 1][1];
+                s = sux0;
+                if (msup >= 1) {
+                    const double sux1 = solnorm[1] * (rot[la][ma + 1][0] * rot[lb][mb + 1][0] +
+                                                      rot[la][ma + 1][2] * rot[lb][mb + 1][2]);
+                    s = s + sux1;
+                }
+            }
+            const double hv = x_ij(b.ao_ip[aa], b.ao_ip[bb], b.ao_vshift[aa], b.ao_vshift[bb], b.ao_kwh[aa],
+                                   b.ao_kwh[bb]) * s;
+            S[(size_t)bb * ld + aa] = s;
+            S[(size_t)aa * ld + bb] = s;
+            h[(size_t)bb * ld + aa] = hv;
+            h[(size_t)aa * ld + bb] = hv;
+        }
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_build_sh(const DevBasis &b, const double *d_coords, double cutoff, double *d_S,
+                            double *d_h, int ld, cudaStream_t st) {
+    if (b.natoms <= 0) return cudaSuccess;
+    dim3 block(16, 8);
+    dim3 grid((b.natoms + block.x - 1) / block.x, (b.natoms + block.y - 1) / block.y);
+    build_sh_kernel<<<grid, block, 0, st>>>(b, d_coords, cutoff, d_S, d_h, ld);
+    return cudaGetLastError();
+}
+
+}  // namespace elhl

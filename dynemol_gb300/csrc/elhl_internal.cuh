@@ -1,0 +1,77 @@
+// Internal declarations shared by the translation units of libelhlprop.so.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+
+#include "../../include/elhl_prop.h"
+
+namespace elhl {
+
+constexpr double kHbar = 6.58264e-4;  // eV ps (constants_m.f:23)
+constexpr int kOrder = 25;            // Taylor order cap (Taylor.f:20)
+constexpr int kMaxFrag = 8;           // fragments tracked by the population reduction
+
+// ---- device-side STO basis (structure of arrays) --------------------------
+struct DevBasis {
+    int natoms = 0, nao = 0, nfrag = 0;
+    int *atom_ao0 = nullptr, *atom_nao = nullptr;
+    int *ao_n = nullptr, *ao_l = nullptr, *ao_m = nullptr, *ao_nzeta = nullptr, *ao_frag = nullptr;
+    double *ao_zeta = nullptr, *ao_coef = nullptr, *ao_ip = nullptr, *ao_kwh = nullptr, *ao_vshift = nullptr;
+};
+
+// S and h (both N x N, column-major, leading dimension ld) from coordinates.
+cudaError_t launch_build_sh(const DevBasis &b, const double *d_coords, double cutoff, double *d_S,
+                            double *d_h, int ld, cudaStream_t st);
+
+// ---- Taylor persistent engine ---------------------------------------------
+// Per-particle control, in device memory.  Written by the host before the
+// launch (tau, t_init, t_max) and by the kernel (results).
+struct TaylorParticle {
+    double tau_in;     // initial tau of the step
+    double save_tau;   // out: tau accepted by the first convergence
+    double tau_out;    // out: tau at the end (the reference's inout tau)
+    long long orders;  // out: expansion orders executed
+    int conv_calls;    // out
+    int substeps;      // out
+    int status;        // out: ELHL_OK / ELHL_ERR_NO_CONVERGENCE / ELHL_ERR_TIMEOUT
+    int psi_slot;      // out: slot holding the propagated Psi
+};
+
+struct TaylorLaunch {
+    const double *H;      // H' (N x N, ld)
+    int N, ld;
+    int nparticles;       // 1 or 2
+    double2 *slots;       // [nparticles][kSlots][2 (bra,ket)][ldv]; Psi in slot 0 in and out
+    int ldv;              // vector stride (>= N)
+    TaylorParticle *part; // [nparticles]
+    double t_init, t_max;
+    double tol, norm_tol;
+    int max_conv_calls;
+    // multi-step mode (fixed nuclei): nsteps > 1 runs the step driver on the device
+    int nsteps;
+    int it0;              // reference counter `it` before the first step
+    double dt_frame;      // dt * frame_step
+    double tau_max;
+    double *pops;         // [nsteps][nparticles][nfrag+1] or nullptr
+    const int *ao_frag;
+    int nfrag;
+    double *t_final;      // out: time after the last step
+    // scratch
+    double *partials;     // [2][nparticles][grid][4]
+    double *pop_partials; // [grid][nparticles][kMaxFrag+1]
+    unsigned *bar_count;  // grid barrier
+    unsigned *bar_gen;
+    int *error;           // global error flag
+};
+constexpr int kSlots = 6;
+
+cudaError_t launch_taylor(const TaylorLaunch &L, int grid, int block, cudaStream_t st);
+int taylor_grid_size(int block, int *grid_out);
+constexpr int kTaylorBlock = 256;
+
+// ---- small helpers ----------------------------------------------------------
+inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+}  // namespace elhl

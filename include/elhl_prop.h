@@ -1,0 +1,206 @@
+/*
+ * elhl_prop.h -- C ABI of libelhlprop.so, the GB300 (sm_103a) electron-hole
+ * wavepacket propagator.
+ *
+ * Two groups of entry points:
+ *
+ *  1. Drop-in replacements for the symbols Dynemol's Fortran host binds by
+ *     implicit interface (all arguments by reference, column-major matrices,
+ *     complex*16 = interleaved double pairs, lowercase name + trailing
+ *     underscore, no hidden string lengths).  They keep the reference's
+ *     argument meaning and "void + print on error" behaviour; the status of
+ *     the last call is available from elhl_last_status().
+ *
+ *  2. The native API (elhl_*): device-resident trajectories that rebuild S, h
+ *     and H' = S^-1 h on the GPU from nuclear coordinates and propagate the
+ *     electron and the hole together, returning an explicit status code.
+ *
+ * All compute runs on the GPU; there is no CPU fallback.  Calls return
+ * ELHL_ERR_NO_DEVICE when no CUDA device is present.
+ */
+#ifndef ELHL_PROP_H
+#define ELHL_PROP_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* complex*16 / cuDoubleComplex layout */
+typedef struct {
+    double re, im;
+} elhl_zcomplex;
+
+/* ---- status codes ------------------------------------------------------- */
+enum {
+    ELHL_OK = 0,
+    ELHL_ERR_BAD_ARG = 1,
+    ELHL_ERR_NO_CONVERGENCE = 2, /* tau retries exhausted (the reference loops forever) */
+    ELHL_ERR_TIMEOUT = 3,        /* a bounded device-side wait gave up */
+    ELHL_ERR_OOM = 4,
+    ELHL_ERR_CUDA = 5,
+    ELHL_ERR_NOT_POSITIVE_DEFINITE = 6, /* Cholesky of S failed */
+    ELHL_ERR_NO_DEVICE = 7,
+    ELHL_ERR_UNSUPPORTED = 8
+};
+
+/* ======================= 1. drop-in symbols ============================== */
+
+/* GPU_Init (GPU_Interface.cpp:226-263): bind device (myid / procs_per_dev) % ndev. */
+void gpu_init_(const int *myid, const int *procs_per_dev);
+
+/* GPU_Finalize (GPU_Interface.cpp:266-282): release library state. */
+void gpu_finalize_(void);
+
+/* GPU_Pin (GPU_Interface.cpp:288-295): page-lock `*bytes` bytes at ptr (cudaHostRegister). */
+void gpu_pin_(void *ptr, const int *bytes);
+
+/* GPU_Unpin (GPU_Interface.cpp:297-302). */
+void gpu_unpin_(void *ptr);
+
+/*
+ * propagation_gpucaller_ (Taylor_gpu.cpp:295-330): Taylor propagation of one
+ * particle under a given H' (host, N x N, ld = N) from t_init to t_max.
+ * tau is read (initial step) and not written back; save_tau receives the tau
+ * accepted by the first convergence (Taylor.f:71).  PSI_bra/PSI_ket are in/out.
+ */
+void propagation_gpucaller_(const int *n, double *tau, double *save_tau, const double *t_init,
+                            const double *t_max, elhl_zcomplex *h_PSI_bra, elhl_zcomplex *h_PSI_ket,
+                            const double *h_H);
+
+/*
+ * propagationelhl_gpucaller_ (Taylor_gpu.cpp:634-736, called from
+ * ElHl_Chebyshev_GPU.f:269-272): one particle, one nuclear step.
+ *   in : S, h (host, N x N, ld = N), PSI_bra/PSI_ket (length N), t_init, t_max, tau
+ *   out: h_H = H' = S^-1 h (host, ld = N); PSI_bra/PSI_ket propagated;
+ *        h_AO_bra = S^-1 PSI_bra (not conjugated; the caller conjugates);
+ *        save_tau.  h_AO_ket is not touched (as in the reference).
+ * Differences from the reference, by design: S^-1 h comes from a Cholesky
+ * factorisation instead of LU; device buffers are re-sized when N grows
+ * instead of being fixed by the first call; non-convergence stops after a
+ * bounded number of tau retries (status ELHL_ERR_NO_CONVERGENCE).
+ */
+void propagationelhl_gpucaller_(const int *N, const double *h_S, const double *h_h, double *h_H,
+                                elhl_zcomplex *h_AO_bra, elhl_zcomplex *h_AO_ket,
+                                elhl_zcomplex *h_PSI_bra, elhl_zcomplex *h_PSI_ket,
+                                const double *t_init, const double *t_max, double *tau,
+                                double *save_tau);
+
+/* Status of the last drop-in call on this thread (ELHL_OK, ...). */
+int elhl_last_status(void);
+const char *elhl_status_string(int status);
+
+/* ======================= 2. native API =================================== */
+
+/* Propagation method / precision of a trajectory. */
+enum {
+    ELHL_METHOD_TAYLOR_REF = 0, /* the reference's adaptive-tau Taylor (Taylor.f) on H', bra and ket */
+    ELHL_METHOD_CHEBYSHEV = 1   /* Chebyshev on the symmetrised H~ = L^-1 h L^-T, ket only */
+};
+enum {
+    ELHL_PREC_FP64 = 0,
+    ELHL_PREC_FP32 = 1,   /* H~ products in FP32, FP64 coefficients / norms */
+    ELHL_PREC_BF16X3 = 2  /* H~ split in three bf16 terms on the tensor cores, FP32 accumulate */
+};
+
+/* STO basis of one system (the STO_basis fields the path reads, types_EHT.f:135-165). */
+typedef struct {
+    int natoms;
+    int nao;
+    const int *atom_ao0;     /* [natoms] first AO of each atom */
+    const int *atom_nao;     /* [natoms] AOs per atom */
+    const int *ao_n;         /* [nao] principal quantum number (1..3) */
+    const int *ao_l;         /* [nao] 0 or 1 */
+    const int *ao_m;         /* [nao] -l..l */
+    const int *ao_nzeta;     /* [nao] 1 or 2 */
+    const double *ao_zeta;   /* [nao*2] exponents, Angstrom^-1 */
+    const double *ao_coef;   /* [nao*2] contraction coefficients */
+    const double *ao_ip;     /* [nao] ionisation potential, eV */
+    const double *ao_kwh;    /* [nao] Wolfsberg-Helmholz k */
+    const double *ao_vshift; /* [nao] on-site shift, eV */
+    const int *ao_frag;      /* [nao] fragment id 0..nfrag-1 (populations) */
+    int nfrag;
+} elhl_basis_desc;
+
+typedef struct {
+    int method;          /* ELHL_METHOD_* */
+    int precision;       /* ELHL_PREC_* */
+    double dt;           /* nuclear step, ps */
+    int frame_step;      /* t_max = dt*frame_step*(it-1) (ElHl_Chebyshev.f:176) */
+    double tol;          /* Taylor `error` (Taylor.f:21), e.g. 1e-8 or 1e-10 */
+    double norm_tol;     /* Taylor `norm_error` (Taylor.f:22) */
+    double cheb_tol;     /* Chebyshev truncation |c_k| < cheb_tol */
+    double cutoff;       /* overlap cutoff, Angstrom (QM_cutoff, 12) */
+    int max_conv_calls;  /* bound on tau retries per particle and step */
+    int ncols;           /* Chebyshev: complex columns (2 = el+hl) */
+} elhl_traj_config;
+
+typedef struct elhl_traj elhl_traj;
+
+void elhl_traj_config_default(elhl_traj_config *cfg);
+
+/* Create a trajectory at the given coordinates (natoms*3, atom-major, Angstrom, host).
+ * Builds S, h and H' on the device. */
+int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const elhl_traj_config *cfg,
+                     elhl_traj **out);
+int elhl_traj_destroy(elhl_traj *tr);
+
+/*
+ * Initial states from fragment molecular orbitals (FMO_analysis / eigen_FMO /
+ * projector('AO'), FMO.f:45-139, :260-350; wiring ElHl_Chebyshev.f:100-129).
+ * For each particle the fragment's S_f and h_f are built on the device at the
+ * current coordinates, H_f C = S_f C E is solved (cuSOLVER dsygvd), MO number
+ * `electron_state` / `hole_state` (1-based, ascending energy) is embedded in the
+ * full basis (zeros outside the fragment) as Psi_ket = C and Psi_bra = S C.
+ * Eigenvector sign: the component of largest magnitude is made positive.
+ */
+int elhl_traj_init_fmo(elhl_traj *tr, int n_el_atoms, const int *el_atoms, int electron_state, int n_hl_atoms,
+                       const int *hl_atoms, int hole_state);
+
+/* Set / get Psi (host, column-major N x ncols: column 0 electron, 1 hole).
+ * psi_bra may be NULL for the Chebyshev method (bra = S ket). */
+int elhl_traj_set_psi(elhl_traj *tr, const elhl_zcomplex *psi_bra, const elhl_zcomplex *psi_ket);
+int elhl_traj_get_psi(elhl_traj *tr, elhl_zcomplex *psi_bra, elhl_zcomplex *psi_ket);
+
+/*
+ * Advance `nsteps` nuclear steps (ElHl_Chebyshev, ElHl_Chebyshev.f:148-291).
+ * coords: NULL = nuclei fixed (S, h, H' kept), else nsteps*natoms*3 host
+ * coordinates, one set per step, rebuilt on the device before that step.
+ * pops (host, may be NULL): nsteps x ncols x (nfrag+1) populations after each step.
+ */
+int elhl_traj_step(elhl_traj *tr, const double *coords, int nsteps, double *pops);
+
+/* Same with device pointers (coords: nsteps*natoms*3 doubles, pops as above). */
+int elhl_traj_step_device(elhl_traj *tr, const double *d_coords, int nsteps, double *d_pops);
+
+/* Copies of the device matrices (host, N x N, ld = N); any pointer may be NULL. */
+int elhl_traj_get_matrices(elhl_traj *tr, double *S, double *h, double *Hp);
+
+/* Counters of the last elhl_traj_step call. */
+typedef struct {
+    long long orders;     /* expansion orders executed, summed over particles */
+    long long conv_calls; /* Taylor convergence attempts */
+    long long substeps;   /* accepted sub-steps */
+    double save_tau[2];   /* per particle */
+    double t;             /* trajectory time, ps */
+    int it;               /* reference step counter */
+    int status;
+    double prop_ms;       /* device time of the propagation kernels (CUDA events on the launch stream) */
+    double rebuild_ms;    /* device time of the S, h, H' rebuilds */
+    int prop_launches;    /* propagation kernel launches */
+    int rebuild_count;    /* rebuilds */
+} elhl_traj_stats;
+int elhl_traj_get_stats(elhl_traj *tr, elhl_traj_stats *st);
+
+/* Run all library work on the caller's CUDA stream (a cudaStream_t passed as
+ * void*), e.g. to order it with the caller's own kernels or to time it with
+ * events on that stream; NULL restores the library's own stream. */
+int elhl_set_stream(void *stream);
+
+/* Library / device information. */
+int elhl_device_count(void);
+int elhl_sm_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
