@@ -32,7 +32,7 @@ EXPORTED_SYMBOLS = (
     "propagationelhl_gpucaller_", "elhl_last_status", "elhl_status_string", "elhl_traj_config_default",
     "elhl_traj_create", "elhl_traj_destroy", "elhl_traj_init_fmo", "elhl_traj_set_psi", "elhl_traj_get_psi", "elhl_traj_step",
     "elhl_traj_step_device", "elhl_traj_get_matrices", "elhl_traj_get_stats", "elhl_device_count",
-    "elhl_sm_count", "elhl_set_stream",
+    "elhl_sm_count", "elhl_set_stream", "elhl_propagate_fixed_scratch",
 )
 
 
@@ -103,6 +103,8 @@ def load(path: str = LIB_PATH):
     L.elhl_device_count.restype = ci
     L.elhl_sm_count.restype = ci
     L.elhl_set_stream.argtypes = [vp]
+    L.elhl_propagate_fixed_scratch.argtypes = [ci, vp, ci, vp, vp, ctypes.c_double, ctypes.c_double,
+                                               ctypes.c_double, dp, vp]
     for s in EXPORTED_SYMBOLS:
         getattr(L, s)
     _lib = L
@@ -259,6 +261,21 @@ class Trajectory:
         st = TrajStats()
         _check(load().elhl_traj_get_stats(self.handle, ctypes.byref(st)), "elhl_traj_get_stats")
         return st
+
+
+FIXED_SCRATCH_MAX_N = 4096
+
+
+def propagate_fixed_scratch(n: int, d_H: int, ld: int, d_psi_bra: int, d_psi_ket: int, t_init: float, t_max: float,
+                            tau: float, stream: int | None = None) -> float:
+    """Allocation-free one-particle propagation on device buffers (integer device
+    pointers); for callers that cannot allocate device memory.  Returns save_tau."""
+    st = ctypes.c_double(0.0)
+    _check(load().elhl_propagate_fixed_scratch(n, ctypes.c_void_p(d_H), ld, ctypes.c_void_p(d_psi_bra),
+                                               ctypes.c_void_p(d_psi_ket), t_init, t_max, tau, ctypes.byref(st),
+                                               ctypes.c_void_p(stream) if stream else None),
+           "elhl_propagate_fixed_scratch")
+    return st.value
 
 
 def set_stream(stream_handle: int | None):

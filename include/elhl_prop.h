@@ -196,6 +196,29 @@ int elhl_traj_get_stats(elhl_traj *tr, elhl_traj_stats *st);
  * events on that stream; NULL restores the library's own stream. */
 int elhl_set_stream(void *stream);
 
+/*
+ * Allocation-free propagation of one particle (no counterpart in the
+ * reference).  Same computation and thresholds as propagation_gpucaller_
+ * (adaptive-tau Taylor, 1e-8), but for callers that cannot allocate device
+ * memory -- a host whose pool allocator owns the device memory, code running
+ * while a CUDA graph capture is in progress elsewhere, or code that must not
+ * risk the device synchronisation cudaMalloc/cudaFree can trigger.  It calls
+ * no cudaMalloc, cudaFree or allocating library routine: all scratch lives in
+ * a fixed device array inside the library (about 0.9 MB, held by every GPU that
+ * loads the library until the process exits).
+ *   d_H         device, n x n column-major H', leading dimension ld >= n
+ *   d_psi_bra/d_psi_ket  device, length n, propagated in place
+ *   save_tau    host, receives the tau accepted by the first convergence
+ *   stream      cudaStream_t as void* (NULL = legacy default stream)
+ * Limit: n <= 4096 (larger n returns ELHL_ERR_BAD_ARG).  The call is
+ * synchronous.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) and should come before any stream capture.  All calls
+ * share the array; calls that overlap on the GPU race.
+ */
+int elhl_propagate_fixed_scratch(int n, const double *d_H, int ld, elhl_zcomplex *d_psi_bra,
+                                 elhl_zcomplex *d_psi_ket, double t_init, double t_max, double tau,
+                                 double *save_tau, void *stream);
+
 /* Library / device information. */
 int elhl_device_count(void);
 int elhl_sm_count(void);
