@@ -120,14 +120,20 @@ def run_ours(args, rank, world):
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     torch.cuda.set_device(dev)
     api.load()
-    stream = torch.cuda.current_stream(dev)
+    # a dedicated (non-default) stream: the library launches on it and the CUDA
+    # events below are recorded on it
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     api.set_stream(stream.cuda_stream)
 
     sysm, dt, moving = workload(args.workload)
     homo = systems.fermi_state(sysm, np.arange(20))
     W, K = args.warmup, args.steps
     coords = step_coords(sysm, moving, W + K + 1, offset=1000 * rank)
-    tr = api.Trajectory(sysm, coords=None if coords is None else coords[0], dt=dt)
+    method = api.METHOD_CHEBYSHEV if args.method == "chebyshev" else api.METHOD_TAYLOR_REF
+    prec = {"fp64": api.PREC_FP64, "fp32": api.PREC_FP32}[args.precision]
+    tr = api.Trajectory(sysm, coords=None if coords is None else coords[0], dt=dt, method=method, precision=prec,
+                        ncols=4 if moving else 2, cheb_tol=1e-12)
     tr.init_fmo(homo + 1, homo)
 
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -202,19 +208,30 @@ def run_ours(args, rank, world):
     tr.close()
 
     N = sysm.nao
-    # roofline of the dominant kernel (the propagation kernel): per executed
-    # expansion order of one particle, H' read once for bra (H'^T) and ket (H'):
-    # bytes = 8 N^2 + 160 N, flops = 8 N^2 (real x complex, 2 columns)
-    per_launch_orders = orders / max(1, K)
-    bytes_per_launch = per_launch_orders * (8.0 * N * N + 160.0 * N)
-    flops_per_launch = per_launch_orders * 8.0 * N * N
-    prop_launch_ms = prop_ms / K
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    achieved_gbs = bytes_per_launch / (prop_launch_ms * 1e-3) / 1e9
-    fp64_tflops = flops_per_launch / (prop_launch_ms * 1e-3) / 1e12
     FP64_PEAK = 1.20  # TFLOP/s, FMA probe measured on this machine's GB300 (profiles/gb300_peaks_probe.md)
+    prop_launch_ms = prop_ms / K
+    if args.method == "taylor":
+        # dominant kernel: taylor_kernel.  Unit = one expansion order of one
+        # particle: H' read once for bra (H'^T) and ket (H'), 2 complex columns:
+        # bytes = 8 N^2 + 160 N, flops = 8 N^2
+        kernel = "taylor_kernel"
+        per_launch_orders = orders / max(1, K)
+        bytes_per_launch = per_launch_orders * (8.0 * N * N + 160.0 * N)
+        flops_per_launch = per_launch_orders * 8.0 * N * N
+    else:
+        # dominant kernel: cheb_kernel.  Unit = one Chebyshev order over m complex
+        # columns: Hs read once (b_H N^2) + 5 x 16 N m vector bytes; flops = 4 N^2 m
+        kernel = "cheb_kernel"
+        m = 4 if moving else 2
+        bH = 8.0 if args.precision == "fp64" else 4.0
+        per_launch_orders = orders / max(1, K) / m
+        bytes_per_launch = per_launch_orders * (bH * N * N + 80.0 * N * m)
+        flops_per_launch = per_launch_orders * 4.0 * N * N * m
+    achieved_gbs = bytes_per_launch / (prop_launch_ms * 1e-3) / 1e9
+    tflops = flops_per_launch / (prop_launch_ms * 1e-3) / 1e12
 
     line = {
         "metric": "psi_propagation_steps_per_s",
@@ -227,10 +244,10 @@ def run_ours(args, rank, world):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64",
+        "dtype": "f64" if args.precision == "fp64" else "f32 products, f64 accumulation",
         "data": "synthetic (seeded geometry, no external dataset)",
         "config": {"workload": WORKLOAD_DESC[args.workload], "N_ao": N, "natoms": sysm.natoms,
-                   "dt_ps": dt, "particles": 2, "method": "taylor_ref", "precision": "fp64",
+                   "dt_ps": dt, "particles": 2, "method": args.method, "precision": args.precision,
                    "moving_nuclei": moving, "l2": "flushed (512 MB write) between timed steps",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": world * Ke / t_e2e, "unit": "steps/s",
@@ -238,9 +255,12 @@ def run_ours(args, rank, world):
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved_gbs / hbm_peak, "traffic": None,
-                     "kernel": "taylor_kernel", "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)",
-                     "fp64_alu": {"achieved_tflops": fp64_tflops, "peak_tflops": FP64_PEAK,
-                                  "frac": fp64_tflops / FP64_PEAK, "peak_source": "of measured (FMA probe)"},
+                     "kernel": kernel, "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)",
+                     "alu": {"achieved_tflops": tflops,
+                             "peak_tflops": FP64_PEAK if args.precision == "fp64" else 70.1,
+                             "frac": tflops / (FP64_PEAK if args.precision == "fp64" else 70.1),
+                             "pipe": "fp64 FMA" if args.precision == "fp64" else "fp32 FMA",
+                             "peak_source": "of measured (FMA probe, profiles/gb300_peaks_probe.md)"},
                      "orders_per_launch": per_launch_orders, "launch_ms": prop_launch_ms},
         "breakdown_ms_per_step": {"propagation": prop_ms / K, "rebuild_S_h_Hprime": rebuild_ms / K},
         "clocks": clk,
@@ -288,6 +308,117 @@ def run_reference(args, rank, world):
     }
 
 
+# ----------------------------------------------------------------- trajectory mix
+def trajectory_mix(ntraj: int, nmin: int = 200, nmax: int = 3000, seed: int = 4):
+    """Uneven C/H/O systems: N drawn uniformly in [nmin, nmax] AOs (seed), each its
+    own jittered cubic cluster (60/30/10 %) -- the batching workload."""
+    from dynemol_gb300 import systems
+    rng = systems.SplitMix64(seed)
+    out = []
+    for i in range(ntraj):
+        target = nmin + (rng.next_u64() % (nmax - nmin + 1))
+        n_atoms = max(8, int(round(target / 3.1)))  # 3.1 AO per atom at 60/30/10 % C/H/O
+        out.append(systems.cubic_cluster(n_atoms=n_atoms, seed=seed + i))
+    return out
+
+
+def run_mix(args, ntraj, steps, warm, precision, dropin_sample):
+    """Batched Chebyshev (one launch per step for the whole mix) vs the plain
+    FP64 drop-in (propagationelhl_gpucaller_ semantics: Taylor, one trajectory
+    per call) on the same mix.  Returns a dict of results."""
+    import torch
+    from dynemol_gb300 import api, systems
+    mix = trajectory_mix(ntraj)
+    dt = 1e-4
+    res = {"ntraj": ntraj, "N_range": [min(s.nao for s in mix), max(s.nao for s in mix)],
+           "N_mean": float(np.mean([s.nao for s in mix])), "dt_ps": dt}
+    out = {}
+    for prec in (api.PREC_FP64, precision):
+        b = api.Batch(mix, dt=dt, precision=prec, ncols=2, cheb_tol=1e-12)
+        b.init_fmo()
+        b.compact()
+        b.step(warm, want_pops=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pops = b.step(steps)
+        el = time.perf_counter() - t0
+        st = b.stats()
+        out[prec] = (pops, el, st)
+        b.close()
+    p64, el64, st64 = out[api.PREC_FP64]
+    pmx, elmx, stmx = out[precision]
+    res["batched_fp64_steps_per_s"] = ntraj * steps / el64
+    res["batched_mixed_steps_per_s"] = ntraj * steps / elmx
+    res["mixed_precision"] = {api.PREC_FP32: "fp32"}.get(precision, "fp64")
+    res["mixed_pop_err_vs_fp64"] = float(np.abs(pmx - p64).max())
+    res["kernel_ms_per_step_mixed"] = stmx.prop_ms / steps
+    # plain FP64 drop-in on a uniform sample of the same mix
+    sample = mix[:: max(1, ntraj // dropin_sample)][:dropin_sample]
+    t_drop, n_drop = 0.0, 0
+    for sysm in sample:
+        tr = api.Trajectory(sysm, dt=dt)
+        homo = systems.fermi_state(sysm, sysm.fragment_atoms("E"))
+        tr.init_fmo(homo + 1, homo)
+        tr.step(None, nsteps=1, want_pops=False)  # warm-up (first step starts at tau_max)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tr.step(None, nsteps=2, want_pops=True)
+        t_drop += time.perf_counter() - t0
+        n_drop += 2
+        tr.close()
+    # the sample's mean cost per trajectory-step, scaled to the mix by sum N^2
+    scale = np.mean([s.nao ** 2 for s in mix]) / np.mean([s.nao ** 2 for s in sample])
+    res["dropin_fp64_steps_per_s"] = n_drop / (t_drop * scale)
+    res["dropin_sample"] = f"{len(sample)} trajectories x 2 steps, cost scaled to the mix by mean N^2 ({scale:.2f})"
+    res["speedup_batched_mixed_vs_dropin_fp64"] = res["batched_mixed_steps_per_s"] / res["dropin_fp64_steps_per_s"]
+    return res
+
+
+def run_serve(args, nreq, rate, steps_scale, nmax, precision, budget):
+    """Poisson stream of propagation requests against an HBM budget (continuous
+    batching).  Returns latency percentiles and aggregate steps/s."""
+    from dynemol_gb300 import api, systems
+    rng = systems.SplitMix64(5)
+    reqs = []
+    t = 0.0
+    for i in range(nreq):
+        u = ((rng.next_u64() >> 11) + 0.5) / 9007199254740992.0
+        t += -np.log(u) / rate
+        u = ((rng.next_u64() >> 11) + 0.5) / 9007199254740992.0
+        N = 256.0 * (nmax / 256.0) ** u  # log-uniform
+        n_atoms = max(8, int(round(N / 3.1)))
+        nsteps = max(1, int((50 + rng.next_u64() % 4951) * steps_scale))
+        cols = 2 * (1 + int(rng.next_u64() % 16))  # even 2..32
+        sysm = systems.cubic_cluster(n_atoms=n_atoms, seed=500 + i)
+        homo = systems.fermi_state(sysm, sysm.fragment_atoms("E"))
+        nf = int(sum(sysm.atom_nao[a] for a in sysm.fragment_atoms("E")))
+        states = [int(1 + (homo - cols // 2 + c) % nf) for c in range(cols)]
+        reqs.append((t, sysm, nsteps, states))
+    sv = api.Server(budget, dt=1e-4, precision=precision, cheb_tol=1e-12)
+    t0 = time.perf_counter()
+    nxt, done, lat, total_steps = 0, 0, [], 0
+    while done < nreq:
+        now = time.perf_counter() - t0
+        while nxt < nreq and reqs[nxt][0] <= now:
+            sv.submit(reqs[nxt][1], reqs[nxt][2], reqs[nxt][3])
+            nxt += 1
+        active, pending = sv.step()
+        for rid in sv.poll():
+            pops, psi, times = sv.result(rid)
+            lat.append(times[2] - times[0])
+            done += 1
+        if active == 0 and pending == 0 and nxt < nreq:
+            time.sleep(max(0.0, reqs[nxt][0] - (time.perf_counter() - t0)))
+    wall = time.perf_counter() - t0
+    total_steps = sum(r[2] for r in reqs)
+    sv.close()
+    lat = np.array(lat)
+    return {"requests": nreq, "arrival_rate_per_s": rate, "N_logrange": [256, nmax], "steps_scale": steps_scale,
+            "columns": "even 2..32", "hbm_budget_GB": budget / 1e9, "wall_s": wall,
+            "aggregate_steps_per_s": total_steps / wall, "latency_p50_s": float(np.percentile(lat, 50)),
+            "latency_p99_s": float(np.percentile(lat, 99))}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -296,6 +427,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ehrenfest", choices=sorted(WORKLOAD_DESC))
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--method", default="taylor", choices=["taylor", "chebyshev"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--mix", type=int, default=0, help="also run the batched-vs-drop-in comparison on a mix "
+                    "of this many trajectories (0 = skip)")
+    ap.add_argument("--serve", type=int, default=0, help="also run a serving stream of this many requests")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
@@ -310,6 +446,14 @@ def main():
         import torch
         torch.distributed.init_process_group("nccl")
     line = run_ours(args, rank, world)
+    if rank == 0 and args.mix:
+        from dynemol_gb300 import api
+        line["north_star_mix"] = run_mix(args, args.mix, steps=5, warm=2, precision=api.PREC_FP32,
+                                         dropin_sample=4)
+    if rank == 0 and args.serve:
+        from dynemol_gb300 import api
+        line["serving"] = run_serve(args, args.serve, rate=200.0, steps_scale=0.02, nmax=4096,
+                                    precision=api.PREC_FP32, budget=150e9)
     if rank == 0:
         if not args.no_cpu_baseline:
             sysm, dt, moving = workload(args.workload)

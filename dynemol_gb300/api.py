@@ -30,9 +30,13 @@ PREC_FP64, PREC_FP32, PREC_BF16X3 = 0, 1, 2
 EXPORTED_SYMBOLS = (
     "gpu_init_", "gpu_finalize_", "gpu_pin_", "gpu_unpin_", "propagation_gpucaller_",
     "propagationelhl_gpucaller_", "elhl_last_status", "elhl_status_string", "elhl_traj_config_default",
-    "elhl_traj_create", "elhl_traj_destroy", "elhl_traj_init_fmo", "elhl_traj_set_psi", "elhl_traj_get_psi", "elhl_traj_step",
-    "elhl_traj_step_device", "elhl_traj_get_matrices", "elhl_traj_get_stats", "elhl_device_count",
-    "elhl_sm_count", "elhl_set_stream", "elhl_propagate_fixed_scratch",
+    "elhl_traj_create", "elhl_traj_destroy", "elhl_traj_init_fmo", "elhl_traj_init_fmo_states", "elhl_traj_set_psi", "elhl_traj_get_psi", "elhl_traj_step",
+    "elhl_traj_step_device", "elhl_traj_energies", "elhl_traj_get_matrices", "elhl_traj_get_stats", "elhl_device_count",
+    "elhl_sm_count", "elhl_set_stream", "elhl_propagate_fixed_scratch", "elhl_bessel_j",
+    "elhl_chebyshev_coefficients", "elhl_batch_create", "elhl_batch_size", "elhl_batch_member",
+    "elhl_batch_compact", "elhl_batch_step", "elhl_batch_get_stats", "elhl_batch_destroy",
+    "elhl_server_create", "elhl_server_submit", "elhl_server_step", "elhl_server_poll", "elhl_server_result",
+    "elhl_server_destroy",
 )
 
 
@@ -52,7 +56,7 @@ class TrajConfig(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int), ("precision", ctypes.c_int), ("dt", ctypes.c_double),
                 ("frame_step", ctypes.c_int), ("tol", ctypes.c_double), ("norm_tol", ctypes.c_double),
                 ("cheb_tol", ctypes.c_double), ("cutoff", ctypes.c_double), ("max_conv_calls", ctypes.c_int),
-                ("ncols", ctypes.c_int)]
+                ("ncols", ctypes.c_int), ("nparticles", ctypes.c_int)]
 
 
 class TrajStats(ctypes.Structure):
@@ -60,6 +64,12 @@ class TrajStats(ctypes.Structure):
                 ("save_tau", ctypes.c_double * 2), ("t", ctypes.c_double), ("it", ctypes.c_int),
                 ("status", ctypes.c_int), ("prop_ms", ctypes.c_double), ("rebuild_ms", ctypes.c_double),
                 ("prop_launches", ctypes.c_int), ("rebuild_count", ctypes.c_int)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("basis", ctypes.POINTER(BasisDesc)), ("coords", ctypes.c_void_p), ("nsteps", ctypes.c_int),
+                ("nparticles", ctypes.c_int), ("n_frag_atoms", ctypes.c_int), ("frag_atoms", ctypes.c_void_p),
+                ("states", ctypes.c_void_p)]
 
 
 _lib = None
@@ -94,17 +104,36 @@ def load(path: str = LIB_PATH):
     L.elhl_traj_create.argtypes = [ctypes.POINTER(BasisDesc), vp, ctypes.POINTER(TrajConfig), ctypes.POINTER(vp)]
     L.elhl_traj_destroy.argtypes = [vp]
     L.elhl_traj_init_fmo.argtypes = [vp, ci, vp, ci, ci, vp, ci]
+    L.elhl_traj_init_fmo_states.argtypes = [vp, ci, vp, ci, vp]
     L.elhl_traj_set_psi.argtypes = [vp, vp, vp]
     L.elhl_traj_get_psi.argtypes = [vp, vp, vp]
     L.elhl_traj_step.argtypes = [vp, vp, ci, vp]
     L.elhl_traj_step_device.argtypes = [vp, vp, ci, vp]
     L.elhl_traj_get_matrices.argtypes = [vp, vp, vp, vp]
+    L.elhl_traj_energies.argtypes = [vp, vp]
     L.elhl_traj_get_stats.argtypes = [vp, ctypes.POINTER(TrajStats)]
     L.elhl_device_count.restype = ci
     L.elhl_sm_count.restype = ci
     L.elhl_set_stream.argtypes = [vp]
     L.elhl_propagate_fixed_scratch.argtypes = [ci, vp, ci, vp, vp, ctypes.c_double, ctypes.c_double,
                                                ctypes.c_double, dp, vp]
+    L.elhl_bessel_j.argtypes = [ctypes.c_double, ci, vp]
+    L.elhl_chebyshev_coefficients.argtypes = [ctypes.c_double, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                              ci, vp, vp, ip]
+    L.elhl_batch_create.argtypes = [ci, vp, vp, ctypes.POINTER(TrajConfig), ctypes.POINTER(vp)]
+    L.elhl_batch_size.argtypes = [vp]
+    L.elhl_batch_member.argtypes = [vp, ci]
+    L.elhl_batch_member.restype = vp
+    L.elhl_batch_compact.argtypes = [vp]
+    L.elhl_batch_step.argtypes = [vp, ci, vp]
+    L.elhl_batch_get_stats.argtypes = [vp, ctypes.POINTER(TrajStats)]
+    L.elhl_batch_destroy.argtypes = [vp]
+    L.elhl_server_create.argtypes = [ctypes.c_double, ctypes.POINTER(TrajConfig), ctypes.POINTER(vp)]
+    L.elhl_server_submit.argtypes = [vp, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_longlong)]
+    L.elhl_server_step.argtypes = [vp, ip, ip]
+    L.elhl_server_poll.argtypes = [vp, vp, ci, ip]
+    L.elhl_server_result.argtypes = [vp, ctypes.c_longlong, vp, vp, vp]
+    L.elhl_server_destroy.argtypes = [vp]
     for s in EXPORTED_SYMBOLS:
         getattr(L, s)
     _lib = L
@@ -189,10 +218,24 @@ def default_config(**kw) -> TrajConfig:
     return c
 
 
+def _basis_desc(system):
+    keep = [system.atom_ao0, system.atom_nao, system.ao_n, system.ao_l, system.ao_m, system.ao_nzeta,
+            system.ao_zeta, system.ao_coef, system.ao_ip, system.ao_kwh, system.ao_vshift, system.ao_frag]
+    return BasisDesc(system.natoms, system.nao, *[_p(a) for a in keep], system.nfrag), keep
+
+
 class Trajectory:
     """Device-resident electron-hole trajectory (S, h, H', Psi live in HBM)."""
 
+    @classmethod
+    def borrowed(cls, system, handle):
+        """Wrap a handle owned elsewhere (a batch member); close() does not free it."""
+        self = cls.__new__(cls)
+        self.sys, self.handle, self.N, self.P, self._owned = system, handle, system.nao, 2, False
+        return self
+
     def __init__(self, system, coords=None, config: TrajConfig | None = None, **cfg_kw):
+        self._owned = True
         L = load()
         self.sys = system
         self._keep = [system.atom_ao0, system.atom_nao, system.ao_n, system.ao_l, system.ao_m, system.ao_nzeta,
@@ -205,12 +248,12 @@ class Trajectory:
                "elhl_traj_create")
         self.handle = h
         self.N = system.nao
-        self.P = 2
+        self.P = int(self.config.nparticles)
 
     def close(self):
-        if getattr(self, "handle", None):
+        if getattr(self, "handle", None) and getattr(self, "_owned", True):
             load().elhl_traj_destroy(self.handle)
-            self.handle = None
+        self.handle = None
 
     def __del__(self):
         try:
@@ -224,6 +267,13 @@ class Trajectory:
         hl = np.ascontiguousarray(self.sys.fragment_atoms("H"), np.int32)
         _check(load().elhl_traj_init_fmo(self.handle, len(el), _p(el), electron_state, len(hl), _p(hl), hole_state),
                "elhl_traj_init_fmo")
+
+    def init_fmo_states(self, states, which: str = "E"):
+        """Chebyshev ensembles: column c = fragment MO states[c] (1-based)."""
+        at = np.ascontiguousarray(self.sys.fragment_atoms(which), np.int32)
+        st = np.ascontiguousarray(states, np.int32)
+        _check(load().elhl_traj_init_fmo_states(self.handle, len(at), _p(at), len(st), _p(st)),
+               "elhl_traj_init_fmo_states")
 
     def set_psi(self, psi_bra, psi_ket):
         b = np.asfortranarray(psi_bra, np.complex128)
@@ -250,6 +300,12 @@ class Trajectory:
         """Device-pointer variant (pointers as integers)."""
         _check(load().elhl_traj_step_device(self.handle, ctypes.c_void_p(d_coords_ptr), nsteps,
                                             ctypes.c_void_p(d_pops_ptr)), "elhl_traj_step_device")
+
+    def energies(self) -> np.ndarray:
+        """Complex wavepacket energy per particle (eV)."""
+        E = np.zeros(self.P, np.complex128)
+        _check(load().elhl_traj_energies(self.handle, _p(E)), "elhl_traj_energies")
+        return E
 
     def matrices(self):
         N = self.N
@@ -278,9 +334,139 @@ def propagate_fixed_scratch(n: int, d_H: int, ld: int, d_psi_bra: int, d_psi_ket
     return st.value
 
 
+def bessel_j(beta: float, kmax: int) -> np.ndarray:
+    """J_0..J_kmax(beta) (host code of the library, no GPU needed)."""
+    J = np.zeros(kmax + 1)
+    _check(load().elhl_bessel_j(beta, kmax, _p(J)), "elhl_bessel_j")
+    return J
+
+
+def chebyshev_coefficients(dt: float, emin: float, emax: float, tol: float = 1e-12, kcap: int = 4000):
+    """Complex c_k of exp(-i dt H / hbar) on [emin, emax] (host code)."""
+    cre, cim = np.zeros(kcap + 1), np.zeros(kcap + 1)
+    K = ctypes.c_int(0)
+    _check(load().elhl_chebyshev_coefficients(dt, emin, emax, tol, kcap, _p(cre), _p(cim), ctypes.byref(K)),
+           "elhl_chebyshev_coefficients")
+    return cre[: K.value + 1] + 1j * cim[: K.value + 1]
+
+
 def set_stream(stream_handle: int | None):
     """Route library work to a caller stream (integer cudaStream_t) or back to its own (None)."""
     _check(load().elhl_set_stream(ctypes.c_void_p(stream_handle) if stream_handle else None), "elhl_set_stream")
+
+
+class Batch:
+    """Many Chebyshev trajectories advanced by one launch per nuclear step."""
+
+    def __init__(self, systems_list, coords_list=None, **cfg_kw):
+        L = load()
+        cfg_kw.setdefault("method", METHOD_CHEBYSHEV)
+        self.config = default_config(**cfg_kw)
+        self.systems = list(systems_list)
+        descs = (BasisDesc * len(self.systems))()
+        self._keep = []
+        cptrs = (ctypes.c_void_p * len(self.systems))()
+        for i, sysm in enumerate(self.systems):
+            d, keep = _basis_desc(sysm)
+            descs[i] = d
+            c = np.ascontiguousarray(sysm.coords if coords_list is None else coords_list[i], np.float64)
+            self._keep += keep + [c]
+            cptrs[i] = c.ctypes.data
+        self._descs, self._cptrs = descs, cptrs
+        h = ctypes.c_void_p()
+        _check(L.elhl_batch_create(len(self.systems), ctypes.cast(descs, ctypes.c_void_p),
+                                   ctypes.cast(cptrs, ctypes.c_void_p), ctypes.byref(self.config), ctypes.byref(h)),
+               "elhl_batch_create")
+        self.handle = h
+        self.members = [Trajectory.borrowed(sysm, ctypes.c_void_p(L.elhl_batch_member(h, i)))
+                        for i, sysm in enumerate(self.systems)]
+
+    def init_fmo(self, electron_state=None, hole_state=None):
+        """Fragment-MO initial states; default LUMO / HOMO of each member's fragment."""
+        from dynemol_gb300.systems import fermi_state
+        for tr, sysm in zip(self.members, self.systems):
+            homo = fermi_state(sysm, sysm.fragment_atoms("E"))
+            tr.init_fmo(electron_state or homo + 1, hole_state or homo)
+
+    def compact(self):
+        _check(load().elhl_batch_compact(self.handle), "elhl_batch_compact")
+
+    def step(self, nsteps: int = 1, want_pops: bool = True):
+        nf1 = self.systems[0].nfrag + 1
+        pops = np.zeros((nsteps, len(self.systems), int(self.config.nparticles), nf1)) if want_pops else None
+        _check(load().elhl_batch_step(self.handle, nsteps, _p(pops)), "elhl_batch_step")
+        return pops
+
+    def stats(self) -> TrajStats:
+        st = TrajStats()
+        _check(load().elhl_batch_get_stats(self.handle, ctypes.byref(st)), "elhl_batch_get_stats")
+        return st
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().elhl_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching propagation server (fixed-nuclei Chebyshev requests)."""
+
+    def __init__(self, hbm_budget_bytes: float, **cfg_kw):
+        cfg_kw.setdefault("method", METHOD_CHEBYSHEV)
+        self.config = default_config(**cfg_kw)
+        h = ctypes.c_void_p()
+        _check(load().elhl_server_create(float(hbm_budget_bytes), ctypes.byref(self.config), ctypes.byref(h)),
+               "elhl_server_create")
+        self.handle = h
+        self.meta = {}
+
+    def submit(self, system, nsteps: int, states, which: str = "E", coords=None) -> int:
+        desc, keep = _basis_desc(system)
+        c = np.ascontiguousarray(system.coords if coords is None else coords, np.float64)
+        at = np.ascontiguousarray(system.fragment_atoms(which), np.int32)
+        st = np.ascontiguousarray(states, np.int32)
+        req = Request(ctypes.pointer(desc), _p(c), nsteps, len(st), len(at), _p(at), _p(st))
+        rid = ctypes.c_longlong(0)
+        _check(load().elhl_server_submit(self.handle, ctypes.byref(req), ctypes.byref(rid)), "elhl_server_submit")
+        self.meta[rid.value] = (system, len(st))
+        return rid.value
+
+    def step(self):
+        a, p = ctypes.c_int(0), ctypes.c_int(0)
+        _check(load().elhl_server_step(self.handle, ctypes.byref(a), ctypes.byref(p)), "elhl_server_step")
+        return a.value, p.value
+
+    def poll(self, max_n: int = 1024):
+        ids = np.zeros(max_n, np.int64)
+        n = ctypes.c_int(0)
+        _check(load().elhl_server_poll(self.handle, _p(ids), max_n, ctypes.byref(n)), "elhl_server_poll")
+        return [int(x) for x in ids[: n.value]]
+
+    def result(self, rid: int):
+        """(populations (P, nfrag+1), kets (N, P), times {submit, admit, done})."""
+        system, P = self.meta.pop(rid)
+        pops = np.zeros((P, system.nfrag + 1))
+        psi = np.zeros((system.nao, P), np.complex128, order="F")
+        times = np.zeros(3)
+        _check(load().elhl_server_result(self.handle, rid, _p(pops), _p(psi), _p(times)), "elhl_server_result")
+        return pops, psi, times
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().elhl_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def device_count() -> int:

@@ -14,8 +14,8 @@
 //                         (hamiltonians.f:33-63, ElHl_Chebyshev.f:313-321)
 //
 // Supported basis: n <= 3, l <= 1, one or two zetas (the H/C/O EHT basis of
-// the workloads).  Table values re(i)=i and reali(i)=1/i are evaluated
-// inline; they are the same IEEE values the reference tabulates.
+// the workloads).  re(i) = i is evaluated inline; 1/i, i! and 1/i! come from
+// device tables holding the same IEEE values the reference tabulates.
 #include "elhl_internal.cuh"
 
 namespace elhl {
@@ -27,13 +27,31 @@ constexpr int kNT = kMaxN + 3 * kMaxL + 1;  // n index bound: na + la + 2 lb <= 
 constexpr int kHR = kNT + 2;                // 1F1 rows (alpha up to namax + 1)
 constexpr int kHC = 2 * kNT + 2;            // 1F1 columns (gamma up to ngmax)
 
-__device__ __forceinline__ double rcp_int(int i) { return i == 0 ? 0.0 : 1.0 / (double)i; }
+// Constant tables (UTIL_OVERLAP, overlap_D.f:1194-1231): 1/i (0 at i = 0), i!
+// and 1/i!.  Filled once per device by init_tables; FP64 division is slow on
+// this part, so the inner loops read tables instead of dividing.
+__device__ double g_reali[1001];
+__device__ double g_fact[32];
+__device__ double g_facti[32];
 
-__device__ double dfact(int n) {
-    double f = 1.0;
-    for (int i = 1; i <= n; ++i) f = f * (double)i;
-    return f;
+__global__ void init_tables_kernel() {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i <= 1000) g_reali[i] = (i == 0) ? 0.0 : 1.0 / (double)i;
+    if (i == 0) {
+        double f = 1.0;
+        g_fact[0] = 1.0;
+        g_facti[0] = 1.0;
+        for (int k = 1; k < 32; ++k) {
+            f = f * (double)k;
+            g_fact[k] = f;
+            g_facti[k] = 1.0 / f;
+        }
+    }
 }
+
+__device__ __forceinline__ double rcp_int(int i) { return __ldg(&g_reali[i]); }
+__device__ __forceinline__ double dfact(int n) { return __ldg(&g_fact[n]); }
+__device__ __forceinline__ double dfacti(int n) { return __ldg(&g_facti[n]); }
 
 // <na la m | nb lb m>, m = 0..min(la, lb), lined-up frame.  Returns false on
 // quantum numbers outside the supported range.
@@ -101,7 +119,7 @@ __device__ bool lined_up_overlap(int na, int la, double za, int nb, int lb, doub
                 for (int k = 0; k <= n + np; ++k) {
                     double sumj = 0.0;
                     for (int j = max(0, k - n); j <= min(k, np); ++j)
-                        sumj = sumj + h1f1[j + 1][k + 2] * (1.0 / dfact(n + j - k)) * (1.0 / dfact(np - j));
+                        sumj = sumj + h1f1[j + 1][k + 2] * dfacti(n + j - k) * dfacti(np - j);
                     sumk = sumk + sumj * auxk;
                     auxk = auxk * zzpR * rcp_int(n + np - k) * rcp_int(k + 2);
                 }
@@ -286,6 +304,13 @@ __global__ void build_sh_kernel(DevBasis b, const double *__restrict__ coords, d
 }
 
 }  // namespace
+
+cudaError_t init_build_tables() {
+    init_tables_kernel<<<(1001 + 255) / 256, 256>>>();
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    return e;
+}
 
 cudaError_t launch_build_sh(const DevBasis &b, const double *d_coords, double cutoff, double *d_S,
                             double *d_h, int ld, cudaStream_t st) {

@@ -1,0 +1,247 @@
+// Batched Chebyshev propagation on the symmetrised Hamiltonian.
+//
+// For S = L L^T, S^-1 h = L^-T H~ L^T with H~ = L^-1 h L^-T symmetric, so
+//   ket:  psi(t) = L^-T exp(-i H~ t/hbar) L^T psi(0)
+//   bra:  bra(t) = L exp(-i H~ t/hbar) L^-1 bra(0)
+// (the reference's bra update with H'^T, Taylor.f:94, is exp(-i h S^-1 t) =
+// L exp(-i H~ t) L^-1).  The transformed columns phi = L^T psi and
+// chi = L^-1 bra are propagated with the Chebyshev expansion of
+// exp(-i tau H~) (Tal-Ezer & Kosloff 1984) on Hs = (H~ - a)/b, spectrum in [-1, 1]:
+//   v_0 = phi, v_1 = Hs v_0, v_{k+1} = 2 Hs v_k - v_{k-1},   phi' = sum_k c_k v_k.
+//
+// One cooperative launch advances every problem of a batch (trajectories of
+// different N and order counts) by one nuclear step.  Each CTA owns fixed row
+// segments (balanced by matrix elements on the host).  Per order it stages the
+// previous vector of a column group in shared memory; warps form a WR x WJ
+// grid over (8-row tiles, slices of j); every warp accumulates 8 rows x MG
+// complex columns in registers (Hs symmetric: row i is the contiguous column i),
+// partial sums meet in shared memory in a fixed order, and the epilogue
+// applies the recurrence and adds c_k v_k to the FP64 accumulator.  A bounded
+// grid barrier separates orders.
+//   T = double : FP64 products;  T = float : FP32 Hs and vectors,
+//   FP64 coefficients and accumulation.
+#include "elhl_internal.cuh"
+#include "grid_sync.cuh"
+
+namespace elhl {
+namespace {
+
+template <typename T> struct Vec2;
+template <> struct Vec2<double> { using type = double2; };
+template <> struct Vec2<float> { using type = float2; };
+
+constexpr int kBlock = 512;
+constexpr int kWarps = kBlock / 32;
+constexpr int kRT = 8;  // rows per warp tile
+
+__device__ __forceinline__ double2 ldcg2(const double2 *p) { return __ldcg(p); }
+__device__ __forceinline__ float2 ldcg2(const float2 *p) { return __ldcg(p); }
+
+// Transposed butterfly: v[0..31] per lane -> lane l returns the warp sum of v[l].
+template <typename T>
+__device__ __forceinline__ T transpose_reduce32(T (&v)[32], int lane) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < o; ++i) {
+            const T send = upper ? v[i] : v[i + o];
+            const T keep = upper ? v[i + o] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    return v[0];
+}
+
+// one order k >= 1 for the rows of segment sg, column group g (MG columns)
+template <typename T, int MG>
+__device__ void order_rows(const ChebProblem &pb, const ChebSegment &sg, int k, int g,
+                           typename Vec2<T>::type *s_v, T *s_part, double cre, double cim) {
+    using T2 = typename Vec2<T>::type;
+    constexpr int NV = kRT * MG * 2;  // accumulators per lane (16, 32 or 64)
+    constexpr int NB = (NV + 31) / 32;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ld = pb.ld, m = pb.m;
+    const T *H = reinterpret_cast<const T *>(pb.H);
+    T2 *vbuf = reinterpret_cast<T2 *>(pb.vbuf);
+    const size_t gstride = (size_t)pb.ldv * MG;         // one column group
+    const size_t bstride = gstride * (m / MG);          // one of the three vector buffers
+    const T2 *vprev = vbuf + (size_t)((k + 2) % 3) * bstride + g * gstride;   // v_{k-1}
+    const T2 *vprev2 = vbuf + (size_t)((k + 1) % 3) * bstride + g * gstride;  // v_{k-2}
+    T2 *vout = vbuf + (size_t)(k % 3) * bstride + g * gstride;                // v_k
+
+    __syncthreads();
+    for (int q = tid; q < ld * MG; q += kBlock) s_v[q] = ldcg2(vprev + q);  // padding rows are zero
+    __syncthreads();
+
+    const int rows = sg.row1 - sg.row0;
+    int WR = 1;
+    while (WR < kWarps && WR * kRT < rows) WR <<= 1;
+    const int WJ = kWarps / WR;
+    const int wr = warp / WJ, wj = warp % WJ;
+    const int jchunk = ((ld + WJ - 1) / WJ + 31) / 32 * 32;
+    const int j0 = wj * jchunk, j1 = min(ld, j0 + jchunk);
+
+    for (int base = sg.row0; base < sg.row1; base += kRT * WR) {
+        const int r0 = base + kRT * wr;
+        T acc[NB * 32];
+#pragma unroll
+        for (int q = 0; q < NB * 32; ++q) acc[q] = T(0);
+        const T *cols[kRT];
+#pragma unroll
+        for (int r = 0; r < kRT; ++r) cols[r] = H + (size_t)min(r0 + r, sg.row1 - 1) * ld;
+        const bool full = (r0 + kRT <= sg.row1);
+        for (int j = j0 + lane; j < j1; j += 32) {
+            T2 x[MG];
+#pragma unroll
+            for (int c = 0; c < MG; ++c) x[c] = s_v[j * MG + c];
+#pragma unroll
+            for (int r = 0; r < kRT; ++r) {
+                const T h = (full || r0 + r < sg.row1) ? cols[r][j] : T(0);
+#pragma unroll
+                for (int c = 0; c < MG; ++c) {
+                    acc[(r * MG + c) * 2 + 0] = fma(h, x[c].x, acc[(r * MG + c) * 2 + 0]);
+                    acc[(r * MG + c) * 2 + 1] = fma(h, x[c].y, acc[(r * MG + c) * 2 + 1]);
+                }
+            }
+        }
+        // warp sums -> shared memory, layout s_part[wj][wr][NV]
+#pragma unroll
+        for (int b = 0; b < NB; ++b) {
+            T tmp[32];
+#pragma unroll
+            for (int q = 0; q < 32; ++q) tmp[q] = acc[b * 32 + q];
+            const T s = transpose_reduce32(tmp, lane);
+            const int idx = b * 32 + lane;
+            if (idx < NV) s_part[((size_t)wj * WR + wr) * NV + idx] = s;
+        }
+        __syncthreads();
+        // epilogue: one thread per (row, column) of the super-tile
+        for (int t = tid; t < WR * kRT * MG; t += kBlock) {
+            const int wrr = t / (kRT * MG), rem = t % (kRT * MG);
+            const int r = rem / MG, c = rem % MG;
+            const int i = base + kRT * wrr + r;
+            if (i >= sg.row1) continue;
+            T yr = T(0), yi = T(0);
+            for (int w = 0; w < WJ; ++w) {
+                yr += s_part[((size_t)w * WR + wrr) * NV + (r * MG + c) * 2 + 0];
+                yi += s_part[((size_t)w * WR + wrr) * NV + (r * MG + c) * 2 + 1];
+            }
+            T2 v;
+            if (k == 1) {
+                v.x = yr;
+                v.y = yi;
+            } else {
+                const T2 w2 = ldcg2(vprev2 + (size_t)i * MG + c);
+                v.x = T(2) * yr - w2.x;
+                v.y = T(2) * yi - w2.y;
+            }
+            vout[(size_t)i * MG + c] = v;
+            const size_t ao = (size_t)i * m + g * MG + c;
+            double2 a = pb.acc[ao];
+            const double vr = (double)v.x, vi = (double)v.y;
+            a.x += cre * vr - cim * vi;
+            a.y += cre * vi + cim * vr;
+            pb.acc[ao] = a;
+        }
+        __syncthreads();
+    }
+}
+
+// order 0: v_0 = phi (rounded to T), acc = c_0 phi (FP64)
+template <typename T, int MG>
+__device__ void order_zero(const ChebProblem &pb, const ChebSegment &sg) {
+    using T2 = typename Vec2<T>::type;
+    T2 *v0 = reinterpret_cast<T2 *>(pb.vbuf);
+    const int m = pb.m;
+    const size_t gstride = (size_t)pb.ldv * MG;
+    const double cre = pb.coef[0].x, cim = pb.coef[0].y;
+    for (int q = threadIdx.x; q < (sg.row1 - sg.row0) * m; q += kBlock) {
+        const int i = sg.row0 + q / m, col = q % m;
+        const int g = col / MG, c = col % MG;
+        const size_t o = (size_t)i * m + col;
+        const double2 p = pb.phi[o];
+        T2 v;
+        v.x = (T)p.x;
+        v.y = (T)p.y;
+        v0[g * gstride + (size_t)i * MG + c] = v;
+        pb.acc[o] = make_double2(cre * p.x - cim * p.y, cre * p.y + cim * p.x);
+    }
+}
+
+template <typename T, int MG>
+__global__ void __launch_bounds__(kBlock, 1) cheb_kernel(ChebLaunch L) {
+    using T2 = typename Vec2<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *s_part = reinterpret_cast<T *>(smem_raw);
+    T2 *s_v = reinterpret_cast<T2 *>(smem_raw + kCheb_part_bytes);
+    const int G = gridDim.x;
+    const int s0 = L.seg_begin[blockIdx.x], s1 = L.seg_begin[blockIdx.x + 1];
+    for (int k = 0; k <= L.kmax; ++k) {
+        for (int s = s0; s < s1; ++s) {
+            const ChebSegment sg = L.segs[s];
+            const ChebProblem &pb = L.probs[sg.prob];
+            if (k > pb.K) continue;
+            if (k == 0) {
+                order_zero<T, MG>(pb, sg);
+            } else {
+                const double cre = pb.coef[k].x, cim = pb.coef[k].y;
+                for (int g = 0; g < pb.m / MG; ++g) order_rows<T, MG>(pb, sg, k, g, s_v, s_part, cre, cim);
+            }
+        }
+        if (!grid_barrier(L.bar_count, L.bar_gen, G, L.error)) return;
+    }
+}
+
+template <typename T, int MG>
+cudaError_t launch_t(const ChebLaunch &L, cudaStream_t st) {
+    auto kern = cheb_kernel<T, MG>;
+    const size_t smem = kCheb_part_bytes + (size_t)L.max_ld * MG * sizeof(typename Vec2<T>::type);
+    if (smem > kCheb_smem_limit) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    ChebLaunch copy = L;
+    void *args[] = {&copy};
+    return cudaLaunchCooperativeKernel((const void *)kern, dim3(L.grid), dim3(kBlock), args, smem, st);
+}
+
+}  // namespace
+
+int cheb_block() { return kBlock; }
+
+int cheb_group_size(int precision, int m, int max_ld) {
+    // FP64 keeps at most 2 staged columns per pass (4 would spill at 128 registers / thread)
+    const bool fp64 = precision == ELHL_PREC_FP64;
+    const size_t c2 = fp64 ? sizeof(double2) : sizeof(float2);
+    for (int mg : {4, 2, 1})
+        if (!(fp64 && mg > 2) && m % mg == 0 && kCheb_part_bytes + (size_t)max_ld * mg * c2 <= kCheb_smem_limit)
+            return mg;
+    return 0;
+}
+
+cudaError_t launch_cheb(const ChebLaunch &L, int precision, int mg, cudaStream_t st) {
+    if (precision == ELHL_PREC_FP64) {
+        switch (mg) {
+            case 1: return launch_t<double, 1>(L, st);
+            case 2: return launch_t<double, 2>(L, st);
+            case 4: return launch_t<double, 4>(L, st);
+        }
+    } else {
+        switch (mg) {
+            case 1: return launch_t<float, 1>(L, st);
+            case 2: return launch_t<float, 2>(L, st);
+            case 4: return launch_t<float, 4>(L, st);
+        }
+    }
+    return cudaErrorInvalidValue;
+}
+
+int cheb_grid_size(int *grid_out) {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return -1;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
+    *grid_out = sms;
+    return 0;
+}
+
+}  // namespace elhl

@@ -10,6 +10,7 @@
 #include <cublas_v2.h>
 #include <cusolverDn.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -66,6 +67,7 @@ struct Context {
     int device = -1, sms = 0, grid = 0;
     cudaStream_t stream = nullptr, copy_stream = nullptr, own_stream = nullptr;
     cusolverDnHandle_t solver = nullptr;
+    cublasHandle_t blas = nullptr;
     unsigned *bar = nullptr;  // [2] count, gen
     int *err = nullptr;
     double *partials = nullptr;
@@ -84,11 +86,14 @@ int ensure_context_locked(int device) {
     g_ctx.device = device;
     CU_TRY(cudaDeviceGetAttribute(&g_ctx.sms, cudaDevAttrMultiProcessorCount, device));
     if (taylor_grid_size(kTaylorBlock, &g_ctx.grid)) return ELHL_ERR_CUDA;
+    CU_TRY(init_build_tables());
     CU_TRY(cudaStreamCreateWithFlags(&g_ctx.own_stream, cudaStreamNonBlocking));
     g_ctx.stream = g_ctx.own_stream;
     CU_TRY(cudaStreamCreateWithFlags(&g_ctx.copy_stream, cudaStreamNonBlocking));
     SOLVER_TRY(cusolverDnCreate(&g_ctx.solver));
     SOLVER_TRY(cusolverDnSetStream(g_ctx.solver, g_ctx.stream));
+    if (cublasCreate(&g_ctx.blas) != CUBLAS_STATUS_SUCCESS) return ELHL_ERR_CUDA;
+    if (cublasSetStream(g_ctx.blas, g_ctx.stream) != CUBLAS_STATUS_SUCCESS) return ELHL_ERR_CUDA;
     if (int rc = dev_alloc(&g_ctx.bar, 2)) return rc;
     if (int rc = dev_alloc(&g_ctx.err, 1)) return rc;
     if (int rc = dev_alloc(&g_ctx.partials, (size_t)2 * 2 * g_ctx.grid * 16)) return rc;
@@ -123,7 +128,7 @@ __global__ void join_complex(const double *__restrict__ m, double2 *__restrict__
 // the sign convention "largest |component| positive" (first index on ties).
 // One block; ket_full must be zeroed by the caller.
 __global__ void embed_fmo(const double *__restrict__ V, int ldf, int nf, int col, const int *__restrict__ aos,
-                          double2 *__restrict__ ket_full) {
+                          double2 *__restrict__ ket_full, int stride) {
     __shared__ double s_val[256];
     __shared__ int s_idx[256];
     const double *c = V + (size_t)col * ldf;
@@ -148,20 +153,25 @@ __global__ void embed_fmo(const double *__restrict__ V, int ldf, int nf, int col
         __syncthreads();
     }
     const double sign = c[s_idx[0]] < 0.0 ? -1.0 : 1.0;
-    for (int k = threadIdx.x; k < nf; k += blockDim.x) ket_full[aos[k]] = make_double2(sign * c[k], 0.0);
+    for (int k = threadIdx.x; k < nf; k += blockDim.x) ket_full[(size_t)aos[k] * stride] = make_double2(sign * c[k], 0.0);
 }
 
 // bra = S ket for a ket supported on the AO list `aos` (real coefficients)
 __global__ void s_times_sparse(const double *__restrict__ S, int ld, int n, const int *__restrict__ aos, int nf,
-                               const double2 *__restrict__ ket, double2 *__restrict__ bra) {
+                               const double2 *__restrict__ ket, double2 *__restrict__ bra, int stride) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     double acc = 0.0;
     for (int k = 0; k < nf; ++k) {
         const int j = aos[k];
-        acc += S[(size_t)j * ld + i] * ket[j].x;  // S symmetric: S(i, j) = S(j, i)
+        acc += S[(size_t)j * ld + i] * ket[(size_t)j * stride].x;  // S symmetric: S(i, j) = S(j, i)
     }
-    bra[i] = make_double2(acc, 0.0);
+    bra[(size_t)i * stride] = make_double2(acc, 0.0);
+}
+
+__global__ void zero_strided(double2 *v, int n, int stride) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[(size_t)i * stride] = make_double2(0.0, 0.0);
 }
 
 // ---- H' = S^-1 h via Cholesky ------------------------------------------------
@@ -182,6 +192,7 @@ struct Factor {
             return ELHL_ERR_CUDA;
         if (int rc = dev_alloc(&work, (size_t)lwork + 1)) return rc;
         if (int rc = dev_alloc(&info, 2)) return rc;
+        CU_TRY(cudaMemset(info, 0, 2 * sizeof(int)));
         if (int rc = dev_alloc(&cols, (size_t)2 * ld)) return rc;
         return ELHL_OK;
     }
@@ -210,11 +221,12 @@ struct Factor {
         CU_TRY(cudaGetLastError());
         return ELHL_OK;
     }
-    int check_info() {
+    // status words of the last potrf (info[0]) and, with solves, potrs (info[1])
+    int check_info(bool with_solve = true) {
         int h[2] = {0, 0};
         CU_TRY(cudaMemcpy(h, info, 2 * sizeof(int), cudaMemcpyDeviceToHost));
         if (h[0] > 0) return ELHL_ERR_NOT_POSITIVE_DEFINITE;
-        if (h[0] < 0 || h[1] != 0) return ELHL_ERR_BAD_ARG;
+        if (h[0] < 0 || (with_solve && h[1] != 0)) return ELHL_ERR_BAD_ARG;
         return ELHL_OK;
     }
 };
@@ -405,6 +417,344 @@ int dropin_single(int n, double tau, double *save_tau, double t_init, double t_m
     return rc;
 }
 
+#define BLAS_TRY(expr)                                                                \
+    do {                                                                              \
+        cublasStatus_t b_ = (expr);                                                   \
+        if (b_ != CUBLAS_STATUS_SUCCESS) {                                            \
+            fprintf(stderr, "elhlprop: %s failed: status %d\n", #expr, (int)b_);      \
+            return ELHL_ERR_CUDA;                                                     \
+        }                                                                             \
+    } while (0)
+
+// ---- Chebyshev state of one problem ------------------------------------------
+// H~ = L^-1 h L^-T (FP64), its scaled copy Hs = (H~ - a)/b in the launch
+// precision, the expansion coefficients and the column buffers.
+__global__ void symmetrize_kernel(double *A, int n, int ld) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= n || j >= n || i <= j) return;
+    const double v = 0.5 * (A[(size_t)j * ld + i] + A[(size_t)i * ld + j]);
+    A[(size_t)j * ld + i] = v;
+    A[(size_t)i * ld + j] = v;
+}
+
+template <typename T>
+__global__ void scale_kernel(const double *__restrict__ Ht, T *__restrict__ Hs, int n, int ld, double a, double binv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= ld || j >= n) return;
+    const double v = (i < n) ? (Ht[(size_t)j * ld + i] - (i == j ? a : 0.0)) * binv : 0.0;
+    Hs[(size_t)j * ld + i] = (T)v;
+}
+
+// pops[p*(nfrag+1) + f] = Re sum_{i in f} conj(psi_ip) bra_ip over column p of
+// [ld][m] arrays; one block per particle, fixed-order tree reduction.
+__global__ void populations_kernel(const double2 *__restrict__ psi, const double2 *__restrict__ bra, int n, int m,
+                                   const int *__restrict__ ao_frag, int nfrag, double *__restrict__ pops) {
+    __shared__ double red[kMaxFrag + 1][256];
+    const int p = blockIdx.x;
+    double acc[kMaxFrag + 1];
+    for (int f = 0; f <= kMaxFrag; ++f) acc[f] = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double2 a = psi[(size_t)i * m + p], b = bra[(size_t)i * m + p];
+        const double v = a.x * b.x + a.y * b.y;
+        if (ao_frag) {
+            const int f = ao_frag[i];
+            if (f >= 0 && f < nfrag && f < kMaxFrag) acc[f] += v;
+        }
+        acc[kMaxFrag] += v;
+    }
+    for (int f = 0; f <= kMaxFrag; ++f) red[f][threadIdx.x] = acc[f];
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o)
+            for (int f = 0; f <= kMaxFrag; ++f) red[f][threadIdx.x] += red[f][threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        for (int f = 0; f < nfrag && f < kMaxFrag; ++f) pops[(size_t)p * (nfrag + 1) + f] = red[f][0];
+        pops[(size_t)p * (nfrag + 1) + nfrag] = red[kMaxFrag][0];
+    }
+}
+
+// After a reduced-precision step: scale particle p's propagated columns (ket
+// column p and, when bra columns are carried, column P + p) so that its total
+// population returns to the target (FP64 norm control).
+__global__ void renormalize_kernel(double2 *cols, int n, int m, int P, const double *pops, int nfrag,
+                                   const double *target) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    for (int p = 0; p < P; ++p) {
+        const double tot = pops[(size_t)p * (nfrag + 1) + nfrag];
+        const double s = (tot > 0.0 && target[p] > 0.0) ? sqrt(target[p] / tot) : 1.0;
+        double2 a = cols[(size_t)i * m + p];
+        cols[(size_t)i * m + p] = make_double2(a.x * s, a.y * s);
+        if (m == 2 * P) {
+            double2 b = cols[(size_t)i * m + P + p];
+            cols[(size_t)i * m + P + p] = make_double2(b.x * s, b.y * s);
+        }
+    }
+}
+
+struct ChebState {
+    int N = 0, ld = 0, m = 0, precision = ELHL_PREC_FP64, K = 0;
+    double *Ht = nullptr;    // FP64 H~
+    void *Hs = nullptr;      // scaled, launch precision
+    void *vbuf = nullptr;
+    double2 *phi = nullptr, *acc = nullptr;  // [ld][m]
+    double2 *coef = nullptr;
+    int coef_cap = 0;
+    double emin = 0.0, emax = 0.0, a = 0.0, b = 1.0;
+    double *lz = nullptr;    // Lanczos vectors [3][ld]
+    int alloc(int N_, int m_, int prec) {
+        N = N_;
+        ld = round_up(N, 32);
+        m = m_;
+        precision = prec;
+        const size_t tsz = prec == ELHL_PREC_FP64 ? sizeof(double) : sizeof(float);
+        if (int rc = dev_alloc(&Ht, (size_t)ld * N)) return rc;
+        CU_TRY(cudaMalloc(&Hs, (size_t)ld * N * tsz));
+        CU_TRY(cudaMalloc(&vbuf, (size_t)3 * ld * m * 2 * tsz));
+        CU_TRY(cudaMemset(vbuf, 0, (size_t)3 * ld * m * 2 * tsz));
+        if (int rc = dev_alloc(&phi, (size_t)ld * m)) return rc;
+        if (int rc = dev_alloc(&acc, (size_t)ld * m)) return rc;
+        CU_TRY(cudaMemset(phi, 0, (size_t)ld * m * sizeof(double2)));
+        CU_TRY(cudaMemset(acc, 0, (size_t)ld * m * sizeof(double2)));
+        if (int rc = dev_alloc(&lz, (size_t)3 * ld)) return rc;
+        return ELHL_OK;
+    }
+    void release() {
+        dev_free(Ht); dev_free(phi); dev_free(acc); dev_free(coef); dev_free(lz);
+        if (Hs) cudaFree(Hs);
+        if (vbuf) cudaFree(vbuf);
+        Hs = vbuf = nullptr;
+        coef_cap = 0;
+    }
+};
+
+// H~ = L^-1 h L^-T from the Cholesky factor (lower) and h, then symmetrised.
+int form_htilde(ChebState &cs, const double *Lfac, const double *h, int ld) {
+    cudaStream_t st = g_ctx.stream;
+    const int n = cs.N;
+    const double one = 1.0;
+    CU_TRY(cudaMemcpy2DAsync(cs.Ht, cs.ld * sizeof(double), h, ld * sizeof(double), n * sizeof(double), n,
+                             cudaMemcpyDeviceToDevice, st));
+    BLAS_TRY(cublasDtrsm(g_ctx.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n,
+                         n, &one, Lfac, ld, cs.Ht, cs.ld));
+    BLAS_TRY(cublasDtrsm(g_ctx.blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n,
+                         n, &one, Lfac, ld, cs.Ht, cs.ld));
+    symmetrize_kernel<<<dim3((n + 127) / 128, n), 128, 0, st>>>(cs.Ht, n, cs.ld);
+    CU_TRY(cudaGetLastError());
+    return ELHL_OK;
+}
+
+__global__ void lanczos_start(double *v, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = 1.0 + 0.5 * sin(1.37 * i + 0.2);  // deterministic, every component present
+}
+
+// Spectral bounds of H~ by FP64 Lanczos (k steps, no reorthogonalisation) with
+// a guard of |beta_k s_k| + 1 % of the width around the extreme Ritz values.
+int lanczos_bounds(ChebState &cs, int ksteps) {
+    const int n = cs.N;
+    cudaStream_t st = g_ctx.stream;
+    double *v = cs.lz, *vp = cs.lz + cs.ld, *w = cs.lz + 2 * cs.ld;
+    lanczos_start<<<(n + 255) / 256, 256, 0, st>>>(v, n);
+    CU_TRY(cudaMemsetAsync(vp, 0, n * sizeof(double), st));
+    double nrm = 0.0;
+    BLAS_TRY(cublasDnrm2(g_ctx.blas, n, v, 1, &nrm));
+    double inv = 1.0 / nrm;
+    BLAS_TRY(cublasDscal(g_ctx.blas, n, &inv, v, 1));
+    const int k = std::min(ksteps, n);
+    std::vector<double> alpha(k), beta(k);
+    double bprev = 0.0;
+    int used = 0;
+    const double one = 1.0, zero = 0.0;
+    for (int j = 0; j < k; ++j) {
+        BLAS_TRY(cublasDsymv(g_ctx.blas, CUBLAS_FILL_MODE_LOWER, n, &one, cs.Ht, cs.ld, v, 1, &zero, w, 1));
+        double al = 0.0;
+        BLAS_TRY(cublasDdot(g_ctx.blas, n, w, 1, v, 1, &al));
+        const double mal = -al, mb = -bprev;
+        BLAS_TRY(cublasDaxpy(g_ctx.blas, n, &mal, v, 1, w, 1));
+        BLAS_TRY(cublasDaxpy(g_ctx.blas, n, &mb, vp, 1, w, 1));
+        double be = 0.0;
+        BLAS_TRY(cublasDnrm2(g_ctx.blas, n, w, 1, &be));
+        alpha[j] = al;
+        beta[j] = be;
+        used = j + 1;
+        if (!(be > 1e-10 * (std::fabs(al) + 1.0))) break;
+        std::swap(vp, v);  // vp <- v
+        const double ib = 1.0 / be;
+        BLAS_TRY(cublasDcopy(g_ctx.blas, n, w, 1, v, 1));
+        BLAS_TRY(cublasDscal(g_ctx.blas, n, &ib, v, 1));
+        bprev = be;
+    }
+    double lo = 0.0, hi = 0.0;
+    tridiagonal_extremes(alpha.data(), beta.data(), used, &lo, &hi);
+    const double bk = beta[used - 1];
+    const double rlo = bk * tridiagonal_last_component(alpha.data(), beta.data(), used, lo);
+    const double rhi = bk * tridiagonal_last_component(alpha.data(), beta.data(), used, hi);
+    const double width = hi - lo;
+    cs.emin = lo - rlo - 0.01 * width;
+    cs.emax = hi + rhi + 0.01 * width;
+    if (!(cs.emax > cs.emin) || !std::isfinite(cs.emin) || !std::isfinite(cs.emax)) return ELHL_ERR_NO_CONVERGENCE;
+    return ELHL_OK;
+}
+
+// Hs and the coefficients for step dt on the current bounds.
+int cheb_prepare(ChebState &cs, double dt, double tol) {
+    cudaStream_t st = g_ctx.stream;
+    cs.a = 0.5 * (cs.emax + cs.emin);
+    cs.b = 0.5 * (cs.emax - cs.emin);
+    const double binv = 1.0 / cs.b;
+    dim3 grid((cs.ld + 127) / 128, cs.N);
+    if (cs.precision == ELHL_PREC_FP64)
+        scale_kernel<double><<<grid, 128, 0, st>>>(cs.Ht, (double *)cs.Hs, cs.N, cs.ld, cs.a, binv);
+    else
+        scale_kernel<float><<<grid, 128, 0, st>>>(cs.Ht, (float *)cs.Hs, cs.N, cs.ld, cs.a, binv);
+    CU_TRY(cudaGetLastError());
+    std::vector<double> cre, cim;
+    int K = 0;
+    if (int rc = chebyshev_coefficients(dt, cs.emin, cs.emax, tol, 20000, cre, cim, &K)) return rc;
+    if (K + 1 > cs.coef_cap) {
+        dev_free(cs.coef);
+        if (int rc = dev_alloc(&cs.coef, (size_t)K + 1)) return rc;
+        cs.coef_cap = K + 1;
+    }
+    std::vector<double2> c(K + 1);
+    for (int k = 0; k <= K; ++k) c[k] = make_double2(cre[k], cim[k]);
+    CU_TRY(cudaMemcpyAsync(cs.coef, c.data(), (K + 1) * sizeof(double2), cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaStreamSynchronize(st));  // c is a host temporary
+    cs.K = K;
+    return ELHL_OK;
+}
+
+// Launch plan for a set of problems: row segments balanced by matrix elements.
+struct ChebPlan {
+    std::vector<ChebProblem> probs;
+    std::vector<ChebSegment> segs;
+    std::vector<int> seg_begin;
+    ChebProblem *d_probs = nullptr;
+    ChebSegment *d_segs = nullptr;
+    int *d_seg_begin = nullptr;
+    int grid = 0, max_ld = 0, kmax = 0, mg = 0, precision = 0;
+    void release() {
+        dev_free(d_probs); dev_free(d_segs); dev_free(d_seg_begin);
+    }
+};
+
+int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
+    pl.release();
+    pl.probs.clear();
+    pl.segs.clear();
+    if (states.empty()) return ELHL_ERR_BAD_ARG;
+    if (cheb_grid_size(&pl.grid)) return ELHL_ERR_CUDA;
+    pl.max_ld = 0;
+    pl.kmax = 0;
+    pl.precision = states[0]->precision;
+    double work = 0.0;
+    int mgcd = 0;  // staged group size must divide every problem's column count
+    for (auto *cs : states) {
+        if (cs->precision != pl.precision || cs->m <= 0) return ELHL_ERR_BAD_ARG;
+        pl.max_ld = std::max(pl.max_ld, cs->ld);
+        work += (double)cs->N * cs->ld;
+        int a = cs->m, b = mgcd;
+        while (b) { const int t = a % b; a = b; b = t; }
+        mgcd = a;
+    }
+    pl.mg = cheb_group_size(pl.precision, mgcd, pl.max_ld);
+    if (!pl.mg) return ELHL_ERR_UNSUPPORTED;
+    for (auto *cs : states) {
+        ChebProblem p{};
+        p.N = cs->N; p.ld = cs->ld; p.ldv = cs->ld; p.m = cs->m; p.K = cs->K;
+        p.H = cs->Hs; p.vbuf = cs->vbuf; p.phi = cs->phi; p.acc = cs->acc; p.coef = cs->coef;
+        pl.probs.push_back(p);
+        pl.kmax = std::max(pl.kmax, cs->K);
+    }
+    // greedy split of the concatenated rows: CTA c fills up to (c+1)/grid of the work
+    const double per = work / pl.grid;
+    pl.seg_begin.assign(pl.grid + 1, 0);
+    int c = 0;
+    double acc_w = 0.0;
+    for (int q = 0; q < (int)states.size(); ++q) {
+        const ChebState *cs = states[q];
+        const double rw = cs->ld;  // work per row
+        int r = 0;
+        while (r < cs->N) {
+            int take = cs->N - r;
+            if (c < pl.grid - 1) {
+                const double room = per * (c + 1) - acc_w;
+                take = std::min(take, std::max(1, (int)std::floor(room / rw + 0.5)));
+            }
+            pl.segs.push_back({q, r, r + take});
+            acc_w += take * rw;
+            r += take;
+            if (c < pl.grid - 1 && acc_w >= per * (c + 1) - 0.5 * rw) {
+                ++c;
+                pl.seg_begin[c] = (int)pl.segs.size();
+            }
+        }
+    }
+    for (int cc = c + 1; cc <= pl.grid; ++cc) pl.seg_begin[cc] = (int)pl.segs.size();
+    if (int rc = dev_alloc(&pl.d_probs, pl.probs.size())) return rc;
+    if (int rc = dev_alloc(&pl.d_segs, pl.segs.size())) return rc;
+    if (int rc = dev_alloc(&pl.d_seg_begin, pl.seg_begin.size())) return rc;
+    CU_TRY(cudaMemcpy(pl.d_probs, pl.probs.data(), pl.probs.size() * sizeof(ChebProblem), cudaMemcpyHostToDevice));
+    CU_TRY(cudaMemcpy(pl.d_segs, pl.segs.data(), pl.segs.size() * sizeof(ChebSegment), cudaMemcpyHostToDevice));
+    CU_TRY(cudaMemcpy(pl.d_seg_begin, pl.seg_begin.data(), pl.seg_begin.size() * sizeof(int), cudaMemcpyHostToDevice));
+    return ELHL_OK;
+}
+
+// refresh per-problem order counts and coefficient pointers after cheb_prepare
+int cheb_plan_refresh(ChebPlan &pl, const std::vector<ChebState *> &states) {
+    pl.kmax = 0;
+    for (size_t q = 0; q < states.size(); ++q) {
+        pl.probs[q].K = states[q]->K;
+        pl.probs[q].coef = states[q]->coef;
+        pl.kmax = std::max(pl.kmax, states[q]->K);
+    }
+    CU_TRY(cudaMemcpy(pl.d_probs, pl.probs.data(), pl.probs.size() * sizeof(ChebProblem), cudaMemcpyHostToDevice));
+    return ELHL_OK;
+}
+
+int cheb_run(ChebPlan &pl) {
+    cudaStream_t st = g_ctx.stream;
+    CU_TRY(cudaMemsetAsync(g_ctx.err, 0, sizeof(int), st));
+    CU_TRY(cudaMemsetAsync(g_ctx.bar, 0, 2 * sizeof(unsigned), st));
+    ChebLaunch L{};
+    L.probs = pl.d_probs;
+    L.segs = pl.d_segs;
+    L.seg_begin = pl.d_seg_begin;
+    L.kmax = pl.kmax;
+    L.max_ld = pl.max_ld;
+    L.grid = pl.grid;
+    L.bar_count = g_ctx.bar;
+    L.bar_gen = g_ctx.bar + 1;
+    L.error = g_ctx.err;
+    CU_TRY(cudaEventRecord(g_ctx.ev[0], st));
+    CU_TRY(launch_cheb(L, pl.precision, pl.mg, st));
+    CU_TRY(cudaEventRecord(g_ctx.ev[1], st));
+    return ELHL_OK;
+}
+
+// Complex columns stored [ld][m] (interleaved) are the rows of a 2m x N
+// column-major real matrix X; right-side triangular operations act on every
+// column at once:  X L  = (L^T x)^T,  X L^-1 = (L^-T x)^T,
+//                  X L^T = (L x)^T,   X L^-T = (L^-1 x)^T.
+int cols_apply(const double *Lfac, int ld, int n, double2 *cols, int m, int col0, int ncols, bool transpose,
+               bool inverse) {
+    const double one = 1.0;
+    double *X = reinterpret_cast<double *>(cols) + 2 * col0;
+    const int rows = 2 * ncols, ldx = 2 * m;
+    const cublasOperation_t op = transpose ? CUBLAS_OP_T : CUBLAS_OP_N;
+    if (inverse) {
+        BLAS_TRY(cublasDtrsm(g_ctx.blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, op, CUBLAS_DIAG_NON_UNIT, rows, n,
+                             &one, Lfac, ld, X, ldx));
+    } else {
+        BLAS_TRY(cublasDtrmm(g_ctx.blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, op, CUBLAS_DIAG_NON_UNIT, rows, n,
+                             &one, Lfac, ld, X, ldx, X, ldx));
+    }
+    return ELHL_OK;
+}
+
 }  // namespace
 
 // =============================== trajectories ===================================
@@ -425,6 +775,12 @@ struct elhl_traj {
     bool first_call = true;
     double save_tau[2] = {0.0, 0.0};
     elhl_traj_stats stats{};
+    // Chebyshev method: AO-basis Psi_ket / Psi_bra as [ld][2] (row i, particle p)
+    ChebState cs;
+    ChebPlan plan;
+    double2 *psi_ao = nullptr, *bra_ao = nullptr, *ro_ket = nullptr, *ro_bra = nullptr;
+    double *target = nullptr;  // per-particle total population to hold (reduced precision)
+    bool cheb() const { return cfg.method == ELHL_METHOD_CHEBYSHEV; }
 };
 
 namespace {
@@ -490,8 +846,121 @@ int rebuild(elhl_traj *tr, const double *d_coords) {
     tr->last_coords = d_coords;
     CU_TRY(cudaEventRecord(g_ctx.ev[2], g_ctx.stream));
     CU_TRY(launch_build_sh(tr->basis, d_coords, tr->cfg.cutoff, tr->S, tr->h, tr->ld, g_ctx.stream));
-    int rc = tr->fac.form_hprime(tr->S, tr->h, tr->Hp, tr->N);
+    int rc = tr->cheb() ? ELHL_OK : tr->fac.form_hprime(tr->S, tr->h, tr->Hp, tr->N);
     CU_TRY(cudaEventRecord(g_ctx.ev[3], g_ctx.stream));
+    return rc;
+}
+
+// Cholesky factor, H~, bounds and coefficients for the current S, h.
+int cheb_rebuild_operator(elhl_traj *tr) {
+    cudaStream_t st = g_ctx.stream;
+    CU_TRY(cudaMemcpy2DAsync(tr->fac.L, tr->ld * sizeof(double), tr->S, tr->ld * sizeof(double), tr->N * sizeof(double),
+                             tr->N, cudaMemcpyDeviceToDevice, st));
+    SOLVER_TRY(cusolverDnDpotrf(g_ctx.solver, CUBLAS_FILL_MODE_LOWER, tr->N, tr->fac.L, tr->ld, tr->fac.work,
+                                tr->fac.lwork, tr->fac.info));
+    if (int rc = tr->fac.check_info(false)) return rc;
+    if (int rc = form_htilde(tr->cs, tr->fac.L, tr->h, tr->ld)) return rc;
+    if (int rc = lanczos_bounds(tr->cs, 40)) return rc;
+    return cheb_prepare(tr->cs, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol);
+}
+
+// phi <- transformed columns of (psi_ao, bra_ao) with the current factor
+int cheb_load_columns(elhl_traj *tr) {
+    cudaStream_t st = g_ctx.stream;
+    ChebState &cs = tr->cs;
+    const int P = tr->P, n = tr->N;
+    const size_t e = sizeof(double2);
+    CU_TRY(cudaMemcpy2DAsync(cs.phi, cs.m * e, tr->psi_ao, P * e, P * e, n, cudaMemcpyDeviceToDevice, st));
+    if (cs.m == 2 * P)
+        CU_TRY(cudaMemcpy2DAsync(cs.phi + P, cs.m * e, tr->bra_ao, P * e, P * e, n, cudaMemcpyDeviceToDevice, st));
+    if (int rc = cols_apply(tr->fac.L, tr->ld, n, cs.phi, cs.m, 0, P, false, false)) return rc;       // L^T psi
+    if (cs.m == 2 * P)
+        if (int rc = cols_apply(tr->fac.L, tr->ld, n, cs.phi, cs.m, P, P, true, true)) return rc;    // L^-1 bra
+    return ELHL_OK;
+}
+
+// psi_ao, bra_ao <- back-transformed columns of acc; populations into d_pops
+int cheb_readout(elhl_traj *tr, const double2 *cols, double *d_pops) {
+    cudaStream_t st = g_ctx.stream;
+    ChebState &cs = tr->cs;
+    const int P = tr->P, n = tr->N;
+    const size_t e = sizeof(double2);
+    CU_TRY(cudaMemcpy2DAsync(tr->psi_ao, P * e, cols, cs.m * e, P * e, n, cudaMemcpyDeviceToDevice, st));
+    if (int rc = cols_apply(tr->fac.L, tr->ld, n, tr->psi_ao, P, 0, P, false, true)) return rc;       // L^-T phi
+    const double2 *bsrc = (cs.m == 2 * P) ? cols + P : cols;
+    CU_TRY(cudaMemcpy2DAsync(tr->bra_ao, P * e, bsrc, cs.m * e, P * e, n, cudaMemcpyDeviceToDevice, st));
+    if (int rc = cols_apply(tr->fac.L, tr->ld, n, tr->bra_ao, P, 0, P, true, false)) return rc;       // L chi
+    if (d_pops) {
+        populations_kernel<<<P, 256, 0, st>>>(tr->psi_ao, tr->bra_ao, n, P, tr->basis.ao_frag, tr->nfrag, d_pops);
+        CU_TRY(cudaGetLastError());
+    }
+    return ELHL_OK;
+}
+
+int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, int nsteps, double *d_pops) {
+    cudaStream_t st = g_ctx.stream;
+    ChebState &cs = tr->cs;
+    const int P = tr->P, nf = tr->nfrag;
+    const size_t pop_per_step = (size_t)P * (nf + 1);
+    const size_t nc = (size_t)tr->natoms * 3;
+    const bool renorm = cs.precision != ELHL_PREC_FP64;
+    double *pops_tmp = nullptr;
+    if (!d_pops && renorm) {
+        if (int rc = dev_alloc(&pops_tmp, pop_per_step)) return rc;
+    }
+    int rc = ELHL_OK;
+    std::vector<ChebState *> one{&cs};
+    if (!coords) rc = cheb_load_columns(tr);
+    for (int s = 0; s < nsteps && !rc; ++s) {
+        if (coords) {
+            const double *dc;
+            if (coords_on_device) {
+                dc = coords + s * nc;
+            } else {
+                if (cudaMemcpyAsync(tr->coords, coords + s * nc, nc * sizeof(double), cudaMemcpyHostToDevice, st) !=
+                    cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
+                dc = tr->coords;
+            }
+            tr->last_coords = dc;
+            if (cudaEventRecord(g_ctx.ev[2], st) != cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
+            if (launch_build_sh(tr->basis, dc, tr->cfg.cutoff, tr->S, tr->h, tr->ld, st) != cudaSuccess) {
+                rc = ELHL_ERR_CUDA;
+                break;
+            }
+            if ((rc = cheb_rebuild_operator(tr))) break;
+            if ((rc = cheb_load_columns(tr))) break;
+            if (cudaEventRecord(g_ctx.ev[3], st) != cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
+            if ((rc = cheb_plan_refresh(tr->plan, one))) break;
+        }
+        if ((rc = cheb_run(tr->plan))) break;
+        double *pp = d_pops ? d_pops + s * pop_per_step : pops_tmp;
+        if ((rc = cheb_readout(tr, cs.acc, pp))) break;
+        if (renorm) {
+            renormalize_kernel<<<(tr->N + 255) / 256, 256, 0, st>>>(cs.acc, tr->N, cs.m, P, pp, nf, tr->target);
+            if (cudaGetLastError() != cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
+            if ((rc = cheb_readout(tr, cs.acc, nullptr))) break;  // AO state follows the renormalised columns
+        }
+        if (cudaMemcpyAsync(cs.phi, cs.acc, (size_t)cs.ld * cs.m * sizeof(double2), cudaMemcpyDeviceToDevice, st) !=
+            cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
+        int err = 0;
+        if (cudaMemcpyAsync(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+            cudaStreamSynchronize(st) != cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
+        if (err) { rc = err; break; }
+        tr->stats.prop_ms += event_ms(0, 1);
+        tr->stats.prop_launches += 1;
+        tr->stats.orders += (long long)cs.K * cs.m;
+        if (coords) {
+            tr->stats.rebuild_ms += event_ms(2, 3);
+            tr->stats.rebuild_count += 1;
+        }
+        tr->stats.substeps += 1;
+        tr->t = tr->t + tr->cfg.dt * tr->cfg.frame_step;
+        tr->it += 1;
+        tr->first_call = false;
+    }
+    dev_free(pops_tmp);
+    for (int p = 0; p < P; ++p) tr->save_tau[p] = tr->cfg.dt / kHbar;
+    tr->stats.status = rc;
     return rc;
 }
 
@@ -522,6 +991,12 @@ int traj_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
         }
     };
     memset(&tr->stats, 0, sizeof(tr->stats));
+    if (tr->cheb()) {
+        if (int rc = cheb_step_impl(tr, coords, coords_on_device, nsteps, d_pops)) return rc;
+        if (pops && !pops_on_device)
+            CU_TRY(cudaMemcpy(pops, d_pops, nsteps * pop_per_step * sizeof(double), cudaMemcpyDeviceToHost));
+        return ELHL_OK;
+    }
     if (!coords) {
         // fixed nuclei: S, h, H' unchanged; the whole run is one launch
         double taus[2];
@@ -593,8 +1068,8 @@ int traj_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
 }
 
 // Initial state of particle p from fragment MO `state` (1-based).
-int fmo_particle(elhl_traj *tr, int nat, const int *atoms, int state, int p) {
-    if (nat <= 0 || !atoms || state < 1) return ELHL_ERR_BAD_ARG;
+int fmo_particle(elhl_traj *tr, int nat, const int *atoms, int state, double2 *ket, double2 *bra, int stride) {
+    if (nat <= 0 || !atoms || state < 1 || !tr->S) return ELHL_ERR_BAD_ARG;
     std::vector<int> ao0, nao, n, l, m, nz, aos;
     std::vector<double> zeta, coef, ip, kwh, vs;
     for (int a = 0; a < nat; ++a) {
@@ -646,10 +1121,9 @@ int fmo_particle(elhl_traj *tr, int nat, const int *atoms, int state, int p) {
                                 nf, hf, ldf, Sf, ldf, w, work, lwork, info) != CUSOLVER_STATUS_SUCCESS)
         rc = ELHL_ERR_CUDA;
     if (!rc) {
-        double2 *ket = tr->tb.ket(p), *bra = tr->tb.bra(p);
-        if (cudaMemsetAsync(ket, 0, tr->N * sizeof(double2), st) != cudaSuccess) rc = ELHL_ERR_CUDA;
-        embed_fmo<<<1, 256, 0, st>>>(hf, ldf, nf, state - 1, daos, ket);
-        s_times_sparse<<<(tr->N + 127) / 128, 128, 0, st>>>(tr->S, tr->ld, tr->N, daos, nf, ket, bra);
+        zero_strided<<<(tr->N + 255) / 256, 256, 0, st>>>(ket, tr->N, stride);
+        embed_fmo<<<1, 256, 0, st>>>(hf, ldf, nf, state - 1, daos, ket, stride);
+        s_times_sparse<<<(tr->N + 127) / 128, 128, 0, st>>>(tr->S, tr->ld, tr->N, daos, nf, ket, bra, stride);
         if (cudaGetLastError() != cudaSuccess) rc = ELHL_ERR_CUDA;
     }
     int hinfo = 0;
@@ -659,6 +1133,44 @@ int fmo_particle(elhl_traj *tr, int nat, const int *atoms, int state, int p) {
     free_basis(fb);
     dev_free(Sf); dev_free(hf); dev_free(w); dev_free(dc); dev_free(work); dev_free(info); dev_free(daos);
     return rc;
+}
+
+int cheb_set_target(elhl_traj *tr);
+
+// Psi (host, column-major N x P) into the [ld][P] AO arrays; bra = S ket when
+// bra is NULL.  The norm target of each particle is its initial total population.
+int cheb_set_psi(elhl_traj *tr, const elhl_zcomplex *bra, const elhl_zcomplex *ket) {
+    if (!bra && !tr->S) return ELHL_ERR_BAD_ARG;  // S was released by elhl_batch_compact
+    const size_t e = sizeof(double2);
+    const int P = tr->P, n = tr->N;
+    for (int p = 0; p < P; ++p)
+        CU_TRY(cudaMemcpy2D(tr->psi_ao + p, P * e, ket + (size_t)p * n, e, e, n, cudaMemcpyHostToDevice));
+    if (bra) {
+        for (int p = 0; p < P; ++p)
+            CU_TRY(cudaMemcpy2D(tr->bra_ao + p, P * e, bra + (size_t)p * n, e, e, n, cudaMemcpyHostToDevice));
+    } else {
+        // bra = S ket: the complex columns as a 2P x N real matrix times S (symmetric)
+        const double one = 1.0, zero = 0.0;
+        BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * P, n, n, &one, (const double *)tr->psi_ao, 2 * P,
+                             tr->S, tr->ld, &zero, (double *)tr->bra_ao, 2 * P));
+    }
+    return cheb_set_target(tr);
+}
+
+// norm target of each particle = its current total population
+int cheb_set_target(elhl_traj *tr) {
+    const int P = tr->P, n = tr->N;
+    double *pops = nullptr;
+    if (int rc = dev_alloc(&pops, (size_t)P * (tr->nfrag + 1))) return rc;
+    populations_kernel<<<P, 256, 0, g_ctx.stream>>>(tr->psi_ao, tr->bra_ao, n, P, tr->basis.ao_frag, tr->nfrag, pops);
+    std::vector<double> h((size_t)P * (tr->nfrag + 1)), tgt(P);
+    cudaError_t ce = cudaMemcpyAsync(h.data(), pops, h.size() * sizeof(double), cudaMemcpyDeviceToHost, g_ctx.stream);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(g_ctx.stream);
+    dev_free(pops);
+    CU_TRY(ce);
+    for (int p = 0; p < P; ++p) tgt[p] = h[(size_t)p * (tr->nfrag + 1) + tr->nfrag];
+    CU_TRY(cudaMemcpy(tr->target, tgt.data(), P * sizeof(double), cudaMemcpyHostToDevice));
+    return ELHL_OK;
 }
 
 }  // namespace
@@ -695,6 +1207,7 @@ int elhl_set_stream(void *stream) {
     CU_TRY(cudaStreamSynchronize(g_ctx.stream));
     g_ctx.stream = stream ? (cudaStream_t)stream : g_ctx.own_stream;
     SOLVER_TRY(cusolverDnSetStream(g_ctx.solver, g_ctx.stream));
+    if (cublasSetStream(g_ctx.blas, g_ctx.stream) != CUBLAS_STATUS_SUCCESS) return ELHL_ERR_CUDA;
     return ELHL_OK;
 }
 
@@ -720,6 +1233,8 @@ void gpu_finalize_(void) {
     dev_free(g_ctx.err);
     dev_free(g_ctx.partials);
     if (g_ctx.solver) cusolverDnDestroy(g_ctx.solver);
+    if (g_ctx.blas) cublasDestroy(g_ctx.blas);
+    g_ctx.blas = nullptr;
     if (g_ctx.own_stream) cudaStreamDestroy(g_ctx.own_stream);
     if (g_ctx.copy_stream) cudaStreamDestroy(g_ctx.copy_stream);
     g_ctx.solver = nullptr;
@@ -770,6 +1285,7 @@ void elhl_traj_config_default(elhl_traj_config *c) {
     c->cutoff = 12.0;
     c->max_conv_calls = 2000;
     c->ncols = 2;
+    c->nparticles = 2;
 }
 
 int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const elhl_traj_config *cfg,
@@ -780,13 +1296,20 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
     if (int rc = ensure_context()) return rc;
     elhl_traj *tr = new elhl_traj();
     if (cfg) tr->cfg = *cfg; else elhl_traj_config_default(&tr->cfg);
-    if (tr->cfg.method != ELHL_METHOD_TAYLOR_REF || tr->cfg.precision != ELHL_PREC_FP64 || tr->cfg.dt <= 0 ||
-        tr->cfg.frame_step <= 0 || tr->cfg.max_conv_calls <= 0) {
+    const bool taylor_ok = tr->cfg.method == ELHL_METHOD_TAYLOR_REF && tr->cfg.precision == ELHL_PREC_FP64;
+    const bool taylor_p = tr->cfg.nparticles == 2;
+    const bool cheb_ok = tr->cfg.method == ELHL_METHOD_CHEBYSHEV &&
+                         (tr->cfg.precision == ELHL_PREC_FP64 || tr->cfg.precision == ELHL_PREC_FP32) &&
+                         tr->cfg.nparticles >= 1 && tr->cfg.nparticles <= 64 &&
+                         (tr->cfg.ncols == tr->cfg.nparticles || tr->cfg.ncols == 2 * tr->cfg.nparticles) &&
+                         tr->cfg.cheb_tol > 0.0;
+    if (!((taylor_ok && taylor_p) || cheb_ok) || tr->cfg.dt <= 0 || tr->cfg.frame_step <= 0 || tr->cfg.max_conv_calls <= 0) {
         delete tr;
         return ELHL_ERR_UNSUPPORTED;
     }
     tr->N = basis->nao;
     tr->ld = round_up(tr->N, 32);
+    tr->P = tr->cfg.nparticles;
     tr->h_ao0.assign(basis->atom_ao0, basis->atom_ao0 + basis->natoms);
     tr->h_nao.assign(basis->atom_nao, basis->atom_nao + basis->natoms);
     tr->h_n.assign(basis->ao_n, basis->ao_n + basis->nao);
@@ -804,16 +1327,27 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
     std::lock_guard<std::mutex> lk(g_ctx.mu);
     if (!rc) rc = dev_alloc(&tr->S, (size_t)tr->ld * tr->N);
     if (!rc) rc = dev_alloc(&tr->h, (size_t)tr->ld * tr->N);
-    if (!rc) rc = dev_alloc(&tr->Hp, (size_t)tr->ld * tr->N);
+    if (!rc && !tr->cheb()) rc = dev_alloc(&tr->Hp, (size_t)tr->ld * tr->N);
     if (!rc) rc = dev_alloc(&tr->coords, (size_t)tr->natoms * 3);
     if (!rc) tr->coords_cap = tr->natoms * 3;
     if (!rc) rc = tr->fac.reserve(tr->N, tr->ld);
-    if (!rc) rc = tr->tb.reserve(tr->N, tr->P);
+    if (!rc && !tr->cheb()) rc = tr->tb.reserve(tr->N, tr->P);
     if (!rc && cudaMemcpy(tr->coords, coords, tr->natoms * 3 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
         rc = ELHL_ERR_CUDA;
     if (!rc) rc = rebuild(tr, tr->coords);
     if (!rc && cudaStreamSynchronize(g_ctx.stream) != cudaSuccess) rc = ELHL_ERR_CUDA;
-    if (!rc) rc = tr->fac.check_info();
+    if (!rc && !tr->cheb()) rc = tr->fac.check_info();  // the Chebyshev set-up factors S below
+    if (!rc && tr->cheb()) {
+        rc = tr->cs.alloc(tr->N, tr->cfg.ncols, tr->cfg.precision);
+        if (!rc) rc = dev_alloc(&tr->psi_ao, (size_t)tr->ld * tr->P);
+        if (!rc) rc = dev_alloc(&tr->bra_ao, (size_t)tr->ld * tr->P);
+        if (!rc) rc = dev_alloc(&tr->target, (size_t)tr->P);
+        if (!rc && cudaMemset(tr->psi_ao, 0, (size_t)tr->ld * tr->P * sizeof(double2)) != cudaSuccess) rc = ELHL_ERR_CUDA;
+        if (!rc && cudaMemset(tr->bra_ao, 0, (size_t)tr->ld * tr->P * sizeof(double2)) != cudaSuccess) rc = ELHL_ERR_CUDA;
+        if (!rc) rc = cheb_rebuild_operator(tr);
+        std::vector<ChebState *> one{&tr->cs};
+        if (!rc) rc = cheb_plan(tr->plan, one);
+    }
     if (rc) {
         free_basis(tr->basis);
         dev_free(tr->S); dev_free(tr->h); dev_free(tr->Hp); dev_free(tr->coords);
@@ -834,6 +1368,9 @@ int elhl_traj_destroy(elhl_traj *tr) {
     dev_free(tr->S); dev_free(tr->h); dev_free(tr->Hp); dev_free(tr->coords); dev_free(tr->pops);
     tr->fac.release();
     tr->tb.release();
+    tr->cs.release();
+    tr->plan.release();
+    dev_free(tr->psi_ao); dev_free(tr->bra_ao); dev_free(tr->target);
     delete tr;
     return ELHL_OK;
 }
@@ -842,13 +1379,78 @@ int elhl_traj_init_fmo(elhl_traj *tr, int n_el_atoms, const int *el_atoms, int e
                        const int *hl_atoms, int hole_state) {
     if (!tr) return ELHL_ERR_BAD_ARG;
     std::lock_guard<std::mutex> lk(g_ctx.mu);
-    if (int rc = fmo_particle(tr, n_el_atoms, el_atoms, electron_state, 0)) return rc;
-    return fmo_particle(tr, n_hl_atoms, hl_atoms, hole_state, 1);
+    if (tr->cheb()) {
+        if (tr->P < 2) return ELHL_ERR_BAD_ARG;
+        if (int rc = fmo_particle(tr, n_el_atoms, el_atoms, electron_state, tr->psi_ao, tr->bra_ao, tr->P)) return rc;
+        if (int rc = fmo_particle(tr, n_hl_atoms, hl_atoms, hole_state, tr->psi_ao + 1, tr->bra_ao + 1, tr->P))
+            return rc;
+        return cheb_set_target(tr);
+    }
+    if (int rc = fmo_particle(tr, n_el_atoms, el_atoms, electron_state, tr->tb.ket(0), tr->tb.bra(0), 1)) return rc;
+    return fmo_particle(tr, n_hl_atoms, hl_atoms, hole_state, tr->tb.ket(1), tr->tb.bra(1), 1);
+}
+
+int elhl_traj_init_fmo_states(elhl_traj *tr, int n_atoms, const int *atoms, int nstates, const int *states) {
+    if (!tr || !tr->cheb() || nstates < 1 || nstates > tr->P || !states) return ELHL_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(g_ctx.mu);
+    for (int c = 0; c < nstates; ++c)
+        if (int rc = fmo_particle(tr, n_atoms, atoms, states[c], tr->psi_ao + c, tr->bra_ao + c, tr->P)) return rc;
+    return cheb_set_target(tr);
+}
+
+int elhl_traj_energies(elhl_traj *tr, elhl_zcomplex *E) {
+    // QuasiParticleEnergies (ElHl_Chebyshev.f:329-371): E_p = sum_ij AO_bra_i h_ij AO_ket_j
+    // with AO_bra = conj(S^-1 Psi_bra) (ElHl_Chebyshev.f:274-275) and AO_ket = Psi_ket.
+    if (!tr || !E || !tr->h || !tr->fac.L) return ELHL_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(g_ctx.mu);
+    cudaStream_t st = g_ctx.stream;
+    const int P = tr->P, n = tr->N;
+    double2 *ket = nullptr, *bra = nullptr, *hk = nullptr;  // [n][P] each
+    int rc = dev_alloc(&ket, (size_t)n * P);
+    if (!rc) rc = dev_alloc(&bra, (size_t)n * P);
+    if (!rc) rc = dev_alloc(&hk, (size_t)n * P);
+    const size_t e = sizeof(double2);
+    for (int p = 0; p < P && !rc; ++p) {
+        const double2 *k = tr->cheb() ? tr->psi_ao + p : tr->tb.ket(p);
+        const double2 *b = tr->cheb() ? tr->bra_ao + p : tr->tb.bra(p);
+        const size_t sp = tr->cheb() ? P * e : e;
+        if (cudaMemcpy2DAsync(ket + p, P * e, k, sp, e, n, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+            cudaMemcpy2DAsync(bra + p, P * e, b, sp, e, n, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+            rc = ELHL_ERR_CUDA;
+    }
+    // S^-1 bra = L^-T L^-1 bra: rows of the 2P x n real view times L^-T then L^-1
+    if (!rc) rc = cols_apply(tr->fac.L, tr->ld, n, bra, P, 0, P, true, true);
+    if (!rc) rc = cols_apply(tr->fac.L, tr->ld, n, bra, P, 0, P, false, true);
+    if (!rc) {
+        const double one = 1.0, zero = 0.0;
+        if (cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * P, n, n, &one, (const double *)ket, 2 * P, tr->h,
+                        tr->ld, &zero, (double *)hk, 2 * P) != CUBLAS_STATUS_SUCCESS)
+            rc = ELHL_ERR_CUDA;  // (h ket)^T = ket^T h, h symmetric
+    }
+    std::vector<double2> hb((size_t)n * P), hh((size_t)n * P);
+    if (!rc && (cudaMemcpyAsync(hb.data(), bra, hb.size() * e, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaMemcpyAsync(hh.data(), hk, hh.size() * e, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess))
+        rc = ELHL_ERR_CUDA;
+    dev_free(ket); dev_free(bra); dev_free(hk);
+    if (rc) return rc;
+    for (int p = 0; p < P; ++p) {
+        double er = 0.0, ei = 0.0;
+        for (int i = 0; i < n; ++i) {
+            const double2 a = hb[(size_t)i * P + p], b = hh[(size_t)i * P + p];  // conj(a) * b
+            er += a.x * b.x + a.y * b.y;
+            ei += a.x * b.y - a.y * b.x;
+        }
+        E[p].re = er;
+        E[p].im = ei;
+    }
+    return ELHL_OK;
 }
 
 int elhl_traj_set_psi(elhl_traj *tr, const elhl_zcomplex *bra, const elhl_zcomplex *ket) {
-    if (!tr || !bra || !ket) return ELHL_ERR_BAD_ARG;
+    if (!tr || !ket || (!bra && !tr->cheb())) return ELHL_ERR_BAD_ARG;
     std::lock_guard<std::mutex> lk(g_ctx.mu);
+    if (tr->cheb()) return cheb_set_psi(tr, bra, ket);
     for (int p = 0; p < tr->P; ++p) {
         CU_TRY(cudaMemcpy(tr->tb.bra(p), bra + (size_t)p * tr->N, tr->N * sizeof(double2), cudaMemcpyHostToDevice));
         CU_TRY(cudaMemcpy(tr->tb.ket(p), ket + (size_t)p * tr->N, tr->N * sizeof(double2), cudaMemcpyHostToDevice));
@@ -860,6 +1462,14 @@ int elhl_traj_get_psi(elhl_traj *tr, elhl_zcomplex *bra, elhl_zcomplex *ket) {
     if (!tr) return ELHL_ERR_BAD_ARG;
     std::lock_guard<std::mutex> lk(g_ctx.mu);
     CU_TRY(cudaStreamSynchronize(g_ctx.stream));
+    if (tr->cheb()) {
+        const size_t e = sizeof(double2);
+        for (int p = 0; p < tr->P; ++p) {
+            if (ket) CU_TRY(cudaMemcpy2D(ket + (size_t)p * tr->N, e, tr->psi_ao + p, tr->P * e, e, tr->N, cudaMemcpyDeviceToHost));
+            if (bra) CU_TRY(cudaMemcpy2D(bra + (size_t)p * tr->N, e, tr->bra_ao + p, tr->P * e, e, tr->N, cudaMemcpyDeviceToHost));
+        }
+        return ELHL_OK;
+    }
     for (int p = 0; p < tr->P; ++p) {
         if (bra) CU_TRY(cudaMemcpy(bra + (size_t)p * tr->N, tr->tb.bra(p), tr->N * sizeof(double2), cudaMemcpyDeviceToHost));
         if (ket) CU_TRY(cudaMemcpy(ket + (size_t)p * tr->N, tr->tb.ket(p), tr->N * sizeof(double2), cudaMemcpyDeviceToHost));
@@ -882,7 +1492,7 @@ int elhl_traj_get_matrices(elhl_traj *tr, double *S, double *h, double *Hp) {
     const size_t col = tr->N * sizeof(double), ldb = tr->ld * sizeof(double);
     if (S) CU_TRY(cudaMemcpy2D(S, col, tr->S, ldb, col, tr->N, cudaMemcpyDeviceToHost));
     if (h) CU_TRY(cudaMemcpy2D(h, col, tr->h, ldb, col, tr->N, cudaMemcpyDeviceToHost));
-    if (Hp) CU_TRY(cudaMemcpy2D(Hp, col, tr->Hp, ldb, col, tr->N, cudaMemcpyDeviceToHost));
+    if (Hp && tr->Hp) CU_TRY(cudaMemcpy2D(Hp, col, tr->Hp, ldb, col, tr->N, cudaMemcpyDeviceToHost));
     return ELHL_OK;
 }
 
@@ -893,6 +1503,396 @@ int elhl_traj_get_stats(elhl_traj *tr, elhl_traj_stats *st) {
     st->save_tau[1] = tr->save_tau[1];
     st->t = tr->t;
     st->it = tr->it;
+    return ELHL_OK;
+}
+
+}  // extern "C"
+
+// =============================== batches ========================================
+// Many Chebyshev trajectories (fixed nuclei) advanced together: one cooperative
+// launch per nuclear step covers every member's orders (persistent kernel over
+// a row-segment work list balanced by matrix elements), then each member's
+// columns are read out and its populations reduced.
+struct elhl_batch {
+    std::vector<elhl_traj *> members;
+    ChebPlan plan;
+    std::vector<ChebState *> states;
+    double *pops = nullptr;
+    size_t pops_cap = 0;
+    bool compact = false;
+    elhl_traj_stats stats{};
+};
+
+extern "C" {
+
+int elhl_batch_create(int ntraj, const elhl_basis_desc *bases, const double *const *coords,
+                      const elhl_traj_config *cfg, elhl_batch **out) {
+    if (!out || ntraj <= 0 || !bases || !coords || !cfg) return ELHL_ERR_BAD_ARG;
+    if (cfg->method != ELHL_METHOD_CHEBYSHEV) return ELHL_ERR_UNSUPPORTED;
+    *out = nullptr;
+    elhl_batch *b = new elhl_batch();
+    int rc = ELHL_OK;
+    for (int i = 0; i < ntraj && !rc; ++i) {
+        elhl_traj *tr = nullptr;
+        rc = elhl_traj_create(&bases[i], coords[i], cfg, &tr);
+        if (!rc) {
+            b->members.push_back(tr);
+            b->states.push_back(&tr->cs);
+            if (tr->nfrag != b->members[0]->nfrag || tr->P != b->members[0]->P) rc = ELHL_ERR_BAD_ARG;
+        }
+    }
+    if (!rc) {
+        std::lock_guard<std::mutex> lk(g_ctx.mu);
+        rc = cheb_plan(b->plan, b->states);
+    }
+    if (rc) {
+        for (auto *tr : b->members) elhl_traj_destroy(tr);
+        b->plan.release();
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return ELHL_OK;
+}
+
+int elhl_batch_size(elhl_batch *b) { return b ? (int)b->members.size() : 0; }
+
+elhl_traj *elhl_batch_member(elhl_batch *b, int i) {
+    if (!b || i < 0 || i >= (int)b->members.size()) return nullptr;
+    return b->members[i];
+}
+
+int elhl_batch_compact(elhl_batch *b) {
+    if (!b) return ELHL_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(g_ctx.mu);
+    CU_TRY(cudaStreamSynchronize(g_ctx.stream));
+    for (auto *tr : b->members) {
+        dev_free(tr->S); dev_free(tr->h); dev_free(tr->cs.Ht); dev_free(tr->cs.lz);
+        tr->tb.release();
+    }
+    b->compact = true;
+    return ELHL_OK;
+}
+
+int elhl_batch_step(elhl_batch *b, int nsteps, double *pops) {
+    if (!b || nsteps <= 0) return ELHL_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(g_ctx.mu);
+    cudaStream_t st = g_ctx.stream;
+    const int nt = (int)b->members.size(), P = b->members[0]->P, nf = b->members[0]->nfrag;
+    const size_t per_traj = (size_t)P * (nf + 1), per_step = per_traj * nt;
+    if (per_step * nsteps > b->pops_cap) {
+        dev_free(b->pops);
+        if (int rc = dev_alloc(&b->pops, per_step * nsteps)) return rc;
+        b->pops_cap = per_step * nsteps;
+    }
+    memset(&b->stats, 0, sizeof(b->stats));
+    for (auto *tr : b->members)
+        if (int rc = cheb_load_columns(tr)) return rc;
+    for (int s = 0; s < nsteps; ++s) {
+        if (int rc = cheb_run(b->plan)) return rc;
+        for (int q = 0; q < nt; ++q) {
+            elhl_traj *tr = b->members[q];
+            ChebState &cs = tr->cs;
+            double *pp = b->pops + s * per_step + q * per_traj;
+            if (int rc = cheb_readout(tr, cs.acc, pp)) return rc;
+            if (cs.precision != ELHL_PREC_FP64) {
+                renormalize_kernel<<<(tr->N + 255) / 256, 256, 0, st>>>(cs.acc, tr->N, cs.m, P, pp, nf, tr->target);
+                CU_TRY(cudaGetLastError());
+                if (int rc = cheb_readout(tr, cs.acc, nullptr)) return rc;
+            }
+            CU_TRY(cudaMemcpyAsync(cs.phi, cs.acc, (size_t)cs.ld * cs.m * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+            tr->t = tr->t + tr->cfg.dt * tr->cfg.frame_step;
+            tr->it += 1;
+            tr->first_call = false;
+        }
+        int err = 0;
+        CU_TRY(cudaMemcpyAsync(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaStreamSynchronize(st));
+        if (err) return err;
+        b->stats.prop_ms += event_ms(0, 1);
+        b->stats.prop_launches += 1;
+        for (auto *cs : b->states) b->stats.orders += (long long)cs->K * cs->m;
+        b->stats.substeps += nt;
+    }
+    if (pops) CU_TRY(cudaMemcpy(pops, b->pops, per_step * nsteps * sizeof(double), cudaMemcpyDeviceToHost));
+    return ELHL_OK;
+}
+
+int elhl_batch_get_stats(elhl_batch *b, elhl_traj_stats *st) {
+    if (!b || !st) return ELHL_ERR_BAD_ARG;
+    *st = b->stats;
+    return ELHL_OK;
+}
+
+int elhl_batch_destroy(elhl_batch *b) {
+    if (!b) return ELHL_ERR_BAD_ARG;
+    for (auto *tr : b->members) elhl_traj_destroy(tr);
+    std::lock_guard<std::mutex> lk(g_ctx.mu);
+    b->plan.release();
+    dev_free(b->pops);
+    delete b;
+    return ELHL_OK;
+}
+
+}  // extern "C"
+
+// =============================== serving ========================================
+// Continuous batching of propagation requests: requests wait FIFO until their
+// estimated device memory fits the HBM budget, are set up on the device
+// (S, h, L, H~, bounds, fragment-MO initial columns), join the running batch at
+// the next step boundary, and leave it when their step count is reached.  Every
+// server step is one cooperative launch over all active requests.
+#include <chrono>
+#include <deque>
+#include <map>
+
+struct ServerRequest {
+    long long id = 0;
+    int nsteps = 0, done_steps = 0, P = 0, nfrag = 0, natoms = 0, nao = 0;
+    std::vector<int> ao0, naoat, n, l, m, nz, frag, frag_atoms, states;
+    std::vector<double> zeta, coef, ip, kwh, vs, coords;
+    double bytes = 0.0;
+    elhl_traj *tr = nullptr;
+    std::vector<double> pops;          // last populations, P x (nfrag+1)
+    std::vector<double2> psi;          // final ket, N x P (column-major)
+    int status = ELHL_OK;
+    double t_submit = 0.0, t_admit = 0.0, t_done = 0.0;  // seconds, host steady clock
+};
+
+static double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct elhl_server {
+    elhl_traj_config cfg;
+    double budget = 0.0, used = 0.0;
+    std::deque<ServerRequest *> pending;
+    std::vector<ServerRequest *> active;
+    std::map<long long, ServerRequest *> finished;
+    std::vector<long long> newly_done;
+    ChebPlan plan;
+    bool plan_dirty = true;
+    long long next_id = 1;
+    double *pops = nullptr;
+    size_t pops_cap = 0;
+    long long steps_done = 0;
+};
+
+static double request_bytes(const elhl_traj_config &cfg, int nao, int P) {
+    const double ld = (double)round_up(nao, 32), tsz = cfg.precision == ELHL_PREC_FP64 ? 8.0 : 4.0;
+    // set-up peak: S, h, H~, L (FP64) + Hs + vectors
+    return ld * nao * (4 * 8.0 + tsz) + ld * cfg.ncols / cfg.nparticles * P * (3 * 2 * tsz + 2 * 16.0) + 1e6;
+}
+
+static int server_admit(elhl_server *sv, ServerRequest *r) {
+    elhl_basis_desc d{};
+    d.natoms = r->natoms; d.nao = r->nao;
+    d.atom_ao0 = r->ao0.data(); d.atom_nao = r->naoat.data();
+    d.ao_n = r->n.data(); d.ao_l = r->l.data(); d.ao_m = r->m.data(); d.ao_nzeta = r->nz.data();
+    d.ao_zeta = r->zeta.data(); d.ao_coef = r->coef.data(); d.ao_ip = r->ip.data(); d.ao_kwh = r->kwh.data();
+    d.ao_vshift = r->vs.data(); d.ao_frag = r->frag.data(); d.nfrag = r->nfrag;
+    elhl_traj_config c = sv->cfg;
+    c.nparticles = r->P;
+    c.ncols = r->P;  // ket columns only (fixed nuclei: bra = S ket)
+    if (int rc = elhl_traj_create(&d, r->coords.data(), &c, &r->tr)) return rc;
+    if (int rc = elhl_traj_init_fmo_states(r->tr, (int)r->frag_atoms.size(), r->frag_atoms.data(), r->P,
+                                           r->states.data()))
+        return rc;
+    std::lock_guard<std::mutex> lk(g_ctx.mu);
+    CU_TRY(cudaStreamSynchronize(g_ctx.stream));
+    elhl_traj *tr = r->tr;
+    dev_free(tr->S); dev_free(tr->h); dev_free(tr->cs.Ht); dev_free(tr->cs.lz);
+    return cheb_load_columns(tr);
+}
+
+extern "C" {
+
+int elhl_server_create(double hbm_budget_bytes, const elhl_traj_config *cfg, elhl_server **out) {
+    if (!out || !cfg || !(hbm_budget_bytes > 0.0)) return ELHL_ERR_BAD_ARG;
+    if (cfg->method != ELHL_METHOD_CHEBYSHEV) return ELHL_ERR_UNSUPPORTED;
+    if (int rc = ensure_context()) return rc;
+    elhl_server *sv = new elhl_server();
+    sv->cfg = *cfg;
+    sv->budget = hbm_budget_bytes;
+    *out = sv;
+    return ELHL_OK;
+}
+
+int elhl_server_submit(elhl_server *sv, const elhl_request *q, long long *id) {
+    if (!sv || !q || !q->basis || !q->coords || q->nsteps <= 0 || q->nparticles < 1 || q->nparticles > 64 ||
+        !q->frag_atoms || q->n_frag_atoms <= 0 || !q->states)
+        return ELHL_ERR_BAD_ARG;
+    if (int rc = validate_basis(q->basis)) return rc;
+    const elhl_basis_desc *b = q->basis;
+    ServerRequest *r = new ServerRequest();
+    r->nsteps = q->nsteps; r->P = q->nparticles; r->nfrag = b->nfrag; r->natoms = b->natoms; r->nao = b->nao;
+    r->ao0.assign(b->atom_ao0, b->atom_ao0 + b->natoms);
+    r->naoat.assign(b->atom_nao, b->atom_nao + b->natoms);
+    r->n.assign(b->ao_n, b->ao_n + b->nao); r->l.assign(b->ao_l, b->ao_l + b->nao);
+    r->m.assign(b->ao_m, b->ao_m + b->nao); r->nz.assign(b->ao_nzeta, b->ao_nzeta + b->nao);
+    r->zeta.assign(b->ao_zeta, b->ao_zeta + 2 * b->nao); r->coef.assign(b->ao_coef, b->ao_coef + 2 * b->nao);
+    r->ip.assign(b->ao_ip, b->ao_ip + b->nao); r->kwh.assign(b->ao_kwh, b->ao_kwh + b->nao);
+    r->vs.assign(b->ao_vshift, b->ao_vshift + b->nao);
+    if (b->ao_frag) r->frag.assign(b->ao_frag, b->ao_frag + b->nao); else r->frag.assign(b->nao, 0);
+    r->coords.assign(q->coords, q->coords + 3 * b->natoms);
+    r->frag_atoms.assign(q->frag_atoms, q->frag_atoms + q->n_frag_atoms);
+    r->states.assign(q->states, q->states + q->nparticles);
+    r->bytes = request_bytes(sv->cfg, b->nao, r->P);
+    if (r->bytes > sv->budget) {
+        delete r;
+        return ELHL_ERR_OOM;  // can never be admitted
+    }
+    r->id = sv->next_id++;
+    r->t_submit = now_s();
+    sv->pending.push_back(r);
+    if (id) *id = r->id;
+    return ELHL_OK;
+}
+
+int elhl_server_step(elhl_server *sv, int *n_active, int *n_pending) {
+    if (!sv) return ELHL_ERR_BAD_ARG;
+    // admission, FIFO, within the budget
+    while (!sv->pending.empty() && sv->used + sv->pending.front()->bytes <= sv->budget) {
+        ServerRequest *r = sv->pending.front();
+        sv->pending.pop_front();
+        r->t_admit = now_s();
+        int rc = server_admit(sv, r);
+        if (rc) {
+            r->status = rc;
+            r->t_done = now_s();
+            if (r->tr) elhl_traj_destroy(r->tr);
+            r->tr = nullptr;
+            sv->finished[r->id] = r;
+            sv->newly_done.push_back(r->id);
+            continue;
+        }
+        sv->used += r->bytes;
+        sv->active.push_back(r);
+        sv->plan_dirty = true;
+    }
+    if (!sv->active.empty()) {
+        std::lock_guard<std::mutex> lk(g_ctx.mu);
+        cudaStream_t st = g_ctx.stream;
+        if (sv->plan_dirty) {
+            std::vector<ChebState *> states;
+            for (auto *r : sv->active) states.push_back(&r->tr->cs);
+            if (int rc = cheb_plan(sv->plan, states)) return rc;
+            sv->plan_dirty = false;
+        }
+        size_t need = 0;
+        for (auto *r : sv->active) need += (size_t)r->P * (r->nfrag + 1);
+        if (need > sv->pops_cap) {
+            dev_free(sv->pops);
+            if (int rc = dev_alloc(&sv->pops, need)) return rc;
+            sv->pops_cap = need;
+        }
+        if (int rc = cheb_run(sv->plan)) return rc;
+        size_t off = 0;
+        for (auto *r : sv->active) {
+            elhl_traj *tr = r->tr;
+            ChebState &cs = tr->cs;
+            double *pp = sv->pops + off;
+            if (int rc = cheb_readout(tr, cs.acc, pp)) return rc;
+            if (cs.precision != ELHL_PREC_FP64) {
+                renormalize_kernel<<<(tr->N + 255) / 256, 256, 0, st>>>(cs.acc, tr->N, cs.m, tr->P, pp, tr->nfrag,
+                                                                        tr->target);
+                CU_TRY(cudaGetLastError());
+                if (int rc = cheb_readout(tr, cs.acc, nullptr)) return rc;
+            }
+            CU_TRY(cudaMemcpyAsync(cs.phi, cs.acc, (size_t)cs.ld * cs.m * sizeof(double2), cudaMemcpyDeviceToDevice,
+                                   st));
+            off += (size_t)r->P * (r->nfrag + 1);
+        }
+        int err = 0;
+        CU_TRY(cudaMemcpyAsync(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaStreamSynchronize(st));
+        if (err) return err;
+        sv->steps_done += (long long)sv->active.size();
+        // retire finished requests
+        off = 0;
+        std::vector<ServerRequest *> keep;
+        for (auto *r : sv->active) {
+            r->done_steps += 1;
+            const size_t np = (size_t)r->P * (r->nfrag + 1);
+            if (r->done_steps >= r->nsteps) {
+                r->pops.resize(np);
+                CU_TRY(cudaMemcpy(r->pops.data(), sv->pops + off, np * sizeof(double), cudaMemcpyDeviceToHost));
+                r->psi.resize((size_t)r->nao * r->P);
+                const size_t e = sizeof(double2);
+                for (int p = 0; p < r->P; ++p)
+                    CU_TRY(cudaMemcpy2D(r->psi.data() + (size_t)p * r->nao, e, r->tr->psi_ao + p, r->P * e, e, r->nao,
+                                        cudaMemcpyDeviceToHost));
+                r->t_done = now_s();
+                sv->used -= r->bytes;
+                sv->plan_dirty = true;
+                sv->finished[r->id] = r;
+                sv->newly_done.push_back(r->id);
+            } else {
+                keep.push_back(r);
+            }
+            off += np;
+        }
+        sv->active.swap(keep);
+    }
+    // destroy retired trajectories outside the context lock
+    for (auto id : sv->newly_done) {
+        ServerRequest *r = sv->finished[id];
+        if (r->tr) {
+            elhl_traj_destroy(r->tr);
+            r->tr = nullptr;
+        }
+    }
+    if (n_active) *n_active = (int)sv->active.size();
+    if (n_pending) *n_pending = (int)sv->pending.size();
+    return ELHL_OK;
+}
+
+int elhl_server_poll(elhl_server *sv, long long *ids, int max, int *n) {
+    if (!sv || !n || (max > 0 && !ids)) return ELHL_ERR_BAD_ARG;
+    int k = 0;
+    while (k < max && !sv->newly_done.empty()) {
+        ids[k++] = sv->newly_done.front();
+        sv->newly_done.erase(sv->newly_done.begin());
+    }
+    *n = k;
+    return ELHL_OK;
+}
+
+int elhl_server_result(elhl_server *sv, long long id, double *pops, elhl_zcomplex *psi_ket, double *times) {
+    if (!sv) return ELHL_ERR_BAD_ARG;
+    auto it = sv->finished.find(id);
+    if (it == sv->finished.end()) return ELHL_ERR_BAD_ARG;
+    ServerRequest *r = it->second;
+    if (pops && !r->pops.empty()) memcpy(pops, r->pops.data(), r->pops.size() * sizeof(double));
+    if (psi_ket && !r->psi.empty()) memcpy(psi_ket, r->psi.data(), r->psi.size() * sizeof(double2));
+    if (times) {
+        times[0] = r->t_submit;
+        times[1] = r->t_admit;
+        times[2] = r->t_done;
+    }
+    const int st = r->status;
+    sv->finished.erase(it);
+    delete r;
+    return st;
+}
+
+int elhl_server_destroy(elhl_server *sv) {
+    if (!sv) return ELHL_ERR_BAD_ARG;
+    for (auto *r : sv->pending) delete r;
+    for (auto *r : sv->active) {
+        if (r->tr) elhl_traj_destroy(r->tr);
+        delete r;
+    }
+    for (auto &kv : sv->finished) {
+        if (kv.second->tr) elhl_traj_destroy(kv.second->tr);
+        delete kv.second;
+    }
+    {
+        std::lock_guard<std::mutex> lk(g_ctx.mu);
+        sv->plan.release();
+        dev_free(sv->pops);
+    }
+    delete sv;
     return ELHL_OK;
 }
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <vector>
 
 #include "../../include/elhl_prop.h"
 
@@ -20,6 +21,9 @@ struct DevBasis {
     int *ao_n = nullptr, *ao_l = nullptr, *ao_m = nullptr, *ao_nzeta = nullptr, *ao_frag = nullptr;
     double *ao_zeta = nullptr, *ao_coef = nullptr, *ao_ip = nullptr, *ao_kwh = nullptr, *ao_vshift = nullptr;
 };
+
+// One-time per-device fill of the overlap kernel's constant tables.
+cudaError_t init_build_tables();
 
 // S and h (both N x N, column-major, leading dimension ld) from coordinates.
 cudaError_t launch_build_sh(const DevBasis &b, const double *d_coords, double cutoff, double *d_S,
@@ -70,6 +74,39 @@ constexpr int kSlots = 6;
 cudaError_t launch_taylor(const TaylorLaunch &L, int grid, int block, cudaStream_t st);
 int taylor_grid_size(int block, int *grid_out);
 constexpr int kTaylorBlock = 256;
+
+// ---- Chebyshev engine (cheb.cu, chebcoef.cu) ---------------------------------
+struct ChebProblem {
+    int N, ld, ldv, m, K;   // size, matrix/vector leading dims (padded rows are 0), complex columns, last order
+    const void *H;          // Hs = (H~ - a)/b in the launch precision, N columns of ld rows (symmetric)
+    void *vbuf;             // [3][m/MG][ldv][MG] complex vectors in the launch precision
+    double2 *phi;           // [ldv][m] input columns (FP64)
+    double2 *acc;           // [ldv][m] output columns (FP64)
+    const double2 *coef;    // [K+1] expansion coefficients (phase folded in)
+};
+struct ChebSegment {
+    int prob, row0, row1;   // rows [row0, row1) of problem `prob` owned by one CTA
+};
+struct ChebLaunch {
+    const ChebProblem *probs;
+    const ChebSegment *segs;
+    const int *seg_begin;   // [grid + 1]: CTA c owns segs[seg_begin[c] .. seg_begin[c+1])
+    int kmax, max_ld, grid;
+    unsigned *bar_count, *bar_gen;
+    int *error;
+};
+constexpr size_t kCheb_part_bytes = 16 * 64 * sizeof(double);  // cross-warp partial sums
+constexpr size_t kCheb_smem_limit = 200 * 1024;
+int cheb_block();
+int cheb_grid_size(int *grid_out);
+int cheb_group_size(int precision, int m, int max_ld);  // columns staged per pass, 0 = unsupported
+cudaError_t launch_cheb(const ChebLaunch &L, int precision, int mg, cudaStream_t st);
+
+int bessel_j_sequence(double beta, int kmax, double *J);
+int chebyshev_coefficients(double dt, double emin, double emax, double tol, int kcap, std::vector<double> &cre,
+                           std::vector<double> &cim, int *K_out);
+void tridiagonal_extremes(const double *alpha, const double *beta, int n, double *lo, double *hi);
+double tridiagonal_last_component(const double *alpha, const double *beta, int n, double theta);
 
 // ---- small helpers ----------------------------------------------------------
 inline int round_up(int x, int m) { return (x + m - 1) / m * m; }

@@ -23,6 +23,7 @@
 #include <cooperative_groups.h>
 
 #include "elhl_internal.cuh"
+#include "grid_sync.cuh"
 
 namespace elhl {
 namespace {
@@ -30,7 +31,6 @@ namespace {
 constexpr int RC = 4;            // rows per register chunk
 constexpr int PMAX = 2;          // particles per launch
 constexpr int PW = 16;           // partial record width (doubles)
-constexpr unsigned long long kBarrierNs = 5000000000ULL;  // 5 s
 
 enum Phase { PH_NORM = 0, PH_CONV = 1, PH_MAIN = 2, PH_DONE = 3 };
 
@@ -42,40 +42,6 @@ struct Ctrl {
     double tau, t, norm_ref, save_tau;
     double cre[kOrder], cim[kOrder];
 };
-
-__device__ __forceinline__ unsigned long long globaltimer() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Sense-reversing grid barrier with a time limit.
-__device__ bool grid_barrier(unsigned *count, unsigned *gen, unsigned nblocks, int *err) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned *vgen = gen;
-        const unsigned g = *vgen;
-        __threadfence();
-        const unsigned prev = atomicAdd(count, 1u);
-        if (prev == nblocks - 1) {
-            atomicExch(count, 0u);
-            __threadfence();
-            atomicAdd(gen, 1u);
-        } else {
-            const unsigned long long t0 = globaltimer();
-            while (*vgen == g) {
-                if (globaltimer() - t0 > kBarrierNs) {
-                    atomicExch(err, ELHL_ERR_TIMEOUT);
-                    break;
-                }
-                __nanosleep(40);
-            }
-        }
-        __threadfence();
-    }
-    __syncthreads();
-    return *(volatile int *)err == 0;
-}
 
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
     return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -267,18 +233,28 @@ __global__ void __launch_bounds__(kTaylorBlock, 1) taylor_kernel(TaylorLaunch L)
                         }
                     }
                 }
-                // block reduction of the PMAX*RC*4 accumulators (fixed tree)
+                // block reduction of the 32 accumulators: transposed butterfly, after
+                // which lane l holds the warp sum of accumulator l (31 shuffles + adds
+                // per lane instead of 5 per accumulator), then a fixed-order sum over warps
+                static_assert(PMAX * RC * 4 == 32, "one accumulator per lane");
+                double v[32];
 #pragma unroll
                 for (int p = 0; p < PMAX; ++p)
 #pragma unroll
                     for (int r = 0; r < RC; ++r)
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            double v = acc[p][r][q];
+                        for (int q = 0; q < 4; ++q) v[(p * RC + r) * 4 + q] = acc[p][r][q];
 #pragma unroll
-                            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-                            if (lane == 0) red[warp][(p * RC + r) * 4 + q] = v;
-                        }
+                for (int o = 16; o > 0; o >>= 1) {
+                    const bool upper = (lane & o) != 0;
+#pragma unroll
+                    for (int i = 0; i < o; ++i) {
+                        const double send = upper ? v[i] : v[i + o];
+                        const double keep = upper ? v[i + o] : v[i];
+                        v[i] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+                    }
+                }
+                red[warp][lane] = v[0];
                 __syncthreads();
                 if (tid < PMAX * RC * 4) {
                     double v = 0.0;
@@ -340,20 +316,31 @@ __global__ void __launch_bounds__(kTaylorBlock, 1) taylor_kernel(TaylorLaunch L)
         // warp p reduces particle p's records in a fixed order (identical in every CTA)
         __shared__ double tot[PMAX][PW];
         if (warp < P) {
+            // only the max |delta| and <bra|ket> fields matter after a GEMV round;
+            // the population fields are read after a norm round only
             const int p = warp;
+            const int nq = (ctrl[p].phase == PH_NORM) ? PW : 4;
             double v[PW];
+#pragma unroll
             for (int q = 0; q < PW; ++q) v[q] = 0.0;
             for (int g = lane; g < G; g += 32) {
                 const double *rec = L.partials + (((size_t)parity * PMAX + p) * G + g) * PW;
                 v[0] = fmax(v[0], __ldcg(rec + 0));
                 v[1] = fmax(v[1], __ldcg(rec + 1));
-                for (int q = 2; q < PW; ++q) v[q] += __ldcg(rec + q);
+                v[2] += __ldcg(rec + 2);
+                v[3] += __ldcg(rec + 3);
+                for (int q = 4; q < nq; ++q) v[q] += __ldcg(rec + q);
             }
+#pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 v[0] = fmax(v[0], __shfl_xor_sync(0xffffffffu, v[0], o));
                 v[1] = fmax(v[1], __shfl_xor_sync(0xffffffffu, v[1], o));
-                for (int q = 2; q < PW; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+                v[2] += __shfl_xor_sync(0xffffffffu, v[2], o);
+                v[3] += __shfl_xor_sync(0xffffffffu, v[3], o);
             }
+            if (nq > 4)
+                for (int o = 16; o > 0; o >>= 1)
+                    for (int q = 4; q < PW; ++q) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
             if (lane == 0)
                 for (int q = 0; q < PW; ++q) tot[p][q] = v[q];
         }

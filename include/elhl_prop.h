@@ -131,7 +131,10 @@ typedef struct {
     double cheb_tol;     /* Chebyshev truncation |c_k| < cheb_tol */
     double cutoff;       /* overlap cutoff, Angstrom (QM_cutoff, 12) */
     int max_conv_calls;  /* bound on tau retries per particle and step */
-    int ncols;           /* Chebyshev: complex columns (2 = el+hl) */
+    int ncols;           /* Chebyshev: propagated complex columns, nparticles (ket only, bra = S ket)
+                            or 2 * nparticles (bra carried as the reference does) */
+    int nparticles;      /* wavefunctions per trajectory: 2 (electron, hole) for the Taylor method;
+                            1..64 for Chebyshev (ensembles) */
 } elhl_traj_config;
 
 typedef struct elhl_traj elhl_traj;
@@ -156,7 +159,11 @@ int elhl_traj_destroy(elhl_traj *tr);
 int elhl_traj_init_fmo(elhl_traj *tr, int n_el_atoms, const int *el_atoms, int electron_state, int n_hl_atoms,
                        const int *hl_atoms, int hole_state);
 
-/* Set / get Psi (host, column-major N x ncols: column 0 electron, 1 hole).
+/* Chebyshev trajectories: column c < nstates becomes fragment MO states[c]
+ * (1-based) of the fragment `atoms`, embedded as in elhl_traj_init_fmo. */
+int elhl_traj_init_fmo_states(elhl_traj *tr, int n_atoms, const int *atoms, int nstates, const int *states);
+
+/* Set / get Psi (host, column-major N x nparticles: column 0 electron, 1 hole).
  * psi_bra may be NULL for the Chebyshev method (bra = S ket). */
 int elhl_traj_set_psi(elhl_traj *tr, const elhl_zcomplex *psi_bra, const elhl_zcomplex *psi_ket);
 int elhl_traj_get_psi(elhl_traj *tr, elhl_zcomplex *psi_bra, elhl_zcomplex *psi_ket);
@@ -171,6 +178,11 @@ int elhl_traj_step(elhl_traj *tr, const double *coords, int nsteps, double *pops
 
 /* Same with device pointers (coords: nsteps*natoms*3 doubles, pops as above). */
 int elhl_traj_step_device(elhl_traj *tr, const double *d_coords, int nsteps, double *d_pops);
+
+/* Wavepacket energies per particle, E_p = sum_ij AO_bra_i h_ij AO_ket_j with
+ * AO_bra = conj(S^-1 Psi_bra), AO_ket = Psi_ket (QuasiParticleEnergies,
+ * ElHl_Chebyshev.f:329-371, evaluated with the Hueckel h).  E: [nparticles]. */
+int elhl_traj_energies(elhl_traj *tr, elhl_zcomplex *E);
 
 /* Copies of the device matrices (host, N x N, ld = N); any pointer may be NULL. */
 int elhl_traj_get_matrices(elhl_traj *tr, double *S, double *h, double *Hp);
@@ -190,6 +202,55 @@ typedef struct {
     int rebuild_count;    /* rebuilds */
 } elhl_traj_stats;
 int elhl_traj_get_stats(elhl_traj *tr, elhl_traj_stats *st);
+
+/* ---- batches: many trajectories in one launch per nuclear step ---------- */
+/* Batched Chebyshev propagation (config: method ELHL_METHOD_CHEBYSHEV, fixed
+ * nuclei) of `ntraj` trajectories of any sizes: bases[i] / coords[i] describe
+ * trajectory i.  Each nuclear step is ONE cooperative launch over all members'
+ * expansion orders, followed by each member's read-out and populations.  No
+ * counterpart in the reference, which propagates one trajectory per process. */
+typedef struct elhl_batch elhl_batch;
+int elhl_batch_create(int ntraj, const elhl_basis_desc *bases, const double *const *coords,
+                      const elhl_traj_config *cfg, elhl_batch **out);
+int elhl_batch_size(elhl_batch *b);
+/* Member i as a trajectory handle (init_fmo / set_psi / get_psi / get_stats). */
+elhl_traj *elhl_batch_member(elhl_batch *b, int i);
+/* Free the members' set-up matrices (S, h, H~) once their initial states are set. */
+int elhl_batch_compact(elhl_batch *b);
+/* pops: nsteps x ntraj x 2 x (nfrag+1) host doubles, or NULL. */
+int elhl_batch_step(elhl_batch *b, int nsteps, double *pops);
+int elhl_batch_get_stats(elhl_batch *b, elhl_traj_stats *st);
+int elhl_batch_destroy(elhl_batch *b);
+
+/* ---- serving: continuous batching of propagation requests -------------- */
+/* A request is one fixed-nuclei Chebyshev propagation: a system, its
+ * coordinates, a step count and `nparticles` initial columns (fragment MOs
+ * `states` of the fragment `frag_atoms`).  Everything is copied at submit.
+ * Requests wait FIFO until their estimated device memory fits the HBM budget,
+ * are set up on the device, join the running batch at the next step boundary
+ * and leave it when done; elhl_server_step is one nuclear step of every
+ * active request (one launch).  No counterpart in the reference. */
+typedef struct {
+    const elhl_basis_desc *basis;
+    const double *coords;   /* natoms*3 */
+    int nsteps;
+    int nparticles;         /* complex columns, 1..64 */
+    int n_frag_atoms;
+    const int *frag_atoms;
+    const int *states;      /* [nparticles], 1-based fragment MO indices */
+} elhl_request;
+typedef struct elhl_server elhl_server;
+int elhl_server_create(double hbm_budget_bytes, const elhl_traj_config *cfg, elhl_server **out);
+/* ELHL_ERR_OOM if the request can never fit the budget. */
+int elhl_server_submit(elhl_server *sv, const elhl_request *req, long long *id);
+int elhl_server_step(elhl_server *sv, int *n_active, int *n_pending);
+/* ids of requests completed since the last poll */
+int elhl_server_poll(elhl_server *sv, long long *ids, int max, int *n);
+/* final populations (nparticles x (nfrag+1)), final kets (N x nparticles,
+ * column-major) and times {submit, admit, done} (s, host steady clock); frees
+ * the request; returns its status. */
+int elhl_server_result(elhl_server *sv, long long id, double *pops, elhl_zcomplex *psi_ket, double *times);
+int elhl_server_destroy(elhl_server *sv);
 
 /* Run all library work on the caller's CUDA stream (a cudaStream_t passed as
  * void*), e.g. to order it with the caller's own kernels or to time it with
@@ -218,6 +279,15 @@ int elhl_set_stream(void *stream);
 int elhl_propagate_fixed_scratch(int n, const double *d_H, int ld, elhl_zcomplex *d_psi_bra,
                                  elhl_zcomplex *d_psi_ket, double t_init, double t_max, double tau,
                                  double *save_tau, void *stream);
+
+/* Host-side mathematics of the Chebyshev method (no GPU needed).
+ * elhl_bessel_j: J_0..J_kmax at beta (Miller backward recurrence).
+ * elhl_chebyshev_coefficients: c_k, k = 0..*K, of exp(-i dt H / hbar) for a
+ * spectrum in [emin, emax] (eV, dt in ps), truncated where |J_k| < tol; the
+ * caller's arrays hold kcap + 1 values. */
+int elhl_bessel_j(double beta, int kmax, double *J);
+int elhl_chebyshev_coefficients(double dt, double emin, double emax, double tol, int kcap, double *cre,
+                                double *cim, int *K);
 
 /* Library / device information. */
 int elhl_device_count(void);

@@ -1,0 +1,90 @@
+"""GPU tests of the Chebyshev propagator (symmetrised H~ = L^-1 h L^-T).
+
+FP64: the same exact propagator as the reference's Taylor series, so parity
+with the oracle and with the exact eigenbasis propagator is tested at 1e-10 in
+populations.  FP32: reduced precision; its error against the exact propagator
+is bounded by 1e-5 after 20 steps (the measured value is reported by
+bench.py)."""
+import numpy as np
+import pytest
+
+from dynemol_gb300 import systems
+
+pytestmark = pytest.mark.gpu
+
+
+def _exact(oracle_mod, sysm, ket0, t):
+    S = oracle_mod.overlap(sysm)
+    h = oracle_mod.huckel(sysm, S)
+    ex = oracle_mod.ExactPropagator(S, h)
+    return oracle_mod.exact_populations(sysm, S, ex.ket(ket0, t)).T
+
+
+def _cheb(elhl, sysm, nsteps, prec, ncols, dt=1e-4):
+    tr = elhl.Trajectory(sysm, dt=dt, method=elhl.METHOD_CHEBYSHEV, precision=prec, ncols=ncols, cheb_tol=1e-14)
+    tr.init_fmo(41, 40)
+    pops = tr.step(None, nsteps=nsteps)
+    b, k = tr.get_psi()
+    st = tr.stats()
+    tr.close()
+    return pops, b, k, st
+
+
+def test_cheb_fp64_fixed_nuclei_vs_exact(elhl, oracle_mod, flake):
+    S = oracle_mod.overlap(flake)
+    bra, ket = oracle_mod.initial_states(flake, S, 41, 40)
+    pops, b, k, st = _cheb(elhl, flake, 20, elhl.PREC_FP64, 2)
+    ref = _exact(oracle_mod, flake, ket, 20 * 1e-4)
+    assert np.abs(pops[-1] - ref).max() < 1e-10
+    assert st.orders > 0
+
+
+def test_cheb_fp64_bra_columns_equal_ket_only(elhl, flake):
+    p2, b2, k2, _ = _cheb(elhl, flake, 5, elhl.PREC_FP64, 2)
+    p4, b4, k4, _ = _cheb(elhl, flake, 5, elhl.PREC_FP64, 4)
+    assert np.abs(p2 - p4).max() < 1e-12
+    assert np.abs(k2 - k4).max() < 1e-11 and np.abs(b2 - b4).max() < 1e-11
+
+
+def test_cheb_fp64_vs_taylor_oracle(elhl, oracle_mod, flake):
+    S = oracle_mod.overlap(flake)
+    bra, ket = oracle_mod.initial_states(flake, S, 41, 40)
+    ref = oracle_mod.ReferenceStep(flake, bra, ket, dt=1e-4, tol=1e-12, norm_tol=1e-12, nthreads=4)
+    rp = np.stack([ref.step().T for _ in range(5)])
+    pops, b, k, _ = _cheb(elhl, flake, 5, elhl.PREC_FP64, 4)
+    assert np.abs(pops - rp).max() < 1e-10
+    assert np.abs(k - ref.ket).max() < 1e-9 and np.abs(b - ref.bra).max() < 1e-9
+
+
+def test_cheb_fp64_moving_nuclei_vs_taylor_oracle(elhl, oracle_mod):
+    """Bra and ket carried through geometry changes (ncols = 4) as the reference does."""
+    sysm = systems.cubic_cluster(n_atoms=64, seed=7)
+    coords = np.stack([systems.perturbed_coords(sysm.coords, i, seed=3) for i in range(4)])
+    S0 = oracle_mod.overlap(sysm, coords[1])
+    bra, ket = oracle_mod.initial_states(sysm, S0, 41, 40)
+    ref = oracle_mod.ReferenceStep(sysm, bra, ket, dt=5e-4, tol=1e-12, norm_tol=1e-12, nthreads=4)
+    rp = np.stack([ref.step(coords[1 + i]).T for i in range(3)])
+    tr = elhl.Trajectory(sysm, coords=coords[1], dt=5e-4, method=elhl.METHOD_CHEBYSHEV, precision=elhl.PREC_FP64,
+                         ncols=4, cheb_tol=1e-14)
+    tr.set_psi(bra, ket)
+    pops = tr.step(coords[1:], nsteps=3)
+    tr.close()
+    assert np.abs(pops - rp).max() < 1e-9
+
+
+def test_cheb_fp32_error_bound(elhl, oracle_mod, flake):
+    S = oracle_mod.overlap(flake)
+    bra, ket = oracle_mod.initial_states(flake, S, 41, 40)
+    pops, b, k, st = _cheb(elhl, flake, 20, elhl.PREC_FP32, 2)
+    ref = _exact(oracle_mod, flake, ket, 20 * 1e-4)
+    err = np.abs(pops[-1] - ref).max()
+    assert err < 1e-5, err
+    # renormalisation after every step keeps the total population from drifting:
+    # each step's (pre-renormalisation) total is within one step's FP32 error of 1
+    assert np.abs(pops[:, :, -1] - 1.0).max() < 1e-6
+
+
+def test_cheb_rejects_bad_config(elhl, flake):
+    with pytest.raises(elhl.ElhlError) as e:
+        elhl.Trajectory(flake, method=elhl.METHOD_CHEBYSHEV, ncols=3)
+    assert e.value.status == elhl.ERR_UNSUPPORTED

@@ -174,3 +174,22 @@ def test_bad_arguments(elhl, flake):
     with pytest.raises(ValueError):
         tr = elhl.Trajectory(flake)
         tr.step(np.zeros(5), nsteps=1)
+
+
+@pytest.mark.parametrize("method", [0, 1])
+def test_energies_match_oracle(elhl, oracle_mod, flake, method):
+    """QuasiParticleEnergies after 3 steps, Taylor and Chebyshev trajectories."""
+    S = oracle_mod.overlap(flake)
+    bra, ket = oracle_mod.initial_states(flake, S, 41, 40)
+    ref = oracle_mod.ReferenceStep(flake, bra, ket, dt=1e-4, tol=1e-12, norm_tol=1e-12, nthreads=4)
+    for _ in range(3):
+        ref.step()
+    Eo = ref.energies()
+    kw = dict(dt=1e-4, tol=1e-12, norm_tol=1e-12) if method == 0 else dict(
+        dt=1e-4, method=elhl.METHOD_CHEBYSHEV, ncols=4, cheb_tol=1e-14)
+    tr = elhl.Trajectory(flake, **kw)
+    tr.set_psi(bra, ket)
+    tr.step(None, nsteps=3)
+    E = tr.energies()
+    tr.close()
+    assert np.abs(E - Eo).max() < 1e-9
