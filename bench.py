@@ -111,6 +111,24 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# ----------------------------------------------------------------- replicas
+def max_over_ranks(t_local: float, world: int) -> float:
+    """Slowest rank's time (replicas: every rank propagates its own trajectory)."""
+    if world <= 1:
+        return t_local
+    import torch
+    import torch.distributed as dist
+    dev = torch.device("cuda", torch.cuda.current_device()) if dist.get_backend() == "nccl" else torch.device("cpu")
+    t = torch.tensor([t_local], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(steps: int, world: int, t_max: float) -> float:
+    """Whole-job steps/s: all ranks' steps over the slowest rank's time."""
+    return world * steps / t_max
+
+
 # ----------------------------------------------------------------- our arm
 def run_ours(args, rank, world):
     import torch
@@ -176,11 +194,7 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize(dev)
     clk = clocks.stop()
     ms = sum(a.elapsed_time(b) for a, b in ev)
-    t_dev = ms / 1e3
-    if world > 1:
-        t = torch.tensor([t_dev], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_dev = float(t.item())
+    t_dev = max_over_ranks(ms / 1e3, world)
 
     # ---- e2e: host buffers through the C ABI (H2D coords + D2H populations each step)
     Ke = K
@@ -199,11 +213,7 @@ def run_ours(args, rank, world):
             h_pops = tr.step(host_coords[i], nsteps=1)
     e1.record(stream)
     torch.cuda.synchronize(dev)
-    t_e2e = e0.elapsed_time(e1) / 1e3
-    if world > 1:
-        t = torch.tensor([t_e2e], device=dev, dtype=torch.float64)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        t_e2e = float(t.item())
+    t_e2e = max_over_ranks(e0.elapsed_time(e1) / 1e3, world)
     api.set_stream(None)
     tr.close()
 
@@ -235,7 +245,7 @@ def run_ours(args, rank, world):
 
     line = {
         "metric": "psi_propagation_steps_per_s",
-        "value": world * K / t_dev,
+        "value": replica_value(K, world, t_dev),
         "unit": "steps/s",
         "n_gpus": world,
         "steps": K,
@@ -250,7 +260,7 @@ def run_ours(args, rank, world):
                    "dt_ps": dt, "particles": 2, "method": args.method, "precision": args.precision,
                    "moving_nuclei": moving, "l2": "flushed (512 MB write) between timed steps",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "e2e": {"value": world * Ke / t_e2e, "unit": "steps/s",
+        "e2e": {"value": replica_value(Ke, world, t_e2e), "unit": "steps/s",
                 "h2d_bytes_per_step": (nc * 8) if moving else 0, "d2h_bytes_per_step": 2 * nf1 * 8},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
@@ -266,6 +276,33 @@ def run_ours(args, rank, world):
         "clocks": clk,
     }
     return line
+
+
+def run_dropin(args, steps: int = 2):
+    """The reference-semantics FP64 Taylor path (the propagationelhl_gpucaller_
+    algorithm) on the same workload and coordinates, device-resident, CUDA events."""
+    import torch
+    from dynemol_gb300 import api, systems
+    sysm, dt, moving = workload(args.workload)
+    homo = systems.fermi_state(sysm, np.arange(20))
+    coords = step_coords(sysm, moving, 4 + steps)
+    tr = api.Trajectory(sysm, coords=None if coords is None else coords[0], dt=dt)
+    tr.init_fmo(homo + 1, homo)
+    stream = torch.cuda.current_stream()
+    api.set_stream(stream.cuda_stream if stream.cuda_stream else None)
+    tr.step(None if coords is None else coords[1:3], nsteps=2, want_pops=False)  # warm-up
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    tr.step(None if coords is None else coords[3:3 + steps], nsteps=steps, want_pops=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    st = tr.stats()
+    tr.close()
+    api.set_stream(None)
+    t = e0.elapsed_time(e1) / 1e3
+    return {"steps_per_s": steps / t, "steps": steps, "orders_per_step": st.orders / steps,
+            "propagation_ms_per_step": st.prop_ms / steps, "rebuild_ms_per_step": st.rebuild_ms / steps}
 
 
 # ----------------------------------------------------------------- CPU sample
@@ -427,10 +464,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="ehrenfest", choices=sorted(WORKLOAD_DESC))
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--method", default="taylor", choices=["taylor", "chebyshev"])
+    ap.add_argument("--method", default="chebyshev", choices=["taylor", "chebyshev"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
-    ap.add_argument("--mix", type=int, default=0, help="also run the batched-vs-drop-in comparison on a mix "
+    ap.add_argument("--mix", type=int, default=64, help="also run the batched-vs-drop-in comparison on a mix "
                     "of this many trajectories (0 = skip)")
+    ap.add_argument("--no-dropin", action="store_true", help="skip the Taylor drop-in measurement")
     ap.add_argument("--serve", type=int, default=0, help="also run a serving stream of this many requests")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
@@ -446,6 +484,8 @@ def main():
         import torch
         torch.distributed.init_process_group("nccl")
     line = run_ours(args, rank, world)
+    if rank == 0 and args.method == "chebyshev" and not args.no_dropin:
+        line["dropin_taylor_fp64"] = run_dropin(args)
     if rank == 0 and args.mix:
         from dynemol_gb300 import api
         line["north_star_mix"] = run_mix(args, args.mix, steps=5, warm=2, precision=api.PREC_FP32,

@@ -53,51 +53,39 @@ __device__ __forceinline__ T transpose_reduce32(T (&v)[32], int lane) {
     return v[0];
 }
 
-// one order k >= 1 for the rows of segment sg, column group g (MG columns)
-template <typename T, int MG>
-__device__ void order_rows(const ChebProblem &pb, const ChebSegment &sg, int k, int g,
-                           typename Vec2<T>::type *s_v, T *s_part, double cre, double cim) {
+// y_i = sum_j M(j, i) x_j for the rows [row0, row1) of one segment, MG complex
+// columns x staged in shared memory (s_v[j*MG + c]); M is column-major with
+// leading dimension ld (column i = row i of M^T).  Calls epi(i, c, yr, yi).
+template <typename T, int MG, typename Epi>
+__device__ void rows_gemv(const T *M, int ld, const typename Vec2<T>::type *s_v, int row0, int row1, T *s_part,
+                          Epi &epi) {
     using T2 = typename Vec2<T>::type;
     constexpr int NV = kRT * MG * 2;  // accumulators per lane (16, 32 or 64)
     constexpr int NB = (NV + 31) / 32;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int ld = pb.ld, m = pb.m;
-    const T *H = reinterpret_cast<const T *>(pb.H);
-    T2 *vbuf = reinterpret_cast<T2 *>(pb.vbuf);
-    const size_t gstride = (size_t)pb.ldv * MG;         // one column group
-    const size_t bstride = gstride * (m / MG);          // one of the three vector buffers
-    const T2 *vprev = vbuf + (size_t)((k + 2) % 3) * bstride + g * gstride;   // v_{k-1}
-    const T2 *vprev2 = vbuf + (size_t)((k + 1) % 3) * bstride + g * gstride;  // v_{k-2}
-    T2 *vout = vbuf + (size_t)(k % 3) * bstride + g * gstride;                // v_k
-
-    __syncthreads();
-    for (int q = tid; q < ld * MG; q += kBlock) s_v[q] = ldcg2(vprev + q);  // padding rows are zero
-    __syncthreads();
-
-    const int rows = sg.row1 - sg.row0;
+    const int rows = row1 - row0;
     int WR = 1;
     while (WR < kWarps && WR * kRT < rows) WR <<= 1;
     const int WJ = kWarps / WR;
     const int wr = warp / WJ, wj = warp % WJ;
     const int jchunk = ((ld + WJ - 1) / WJ + 31) / 32 * 32;
     const int j0 = wj * jchunk, j1 = min(ld, j0 + jchunk);
-
-    for (int base = sg.row0; base < sg.row1; base += kRT * WR) {
+    for (int base = row0; base < row1; base += kRT * WR) {
         const int r0 = base + kRT * wr;
         T acc[NB * 32];
 #pragma unroll
         for (int q = 0; q < NB * 32; ++q) acc[q] = T(0);
         const T *cols[kRT];
 #pragma unroll
-        for (int r = 0; r < kRT; ++r) cols[r] = H + (size_t)min(r0 + r, sg.row1 - 1) * ld;
-        const bool full = (r0 + kRT <= sg.row1);
+        for (int r = 0; r < kRT; ++r) cols[r] = M + (size_t)min(r0 + r, row1 - 1) * ld;
+        const bool full = (r0 + kRT <= row1);
         for (int j = j0 + lane; j < j1; j += 32) {
             T2 x[MG];
 #pragma unroll
             for (int c = 0; c < MG; ++c) x[c] = s_v[j * MG + c];
 #pragma unroll
             for (int r = 0; r < kRT; ++r) {
-                const T h = (full || r0 + r < sg.row1) ? cols[r][j] : T(0);
+                const T h = (full || r0 + r < row1) ? cols[r][j] : T(0);
 #pragma unroll
                 for (int c = 0; c < MG; ++c) {
                     acc[(r * MG + c) * 2 + 0] = fma(h, x[c].x, acc[(r * MG + c) * 2 + 0]);
@@ -111,61 +99,101 @@ __device__ void order_rows(const ChebProblem &pb, const ChebSegment &sg, int k, 
             T tmp[32];
 #pragma unroll
             for (int q = 0; q < 32; ++q) tmp[q] = acc[b * 32 + q];
-            const T s = transpose_reduce32(tmp, lane);
+            const T sm = transpose_reduce32(tmp, lane);
             const int idx = b * 32 + lane;
-            if (idx < NV) s_part[((size_t)wj * WR + wr) * NV + idx] = s;
+            if (idx < NV) s_part[((size_t)wj * WR + wr) * NV + idx] = sm;
         }
         __syncthreads();
-        // epilogue: one thread per (row, column) of the super-tile
+        // epilogue: one thread per (row, column) of the super-tile, fixed-order sum over j slices
         for (int t = tid; t < WR * kRT * MG; t += kBlock) {
             const int wrr = t / (kRT * MG), rem = t % (kRT * MG);
             const int r = rem / MG, c = rem % MG;
             const int i = base + kRT * wrr + r;
-            if (i >= sg.row1) continue;
+            if (i >= row1) continue;
             T yr = T(0), yi = T(0);
             for (int w = 0; w < WJ; ++w) {
                 yr += s_part[((size_t)w * WR + wrr) * NV + (r * MG + c) * 2 + 0];
                 yi += s_part[((size_t)w * WR + wrr) * NV + (r * MG + c) * 2 + 1];
             }
-            T2 v;
-            if (k == 1) {
-                v.x = yr;
-                v.y = yi;
-            } else {
-                const T2 w2 = ldcg2(vprev2 + (size_t)i * MG + c);
-                v.x = T(2) * yr - w2.x;
-                v.y = T(2) * yi - w2.y;
-            }
-            vout[(size_t)i * MG + c] = v;
-            const size_t ao = (size_t)i * m + g * MG + c;
-            double2 a = pb.acc[ao];
-            const double vr = (double)v.x, vi = (double)v.y;
-            a.x += cre * vr - cim * vi;
-            a.y += cre * vi + cim * vr;
-            pb.acc[ao] = a;
+            epi(i, c, yr, yi);
         }
         __syncthreads();
     }
 }
 
-// order 0: v_0 = phi (rounded to T), acc = c_0 phi (FP64)
+// epilogue of one order: recurrence + FP64 accumulation of c_k v_k
 template <typename T, int MG>
-__device__ void order_zero(const ChebProblem &pb, const ChebSegment &sg) {
+struct OrderEpi {
+    using T2 = typename Vec2<T>::type;
+    const T2 *vprev2;
+    T2 *vout;
+    double2 *acc;
+    int k, m, g;
+    double cre, cim;
+    __device__ void operator()(int i, int c, T yr, T yi) {
+        T2 v;
+        if (k == 1) {
+            v.x = yr;
+            v.y = yi;
+        } else {
+            const T2 w2 = ldcg2(vprev2 + (size_t)i * MG + c);
+            v.x = T(2) * yr - w2.x;
+            v.y = T(2) * yi - w2.y;
+        }
+        vout[(size_t)i * MG + c] = v;
+        const size_t ao = (size_t)i * m + g * MG + c;
+        double2 a = acc[ao];
+        const double vr = (double)v.x, vi = (double)v.y;
+        a.x += cre * vr - cim * vi;
+        a.y += cre * vi + cim * vr;
+        acc[ao] = a;
+    }
+};
+
+// one order k >= 1 for the rows of segment sg, column group g (MG columns)
+template <typename T, int MG>
+__device__ void order_rows(const ChebProblem &pb, const ChebSegment &sg, int k, int g, int parity,
+                           typename Vec2<T>::type *s_v, T *s_part, double cre, double cim) {
+    using T2 = typename Vec2<T>::type;
+    const int tid = threadIdx.x;
+    const int ld = pb.ld, m = pb.m;
+    T2 *vbuf = reinterpret_cast<T2 *>(pb.vbuf);
+    const size_t gstride = (size_t)pb.ldv * MG;         // one column group
+    const size_t bstride = gstride * (m / MG);          // one of the three vector buffers
+    const T2 *vprev = vbuf + (size_t)((k + 2) % 3) * bstride + g * gstride;   // v_{k-1}
+    __syncthreads();
+    for (int q = tid; q < ld * MG; q += kBlock) s_v[q] = ldcg2(vprev + q);  // padding rows are zero
+    __syncthreads();
+    OrderEpi<T, MG> epi{vbuf + (size_t)((k + 1) % 3) * bstride + g * gstride,
+                        vbuf + (size_t)(k % 3) * bstride + g * gstride, pb.col[parity ^ 1], k, m, g, cre, cim};
+    rows_gemv<T, MG>(reinterpret_cast<const T *>(pb.H), ld, s_v, sg.row0, sg.row1, s_part, epi);
+}
+
+// order 0: v_0 = s phi (rounded to T), acc = c_0 s phi (FP64); s = renormalisation factor
+template <typename T, int MG>
+__device__ void order_zero(const ChebProblem &pb, const ChebSegment &sg, int parity) {
     using T2 = typename Vec2<T>::type;
     T2 *v0 = reinterpret_cast<T2 *>(pb.vbuf);
     const int m = pb.m;
     const size_t gstride = (size_t)pb.ldv * MG;
     const double cre = pb.coef[0].x, cim = pb.coef[0].y;
+    const double2 *phi = pb.col[parity];
+    double2 *acc = pb.col[parity ^ 1];
     for (int q = threadIdx.x; q < (sg.row1 - sg.row0) * m; q += kBlock) {
         const int i = sg.row0 + q / m, col = q % m;
         const int g = col / MG, c = col % MG;
         const size_t o = (size_t)i * m + col;
-        const double2 p = pb.phi[o];
+        double2 p = phi[o];
+        if (pb.scale) {
+            const double sc = pb.scale[col % pb.P];
+            p.x *= sc;
+            p.y *= sc;
+        }
         T2 v;
         v.x = (T)p.x;
         v.y = (T)p.y;
         v0[g * gstride + (size_t)i * MG + c] = v;
-        pb.acc[o] = make_double2(cre * p.x - cim * p.y, cre * p.y + cim * p.x);
+        acc[o] = make_double2(cre * p.x - cim * p.y, cre * p.y + cim * p.x);
     }
 }
 
@@ -183,13 +211,106 @@ __global__ void __launch_bounds__(kBlock, 1) cheb_kernel(ChebLaunch L) {
             const ChebProblem &pb = L.probs[sg.prob];
             if (k > pb.K) continue;
             if (k == 0) {
-                order_zero<T, MG>(pb, sg);
+                order_zero<T, MG>(pb, sg, L.parity);
             } else {
                 const double cre = pb.coef[k].x, cim = pb.coef[k].y;
-                for (int g = 0; g < pb.m / MG; ++g) order_rows<T, MG>(pb, sg, k, g, s_v, s_part, cre, cim);
+                for (int g = 0; g < pb.m / MG; ++g)
+                    order_rows<T, MG>(pb, sg, k, g, L.parity, s_v, s_part, cre, cim);
             }
         }
         if (!grid_barrier(L.bar_count, L.bar_gen, G, L.error)) return;
+    }
+}
+
+// ---- read-out: psi = L^-T phi (A = L^-1), bra = L chi (B = L^T), population partials
+template <typename T, int MG>
+struct ReadEpi {
+    double2 *out;
+    int P, c0;  // out column base
+    __device__ void operator()(int i, int c, T yr, T yi) {
+        out[(size_t)i * P + c0 + c] = make_double2((double)yr, (double)yi);
+    }
+};
+
+template <typename T, int MG>
+__global__ void __launch_bounds__(kBlock, 1) readout_kernel(ChebLaunch L) {
+    using T2 = typename Vec2<T>::type;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *s_part = reinterpret_cast<T *>(smem_raw);
+    T2 *s_v = reinterpret_cast<T2 *>(smem_raw + kCheb_part_bytes);
+    __shared__ double s_pop[kBlock];
+    const int tid = threadIdx.x;
+    const int s0 = L.seg_begin[blockIdx.x], s1 = L.seg_begin[blockIdx.x + 1];
+    for (int s = s0; s < s1; ++s) {
+        const ChebSegment sg = L.segs[s];
+        const ChebProblem &pb = L.probs[sg.prob];
+        if (!pb.A) continue;
+        const int ld = pb.ld, m = pb.m, P = pb.P;
+        const double2 *cols = pb.col[L.parity ^ 1];  // the step's propagated columns
+        for (int pass = 0; pass < 2; ++pass) {       // 0: psi from ket columns, 1: bra
+            const T *M = reinterpret_cast<const T *>(pass == 0 ? pb.A : pb.B);
+            const int src0 = (pass == 1 && m == 2 * P) ? P : 0;
+            double2 *out = pass == 0 ? pb.psi : pb.bra;
+            for (int g = 0; g < P / MG; ++g) {
+                __syncthreads();
+                for (int q = tid; q < ld * MG; q += kBlock) {
+                    const int j = q / MG, c = q % MG;
+                    const double2 v = j < pb.N ? __ldcg(cols + (size_t)j * m + src0 + g * MG + c) : make_double2(0, 0);
+                    T2 t;
+                    t.x = (T)v.x;
+                    t.y = (T)v.y;
+                    s_v[q] = t;
+                }
+                __syncthreads();
+                ReadEpi<T, MG> epi{out, P, g * MG};
+                rows_gemv<T, MG>(M, ld, s_v, sg.row0, sg.row1, s_part, epi);
+            }
+        }
+        __syncthreads();
+        // population partials of this segment: Re conj(psi_ip) bra_ip per (column, fragment)
+        const int nf = min(pb.nfrag, kMaxFrag);
+        double *dst = L.seg_pops + (size_t)s * kMaxCols * (kMaxFrag + 1);
+        for (int p = 0; p < P; ++p) {
+            for (int f = 0; f <= nf; ++f) {
+                double a = 0.0;
+                for (int i = sg.row0 + tid; i < sg.row1; i += kBlock) {
+                    const bool in = (f == nf) || (pb.ao_frag && pb.ao_frag[i] == f);
+                    if (in) {
+                        const double2 x = pb.psi[(size_t)i * P + p], y = pb.bra[(size_t)i * P + p];
+                        a += x.x * y.x + x.y * y.y;
+                    }
+                }
+                s_pop[tid] = a;
+                __syncthreads();
+                for (int o = kBlock / 2; o > 0; o >>= 1) {
+                    if (tid < o) s_pop[tid] += s_pop[tid + o];
+                    __syncthreads();
+                }
+                if (tid == 0) dst[p * (kMaxFrag + 1) + f] = s_pop[0];
+                __syncthreads();
+            }
+        }
+    }
+}
+
+// one block per problem: sum its segments' partials in order -> populations of
+// this step; renormalisation factor for the next step (reduced precision)
+__global__ void reduce_pops_kernel(ChebLaunch L, int nprob) {
+    const int q = blockIdx.x;
+    if (q >= nprob) return;
+    const ChebProblem &pb = L.probs[q];
+    if (!pb.A) return;
+    const int nf = min(pb.nfrag, kMaxFrag), P = pb.P;
+    for (int t = threadIdx.x; t < P * (nf + 1); t += blockDim.x) {
+        const int p = t / (nf + 1), f = t % (nf + 1);
+        double a = 0.0;
+        for (int s = L.prob_seg0[q]; s < L.prob_seg0[q + 1]; ++s)
+            a += L.seg_pops[(size_t)s * kMaxCols * (kMaxFrag + 1) + p * (kMaxFrag + 1) + f];
+        if (L.pops) L.pops[pb.pops_off + p * (pb.nfrag + 1) + (f == nf ? pb.nfrag : f)] = a;
+        if (f == nf && pb.scale_out) {
+            const double tot = a, tgt = pb.target ? pb.target[p] : 0.0;
+            pb.scale_out[p] = (tot > 0.0 && tgt > 0.0) ? sqrt(tgt / tot) : 1.0;
+        }
     }
 }
 
@@ -205,7 +326,37 @@ cudaError_t launch_t(const ChebLaunch &L, cudaStream_t st) {
     return cudaLaunchCooperativeKernel((const void *)kern, dim3(L.grid), dim3(kBlock), args, smem, st);
 }
 
+template <typename T, int MG>
+cudaError_t launch_readout_t(const ChebLaunch &L, int nprob, cudaStream_t st) {
+    auto kern = readout_kernel<T, MG>;
+    const size_t smem = kCheb_part_bytes + (size_t)L.max_ld * MG * sizeof(typename Vec2<T>::type);
+    if (smem > kCheb_smem_limit) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    kern<<<L.grid, kBlock, smem, st>>>(L);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    reduce_pops_kernel<<<nprob, 128, 0, st>>>(L, nprob);
+    return cudaGetLastError();
+}
+
 }  // namespace
+
+cudaError_t launch_readout(const ChebLaunch &L, int nprob, int precision, int mg, cudaStream_t st) {
+    if (precision == ELHL_PREC_FP64) {
+        switch (mg) {
+            case 1: return launch_readout_t<double, 1>(L, nprob, st);
+            case 2: return launch_readout_t<double, 2>(L, nprob, st);
+        }
+    } else {
+        switch (mg) {
+            case 1: return launch_readout_t<float, 1>(L, nprob, st);
+            case 2: return launch_readout_t<float, 2>(L, nprob, st);
+            case 4: return launch_readout_t<float, 4>(L, nprob, st);
+        }
+    }
+    return cudaErrorInvalidValue;
+}
 
 int cheb_block() { return kBlock; }
 

@@ -496,6 +496,16 @@ __global__ void renormalize_kernel(double2 *cols, int n, int m, int P, const dou
 
 struct ChebState {
     int N = 0, ld = 0, m = 0, precision = ELHL_PREC_FP64, K = 0;
+    int parity = 0;            // phi/acc role of col[0], col[1] for the device read-out path
+    void *A = nullptr, *B = nullptr;   // L^-1, L^T in the launch precision (fixed nuclei read-out)
+    bool readout_ready = false, cols_current = false;
+    double *scale = nullptr;   // [P] pending renormalisation factor (reduced precision), 1 otherwise
+    // read-out outputs, owned by the trajectory
+    int P = 0, nfrag = 0;
+    double2 *psi_out = nullptr, *bra_out = nullptr;
+    const int *ao_frag = nullptr;
+    double *target = nullptr;
+    double2 *cin() { return parity ? acc : phi; }
     double *Ht = nullptr;    // FP64 H~
     void *Hs = nullptr;      // scaled, launch precision
     void *vbuf = nullptr;
@@ -519,14 +529,20 @@ struct ChebState {
         CU_TRY(cudaMemset(phi, 0, (size_t)ld * m * sizeof(double2)));
         CU_TRY(cudaMemset(acc, 0, (size_t)ld * m * sizeof(double2)));
         if (int rc = dev_alloc(&lz, (size_t)3 * ld)) return rc;
+        if (int rc = dev_alloc(&scale, (size_t)kMaxCols)) return rc;
+        std::vector<double> ones(kMaxCols, 1.0);
+        CU_TRY(cudaMemcpy(scale, ones.data(), kMaxCols * sizeof(double), cudaMemcpyHostToDevice));
         return ELHL_OK;
     }
     void release() {
-        dev_free(Ht); dev_free(phi); dev_free(acc); dev_free(coef); dev_free(lz);
+        dev_free(Ht); dev_free(phi); dev_free(acc); dev_free(coef); dev_free(lz); dev_free(scale);
         if (Hs) cudaFree(Hs);
         if (vbuf) cudaFree(vbuf);
-        Hs = vbuf = nullptr;
+        if (A) cudaFree(A);
+        if (B) cudaFree(B);
+        Hs = vbuf = A = B = nullptr;
         coef_cap = 0;
+        readout_ready = false;
     }
 };
 
@@ -627,17 +643,71 @@ int cheb_prepare(ChebState &cs, double dt, double tol) {
     return ELHL_OK;
 }
 
+__global__ void identity_kernel(double *A, int n, int ld) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i < ld && j < n) A[(size_t)j * ld + i] = (i == j) ? 1.0 : 0.0;
+}
+
+// dst(i, j) = src(j, i) if transpose else src(i, j), in T, keeping only the
+// lower triangle of src (potrf leaves the other triangle untouched); rows >= n are zero
+template <typename T>
+__global__ void convert_kernel(const double *__restrict__ src, T *__restrict__ dst, int n, int ld, bool transpose) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= ld || j >= n) return;
+    double v = 0.0;
+    if (i < n) {
+        if (transpose) v = (j >= i) ? src[(size_t)i * ld + j] : 0.0;  // src(j, i), j >= i
+        else v = (i >= j) ? src[(size_t)j * ld + i] : 0.0;            // src(i, j), i >= j
+    }
+    dst[(size_t)j * ld + i] = (T)v;
+}
+
+// A = L^-1 and B = L^T (launch precision) for the device read-out of fixed nuclei.
+int cheb_prepare_readout(ChebState &cs, const double *Lfac) {
+    cudaStream_t st = g_ctx.stream;
+    const int n = cs.N, ld = cs.ld;
+    const size_t tsz = cs.precision == ELHL_PREC_FP64 ? sizeof(double) : sizeof(float);
+    if (!cs.A) CU_TRY(cudaMalloc(&cs.A, (size_t)ld * n * tsz));
+    if (!cs.B) CU_TRY(cudaMalloc(&cs.B, (size_t)ld * n * tsz));
+    double *tmp = nullptr;
+    if (int rc = dev_alloc(&tmp, (size_t)ld * n)) return rc;
+    dim3 grid((ld + 127) / 128, n);
+    identity_kernel<<<grid, 128, 0, st>>>(tmp, n, ld);
+    const double one = 1.0;
+    int rc = ELHL_OK;
+    if (cublasDtrsm(g_ctx.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n,
+                    &one, Lfac, ld, tmp, ld) != CUBLAS_STATUS_SUCCESS)
+        rc = ELHL_ERR_CUDA;
+    if (!rc) {
+        if (cs.precision == ELHL_PREC_FP64) {
+            convert_kernel<double><<<grid, 128, 0, st>>>(tmp, (double *)cs.A, n, ld, false);
+            convert_kernel<double><<<grid, 128, 0, st>>>(Lfac, (double *)cs.B, n, ld, true);
+        } else {
+            convert_kernel<float><<<grid, 128, 0, st>>>(tmp, (float *)cs.A, n, ld, false);
+            convert_kernel<float><<<grid, 128, 0, st>>>(Lfac, (float *)cs.B, n, ld, true);
+        }
+        if (cudaGetLastError() != cudaSuccess) rc = ELHL_ERR_CUDA;
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess && !rc) rc = ELHL_ERR_CUDA;
+    dev_free(tmp);
+    if (!rc) cs.readout_ready = true;
+    return rc;
+}
+
 // Launch plan for a set of problems: row segments balanced by matrix elements.
 struct ChebPlan {
     std::vector<ChebProblem> probs;
     std::vector<ChebSegment> segs;
     std::vector<int> seg_begin;
+    std::vector<int> prob_seg0;
     ChebProblem *d_probs = nullptr;
     ChebSegment *d_segs = nullptr;
-    int *d_seg_begin = nullptr;
-    int grid = 0, max_ld = 0, kmax = 0, mg = 0, precision = 0;
+    int *d_seg_begin = nullptr, *d_prob_seg0 = nullptr;
+    double *d_seg_pops = nullptr;
+    int grid = 0, max_ld = 0, kmax = 0, mg = 0, mg_read = 0, precision = 0, parity = 0;
+    size_t pops_per_step = 0;  // populations of all problems in one step
     void release() {
-        dev_free(d_probs); dev_free(d_segs); dev_free(d_seg_begin);
+        dev_free(d_probs); dev_free(d_segs); dev_free(d_seg_begin); dev_free(d_prob_seg0); dev_free(d_seg_pops);
     }
 };
 
@@ -662,12 +732,33 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
     }
     pl.mg = cheb_group_size(pl.precision, mgcd, pl.max_ld);
     if (!pl.mg) return ELHL_ERR_UNSUPPORTED;
+    int pgcd = 0;  // read-out groups must divide every problem's ket columns
+    for (auto *cs : states) {
+        int a = std::max(cs->P, 1), b = pgcd;
+        while (b) { const int t = a % b; a = b; b = t; }
+        pgcd = a;
+    }
+    pl.mg_read = cheb_group_size(pl.precision, pgcd, pl.max_ld);
+    pl.pops_per_step = 0;
+    pl.parity = states[0]->parity;
     for (auto *cs : states) {
         ChebProblem p{};
         p.N = cs->N; p.ld = cs->ld; p.ldv = cs->ld; p.m = cs->m; p.K = cs->K;
-        p.H = cs->Hs; p.vbuf = cs->vbuf; p.phi = cs->phi; p.acc = cs->acc; p.coef = cs->coef;
+        p.H = cs->Hs; p.vbuf = cs->vbuf; p.col[0] = cs->phi; p.col[1] = cs->acc; p.coef = cs->coef;
+        p.P = cs->P;
+        const bool dev = cs->readout_ready && pl.mg_read;
+        p.A = dev ? cs->A : nullptr;
+        p.B = dev ? cs->B : nullptr;
+        p.psi = cs->psi_out; p.bra = cs->bra_out; p.ao_frag = cs->ao_frag; p.nfrag = cs->nfrag;
+        p.pops_off = (int)pl.pops_per_step;
+        const bool renorm = dev && cs->precision != ELHL_PREC_FP64;
+        p.scale = renorm ? cs->scale : nullptr;
+        p.scale_out = renorm ? cs->scale : nullptr;
+        p.target = renorm ? cs->target : nullptr;
+        pl.pops_per_step += (size_t)cs->P * (cs->nfrag + 1);
         pl.probs.push_back(p);
         pl.kmax = std::max(pl.kmax, cs->K);
+        if (cs->parity != pl.parity) return ELHL_ERR_BAD_ARG;
     }
     // greedy split of the concatenated rows: CTA c fills up to (c+1)/grid of the work
     const double per = work / pl.grid;
@@ -694,6 +785,12 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
         }
     }
     for (int cc = c + 1; cc <= pl.grid; ++cc) pl.seg_begin[cc] = (int)pl.segs.size();
+    pl.prob_seg0.assign(states.size() + 1, 0);
+    for (size_t i = 0; i < pl.segs.size(); ++i) pl.prob_seg0[pl.segs[i].prob + 1] = (int)i + 1;
+    for (size_t q = 1; q <= states.size(); ++q) pl.prob_seg0[q] = std::max(pl.prob_seg0[q], pl.prob_seg0[q - 1]);
+    if (int rc = dev_alloc(&pl.d_prob_seg0, pl.prob_seg0.size())) return rc;
+    CU_TRY(cudaMemcpy(pl.d_prob_seg0, pl.prob_seg0.data(), pl.prob_seg0.size() * sizeof(int), cudaMemcpyHostToDevice));
+    if (int rc = dev_alloc(&pl.d_seg_pops, pl.segs.size() * kMaxCols * (kMaxFrag + 1))) return rc;
     if (int rc = dev_alloc(&pl.d_probs, pl.probs.size())) return rc;
     if (int rc = dev_alloc(&pl.d_segs, pl.segs.size())) return rc;
     if (int rc = dev_alloc(&pl.d_seg_begin, pl.seg_begin.size())) return rc;
@@ -729,9 +826,68 @@ int cheb_run(ChebPlan &pl) {
     L.bar_count = g_ctx.bar;
     L.bar_gen = g_ctx.bar + 1;
     L.error = g_ctx.err;
+    L.prob_seg0 = pl.d_prob_seg0;
+    L.parity = pl.parity;
+    L.seg_pops = pl.d_seg_pops;
     CU_TRY(cudaEventRecord(g_ctx.ev[0], st));
     CU_TRY(launch_cheb(L, pl.precision, pl.mg, st));
     CU_TRY(cudaEventRecord(g_ctx.ev[1], st));
+    return ELHL_OK;
+}
+
+// One fixed-nuclei step with the device read-out: propagation launch, read-out
+// launch (+ population reduction), then the columns swap roles.  No host sync.
+int cheb_dev_step(ChebPlan &pl, const std::vector<ChebState *> &states, double *d_pops_step) {
+    if (int rc = cheb_run(pl)) return rc;
+    ChebLaunch L{};
+    L.probs = pl.d_probs;
+    L.segs = pl.d_segs;
+    L.seg_begin = pl.d_seg_begin;
+    L.prob_seg0 = pl.d_prob_seg0;
+    L.max_ld = pl.max_ld;
+    L.grid = pl.grid;
+    L.parity = pl.parity;
+    L.seg_pops = pl.d_seg_pops;
+    L.pops = d_pops_step;
+    CU_TRY(launch_readout(L, (int)pl.probs.size(), pl.precision, pl.mg_read, g_ctx.stream));
+    pl.parity ^= 1;
+    for (auto *cs : states) cs->parity = pl.parity;
+    return ELHL_OK;
+}
+
+// apply the pending renormalisation factor to the next input columns and the
+// AO-basis outputs, then reset it to 1 (end of a multi-step call)
+__global__ void settle_scale_kernel(double2 *cols, int m, double2 *psi, double2 *bra, int n, int P, double *scale) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        for (int c = 0; c < m; ++c) {
+            const double sc = scale[c % P];
+            double2 v = cols[(size_t)i * m + c];
+            cols[(size_t)i * m + c] = make_double2(v.x * sc, v.y * sc);
+        }
+        for (int p = 0; p < P; ++p) {
+            const double sc = scale[p];
+            double2 a = psi[(size_t)i * P + p], b = bra[(size_t)i * P + p];
+            psi[(size_t)i * P + p] = make_double2(a.x * sc, a.y * sc);
+            bra[(size_t)i * P + p] = make_double2(b.x * sc, b.y * sc);
+        }
+    }
+}
+
+__global__ void ones_kernel(double *v, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = 1.0;
+}
+
+int cheb_settle(const std::vector<ChebState *> &states) {
+    cudaStream_t st = g_ctx.stream;
+    for (auto *cs : states) {
+        if (cs->precision == ELHL_PREC_FP64) continue;
+        settle_scale_kernel<<<(cs->N + 255) / 256, 256, 0, st>>>(cs->cin(), cs->m, cs->psi_out, cs->bra_out, cs->N,
+                                                                 cs->P, cs->scale);
+        ones_kernel<<<1, kMaxCols, 0, st>>>(cs->scale, kMaxCols);
+    }
+    CU_TRY(cudaGetLastError());
     return ELHL_OK;
 }
 
@@ -870,12 +1026,14 @@ int cheb_load_columns(elhl_traj *tr) {
     ChebState &cs = tr->cs;
     const int P = tr->P, n = tr->N;
     const size_t e = sizeof(double2);
-    CU_TRY(cudaMemcpy2DAsync(cs.phi, cs.m * e, tr->psi_ao, P * e, P * e, n, cudaMemcpyDeviceToDevice, st));
+    double2 *in = cs.cin();
+    CU_TRY(cudaMemcpy2DAsync(in, cs.m * e, tr->psi_ao, P * e, P * e, n, cudaMemcpyDeviceToDevice, st));
     if (cs.m == 2 * P)
-        CU_TRY(cudaMemcpy2DAsync(cs.phi + P, cs.m * e, tr->bra_ao, P * e, P * e, n, cudaMemcpyDeviceToDevice, st));
-    if (int rc = cols_apply(tr->fac.L, tr->ld, n, cs.phi, cs.m, 0, P, false, false)) return rc;       // L^T psi
+        CU_TRY(cudaMemcpy2DAsync(in + P, cs.m * e, tr->bra_ao, P * e, P * e, n, cudaMemcpyDeviceToDevice, st));
+    if (int rc = cols_apply(tr->fac.L, tr->ld, n, in, cs.m, 0, P, false, false)) return rc;       // L^T psi
     if (cs.m == 2 * P)
-        if (int rc = cols_apply(tr->fac.L, tr->ld, n, cs.phi, cs.m, P, P, true, true)) return rc;    // L^-1 bra
+        if (int rc = cols_apply(tr->fac.L, tr->ld, n, in, cs.m, P, P, true, true)) return rc;    // L^-1 bra
+    cs.cols_current = true;
     return ELHL_OK;
 }
 
@@ -903,14 +1061,43 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
     const int P = tr->P, nf = tr->nfrag;
     const size_t pop_per_step = (size_t)P * (nf + 1);
     const size_t nc = (size_t)tr->natoms * 3;
+    std::vector<ChebState *> one{&cs};
+    int rc = ELHL_OK;
+    if (!coords && !cs.readout_ready && tr->fac.L) {
+        // fixed nuclei after moving steps: factor-based read-out matrices for the current L
+        if ((rc = cheb_prepare_readout(cs, tr->fac.L))) return rc;
+        if ((rc = cheb_plan(tr->plan, one))) return rc;
+    }
+    if (!coords && cs.readout_ready && tr->plan.mg_read) {
+        // ---- fixed nuclei, device read-out: two launches per step, no host sync
+        if (!cs.cols_current && (rc = cheb_load_columns(tr))) return rc;
+        CU_TRY(cudaEventRecord(g_ctx.ev[2], st));
+        for (int s = 0; s < nsteps; ++s)
+            if ((rc = cheb_dev_step(tr->plan, one, d_pops ? d_pops + s * pop_per_step : nullptr))) return rc;
+        CU_TRY(cudaEventRecord(g_ctx.ev[3], st));
+        if ((rc = cheb_settle(one))) return rc;
+        int err = 0;
+        CU_TRY(cudaMemcpyAsync(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaStreamSynchronize(st));
+        if (err) return err;
+        tr->stats.prop_ms += event_ms(0, 1) * nsteps;  // last launch x launches
+        tr->stats.rebuild_ms += 0.0;
+        tr->stats.prop_launches += nsteps;
+        tr->stats.orders += (long long)cs.K * cs.m * nsteps;
+        tr->stats.substeps += nsteps;
+        for (int s = 0; s < nsteps; ++s) tr->t = tr->t + tr->cfg.dt * tr->cfg.frame_step;
+        tr->it += nsteps;
+        tr->first_call = false;
+        for (int p = 0; p < P; ++p) tr->save_tau[p] = tr->cfg.dt / kHbar;
+        return ELHL_OK;
+    }
+    // ---- moving nuclei (or no device read-out): factor-based read-out through cuBLAS
     const bool renorm = cs.precision != ELHL_PREC_FP64;
     double *pops_tmp = nullptr;
     if (!d_pops && renorm) {
-        if (int rc = dev_alloc(&pops_tmp, pop_per_step)) return rc;
+        if ((rc = dev_alloc(&pops_tmp, pop_per_step))) return rc;
     }
-    int rc = ELHL_OK;
-    std::vector<ChebState *> one{&cs};
-    if (!coords) rc = cheb_load_columns(tr);
+    if (!coords && !cs.cols_current) rc = cheb_load_columns(tr);
     for (int s = 0; s < nsteps && !rc; ++s) {
         if (coords) {
             const double *dc;
@@ -928,20 +1115,22 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
                 break;
             }
             if ((rc = cheb_rebuild_operator(tr))) break;
+            cs.readout_ready = false;  // L changed
             if ((rc = cheb_load_columns(tr))) break;
             if (cudaEventRecord(g_ctx.ev[3], st) != cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
             if ((rc = cheb_plan_refresh(tr->plan, one))) break;
         }
         if ((rc = cheb_run(tr->plan))) break;
+        double2 *out = cs.parity ? cs.phi : cs.acc;
         double *pp = d_pops ? d_pops + s * pop_per_step : pops_tmp;
-        if ((rc = cheb_readout(tr, cs.acc, pp))) break;
+        if ((rc = cheb_readout(tr, out, pp))) break;
         if (renorm) {
-            renormalize_kernel<<<(tr->N + 255) / 256, 256, 0, st>>>(cs.acc, tr->N, cs.m, P, pp, nf, tr->target);
+            renormalize_kernel<<<(tr->N + 255) / 256, 256, 0, st>>>(out, tr->N, cs.m, P, pp, nf, tr->target);
             if (cudaGetLastError() != cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
-            if ((rc = cheb_readout(tr, cs.acc, nullptr))) break;  // AO state follows the renormalised columns
+            if ((rc = cheb_readout(tr, out, nullptr))) break;  // AO state follows the renormalised columns
         }
-        if (cudaMemcpyAsync(cs.phi, cs.acc, (size_t)cs.ld * cs.m * sizeof(double2), cudaMemcpyDeviceToDevice, st) !=
-            cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
+        tr->plan.parity ^= 1;
+        cs.parity = tr->plan.parity;
         int err = 0;
         if (cudaMemcpyAsync(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
             cudaStreamSynchronize(st) != cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
@@ -1160,6 +1349,7 @@ int cheb_set_psi(elhl_traj *tr, const elhl_zcomplex *bra, const elhl_zcomplex *k
 // norm target of each particle = its current total population
 int cheb_set_target(elhl_traj *tr) {
     const int P = tr->P, n = tr->N;
+    tr->cs.cols_current = false;  // a new state: columns reload from psi_ao / bra_ao
     double *pops = nullptr;
     if (int rc = dev_alloc(&pops, (size_t)P * (tr->nfrag + 1))) return rc;
     populations_kernel<<<P, 256, 0, g_ctx.stream>>>(tr->psi_ao, tr->bra_ao, n, P, tr->basis.ao_frag, tr->nfrag, pops);
@@ -1345,6 +1535,10 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
         if (!rc && cudaMemset(tr->psi_ao, 0, (size_t)tr->ld * tr->P * sizeof(double2)) != cudaSuccess) rc = ELHL_ERR_CUDA;
         if (!rc && cudaMemset(tr->bra_ao, 0, (size_t)tr->ld * tr->P * sizeof(double2)) != cudaSuccess) rc = ELHL_ERR_CUDA;
         if (!rc) rc = cheb_rebuild_operator(tr);
+        ChebState &cs = tr->cs;
+        cs.P = tr->P; cs.nfrag = tr->nfrag; cs.psi_out = tr->psi_ao; cs.bra_out = tr->bra_ao;
+        cs.ao_frag = tr->basis.ao_frag; cs.target = tr->target;
+        if (!rc) rc = cheb_prepare_readout(cs, tr->fac.L);
         std::vector<ChebState *> one{&tr->cs};
         if (!rc) rc = cheb_plan(tr->plan, one);
     }
@@ -1586,34 +1780,28 @@ int elhl_batch_step(elhl_batch *b, int nsteps, double *pops) {
         b->pops_cap = per_step * nsteps;
     }
     memset(&b->stats, 0, sizeof(b->stats));
+    if (!b->plan.mg_read) return ELHL_ERR_UNSUPPORTED;
     for (auto *tr : b->members)
-        if (int rc = cheb_load_columns(tr)) return rc;
+        if (!tr->cs.cols_current)
+            if (int rc = cheb_load_columns(tr)) return rc;
+    (void)per_traj;
     for (int s = 0; s < nsteps; ++s) {
-        if (int rc = cheb_run(b->plan)) return rc;
-        for (int q = 0; q < nt; ++q) {
-            elhl_traj *tr = b->members[q];
-            ChebState &cs = tr->cs;
-            double *pp = b->pops + s * per_step + q * per_traj;
-            if (int rc = cheb_readout(tr, cs.acc, pp)) return rc;
-            if (cs.precision != ELHL_PREC_FP64) {
-                renormalize_kernel<<<(tr->N + 255) / 256, 256, 0, st>>>(cs.acc, tr->N, cs.m, P, pp, nf, tr->target);
-                CU_TRY(cudaGetLastError());
-                if (int rc = cheb_readout(tr, cs.acc, nullptr)) return rc;
-            }
-            CU_TRY(cudaMemcpyAsync(cs.phi, cs.acc, (size_t)cs.ld * cs.m * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+        if (int rc = cheb_dev_step(b->plan, b->states, b->pops + s * per_step)) return rc;
+        for (auto *tr : b->members) {
             tr->t = tr->t + tr->cfg.dt * tr->cfg.frame_step;
             tr->it += 1;
             tr->first_call = false;
         }
-        int err = 0;
-        CU_TRY(cudaMemcpyAsync(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost, st));
-        CU_TRY(cudaStreamSynchronize(st));
-        if (err) return err;
-        b->stats.prop_ms += event_ms(0, 1);
-        b->stats.prop_launches += 1;
-        for (auto *cs : b->states) b->stats.orders += (long long)cs->K * cs->m;
-        b->stats.substeps += nt;
     }
+    if (int rc = cheb_settle(b->states)) return rc;
+    int err = 0;
+    CU_TRY(cudaMemcpyAsync(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
+    if (err) return err;
+    b->stats.prop_ms += event_ms(0, 1) * nsteps;
+    b->stats.prop_launches += nsteps;
+    for (auto *cs : b->states) b->stats.orders += (long long)cs->K * cs->m * nsteps;
+    b->stats.substeps += (long long)nt * nsteps;
     if (pops) CU_TRY(cudaMemcpy(pops, b->pops, per_step * nsteps * sizeof(double), cudaMemcpyDeviceToHost));
     return ELHL_OK;
 }
@@ -1672,6 +1860,7 @@ struct elhl_server {
     std::vector<long long> newly_done;
     ChebPlan plan;
     bool plan_dirty = true;
+    int parity = 0;
     long long next_id = 1;
     double *pops = nullptr;
     size_t pops_cap = 0;
@@ -1699,10 +1888,12 @@ static int server_admit(elhl_server *sv, ServerRequest *r) {
                                            r->states.data()))
         return rc;
     std::lock_guard<std::mutex> lk(g_ctx.mu);
-    CU_TRY(cudaStreamSynchronize(g_ctx.stream));
     elhl_traj *tr = r->tr;
+    tr->cs.parity = sv->parity;  // join the running batch's column roles
+    if (int rc = cheb_load_columns(tr)) return rc;
+    CU_TRY(cudaStreamSynchronize(g_ctx.stream));
     dev_free(tr->S); dev_free(tr->h); dev_free(tr->cs.Ht); dev_free(tr->cs.lz);
-    return cheb_load_columns(tr);
+    return ELHL_OK;
 }
 
 extern "C" {
@@ -1786,23 +1977,17 @@ int elhl_server_step(elhl_server *sv, int *n_active, int *n_pending) {
             if (int rc = dev_alloc(&sv->pops, need)) return rc;
             sv->pops_cap = need;
         }
-        if (int rc = cheb_run(sv->plan)) return rc;
+        std::vector<ChebState *> states;
+        for (auto *r : sv->active) states.push_back(&r->tr->cs);
+        if (!sv->plan.mg_read) return ELHL_ERR_UNSUPPORTED;
+        if (int rc = cheb_dev_step(sv->plan, states, sv->pops)) return rc;
+        sv->parity = sv->plan.parity;
+        std::vector<ChebState *> leaving;
+        for (auto *r : sv->active)
+            if (r->done_steps + 1 >= r->nsteps) leaving.push_back(&r->tr->cs);
+        if (!leaving.empty())
+            if (int rc = cheb_settle(leaving)) return rc;
         size_t off = 0;
-        for (auto *r : sv->active) {
-            elhl_traj *tr = r->tr;
-            ChebState &cs = tr->cs;
-            double *pp = sv->pops + off;
-            if (int rc = cheb_readout(tr, cs.acc, pp)) return rc;
-            if (cs.precision != ELHL_PREC_FP64) {
-                renormalize_kernel<<<(tr->N + 255) / 256, 256, 0, st>>>(cs.acc, tr->N, cs.m, tr->P, pp, tr->nfrag,
-                                                                        tr->target);
-                CU_TRY(cudaGetLastError());
-                if (int rc = cheb_readout(tr, cs.acc, nullptr)) return rc;
-            }
-            CU_TRY(cudaMemcpyAsync(cs.phi, cs.acc, (size_t)cs.ld * cs.m * sizeof(double2), cudaMemcpyDeviceToDevice,
-                                   st));
-            off += (size_t)r->P * (r->nfrag + 1);
-        }
         int err = 0;
         CU_TRY(cudaMemcpyAsync(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost, st));
         CU_TRY(cudaStreamSynchronize(st));

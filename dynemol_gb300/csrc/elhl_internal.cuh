@@ -76,13 +76,22 @@ int taylor_grid_size(int block, int *grid_out);
 constexpr int kTaylorBlock = 256;
 
 // ---- Chebyshev engine (cheb.cu, chebcoef.cu) ---------------------------------
+constexpr int kMaxCols = 64;  // ket columns per problem (read-out partial layout)
 struct ChebProblem {
     int N, ld, ldv, m, K;   // size, matrix/vector leading dims (padded rows are 0), complex columns, last order
     const void *H;          // Hs = (H~ - a)/b in the launch precision, N columns of ld rows (symmetric)
     void *vbuf;             // [3][m/MG][ldv][MG] complex vectors in the launch precision
-    double2 *phi;           // [ldv][m] input columns (FP64)
-    double2 *acc;           // [ldv][m] output columns (FP64)
+    double2 *col[2];        // ping-pong columns [ldv][m] (FP64): col[parity] in, col[parity^1] out
     const double2 *coef;    // [K+1] expansion coefficients (phase folded in)
+    const double *scale;    // [P] factor applied to the input columns (renormalisation) or nullptr
+    // read-out (fixed nuclei): P ket columns; bra from columns P..2P-1 when m == 2P, else from the kets
+    int P;
+    const void *A, *B;      // L^-1 and L^T in the launch precision (ld x N), nullptr = no device read-out
+    double2 *psi, *bra;     // [ldv][P] AO-basis Psi_ket / Psi_bra outputs
+    const int *ao_frag;
+    int nfrag, pops_off;    // populations of this problem at pops + pops_off, P x (nfrag+1)
+    const double *target;   // [P] norm targets for the renormalisation factor, or nullptr
+    double *scale_out;      // [P] factor for the next step, or nullptr
 };
 struct ChebSegment {
     int prob, row0, row1;   // rows [row0, row1) of problem `prob` owned by one CTA
@@ -91,9 +100,12 @@ struct ChebLaunch {
     const ChebProblem *probs;
     const ChebSegment *segs;
     const int *seg_begin;   // [grid + 1]: CTA c owns segs[seg_begin[c] .. seg_begin[c+1])
-    int kmax, max_ld, grid;
+    const int *prob_seg0;   // [nprob + 1]: problem q owns segs[prob_seg0[q] .. prob_seg0[q+1])
+    int kmax, max_ld, grid, parity;
     unsigned *bar_count, *bar_gen;
     int *error;
+    double *seg_pops;       // [nseg][kMaxCols][kMaxFrag+1] read-out partials
+    double *pops;           // this step's populations block, or nullptr
 };
 constexpr size_t kCheb_part_bytes = 16 * 64 * sizeof(double);  // cross-warp partial sums
 constexpr size_t kCheb_smem_limit = 200 * 1024;
@@ -101,6 +113,7 @@ int cheb_block();
 int cheb_grid_size(int *grid_out);
 int cheb_group_size(int precision, int m, int max_ld);  // columns staged per pass, 0 = unsupported
 cudaError_t launch_cheb(const ChebLaunch &L, int precision, int mg, cudaStream_t st);
+cudaError_t launch_readout(const ChebLaunch &L, int nprob, int precision, int mg, cudaStream_t st);
 
 int bessel_j_sequence(double beta, int kmax, double *J);
 int chebyshev_coefficients(double dt, double emin, double emax, double tol, int kcap, std::vector<double> &cre,
