@@ -411,6 +411,38 @@ def run_mix(args, ntraj, steps, warm, precision, dropin_sample):
     return res
 
 
+def run_precision_study(args, steps=5, ncols=64, nao=8192):
+    """Config 3: C/H honeycomb sheet with N = 8192 AOs, 64 complex columns
+    (seeded random fragment MOs), fixed nuclei, dt 0.1 fs.  FP32 runs H.Psi as
+    tensor-core GEMMs (FP32-accuracy emulation); FP64 runs the GEMV kernel.
+    Reports steps/s of the 64-column block and the population error per step."""
+    import torch
+    from dynemol_gb300 import api, systems
+    sysm = systems.honeycomb_sheet(nao)
+    nf = int(sum(sysm.atom_nao[a] for a in sysm.fragment_atoms("E")))
+    states = (systems.SplitMix64(3).permutation(nf)[:ncols] + 1).tolist()
+    res = {"N_ao": sysm.nao, "columns": ncols, "dt_ps": 1e-4, "steps": steps}
+    pops = {}
+    for prec, name in ((api.PREC_FP64, "fp64"), (api.PREC_FP32, "fp32_tensor_gemm")):
+        tr = api.Trajectory(sysm, dt=1e-4, method=api.METHOD_CHEBYSHEV, precision=prec, ncols=ncols,
+                            nparticles=ncols, cheb_tol=1e-12)
+        tr.init_fmo_states(states)
+        tr.step(None, nsteps=1, want_pops=False)
+        tr.init_fmo_states(states)  # same start for both precisions
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pops[name] = tr.step(None, nsteps=steps)
+        el = time.perf_counter() - t0
+        st = tr.stats()
+        res[name] = {"steps_per_s": steps / el, "kernel_ms_per_step": st.prop_ms / steps,
+                     "orders_per_step": st.orders / steps / ncols}
+        tr.close()
+    err = np.abs(pops["fp32_tensor_gemm"] - pops["fp64"]).max(axis=(1, 2))
+    res["pop_err_per_step_fp32_vs_fp64"] = [float(x) for x in err]
+    res["speedup_fp32_tensor_vs_fp64"] = res["fp32_tensor_gemm"]["steps_per_s"] / res["fp64"]["steps_per_s"]
+    return res
+
+
 def run_serve(args, nreq, rate, steps_scale, nmax, precision, budget):
     """Poisson stream of propagation requests against an HBM budget (continuous
     batching).  Returns latency percentiles and aggregate steps/s."""
@@ -470,6 +502,7 @@ def main():
                     "of this many trajectories (0 = skip)")
     ap.add_argument("--no-dropin", action="store_true", help="skip the Taylor drop-in measurement")
     ap.add_argument("--serve", type=int, default=0, help="also run a serving stream of this many requests")
+    ap.add_argument("--precision-study", action="store_true", help="also run the N = 8192, 64-column study")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
@@ -490,6 +523,8 @@ def main():
         from dynemol_gb300 import api
         line["north_star_mix"] = run_mix(args, args.mix, steps=5, warm=2, precision=api.PREC_FP32,
                                          dropin_sample=4)
+    if rank == 0 and args.precision_study:
+        line["precision_study"] = run_precision_study(args)
     if rank == 0 and args.serve:
         from dynemol_gb300 import api
         line["serving"] = run_serve(args, args.serve, rate=200.0, steps_scale=0.02, nmax=4096,

@@ -23,6 +23,7 @@ using namespace elhl;
 namespace {
 
 thread_local int g_last_status = ELHL_OK;
+constexpr int kGemmMinCols = 8;  // complex columns from which H.Psi runs as a tensor-core GEMM
 
 #define CU_TRY(expr)                                                                  \
     do {                                                                              \
@@ -68,6 +69,8 @@ struct Context {
     cudaStream_t stream = nullptr, copy_stream = nullptr, own_stream = nullptr;
     cusolverDnHandle_t solver = nullptr;
     cublasHandle_t blas = nullptr;
+    cublasHandle_t blas_tc = nullptr;  // tensor-core emulated FP32 GEMMs (GEMM regime), fixed workspace
+    void *tc_ws = nullptr;
     unsigned *bar = nullptr;  // [2] count, gen
     int *err = nullptr;
     double *partials = nullptr;
@@ -94,6 +97,12 @@ int ensure_context_locked(int device) {
     SOLVER_TRY(cusolverDnSetStream(g_ctx.solver, g_ctx.stream));
     if (cublasCreate(&g_ctx.blas) != CUBLAS_STATUS_SUCCESS) return ELHL_ERR_CUDA;
     if (cublasSetStream(g_ctx.blas, g_ctx.stream) != CUBLAS_STATUS_SUCCESS) return ELHL_ERR_CUDA;
+    if (cublasCreate(&g_ctx.blas_tc) != CUBLAS_STATUS_SUCCESS) return ELHL_ERR_CUDA;
+    if (cublasSetStream(g_ctx.blas_tc, g_ctx.stream) != CUBLAS_STATUS_SUCCESS) return ELHL_ERR_CUDA;
+    CU_TRY(cudaMalloc(&g_ctx.tc_ws, 64u << 20));
+    if (cublasSetWorkspace(g_ctx.blas_tc, g_ctx.tc_ws, 64u << 20) != CUBLAS_STATUS_SUCCESS) return ELHL_ERR_CUDA;
+    cublasSetMathMode(g_ctx.blas_tc, CUBLAS_FP32_EMULATED_BF16X9_MATH);
+    cublasSetEmulationStrategy(g_ctx.blas_tc, CUBLAS_EMULATION_STRATEGY_EAGER);
     if (int rc = dev_alloc(&g_ctx.bar, 2)) return rc;
     if (int rc = dev_alloc(&g_ctx.err, 1)) return rc;
     if (int rc = dev_alloc(&g_ctx.partials, (size_t)2 * 2 * g_ctx.grid * 16)) return rc;
@@ -506,6 +515,12 @@ struct ChebState {
     const int *ao_frag = nullptr;
     double *target = nullptr;
     double2 *cin() { return parity ? acc : phi; }
+    // GEMM regime (many columns, FP32): tensor-core GEMMs per order, one CUDA graph per step parity
+    bool gemm = false;
+    float *Y = nullptr;        // [ld][m] complex (2m x ld real), GEMM output
+    float *Vf = nullptr;       // [ld][m] complex FP32 copy of the propagated columns (read-out input)
+    double *gpops = nullptr;   // [P][nfrag+1] populations of the last step
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
     double *Ht = nullptr;    // FP64 H~
     void *Hs = nullptr;      // scaled, launch precision
     void *vbuf = nullptr;
@@ -513,6 +528,7 @@ struct ChebState {
     double2 *coef = nullptr;
     int coef_cap = 0;
     double emin = 0.0, emax = 0.0, a = 0.0, b = 1.0;
+    double2 c0{1.0, 0.0};    // host copy of the order-0 coefficient
     double *lz = nullptr;    // Lanczos vectors [3][ld]
     int alloc(int N_, int m_, int prec) {
         N = N_;
@@ -535,6 +551,14 @@ struct ChebState {
         return ELHL_OK;
     }
     void release() {
+        for (auto &g : graph) {
+            if (g) cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+        if (Y) cudaFree(Y);
+        if (Vf) cudaFree(Vf);
+        Y = Vf = nullptr;
+        dev_free(gpops);
         dev_free(Ht); dev_free(phi); dev_free(acc); dev_free(coef); dev_free(lz); dev_free(scale);
         if (Hs) cudaFree(Hs);
         if (vbuf) cudaFree(vbuf);
@@ -637,6 +661,11 @@ int cheb_prepare(ChebState &cs, double dt, double tol) {
     }
     std::vector<double2> c(K + 1);
     for (int k = 0; k <= K; ++k) c[k] = make_double2(cre[k], cim[k]);
+    cs.c0 = c[0];
+    for (auto &g : cs.graph) {  // recorded with the old coefficients
+        if (g) cudaGraphExecDestroy(g);
+        g = nullptr;
+    }
     CU_TRY(cudaMemcpyAsync(cs.coef, c.data(), (K + 1) * sizeof(double2), cudaMemcpyHostToDevice, st));
     CU_TRY(cudaStreamSynchronize(st));  // c is a host temporary
     cs.K = K;
@@ -692,6 +721,122 @@ int cheb_prepare_readout(ChebState &cs, const double *Lfac) {
     dev_free(tmp);
     if (!rc) cs.readout_ready = true;
     return rc;
+}
+
+// ---- GEMM regime kernels (complex columns [ld][m], element-wise) -------------
+__global__ void gemm_order0_kernel(const double2 *__restrict__ phi, const double *__restrict__ scale, int P, int n,
+                                   int m, double2 c0, float2 *__restrict__ v0, double2 *__restrict__ acc) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n * m) return;
+    double2 p = phi[q];
+    const double sc = scale ? scale[(q % m) % P] : 1.0;
+    p.x *= sc;
+    p.y *= sc;
+    v0[q] = make_float2((float)p.x, (float)p.y);
+    acc[q] = make_double2(c0.x * p.x - c0.y * p.y, c0.x * p.y + c0.y * p.x);
+}
+
+__global__ void gemm_epilogue_kernel(const float2 *__restrict__ Y, const float2 *__restrict__ vprev2,
+                                     float2 *__restrict__ vout, double2 *__restrict__ acc, const double2 *coef, int k,
+                                     int nm) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nm) return;
+    const float2 y = Y[q];
+    float2 v;
+    if (k == 1) {
+        v = y;
+    } else {
+        const float2 w = vprev2[q];
+        v = make_float2(2.0f * y.x - w.x, 2.0f * y.y - w.y);
+    }
+    vout[q] = v;
+    const double2 c = coef[k];
+    double2 a = acc[q];
+    a.x += c.x * (double)v.x - c.y * (double)v.y;
+    a.y += c.x * (double)v.y + c.y * (double)v.x;
+    acc[q] = a;
+}
+
+__global__ void to_float2_kernel(const double2 *__restrict__ src, float2 *__restrict__ dst, int nm) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < nm) dst[q] = make_float2((float)src[q].x, (float)src[q].y);
+}
+
+__global__ void to_double2_kernel(const float2 *__restrict__ src, double2 *__restrict__ dst, int nm) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < nm) dst[q] = make_double2((double)src[q].x, (double)src[q].y);
+}
+
+__global__ void scale_from_pops_kernel(const double *pops, int P, int nfrag, const double *target, double *scale) {
+    const int p = threadIdx.x;
+    if (p < P) {
+        const double tot = pops[(size_t)p * (nfrag + 1) + nfrag];
+        scale[p] = (tot > 0.0 && target[p] > 0.0) ? sqrt(target[p] / tot) : 1.0;
+    }
+}
+
+// Yt (2m x n) = Vt (2m x n, ld 2m) * M (n x n, ld), FP32 data, tensor cores with
+// FP32-accuracy emulation (three BF16 terms per operand)
+int gemm_vt(cublasHandle_t h, int m2, int n, const float *Vt, const float *M, int ld, float *Yt) {
+    const float one = 1.0f, zero = 0.0f;
+    BLAS_TRY(cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m2, n, n, &one, Vt, CUDA_R_32F, m2, M, CUDA_R_32F, ld, &zero,
+                          Yt, CUDA_R_32F, m2, CUBLAS_COMPUTE_32F_EMULATED_16BFX9, CUBLAS_GEMM_DEFAULT));
+    return ELHL_OK;
+}
+
+// Enqueue one GEMM-regime step (fixed nuclei, FP32, ket columns only) on the
+// context stream: order 0, K x (tensor-core GEMM + recurrence epilogue), read-out
+// GEMMs with A = L^-1 and B = L^T, populations into cs.gpops, renormalisation factor.
+int cheb_gemm_enqueue(ChebState &cs, int parity) {
+    cudaStream_t st = g_ctx.stream;
+    const int n = cs.N, m = cs.m, nm = n * m, tb = 256, nb = (nm + tb - 1) / tb;
+    float2 *vb = reinterpret_cast<float2 *>(cs.vbuf);
+    const size_t vs = (size_t)cs.ld * m;
+    const double2 *in = parity ? cs.acc : cs.phi;
+    double2 *out = parity ? cs.phi : cs.acc;
+    const bool renorm = true;
+    gemm_order0_kernel<<<nb, tb, 0, st>>>(in, renorm ? cs.scale : nullptr, cs.P, n, m, cs.c0, vb, out);
+    for (int k = 1; k <= cs.K; ++k) {
+        if (int rc = gemm_vt(g_ctx.blas_tc, 2 * m, n, reinterpret_cast<const float *>(vb + ((k + 2) % 3) * vs),
+                             reinterpret_cast<const float *>(cs.Hs), cs.ld, cs.Y))
+            return rc;
+        gemm_epilogue_kernel<<<nb, tb, 0, st>>>(reinterpret_cast<const float2 *>(cs.Y), vb + ((k + 1) % 3) * vs,
+                                                vb + (k % 3) * vs, out, cs.coef, k, nm);
+    }
+    to_float2_kernel<<<nb, tb, 0, st>>>(out, reinterpret_cast<float2 *>(cs.Vf), nm);
+    if (int rc = gemm_vt(g_ctx.blas_tc, 2 * m, n, cs.Vf, reinterpret_cast<const float *>(cs.A), cs.ld, cs.Y)) return rc;
+    to_double2_kernel<<<nb, tb, 0, st>>>(reinterpret_cast<const float2 *>(cs.Y), cs.psi_out, nm);
+    if (int rc = gemm_vt(g_ctx.blas_tc, 2 * m, n, cs.Vf, reinterpret_cast<const float *>(cs.B), cs.ld, cs.Y)) return rc;
+    to_double2_kernel<<<nb, tb, 0, st>>>(reinterpret_cast<const float2 *>(cs.Y), cs.bra_out, nm);
+    populations_kernel<<<cs.P, 256, 0, st>>>(cs.psi_out, cs.bra_out, n, cs.P, cs.ao_frag, cs.nfrag, cs.gpops);
+    scale_from_pops_kernel<<<1, kMaxCols, 0, st>>>(cs.gpops, cs.P, cs.nfrag, cs.target, cs.scale);
+    CU_TRY(cudaGetLastError());
+    return ELHL_OK;
+}
+
+// one GEMM-regime step: replay the step graph of this parity (captured on first use)
+int cheb_gemm_step(ChebState &cs) {
+    cudaStream_t st = g_ctx.stream;
+    cudaGraphExec_t &ge = cs.graph[cs.parity];
+    if (!ge) {
+        cudaGraph_t g = nullptr;
+        CU_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        int rc = cheb_gemm_enqueue(cs, cs.parity);
+        cudaError_t e = cudaStreamEndCapture(st, &g);
+        if (rc) {
+            if (g) cudaGraphDestroy(g);
+            return rc;
+        }
+        CU_TRY(e);
+        e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        CU_TRY(e);
+    }
+    CU_TRY(cudaEventRecord(g_ctx.ev[0], st));
+    CU_TRY(cudaGraphLaunch(ge, st));
+    CU_TRY(cudaEventRecord(g_ctx.ev[1], st));
+    cs.parity ^= 1;
+    return ELHL_OK;
 }
 
 // Launch plan for a set of problems: row segments balanced by matrix elements.
@@ -1068,12 +1213,21 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
         if ((rc = cheb_prepare_readout(cs, tr->fac.L))) return rc;
         if ((rc = cheb_plan(tr->plan, one))) return rc;
     }
-    if (!coords && cs.readout_ready && tr->plan.mg_read) {
-        // ---- fixed nuclei, device read-out: two launches per step, no host sync
+    if (!coords && cs.readout_ready && (tr->plan.mg_read || cs.gemm)) {
+        // ---- fixed nuclei, device read-out: two launches (or one graph) per step, no host sync
         if (!cs.cols_current && (rc = cheb_load_columns(tr))) return rc;
         CU_TRY(cudaEventRecord(g_ctx.ev[2], st));
-        for (int s = 0; s < nsteps; ++s)
+        for (int s = 0; s < nsteps; ++s) {
+            if (cs.gemm) {
+                if ((rc = cheb_gemm_step(cs))) return rc;
+                tr->plan.parity = cs.parity;
+                if (d_pops)
+                    CU_TRY(cudaMemcpyAsync(d_pops + s * pop_per_step, cs.gpops, pop_per_step * sizeof(double),
+                                           cudaMemcpyDeviceToDevice, st));
+                continue;
+            }
             if ((rc = cheb_dev_step(tr->plan, one, d_pops ? d_pops + s * pop_per_step : nullptr))) return rc;
+        }
         CU_TRY(cudaEventRecord(g_ctx.ev[3], st));
         if ((rc = cheb_settle(one))) return rc;
         int err = 0;
@@ -1398,6 +1552,7 @@ int elhl_set_stream(void *stream) {
     g_ctx.stream = stream ? (cudaStream_t)stream : g_ctx.own_stream;
     SOLVER_TRY(cusolverDnSetStream(g_ctx.solver, g_ctx.stream));
     if (cublasSetStream(g_ctx.blas, g_ctx.stream) != CUBLAS_STATUS_SUCCESS) return ELHL_ERR_CUDA;
+    if (cublasSetStream(g_ctx.blas_tc, g_ctx.stream) != CUBLAS_STATUS_SUCCESS) return ELHL_ERR_CUDA;
     return ELHL_OK;
 }
 
@@ -1424,7 +1579,10 @@ void gpu_finalize_(void) {
     dev_free(g_ctx.partials);
     if (g_ctx.solver) cusolverDnDestroy(g_ctx.solver);
     if (g_ctx.blas) cublasDestroy(g_ctx.blas);
-    g_ctx.blas = nullptr;
+    if (g_ctx.blas_tc) cublasDestroy(g_ctx.blas_tc);
+    g_ctx.blas = g_ctx.blas_tc = nullptr;
+    if (g_ctx.tc_ws) cudaFree(g_ctx.tc_ws);
+    g_ctx.tc_ws = nullptr;
     if (g_ctx.own_stream) cudaStreamDestroy(g_ctx.own_stream);
     if (g_ctx.copy_stream) cudaStreamDestroy(g_ctx.copy_stream);
     g_ctx.solver = nullptr;
@@ -1539,6 +1697,14 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
         cs.P = tr->P; cs.nfrag = tr->nfrag; cs.psi_out = tr->psi_ao; cs.bra_out = tr->bra_ao;
         cs.ao_frag = tr->basis.ao_frag; cs.target = tr->target;
         if (!rc) rc = cheb_prepare_readout(cs, tr->fac.L);
+        // GEMM regime: many ket columns in FP32 -> tensor-core GEMMs per order
+        if (!rc && cs.precision == ELHL_PREC_FP32 && cs.m == cs.P && cs.P >= kGemmMinCols) {
+            cs.gemm = true;
+            if (cudaMalloc(&cs.Y, (size_t)cs.ld * cs.m * sizeof(float2)) != cudaSuccess ||
+                cudaMalloc(&cs.Vf, (size_t)cs.ld * cs.m * sizeof(float2)) != cudaSuccess)
+                rc = ELHL_ERR_OOM;
+            if (!rc) rc = dev_alloc(&cs.gpops, (size_t)cs.P * (cs.nfrag + 1));
+        }
         std::vector<ChebState *> one{&tr->cs};
         if (!rc) rc = cheb_plan(tr->plan, one);
     }

@@ -88,3 +88,26 @@ def test_cheb_rejects_bad_config(elhl, flake):
     with pytest.raises(elhl.ElhlError) as e:
         elhl.Trajectory(flake, method=elhl.METHOD_CHEBYSHEV, ncols=3)
     assert e.value.status == elhl.ERR_UNSUPPORTED
+
+
+def test_gemm_regime_fp32_matches_fp64(elhl, oracle_mod):
+    """8 FP32 ket columns run as tensor-core GEMMs per order (CUDA graph per step);
+    populations within 1e-6 of the FP64 path and of the exact propagator."""
+    sysm = systems.cubic_cluster(n_atoms=60, seed=9)
+    states = [30, 35, 38, 40, 41, 44, 47, 52]
+    out = {}
+    for prec in (elhl.PREC_FP64, elhl.PREC_FP32):
+        tr = elhl.Trajectory(sysm, dt=1e-4, method=elhl.METHOD_CHEBYSHEV, precision=prec, ncols=8, nparticles=8,
+                             cheb_tol=1e-14)
+        tr.init_fmo_states(states)
+        out[prec] = tr.step(None, nsteps=4)
+        tr.close()
+    assert np.abs(out[elhl.PREC_FP32] - out[elhl.PREC_FP64]).max() < 1e-6
+    S = oracle_mod.overlap(sysm)
+    h = oracle_mod.huckel(sysm, S)
+    ex = oracle_mod.ExactPropagator(S, h)
+    for c, st in enumerate(states[:3]):
+        ket0, _ = oracle_mod.fragment_mo(sysm, "E", st)
+        ref = oracle_mod.exact_populations(sysm, S, ex.ket(ket0.astype(complex), 4e-4))
+        assert np.abs(out[elhl.PREC_FP64][-1, c] - ref).max() < 1e-10
+        assert np.abs(out[elhl.PREC_FP32][-1, c] - ref).max() < 1e-6
