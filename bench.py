@@ -52,9 +52,9 @@ def workload(name: str):
 
 WORKLOAD_DESC = {
     "ehrenfest": "C/H/O cluster 1200 atoms (60/30/10%), jittered 1.4 A cubic lattice, moving nuclei "
-                 "(sigma 0.02 A per step), dt 0.5 fs, FP64 Taylor (reference semantics), el+hl bra/ket",
-    "flake": "C100H50 honeycomb flake (sigma 0.03 A), fixed nuclei, dt 0.1 fs, FP64 Taylor, el+hl bra/ket",
-    "small": "C/H/O cluster 300 atoms, moving nuclei, dt 0.5 fs, FP64 Taylor",
+                 "(sigma 0.02 A per step), dt 0.5 fs, S, h, Cholesky and L^-1 rebuilt every step, el+hl bra/ket",
+    "flake": "C100H50 honeycomb flake (sigma 0.03 A), fixed nuclei, dt 0.1 fs, el+hl bra/ket",
+    "small": "C/H/O cluster 300 atoms, moving nuclei, dt 0.5 fs, el+hl bra/ket",
 }
 
 
@@ -149,7 +149,7 @@ def run_ours(args, rank, world):
     W, K = args.warmup, args.steps
     coords = step_coords(sysm, moving, W + K + 1, offset=1000 * rank)
     method = api.METHOD_CHEBYSHEV if args.method == "chebyshev" else api.METHOD_TAYLOR_REF
-    prec = {"fp64": api.PREC_FP64, "fp32": api.PREC_FP32}[args.precision]
+    prec = {"fp64": api.PREC_FP64, "fp32": api.PREC_FP32, "bf16x3": api.PREC_BF16X3}[args.precision]
     tr = api.Trajectory(sysm, coords=None if coords is None else coords[0], dt=dt, method=method, precision=prec,
                         ncols=4 if moving else 2, cheb_tol=1e-12)
     tr.init_fmo(homo + 1, homo)
@@ -191,6 +191,7 @@ def run_ours(args, rank, world):
         rebuild_ms += st.rebuild_ms
         orders += st.orders
         launches += st.prop_launches + st.rebuild_count
+    tile = {"tile_cols": st.tile_cols, "phases": st.phases} if method == api.METHOD_CHEBYSHEV else {}
     torch.cuda.synchronize(dev)
     clk = clocks.stop()
     ms = sum(a.elapsed_time(b) for a, b in ev)
@@ -233,13 +234,17 @@ def run_ours(args, rank, world):
         flops_per_launch = per_launch_orders * 8.0 * N * N
     else:
         # dominant kernel: cheb_kernel.  Unit = one Chebyshev order over m complex
-        # columns: Hs read once (b_H N^2) + 5 x 16 N m vector bytes; flops = 4 N^2 m
+        # columns.  Fixed nuclei (explicit Hs): Hs read once (b_H N^2) + 5 x 16 N m
+        # vector bytes, flops 4 N^2 m.  Moving nuclei (implicit G (h/b) G^T, three
+        # phases): N^2/2 + N^2 + N^2/2 matrix elements (b_H 2 N^2) + 9 x 16 N m vector
+        # bytes, flops 8 N^2 m
         kernel = "cheb_kernel"
         m = 4 if moving else 2
         bH = 8.0 if args.precision == "fp64" else 4.0
+        elems, vec = (2.0 * N * N, 144.0) if moving else (1.0 * N * N, 80.0)
         per_launch_orders = orders / max(1, K) / m
-        bytes_per_launch = per_launch_orders * (bH * N * N + 80.0 * N * m)
-        flops_per_launch = per_launch_orders * 4.0 * N * N * m
+        bytes_per_launch = per_launch_orders * (bH * elems + vec * N * m)
+        flops_per_launch = per_launch_orders * 4.0 * elems * m
     achieved_gbs = bytes_per_launch / (prop_launch_ms * 1e-3) / 1e9
     tflops = flops_per_launch / (prop_launch_ms * 1e-3) / 1e12
 
@@ -258,7 +263,7 @@ def run_ours(args, rank, world):
         "data": "synthetic (seeded geometry, no external dataset)",
         "config": {"workload": WORKLOAD_DESC[args.workload], "N_ao": N, "natoms": sysm.natoms,
                    "dt_ps": dt, "particles": 2, "method": args.method, "precision": args.precision,
-                   "moving_nuclei": moving, "l2": "flushed (512 MB write) between timed steps",
+                   "moving_nuclei": moving, "l2": "flushed (512 MB write) between timed steps", **tile,
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "e2e": {"value": replica_value(Ke, world, t_e2e), "unit": "steps/s",
                 "h2d_bytes_per_step": (nc * 8) if moving else 0, "d2h_bytes_per_step": 2 * nf1 * 8},
@@ -272,7 +277,7 @@ def run_ours(args, rank, world):
                              "pipe": "fp64 FMA" if args.precision == "fp64" else "fp32 FMA",
                              "peak_source": "of measured (FMA probe, profiles/gb300_peaks_probe.md)"},
                      "orders_per_launch": per_launch_orders, "launch_ms": prop_launch_ms},
-        "breakdown_ms_per_step": {"propagation": prop_ms / K, "rebuild_S_h_Hprime": rebuild_ms / K},
+        "breakdown_ms_per_step": {"propagation": prop_ms / K, "rebuild_S_h_operator": rebuild_ms / K},
         "clocks": clk,
     }
     return line
@@ -386,7 +391,7 @@ def run_mix(args, ntraj, steps, warm, precision, dropin_sample):
     pmx, elmx, stmx = out[precision]
     res["batched_fp64_steps_per_s"] = ntraj * steps / el64
     res["batched_mixed_steps_per_s"] = ntraj * steps / elmx
-    res["mixed_precision"] = {api.PREC_FP32: "fp32"}.get(precision, "fp64")
+    res["mixed_precision"] = {api.PREC_FP32: "fp32", api.PREC_BF16X3: "bf16x3"}.get(precision, "fp64")
     res["mixed_pop_err_vs_fp64"] = float(np.abs(pmx - p64).max())
     res["kernel_ms_per_step_mixed"] = stmx.prop_ms / steps
     # plain FP64 drop-in on a uniform sample of the same mix
@@ -414,8 +419,9 @@ def run_mix(args, ntraj, steps, warm, precision, dropin_sample):
 def run_precision_study(args, steps=5, ncols=64, nao=8192):
     """Config 3: C/H honeycomb sheet with N = 8192 AOs, 64 complex columns
     (seeded random fragment MOs), fixed nuclei, dt 0.1 fs.  FP32 runs H.Psi as
-    tensor-core GEMMs (FP32-accuracy emulation); FP64 runs the GEMV kernel.
-    Reports steps/s of the 64-column block and the population error per step."""
+    FP32 GEMMs on the FP32 pipes, BF16X3 as tensor-core GEMMs (three BF16 terms
+    per operand); FP64 runs the GEMV kernel.  Reports steps/s of the 64-column
+    block and the population error per step against FP64."""
     import torch
     from dynemol_gb300 import api, systems
     sysm = systems.honeycomb_sheet(nao)
@@ -423,7 +429,8 @@ def run_precision_study(args, steps=5, ncols=64, nao=8192):
     states = (systems.SplitMix64(3).permutation(nf)[:ncols] + 1).tolist()
     res = {"N_ao": sysm.nao, "columns": ncols, "dt_ps": 1e-4, "steps": steps}
     pops = {}
-    for prec, name in ((api.PREC_FP64, "fp64"), (api.PREC_FP32, "fp32_tensor_gemm")):
+    variants = ((api.PREC_FP64, "fp64"), (api.PREC_FP32, "fp32_gemm"), (api.PREC_BF16X3, "bf16x3_tensor_gemm"))
+    for prec, name in variants:
         tr = api.Trajectory(sysm, dt=1e-4, method=api.METHOD_CHEBYSHEV, precision=prec, ncols=ncols,
                             nparticles=ncols, cheb_tol=1e-12)
         tr.init_fmo_states(states)
@@ -437,9 +444,11 @@ def run_precision_study(args, steps=5, ncols=64, nao=8192):
         res[name] = {"steps_per_s": steps / el, "kernel_ms_per_step": st.prop_ms / steps,
                      "orders_per_step": st.orders / steps / ncols}
         tr.close()
-    err = np.abs(pops["fp32_tensor_gemm"] - pops["fp64"]).max(axis=(1, 2))
-    res["pop_err_per_step_fp32_vs_fp64"] = [float(x) for x in err]
-    res["speedup_fp32_tensor_vs_fp64"] = res["fp32_tensor_gemm"]["steps_per_s"] / res["fp64"]["steps_per_s"]
+    for _, name in variants[1:]:
+        err = np.abs(pops[name] - pops["fp64"])
+        res[name]["pop_err_per_step_vs_fp64"] = [float(x) for x in err[:, :, :-1].max(axis=(1, 2))]
+        res[name]["norm_err_per_step_vs_fp64"] = [float(x) for x in err[:, :, -1].max(axis=1)]
+        res[name]["speedup_vs_fp64"] = res[name]["steps_per_s"] / res["fp64"]["steps_per_s"]
     return res
 
 
@@ -497,7 +506,7 @@ def main():
     ap.add_argument("--workload", default="ehrenfest", choices=sorted(WORKLOAD_DESC))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--method", default="chebyshev", choices=["taylor", "chebyshev"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "bf16x3"])
     ap.add_argument("--mix", type=int, default=64, help="also run the batched-vs-drop-in comparison on a mix "
                     "of this many trajectories (0 = skip)")
     ap.add_argument("--no-dropin", action="store_true", help="skip the Taylor drop-in measurement")

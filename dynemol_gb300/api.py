@@ -28,7 +28,8 @@ METHOD_TAYLOR_REF, METHOD_CHEBYSHEV = 0, 1
 PREC_FP64, PREC_FP32, PREC_BF16X3 = 0, 1, 2
 
 EXPORTED_SYMBOLS = (
-    "gpu_init_", "gpu_finalize_", "gpu_pin_", "gpu_unpin_", "propagation_gpucaller_",
+    "gpu_init_", "gpu_finalize_", "gpu_pin_", "gpu_unpin_", "propagation_gpucaller_", "ehrenfestkernel_gpu_",
+    "ehrenfestkernel2_gpu_", "elhl_ehrenfest_forces",
     "propagationelhl_gpucaller_", "elhl_last_status", "elhl_status_string", "elhl_traj_config_default",
     "elhl_traj_create", "elhl_traj_destroy", "elhl_traj_init_fmo", "elhl_traj_init_fmo_states", "elhl_traj_set_psi", "elhl_traj_get_psi", "elhl_traj_step",
     "elhl_traj_step_device", "elhl_traj_energies", "elhl_traj_get_matrices", "elhl_traj_get_stats", "elhl_device_count",
@@ -63,7 +64,8 @@ class TrajStats(ctypes.Structure):
     _fields_ = [("orders", ctypes.c_longlong), ("conv_calls", ctypes.c_longlong), ("substeps", ctypes.c_longlong),
                 ("save_tau", ctypes.c_double * 2), ("t", ctypes.c_double), ("it", ctypes.c_int),
                 ("status", ctypes.c_int), ("prop_ms", ctypes.c_double), ("rebuild_ms", ctypes.c_double),
-                ("prop_launches", ctypes.c_int), ("rebuild_count", ctypes.c_int)]
+                ("prop_launches", ctypes.c_int), ("rebuild_count", ctypes.c_int), ("tile_cols", ctypes.c_int),
+                ("phases", ctypes.c_int)]
 
 
 class Request(ctypes.Structure):
@@ -96,6 +98,12 @@ def load(path: str = LIB_PATH):
     L.propagation_gpucaller_.restype = None
     L.propagationelhl_gpucaller_.argtypes = [ip, vp, vp, vp, vp, vp, vp, vp, dp, dp, dp, dp]
     L.propagationelhl_gpucaller_.restype = None
+    L.ehrenfestkernel_gpu_.argtypes = [ip, vp, vp, vp, vp]
+    L.ehrenfestkernel_gpu_.restype = None
+    L.ehrenfestkernel2_gpu_.argtypes = [ip, vp, vp, vp, vp, vp]
+    L.ehrenfestkernel2_gpu_.restype = None
+    L.elhl_ehrenfest_forces.argtypes = [ctypes.POINTER(BasisDesc), vp, vp, ctypes.c_double, ctypes.c_double, vp]
+    L.elhl_ehrenfest_forces.restype = ci
     L.elhl_last_status.restype = ci
     L.elhl_status_string.argtypes = [ci]
     L.elhl_status_string.restype = ctypes.c_char_p
@@ -207,6 +215,37 @@ def propagation_gpucaller(Hp, psi_bra, psi_ket, t_init, t_max, tau):
                              _p(psi_bra), _p(psi_ket), _p(Hp))
     _check(L.elhl_last_status(), "propagation_gpucaller_")
     return psi_bra, psi_ket, st.value
+
+
+def ehrenfest_kernel(H, X, A=None, bra=None, ket=None) -> np.ndarray:
+    """K = X o A - H A (ehrenfestkernel_gpu_), or with A from bra/ket (N x 2,
+    ehrenfestkernel2_gpu_)."""
+    L = load()
+    N = H.shape[0]
+    H = np.asfortranarray(H, np.float64)
+    X = np.asfortranarray(X, np.float64)
+    K = np.zeros((N, N), order="F")
+    n = ctypes.byref(ctypes.c_int(N))
+    if A is not None:
+        A = np.asfortranarray(A, np.float64)
+        L.ehrenfestkernel_gpu_(n, _p(H), _p(A), _p(X), _p(K))
+    else:
+        b = np.asfortranarray(bra, np.complex128)
+        k = np.asfortranarray(ket, np.complex128)
+        L.ehrenfestkernel2_gpu_(n, _p(b), _p(k), _p(H), _p(X), _p(K))
+    _check(L.elhl_last_status(), "ehrenfestkernel_gpu_")
+    return K
+
+
+def ehrenfest_forces(system, kernel, coords=None, delta: float = 1e-8, cutoff: float = 12.0) -> np.ndarray:
+    """Ehrenfest (Hellmann-Feynman-Pulay) forces, natoms x 3, in N (elhl_ehrenfest_forces)."""
+    L = load()
+    desc, keep = _basis_desc(system)
+    c = np.ascontiguousarray(system.coords if coords is None else coords, np.float64)
+    K = np.asfortranarray(kernel, np.float64)
+    out = np.zeros((system.natoms, 3))
+    _check(L.elhl_ehrenfest_forces(ctypes.byref(desc), _p(c), _p(K), delta, cutoff, _p(out)), "elhl_ehrenfest_forces")
+    return out
 
 
 # ---------------------------------------------------------------- trajectories

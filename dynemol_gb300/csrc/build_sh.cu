@@ -201,29 +201,71 @@ __device__ __forceinline__ double x_ij(double ipi, double ipj, double vi, double
     return keff * c2 * 0.5 + c4;
 }
 
-__global__ void build_sh_kernel(DevBasis b, const double *__restrict__ coords, double cutoff,
-                                double *__restrict__ S, double *__restrict__ h, int ld) {
-    const int ia = blockIdx.y * blockDim.y + threadIdx.y;
-    const int ib = blockIdx.x * blockDim.x + threadIdx.x;
-    if (ia >= b.natoms || ib >= b.natoms || ib > ia) return;
+// Shells of one atom: runs of consecutive AOs with the same n, l, zetas and
+// coefficients (the m components of one radial function).  The lined-up
+// overlaps depend on the shells only, so they are computed once per shell pair
+// and the rotation is applied per AO pair.
+constexpr int kMaxShell = 4;
+
+__device__ bool same_radial(const DevBasis &b, int x, int y) {
+    return b.ao_n[x] == b.ao_n[y] && b.ao_l[x] == b.ao_l[y] && b.ao_nzeta[x] == b.ao_nzeta[y] &&
+           b.ao_zeta[2 * x] == b.ao_zeta[2 * y] && b.ao_zeta[2 * x + 1] == b.ao_zeta[2 * y + 1] &&
+           b.ao_coef[2 * x] == b.ao_coef[2 * y] && b.ao_coef[2 * x + 1] == b.ao_coef[2 * y + 1];
+}
+
+// shell index of every AO of an atom (ao0, nao); returns the shell count, or
+// -1 when the atom has more than kMaxShell shells.  first[s] = first AO of shell s.
+__device__ int atom_shells(const DevBasis &b, int ao0, int nao, int *first, int *shell_of) {
+    int ns = 0;
+    for (int j = 0; j < nao; ++j) {
+        if (j == 0 || !same_radial(b, ao0 + j, ao0 + j - 1)) {
+            if (ns == kMaxShell) return -1;
+            first[ns++] = ao0 + j;
+        }
+        shell_of[j] = ns - 1;
+    }
+    return ns;
+}
+
+// normalised, contracted lined-up overlaps <aa|bb>_m, m = 0..min(la, lb)
+// (the SOLAP + GET_ANOR part of BUILD_OVERLAP_MATRIX, overlap_D.f:228-280)
+__device__ void contracted_overlap(const DevBasis &b, int aa, int bb, double R, double *solnorm) {
+    const int na = b.ao_n[aa], la = b.ao_l[aa];
+    const int nb = b.ao_n[bb], lb = b.ao_l[bb];
+    const double aux = 1.0 / (dfact(na + na) * dfact(nb + nb));
+    const int msup = min(la, lb);
+    solnorm[0] = solnorm[1] = 0.0;
+    for (int j = 0; j < b.ao_nzeta[bb]; ++j) {
+        for (int i = 0; i < b.ao_nzeta[aa]; ++i) {
+            const double eb = b.ao_zeta[2 * bb + j], ea = b.ao_zeta[2 * aa + i];
+            double sol[kMaxL + 1];
+            if (!lined_up_overlap(na, la, ea, nb, lb, eb, R, sol)) {
+                sol[0] = sol[1] = __longlong_as_double(0x7ff8000000000000ULL);  // NaN marks unsupported
+            }
+            double an = anor(ea, eb, na, nb, la, lb, aux);
+            double part[kMaxL + 1];
+            for (int m = 0; m <= msup - 1; ++m) {
+                part[m] = sol[m] * an;
+                an = an / sqrt((la + m + 1.0) * (la - m) * (lb + m + 1.0) * (lb - m));
+                if (m == 0) an = an + an;
+            }
+            part[msup] = sol[msup] * an;
+            const double cc = b.ao_coef[2 * aa + i] * b.ao_coef[2 * bb + j];
+            for (int k = 0; k <= msup; ++k) solnorm[k] = solnorm[k] + cc * part[k];
+        }
+    }
+}
+
+// S block of atoms ia != ib for B - A = (xab, yab, zab) (Angstrom): calls
+// out(ja, jb, s) for every AO pair (a0 + ja of ia, b0 + jb of ib); s = 0 beyond
+// the cutoff.  ROTATIONOVERLAP (overlap_D.f:520-583, l <= 1), SOLAP + GET_ANOR
+// once per shell pair, rotation to the molecular frame per AO pair
+// (BUILD_OVERLAP_MATRIX, overlap_D.f:228-291).
+template <typename Out>
+__device__ void pair_overlap_block(const DevBasis &b, int ia, int ib, double xab, double yab, double zab,
+                                   double cutoff, Out &&out) {
     const int a0 = b.atom_ao0[ia], na_ao = b.atom_nao[ia];
     const int b0 = b.atom_ao0[ib], nb_ao = b.atom_nao[ib];
-
-    if (ia == ib) {  // diagonal block: S = 1, h = IP + V_shift; same-atom off-diagonals 0
-        for (int jb = 0; jb < nb_ao; ++jb)
-            for (int ja = 0; ja < na_ao; ++ja) {
-                const int r = a0 + ja, c = b0 + jb;
-                const size_t o = (size_t)c * ld + r;
-                S[o] = (r == c) ? 1.0 : 0.0;
-                h[o] = (r == c) ? b.ao_ip[r] + b.ao_vshift[r] : 0.0;
-            }
-        return;
-    }
-
-    // B - A vector, lined-up frame (ROTATIONOVERLAP, overlap_D.f:558-574)
-    const double xab = coords[3 * ib] - coords[3 * ia];
-    const double yab = coords[3 * ib + 1] - coords[3 * ia + 1];
-    const double zab = coords[3 * ib + 2] - coords[3 * ia + 2];
     const double xy = sqrt(xab * xab + yab * yab);
     double sinal = 0.0, cosal = 1.0;
     if (xy > 1.0e-10) {
@@ -255,35 +297,31 @@ __global__ void build_sh_kernel(DevBasis b, const double *__restrict__ coords, d
         rot[1][0][0] = d11 * cosal + d1m * cosal;
     }
 
+    // lined-up overlaps once per shell pair (per AO pair when an atom has more shells)
+    int fa[kMaxShell], fb[kMaxShell], sha[16], shb[16];
+    const int nsa = (inside && na_ao <= 16) ? atom_shells(b, a0, na_ao, fa, sha) : -1;
+    const int nsb = (inside && nb_ao <= 16) ? atom_shells(b, b0, nb_ao, fb, shb) : -1;
+    const bool shells = nsa > 0 && nsb > 0;
+    double sn[kMaxShell][kMaxShell][kMaxL + 1];
+    if (shells)
+        for (int q = 0; q < nsb; ++q)
+            for (int p = 0; p < nsa; ++p) contracted_overlap(b, fa[p], fb[q], R, sn[p][q]);
+
     for (int jb = 0; jb < nb_ao; ++jb) {
         const int bb = b0 + jb;
         for (int ja = 0; ja < na_ao; ++ja) {
             const int aa = a0 + ja;
             double s = 0.0;
             if (inside) {
-                const int na = b.ao_n[aa], la = b.ao_l[aa], ma = b.ao_m[aa];
-                const int nb = b.ao_n[bb], lb = b.ao_l[bb], mb = b.ao_m[bb];
-                const double aux = 1.0 / (dfact(na + na) * dfact(nb + nb));
+                const int la = b.ao_l[aa], ma = b.ao_m[aa];
+                const int lb = b.ao_l[bb], mb = b.ao_m[bb];
                 const int msup = min(la, lb);
-                double solnorm[kMaxL + 1] = {0.0, 0.0};
-                for (int j = 0; j < b.ao_nzeta[bb]; ++j) {
-                    for (int i = 0; i < b.ao_nzeta[aa]; ++i) {
-                        const double eb = b.ao_zeta[2 * bb + j], ea = b.ao_zeta[2 * aa + i];
-                        double sol[kMaxL + 1];
-                        if (!lined_up_overlap(na, la, ea, nb, lb, eb, R, sol)) {
-                            sol[0] = sol[1] = __longlong_as_double(0x7ff8000000000000ULL);  // NaN marks unsupported
-                        }
-                        double an = anor(ea, eb, na, nb, la, lb, aux);
-                        double part[kMaxL + 1];
-                        for (int m = 0; m <= msup - 1; ++m) {
-                            part[m] = sol[m] * an;
-                            an = an / sqrt((la + m + 1.0) * (la - m) * (lb + m + 1.0) * (lb - m));
-                            if (m == 0) an = an + an;
-                        }
-                        part[msup] = sol[msup] * an;
-                        const double cc = b.ao_coef[2 * aa + i] * b.ao_coef[2 * bb + j];
-                        for (int k = 0; k <= msup; ++k) solnorm[k] = solnorm[k] + cc * part[k];
-                    }
+                double solnorm[kMaxL + 1];
+                if (shells) {
+                    solnorm[0] = sn[sha[ja]][shb[jb]][0];
+                    solnorm[1] = sn[sha[ja]][shb[jb]][1];
+                } else {
+                    contracted_overlap(b, aa, bb, R, solnorm);
                 }
                 double sux0 = solnorm[0] * rot[la][ma + 1][1] * rot[lb][mb + 1][1];
                 s = sux0;
@@ -293,14 +331,97 @@ __global__ void build_sh_kernel(DevBasis b, const double *__restrict__ coords, d
                     s = s + sux1;
                 }
             }
-            const double hv = x_ij(b.ao_ip[aa], b.ao_ip[bb], b.ao_vshift[aa], b.ao_vshift[bb], b.ao_kwh[aa],
-                                   b.ao_kwh[bb]) * s;
-            S[(size_t)bb * ld + aa] = s;
-            S[(size_t)aa * ld + bb] = s;
-            h[(size_t)bb * ld + aa] = hv;
-            h[(size_t)aa * ld + bb] = hv;
+            out(ja, jb, s);
         }
     }
+}
+
+__global__ void build_sh_kernel(DevBasis b, const double *__restrict__ coords, double cutoff,
+                                double *__restrict__ S, double *__restrict__ h, int ld) {
+    const int ia = blockIdx.y * blockDim.y + threadIdx.y;
+    const int ib = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ia >= b.natoms || ib >= b.natoms || ib > ia) return;
+    const int a0 = b.atom_ao0[ia], na_ao = b.atom_nao[ia];
+    const int b0 = b.atom_ao0[ib], nb_ao = b.atom_nao[ib];
+
+    if (ia == ib) {  // diagonal block: S = 1, h = IP + V_shift; same-atom off-diagonals 0
+        for (int jb = 0; jb < nb_ao; ++jb)
+            for (int ja = 0; ja < na_ao; ++ja) {
+                const int r = a0 + ja, c = b0 + jb;
+                const size_t o = (size_t)c * ld + r;
+                S[o] = (r == c) ? 1.0 : 0.0;
+                h[o] = (r == c) ? b.ao_ip[r] + b.ao_vshift[r] : 0.0;
+            }
+        return;
+    }
+    // B - A vector, lined-up frame (ROTATIONOVERLAP, overlap_D.f:558-574)
+    const double xab = coords[3 * ib] - coords[3 * ia];
+    const double yab = coords[3 * ib + 1] - coords[3 * ia + 1];
+    const double zab = coords[3 * ib + 2] - coords[3 * ia + 2];
+    pair_overlap_block(b, ia, ib, xab, yab, zab, cutoff, [&](int ja, int jb, double s) {
+        const int aa = a0 + ja, bb = b0 + jb;
+        const double hv = x_ij(b.ao_ip[aa], b.ao_ip[bb], b.ao_vshift[aa], b.ao_vshift[bb], b.ao_kwh[aa],
+                               b.ao_kwh[bb]) * s;
+        S[(size_t)bb * ld + aa] = s;
+        S[(size_t)aa * ld + bb] = s;
+        h[(size_t)bb * ld + aa] = hv;
+        h[(size_t)aa * ld + bb] = hv;
+    });
+}
+
+// Pulay (overlap-derivative) force terms of the Ehrenfest force
+// (Ehrenfest, diabatic-Ehren.f:163-230): for every atom pair K < L with
+// R_KL < cutoff and every direction, dS(j in L, i in K)/dR_K by central
+// differences of the S block rebuilt with atom K displaced by +-delta
+// (PULAY_OVERLAP, overlap_D.f:314-463), and
+//   F[K][L][xyz] = -sum_{j in L} sum_{i in K} dS_ji/dR_K Kernel(i, j)
+// (Kernel column-major, ld = ldk).  One thread per (L, K) pair; F is natoms x
+// natoms x 3, written for K < L only.
+constexpr int kMaxAoAtom = 16;
+
+__global__ void pulay_pairs_kernel(DevBasis b, const double *__restrict__ coords, double cutoff, double delta,
+                                   const double *__restrict__ kernel, int ldk, double *__restrict__ F) {
+    const int L = blockIdx.y * blockDim.y + threadIdx.y;  // ia in PULAY_OVERLAP
+    const int K = blockIdx.x * blockDim.x + threadIdx.x;  // the displaced site, ib
+    if (L >= b.natoms || K >= L) return;
+    const int nat = b.natoms;
+    const double dx = coords[3 * K] - coords[3 * L], dy = coords[3 * K + 1] - coords[3 * L + 1],
+                 dz = coords[3 * K + 2] - coords[3 * L + 2];
+    const double R = sqrt(dx * dx + dy * dy + dz * dz);
+    double f[3] = {0.0, 0.0, 0.0};
+    const int a0 = b.atom_ao0[L], na = b.atom_nao[L], b0 = b.atom_ao0[K], nb = b.atom_nao[K];
+    if (R < cutoff && na <= kMaxAoAtom && nb <= kMaxAoAtom) {
+        double fwd[kMaxAoAtom * kMaxAoAtom];
+        for (int xyz = 0; xyz < 3; ++xyz) {
+            double pk[3] = {coords[3 * K], coords[3 * K + 1], coords[3 * K + 2]};
+            pk[xyz] = coords[3 * K + xyz] + delta;
+            pair_overlap_block(b, L, K, pk[0] - coords[3 * L], pk[1] - coords[3 * L + 1], pk[2] - coords[3 * L + 2],
+                               cutoff, [&](int ja, int jb, double s) { fwd[ja * kMaxAoAtom + jb] = s; });
+            pk[xyz] = coords[3 * K + xyz] - delta;
+            double acc = 0.0;
+            pair_overlap_block(b, L, K, pk[0] - coords[3 * L], pk[1] - coords[3 * L + 1], pk[2] - coords[3 * L + 2],
+                               cutoff, [&](int ja, int jb, double s) {
+                                   const double g = (fwd[ja * kMaxAoAtom + jb] - s) / (2.0 * delta);
+                                   acc = acc - g * kernel[(size_t)(a0 + ja) * ldk + (b0 + jb)];
+                               });
+            f[xyz] = acc;
+        }
+    }
+    for (int xyz = 0; xyz < 3; ++xyz) F[((size_t)K * nat + L) * 3 + xyz] = f[xyz];
+}
+
+// force(a)[xyz] = scale * (sum_{L > a} F[a][L] - sum_{K < a} F[K][a]), fixed order
+// (the atom(i)%Ehrenfest sum over F_snd, diabatic-Ehren.f:140-148 with 216-223)
+__global__ void pulay_reduce_kernel(const double *__restrict__ F, int nat, double scale, double *__restrict__ force) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * nat) return;
+    const int a = t / 3, xyz = t % 3;
+    double s = 0.0;
+    for (int q = 0; q < nat; ++q) {
+        if (q > a) s = s + F[((size_t)a * nat + q) * 3 + xyz];
+        else if (q < a) s = s - F[((size_t)q * nat + a) * 3 + xyz];
+    }
+    force[t] = scale * s;
 }
 
 }  // namespace
@@ -310,6 +431,17 @@ cudaError_t init_build_tables() {
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     return e;
+}
+
+cudaError_t launch_pulay_forces(const DevBasis &b, const double *d_coords, double cutoff, double delta,
+                                const double *d_kernel, int ldk, double *d_F, double scale, double *d_force,
+                                cudaStream_t st) {
+    if (b.natoms <= 0) return cudaSuccess;
+    dim3 block(16, 8);
+    dim3 grid((b.natoms + block.x - 1) / block.x, (b.natoms + block.y - 1) / block.y);
+    pulay_pairs_kernel<<<grid, block, 0, st>>>(b, d_coords, cutoff, delta, d_kernel, ldk, d_F);
+    pulay_reduce_kernel<<<(3 * b.natoms + 127) / 128, 128, 0, st>>>(d_F, b.natoms, scale, d_force);
+    return cudaGetLastError();
 }
 
 cudaError_t launch_build_sh(const DevBasis &b, const double *d_coords, double cutoff, double *d_S,

@@ -32,16 +32,27 @@ template <> struct Vec2<float> { using type = float2; };
 
 constexpr int kBlock = 512;
 constexpr int kWarps = kBlock / 32;
-constexpr int kRT = 8;  // rows per warp tile
+// rows per warp tile: FP32 reuses each staged x over 8 rows (shared-memory
+// bandwidth); FP64 is bound by its FMA pipe, so 2-row tiles keep the per-CTA
+// row counts (about N / 152) from wasting FMAs on partial tiles
+template <typename T> struct RowTile;
+template <> struct RowTile<double> { static constexpr int value = 2; };
+template <> struct RowTile<float> { static constexpr int value = 8; };
 
 __device__ __forceinline__ double2 ldcg2(const double2 *p) { return __ldcg(p); }
 __device__ __forceinline__ float2 ldcg2(const float2 *p) { return __ldcg(p); }
 
-// Transposed butterfly: v[0..31] per lane -> lane l returns the warp sum of v[l].
-template <typename T>
-__device__ __forceinline__ T transpose_reduce32(T (&v)[32], int lane) {
+// Warp sums of NV values (NV = 4 ... 32) per lane: plain butterflies over the
+// lane bits >= log2(NV), then a transposed butterfly over the low bits; lane l
+// returns the warp sum of v[l % NV].
+template <typename T, int NV>
+__device__ __forceinline__ T warp_sums(T (&v)[NV], int lane) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+    for (int o = 16; o >= NV; o >>= 1)
+#pragma unroll
+        for (int i = 0; i < NV; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+#pragma unroll
+    for (int o = NV / 2; o > 0; o >>= 1) {
         const bool upper = (lane & o) != 0;
 #pragma unroll
         for (int i = 0; i < o; ++i) {
@@ -56,52 +67,91 @@ __device__ __forceinline__ T transpose_reduce32(T (&v)[32], int lane) {
 // y_i = sum_j M(j, i) x_j for the rows [row0, row1) of one segment, MG complex
 // columns x staged in shared memory (s_v[j*MG + c]); M is column-major with
 // leading dimension ld (column i = row i of M^T).  Calls epi(i, c, yr, yi).
-template <typename T, int MG, typename Epi>
+// TRI = 0: full columns; 1: column i is zero above row i (M = L^-1, j >= i);
+// 2: column i is zero below row i (M = L^T or L^-T, j <= i).  The j range of a
+// super-tile is cut to its non-zero part (widened to multiples of 32; the
+// stored zeros inside it are read as they are).  Rows past row1 in a warp's
+// 8-row tile issue no loads and no FMAs.
+template <typename T, int MG, int TRI, typename Epi>
 __device__ void rows_gemv(const T *M, int ld, const typename Vec2<T>::type *s_v, int row0, int row1, T *s_part,
                           Epi &epi) {
     using T2 = typename Vec2<T>::type;
-    constexpr int NV = kRT * MG * 2;  // accumulators per lane (16, 32 or 64)
-    constexpr int NB = (NV + 31) / 32;
+    constexpr int kRT = RowTile<T>::value;
+    constexpr int NV = kRT * MG * 2;   // accumulators per lane (4 ... 64)
+    constexpr int NW = NV < 32 ? NV : 32;
+    constexpr int NB = NV / NW;        // warp-sum batches
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int rows = row1 - row0;
     int WR = 1;
     while (WR < kWarps && WR * kRT < rows) WR <<= 1;
     const int WJ = kWarps / WR;
     const int wr = warp / WJ, wj = warp % WJ;
-    const int jchunk = ((ld + WJ - 1) / WJ + 31) / 32 * 32;
-    const int j0 = wj * jchunk, j1 = min(ld, j0 + jchunk);
     for (int base = row0; base < row1; base += kRT * WR) {
+        const int tile_end = min(row1, base + kRT * WR);
+        const int jlo = TRI == 1 ? (base & ~31) : 0;
+        const int jhi = TRI == 2 ? min(ld, (tile_end + 31) & ~31) : ld;
+        const int jchunk = ((jhi - jlo + WJ - 1) / WJ + 31) / 32 * 32;
+        const int j0 = jlo + wj * jchunk, j1 = min(jhi, j0 + jchunk);
         const int r0 = base + kRT * wr;
-        T acc[NB * 32];
+        const int nr = min(kRT, row1 - r0);  // rows of this warp's tile (<= 0: none)
+        T acc[NV];
 #pragma unroll
-        for (int q = 0; q < NB * 32; ++q) acc[q] = T(0);
+        for (int q = 0; q < NV; ++q) acc[q] = T(0);
         const T *cols[kRT];
 #pragma unroll
         for (int r = 0; r < kRT; ++r) cols[r] = M + (size_t)min(r0 + r, row1 - 1) * ld;
-        const bool full = (r0 + kRT <= row1);
-        for (int j = j0 + lane; j < j1; j += 32) {
+        // two j positions per iteration: the 2 x kRT column loads are issued before
+        // the FMAs that consume them (more L2 requests in flight per warp)
+        int j = j0 + lane;
+        for (; j + 32 < j1; j += 64) {
+            T h0[kRT], h1[kRT];
+#pragma unroll
+            for (int r = 0; r < kRT; ++r) {
+                h0[r] = r < nr ? cols[r][j] : T(0);
+                h1[r] = r < nr ? cols[r][j + 32] : T(0);
+            }
+#pragma unroll
+            for (int u = 0; u < 2; ++u) {
+                T2 x[MG];
+#pragma unroll
+                for (int c = 0; c < MG; ++c) x[c] = s_v[(j + 32 * u) * MG + c];
+#pragma unroll
+                for (int r = 0; r < kRT; ++r) {
+                    if (r < nr) {  // warp-uniform
+                        const T h = u ? h1[r] : h0[r];
+#pragma unroll
+                        for (int c = 0; c < MG; ++c) {
+                            acc[(r * MG + c) * 2 + 0] = fma(h, x[c].x, acc[(r * MG + c) * 2 + 0]);
+                            acc[(r * MG + c) * 2 + 1] = fma(h, x[c].y, acc[(r * MG + c) * 2 + 1]);
+                        }
+                    }
+                }
+            }
+        }
+        for (; j < j1; j += 32) {
             T2 x[MG];
 #pragma unroll
             for (int c = 0; c < MG; ++c) x[c] = s_v[j * MG + c];
 #pragma unroll
             for (int r = 0; r < kRT; ++r) {
-                const T h = (full || r0 + r < row1) ? cols[r][j] : T(0);
+                if (r < nr) {
+                    const T h = cols[r][j];
 #pragma unroll
-                for (int c = 0; c < MG; ++c) {
-                    acc[(r * MG + c) * 2 + 0] = fma(h, x[c].x, acc[(r * MG + c) * 2 + 0]);
-                    acc[(r * MG + c) * 2 + 1] = fma(h, x[c].y, acc[(r * MG + c) * 2 + 1]);
+                    for (int c = 0; c < MG; ++c) {
+                        acc[(r * MG + c) * 2 + 0] = fma(h, x[c].x, acc[(r * MG + c) * 2 + 0]);
+                        acc[(r * MG + c) * 2 + 1] = fma(h, x[c].y, acc[(r * MG + c) * 2 + 1]);
+                    }
                 }
             }
         }
         // warp sums -> shared memory, layout s_part[wj][wr][NV]
 #pragma unroll
         for (int b = 0; b < NB; ++b) {
-            T tmp[32];
+            T tmp[NW];
 #pragma unroll
-            for (int q = 0; q < 32; ++q) tmp[q] = acc[b * 32 + q];
-            const T sm = transpose_reduce32(tmp, lane);
-            const int idx = b * 32 + lane;
-            if (idx < NV) s_part[((size_t)wj * WR + wr) * NV + idx] = sm;
+            for (int q = 0; q < NW; ++q) tmp[q] = acc[b * NW + q];
+            const T sm = warp_sums<T, NW>(tmp, lane);
+            if (lane < NW) s_part[((size_t)wj * WR + wr) * NV + b * NW + lane] = sm;
         }
         __syncthreads();
         // epilogue: one thread per (row, column) of the super-tile, fixed-order sum over j slices
@@ -130,7 +180,14 @@ struct OrderEpi {
     double2 *acc;
     int k, m, g;
     double cre, cim;
+    const T2 *vprev1;  // implicit operator: y -= shift v_{k-1}; nullptr for an explicit Hs
+    T shift;
     __device__ void operator()(int i, int c, T yr, T yi) {
+        if (vprev1) {
+            const T2 p = ldcg2(vprev1 + (size_t)i * MG + c);
+            yr -= shift * p.x;
+            yi -= shift * p.y;
+        }
         T2 v;
         if (k == 1) {
             v.x = yr;
@@ -165,8 +222,55 @@ __device__ void order_rows(const ChebProblem &pb, const ChebSegment &sg, int k, 
     for (int q = tid; q < ld * MG; q += kBlock) s_v[q] = ldcg2(vprev + q);  // padding rows are zero
     __syncthreads();
     OrderEpi<T, MG> epi{vbuf + (size_t)((k + 1) % 3) * bstride + g * gstride,
-                        vbuf + (size_t)(k % 3) * bstride + g * gstride, pb.col[parity ^ 1], k, m, g, cre, cim};
-    rows_gemv<T, MG>(reinterpret_cast<const T *>(pb.H), ld, s_v, sg.row0, sg.row1, s_part, epi);
+                        vbuf + (size_t)(k % 3) * bstride + g * gstride,
+                        pb.col[parity ^ 1], k, m, g, cre, cim, nullptr, T(0)};
+    rows_gemv<T, MG, 0>(reinterpret_cast<const T *>(pb.H), ld, s_v, sg.row0, sg.row1, s_part, epi);
+}
+
+template <typename T, int MG>
+struct StoreEpi {
+    typename Vec2<T>::type *dst;  // one column group [ldv][MG]
+    __device__ void operator()(int i, int c, T yr, T yi) {
+        typename Vec2<T>::type v;
+        v.x = yr;
+        v.y = yi;
+        dst[(size_t)i * MG + c] = v;
+    }
+};
+
+// Phase ph of order k >= 1 of an implicit problem, column group g, over the
+// CTA's segments [s0, s1): 0: w = G^T v_{k-1};  1: y = (h/b) w;
+// 2: v_k from G y - shift v_{k-1} (recurrence + accumulation).  The staged
+// vector is shared by all of the CTA's segments.
+template <typename T, int MG>
+__device__ void implicit_phase(const ChebLaunch &L, const ChebProblem &pb, int s0, int s1, int k, int ph, int g,
+                               typename Vec2<T>::type *s_v, T *s_part, double cre, double cim) {
+    using T2 = typename Vec2<T>::type;
+    const int ld = pb.ld, m = pb.m;
+    T2 *vbuf = reinterpret_cast<T2 *>(pb.vbuf);
+    T2 *wb = reinterpret_cast<T2 *>(pb.wb);
+    const size_t gstride = (size_t)pb.ldv * MG;
+    const size_t bstride = gstride * (m / MG);
+    const T2 *vprev = vbuf + (size_t)((k + 2) % 3) * bstride + g * gstride;  // v_{k-1}
+    const T2 *src = ph == 0 ? vprev : wb + (size_t)(ph - 1) * bstride + g * gstride;
+    __syncthreads();
+    for (int q = threadIdx.x; q < ld * MG; q += kBlock) s_v[q] = ldcg2(src + q);  // padding rows are zero
+    __syncthreads();
+    for (int s = s0; s < s1; ++s) {
+        const ChebSegment sg = L.segs[s];
+        if (ph == 0) {
+            StoreEpi<T, MG> epi{wb + g * gstride};
+            rows_gemv<T, MG, 1>(reinterpret_cast<const T *>(pb.G), ld, s_v, sg.row0, sg.row1, s_part, epi);
+        } else if (ph == 1) {
+            StoreEpi<T, MG> epi{wb + bstride + g * gstride};
+            rows_gemv<T, MG, 0>(reinterpret_cast<const T *>(pb.H), ld, s_v, sg.row0, sg.row1, s_part, epi);
+        } else {
+            OrderEpi<T, MG> epi{vbuf + (size_t)((k + 1) % 3) * bstride + g * gstride,
+                                vbuf + (size_t)(k % 3) * bstride + g * gstride,
+                                pb.col[L.parity ^ 1], k, m, g, cre, cim, vprev, (T)pb.shift};
+            rows_gemv<T, MG, 2>(reinterpret_cast<const T *>(pb.Gt), ld, s_v, sg.row0, sg.row1, s_part, epi);
+        }
+    }
 }
 
 // order 0: v_0 = s phi (rounded to T), acc = c_0 s phi (FP64); s = renormalisation factor
@@ -206,19 +310,33 @@ __global__ void __launch_bounds__(kBlock, 1) cheb_kernel(ChebLaunch L) {
     const int G = gridDim.x;
     const int s0 = L.seg_begin[blockIdx.x], s1 = L.seg_begin[blockIdx.x + 1];
     for (int k = 0; k <= L.kmax; ++k) {
-        for (int s = s0; s < s1; ++s) {
-            const ChebSegment sg = L.segs[s];
-            const ChebProblem &pb = L.probs[sg.prob];
-            if (k > pb.K) continue;
-            if (k == 0) {
-                order_zero<T, MG>(pb, sg, L.parity);
+        const int nph = k == 0 ? 1 : L.nphase;
+        for (int ph = 0; ph < nph; ++ph) {
+            if (L.nphase == 3) {  // one implicit problem
+                const ChebProblem &pb = L.probs[0];
+                if (k == 0) {
+                    for (int s = s0; s < s1; ++s) order_zero<T, MG>(pb, L.segs[s], L.parity);
+                } else if (k <= pb.K && s0 < s1) {
+                    const double cre = pb.coef[k].x, cim = pb.coef[k].y;
+                    for (int g = 0; g < pb.m / MG; ++g)
+                        implicit_phase<T, MG>(L, pb, s0, s1, k, ph, g, s_v, s_part, cre, cim);
+                }
             } else {
-                const double cre = pb.coef[k].x, cim = pb.coef[k].y;
-                for (int g = 0; g < pb.m / MG; ++g)
-                    order_rows<T, MG>(pb, sg, k, g, L.parity, s_v, s_part, cre, cim);
+                for (int s = s0; s < s1; ++s) {
+                    const ChebSegment sg = L.segs[s];
+                    const ChebProblem &pb = L.probs[sg.prob];
+                    if (k > pb.K) continue;
+                    if (k == 0) {
+                        order_zero<T, MG>(pb, sg, L.parity);
+                    } else {
+                        const double cre = pb.coef[k].x, cim = pb.coef[k].y;
+                        for (int g = 0; g < pb.m / MG; ++g)
+                            order_rows<T, MG>(pb, sg, k, g, L.parity, s_v, s_part, cre, cim);
+                    }
+                }
             }
+            if (!grid_barrier(L.bar_count, L.bar_gen, G, L.error)) return;
         }
-        if (!grid_barrier(L.bar_count, L.bar_gen, G, L.error)) return;
     }
 }
 
@@ -263,7 +381,10 @@ __global__ void __launch_bounds__(kBlock, 1) readout_kernel(ChebLaunch L) {
                 }
                 __syncthreads();
                 ReadEpi<T, MG> epi{out, P, g * MG};
-                rows_gemv<T, MG>(M, ld, s_v, sg.row0, sg.row1, s_part, epi);
+                if (pass == 0)
+                    rows_gemv<T, MG, 1>(M, ld, s_v, sg.row0, sg.row1, s_part, epi);  // A = L^-1: j >= i
+                else
+                    rows_gemv<T, MG, 2>(M, ld, s_v, sg.row0, sg.row1, s_part, epi);  // B = L^T: j <= i
             }
         }
         __syncthreads();
@@ -347,6 +468,7 @@ cudaError_t launch_readout(const ChebLaunch &L, int nprob, int precision, int mg
         switch (mg) {
             case 1: return launch_readout_t<double, 1>(L, nprob, st);
             case 2: return launch_readout_t<double, 2>(L, nprob, st);
+            case 4: return launch_readout_t<double, 4>(L, nprob, st);
         }
     } else {
         switch (mg) {
@@ -361,12 +483,10 @@ cudaError_t launch_readout(const ChebLaunch &L, int nprob, int precision, int mg
 int cheb_block() { return kBlock; }
 
 int cheb_group_size(int precision, int m, int max_ld) {
-    // FP64 keeps at most 2 staged columns per pass (4 would spill at 128 registers / thread)
-    const bool fp64 = precision == ELHL_PREC_FP64;
-    const size_t c2 = fp64 ? sizeof(double2) : sizeof(float2);
+    // the largest of 4, 2, 1 staged columns that divides m and fits in shared memory
+    const size_t c2 = precision == ELHL_PREC_FP64 ? sizeof(double2) : sizeof(float2);
     for (int mg : {4, 2, 1})
-        if (!(fp64 && mg > 2) && m % mg == 0 && kCheb_part_bytes + (size_t)max_ld * mg * c2 <= kCheb_smem_limit)
-            return mg;
+        if (m % mg == 0 && kCheb_part_bytes + (size_t)max_ld * mg * c2 <= kCheb_smem_limit) return mg;
     return 0;
 }
 

@@ -13,7 +13,9 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <vector>
 
 #include "elhl_internal.cuh"
@@ -23,7 +25,11 @@ using namespace elhl;
 namespace {
 
 thread_local int g_last_status = ELHL_OK;
-constexpr int kGemmMinCols = 8;  // complex columns from which H.Psi runs as a tensor-core GEMM
+constexpr int kGemmMinCols = 16;  // ket columns (one per particle) from which H.Psi runs as one GEMM per order
+#ifndef ELHL_GEMM_MIN_N
+#define ELHL_GEMM_MIN_N 2048
+#endif
+constexpr int kGemmMinN = ELHL_GEMM_MIN_N;  // ... on a basis at least this large (smaller ones stay on the row kernel)
 
 #define CU_TRY(expr)                                                                  \
     do {                                                                              \
@@ -529,7 +535,16 @@ struct ChebState {
     int coef_cap = 0;
     double emin = 0.0, emax = 0.0, a = 0.0, b = 1.0;
     double2 c0{1.0, 0.0};    // host copy of the order-0 coefficient
-    double *lz = nullptr;    // Lanczos vectors [3][ld]
+    double *lz = nullptr;    // Lanczos vectors [4][ld]
+    // implicit operator (geometry changing every step): Ht holds G = L^-1 in FP64,
+    // Hs = h/b, A = G and Gt = G^T in the launch precision; no H~ is formed
+    bool implicit = false;
+    void *Gt = nullptr;
+    void *wb = nullptr;      // [2][ld][m] launch precision (phase intermediates)
+    void *tri_ws = nullptr;  // trtri device workspace
+    size_t tri_dev = 0, tri_host = 0;
+    std::vector<unsigned char> tri_hbuf;
+    int *tinfo = nullptr;
     int alloc(int N_, int m_, int prec) {
         N = N_;
         ld = round_up(N, 32);
@@ -544,7 +559,7 @@ struct ChebState {
         if (int rc = dev_alloc(&acc, (size_t)ld * m)) return rc;
         CU_TRY(cudaMemset(phi, 0, (size_t)ld * m * sizeof(double2)));
         CU_TRY(cudaMemset(acc, 0, (size_t)ld * m * sizeof(double2)));
-        if (int rc = dev_alloc(&lz, (size_t)3 * ld)) return rc;
+        if (int rc = dev_alloc(&lz, (size_t)4 * ld)) return rc;
         if (int rc = dev_alloc(&scale, (size_t)kMaxCols)) return rc;
         std::vector<double> ones(kMaxCols, 1.0);
         CU_TRY(cudaMemcpy(scale, ones.data(), kMaxCols * sizeof(double), cudaMemcpyHostToDevice));
@@ -558,6 +573,13 @@ struct ChebState {
         if (Y) cudaFree(Y);
         if (Vf) cudaFree(Vf);
         Y = Vf = nullptr;
+        if (Gt) cudaFree(Gt);
+        if (wb) cudaFree(wb);
+        if (tri_ws) cudaFree(tri_ws);
+        Gt = wb = tri_ws = nullptr;
+        tri_dev = tri_host = 0;
+        dev_free(tinfo);
+        implicit = false;
         dev_free(gpops);
         dev_free(Ht); dev_free(phi); dev_free(acc); dev_free(coef); dev_free(lz); dev_free(scale);
         if (Hs) cudaFree(Hs);
@@ -593,10 +615,11 @@ __global__ void lanczos_start(double *v, int n) {
 
 // Spectral bounds of H~ by FP64 Lanczos (k steps, no reorthogonalisation) with
 // a guard of |beta_k s_k| + 1 % of the width around the extreme Ritz values.
-int lanczos_bounds(ChebState &cs, int ksteps) {
+// h == nullptr: H~ is cs.Ht; otherwise H~ v = G h G^T v with G = L^-1 in cs.Ht.
+int lanczos_bounds(ChebState &cs, int ksteps, const double *h = nullptr) {
     const int n = cs.N;
     cudaStream_t st = g_ctx.stream;
-    double *v = cs.lz, *vp = cs.lz + cs.ld, *w = cs.lz + 2 * cs.ld;
+    double *v = cs.lz, *vp = cs.lz + cs.ld, *w = cs.lz + 2 * cs.ld, *t = cs.lz + 3 * cs.ld;
     lanczos_start<<<(n + 255) / 256, 256, 0, st>>>(v, n);
     CU_TRY(cudaMemsetAsync(vp, 0, n * sizeof(double), st));
     double nrm = 0.0;
@@ -609,7 +632,14 @@ int lanczos_bounds(ChebState &cs, int ksteps) {
     int used = 0;
     const double one = 1.0, zero = 0.0;
     for (int j = 0; j < k; ++j) {
-        BLAS_TRY(cublasDsymv(g_ctx.blas, CUBLAS_FILL_MODE_LOWER, n, &one, cs.Ht, cs.ld, v, 1, &zero, w, 1));
+        if (h) {  // cs.Ht = G with a zero upper triangle: plain GEMVs (trmv is column-sequential)
+            BLAS_TRY(cublasDgemv(g_ctx.blas, CUBLAS_OP_T, n, n, &one, cs.Ht, cs.ld, v, 1, &zero, t, 1));  // G^T v
+            BLAS_TRY(cublasDgemv(g_ctx.blas, CUBLAS_OP_N, n, n, &one, h, cs.ld, t, 1, &zero, w, 1));      // h (.)
+            BLAS_TRY(cublasDgemv(g_ctx.blas, CUBLAS_OP_N, n, n, &one, cs.Ht, cs.ld, w, 1, &zero, t, 1));  // G (.)
+            std::swap(w, t);
+        } else {
+            BLAS_TRY(cublasDsymv(g_ctx.blas, CUBLAS_FILL_MODE_LOWER, n, &one, cs.Ht, cs.ld, v, 1, &zero, w, 1));
+        }
         double al = 0.0;
         BLAS_TRY(cublasDdot(g_ctx.blas, n, w, 1, v, 1, &al));
         const double mal = -al, mb = -bprev;
@@ -639,17 +669,21 @@ int lanczos_bounds(ChebState &cs, int ksteps) {
     return ELHL_OK;
 }
 
-// Hs and the coefficients for step dt on the current bounds.
-int cheb_prepare(ChebState &cs, double dt, double tol) {
+// Hs and the coefficients for step dt on the current bounds.  Explicit:
+// Hs = (H~ - a)/b from cs.Ht; implicit (h given): Hs = h/b, the shift a/b is
+// applied by the kernel.
+int cheb_prepare(ChebState &cs, double dt, double tol, const double *h = nullptr) {
     cudaStream_t st = g_ctx.stream;
     cs.a = 0.5 * (cs.emax + cs.emin);
     cs.b = 0.5 * (cs.emax - cs.emin);
     const double binv = 1.0 / cs.b;
     dim3 grid((cs.ld + 127) / 128, cs.N);
+    const double *src = h ? h : cs.Ht;
+    const double a = h ? 0.0 : cs.a;
     if (cs.precision == ELHL_PREC_FP64)
-        scale_kernel<double><<<grid, 128, 0, st>>>(cs.Ht, (double *)cs.Hs, cs.N, cs.ld, cs.a, binv);
+        scale_kernel<double><<<grid, 128, 0, st>>>(src, (double *)cs.Hs, cs.N, cs.ld, a, binv);
     else
-        scale_kernel<float><<<grid, 128, 0, st>>>(cs.Ht, (float *)cs.Hs, cs.N, cs.ld, cs.a, binv);
+        scale_kernel<float><<<grid, 128, 0, st>>>(src, (float *)cs.Hs, cs.N, cs.ld, a, binv);
     CU_TRY(cudaGetLastError());
     std::vector<double> cre, cim;
     int K = 0;
@@ -672,11 +706,6 @@ int cheb_prepare(ChebState &cs, double dt, double tol) {
     return ELHL_OK;
 }
 
-__global__ void identity_kernel(double *A, int n, int ld) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-    if (i < ld && j < n) A[(size_t)j * ld + i] = (i == j) ? 1.0 : 0.0;
-}
-
 // dst(i, j) = src(j, i) if transpose else src(i, j), in T, keeping only the
 // lower triangle of src (potrf leaves the other triangle untouched); rows >= n are zero
 template <typename T>
@@ -691,6 +720,60 @@ __global__ void convert_kernel(const double *__restrict__ src, T *__restrict__ d
     dst[(size_t)j * ld + i] = (T)v;
 }
 
+// In-place inverse of the lower-triangular n x n block A (leading dimension ld):
+// [L11 0; L21 L22]^-1 = [G11 0; -G22 L21 G11  G22], recursively.  Blocks of at
+// most kTriBase rows go to cuSOLVER trtri; the off-diagonal blocks are two
+// in-place cuBLAS DTRMMs, so almost all of the N^3/3 flops run in large
+// triangular-times-square products (cuSOLVER's own trtri at N = 3720 spends
+// most of its time in 32 x 32 tiles).
+constexpr int kTriBase = 512;
+
+int tri_inverse(ChebState &cs, double *A, int n, int ld) {
+    if (n <= kTriBase) {
+        size_t dev = 0, host = 0;
+        SOLVER_TRY(cusolverDnXtrtri_bufferSize(g_ctx.solver, CUBLAS_FILL_MODE_LOWER, CUBLAS_DIAG_NON_UNIT, n,
+                                               CUDA_R_64F, A, ld, &dev, &host));
+        if (dev > cs.tri_dev || !cs.tri_ws) {
+            CU_TRY(cudaStreamSynchronize(g_ctx.stream));
+            if (cs.tri_ws) cudaFree(cs.tri_ws);
+            cs.tri_ws = nullptr;
+            cs.tri_dev = std::max<size_t>(dev, 16);
+            CU_TRY(cudaMalloc(&cs.tri_ws, cs.tri_dev));
+        }
+        if (host > cs.tri_host || cs.tri_hbuf.empty()) {
+            cs.tri_host = std::max<size_t>(host, 16);
+            cs.tri_hbuf.assign(cs.tri_host, 0);
+        }
+        SOLVER_TRY(cusolverDnXtrtri(g_ctx.solver, CUBLAS_FILL_MODE_LOWER, CUBLAS_DIAG_NON_UNIT, n, CUDA_R_64F, A, ld,
+                                    cs.tri_ws, cs.tri_dev, cs.tri_hbuf.data(), cs.tri_host, cs.tinfo));
+        return ELHL_OK;
+    }
+    const int n1 = std::min(n - 1, (n / 2 + 63) / 64 * 64), n2 = n - n1;
+    double *A11 = A, *A21 = A + n1, *A22 = A + (size_t)n1 * ld + n1;
+    if (int rc = tri_inverse(cs, A11, n1, ld)) return rc;
+    if (int rc = tri_inverse(cs, A22, n2, ld)) return rc;
+    const double m1 = -1.0, one = 1.0;
+    BLAS_TRY(cublasDtrmm(g_ctx.blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n2,
+                         n1, &m1, A11, ld, A21, ld, A21, ld));  // -L21 G11
+    BLAS_TRY(cublasDtrmm(g_ctx.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n2,
+                         n1, &one, A22, ld, A21, ld, A21, ld));  // G22 (.)
+    return ELHL_OK;
+}
+
+// G = L^-1 (FP64, lower; the upper triangle keeps what dst held) from a copy of
+// the Cholesky factor: N^3/3 flops.
+int invert_factor(ChebState &cs, const double *Lfac, double *dst) {
+    cudaStream_t st = g_ctx.stream;
+    const int n = cs.N, ld = cs.ld;
+    CU_TRY(cudaMemcpy2DAsync(dst, ld * sizeof(double), Lfac, ld * sizeof(double), n * sizeof(double), n,
+                             cudaMemcpyDeviceToDevice, st));
+    if (!cs.tinfo) {
+        if (int rc = dev_alloc(&cs.tinfo, 1)) return rc;
+        CU_TRY(cudaMemset(cs.tinfo, 0, sizeof(int)));
+    }
+    return tri_inverse(cs, dst, n, ld);
+}
+
 // A = L^-1 and B = L^T (launch precision) for the device read-out of fixed nuclei.
 int cheb_prepare_readout(ChebState &cs, const double *Lfac) {
     cudaStream_t st = g_ctx.stream;
@@ -701,12 +784,7 @@ int cheb_prepare_readout(ChebState &cs, const double *Lfac) {
     double *tmp = nullptr;
     if (int rc = dev_alloc(&tmp, (size_t)ld * n)) return rc;
     dim3 grid((ld + 127) / 128, n);
-    identity_kernel<<<grid, 128, 0, st>>>(tmp, n, ld);
-    const double one = 1.0;
-    int rc = ELHL_OK;
-    if (cublasDtrsm(g_ctx.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n, n,
-                    &one, Lfac, ld, tmp, ld) != CUBLAS_STATUS_SUCCESS)
-        rc = ELHL_ERR_CUDA;
+    int rc = invert_factor(cs, Lfac, tmp);
     if (!rc) {
         if (cs.precision == ELHL_PREC_FP64) {
             convert_kernel<double><<<grid, 128, 0, st>>>(tmp, (double *)cs.A, n, ld, false);
@@ -721,6 +799,47 @@ int cheb_prepare_readout(ChebState &cs, const double *Lfac) {
     dev_free(tmp);
     if (!rc) cs.readout_ready = true;
     return rc;
+}
+
+// zero the strictly upper triangle and the padding rows of an ld x n matrix
+__global__ void lower_only_kernel(double *A, int n, int ld) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i < ld && j < n && (i < j || i >= n)) A[(size_t)j * ld + i] = 0.0;
+}
+
+// Implicit operator for the current factor and h: G = L^-1 (FP64, in cs.Ht),
+// bounds by Lanczos on G h G^T, Hs = h/b, and A = G, Gt = G^T, B = L^T in the
+// launch precision.  N^3/3 flops (trtri) instead of the 2 N^3 of forming H~.
+int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, double dt, double tol) {
+    cudaStream_t st = g_ctx.stream;
+    const int n = cs.N, ld = cs.ld;
+    const size_t tsz = cs.precision == ELHL_PREC_FP64 ? sizeof(double) : sizeof(float);
+    if (!cs.A) CU_TRY(cudaMalloc(&cs.A, (size_t)ld * n * tsz));
+    if (!cs.B) CU_TRY(cudaMalloc(&cs.B, (size_t)ld * n * tsz));
+    if (!cs.Gt) CU_TRY(cudaMalloc(&cs.Gt, (size_t)ld * n * tsz));
+    if (!cs.wb) {
+        CU_TRY(cudaMalloc(&cs.wb, (size_t)2 * ld * cs.m * 2 * tsz));
+        CU_TRY(cudaMemset(cs.wb, 0, (size_t)2 * ld * cs.m * 2 * tsz));
+    }
+    if (int rc = invert_factor(cs, Lfac, cs.Ht)) return rc;
+    lower_only_kernel<<<dim3((ld + 127) / 128, n), 128, 0, st>>>(cs.Ht, n, ld);
+    CU_TRY(cudaGetLastError());
+    if (int rc = lanczos_bounds(cs, 40, h)) return rc;
+    if (int rc = cheb_prepare(cs, dt, tol, h)) return rc;
+    dim3 grid((ld + 127) / 128, n);
+    if (cs.precision == ELHL_PREC_FP64) {
+        convert_kernel<double><<<grid, 128, 0, st>>>(cs.Ht, (double *)cs.A, n, ld, false);
+        convert_kernel<double><<<grid, 128, 0, st>>>(cs.Ht, (double *)cs.Gt, n, ld, true);
+        convert_kernel<double><<<grid, 128, 0, st>>>(Lfac, (double *)cs.B, n, ld, true);
+    } else {
+        convert_kernel<float><<<grid, 128, 0, st>>>(cs.Ht, (float *)cs.A, n, ld, false);
+        convert_kernel<float><<<grid, 128, 0, st>>>(cs.Ht, (float *)cs.Gt, n, ld, true);
+        convert_kernel<float><<<grid, 128, 0, st>>>(Lfac, (float *)cs.B, n, ld, true);
+    }
+    CU_TRY(cudaGetLastError());
+    cs.implicit = true;
+    cs.readout_ready = true;
+    return ELHL_OK;
 }
 
 // ---- GEMM regime kernels (complex columns [ld][m], element-wise) -------------
@@ -775,12 +894,15 @@ __global__ void scale_from_pops_kernel(const double *pops, int P, int nfrag, con
     }
 }
 
-// Yt (2m x n) = Vt (2m x n, ld 2m) * M (n x n, ld), FP32 data, tensor cores with
-// FP32-accuracy emulation (three BF16 terms per operand)
-int gemm_vt(cublasHandle_t h, int m2, int n, const float *Vt, const float *M, int ld, float *Yt) {
+// Yt (2m x n) = Vt (2m x n, ld 2m) * M (n x n, ld), FP32 data.  ELHL_PREC_FP32:
+// FP32 FMAs with round-to-nearest sums (PEDANTIC: no reduced-precision path);
+// ELHL_PREC_BF16X3: tensor cores with each operand split in three BF16 terms.
+int gemm_vt(cublasHandle_t h, int precision, int m2, int n, const float *Vt, const float *M, int ld, float *Yt) {
     const float one = 1.0f, zero = 0.0f;
+    const cublasComputeType_t ct =
+        precision == ELHL_PREC_BF16X3 ? CUBLAS_COMPUTE_32F_EMULATED_16BFX9 : CUBLAS_COMPUTE_32F_PEDANTIC;
     BLAS_TRY(cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, m2, n, n, &one, Vt, CUDA_R_32F, m2, M, CUDA_R_32F, ld, &zero,
-                          Yt, CUDA_R_32F, m2, CUBLAS_COMPUTE_32F_EMULATED_16BFX9, CUBLAS_GEMM_DEFAULT));
+                          Yt, CUDA_R_32F, m2, ct, CUBLAS_GEMM_DEFAULT));
     return ELHL_OK;
 }
 
@@ -797,16 +919,21 @@ int cheb_gemm_enqueue(ChebState &cs, int parity) {
     const bool renorm = true;
     gemm_order0_kernel<<<nb, tb, 0, st>>>(in, renorm ? cs.scale : nullptr, cs.P, n, m, cs.c0, vb, out);
     for (int k = 1; k <= cs.K; ++k) {
-        if (int rc = gemm_vt(g_ctx.blas_tc, 2 * m, n, reinterpret_cast<const float *>(vb + ((k + 2) % 3) * vs),
+        if (int rc = gemm_vt(g_ctx.blas_tc, cs.precision, 2 * m, n,
+                             reinterpret_cast<const float *>(vb + ((k + 2) % 3) * vs),
                              reinterpret_cast<const float *>(cs.Hs), cs.ld, cs.Y))
             return rc;
         gemm_epilogue_kernel<<<nb, tb, 0, st>>>(reinterpret_cast<const float2 *>(cs.Y), vb + ((k + 1) % 3) * vs,
                                                 vb + (k % 3) * vs, out, cs.coef, k, nm);
     }
     to_float2_kernel<<<nb, tb, 0, st>>>(out, reinterpret_cast<float2 *>(cs.Vf), nm);
-    if (int rc = gemm_vt(g_ctx.blas_tc, 2 * m, n, cs.Vf, reinterpret_cast<const float *>(cs.A), cs.ld, cs.Y)) return rc;
+    if (int rc = gemm_vt(g_ctx.blas_tc, cs.precision, 2 * m, n, cs.Vf, reinterpret_cast<const float *>(cs.A), cs.ld,
+                         cs.Y))
+        return rc;
     to_double2_kernel<<<nb, tb, 0, st>>>(reinterpret_cast<const float2 *>(cs.Y), cs.psi_out, nm);
-    if (int rc = gemm_vt(g_ctx.blas_tc, 2 * m, n, cs.Vf, reinterpret_cast<const float *>(cs.B), cs.ld, cs.Y)) return rc;
+    if (int rc = gemm_vt(g_ctx.blas_tc, cs.precision, 2 * m, n, cs.Vf, reinterpret_cast<const float *>(cs.B), cs.ld,
+                         cs.Y))
+        return rc;
     to_double2_kernel<<<nb, tb, 0, st>>>(reinterpret_cast<const float2 *>(cs.Y), cs.bra_out, nm);
     populations_kernel<<<cs.P, 256, 0, st>>>(cs.psi_out, cs.bra_out, n, cs.P, cs.ao_frag, cs.nfrag, cs.gpops);
     scale_from_pops_kernel<<<1, kMaxCols, 0, st>>>(cs.gpops, cs.P, cs.nfrag, cs.target, cs.scale);
@@ -850,11 +977,14 @@ struct ChebPlan {
     int *d_seg_begin = nullptr, *d_prob_seg0 = nullptr;
     double *d_seg_pops = nullptr;
     int grid = 0, max_ld = 0, kmax = 0, mg = 0, mg_read = 0, precision = 0, parity = 0;
+    int nphase = 1;            // 3: one implicit problem
     size_t pops_per_step = 0;  // populations of all problems in one step
     void release() {
         dev_free(d_probs); dev_free(d_segs); dev_free(d_seg_begin); dev_free(d_prob_seg0); dev_free(d_seg_pops);
     }
 };
+
+int tune_plan(ChebPlan &pl, int mgcd);
 
 int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
     pl.release();
@@ -886,6 +1016,9 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
     pl.mg_read = cheb_group_size(pl.precision, pgcd, pl.max_ld);
     pl.pops_per_step = 0;
     pl.parity = states[0]->parity;
+    const bool implicit = states[0]->implicit;
+    if (implicit && states.size() != 1) return ELHL_ERR_UNSUPPORTED;
+    pl.nphase = implicit ? 3 : 1;
     for (auto *cs : states) {
         ChebProblem p{};
         p.N = cs->N; p.ld = cs->ld; p.ldv = cs->ld; p.m = cs->m; p.K = cs->K;
@@ -900,17 +1033,35 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
         p.scale = renorm ? cs->scale : nullptr;
         p.scale_out = renorm ? cs->scale : nullptr;
         p.target = renorm ? cs->target : nullptr;
+        if (cs->implicit) {
+            p.G = cs->A;
+            p.Gt = cs->Gt;
+            p.wb = cs->wb;
+            p.shift = cs->a / cs->b;
+        }
         pl.pops_per_step += (size_t)cs->P * (cs->nfrag + 1);
         pl.probs.push_back(p);
         pl.kmax = std::max(pl.kmax, cs->K);
         if (cs->parity != pl.parity) return ELHL_ERR_BAD_ARG;
     }
+    pl.seg_begin.assign(pl.grid + 1, 0);
+    if (implicit) {
+        // 2 x grid equal row chunks, CTA c owning chunks c and 2 grid - 1 - c: the
+        // triangular phases (G^T: j >= i, G: j <= i) then cost every CTA the same
+        const int N = states[0]->N, nch = 2 * pl.grid;
+        for (int c = 0; c < pl.grid; ++c) {
+            for (int q : {c, nch - 1 - c}) {
+                const int r0 = (int)((long long)N * q / nch), r1 = (int)((long long)N * (q + 1) / nch);
+                if (r1 > r0) pl.segs.push_back({0, r0, r1});
+            }
+            pl.seg_begin[c + 1] = (int)pl.segs.size();
+        }
+    }
     // greedy split of the concatenated rows: CTA c fills up to (c+1)/grid of the work
     const double per = work / pl.grid;
-    pl.seg_begin.assign(pl.grid + 1, 0);
-    int c = 0;
+    int c = implicit ? pl.grid : 0;
     double acc_w = 0.0;
-    for (int q = 0; q < (int)states.size(); ++q) {
+    for (int q = 0; q < (int)states.size() && !implicit; ++q) {
         const ChebState *cs = states[q];
         const double rw = cs->ld;  // work per row
         int r = 0;
@@ -929,7 +1080,8 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
             }
         }
     }
-    for (int cc = c + 1; cc <= pl.grid; ++cc) pl.seg_begin[cc] = (int)pl.segs.size();
+    if (!implicit)
+        for (int cc = c + 1; cc <= pl.grid; ++cc) pl.seg_begin[cc] = (int)pl.segs.size();
     pl.prob_seg0.assign(states.size() + 1, 0);
     for (size_t i = 0; i < pl.segs.size(); ++i) pl.prob_seg0[pl.segs[i].prob + 1] = (int)i + 1;
     for (size_t q = 1; q <= states.size(); ++q) pl.prob_seg0[q] = std::max(pl.prob_seg0[q], pl.prob_seg0[q - 1]);
@@ -942,18 +1094,90 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
     CU_TRY(cudaMemcpy(pl.d_probs, pl.probs.data(), pl.probs.size() * sizeof(ChebProblem), cudaMemcpyHostToDevice));
     CU_TRY(cudaMemcpy(pl.d_segs, pl.segs.data(), pl.segs.size() * sizeof(ChebSegment), cudaMemcpyHostToDevice));
     CU_TRY(cudaMemcpy(pl.d_seg_begin, pl.seg_begin.data(), pl.seg_begin.size() * sizeof(int), cudaMemcpyHostToDevice));
-    return ELHL_OK;
+    return tune_plan(pl, mgcd);
 }
 
 // refresh per-problem order counts and coefficient pointers after cheb_prepare
 int cheb_plan_refresh(ChebPlan &pl, const std::vector<ChebState *> &states) {
+    if (pl.nphase != (states[0]->implicit ? 3 : 1)) return cheb_plan(pl, states);  // operator form changed
     pl.kmax = 0;
     for (size_t q = 0; q < states.size(); ++q) {
         pl.probs[q].K = states[q]->K;
         pl.probs[q].coef = states[q]->coef;
+        if (states[q]->implicit) pl.probs[q].shift = states[q]->a / states[q]->b;
         pl.kmax = std::max(pl.kmax, states[q]->K);
     }
     CU_TRY(cudaMemcpy(pl.d_probs, pl.probs.data(), pl.probs.size() * sizeof(ChebProblem), cudaMemcpyHostToDevice));
+    return ELHL_OK;
+}
+
+ChebLaunch plan_launch(const ChebPlan &pl) {
+    ChebLaunch L{};
+    L.probs = pl.d_probs;
+    L.segs = pl.d_segs;
+    L.seg_begin = pl.d_seg_begin;
+    L.kmax = pl.kmax;
+    L.max_ld = pl.max_ld;
+    L.grid = pl.grid;
+    L.bar_count = g_ctx.bar;
+    L.bar_gen = g_ctx.bar + 1;
+    L.error = g_ctx.err;
+    L.prob_seg0 = pl.d_prob_seg0;
+    L.parity = pl.parity;
+    L.seg_pops = pl.d_seg_pops;
+    L.nphase = pl.nphase;
+    return L;
+}
+
+// Autotuner of the propagation tile: the number of complex columns staged per
+// pass over the matrix (4, 2 or 1 where it divides every problem's column count
+// and fits in shared memory) sets the accumulator tile of every warp (row tile x
+// columns) and the passes per order.  Each candidate runs the plan itself for
+// up to 4 orders (twice; the second run is timed with CUDA events); the fastest
+// is kept per (precision, column gcd, phases, padded size, total elements).  A
+// trial only writes the output columns and recurrence buffers, which the next
+// real launch overwrites.
+std::map<std::tuple<int, int, int, int, int>, int> g_tile_cache;
+
+int tune_plan(ChebPlan &pl, int mgcd) {
+    std::vector<int> cand;
+    for (int mg : {4, 2, 1})
+        if (mgcd % mg == 0 && cheb_group_size(pl.precision, mg, pl.max_ld) == mg) cand.push_back(mg);
+    if (cand.size() < 2 || pl.kmax < 1) return ELHL_OK;
+    double elems = 0.0;
+    for (const auto &p : pl.probs) elems += (double)p.N * p.ld;
+    const auto key = std::make_tuple(pl.precision, mgcd, pl.nphase, (pl.max_ld + 255) / 256, (int)std::log2(elems + 1));
+    auto it = g_tile_cache.find(key);
+    if (it != g_tile_cache.end()) {
+        pl.mg = it->second;
+        return ELHL_OK;
+    }
+    cudaStream_t st = g_ctx.stream;
+    ChebLaunch L = plan_launch(pl);
+    L.kmax = std::min(pl.kmax, 4);
+    float best = 3.0e38f;
+    int best_mg = pl.mg;
+    for (int mg : cand) {
+        float ms = 0.0f;
+        for (int rep = 0; rep < 2; ++rep) {
+            CU_TRY(cudaMemsetAsync(g_ctx.err, 0, sizeof(int), st));
+            CU_TRY(cudaMemsetAsync(g_ctx.bar, 0, 2 * sizeof(unsigned), st));
+            CU_TRY(cudaEventRecord(g_ctx.ev[0], st));
+            CU_TRY(launch_cheb(L, pl.precision, mg, st));
+            CU_TRY(cudaEventRecord(g_ctx.ev[1], st));
+        }
+        CU_TRY(cudaEventSynchronize(g_ctx.ev[1]));
+        CU_TRY(cudaEventElapsedTime(&ms, g_ctx.ev[0], g_ctx.ev[1]));
+        int err = 0;
+        CU_TRY(cudaMemcpy(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost));
+        if (err) return err;
+        if (ms < best) {
+            best = ms;
+            best_mg = mg;
+        }
+    }
+    pl.mg = best_mg;
+    g_tile_cache[key] = best_mg;
     return ELHL_OK;
 }
 
@@ -974,6 +1198,7 @@ int cheb_run(ChebPlan &pl) {
     L.prob_seg0 = pl.d_prob_seg0;
     L.parity = pl.parity;
     L.seg_pops = pl.d_seg_pops;
+    L.nphase = pl.nphase;
     CU_TRY(cudaEventRecord(g_ctx.ev[0], st));
     CU_TRY(launch_cheb(L, pl.precision, pl.mg, st));
     CU_TRY(cudaEventRecord(g_ctx.ev[1], st));
@@ -1053,6 +1278,76 @@ int cols_apply(const double *Lfac, int ld, int n, double2 *cols, int m, int col0
         BLAS_TRY(cublasDtrmm(g_ctx.blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, op, CUBLAS_DIAG_NON_UNIT, rows, n,
                              &one, Lfac, ld, X, ldx, X, ldx));
     }
+    return ELHL_OK;
+}
+
+// ---- Ehrenfest force kernel pieces ---------------------------------------------
+// K = X o A (Hadamard), then K -= H A by one DGEMM (alpha = -1, beta = 1):
+// the K = X o A - H A of hadamard_minus (Chebyshev_gpu_kernels.cu:358-389) with
+// ehrenfestkernel_gpu_ (Taylor_gpu.cpp:743-791).
+__global__ void hadamard_kernel(const double *__restrict__ X, const double *__restrict__ A, double *__restrict__ K,
+                                int n, int ld) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i < n && j < n) K[(size_t)j * ld + i] = X[(size_t)j * ld + i] * A[(size_t)j * ld + i];
+}
+
+// A = (rho + rho^T)/2, rho_ij = Re(ket_j1 bra_i1) - Re(ket_j2 bra_i2)
+// (calculate_A / calculate_rho_kernel, Chebyshev_gpu_kernels.cu:394-455); bra/ket [2][n]
+__global__ void ehrenfest_a_kernel(const double2 *__restrict__ bra, const double2 *__restrict__ ket, double *A,
+                                   int n, int ld) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= n || j >= n) return;
+    auto rho = [&](int r, int c) {
+        const double2 k1 = ket[c], b1 = bra[r], k2 = ket[n + c], b2 = bra[n + r];
+        return (k1.x * b1.x - k1.y * b1.y) - (k2.x * b2.x - k2.y * b2.y);
+    };
+    A[(size_t)j * ld + i] = 0.5 * (rho(i, j) + rho(j, i));
+}
+
+struct EhrenfestBuffers {
+    int n = 0, ld = 0;
+    double *H = nullptr, *A = nullptr, *X = nullptr, *K = nullptr;
+    double2 *bk = nullptr;
+    int reserve(int n_) {
+        if (H && n_ <= n) return ELHL_OK;
+        dev_free(H); dev_free(A); dev_free(X); dev_free(K); dev_free(bk);
+        n = n_;
+        ld = round_up(n, 32);
+        if (int rc = dev_alloc(&H, (size_t)ld * n)) return rc;
+        if (int rc = dev_alloc(&A, (size_t)ld * n)) return rc;
+        if (int rc = dev_alloc(&X, (size_t)ld * n)) return rc;
+        if (int rc = dev_alloc(&K, (size_t)ld * n)) return rc;
+        return dev_alloc(&bk, (size_t)4 * n);
+    }
+};
+EhrenfestBuffers g_ehr;
+
+int ehrenfest_impl(int n, const double *hH, const double *hA, const elhl_zcomplex *hbra, const elhl_zcomplex *hket,
+                   const double *hX, double *hK) {
+    if (n <= 0 || !hH || !hX || !hK || (!hA && (!hbra || !hket))) return ELHL_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(g_ctx.mu);
+    if (int rc = ensure_context_locked(-1)) return rc;
+    if (int rc = g_ehr.reserve(n)) return rc;
+    cudaStream_t st = g_ctx.stream;
+    const int ld = g_ehr.ld;
+    const size_t col = n * sizeof(double), ldb = ld * sizeof(double);
+    dim3 grid((n + 127) / 128, n);
+    CU_TRY(cudaMemcpy2DAsync(g_ehr.H, ldb, hH, col, col, n, cudaMemcpyHostToDevice, st));
+    CU_TRY(cudaMemcpy2DAsync(g_ehr.X, ldb, hX, col, col, n, cudaMemcpyHostToDevice, st));
+    if (hA) {
+        CU_TRY(cudaMemcpy2DAsync(g_ehr.A, ldb, hA, col, col, n, cudaMemcpyHostToDevice, st));
+    } else {
+        CU_TRY(cudaMemcpyAsync(g_ehr.bk, hbra, 2 * n * sizeof(double2), cudaMemcpyHostToDevice, st));
+        CU_TRY(cudaMemcpyAsync(g_ehr.bk + 2 * n, hket, 2 * n * sizeof(double2), cudaMemcpyHostToDevice, st));
+        ehrenfest_a_kernel<<<grid, 128, 0, st>>>(g_ehr.bk, g_ehr.bk + 2 * n, g_ehr.A, n, ld);
+    }
+    hadamard_kernel<<<grid, 128, 0, st>>>(g_ehr.X, g_ehr.A, g_ehr.K, n, ld);
+    CU_TRY(cudaGetLastError());
+    const double m1 = -1.0, one = 1.0;
+    BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &m1, g_ehr.H, ld, g_ehr.A, ld, &one, g_ehr.K,
+                         ld));
+    CU_TRY(cudaMemcpy2DAsync(hK, col, g_ehr.K, ldb, col, n, cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaStreamSynchronize(st));
     return ELHL_OK;
 }
 
@@ -1152,14 +1447,19 @@ int rebuild(elhl_traj *tr, const double *d_coords) {
     return rc;
 }
 
-// Cholesky factor, H~, bounds and coefficients for the current S, h.
-int cheb_rebuild_operator(elhl_traj *tr) {
+// Cholesky factor, then the operator for the current S, h: explicit H~ (formed
+// once for fixed nuclei, 2 N^3 flops) or implicit G h G^T (a geometry that
+// changes every step, N^3/3 flops); bounds and coefficients.
+int cheb_rebuild_operator(elhl_traj *tr, bool implicit = false) {
     cudaStream_t st = g_ctx.stream;
     CU_TRY(cudaMemcpy2DAsync(tr->fac.L, tr->ld * sizeof(double), tr->S, tr->ld * sizeof(double), tr->N * sizeof(double),
                              tr->N, cudaMemcpyDeviceToDevice, st));
     SOLVER_TRY(cusolverDnDpotrf(g_ctx.solver, CUBLAS_FILL_MODE_LOWER, tr->N, tr->fac.L, tr->ld, tr->fac.work,
                                 tr->fac.lwork, tr->fac.info));
     if (int rc = tr->fac.check_info(false)) return rc;
+    if (implicit)
+        return cheb_prepare_implicit(tr->cs, tr->fac.L, tr->h, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol);
+    tr->cs.implicit = false;
     if (int rc = form_htilde(tr->cs, tr->fac.L, tr->h, tr->ld)) return rc;
     if (int rc = lanczos_bounds(tr->cs, 40)) return rc;
     return cheb_prepare(tr->cs, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol);
@@ -1208,6 +1508,12 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
     const size_t nc = (size_t)tr->natoms * 3;
     std::vector<ChebState *> one{&cs};
     int rc = ELHL_OK;
+    if (!coords && cs.implicit && cs.gemm) {
+        // GEMM regime after moving steps: form H~ for the current geometry
+        if ((rc = cheb_rebuild_operator(tr, false))) return rc;
+        if ((rc = cheb_prepare_readout(cs, tr->fac.L))) return rc;
+        if ((rc = cheb_plan(tr->plan, one))) return rc;
+    }
     if (!coords && !cs.readout_ready && tr->fac.L) {
         // fixed nuclei after moving steps: factor-based read-out matrices for the current L
         if ((rc = cheb_prepare_readout(cs, tr->fac.L))) return rc;
@@ -1268,8 +1574,7 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
                 rc = ELHL_ERR_CUDA;
                 break;
             }
-            if ((rc = cheb_rebuild_operator(tr))) break;
-            cs.readout_ready = false;  // L changed
+            if ((rc = cheb_rebuild_operator(tr, true))) break;  // implicit: A, B follow the new L
             if ((rc = cheb_load_columns(tr))) break;
             if (cudaEventRecord(g_ctx.ev[3], st) != cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
             if ((rc = cheb_plan_refresh(tr->plan, one))) break;
@@ -1335,7 +1640,10 @@ int traj_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
     };
     memset(&tr->stats, 0, sizeof(tr->stats));
     if (tr->cheb()) {
-        if (int rc = cheb_step_impl(tr, coords, coords_on_device, nsteps, d_pops)) return rc;
+        const int rc = cheb_step_impl(tr, coords, coords_on_device, nsteps, d_pops);
+        tr->stats.tile_cols = tr->cs.gemm ? 0 : tr->plan.mg;
+        tr->stats.phases = tr->plan.nphase;
+        if (rc) return rc;
         if (pops && !pops_on_device)
             CU_TRY(cudaMemcpy(pops, d_pops, nsteps * pop_per_step * sizeof(double), cudaMemcpyDeviceToHost));
         return ELHL_OK;
@@ -1603,6 +1911,17 @@ void gpu_unpin_(void *ptr) {
     g_last_status = e == cudaSuccess ? ELHL_OK : ELHL_ERR_CUDA;
 }
 
+void ehrenfestkernel_gpu_(const int *N, const double *h_H, const double *h_A, const double *h_X, double *h_K) {
+    g_last_status = N ? ehrenfest_impl(*N, h_H, h_A, nullptr, nullptr, h_X, h_K) : ELHL_ERR_BAD_ARG;
+    if (g_last_status) fprintf(stderr, "elhlprop: ehrenfestkernel_gpu_: %s\n", elhl_status_string(g_last_status));
+}
+
+void ehrenfestkernel2_gpu_(const int *N, const elhl_zcomplex *h_bra, const elhl_zcomplex *h_ket, const double *h_H,
+                           const double *h_X, double *h_K) {
+    g_last_status = N ? ehrenfest_impl(*N, h_H, nullptr, h_bra, h_ket, h_X, h_K) : ELHL_ERR_BAD_ARG;
+    if (g_last_status) fprintf(stderr, "elhlprop: ehrenfestkernel2_gpu_: %s\n", elhl_status_string(g_last_status));
+}
+
 void propagation_gpucaller_(const int *n, double *tau, double *save_tau, const double *t_init, const double *t_max,
                             elhl_zcomplex *h_PSI_bra, elhl_zcomplex *h_PSI_ket, const double *h_H) {
     if (!n || !tau || !t_init || !t_max) { g_last_status = ELHL_ERR_BAD_ARG; return; }
@@ -1636,6 +1955,36 @@ void elhl_traj_config_default(elhl_traj_config *c) {
     c->nparticles = 2;
 }
 
+int elhl_ehrenfest_forces(const elhl_basis_desc *basis, const double *coords, const double *kernel, double delta,
+                          double cutoff, double *forces) {
+    if (!coords || !kernel || !forces) return ELHL_ERR_BAD_ARG;
+    if (int rc = validate_basis(basis)) return rc;
+    if (!(delta > 0.0)) delta = 1.0e-8;   // diabatic-Ehren.f:32
+    if (!(cutoff > 0.0)) cutoff = 12.0;   // cutoff_Angs
+    std::lock_guard<std::mutex> lk(g_ctx.mu);
+    if (int rc = ensure_context_locked(-1)) return rc;
+    cudaStream_t st = g_ctx.stream;
+    const int nat = basis->natoms, n = basis->nao;
+    DevBasis db{};
+    double *d_coords = nullptr, *d_kernel = nullptr, *d_F = nullptr, *d_force = nullptr;
+    int rc = upload_basis(db, basis);
+    if (!rc) rc = dev_alloc(&d_coords, (size_t)nat * 3);
+    if (!rc) rc = dev_alloc(&d_kernel, (size_t)n * n);
+    if (!rc) rc = dev_alloc(&d_F, (size_t)nat * nat * 3);
+    if (!rc) rc = dev_alloc(&d_force, (size_t)nat * 3);
+    if (!rc && (cudaMemcpyAsync(d_coords, coords, (size_t)nat * 3 * sizeof(double), cudaMemcpyHostToDevice, st) ||
+                cudaMemcpyAsync(d_kernel, kernel, (size_t)n * n * sizeof(double), cudaMemcpyHostToDevice, st)))
+        rc = ELHL_ERR_CUDA;
+    if (!rc && launch_pulay_forces(db, d_coords, cutoff, delta, d_kernel, n, d_F, 2.0 * 1.602176565e-9, d_force, st))
+        rc = ELHL_ERR_CUDA;
+    if (!rc && (cudaMemcpyAsync(forces, d_force, (size_t)nat * 3 * sizeof(double), cudaMemcpyDeviceToHost, st) ||
+                cudaStreamSynchronize(st)))
+        rc = ELHL_ERR_CUDA;
+    free_basis(db);
+    dev_free(d_coords); dev_free(d_kernel); dev_free(d_F); dev_free(d_force);
+    return rc;
+}
+
 int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const elhl_traj_config *cfg,
                      elhl_traj **out) {
     if (!out || !coords) return ELHL_ERR_BAD_ARG;
@@ -1647,7 +1996,8 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
     const bool taylor_ok = tr->cfg.method == ELHL_METHOD_TAYLOR_REF && tr->cfg.precision == ELHL_PREC_FP64;
     const bool taylor_p = tr->cfg.nparticles == 2;
     const bool cheb_ok = tr->cfg.method == ELHL_METHOD_CHEBYSHEV &&
-                         (tr->cfg.precision == ELHL_PREC_FP64 || tr->cfg.precision == ELHL_PREC_FP32) &&
+                         (tr->cfg.precision == ELHL_PREC_FP64 || tr->cfg.precision == ELHL_PREC_FP32 ||
+                          tr->cfg.precision == ELHL_PREC_BF16X3) &&
                          tr->cfg.nparticles >= 1 && tr->cfg.nparticles <= 64 &&
                          (tr->cfg.ncols == tr->cfg.nparticles || tr->cfg.ncols == 2 * tr->cfg.nparticles) &&
                          tr->cfg.cheb_tol > 0.0;
@@ -1697,8 +2047,8 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
         cs.P = tr->P; cs.nfrag = tr->nfrag; cs.psi_out = tr->psi_ao; cs.bra_out = tr->bra_ao;
         cs.ao_frag = tr->basis.ao_frag; cs.target = tr->target;
         if (!rc) rc = cheb_prepare_readout(cs, tr->fac.L);
-        // GEMM regime: many ket columns in FP32 -> tensor-core GEMMs per order
-        if (!rc && cs.precision == ELHL_PREC_FP32 && cs.m == cs.P && cs.P >= kGemmMinCols) {
+        // GEMM regime: many ket columns in FP32 / BF16X3 -> one GEMM per order
+        if (!rc && cs.precision != ELHL_PREC_FP64 && cs.m == cs.P && cs.P >= kGemmMinCols && cs.N >= kGemmMinN) {
             cs.gemm = true;
             if (cudaMalloc(&cs.Y, (size_t)cs.ld * cs.m * sizeof(float2)) != cudaSuccess ||
                 cudaMalloc(&cs.Vf, (size_t)cs.ld * cs.m * sizeof(float2)) != cudaSuccess)
@@ -1966,6 +2316,8 @@ int elhl_batch_step(elhl_batch *b, int nsteps, double *pops) {
     if (err) return err;
     b->stats.prop_ms += event_ms(0, 1) * nsteps;
     b->stats.prop_launches += nsteps;
+    b->stats.tile_cols = b->plan.mg;
+    b->stats.phases = b->plan.nphase;
     for (auto *cs : b->states) b->stats.orders += (long long)cs->K * cs->m * nsteps;
     b->stats.substeps += (long long)nt * nsteps;
     if (pops) CU_TRY(cudaMemcpy(pops, b->pops, per_step * nsteps * sizeof(double), cudaMemcpyDeviceToHost));

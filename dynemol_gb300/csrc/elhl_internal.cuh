@@ -26,6 +26,10 @@ struct DevBasis {
 cudaError_t init_build_tables();
 
 // S and h (both N x N, column-major, leading dimension ld) from coordinates.
+// Ehrenfest Pulay forces: F (natoms^2 x 3 scratch) and force (natoms x 3) on the device
+cudaError_t launch_pulay_forces(const DevBasis &b, const double *d_coords, double cutoff, double delta,
+                                const double *d_kernel, int ldk, double *d_F, double scale, double *d_force,
+                                cudaStream_t st);
 cudaError_t launch_build_sh(const DevBasis &b, const double *d_coords, double cutoff, double *d_S,
                             double *d_h, int ld, cudaStream_t st);
 
@@ -92,6 +96,12 @@ struct ChebProblem {
     int nfrag, pops_off;    // populations of this problem at pops + pops_off, P x (nfrag+1)
     const double *target;   // [P] norm targets for the renormalisation factor, or nullptr
     double *scale_out;      // [P] factor for the next step, or nullptr
+    // implicit operator (geometry changing every step): H holds h/b, G = L^-1 (lower,
+    // zeros above the diagonal), Gt = G^T (upper), and one order applies
+    // Hs v = G (h/b) G^T v - shift v in three grid-synchronised phases.  G == nullptr: explicit Hs.
+    const void *G, *Gt;
+    void *wb;               // [2][m/MG][ldv][MG] launch precision: w = G^T v, y = (h/b) w
+    double shift;           // a / b
 };
 struct ChebSegment {
     int prob, row0, row1;   // rows [row0, row1) of problem `prob` owned by one CTA
@@ -106,6 +116,7 @@ struct ChebLaunch {
     int *error;
     double *seg_pops;       // [nseg][kMaxCols][kMaxFrag+1] read-out partials
     double *pops;           // this step's populations block, or nullptr
+    int nphase;             // grid phases per order: 1 (explicit Hs) or 3 (one implicit problem)
 };
 constexpr size_t kCheb_part_bytes = 16 * 64 * sizeof(double);  // cross-warp partial sums
 constexpr size_t kCheb_smem_limit = 200 * 1024;

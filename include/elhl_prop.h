@@ -85,6 +85,17 @@ void propagationelhl_gpucaller_(const int *N, const double *h_S, const double *h
                                 const double *t_init, const double *t_max, double *tau,
                                 double *save_tau);
 
+/*
+ * Ehrenfest force kernel pieces (Taylor_gpu.cpp:743-791, :795-874; kernels
+ * Chebyshev_gpu_kernels.cu:358-455), host N x N column-major, ld = N:
+ *   ehrenfestkernel_gpu_ : K = X o A - H A   (o = element-wise product)
+ *   ehrenfestkernel2_gpu_: the same with A = (rho + rho^T)/2,
+ *       rho_ij = Re(ket_j,1 bra_i,1) - Re(ket_j,2 bra_i,2); bra/ket are N x 2.
+ */
+void ehrenfestkernel_gpu_(const int *N, const double *h_H, const double *h_A, const double *h_X, double *h_K);
+void ehrenfestkernel2_gpu_(const int *N, const elhl_zcomplex *h_bra, const elhl_zcomplex *h_ket, const double *h_H,
+                           const double *h_X, double *h_K);
+
 /* Status of the last drop-in call on this thread (ELHL_OK, ...). */
 int elhl_last_status(void);
 const char *elhl_status_string(int status);
@@ -98,8 +109,12 @@ enum {
 };
 enum {
     ELHL_PREC_FP64 = 0,
-    ELHL_PREC_FP32 = 1,   /* H~ products in FP32, FP64 coefficients / norms */
-    ELHL_PREC_BF16X3 = 2  /* H~ split in three bf16 terms on the tensor cores, FP32 accumulate */
+    ELHL_PREC_FP32 = 1,   /* Chebyshev: FP32 H~ and series vectors, FP64 coefficients, sums and norms;
+                             with >= 16 ket columns (one per particle) and N >= 2048, H~.Psi runs as
+                             FP32 GEMMs on the FP32 pipes (cuBLAS, FP32 sums along N) */
+    ELHL_PREC_BF16X3 = 2  /* Chebyshev: as FP32, but those GEMMs run on the tensor cores with each
+                             FP32 operand split in three bf16 terms; outside the GEMM regime it runs
+                             as FP32 */
 };
 
 /* STO basis of one system (the STO_basis fields the path reads, types_EHT.f:135-165). */
@@ -140,6 +155,21 @@ typedef struct {
 typedef struct elhl_traj elhl_traj;
 
 void elhl_traj_config_default(elhl_traj_config *cfg);
+
+/*
+ * Ehrenfest (Hellmann-Feynman-Pulay) forces on every atom of one geometry
+ * (Diabatic_Ehrenfest / Ehrenfest, diabatic-Ehren.f:36-150, :163-230).  For
+ * each atom pair K < L closer than `cutoff` and each direction, dS(j in L,
+ * i in K)/dR_K is the central difference of the S block rebuilt with atom K
+ * displaced by +-delta (PULAY_OVERLAP, overlap_D.f:314-463), and
+ *   F_K(L) = -sum_{j in L, i in K} dS_ji/dR_K * kernel(i, j),
+ *   forces[a][xyz] = 2 * 1.602176565e-9 * (sum_{L > a} F_a(L) - sum_{K < a} F_K(a))  [N].
+ * kernel: host N x N column-major (ld = N), the ehrenfestkernel2_gpu_ output
+ * X o A - H' A.  coords: natoms x 3 Angstrom.  delta <= 0 selects the
+ * reference's 1e-8 Angstrom, cutoff <= 0 its 12 Angstrom.  forces: natoms x 3.
+ */
+int elhl_ehrenfest_forces(const elhl_basis_desc *basis, const double *coords, const double *kernel, double delta,
+                          double cutoff, double *forces);
 
 /* Create a trajectory at the given coordinates (natoms*3, atom-major, Angstrom, host).
  * Builds S, h and H' on the device. */
@@ -200,6 +230,8 @@ typedef struct {
     double rebuild_ms;    /* device time of the S, h, H' rebuilds */
     int prop_launches;    /* propagation kernel launches */
     int rebuild_count;    /* rebuilds */
+    int tile_cols;        /* Chebyshev: complex columns per matrix pass chosen by the autotuner (0: GEMM regime) */
+    int phases;           /* Chebyshev: grid phases per order (1 explicit H~, 3 implicit G h G^T) */
 } elhl_traj_stats;
 int elhl_traj_get_stats(elhl_traj *tr, elhl_traj_stats *st);
 

@@ -315,3 +315,43 @@ def exact_populations(sys, S, psi_ket_t):
     if psi_ket_t.ndim == 1:
         return populations(sys, bra, psi_ket_t)
     return np.stack([populations(sys, bra[:, p], psi_ket_t[:, p]) for p in range(psi_ket_t.shape[1])], 1)
+
+
+# ------------------------------------------------------------------ Ehrenfest pieces
+def ehrenfest_kernel(H, X, A=None, bra=None, ket=None):
+    """K = X o A - H A (hadamard_minus after the DGEMM, Taylor_gpu.cpp:776-781); with
+    bra/ket (N x 2): A = (rho + rho^T)/2, rho_ij = Re(ket_j1 bra_i1) - Re(ket_j2 bra_i2)
+    (calculate_rho_kernel / calculate_A, Chebyshev_gpu_kernels.cu:394-455)."""
+    if A is None:
+        rho = np.real(np.outer(bra[:, 0], ket[:, 0])) - np.real(np.outer(bra[:, 1], ket[:, 1]))
+        A = 0.5 * (rho + rho.T)
+    return X * A - H @ A
+
+
+def pulay_forces(sys, kernel, coords=None, delta=1e-8, cutoff=12.0):
+    """Ehrenfest (Hellmann-Feynman-Pulay) forces, natoms x 3 in N (Ehrenfest and
+    Diabatic_Ehrenfest, diabatic-Ehren.f:163-230 and :100-150): per atom K and
+    direction, S rebuilt with K displaced by +-delta (PULAY_OVERLAP,
+    overlap_D.f:314-463, here the whole S), grad_S = (S_fwd - S_bck) / (2 delta)
+    over the columns of K, F_K(L) = -sum_{j in L, i in K} grad_S(j, i) kernel(i, j)
+    for the atoms L > K closer than the cutoff (preprocess, :316-324), and
+    force(a) = 2 e2N (sum_{L > a} F_a(L) - sum_{K < a} F_K(a))."""
+    X = np.array(sys.coords if coords is None else coords, np.float64)
+    nat = sys.natoms
+    F = np.zeros((nat, nat, 3))
+    aos = [np.arange(sys.atom_ao0[a], sys.atom_ao0[a] + sys.atom_nao[a]) for a in range(nat)]
+    for K in range(nat):
+        for xyz in range(3):
+            Xf = X.copy(); Xf[K, xyz] += delta
+            Xb = X.copy(); Xb[K, xyz] -= delta
+            Sf = overlap(sys, Xf, cutoff=cutoff)
+            Sb = overlap(sys, Xb, cutoff=cutoff)
+            for L in range(K + 1, nat):
+                if not np.sqrt(((X[K] - X[L]) ** 2).sum()) < cutoff:
+                    continue
+                g = (Sf[np.ix_(aos[L], aos[K])] - Sb[np.ix_(aos[L], aos[K])]) / (2.0 * delta)
+                F[K, L, xyz] = -(g * kernel[np.ix_(aos[K], aos[L])].T).sum()
+    force = np.zeros((nat, 3))
+    for a in range(nat):
+        force[a] = F[a, a + 1:].sum(0) - F[:a, a].sum(0)
+    return 2.0 * 1.602176565e-9 * force

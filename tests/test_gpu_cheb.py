@@ -72,6 +72,47 @@ def test_cheb_fp64_moving_nuclei_vs_taylor_oracle(elhl, oracle_mod):
     assert np.abs(pops - rp).max() < 1e-9
 
 
+@pytest.mark.parametrize("prec_name,tol", [("fp64", 1e-11), ("fp32", 5e-6)])
+def test_implicit_operator_matches_explicit(elhl, flake, prec_name, tol):
+    """Steps given coordinates run the implicit operator G (h/b) G^T (three phases
+    per order, G = L^-1 by trtri); fixed-nuclei steps run the explicit H~.  Same
+    geometry, same result; fixed steps after moving ones keep the implicit form."""
+    prec = {"fp64": elhl.PREC_FP64, "fp32": elhl.PREC_FP32}[prec_name]
+    kw = dict(dt=1e-4, method=elhl.METHOD_CHEBYSHEV, precision=prec, ncols=4, cheb_tol=1e-14)
+    tr = elhl.Trajectory(flake, **kw)
+    tr.init_fmo(41, 40)
+    p_ex = tr.step(None, nsteps=4)
+    b_ex, k_ex = tr.get_psi()
+    tr.close()
+    tr = elhl.Trajectory(flake, coords=flake.coords, **kw)
+    tr.init_fmo(41, 40)
+    c = np.stack([flake.coords] * 2)
+    p_im = np.concatenate([tr.step(c, nsteps=2), tr.step(None, nsteps=2)])
+    b_im, k_im = tr.get_psi()
+    tr.close()
+    assert np.abs(p_im - p_ex).max() < tol
+    assert np.abs(k_im - k_ex).max() < 10 * tol and np.abs(b_im - b_ex).max() < 10 * tol
+
+
+def test_implicit_operator_cluster_vs_exact(elhl, oracle_mod):
+    """N = 1860 (600-atom cluster): every CTA owns two row chunks of the implicit
+    plan; populations after two steps through the moving-nuclei path (unchanged
+    geometry) against the exact generalized-eigenbasis propagator."""
+    sysm = systems.cubic_cluster(n_atoms=600, seed=11)
+    S = oracle_mod.overlap(sysm)
+    homo = systems.fermi_state(sysm, sysm.fragment_atoms("E"))
+    tr = elhl.Trajectory(sysm, coords=sysm.coords, dt=2e-4, method=elhl.METHOD_CHEBYSHEV,
+                         precision=elhl.PREC_FP64, ncols=4, cheb_tol=1e-14)
+    tr.init_fmo(homo + 1, homo)
+    pops = tr.step(np.stack([sysm.coords] * 2), nsteps=2)
+    tr.close()
+    ket0, _ = oracle_mod.fragment_mo(sysm, "E", homo + 1)
+    ref = _exact(oracle_mod, sysm, np.column_stack([ket0, oracle_mod.fragment_mo(sysm, "H", homo)[0]]).astype(complex),
+                 4e-4)
+    assert np.abs(pops[-1] - ref).max() < 1e-9
+    assert np.abs(pops[:, :, -1] - 1.0).max() < 1e-11
+
+
 def test_cheb_fp32_error_bound(elhl, oracle_mod, flake):
     S = oracle_mod.overlap(flake)
     bra, ket = oracle_mod.initial_states(flake, S, 41, 40)
@@ -90,19 +131,31 @@ def test_cheb_rejects_bad_config(elhl, flake):
     assert e.value.status == elhl.ERR_UNSUPPORTED
 
 
-def test_gemm_regime_fp32_matches_fp64(elhl, oracle_mod):
-    """8 FP32 ket columns run as tensor-core GEMMs per order (CUDA graph per step);
-    populations within 1e-6 of the FP64 path and of the exact propagator."""
-    sysm = systems.cubic_cluster(n_atoms=60, seed=9)
-    states = [30, 35, 38, 40, 41, 44, 47, 52]
+@pytest.mark.parametrize("prec_name", ["fp32", "bf16x3"])
+def test_gemm_regime_matches_fp64(elhl, oracle_mod, prec_name):
+    """N = 2170 with 16 ket columns: H~.Psi runs as one cuBLAS GEMM per order
+    (CUDA graph per step).  Fragment populations within 1e-6 of the FP64 path
+    and of the exact propagator over 4 steps.  The per-step total (before the
+    next step's renormalisation) is held to 2e-6: cuBLAS sums each output over
+    N = 2170 terms in one FP32 chain (measured 1.3e-6 at 8 columns; the row
+    kernel's tree sums give 2.7e-7)."""
+    prec32 = {"fp32": elhl.PREC_FP32, "bf16x3": elhl.PREC_BF16X3}[prec_name]
+    tol = 1e-6
+    sysm = systems.cubic_cluster(n_atoms=700, seed=9)
+    assert sysm.nao >= 2048
+    states = list(range(22, 54, 2))
     out = {}
-    for prec in (elhl.PREC_FP64, elhl.PREC_FP32):
-        tr = elhl.Trajectory(sysm, dt=1e-4, method=elhl.METHOD_CHEBYSHEV, precision=prec, ncols=8, nparticles=8,
-                             cheb_tol=1e-14)
+    for prec in (elhl.PREC_FP64, prec32):
+        tr = elhl.Trajectory(sysm, dt=1e-4, method=elhl.METHOD_CHEBYSHEV, precision=prec, ncols=16,
+                             nparticles=16, cheb_tol=1e-14)
         tr.init_fmo_states(states)
         out[prec] = tr.step(None, nsteps=4)
+        if prec == prec32:
+            assert tr.stats().tile_cols == 0  # GEMM regime
         tr.close()
-    assert np.abs(out[elhl.PREC_FP32] - out[elhl.PREC_FP64]).max() < 1e-6
+    err = np.abs(out[prec32] - out[elhl.PREC_FP64])
+    assert err[:, :, :-1].max() < tol
+    assert err[:, :, -1].max() < 2 * tol
     S = oracle_mod.overlap(sysm)
     h = oracle_mod.huckel(sysm, S)
     ex = oracle_mod.ExactPropagator(S, h)
@@ -110,4 +163,4 @@ def test_gemm_regime_fp32_matches_fp64(elhl, oracle_mod):
         ket0, _ = oracle_mod.fragment_mo(sysm, "E", st)
         ref = oracle_mod.exact_populations(sysm, S, ex.ket(ket0.astype(complex), 4e-4))
         assert np.abs(out[elhl.PREC_FP64][-1, c] - ref).max() < 1e-10
-        assert np.abs(out[elhl.PREC_FP32][-1, c] - ref).max() < 1e-6
+        assert np.abs(out[prec32][-1, c, :-1] - ref[:-1]).max() < tol

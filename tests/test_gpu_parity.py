@@ -193,3 +193,20 @@ def test_energies_match_oracle(elhl, oracle_mod, flake, method):
     E = tr.energies()
     tr.close()
     assert np.abs(E - Eo).max() < 1e-9
+
+
+def test_ehrenfest_kernels(elhl, oracle_mod, flake):
+    """ehrenfestkernel_gpu_ / ehrenfestkernel2_gpu_ against the oracle (FP64 DGEMM, 1e-10 relative)."""
+    rng = np.random.default_rng(4)
+    S = oracle_mod.overlap(flake)
+    h = oracle_mod.huckel(flake, S)
+    Hp = oracle_mod.h_prime(oracle_mod.sy_invert(S), h)
+    X = rng.normal(size=Hp.shape)
+    A = rng.normal(size=Hp.shape)
+    K = elhl.ehrenfest_kernel(Hp, X, A=A)
+    Ko = oracle_mod.ehrenfest_kernel(Hp, X, A=A)
+    assert np.abs(K - Ko).max() < 1e-10 * np.abs(Ko).max()
+    bra, ket = oracle_mod.initial_states(flake, S, 41, 40)
+    K2 = elhl.ehrenfest_kernel(Hp, X, bra=bra, ket=ket)
+    K2o = oracle_mod.ehrenfest_kernel(Hp, X, bra=bra, ket=ket)
+    assert np.abs(K2 - K2o).max() < 1e-10 * np.abs(K2o).max()

@@ -181,3 +181,20 @@ def test_no_convergence_is_bounded(oracle_mod):
     v = np.array([1.0 + 0j, 0, 0])
     _, _, _, _, st = oracle_mod.propagate(Hp, v, v, 0.0, 1e-4, 0.15, max_conv_calls=5)
     assert st.status == 1 and st.conv_calls == 5
+
+
+def test_pulay_forces_h2_closed_form(oracle_mod):
+    """Two H 1s STOs (equal zeta): S(R) = e^{-zR}(1 + zR + (zR)^2/3); with
+    kernel(0, 1) = kernel(1, 0) = 1 the force on atom 0 is
+    2 e2N (-dS/dx_0) and on atom 1 its negative."""
+    sysm = two_atom("H", "H", [0.74, 0.21, -0.13])
+    X = sysm.coords
+    kern = np.array([[0.0, 1.0], [1.0, 0.0]])
+    f = oracle_mod.pulay_forces(sysm, kern, delta=1e-5)
+    z = sysm.ao_zeta[0, 0]
+    R = np.linalg.norm(X[1] - X[0])
+    dS_dR = -z * np.exp(-z * R) * (1 + z * R + (z * R) ** 2 / 3) + np.exp(-z * R) * (z + 2 * z * z * R / 3)
+    dS_dx0 = dS_dR * (X[0] - X[1]) / R
+    ref0 = 2 * 1.602176565e-9 * (-dS_dx0)
+    assert np.abs(f[0] - ref0).max() < 1e-8 * np.abs(ref0).max()
+    assert np.abs(f[0] + f[1]).max() < 1e-20
