@@ -47,6 +47,8 @@ def workload(name: str):
         return systems.honeycomb_flake(), 1.0e-4, False
     if name == "small":       # quick check: 300-atom cluster, moving nuclei
         return systems.cubic_cluster(n_atoms=300, seed=2), 5.0e-4, True
+    if name == "medium":      # profiling case: 900-atom cluster (N = 2790), G + h + G^T above L2
+        return systems.cubic_cluster(n_atoms=900, seed=2), 5.0e-4, True
     raise ValueError(name)
 
 
@@ -55,6 +57,7 @@ WORKLOAD_DESC = {
                  "(sigma 0.02 A per step), dt 0.5 fs, S, h, Cholesky and L^-1 rebuilt every step, el+hl bra/ket",
     "flake": "C100H50 honeycomb flake (sigma 0.03 A), fixed nuclei, dt 0.1 fs, el+hl bra/ket",
     "small": "C/H/O cluster 300 atoms, moving nuclei, dt 0.5 fs, el+hl bra/ket",
+    "medium": "C/H/O cluster 900 atoms, moving nuclei, dt 0.5 fs, el+hl bra/ket",
 }
 
 
@@ -178,7 +181,7 @@ def run_ours(args, rank, world):
     clocks = ClockSampler()
     clocks.start()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-    prop_ms = rebuild_ms = 0.0
+    prop_ms = rebuild_ms = sh_ms = factor_ms = inverse_ms = 0.0
     orders = launches = 0
     torch.cuda.synchronize(dev)
     for i in range(K):
@@ -189,6 +192,9 @@ def run_ours(args, rank, world):
         st = tr.stats()
         prop_ms += st.prop_ms
         rebuild_ms += st.rebuild_ms
+        sh_ms += st.sh_ms
+        factor_ms += st.factor_ms
+        inverse_ms += st.inverse_ms
         orders += st.orders
         launches += st.prop_launches + st.rebuild_count
     tile = {"tile_cols": st.tile_cols, "phases": st.phases} if method == api.METHOD_CHEBYSHEV else {}
@@ -277,7 +283,11 @@ def run_ours(args, rank, world):
                              "pipe": "fp64 FMA" if args.precision == "fp64" else "fp32 FMA",
                              "peak_source": "of measured (FMA probe, profiles/gb300_peaks_probe.md)"},
                      "orders_per_launch": per_launch_orders, "launch_ms": prop_launch_ms},
-        "breakdown_ms_per_step": {"propagation": prop_ms / K, "rebuild_S_h_operator": rebuild_ms / K},
+        "breakdown_ms_per_step": {"propagation": prop_ms / K, "rebuild_S_h_operator": rebuild_ms / K,
+                                  "rebuild_parts": {"S_h_build": sh_ms / K, "cholesky": factor_ms / K,
+                                                    "inverse_L": inverse_ms / K,
+                                                    "bounds_columns_other": (rebuild_ms - sh_ms - factor_ms
+                                                                             - inverse_ms) / K}},
         "clocks": clk,
     }
     return line

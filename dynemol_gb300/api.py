@@ -65,7 +65,8 @@ class TrajStats(ctypes.Structure):
                 ("save_tau", ctypes.c_double * 2), ("t", ctypes.c_double), ("it", ctypes.c_int),
                 ("status", ctypes.c_int), ("prop_ms", ctypes.c_double), ("rebuild_ms", ctypes.c_double),
                 ("prop_launches", ctypes.c_int), ("rebuild_count", ctypes.c_int), ("tile_cols", ctypes.c_int),
-                ("phases", ctypes.c_int)]
+                ("phases", ctypes.c_int), ("sh_ms", ctypes.c_double), ("factor_ms", ctypes.c_double),
+                ("inverse_ms", ctypes.c_double)]
 
 
 class Request(ctypes.Structure):

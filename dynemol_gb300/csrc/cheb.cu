@@ -101,8 +101,10 @@ __device__ void rows_gemv(const T *M, int ld, const typename Vec2<T>::type *s_v,
 #pragma unroll
         for (int r = 0; r < kRT; ++r) cols[r] = M + (size_t)min(r0 + r, row1 - 1) * ld;
         // two j positions per iteration: the 2 x kRT column loads are issued before
-        // the FMAs that consume them (more L2 requests in flight per warp)
-        int j = j0 + lane;
+        // the FMAs that consume them (more L2 requests in flight per warp).  Warps
+        // whose tile lies past row1 skip the loop (a warp-uniform branch, so their
+        // FMAs are not issued at all).
+        int j = nr > 0 ? j0 + lane : j1;
         for (; j + 32 < j1; j += 64) {
             T h0[kRT], h1[kRT];
 #pragma unroll

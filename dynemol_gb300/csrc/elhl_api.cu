@@ -80,10 +80,22 @@ struct Context {
     unsigned *bar = nullptr;  // [2] count, gen
     int *err = nullptr;
     double *partials = nullptr;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};  // prop begin/end, rebuild begin/end
+    // 0/1 propagation begin/end, 2/3 rebuild begin/end, 4 S/h built, 5 factorised, 6 inverse formed
+    cudaEvent_t ev[7] = {};
     std::mutex mu;
 };
 Context g_ctx;
+
+// Copies ordered with the library stream.  The library's streams are created
+// non-blocking, so a plain cudaMemcpy (legacy default stream) is not ordered
+// with their work; device-to-host copies also wait for the data.
+cudaError_t copy_h2d(void *dst, const void *src, size_t bytes) {
+    return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, g_ctx.stream);
+}
+cudaError_t copy_d2h(void *dst, const void *src, size_t bytes) {
+    cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, g_ctx.stream);
+    return e != cudaSuccess ? e : cudaStreamSynchronize(g_ctx.stream);
+}
 
 int ensure_context_locked(int device) {
     if (g_ctx.ready && (device < 0 || device == g_ctx.device)) return ELHL_OK;
@@ -237,9 +249,10 @@ struct Factor {
         return ELHL_OK;
     }
     // status words of the last potrf (info[0]) and, with solves, potrs (info[1])
-    int check_info(bool with_solve = true) {
+    int check_info(bool with_solve = true) {  // waits for the factorisation on the library stream
         int h[2] = {0, 0};
-        CU_TRY(cudaMemcpy(h, info, 2 * sizeof(int), cudaMemcpyDeviceToHost));
+        CU_TRY(cudaMemcpyAsync(h, info, 2 * sizeof(int), cudaMemcpyDeviceToHost, g_ctx.stream));
+        CU_TRY(cudaStreamSynchronize(g_ctx.stream));
         if (h[0] > 0) return ELHL_ERR_NOT_POSITIVE_DEFINITE;
         if (h[0] < 0 || (with_solve && h[1] != 0)) return ELHL_ERR_BAD_ARG;
         return ELHL_OK;
@@ -562,7 +575,7 @@ struct ChebState {
         if (int rc = dev_alloc(&lz, (size_t)4 * ld)) return rc;
         if (int rc = dev_alloc(&scale, (size_t)kMaxCols)) return rc;
         std::vector<double> ones(kMaxCols, 1.0);
-        CU_TRY(cudaMemcpy(scale, ones.data(), kMaxCols * sizeof(double), cudaMemcpyHostToDevice));
+        CU_TRY(copy_h2d(scale, ones.data(), kMaxCols * sizeof(double)));
         return ELHL_OK;
     }
     void release() {
@@ -822,6 +835,7 @@ int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, do
         CU_TRY(cudaMemset(cs.wb, 0, (size_t)2 * ld * cs.m * 2 * tsz));
     }
     if (int rc = invert_factor(cs, Lfac, cs.Ht)) return rc;
+    CU_TRY(cudaEventRecord(g_ctx.ev[6], st));
     lower_only_kernel<<<dim3((ld + 127) / 128, n), 128, 0, st>>>(cs.Ht, n, ld);
     CU_TRY(cudaGetLastError());
     if (int rc = lanczos_bounds(cs, 40, h)) return rc;
@@ -1086,14 +1100,14 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
     for (size_t i = 0; i < pl.segs.size(); ++i) pl.prob_seg0[pl.segs[i].prob + 1] = (int)i + 1;
     for (size_t q = 1; q <= states.size(); ++q) pl.prob_seg0[q] = std::max(pl.prob_seg0[q], pl.prob_seg0[q - 1]);
     if (int rc = dev_alloc(&pl.d_prob_seg0, pl.prob_seg0.size())) return rc;
-    CU_TRY(cudaMemcpy(pl.d_prob_seg0, pl.prob_seg0.data(), pl.prob_seg0.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CU_TRY(copy_h2d(pl.d_prob_seg0, pl.prob_seg0.data(), pl.prob_seg0.size() * sizeof(int)));
     if (int rc = dev_alloc(&pl.d_seg_pops, pl.segs.size() * kMaxCols * (kMaxFrag + 1))) return rc;
     if (int rc = dev_alloc(&pl.d_probs, pl.probs.size())) return rc;
     if (int rc = dev_alloc(&pl.d_segs, pl.segs.size())) return rc;
     if (int rc = dev_alloc(&pl.d_seg_begin, pl.seg_begin.size())) return rc;
-    CU_TRY(cudaMemcpy(pl.d_probs, pl.probs.data(), pl.probs.size() * sizeof(ChebProblem), cudaMemcpyHostToDevice));
-    CU_TRY(cudaMemcpy(pl.d_segs, pl.segs.data(), pl.segs.size() * sizeof(ChebSegment), cudaMemcpyHostToDevice));
-    CU_TRY(cudaMemcpy(pl.d_seg_begin, pl.seg_begin.data(), pl.seg_begin.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CU_TRY(copy_h2d(pl.d_probs, pl.probs.data(), pl.probs.size() * sizeof(ChebProblem)));
+    CU_TRY(copy_h2d(pl.d_segs, pl.segs.data(), pl.segs.size() * sizeof(ChebSegment)));
+    CU_TRY(copy_h2d(pl.d_seg_begin, pl.seg_begin.data(), pl.seg_begin.size() * sizeof(int)));
     return tune_plan(pl, mgcd);
 }
 
@@ -1107,7 +1121,7 @@ int cheb_plan_refresh(ChebPlan &pl, const std::vector<ChebState *> &states) {
         if (states[q]->implicit) pl.probs[q].shift = states[q]->a / states[q]->b;
         pl.kmax = std::max(pl.kmax, states[q]->K);
     }
-    CU_TRY(cudaMemcpy(pl.d_probs, pl.probs.data(), pl.probs.size() * sizeof(ChebProblem), cudaMemcpyHostToDevice));
+    CU_TRY(copy_h2d(pl.d_probs, pl.probs.data(), pl.probs.size() * sizeof(ChebProblem)));
     return ELHL_OK;
 }
 
@@ -1169,7 +1183,7 @@ int tune_plan(ChebPlan &pl, int mgcd) {
         CU_TRY(cudaEventSynchronize(g_ctx.ev[1]));
         CU_TRY(cudaEventElapsedTime(&ms, g_ctx.ev[0], g_ctx.ev[1]));
         int err = 0;
-        CU_TRY(cudaMemcpy(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost));
+        CU_TRY(copy_d2h(&err, g_ctx.err, sizeof(int)));
         if (err) return err;
         if (ms < best) {
             best = ms;
@@ -1387,12 +1401,12 @@ int upload_basis(DevBasis &d, const elhl_basis_desc *b) {
     d.nfrag = b->nfrag;
     auto up_i = [](int **dst, const int *src, size_t n) -> int {
         if (int rc = dev_alloc(dst, n)) return rc;
-        CU_TRY(cudaMemcpy(*dst, src, n * sizeof(int), cudaMemcpyHostToDevice));
+        CU_TRY(copy_h2d(*dst, src, n * sizeof(int)));
         return ELHL_OK;
     };
     auto up_d = [](double **dst, const double *src, size_t n) -> int {
         if (int rc = dev_alloc(dst, n)) return rc;
-        CU_TRY(cudaMemcpy(*dst, src, n * sizeof(double), cudaMemcpyHostToDevice));
+        CU_TRY(copy_h2d(*dst, src, n * sizeof(double)));
         return ELHL_OK;
     };
     int rc = 0;
@@ -1456,6 +1470,7 @@ int cheb_rebuild_operator(elhl_traj *tr, bool implicit = false) {
                              tr->N, cudaMemcpyDeviceToDevice, st));
     SOLVER_TRY(cusolverDnDpotrf(g_ctx.solver, CUBLAS_FILL_MODE_LOWER, tr->N, tr->fac.L, tr->ld, tr->fac.work,
                                 tr->fac.lwork, tr->fac.info));
+    CU_TRY(cudaEventRecord(g_ctx.ev[5], st));
     if (int rc = tr->fac.check_info(false)) return rc;
     if (implicit)
         return cheb_prepare_implicit(tr->cs, tr->fac.L, tr->h, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol);
@@ -1574,6 +1589,7 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
                 rc = ELHL_ERR_CUDA;
                 break;
             }
+            if (cudaEventRecord(g_ctx.ev[4], st) != cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
             if ((rc = cheb_rebuild_operator(tr, true))) break;  // implicit: A, B follow the new L
             if ((rc = cheb_load_columns(tr))) break;
             if (cudaEventRecord(g_ctx.ev[3], st) != cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
@@ -1599,6 +1615,9 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
         tr->stats.orders += (long long)cs.K * cs.m;
         if (coords) {
             tr->stats.rebuild_ms += event_ms(2, 3);
+            tr->stats.sh_ms += event_ms(2, 4);
+            tr->stats.factor_ms += event_ms(4, 5);
+            tr->stats.inverse_ms += event_ms(5, 6);
             tr->stats.rebuild_count += 1;
         }
         tr->stats.substeps += 1;
@@ -1645,7 +1664,7 @@ int traj_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
         tr->stats.phases = tr->plan.nphase;
         if (rc) return rc;
         if (pops && !pops_on_device)
-            CU_TRY(cudaMemcpy(pops, d_pops, nsteps * pop_per_step * sizeof(double), cudaMemcpyDeviceToHost));
+            CU_TRY(copy_d2h(pops, d_pops, nsteps * pop_per_step * sizeof(double)));
         return ELHL_OK;
     }
     if (!coords) {
@@ -1714,7 +1733,7 @@ int traj_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
         }
     }
     if (pops && !pops_on_device)
-        CU_TRY(cudaMemcpy(pops, d_pops, nsteps * pop_per_step * sizeof(double), cudaMemcpyDeviceToHost));
+        CU_TRY(copy_d2h(pops, d_pops, nsteps * pop_per_step * sizeof(double)));
     return ELHL_OK;
 }
 
@@ -1741,7 +1760,7 @@ int fmo_particle(elhl_traj *tr, int nat, const int *atoms, int state, double2 *k
     if (state > nf) return ELHL_ERR_BAD_ARG;
     // fragment coordinates gathered from the current device coordinates
     std::vector<double> all((size_t)tr->natoms * 3), sub((size_t)nat * 3);
-    CU_TRY(cudaMemcpy(all.data(), tr->last_coords, all.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    CU_TRY(copy_d2h(all.data(), tr->last_coords, all.size() * sizeof(double)));
     for (int a = 0; a < nat; ++a)
         for (int k = 0; k < 3; ++k) sub[3 * a + k] = all[3 * (size_t)atoms[a] + k];
     elhl_basis_desc d{};
@@ -1760,8 +1779,8 @@ int fmo_particle(elhl_traj *tr, int nat, const int *atoms, int state, double2 *k
     if (!rc) rc = dev_alloc(&dc, sub.size());
     if (!rc) rc = dev_alloc(&info, 1);
     if (!rc) rc = dev_alloc(&daos, (size_t)nf);
-    if (!rc && cudaMemcpy(dc, sub.data(), sub.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) rc = ELHL_ERR_CUDA;
-    if (!rc && cudaMemcpy(daos, aos.data(), nf * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) rc = ELHL_ERR_CUDA;
+    if (!rc && copy_h2d(dc, sub.data(), sub.size() * sizeof(double)) != cudaSuccess) rc = ELHL_ERR_CUDA;
+    if (!rc && copy_h2d(daos, aos.data(), nf * sizeof(int)) != cudaSuccess) rc = ELHL_ERR_CUDA;
     if (!rc && launch_build_sh(fb, dc, tr->cfg.cutoff, Sf, hf, ldf, st) != cudaSuccess) rc = ELHL_ERR_CUDA;
     if (!rc && cusolverDnDsygvd_bufferSize(g_ctx.solver, CUSOLVER_EIG_TYPE_1, CUSOLVER_EIG_MODE_VECTOR,
                                            CUBLAS_FILL_MODE_LOWER, nf, hf, ldf, Sf, ldf, w, &lwork) !=
@@ -1821,7 +1840,7 @@ int cheb_set_target(elhl_traj *tr) {
     dev_free(pops);
     CU_TRY(ce);
     for (int p = 0; p < P; ++p) tgt[p] = h[(size_t)p * (tr->nfrag + 1) + tr->nfrag];
-    CU_TRY(cudaMemcpy(tr->target, tgt.data(), P * sizeof(double), cudaMemcpyHostToDevice));
+    CU_TRY(copy_h2d(tr->target, tgt.data(), P * sizeof(double)));
     return ELHL_OK;
 }
 
@@ -2030,7 +2049,7 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
     if (!rc) tr->coords_cap = tr->natoms * 3;
     if (!rc) rc = tr->fac.reserve(tr->N, tr->ld);
     if (!rc && !tr->cheb()) rc = tr->tb.reserve(tr->N, tr->P);
-    if (!rc && cudaMemcpy(tr->coords, coords, tr->natoms * 3 * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+    if (!rc && copy_h2d(tr->coords, coords, tr->natoms * 3 * sizeof(double)) != cudaSuccess)
         rc = ELHL_ERR_CUDA;
     if (!rc) rc = rebuild(tr, tr->coords);
     if (!rc && cudaStreamSynchronize(g_ctx.stream) != cudaSuccess) rc = ELHL_ERR_CUDA;
@@ -2162,8 +2181,8 @@ int elhl_traj_set_psi(elhl_traj *tr, const elhl_zcomplex *bra, const elhl_zcompl
     std::lock_guard<std::mutex> lk(g_ctx.mu);
     if (tr->cheb()) return cheb_set_psi(tr, bra, ket);
     for (int p = 0; p < tr->P; ++p) {
-        CU_TRY(cudaMemcpy(tr->tb.bra(p), bra + (size_t)p * tr->N, tr->N * sizeof(double2), cudaMemcpyHostToDevice));
-        CU_TRY(cudaMemcpy(tr->tb.ket(p), ket + (size_t)p * tr->N, tr->N * sizeof(double2), cudaMemcpyHostToDevice));
+        CU_TRY(copy_h2d(tr->tb.bra(p), bra + (size_t)p * tr->N, tr->N * sizeof(double2)));
+        CU_TRY(copy_h2d(tr->tb.ket(p), ket + (size_t)p * tr->N, tr->N * sizeof(double2)));
     }
     return ELHL_OK;
 }
@@ -2181,8 +2200,8 @@ int elhl_traj_get_psi(elhl_traj *tr, elhl_zcomplex *bra, elhl_zcomplex *ket) {
         return ELHL_OK;
     }
     for (int p = 0; p < tr->P; ++p) {
-        if (bra) CU_TRY(cudaMemcpy(bra + (size_t)p * tr->N, tr->tb.bra(p), tr->N * sizeof(double2), cudaMemcpyDeviceToHost));
-        if (ket) CU_TRY(cudaMemcpy(ket + (size_t)p * tr->N, tr->tb.ket(p), tr->N * sizeof(double2), cudaMemcpyDeviceToHost));
+        if (bra) CU_TRY(copy_d2h(bra + (size_t)p * tr->N, tr->tb.bra(p), tr->N * sizeof(double2)));
+        if (ket) CU_TRY(copy_d2h(ket + (size_t)p * tr->N, tr->tb.ket(p), tr->N * sizeof(double2)));
     }
     return ELHL_OK;
 }
@@ -2320,7 +2339,7 @@ int elhl_batch_step(elhl_batch *b, int nsteps, double *pops) {
     b->stats.phases = b->plan.nphase;
     for (auto *cs : b->states) b->stats.orders += (long long)cs->K * cs->m * nsteps;
     b->stats.substeps += (long long)nt * nsteps;
-    if (pops) CU_TRY(cudaMemcpy(pops, b->pops, per_step * nsteps * sizeof(double), cudaMemcpyDeviceToHost));
+    if (pops) CU_TRY(copy_d2h(pops, b->pops, per_step * nsteps * sizeof(double)));
     return ELHL_OK;
 }
 
@@ -2519,7 +2538,7 @@ int elhl_server_step(elhl_server *sv, int *n_active, int *n_pending) {
             const size_t np = (size_t)r->P * (r->nfrag + 1);
             if (r->done_steps >= r->nsteps) {
                 r->pops.resize(np);
-                CU_TRY(cudaMemcpy(r->pops.data(), sv->pops + off, np * sizeof(double), cudaMemcpyDeviceToHost));
+                CU_TRY(copy_d2h(r->pops.data(), sv->pops + off, np * sizeof(double)));
                 r->psi.resize((size_t)r->nao * r->P);
                 const size_t e = sizeof(double2);
                 for (int p = 0; p < r->P; ++p)

@@ -232,6 +232,9 @@ typedef struct {
     int rebuild_count;    /* rebuilds */
     int tile_cols;        /* Chebyshev: complex columns per matrix pass chosen by the autotuner (0: GEMM regime) */
     int phases;           /* Chebyshev: grid phases per order (1 explicit H~, 3 implicit G h G^T) */
+    double sh_ms;         /* moving nuclei: device time of the S, h build */
+    double factor_ms;     /* ... of the Cholesky factorisation of S */
+    double inverse_ms;    /* ... of G = L^-1 (implicit operator) */
 } elhl_traj_stats;
 int elhl_traj_get_stats(elhl_traj *tr, elhl_traj_stats *st);
 
