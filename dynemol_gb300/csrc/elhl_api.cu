@@ -558,6 +558,7 @@ struct ChebState {
     size_t tri_dev = 0, tri_host = 0;
     std::vector<unsigned char> tri_hbuf;
     int *tinfo = nullptr;
+    double *cscratch = nullptr;  // [2m][ld] column-transform output
     int alloc(int N_, int m_, int prec) {
         N = N_;
         ld = round_up(N, 32);
@@ -572,7 +573,7 @@ struct ChebState {
         if (int rc = dev_alloc(&acc, (size_t)ld * m)) return rc;
         CU_TRY(cudaMemset(phi, 0, (size_t)ld * m * sizeof(double2)));
         CU_TRY(cudaMemset(acc, 0, (size_t)ld * m * sizeof(double2)));
-        if (int rc = dev_alloc(&lz, (size_t)4 * ld)) return rc;
+        if (int rc = dev_alloc(&lz, (size_t)4 * ld + 128)) return rc;  // 4 vectors + the tridiagonal record
         if (int rc = dev_alloc(&scale, (size_t)kMaxCols)) return rc;
         std::vector<double> ones(kMaxCols, 1.0);
         CU_TRY(copy_h2d(scale, ones.data(), kMaxCols * sizeof(double)));
@@ -592,6 +593,7 @@ struct ChebState {
         Gt = wb = tri_ws = nullptr;
         tri_dev = tri_host = 0;
         dev_free(tinfo);
+        dev_free(cscratch);
         implicit = false;
         dev_free(gpops);
         dev_free(Ht); dev_free(phi); dev_free(acc); dev_free(coef); dev_free(lz); dev_free(scale);
@@ -626,55 +628,101 @@ __global__ void lanczos_start(double *v, int n) {
     if (i < n) v[i] = 1.0 + 0.5 * sin(1.37 * i + 0.2);  // deterministic, every component present
 }
 
+constexpr int kLzBlock = 1024;
+
+// sum over the block in a fixed order (every thread returns it)
+__device__ double lz_block_sum(double x, double *s) {
+    const int t = threadIdx.x;
+    s[t] = x;
+    __syncthreads();
+    for (int o = kLzBlock / 2; o > 0; o >>= 1) {
+        if (t < o) s[t] += s[t + o];
+        __syncthreads();
+    }
+    const double r = s[0];
+    __syncthreads();
+    return r;
+}
+
+// v <- v / |v| (one block)
+__global__ void __launch_bounds__(kLzBlock) lanczos_normalize_kernel(double *v, int n) {
+    __shared__ double s[kLzBlock];
+    double a = 0.0;
+    for (int i = threadIdx.x; i < n; i += kLzBlock) a += v[i] * v[i];
+    const double inv = 1.0 / sqrt(lz_block_sum(a, s));
+    for (int i = threadIdx.x; i < n; i += kLzBlock) v[i] *= inv;
+}
+
+// One Lanczos update after w = H v (one block, fixed-order sums):
+//   alpha_j = w.v, w <- w - alpha_j v - beta_{j-1} vp, beta_j = |w|,
+//   vp <- v, v <- w / beta_j.
+// rec[0..k) alpha, rec[k..2k) beta, rec[2k] = steps used once the recursion
+// breaks down (beta ~ 0), after which later updates do nothing.
+__global__ void __launch_bounds__(kLzBlock) lanczos_update_kernel(double *v, double *vp, double *w, int n,
+                                                                  double *rec, int k, int j) {
+    __shared__ double s[kLzBlock];
+    if (rec[2 * k] > 0.0) return;
+    double a = 0.0;
+    for (int i = threadIdx.x; i < n; i += kLzBlock) a += w[i] * v[i];
+    a = lz_block_sum(a, s);
+    const double bprev = j > 0 ? rec[k + j - 1] : 0.0;
+    double b = 0.0;
+    for (int i = threadIdx.x; i < n; i += kLzBlock) {
+        const double x = w[i] - a * v[i] - bprev * vp[i];
+        w[i] = x;
+        b += x * x;
+    }
+    b = sqrt(lz_block_sum(b, s));
+    if (threadIdx.x == 0) {
+        rec[j] = a;
+        rec[k + j] = b;
+        if (!(b > 1e-10 * (fabs(a) + 1.0))) rec[2 * k] = j + 1;
+    }
+    if (!(b > 1e-10 * (fabs(a) + 1.0))) return;
+    const double ib = 1.0 / b;
+    for (int i = threadIdx.x; i < n; i += kLzBlock) {
+        vp[i] = v[i];
+        v[i] = w[i] * ib;
+    }
+}
+
 // Spectral bounds of H~ by FP64 Lanczos (k steps, no reorthogonalisation) with
 // a guard of |beta_k s_k| + 1 % of the width around the extreme Ritz values.
-// h == nullptr: H~ is cs.Ht; otherwise H~ v = G h G^T v with G = L^-1 in cs.Ht.
+// h == nullptr: H~ is cs.Ht; otherwise H~ v = G h G^T v with G = L^-1 in cs.Ht
+// (zero upper triangle: plain GEMVs).  The recursion runs on the device without
+// host round trips; the tridiagonal matrix is read back once.
 int lanczos_bounds(ChebState &cs, int ksteps, const double *h = nullptr) {
     const int n = cs.N;
     cudaStream_t st = g_ctx.stream;
     double *v = cs.lz, *vp = cs.lz + cs.ld, *w = cs.lz + 2 * cs.ld, *t = cs.lz + 3 * cs.ld;
+    const int k = std::min(std::min(ksteps, n), 63);
+    double *rec = cs.lz + 4 * cs.ld;  // [2k + 1] <= 127 doubles
     lanczos_start<<<(n + 255) / 256, 256, 0, st>>>(v, n);
     CU_TRY(cudaMemsetAsync(vp, 0, n * sizeof(double), st));
-    double nrm = 0.0;
-    BLAS_TRY(cublasDnrm2(g_ctx.blas, n, v, 1, &nrm));
-    double inv = 1.0 / nrm;
-    BLAS_TRY(cublasDscal(g_ctx.blas, n, &inv, v, 1));
-    const int k = std::min(ksteps, n);
-    std::vector<double> alpha(k), beta(k);
-    double bprev = 0.0;
-    int used = 0;
+    CU_TRY(cudaMemsetAsync(rec, 0, (2 * k + 1) * sizeof(double), st));
+    lanczos_normalize_kernel<<<1, kLzBlock, 0, st>>>(v, n);
     const double one = 1.0, zero = 0.0;
     for (int j = 0; j < k; ++j) {
-        if (h) {  // cs.Ht = G with a zero upper triangle: plain GEMVs (trmv is column-sequential)
+        if (h) {
             BLAS_TRY(cublasDgemv(g_ctx.blas, CUBLAS_OP_T, n, n, &one, cs.Ht, cs.ld, v, 1, &zero, t, 1));  // G^T v
             BLAS_TRY(cublasDgemv(g_ctx.blas, CUBLAS_OP_N, n, n, &one, h, cs.ld, t, 1, &zero, w, 1));      // h (.)
             BLAS_TRY(cublasDgemv(g_ctx.blas, CUBLAS_OP_N, n, n, &one, cs.Ht, cs.ld, w, 1, &zero, t, 1));  // G (.)
-            std::swap(w, t);
+            lanczos_update_kernel<<<1, kLzBlock, 0, st>>>(v, vp, t, n, rec, k, j);
         } else {
             BLAS_TRY(cublasDsymv(g_ctx.blas, CUBLAS_FILL_MODE_LOWER, n, &one, cs.Ht, cs.ld, v, 1, &zero, w, 1));
+            lanczos_update_kernel<<<1, kLzBlock, 0, st>>>(v, vp, w, n, rec, k, j);
         }
-        double al = 0.0;
-        BLAS_TRY(cublasDdot(g_ctx.blas, n, w, 1, v, 1, &al));
-        const double mal = -al, mb = -bprev;
-        BLAS_TRY(cublasDaxpy(g_ctx.blas, n, &mal, v, 1, w, 1));
-        BLAS_TRY(cublasDaxpy(g_ctx.blas, n, &mb, vp, 1, w, 1));
-        double be = 0.0;
-        BLAS_TRY(cublasDnrm2(g_ctx.blas, n, w, 1, &be));
-        alpha[j] = al;
-        beta[j] = be;
-        used = j + 1;
-        if (!(be > 1e-10 * (std::fabs(al) + 1.0))) break;
-        std::swap(vp, v);  // vp <- v
-        const double ib = 1.0 / be;
-        BLAS_TRY(cublasDcopy(g_ctx.blas, n, w, 1, v, 1));
-        BLAS_TRY(cublasDscal(g_ctx.blas, n, &ib, v, 1));
-        bprev = be;
     }
+    CU_TRY(cudaGetLastError());
+    std::vector<double> r(2 * k + 1);
+    CU_TRY(copy_d2h(r.data(), rec, r.size() * sizeof(double)));
+    const int used = r[2 * k] > 0.0 ? (int)r[2 * k] : k;
+    const double *alpha = r.data(), *beta = r.data() + k;
     double lo = 0.0, hi = 0.0;
-    tridiagonal_extremes(alpha.data(), beta.data(), used, &lo, &hi);
+    tridiagonal_extremes(alpha, beta, used, &lo, &hi);
     const double bk = beta[used - 1];
-    const double rlo = bk * tridiagonal_last_component(alpha.data(), beta.data(), used, lo);
-    const double rhi = bk * tridiagonal_last_component(alpha.data(), beta.data(), used, hi);
+    const double rlo = bk * tridiagonal_last_component(alpha, beta, used, lo);
+    const double rhi = bk * tridiagonal_last_component(alpha, beta, used, hi);
     const double width = hi - lo;
     cs.emin = lo - rlo - 0.01 * width;
     cs.emax = hi + rhi + 0.01 * width;
@@ -740,6 +788,40 @@ __global__ void convert_kernel(const double *__restrict__ src, T *__restrict__ d
 // triangular-times-square products (cuSOLVER's own trtri at N = 3720 spends
 // most of its time in 32 x 32 tiles).
 constexpr int kTriBase = 512;
+constexpr int kTrmmBase = 256;
+
+// In-place triangular products with the lower-triangular T (ld), recursively:
+// large blocks become DGEMMs (cuBLAS DTRMM at these sizes runs on 32 x 32
+// tiles), blocks of at most kTrmmBase rows use DTRMM.
+//   right: X (m x n) <- alpha X T,  T n x n:  [X1 X2] T = [X1 T11 + X2 T21, X2 T22]
+int trmm_right(double alpha, const double *T, int ldt, double *X, int ldx, int m, int n) {
+    if (n <= kTrmmBase) {
+        BLAS_TRY(cublasDtrmm(g_ctx.blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT,
+                             m, n, &alpha, T, ldt, X, ldx, X, ldx));
+        return ELHL_OK;
+    }
+    const int n1 = (n / 2 + 63) / 64 * 64, n2 = n - n1;
+    const double one = 1.0;
+    if (int rc = trmm_right(alpha, T, ldt, X, ldx, m, n1)) return rc;  // X1 T11
+    BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, m, n1, n2, &alpha, X + (size_t)n1 * ldx, ldx, T + n1,
+                         ldt, &one, X, ldx));                            // + X2 T21
+    return trmm_right(alpha, T + (size_t)n1 * ldt + n1, ldt, X + (size_t)n1 * ldx, ldx, m, n2);  // X2 T22
+}
+
+//   left: X (m x n) <- alpha T X,  T m x m:  T [X1; X2] = [T11 X1; T21 X1 + T22 X2]
+int trmm_left(double alpha, const double *T, int ldt, double *X, int ldx, int m, int n) {
+    if (m <= kTrmmBase) {
+        BLAS_TRY(cublasDtrmm(g_ctx.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT,
+                             m, n, &alpha, T, ldt, X, ldx, X, ldx));
+        return ELHL_OK;
+    }
+    const int m1 = (m / 2 + 63) / 64 * 64, m2 = m - m1;
+    const double one = 1.0;
+    if (int rc = trmm_left(alpha, T + (size_t)m1 * ldt + m1, ldt, X + m1, ldx, m2, n)) return rc;  // T22 X2
+    BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, m2, n, m1, &alpha, T + m1, ldt, X, ldx, &one, X + m1,
+                         ldx));                                          // + T21 X1
+    return trmm_left(alpha, T, ldt, X, ldx, m1, n);                     // T11 X1
+}
 
 int tri_inverse(ChebState &cs, double *A, int n, int ld) {
     if (n <= kTriBase) {
@@ -765,12 +847,8 @@ int tri_inverse(ChebState &cs, double *A, int n, int ld) {
     double *A11 = A, *A21 = A + n1, *A22 = A + (size_t)n1 * ld + n1;
     if (int rc = tri_inverse(cs, A11, n1, ld)) return rc;
     if (int rc = tri_inverse(cs, A22, n2, ld)) return rc;
-    const double m1 = -1.0, one = 1.0;
-    BLAS_TRY(cublasDtrmm(g_ctx.blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n2,
-                         n1, &m1, A11, ld, A21, ld, A21, ld));  // -L21 G11
-    BLAS_TRY(cublasDtrmm(g_ctx.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n2,
-                         n1, &one, A22, ld, A21, ld, A21, ld));  // G22 (.)
-    return ELHL_OK;
+    if (int rc = trmm_right(-1.0, A11, ld, A21, ld, n2, n1)) return rc;  // -L21 G11
+    return trmm_left(1.0, A22, ld, A21, ld, n2, n1);                     // G22 (.)
 }
 
 // G = L^-1 (FP64, lower; the upper triangle keeps what dst held) from a copy of
@@ -834,6 +912,11 @@ int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, do
         CU_TRY(cudaMalloc(&cs.wb, (size_t)2 * ld * cs.m * 2 * tsz));
         CU_TRY(cudaMemset(cs.wb, 0, (size_t)2 * ld * cs.m * 2 * tsz));
     }
+    if (!cs.cscratch)
+        if (int rc = dev_alloc(&cs.cscratch, (size_t)2 * cs.m * ld)) return rc;
+    // L with a zero upper triangle (potrf leaves S there): the dense column transforms read all of it
+    lower_only_kernel<<<dim3((ld + 127) / 128, n), 128, 0, st>>>(const_cast<double *>(Lfac), n, ld);
+    CU_TRY(cudaGetLastError());
     if (int rc = invert_factor(cs, Lfac, cs.Ht)) return rc;
     CU_TRY(cudaEventRecord(g_ctx.ev[6], st));
     lower_only_kernel<<<dim3((ld + 127) / 128, n), 128, 0, st>>>(cs.Ht, n, ld);
@@ -1295,6 +1378,23 @@ int cols_apply(const double *Lfac, int ld, int n, double2 *cols, int m, int col0
     return ELHL_OK;
 }
 
+// The same four transforms with dense FP64 factors (zeros above the diagonal):
+// M = G = L^-1 for the inverse ones, M = L otherwise; one DGEMM X op(M) into
+// scratch (2 ncols x n) and a strided copy back.  The implicit operator keeps
+// both factors, and a DGEMM over a few rows costs one read of M, where a
+// right-side TRSM with 4 rows runs as a long chain of small launches.
+int cols_apply_dense(const double *L, const double *G, int ld, int n, double2 *cols, int m, int col0, int ncols,
+                     bool transpose, bool inverse, double *scratch) {
+    const double one = 1.0, zero = 0.0;
+    double *X = reinterpret_cast<double *>(cols) + 2 * col0;
+    const int rows = 2 * ncols, ldx = 2 * m;
+    BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, transpose ? CUBLAS_OP_T : CUBLAS_OP_N, rows, n, n, &one, X, ldx,
+                         inverse ? G : L, ld, &zero, scratch, rows));
+    CU_TRY(cudaMemcpy2DAsync(X, ldx * sizeof(double), scratch, rows * sizeof(double), rows * sizeof(double), n,
+                             cudaMemcpyDeviceToDevice, g_ctx.stream));
+    return ELHL_OK;
+}
+
 // ---- Ehrenfest force kernel pieces ---------------------------------------------
 // K = X o A (Hadamard), then K -= H A by one DGEMM (alpha = -1, beta = 1):
 // the K = X o A - H A of hadamard_minus (Chebyshev_gpu_kernels.cu:358-389) with
@@ -1490,6 +1590,14 @@ int cheb_load_columns(elhl_traj *tr) {
     CU_TRY(cudaMemcpy2DAsync(in, cs.m * e, tr->psi_ao, P * e, P * e, n, cudaMemcpyDeviceToDevice, st));
     if (cs.m == 2 * P)
         CU_TRY(cudaMemcpy2DAsync(in + P, cs.m * e, tr->bra_ao, P * e, P * e, n, cudaMemcpyDeviceToDevice, st));
+    if (cs.implicit) {  // dense L (zeroed upper triangle) and G = L^-1
+        if (int rc = cols_apply_dense(tr->fac.L, cs.Ht, tr->ld, n, in, cs.m, 0, P, false, false, cs.cscratch)) return rc;
+        if (cs.m == 2 * P)
+            if (int rc = cols_apply_dense(tr->fac.L, cs.Ht, tr->ld, n, in, cs.m, P, P, true, true, cs.cscratch))
+                return rc;
+        cs.cols_current = true;
+        return ELHL_OK;
+    }
     if (int rc = cols_apply(tr->fac.L, tr->ld, n, in, cs.m, 0, P, false, false)) return rc;       // L^T psi
     if (cs.m == 2 * P)
         if (int rc = cols_apply(tr->fac.L, tr->ld, n, in, cs.m, P, P, true, true)) return rc;    // L^-1 bra
@@ -1504,10 +1612,17 @@ int cheb_readout(elhl_traj *tr, const double2 *cols, double *d_pops) {
     const int P = tr->P, n = tr->N;
     const size_t e = sizeof(double2);
     CU_TRY(cudaMemcpy2DAsync(tr->psi_ao, P * e, cols, cs.m * e, P * e, n, cudaMemcpyDeviceToDevice, st));
-    if (int rc = cols_apply(tr->fac.L, tr->ld, n, tr->psi_ao, P, 0, P, false, true)) return rc;       // L^-T phi
     const double2 *bsrc = (cs.m == 2 * P) ? cols + P : cols;
     CU_TRY(cudaMemcpy2DAsync(tr->bra_ao, P * e, bsrc, cs.m * e, P * e, n, cudaMemcpyDeviceToDevice, st));
-    if (int rc = cols_apply(tr->fac.L, tr->ld, n, tr->bra_ao, P, 0, P, true, false)) return rc;       // L chi
+    if (cs.implicit) {
+        if (int rc = cols_apply_dense(tr->fac.L, cs.Ht, tr->ld, n, tr->psi_ao, P, 0, P, false, true, cs.cscratch))
+            return rc;  // L^-T phi
+        if (int rc = cols_apply_dense(tr->fac.L, cs.Ht, tr->ld, n, tr->bra_ao, P, 0, P, true, false, cs.cscratch))
+            return rc;  // L chi
+    } else {
+        if (int rc = cols_apply(tr->fac.L, tr->ld, n, tr->psi_ao, P, 0, P, false, true)) return rc;   // L^-T phi
+        if (int rc = cols_apply(tr->fac.L, tr->ld, n, tr->bra_ao, P, 0, P, true, false)) return rc;   // L chi
+    }
     if (d_pops) {
         populations_kernel<<<P, 256, 0, st>>>(tr->psi_ao, tr->bra_ao, n, P, tr->basis.ao_frag, tr->nfrag, d_pops);
         CU_TRY(cudaGetLastError());
