@@ -54,7 +54,7 @@ def workload(name: str):
 
 WORKLOAD_DESC = {
     "ehrenfest": "C/H/O cluster 1200 atoms (60/30/10%), jittered 1.4 A cubic lattice, moving nuclei "
-                 "(sigma 0.02 A per step), dt 0.5 fs, S, h, Cholesky and L^-1 rebuilt every step, el+hl bra/ket",
+                 "(sigma 0.02 A per step), dt 0.5 fs, S, h and the propagation operator rebuilt every step, el+hl bra/ket",
     "flake": "C100H50 honeycomb flake (sigma 0.03 A), fixed nuclei, dt 0.1 fs, el+hl bra/ket",
     "small": "C/H/O cluster 300 atoms, moving nuclei, dt 0.5 fs, el+hl bra/ket",
     "medium": "C/H/O cluster 900 atoms, moving nuclei, dt 0.5 fs, el+hl bra/ket",
