@@ -540,6 +540,11 @@ struct ChebState {
     float *Vf = nullptr;       // [ld][m] complex FP32 copy of the propagated columns (read-out input)
     double *gpops = nullptr;   // [P][nfrag+1] populations of the last step
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    // BF16X3 on the hand-written tcgen05 GEMM: Hs and the order's block split in three BF16 terms
+    bool umma = false;
+    int usplits = 1;           // K split of the tensor-core GEMM (partial tiles in Y)
+    __nv_bfloat16 *hsplit[3] = {nullptr, nullptr, nullptr};  // N rows of ld (Hs symmetric: row = column)
+    __nv_bfloat16 *vsplit[3] = {nullptr, nullptr, nullptr};  // 2m rows of ld (K-major block)
     double *Ht = nullptr;    // FP64 H~
     void *Hs = nullptr;      // scaled, launch precision
     void *vbuf = nullptr;
@@ -587,6 +592,12 @@ struct ChebState {
         if (Y) cudaFree(Y);
         if (Vf) cudaFree(Vf);
         Y = Vf = nullptr;
+        for (int t = 0; t < 3; ++t) {
+            if (hsplit[t]) cudaFree(hsplit[t]);
+            if (vsplit[t]) cudaFree(vsplit[t]);
+            hsplit[t] = vsplit[t] = nullptr;
+        }
+        umma = false;
         if (Gt) cudaFree(Gt);
         if (wb) cudaFree(wb);
         if (tri_ws) cudaFree(tri_ws);
@@ -764,6 +775,10 @@ int cheb_prepare(ChebState &cs, double dt, double tol, const double *h = nullptr
     CU_TRY(cudaMemcpyAsync(cs.coef, c.data(), (K + 1) * sizeof(double2), cudaMemcpyHostToDevice, st));
     CU_TRY(cudaStreamSynchronize(st));  // c is a host temporary
     cs.K = K;
+    if (cs.umma && !h) {  // the tensor-core GEMM reads Hs as three BF16 terms
+        if (int rc = split3_bf16(reinterpret_cast<const float *>(cs.Hs), cs.N, cs.N, cs.ld, cs.hsplit, cs.ld, false, st))
+            return rc;
+    }
     return ELHL_OK;
 }
 
@@ -952,18 +967,25 @@ __global__ void gemm_order0_kernel(const double2 *__restrict__ phi, const double
     acc[q] = make_double2(c0.x * p.x - c0.y * p.y, c0.x * p.y + c0.y * p.x);
 }
 
-__global__ void gemm_epilogue_kernel(const float2 *__restrict__ Y, const float2 *__restrict__ vprev2,
-                                     float2 *__restrict__ vout, double2 *__restrict__ acc, const double2 *coef, int k,
-                                     int nm) {
+// y = sum of the nsplit partial products (FP64, fixed order), v_k = 2 y - v_{k-2}
+// (v_1 = y) rounded to FP32, acc += c_k v_k in FP64
+__global__ void gemm_epilogue_kernel(const float2 *__restrict__ Y, int nsplit, size_t split_stride,
+                                     const float2 *__restrict__ vprev2, float2 *__restrict__ vout,
+                                     double2 *__restrict__ acc, const double2 *coef, int k, int nm) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nm) return;
-    const float2 y = Y[q];
+    double yx = 0.0, yy = 0.0;
+    for (int s = 0; s < nsplit; ++s) {
+        const float2 t = Y[s * split_stride + q];
+        yx += (double)t.x;
+        yy += (double)t.y;
+    }
     float2 v;
     if (k == 1) {
-        v = y;
+        v = make_float2((float)yx, (float)yy);
     } else {
         const float2 w = vprev2[q];
-        v = make_float2(2.0f * y.x - w.x, 2.0f * y.y - w.y);
+        v = make_float2((float)(2.0 * yx - (double)w.x), (float)(2.0 * yy - (double)w.y));
     }
     vout[q] = v;
     const double2 c = coef[k];
@@ -1016,11 +1038,18 @@ int cheb_gemm_enqueue(ChebState &cs, int parity) {
     const bool renorm = true;
     gemm_order0_kernel<<<nb, tb, 0, st>>>(in, renorm ? cs.scale : nullptr, cs.P, n, m, cs.c0, vb, out);
     for (int k = 1; k <= cs.K; ++k) {
-        if (int rc = gemm_vt(g_ctx.blas_tc, cs.precision, 2 * m, n,
-                             reinterpret_cast<const float *>(vb + ((k + 2) % 3) * vs),
-                             reinterpret_cast<const float *>(cs.Hs), cs.ld, cs.Y))
+        const float *vprev = reinterpret_cast<const float *>(vb + ((k + 2) % 3) * vs);
+        if (cs.umma) {  // Y (N x 2m) = Hs V^T on the tensor cores (Hs symmetric), three BF16 terms each
+            if (int rc = split3_bf16(vprev, n, 2 * m, 2 * m, cs.vsplit, cs.ld, true, st)) return rc;
+            if (int rc = umma_bf16x3_gemm(cs.hsplit, cs.ld, cs.vsplit, cs.ld, n, n, 2 * m, cs.usplits, cs.Y,
+                                          g_ctx.err, st))
+                return rc;
+        } else if (int rc = gemm_vt(g_ctx.blas_tc, cs.precision, 2 * m, n, vprev,
+                                    reinterpret_cast<const float *>(cs.Hs), cs.ld, cs.Y)) {
             return rc;
-        gemm_epilogue_kernel<<<nb, tb, 0, st>>>(reinterpret_cast<const float2 *>(cs.Y), vb + ((k + 1) % 3) * vs,
+        }
+        gemm_epilogue_kernel<<<nb, tb, 0, st>>>(reinterpret_cast<const float2 *>(cs.Y), cs.umma ? cs.usplits : 1,
+                                                (size_t)n * m, vb + ((k + 1) % 3) * vs,
                                                 vb + (k % 3) * vs, out, cs.coef, k, nm);
     }
     to_float2_kernel<<<nb, tb, 0, st>>>(out, reinterpret_cast<float2 *>(cs.Vf), nm);
@@ -2188,6 +2217,25 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
                 cudaMalloc(&cs.Vf, (size_t)cs.ld * cs.m * sizeof(float2)) != cudaSuccess)
                 rc = ELHL_ERR_OOM;
             if (!rc) rc = dev_alloc(&cs.gpops, (size_t)cs.P * (cs.nfrag + 1));
+            // BF16X3 with 16, 32 or 64 columns: the hand-written tcgen05 GEMM (else cuBLAS emulation)
+            if (!rc && cs.precision == ELHL_PREC_BF16X3 && umma_supported_n2(2 * cs.m)) {
+                for (int t = 0; t < 3 && !rc; ++t)
+                    if (cudaMalloc(&cs.hsplit[t], (size_t)cs.ld * cs.N * sizeof(__nv_bfloat16)) != cudaSuccess ||
+                        cudaMalloc(&cs.vsplit[t], (size_t)cs.ld * 2 * cs.m * sizeof(__nv_bfloat16)) != cudaSuccess)
+                        rc = ELHL_ERR_OOM;
+                cs.usplits = umma_splits(cs.N, cs.N);
+                if (!rc && cs.usplits > 1) {  // Y holds one partial tile per split
+                    cudaFree(cs.Y);
+                    cs.Y = nullptr;
+                    if (cudaMalloc(&cs.Y, (size_t)cs.usplits * cs.N * cs.m * sizeof(float2)) != cudaSuccess)
+                        rc = ELHL_ERR_OOM;
+                }
+                if (!rc) {
+                    cs.umma = true;
+                    rc = split3_bf16(reinterpret_cast<const float *>(cs.Hs), cs.N, cs.N, cs.ld, cs.hsplit, cs.ld,
+                                     false, g_ctx.stream);
+                }
+            }
         }
         std::vector<ChebState *> one{&tr->cs};
         if (!rc) rc = cheb_plan(tr->plan, one);

@@ -1,6 +1,7 @@
 // Internal declarations shared by the translation units of libelhlprop.so.
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
@@ -125,6 +126,18 @@ int cheb_grid_size(int *grid_out);
 int cheb_group_size(int precision, int m, int max_ld);  // columns staged per pass, 0 = unsupported
 cudaError_t launch_cheb(const ChebLaunch &L, int precision, int mg, cudaStream_t st);
 cudaError_t launch_readout(const ChebLaunch &L, int nprob, int precision, int mg, cudaStream_t st);
+
+// Split-precision tensor-core GEMM (umma_gemm.cu): sum over s < splits of Y_s
+// (rows x n2, row-major FP32, Y_s = Y + s rows n2) = sum over the BF16 terms
+// (i + j <= 2) of A_i (rows x K, K contiguous, ld lda) times B_j^T (B_j: n2 x K,
+// ld ldb).  n2 in {32, 64, 128}; umma_splits picks the K split.
+size_t umma_smem_bytes(int n2);
+int umma_supported_n2(int n2);
+int umma_splits(int rows, int K);
+int split3_bf16(const float *src, int rows, int cols, int lds, __nv_bfloat16 *const dst[3], int ldd, bool transpose,
+                cudaStream_t st);
+int umma_bf16x3_gemm(const __nv_bfloat16 *const A[3], int lda, const __nv_bfloat16 *const B[3], int ldb, int rows,
+                     int K, int n2, int splits, float *Y, int *d_error, cudaStream_t st);
 
 int bessel_j_sequence(double beta, int kmax, double *J);
 int chebyshev_coefficients(double dt, double emin, double emax, double tol, int kcap, std::vector<double> &cre,

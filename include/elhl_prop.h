@@ -113,8 +113,9 @@ enum {
                              with >= 16 ket columns (one per particle) and N >= 2048, H~.Psi runs as
                              FP32 GEMMs on the FP32 pipes (cuBLAS, FP32 sums along N) */
     ELHL_PREC_BF16X3 = 2  /* Chebyshev: as FP32, but those GEMMs run on the tensor cores with each
-                             FP32 operand split in three bf16 terms; outside the GEMM regime it runs
-                             as FP32 */
+                             FP32 operand split in three bf16 terms: a hand-written tcgen05/TMA kernel
+                             for 16, 32 or 64 columns (cuBLAS emulation otherwise); outside the GEMM
+                             regime it runs as FP32 */
 };
 
 /* STO basis of one system (the STO_basis fields the path reads, types_EHT.f:135-165). */
