@@ -20,6 +20,8 @@
 // grid barrier separates orders.
 //   T = double : FP64 products;  T = float : FP32 Hs and vectors,
 //   FP64 coefficients and accumulation.
+#include <type_traits>
+
 #include "elhl_internal.cuh"
 #include "grid_sync.cuh"
 
@@ -105,6 +107,43 @@ __device__ void rows_gemv(const T *M, int ld, const typename Vec2<T>::type *s_v,
         // whose tile lies past row1 skip the loop (a warp-uniform branch, so their
         // FMAs are not issued at all).
         int j = nr > 0 ? j0 + lane : j1;
+        if constexpr (sizeof(T) == 4 && MG <= 2) {
+            // FP32: four consecutive j per lane (16-byte loads, 512 B per row per warp
+            // instruction); full tiles run without per-row predicates.  j0, j1 and ld
+            // are multiples of 32, so a float4 never crosses j1.
+            auto sweep = [&](auto full) {
+                constexpr bool kFull = decltype(full)::value;
+                for (int jv = j0 + 4 * lane; jv < j1; jv += 128) {
+                    float4 hv[kRT];
+#pragma unroll
+                    for (int r = 0; r < kRT; ++r)
+                        hv[r] = (kFull || r < nr) ? *reinterpret_cast<const float4 *>(cols[r] + jv)
+                                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        T2 x[MG];
+#pragma unroll
+                        for (int c = 0; c < MG; ++c) x[c] = s_v[(jv + u) * MG + c];
+#pragma unroll
+                        for (int r = 0; r < kRT; ++r) {
+                            if (kFull || r < nr) {
+                                const T h = u == 0 ? hv[r].x : u == 1 ? hv[r].y : u == 2 ? hv[r].z : hv[r].w;
+#pragma unroll
+                                for (int c = 0; c < MG; ++c) {
+                                    acc[(r * MG + c) * 2 + 0] = fma(h, x[c].x, acc[(r * MG + c) * 2 + 0]);
+                                    acc[(r * MG + c) * 2 + 1] = fma(h, x[c].y, acc[(r * MG + c) * 2 + 1]);
+                                }
+                            }
+                        }
+                    }
+                }
+            };
+            if (nr == kRT)
+                sweep(std::true_type{});
+            else if (nr > 0)
+                sweep(std::false_type{});
+            j = j1;  // the scalar loops below have nothing left
+        }
         for (; j + 32 < j1; j += 64) {
             T h0[kRT], h1[kRT];
 #pragma unroll
