@@ -41,6 +41,14 @@ template <typename T> struct RowTile;
 template <> struct RowTile<double> { static constexpr int value = 2; };
 template <> struct RowTile<float> { static constexpr int value = 8; };
 
+template <typename T> struct Vec16;  // 16-byte vector of T
+template <> struct Vec16<double> { using type = double2; };
+template <> struct Vec16<float> { using type = float4; };
+__device__ __forceinline__ double lane_elem(const double2 &v, int u) { return u == 0 ? v.x : v.y; }
+__device__ __forceinline__ float lane_elem(const float4 &v, int u) {
+    return u == 0 ? v.x : u == 1 ? v.y : u == 2 ? v.z : v.w;
+}
+
 __device__ __forceinline__ double2 ldcg2(const double2 *p) { return __ldcg(p); }
 __device__ __forceinline__ float2 ldcg2(const float2 *p) { return __ldcg(p); }
 
@@ -102,89 +110,42 @@ __device__ void rows_gemv(const T *M, int ld, const typename Vec2<T>::type *s_v,
         const T *cols[kRT];
 #pragma unroll
         for (int r = 0; r < kRT; ++r) cols[r] = M + (size_t)min(r0 + r, row1 - 1) * ld;
-        // two j positions per iteration: the 2 x kRT column loads are issued before
-        // the FMAs that consume them (more L2 requests in flight per warp).  Warps
-        // whose tile lies past row1 skip the loop (a warp-uniform branch, so their
-        // FMAs are not issued at all).
-        int j = nr > 0 ? j0 + lane : j1;
-        if constexpr (sizeof(T) == 4 && MG <= 2) {
-            // FP32: four consecutive j per lane (16-byte loads, 512 B per row per warp
-            // instruction); full tiles run without per-row predicates.  j0, j1 and ld
-            // are multiples of 32, so a float4 never crosses j1.
-            auto sweep = [&](auto full) {
-                constexpr bool kFull = decltype(full)::value;
-                for (int jv = j0 + 4 * lane; jv < j1; jv += 128) {
-                    float4 hv[kRT];
+        // 16-byte loads: VE consecutive j per lane, 512 B per row per warp
+        // instruction; full tiles run without per-row predicates, and warps whose
+        // tile lies past row1 skip the sweep (a warp-uniform branch: no FMAs
+        // issued).  j0, j1 and ld are multiples of 32, so a vector never crosses j1.
+        constexpr int VE = 16 / (int)sizeof(T);
+        using TV = typename Vec16<T>::type;
+        auto sweep = [&](auto full) {
+            constexpr bool kFull = decltype(full)::value;
+            for (int jv = j0 + VE * lane; jv < j1; jv += 32 * VE) {
+                TV hv[kRT];
 #pragma unroll
-                    for (int r = 0; r < kRT; ++r)
-                        hv[r] = (kFull || r < nr) ? *reinterpret_cast<const float4 *>(cols[r] + jv)
-                                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int r = 0; r < kRT; ++r)
+                    hv[r] = (kFull || r < nr) ? *reinterpret_cast<const TV *>(cols[r] + jv) : TV{};
 #pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        T2 x[MG];
+                for (int u = 0; u < VE; ++u) {
+                    T2 x[MG];
 #pragma unroll
-                        for (int c = 0; c < MG; ++c) x[c] = s_v[(jv + u) * MG + c];
+                    for (int c = 0; c < MG; ++c) x[c] = s_v[(jv + u) * MG + c];
 #pragma unroll
-                        for (int r = 0; r < kRT; ++r) {
-                            if (kFull || r < nr) {
-                                const T h = u == 0 ? hv[r].x : u == 1 ? hv[r].y : u == 2 ? hv[r].z : hv[r].w;
+                    for (int r = 0; r < kRT; ++r) {
+                        if (kFull || r < nr) {
+                            const T h = lane_elem(hv[r], u);
 #pragma unroll
-                                for (int c = 0; c < MG; ++c) {
-                                    acc[(r * MG + c) * 2 + 0] = fma(h, x[c].x, acc[(r * MG + c) * 2 + 0]);
-                                    acc[(r * MG + c) * 2 + 1] = fma(h, x[c].y, acc[(r * MG + c) * 2 + 1]);
-                                }
+                            for (int c = 0; c < MG; ++c) {
+                                acc[(r * MG + c) * 2 + 0] = fma(h, x[c].x, acc[(r * MG + c) * 2 + 0]);
+                                acc[(r * MG + c) * 2 + 1] = fma(h, x[c].y, acc[(r * MG + c) * 2 + 1]);
                             }
                         }
                     }
                 }
-            };
-            if (nr == kRT)
-                sweep(std::true_type{});
-            else if (nr > 0)
-                sweep(std::false_type{});
-            j = j1;  // the scalar loops below have nothing left
-        }
-        for (; j + 32 < j1; j += 64) {
-            T h0[kRT], h1[kRT];
-#pragma unroll
-            for (int r = 0; r < kRT; ++r) {
-                h0[r] = r < nr ? cols[r][j] : T(0);
-                h1[r] = r < nr ? cols[r][j + 32] : T(0);
             }
-#pragma unroll
-            for (int u = 0; u < 2; ++u) {
-                T2 x[MG];
-#pragma unroll
-                for (int c = 0; c < MG; ++c) x[c] = s_v[(j + 32 * u) * MG + c];
-#pragma unroll
-                for (int r = 0; r < kRT; ++r) {
-                    if (r < nr) {  // warp-uniform
-                        const T h = u ? h1[r] : h0[r];
-#pragma unroll
-                        for (int c = 0; c < MG; ++c) {
-                            acc[(r * MG + c) * 2 + 0] = fma(h, x[c].x, acc[(r * MG + c) * 2 + 0]);
-                            acc[(r * MG + c) * 2 + 1] = fma(h, x[c].y, acc[(r * MG + c) * 2 + 1]);
-                        }
-                    }
-                }
-            }
-        }
-        for (; j < j1; j += 32) {
-            T2 x[MG];
-#pragma unroll
-            for (int c = 0; c < MG; ++c) x[c] = s_v[j * MG + c];
-#pragma unroll
-            for (int r = 0; r < kRT; ++r) {
-                if (r < nr) {
-                    const T h = cols[r][j];
-#pragma unroll
-                    for (int c = 0; c < MG; ++c) {
-                        acc[(r * MG + c) * 2 + 0] = fma(h, x[c].x, acc[(r * MG + c) * 2 + 0]);
-                        acc[(r * MG + c) * 2 + 1] = fma(h, x[c].y, acc[(r * MG + c) * 2 + 1]);
-                    }
-                }
-            }
-        }
+        };
+        if (nr == kRT)
+            sweep(std::true_type{});
+        else if (nr > 0)
+            sweep(std::false_type{});
         // warp sums -> shared memory, layout s_part[wj][wr][NV]
 #pragma unroll
         for (int b = 0; b < NB; ++b) {
