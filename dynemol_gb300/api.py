@@ -29,7 +29,7 @@ PREC_FP64, PREC_FP32, PREC_BF16X3 = 0, 1, 2
 
 EXPORTED_SYMBOLS = (
     "gpu_init_", "gpu_finalize_", "gpu_pin_", "gpu_unpin_", "propagation_gpucaller_", "ehrenfestkernel_gpu_",
-    "ehrenfestkernel2_gpu_", "elhl_ehrenfest_forces",
+    "ehrenfestkernel2_gpu_", "elhl_ehrenfest_forces", "elhl_huckel_with_fields",
     "propagationelhl_gpucaller_", "elhl_last_status", "elhl_status_string", "elhl_traj_config_default",
     "elhl_traj_create", "elhl_traj_destroy", "elhl_traj_init_fmo", "elhl_traj_init_fmo_states", "elhl_traj_set_psi", "elhl_traj_get_psi", "elhl_traj_step",
     "elhl_traj_step_device", "elhl_traj_energies", "elhl_traj_get_matrices", "elhl_traj_get_stats", "elhl_device_count",
@@ -105,6 +105,8 @@ def load(path: str = LIB_PATH):
     L.ehrenfestkernel2_gpu_.restype = None
     L.elhl_ehrenfest_forces.argtypes = [ctypes.POINTER(BasisDesc), vp, vp, ctypes.c_double, ctypes.c_double, vp]
     L.elhl_ehrenfest_forces.restype = ci
+    L.elhl_huckel_with_fields.argtypes = [ctypes.POINTER(BasisDesc), vp, vp, vp, vp, ctypes.c_double, vp]
+    L.elhl_huckel_with_fields.restype = ci
     L.elhl_last_status.restype = ci
     L.elhl_status_string.argtypes = [ci]
     L.elhl_status_string.restype = ctypes.c_char_p
@@ -247,6 +249,20 @@ def ehrenfest_forces(system, kernel, coords=None, delta: float = 1e-8, cutoff: f
     out = np.zeros((system.natoms, 3))
     _check(L.elhl_ehrenfest_forces(ctypes.byref(desc), _p(c), _p(K), delta, cutoff, _p(out)), "elhl_ehrenfest_forces")
     return out
+
+
+def huckel_with_fields(system, S, dp_ao, dp4, coords=None, cutoff: float = 12.0) -> np.ndarray:
+    """h with environment fields (elhl_huckel_with_fields); dp_ao N x N x 3, dp4 natoms x natoms x 4."""
+    L = load()
+    desc, keep = _basis_desc(system)
+    c = np.ascontiguousarray(system.coords if coords is None else coords, np.float64)
+    S = np.asfortranarray(S, np.float64)
+    dp = np.asfortranarray(dp_ao, np.float64)
+    d4 = np.asfortranarray(dp4, np.float64)
+    h = np.zeros((system.nao, system.nao), order="F")
+    _check(L.elhl_huckel_with_fields(ctypes.byref(desc), _p(c), _p(S), _p(dp), _p(d4), cutoff, _p(h)),
+           "elhl_huckel_with_fields")
+    return h
 
 
 # ---------------------------------------------------------------- trajectories

@@ -410,6 +410,54 @@ __global__ void pulay_pairs_kernel(DevBasis b, const double *__restrict__ coords
     for (int xyz = 0; xyz < 3; ++xyz) F[((size_t)K * nat + L) * 3 + xyz] = f[xyz];
 }
 
+// Extended-Hueckel Hamiltonian with environment fields (even_more_extended_Huckel
+// and Huckel_with_FIELDS, hamiltonians.f:69-264), one thread per atom pair
+// ia > ib closer than the cutoff: for i in ia, j in ib
+//   h_ij = X_ij S_ij - [S_ij DP_1 + (mu_ij - (r0 - R_i) S_ij) . DP_2..4]   (|S_ij| > 1e-7)
+// with r0 the midpoint of the two atoms, mu = dp_ao (the AO dipole matrix,
+// N x N x 3, ld N) and DP the 4-vector (potential, field) of the pair, dp4
+// (natoms x natoms x 4, entry (ia, ib)); h_ji = h_ij, h_ii = IP_i + V_shift_i.
+// h must be zero on entry (blocks beyond the cutoff and same-atom off-diagonals stay 0).
+__global__ void huckel_fields_kernel(DevBasis b, const double *__restrict__ coords, double cutoff,
+                                     const double *__restrict__ S, int lds, const double *__restrict__ dp_ao,
+                                     const double *__restrict__ dp4, double *__restrict__ h, int ldh) {
+    const int ia = blockIdx.y * blockDim.y + threadIdx.y;
+    const int ib = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nat = b.natoms, n = b.nao;
+    if (ia >= nat || ib >= nat || ib > ia) return;
+    const int a0 = b.atom_ao0[ia], na_ao = b.atom_nao[ia];
+    const int b0 = b.atom_ao0[ib], nb_ao = b.atom_nao[ib];
+    if (ia == ib) {
+        for (int ja = 0; ja < na_ao; ++ja) h[(size_t)(a0 + ja) * ldh + a0 + ja] = b.ao_ip[a0 + ja] + b.ao_vshift[a0 + ja];
+        return;
+    }
+    const double dx = coords[3 * ib] - coords[3 * ia], dy = coords[3 * ib + 1] - coords[3 * ia + 1],
+                 dz = coords[3 * ib + 2] - coords[3 * ia + 2];
+    if (sqrt(dx * dx + dy * dy + dz * dz) > cutoff) return;
+    const double Ri[3] = {coords[3 * ia], coords[3 * ia + 1], coords[3 * ia + 2]};
+    const double r0[3] = {(coords[3 * ia] + coords[3 * ib]) / 2.0, (coords[3 * ia + 1] + coords[3 * ib + 1]) / 2.0,
+                          (coords[3 * ia + 2] + coords[3 * ib + 2]) / 2.0};
+    const size_t nn = (size_t)nat * nat;
+    const double DP[4] = {dp4[(size_t)ib * nat + ia], dp4[nn + (size_t)ib * nat + ia],
+                          dp4[2 * nn + (size_t)ib * nat + ia], dp4[3 * nn + (size_t)ib * nat + ia]};
+    const size_t n2 = (size_t)n * n;
+    for (int jb = 0; jb < nb_ao; ++jb) {
+        const int j = b0 + jb;
+        for (int ja = 0; ja < na_ao; ++ja) {
+            const int i = a0 + ja;
+            const double sij = S[(size_t)j * lds + i];
+            double v = x_ij(b.ao_ip[i], b.ao_ip[j], b.ao_vshift[i], b.ao_vshift[j], b.ao_kwh[i], b.ao_kwh[j]) * sij;
+            if (fabs(sij) > 1.0e-7) {
+                double vec[3];
+                for (int c = 0; c < 3; ++c) vec[c] = dp_ao[c * n2 + (size_t)j * n + i] - (r0[c] - Ri[c]) * sij;
+                v = v - (sij * DP[0] + (vec[0] * DP[1] + vec[1] * DP[2] + vec[2] * DP[3]));
+            }
+            h[(size_t)j * ldh + i] = v;
+            h[(size_t)i * ldh + j] = v;
+        }
+    }
+}
+
 // force(a)[xyz] = scale * (sum_{L > a} F[a][L] - sum_{K < a} F[K][a]), fixed order
 // (the atom(i)%Ehrenfest sum over F_snd, diabatic-Ehren.f:140-148 with 216-223)
 __global__ void pulay_reduce_kernel(const double *__restrict__ F, int nat, double scale, double *__restrict__ force) {
@@ -441,6 +489,15 @@ cudaError_t launch_pulay_forces(const DevBasis &b, const double *d_coords, doubl
     dim3 grid((b.natoms + block.x - 1) / block.x, (b.natoms + block.y - 1) / block.y);
     pulay_pairs_kernel<<<grid, block, 0, st>>>(b, d_coords, cutoff, delta, d_kernel, ldk, d_F);
     pulay_reduce_kernel<<<(3 * b.natoms + 127) / 128, 128, 0, st>>>(d_F, b.natoms, scale, d_force);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_huckel_fields(const DevBasis &b, const double *d_coords, double cutoff, const double *d_S, int lds,
+                                 const double *d_dp_ao, const double *d_dp4, double *d_h, int ldh, cudaStream_t st) {
+    if (b.natoms <= 0) return cudaSuccess;
+    dim3 block(16, 8);
+    dim3 grid((b.natoms + block.x - 1) / block.x, (b.natoms + block.y - 1) / block.y);
+    huckel_fields_kernel<<<grid, block, 0, st>>>(b, d_coords, cutoff, d_S, lds, d_dp_ao, d_dp4, d_h, ldh);
     return cudaGetLastError();
 }
 

@@ -2148,6 +2148,36 @@ int elhl_ehrenfest_forces(const elhl_basis_desc *basis, const double *coords, co
     return rc;
 }
 
+int elhl_huckel_with_fields(const elhl_basis_desc *basis, const double *coords, const double *S, const double *dp_ao,
+                            const double *dp4, double cutoff, double *h) {
+    if (!coords || !S || !dp_ao || !dp4 || !h) return ELHL_ERR_BAD_ARG;
+    if (int rc = validate_basis(basis)) return rc;
+    if (!(cutoff > 0.0)) cutoff = 12.0;
+    std::lock_guard<std::mutex> lk(g_ctx.mu);
+    if (int rc = ensure_context_locked(-1)) return rc;
+    cudaStream_t st = g_ctx.stream;
+    const int nat = basis->natoms, n = basis->nao;
+    const size_t nn = (size_t)n * n, aa = (size_t)nat * nat;
+    DevBasis db{};
+    double *d_coords = nullptr, *d_S = nullptr, *d_dp = nullptr, *d_dp4 = nullptr, *d_h = nullptr;
+    int rc = upload_basis(db, basis);
+    if (!rc) rc = dev_alloc(&d_coords, (size_t)nat * 3);
+    if (!rc) rc = dev_alloc(&d_S, nn);
+    if (!rc) rc = dev_alloc(&d_dp, 3 * nn);
+    if (!rc) rc = dev_alloc(&d_dp4, 4 * aa);
+    if (!rc) rc = dev_alloc(&d_h, nn);
+    if (!rc && (copy_h2d(d_coords, coords, (size_t)nat * 3 * sizeof(double)) ||
+                copy_h2d(d_S, S, nn * sizeof(double)) || copy_h2d(d_dp, dp_ao, 3 * nn * sizeof(double)) ||
+                copy_h2d(d_dp4, dp4, 4 * aa * sizeof(double)) ||
+                cudaMemsetAsync(d_h, 0, nn * sizeof(double), st)))
+        rc = ELHL_ERR_CUDA;
+    if (!rc && launch_huckel_fields(db, d_coords, cutoff, d_S, n, d_dp, d_dp4, d_h, n, st)) rc = ELHL_ERR_CUDA;
+    if (!rc && copy_d2h(h, d_h, nn * sizeof(double))) rc = ELHL_ERR_CUDA;
+    free_basis(db);
+    dev_free(d_coords); dev_free(d_S); dev_free(d_dp); dev_free(d_dp4); dev_free(d_h);
+    return rc;
+}
+
 int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const elhl_traj_config *cfg,
                      elhl_traj **out) {
     if (!out || !coords) return ELHL_ERR_BAD_ARG;

@@ -27,6 +27,9 @@ struct DevBasis {
 cudaError_t init_build_tables();
 
 // S and h (both N x N, column-major, leading dimension ld) from coordinates.
+// Hueckel Hamiltonian with environment fields (h zeroed by the caller)
+cudaError_t launch_huckel_fields(const DevBasis &b, const double *d_coords, double cutoff, const double *d_S, int lds,
+                                 const double *d_dp_ao, const double *d_dp4, double *d_h, int ldh, cudaStream_t st);
 // Ehrenfest Pulay forces: F (natoms^2 x 3 scratch) and force (natoms x 3) on the device
 cudaError_t launch_pulay_forces(const DevBasis &b, const double *d_coords, double cutoff, double delta,
                                 const double *d_kernel, int ldk, double *d_F, double scale, double *d_force,

@@ -172,6 +172,20 @@ void elhl_traj_config_default(elhl_traj_config *cfg);
 int elhl_ehrenfest_forces(const elhl_basis_desc *basis, const double *coords, const double *kernel, double delta,
                           double cutoff, double *forces);
 
+/*
+ * Extended-Hueckel Hamiltonian with environment fields (even_more_extended_Huckel
+ * and Huckel_with_FIELDS, hamiltonians.f:69-264, the EnvField_ case): for AOs i
+ * of atom a > b and j of atom b, closer than `cutoff` (<= 0: 12 Angstrom),
+ *   h_ij = X_ij S_ij - [S_ij DP_1 + (mu_ij - (r0 - R_a) S_ij) . DP_2..4]  when |S_ij| > 1e-7,
+ * r0 the midpoint of the atoms, h_ji = h_ij, h_ii = IP_i + V_shift_i, other entries 0.
+ * S: host N x N (ld N); dp_ao: the AO dipole matrix DP_matrix_AO, host N x N x 3
+ * column-major; dp4: the environment's potential and field per atom pair,
+ * DP_4_matrix, host natoms x natoms x 4 column-major, entry (a, b) for a > b.
+ * h: host N x N output.
+ */
+int elhl_huckel_with_fields(const elhl_basis_desc *basis, const double *coords, const double *S, const double *dp_ao,
+                            const double *dp4, double cutoff, double *h);
+
 /* Create a trajectory at the given coordinates (natoms*3, atom-major, Angstrom, host).
  * Builds S, h and H' on the device. */
 int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const elhl_traj_config *cfg,

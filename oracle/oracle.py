@@ -355,3 +355,41 @@ def pulay_forces(sys, kernel, coords=None, delta=1e-8, cutoff=12.0):
     for a in range(nat):
         force[a] = F[a, a + 1:].sum(0) - F[:a, a].sum(0)
     return 2.0 * 1.602176565e-9 * force
+
+
+def huckel_with_fields(sys, S, dp_ao, dp4, coords=None, cutoff=12.0):
+    """Extended-Hueckel h with environment fields, the EnvField_ case of
+    even_more_extended_Huckel / Huckel_with_FIELDS (hamiltonians.f:69-264):
+    for AOs i of atom a > b and j of atom b within the cutoff,
+    h_ij = X_ij S_ij - [S_ij DP_1 + (mu_ij - (r0 - R_a) S_ij) . DP_2..4] when |S_ij| > low_prec
+    (1e-7, constants_m.f:26), h_ji = h_ij; h_ii = IP + V_shift."""
+    X = np.array(sys.coords if coords is None else coords, np.float64)
+    n = sys.nao
+    h = np.zeros((n, n), order="F")
+    for i in range(n):
+        h[i, i] = sys.ao_ip[i] + sys.ao_vshift[i]
+    for b in range(sys.natoms):
+        for a in range(b + 1, sys.natoms):
+            if np.sqrt(((X[b] - X[a]) ** 2).sum()) > cutoff:
+                continue
+            Ri = X[a]
+            r0 = (X[a] + X[b]) / 2.0
+            DP = dp4[a, b, :]
+            for jb in range(sys.atom_nao[b]):
+                j = sys.atom_ao0[b] + jb
+                for ja in range(sys.atom_nao[a]):
+                    i = sys.atom_ao0[a] + ja
+                    s = S[i, j]
+                    c1 = sys.ao_ip[i] - sys.ao_ip[j]
+                    c2 = sys.ao_ip[i] + sys.ao_ip[j]
+                    c3 = (c1 / c2) * (c1 / c2)
+                    c4 = (sys.ao_vshift[i] + sys.ao_vshift[j]) * 0.5
+                    k = (sys.ao_kwh[i] + sys.ao_kwh[j]) * 0.5
+                    keff = k + c3 + c3 * c3 * (1.0 - k)
+                    v = (keff * c2 * 0.5 + c4) * s
+                    if abs(s) > 1e-7:
+                        vec = dp_ao[i, j, :] - (r0 - Ri) * s
+                        v = v - (s * DP[0] + (vec[0] * DP[1] + vec[1] * DP[2] + vec[2] * DP[3]))
+                    h[i, j] = v
+                    h[j, i] = v
+    return h

@@ -58,3 +58,15 @@ def test_forces_from_propagated_state(elhl, oracle_mod, flake):
     f = elhl.ehrenfest_forces(sub, Ko[:n, :n], delta=1e-5)
     fo = oracle_mod.pulay_forces(sub, Ko[:n, :n], delta=1e-5)
     assert np.abs(f - fo).max() < 1e-9 * np.abs(fo).max()
+
+
+def test_huckel_with_fields_matches_oracle(elhl, oracle_mod, cluster):
+    """elhl_huckel_with_fields against the oracle with random dipole matrix and
+    pair fields (the same IEEE operations: 1e-13 relative)."""
+    rng = np.random.default_rng(7)
+    S = oracle_mod.overlap(cluster)
+    dp_ao = rng.normal(size=(cluster.nao, cluster.nao, 3))
+    dp4 = rng.normal(size=(cluster.natoms, cluster.natoms, 4))
+    h = elhl.huckel_with_fields(cluster, S, dp_ao, dp4)
+    ho = oracle_mod.huckel_with_fields(cluster, S, dp_ao, dp4)
+    assert np.abs(h - ho).max() < 1e-13 * np.abs(ho).max()

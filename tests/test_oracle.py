@@ -198,3 +198,28 @@ def test_pulay_forces_h2_closed_form(oracle_mod):
     ref0 = 2 * 1.602176565e-9 * (-dS_dx0)
     assert np.abs(f[0] - ref0).max() < 1e-8 * np.abs(ref0).max()
     assert np.abs(f[0] + f[1]).max() < 1e-20
+
+
+def test_huckel_with_fields_zero_field_is_huckel(oracle_mod):
+    """With zero dipole matrix and zero fields the field Hamiltonian is the plain
+    Wolfsberg-Helmholz h of the oracle's C restatement."""
+    from dynemol_gb300 import systems
+    c = systems.cubic_cluster(n_atoms=12, seed=3)
+    S = oracle_mod.overlap(c)
+    h0 = oracle_mod.huckel(c, S)
+    hf = oracle_mod.huckel_with_fields(c, S, np.zeros((c.nao, c.nao, 3)), np.zeros((c.natoms, c.natoms, 4)))
+    assert np.abs(hf - h0).max() < 1e-14 * np.abs(h0).max()
+
+
+def test_huckel_with_fields_uniform_potential(oracle_mod):
+    """A uniform potential phi (DP_1 = phi, no field) shifts every off-diagonal
+    element with |S_ij| > 1e-7 by -phi S_ij."""
+    from dynemol_gb300 import systems
+    c = systems.cubic_cluster(n_atoms=12, seed=3)
+    S = oracle_mod.overlap(c)
+    dp4 = np.zeros((c.natoms, c.natoms, 4))
+    dp4[:, :, 0] = 0.37
+    hf = oracle_mod.huckel_with_fields(c, S, np.zeros((c.nao, c.nao, 3)), dp4)
+    h0 = oracle_mod.huckel(c, S)
+    off = ~np.eye(c.nao, dtype=bool) & (np.abs(S) > 1e-7)
+    assert np.abs((hf - h0)[off] + 0.37 * S[off]).max() < 1e-13
