@@ -131,6 +131,24 @@ def test_cheb_rejects_bad_config(elhl, flake):
     assert e.value.status == elhl.ERR_UNSUPPORTED
 
 
+@pytest.mark.parametrize("ncols", [32, 64])
+def test_bf16x3_tensor_gemm_column_blocks(elhl, ncols):
+    """The tcgen05 GEMM with 2m = 64 and 128 (N = 2170, partial 128-row tile at the
+    end, K split): populations within 1e-6 of FP64 over 3 steps."""
+    sysm = systems.cubic_cluster(n_atoms=700, seed=9)
+    states = list(range(1, ncols + 1))
+    out = {}
+    for prec in (elhl.PREC_FP64, elhl.PREC_BF16X3):
+        tr = elhl.Trajectory(sysm, dt=1e-4, method=elhl.METHOD_CHEBYSHEV, precision=prec, ncols=ncols,
+                             nparticles=ncols, cheb_tol=1e-12)
+        tr.init_fmo_states(states)
+        out[prec] = tr.step(None, nsteps=3)
+        tr.close()
+    err = np.abs(out[elhl.PREC_BF16X3] - out[elhl.PREC_FP64])
+    assert err[:, :, :-1].max() < 1e-6
+    assert err[:, :, -1].max() < 2e-6
+
+
 @pytest.mark.parametrize("prec_name", ["fp32", "bf16x3"])
 def test_gemm_regime_matches_fp64(elhl, oracle_mod, prec_name):
     """N = 2170 with 16 ket columns: H~.Psi runs as one cuBLAS GEMM per order
