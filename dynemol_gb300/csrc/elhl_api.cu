@@ -802,8 +802,14 @@ __global__ void convert_kernel(const double *__restrict__ src, T *__restrict__ d
 // in-place cuBLAS DTRMMs, so almost all of the N^3/3 flops run in large
 // triangular-times-square products (cuSOLVER's own trtri at N = 3720 spends
 // most of its time in 32 x 32 tiles).
-constexpr int kTriBase = 512;
-constexpr int kTrmmBase = 256;
+#ifndef ELHL_TRI_BASE
+#define ELHL_TRI_BASE 256
+#endif
+#ifndef ELHL_TRMM_BASE
+#define ELHL_TRMM_BASE 256
+#endif
+constexpr int kTriBase = ELHL_TRI_BASE;    // blocks inverted by cuSOLVER trtri
+constexpr int kTrmmBase = ELHL_TRMM_BASE;  // triangular products left to cuBLAS DTRMM
 
 // In-place triangular products with the lower-triangular T (ld), recursively:
 // large blocks become DGEMMs (cuBLAS DTRMM at these sizes runs on 32 x 32
@@ -1104,6 +1110,8 @@ struct ChebPlan {
     double *d_seg_pops = nullptr;
     int grid = 0, max_ld = 0, kmax = 0, mg = 0, mg_read = 0, precision = 0, parity = 0;
     int nphase = 1;            // 3: one implicit problem
+    int mgcd = 0;              // gcd of the problems' column counts
+    bool tuned = false;        // tile measured (on the plan's first run)
     size_t pops_per_step = 0;  // populations of all problems in one step
     void release() {
         dev_free(d_probs); dev_free(d_segs); dev_free(d_seg_begin); dev_free(d_prob_seg0); dev_free(d_seg_pops);
@@ -1220,7 +1228,9 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
     CU_TRY(copy_h2d(pl.d_probs, pl.probs.data(), pl.probs.size() * sizeof(ChebProblem)));
     CU_TRY(copy_h2d(pl.d_segs, pl.segs.data(), pl.segs.size() * sizeof(ChebSegment)));
     CU_TRY(copy_h2d(pl.d_seg_begin, pl.seg_begin.data(), pl.seg_begin.size() * sizeof(int)));
-    return tune_plan(pl, mgcd);
+    pl.mgcd = mgcd;
+    pl.tuned = false;  // measured on the first run (plans of batch members never run)
+    return ELHL_OK;
 }
 
 // refresh per-problem order counts and coefficient pointers after cheb_prepare
@@ -1309,6 +1319,10 @@ int tune_plan(ChebPlan &pl, int mgcd) {
 
 int cheb_run(ChebPlan &pl) {
     cudaStream_t st = g_ctx.stream;
+    if (!pl.tuned) {
+        if (int rc = tune_plan(pl, pl.mgcd)) return rc;
+        pl.tuned = true;
+    }
     CU_TRY(cudaMemsetAsync(g_ctx.err, 0, sizeof(int), st));
     CU_TRY(cudaMemsetAsync(g_ctx.bar, 0, 2 * sizeof(unsigned), st));
     ChebLaunch L{};
