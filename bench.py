@@ -230,6 +230,7 @@ def run_ours(args, rank, world):
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
     FP64_PEAK = 1.20  # TFLOP/s, FMA probe measured on this machine's GB300 (profiles/gb300_peaks_probe.md)
     prop_launch_ms = prop_ms / K
+    traffic_per_launch = None
     if args.method == "taylor":
         # dominant kernel: taylor_kernel.  Unit = one expansion order of one
         # particle: H' read once for bra (H'^T) and ket (H'), 2 complex columns:
@@ -251,6 +252,12 @@ def run_ours(args, rank, world):
         per_launch_orders = orders / max(1, K) / m
         bytes_per_launch = per_launch_orders * (bH * elems + vec * N * m)
         flops_per_launch = per_launch_orders * 4.0 * elems * m
+        if moving and args.precision == "fp64":
+            # DRAM traffic per matrix element and order measured by ncu on the same
+            # kernel at N = 2790 (profiles/cheb_kernel_implicit_cluster900_fp64_ncu.md:
+            # 18.68 GB read + 0.11 GB written over 149 orders of 2 N^2 elements);
+            # traffic grows with N^2 and the orders, so it is scaled to this launch
+            traffic_per_launch = 8.10 * elems * per_launch_orders
     achieved_gbs = bytes_per_launch / (prop_launch_ms * 1e-3) / 1e9
     tflops = flops_per_launch / (prop_launch_ms * 1e-3) / 1e12
 
@@ -275,7 +282,7 @@ def run_ours(args, rank, world):
                 "h2d_bytes_per_step": (nc * 8) if moving else 0, "d2h_bytes_per_step": 2 * nf1 * 8},
         "gpu_launches": launches,
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved_gbs / hbm_peak, "traffic": None,
+                     "frac": achieved_gbs / hbm_peak, "traffic": traffic_per_launch,
                      "kernel": kernel, "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)",
                      "alu": {"achieved_tflops": tflops,
                              "peak_tflops": FP64_PEAK if args.precision == "fp64" else 70.1,
