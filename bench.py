@@ -152,7 +152,8 @@ def run_ours(args, rank, world):
     W, K = args.warmup, args.steps
     coords = step_coords(sysm, moving, W + K + 1, offset=1000 * rank)
     method = api.METHOD_CHEBYSHEV if args.method == "chebyshev" else api.METHOD_TAYLOR_REF
-    prec = {"fp64": api.PREC_FP64, "fp32": api.PREC_FP32, "bf16x3": api.PREC_BF16X3}[args.precision]
+    prec = {"fp64": api.PREC_FP64, "fp32": api.PREC_FP32, "bf16x3": api.PREC_BF16X3,
+            "df64": api.PREC_DF64}[args.precision]
     tr = api.Trajectory(sysm, coords=None if coords is None else coords[0], dt=dt, method=method, precision=prec,
                         ncols=4 if moving else 2, cheb_tol=1e-12)
     tr.init_fmo(homo + 1, homo)
@@ -247,18 +248,23 @@ def run_ours(args, rank, world):
         # bytes, flops 8 N^2 m
         kernel = "cheb_kernel"
         m = 4 if moving else 2
-        bH = 8.0 if args.precision == "fp64" else 4.0
+        bH = 8.0 if args.precision in ("fp64", "df64") else 4.0
         elems, vec = (2.0 * N * N, 144.0) if moving else (1.0 * N * N, 80.0)
         per_launch_orders = orders / max(1, K) / m
         bytes_per_launch = per_launch_orders * (bH * elems + vec * N * m)
         flops_per_launch = per_launch_orders * 4.0 * elems * m
-        if moving and args.precision == "fp64":
+        if moving and args.precision in ("fp64", "df64"):
             # DRAM traffic per matrix element and order measured by ncu on the same
             # kernel at N = 2790 (profiles/cheb_kernel_implicit_cluster900_fp64_ncu.md:
             # 18.68 GB read + 0.11 GB written over 149 orders of 2 N^2 elements);
             # traffic grows with N^2 and the orders, so it is scaled to this launch
             traffic_per_launch = 8.10 * elems * per_launch_orders
     achieved_gbs = bytes_per_launch / (prop_launch_ms * 1e-3) / 1e9
+    # ALU bound: FP64 FMA pipe; FP32 FMA pipe; DF64 = FP32 pipe at 12 FP32
+    # instructions per FP64-equivalent FMA (peak 70.1 / 12 FP64-equivalent TFLOP/s)
+    alu_peak, alu_pipe = {"fp64": (FP64_PEAK, "fp64 FMA"),
+                          "df64": (70.1 / 12.0, "fp32 FMA, 12 instructions per df64 FMA")}.get(
+        args.precision, (70.1, "fp32 FMA"))
     tflops = flops_per_launch / (prop_launch_ms * 1e-3) / 1e12
 
     line = {
@@ -272,7 +278,8 @@ def run_ours(args, rank, world):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f64" if args.precision == "fp64" else "f32 products, f64 accumulation",
+        "dtype": {"fp64": "f64", "df64": "f64-accurate FP32 pairs (df64), f64 recurrence"}.get(
+            args.precision, "f32 products, f64 accumulation"),
         "data": "synthetic (seeded geometry, no external dataset)",
         "config": {"workload": WORKLOAD_DESC[args.workload], "N_ao": N, "natoms": sysm.natoms,
                    "dt_ps": dt, "particles": 2, "method": args.method, "precision": args.precision,
@@ -285,9 +292,9 @@ def run_ours(args, rank, world):
                      "frac": achieved_gbs / hbm_peak, "traffic": traffic_per_launch,
                      "kernel": kernel, "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)",
                      "alu": {"achieved_tflops": tflops,
-                             "peak_tflops": FP64_PEAK if args.precision == "fp64" else 70.1,
-                             "frac": tflops / (FP64_PEAK if args.precision == "fp64" else 70.1),
-                             "pipe": "fp64 FMA" if args.precision == "fp64" else "fp32 FMA",
+                             "peak_tflops": alu_peak,
+                             "frac": tflops / alu_peak,
+                             "pipe": alu_pipe,
                              "peak_source": "of measured (FMA probe, profiles/gb300_peaks_probe.md)"},
                      "orders_per_launch": per_launch_orders, "launch_ms": prop_launch_ms},
         "breakdown_ms_per_step": {"propagation": prop_ms / K, "rebuild_S_h_operator": rebuild_ms / K,
@@ -523,7 +530,7 @@ def main():
     ap.add_argument("--workload", default="ehrenfest", choices=sorted(WORKLOAD_DESC))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--method", default="chebyshev", choices=["taylor", "chebyshev"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "bf16x3"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "bf16x3", "df64"])
     ap.add_argument("--mix", type=int, default=64, help="also run the batched-vs-drop-in comparison on a mix "
                     "of this many trajectories (0 = skip)")
     ap.add_argument("--no-dropin", action="store_true", help="skip the Taylor drop-in measurement")

@@ -437,6 +437,253 @@ __global__ void reduce_pops_kernel(ChebLaunch L, int nprob) {
     }
 }
 
+// ============================ double-float (DF64) ================================
+// GB300's FP64 pipe runs at 1/58 of its FP32 rate.  ELHL_PREC_DF64 keeps the
+// operator and the series vectors as unevaluated sums hi + lo of two FP32
+// numbers (48-bit significands, about 4e-15 relative) and evaluates the
+// products on the FP32 pipes: Dekker's exact product error by FMA and Knuth's
+// TwoSum for the running sums, with round-to-nearest intrinsics so that no
+// operation is contracted.  Sums leave the row loop in FP64; the recurrence and
+// the accumulation of c_k v_k are FP64 as in the other precisions.  Implicit
+// operator only (G, h/b and G^T stored as float2 = (hi, lo)).
+
+__device__ __forceinline__ float2 df_split(double x) {
+    const float h = __double2float_rn(x);
+    return make_float2(h, __double2float_rn(x - (double)h));
+}
+
+__device__ __forceinline__ float4 df_split2(double re, double im) {
+    const float2 a = df_split(re), b = df_split(im);
+    return make_float4(a.x, a.y, b.x, b.y);
+}
+
+// (sh, sl) += (ah + al)(bh + bl), dropping al bl (2^-48 relative)
+__device__ __forceinline__ void df_fma(float &sh, float &sl, float ah, float al, float bh, float bl) {
+    const float p = __fmul_rn(ah, bh);
+    float e = __fmaf_rn(ah, bh, -p);
+    e = __fmaf_rn(ah, bl, e);
+    e = __fmaf_rn(al, bh, e);
+    const float t = __fadd_rn(sh, p);
+    const float z = __fsub_rn(t, sh);
+    const float y = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, z)), __fsub_rn(p, z));
+    sl = __fadd_rn(sl, __fadd_rn(y, e));
+    sh = t;
+}
+
+// rows_gemv for DF64: y_i = sum_j M(j, i) x_j, M float2 (hi, lo) column-major,
+// x staged as float4 (re hi, re lo, im hi, im lo); calls epi(i, c, yr, yi) with
+// FP64 sums.  Same tiling, triangular ranges and warp sums as rows_gemv.
+template <int MG, int TRI, typename Epi>
+__device__ void rows_gemv_df(const float2 *M, int ld, const float4 *s_v, int row0, int row1, double *s_part,
+                             Epi &epi) {
+    constexpr int kRT = 4;             // rows per warp tile
+    constexpr int NV = kRT * MG * 2;   // sums per lane (8 ... 32)
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int rows = row1 - row0;
+    int WR = 1;
+    while (WR < kWarps && WR * kRT < rows) WR <<= 1;
+    const int WJ = kWarps / WR;
+    const int wr = warp / WJ, wj = warp % WJ;
+    for (int base = row0; base < row1; base += kRT * WR) {
+        const int tile_end = min(row1, base + kRT * WR);
+        const int jlo = TRI == 1 ? (base & ~31) : 0;
+        const int jhi = TRI == 2 ? min(ld, (tile_end + 31) & ~31) : ld;
+        const int jchunk = ((jhi - jlo + WJ - 1) / WJ + 31) / 32 * 32;
+        const int j0 = jlo + wj * jchunk, j1 = min(jhi, j0 + jchunk);
+        const int r0 = base + kRT * wr;
+        const int nr = min(kRT, row1 - r0);
+        float ah[NV], al[NV];
+#pragma unroll
+        for (int q = 0; q < NV; ++q) ah[q] = al[q] = 0.f;
+        const float2 *cols[kRT];
+#pragma unroll
+        for (int r = 0; r < kRT; ++r) cols[r] = M + (size_t)min(r0 + r, row1 - 1) * ld;
+        // 16-byte loads: two (hi, lo) elements per lane, 512 B per row per warp instruction
+        auto sweep = [&](auto full) {
+            constexpr bool kFull = decltype(full)::value;
+            for (int jv = j0 + 2 * lane; jv < j1; jv += 64) {
+                float4 hv[kRT];
+#pragma unroll
+                for (int r = 0; r < kRT; ++r)
+                    hv[r] = (kFull || r < nr) ? *reinterpret_cast<const float4 *>(cols[r] + jv)
+                                              : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int u = 0; u < 2; ++u) {
+                    float4 x[MG];
+#pragma unroll
+                    for (int c = 0; c < MG; ++c) x[c] = s_v[(jv + u) * MG + c];
+#pragma unroll
+                    for (int r = 0; r < kRT; ++r) {
+                        if (kFull || r < nr) {
+                            const float hh = u ? hv[r].z : hv[r].x, hl = u ? hv[r].w : hv[r].y;
+#pragma unroll
+                            for (int c = 0; c < MG; ++c) {
+                                const int k = (r * MG + c) * 2;
+                                df_fma(ah[k], al[k], hh, hl, x[c].x, x[c].y);
+                                df_fma(ah[k + 1], al[k + 1], hh, hl, x[c].z, x[c].w);
+                            }
+                        }
+                    }
+                }
+            }
+        };
+        if (nr == kRT)
+            sweep(std::true_type{});
+        else if (nr > 0)
+            sweep(std::false_type{});
+        // FP64 warp sums, then the fixed-order sum over the WJ slices
+        constexpr int NW = NV < 32 ? NV : 32;
+#pragma unroll
+        for (int b = 0; b < NV / NW; ++b) {
+            double tmp[NW];
+#pragma unroll
+            for (int q = 0; q < NW; ++q) tmp[q] = (double)ah[b * NW + q] + (double)al[b * NW + q];
+            const double sm = warp_sums<double, NW>(tmp, lane);
+            if (lane < NW) s_part[((size_t)wj * WR + wr) * NV + b * NW + lane] = sm;
+        }
+        __syncthreads();
+        for (int t = tid; t < WR * kRT * MG; t += kBlock) {
+            const int wrr = t / (kRT * MG), rem = t % (kRT * MG);
+            const int r = rem / MG, c = rem % MG;
+            const int i = base + kRT * wrr + r;
+            if (i >= row1) continue;
+            double yr = 0.0, yi = 0.0;
+            for (int w = 0; w < WJ; ++w) {
+                yr += s_part[((size_t)w * WR + wrr) * NV + (r * MG + c) * 2 + 0];
+                yi += s_part[((size_t)w * WR + wrr) * NV + (r * MG + c) * 2 + 1];
+            }
+            epi(i, c, yr, yi);
+        }
+        __syncthreads();
+    }
+}
+
+template <int MG>
+struct StoreEpiDF {
+    float4 *dst;
+    __device__ void operator()(int i, int c, double yr, double yi) { dst[(size_t)i * MG + c] = df_split2(yr, yi); }
+};
+
+// recurrence in FP64: y -= shift v_{k-1}; v_k = 2 y - v_{k-2} (v_1 = y), stored as
+// DF64; acc += c_k v_k
+template <int MG>
+struct OrderEpiDF {
+    const float4 *vprev2;
+    float4 *vout;
+    double2 *acc;
+    int k, m, g;
+    double cre, cim;
+    const float4 *vprev1;
+    double shift;
+    __device__ void operator()(int i, int c, double yr, double yi) {
+        const float4 p = __ldcg(vprev1 + (size_t)i * MG + c);
+        yr -= shift * ((double)p.x + (double)p.y);
+        yi -= shift * ((double)p.z + (double)p.w);
+        double vr = yr, vi = yi;
+        if (k > 1) {
+            const float4 w = __ldcg(vprev2 + (size_t)i * MG + c);
+            vr = 2.0 * yr - ((double)w.x + (double)w.y);
+            vi = 2.0 * yi - ((double)w.z + (double)w.w);
+        }
+        vout[(size_t)i * MG + c] = df_split2(vr, vi);
+        const size_t ao = (size_t)i * m + g * MG + c;
+        double2 a = acc[ao];
+        a.x += cre * vr - cim * vi;
+        a.y += cre * vi + cim * vr;
+        acc[ao] = a;
+    }
+};
+
+template <int MG>
+__device__ void order_zero_df(const ChebProblem &pb, const ChebSegment &sg, int parity) {
+    float4 *v0 = reinterpret_cast<float4 *>(pb.vbuf);
+    const int m = pb.m;
+    const size_t gstride = (size_t)pb.ldv * MG;
+    const double cre = pb.coef[0].x, cim = pb.coef[0].y;
+    const double2 *phi = pb.col[parity];
+    double2 *acc = pb.col[parity ^ 1];
+    for (int q = threadIdx.x; q < (sg.row1 - sg.row0) * m; q += kBlock) {
+        const int i = sg.row0 + q / m, col = q % m;
+        const int g = col / MG, c = col % MG;
+        const size_t o = (size_t)i * m + col;
+        double2 p = phi[o];
+        if (pb.scale) {
+            const double sc = pb.scale[col % pb.P];
+            p.x *= sc;
+            p.y *= sc;
+        }
+        v0[g * gstride + (size_t)i * MG + c] = df_split2(p.x, p.y);
+        acc[o] = make_double2(cre * p.x - cim * p.y, cre * p.y + cim * p.x);
+    }
+}
+
+template <int MG>
+__device__ void implicit_phase_df(const ChebLaunch &L, const ChebProblem &pb, int s0, int s1, int k, int ph, int g,
+                                  float4 *s_v, double *s_part, double cre, double cim) {
+    const int ld = pb.ld, m = pb.m;
+    float4 *vbuf = reinterpret_cast<float4 *>(pb.vbuf);
+    float4 *wb = reinterpret_cast<float4 *>(pb.wb);
+    const size_t gstride = (size_t)pb.ldv * MG;
+    const size_t bstride = gstride * (m / MG);
+    const float4 *vprev = vbuf + (size_t)((k + 2) % 3) * bstride + g * gstride;
+    const float4 *src = ph == 0 ? vprev : wb + (size_t)(ph - 1) * bstride + g * gstride;
+    __syncthreads();
+    for (int q = threadIdx.x; q < ld * MG; q += kBlock) s_v[q] = __ldcg(src + q);
+    __syncthreads();
+    for (int s = s0; s < s1; ++s) {
+        const ChebSegment sg = L.segs[s];
+        if (ph == 0) {
+            StoreEpiDF<MG> epi{wb + g * gstride};
+            rows_gemv_df<MG, 1>(reinterpret_cast<const float2 *>(pb.G), ld, s_v, sg.row0, sg.row1, s_part, epi);
+        } else if (ph == 1) {
+            StoreEpiDF<MG> epi{wb + bstride + g * gstride};
+            rows_gemv_df<MG, 0>(reinterpret_cast<const float2 *>(pb.H), ld, s_v, sg.row0, sg.row1, s_part, epi);
+        } else {
+            OrderEpiDF<MG> epi{vbuf + (size_t)((k + 1) % 3) * bstride + g * gstride,
+                               vbuf + (size_t)(k % 3) * bstride + g * gstride,
+                               pb.col[L.parity ^ 1], k, m, g, cre, cim, vprev, pb.shift};
+            rows_gemv_df<MG, 2>(reinterpret_cast<const float2 *>(pb.Gt), ld, s_v, sg.row0, sg.row1, s_part, epi);
+        }
+    }
+}
+
+// one launch per step, implicit operator (one problem, three phases per order)
+template <int MG>
+__global__ void __launch_bounds__(kBlock, 1) cheb_df_kernel(ChebLaunch L) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    double *s_part = reinterpret_cast<double *>(smem_raw);
+    float4 *s_v = reinterpret_cast<float4 *>(smem_raw + kCheb_part_bytes);
+    const int G = gridDim.x;
+    const int s0 = L.seg_begin[blockIdx.x], s1 = L.seg_begin[blockIdx.x + 1];
+    const ChebProblem &pb = L.probs[0];
+    for (int k = 0; k <= L.kmax; ++k) {
+        const int nph = k == 0 ? 1 : 3;
+        for (int ph = 0; ph < nph; ++ph) {
+            if (k == 0) {
+                for (int s = s0; s < s1; ++s) order_zero_df<MG>(pb, L.segs[s], L.parity);
+            } else if (k <= pb.K && s0 < s1) {
+                const double cre = pb.coef[k].x, cim = pb.coef[k].y;
+                for (int g = 0; g < pb.m / MG; ++g)
+                    implicit_phase_df<MG>(L, pb, s0, s1, k, ph, g, s_v, s_part, cre, cim);
+            }
+            if (!grid_barrier(L.bar_count, L.bar_gen, G, L.error)) return;
+        }
+    }
+}
+
+template <int MG>
+cudaError_t launch_df(const ChebLaunch &L, cudaStream_t st) {
+    if (L.nphase != 3) return cudaErrorInvalidValue;  // implicit operator only
+    auto kern = cheb_df_kernel<MG>;
+    const size_t smem = kCheb_part_bytes + (size_t)L.max_ld * MG * sizeof(float4);
+    if (smem > kCheb_smem_limit) return cudaErrorInvalidValue;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    ChebLaunch copy = L;
+    void *args[] = {&copy};
+    return cudaLaunchCooperativeKernel((const void *)kern, dim3(L.grid), dim3(kBlock), args, smem, st);
+}
+
 template <typename T, int MG>
 cudaError_t launch_t(const ChebLaunch &L, cudaStream_t st) {
     auto kern = cheb_kernel<T, MG>;
@@ -486,13 +733,21 @@ int cheb_block() { return kBlock; }
 
 int cheb_group_size(int precision, int m, int max_ld) {
     // the largest of 4, 2, 1 staged columns that divides m and fits in shared memory
-    const size_t c2 = precision == ELHL_PREC_FP64 ? sizeof(double2) : sizeof(float2);
+    const size_t c2 = (precision == ELHL_PREC_FP64 || precision == ELHL_PREC_DF64) ? sizeof(double2) : sizeof(float2);
     for (int mg : {4, 2, 1})
         if (m % mg == 0 && kCheb_part_bytes + (size_t)max_ld * mg * c2 <= kCheb_smem_limit) return mg;
     return 0;
 }
 
 cudaError_t launch_cheb(const ChebLaunch &L, int precision, int mg, cudaStream_t st) {
+    if (precision == ELHL_PREC_DF64) {
+        switch (mg) {
+            case 1: return launch_df<1>(L, st);
+            case 2: return launch_df<2>(L, st);
+            case 4: return launch_df<4>(L, st);
+        }
+        return cudaErrorInvalidValue;
+    }
     if (precision == ELHL_PREC_FP64) {
         switch (mg) {
             case 1: return launch_t<double, 1>(L, st);

@@ -522,6 +522,25 @@ __global__ void renormalize_kernel(double2 *cols, int n, int m, int P, const dou
     }
 }
 
+// 8-byte storage per real element: FP64, or a DF64 (hi, lo) pair of FP32
+inline bool wide_storage(int prec) { return prec == ELHL_PREC_FP64 || prec == ELHL_PREC_DF64; }
+// reduced precision: renormalised every step, GEMM regime possible
+inline bool reduced_precision(int prec) { return prec == ELHL_PREC_FP32 || prec == ELHL_PREC_BF16X3; }
+
+// x -> (hi, lo) FP32 pair (DF64 storage), zero rows >= n
+__global__ void split_df_kernel(const double *__restrict__ src, float2 *__restrict__ dst, int n, int ld, double a,
+                                double binv, bool transpose_lower) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i >= ld || j >= n) return;
+    double v = 0.0;
+    if (i < n) {
+        if (transpose_lower) v = (j >= i) ? src[(size_t)i * ld + j] : 0.0;  // dst(i, j) = src(j, i), j >= i
+        else v = (src[(size_t)j * ld + i] - (i == j ? a : 0.0)) * binv;
+    }
+    const float h = __double2float_rn(v);
+    dst[(size_t)j * ld + i] = make_float2(h, __double2float_rn(v - (double)h));
+}
+
 struct ChebState {
     int N = 0, ld = 0, m = 0, precision = ELHL_PREC_FP64, K = 0;
     int parity = 0;            // phi/acc role of col[0], col[1] for the device read-out path
@@ -569,7 +588,7 @@ struct ChebState {
         ld = round_up(N, 32);
         m = m_;
         precision = prec;
-        const size_t tsz = prec == ELHL_PREC_FP64 ? sizeof(double) : sizeof(float);
+        const size_t tsz = wide_storage(prec) ? sizeof(double) : sizeof(float);
         if (int rc = dev_alloc(&Ht, (size_t)ld * N)) return rc;
         CU_TRY(cudaMalloc(&Hs, (size_t)ld * N * tsz));
         CU_TRY(cudaMalloc(&vbuf, (size_t)3 * ld * m * 2 * tsz));
@@ -752,7 +771,9 @@ int cheb_prepare(ChebState &cs, double dt, double tol, const double *h = nullptr
     dim3 grid((cs.ld + 127) / 128, cs.N);
     const double *src = h ? h : cs.Ht;
     const double a = h ? 0.0 : cs.a;
-    if (cs.precision == ELHL_PREC_FP64)
+    if (cs.precision == ELHL_PREC_DF64)
+        split_df_kernel<<<grid, 128, 0, st>>>(src, (float2 *)cs.Hs, cs.N, cs.ld, a, binv, false);
+    else if (cs.precision == ELHL_PREC_FP64)
         scale_kernel<double><<<grid, 128, 0, st>>>(src, (double *)cs.Hs, cs.N, cs.ld, a, binv);
     else
         scale_kernel<float><<<grid, 128, 0, st>>>(src, (float *)cs.Hs, cs.N, cs.ld, a, binv);
@@ -925,7 +946,7 @@ __global__ void lower_only_kernel(double *A, int n, int ld) {
 int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, double dt, double tol) {
     cudaStream_t st = g_ctx.stream;
     const int n = cs.N, ld = cs.ld;
-    const size_t tsz = cs.precision == ELHL_PREC_FP64 ? sizeof(double) : sizeof(float);
+    const size_t tsz = wide_storage(cs.precision) ? sizeof(double) : sizeof(float);
     if (!cs.A) CU_TRY(cudaMalloc(&cs.A, (size_t)ld * n * tsz));
     if (!cs.B) CU_TRY(cudaMalloc(&cs.B, (size_t)ld * n * tsz));
     if (!cs.Gt) CU_TRY(cudaMalloc(&cs.Gt, (size_t)ld * n * tsz));
@@ -945,6 +966,14 @@ int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, do
     if (int rc = lanczos_bounds(cs, 40, h)) return rc;
     if (int rc = cheb_prepare(cs, dt, tol, h)) return rc;
     dim3 grid((ld + 127) / 128, n);
+    if (cs.precision == ELHL_PREC_DF64) {  // G and G^T as (hi, lo) pairs; no device read-out matrices
+        split_df_kernel<<<grid, 128, 0, st>>>(cs.Ht, (float2 *)cs.A, n, ld, 0.0, 1.0, false);
+        split_df_kernel<<<grid, 128, 0, st>>>(cs.Ht, (float2 *)cs.Gt, n, ld, 0.0, 1.0, true);
+        CU_TRY(cudaGetLastError());
+        cs.implicit = true;
+        cs.readout_ready = false;  // read-out through the FP64 dense transforms
+        return ELHL_OK;
+    }
     if (cs.precision == ELHL_PREC_FP64) {
         convert_kernel<double><<<grid, 128, 0, st>>>(cs.Ht, (double *)cs.A, n, ld, false);
         convert_kernel<double><<<grid, 128, 0, st>>>(cs.Ht, (double *)cs.Gt, n, ld, true);
@@ -1163,7 +1192,7 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
         p.B = dev ? cs->B : nullptr;
         p.psi = cs->psi_out; p.bra = cs->bra_out; p.ao_frag = cs->ao_frag; p.nfrag = cs->nfrag;
         p.pops_off = (int)pl.pops_per_step;
-        const bool renorm = dev && cs->precision != ELHL_PREC_FP64;
+        const bool renorm = dev && reduced_precision(cs->precision);
         p.scale = renorm ? cs->scale : nullptr;
         p.scale_out = renorm ? cs->scale : nullptr;
         p.target = renorm ? cs->target : nullptr;
@@ -1392,7 +1421,7 @@ __global__ void ones_kernel(double *v, int n) {
 int cheb_settle(const std::vector<ChebState *> &states) {
     cudaStream_t st = g_ctx.stream;
     for (auto *cs : states) {
-        if (cs->precision == ELHL_PREC_FP64) continue;
+        if (!reduced_precision(cs->precision)) continue;
         settle_scale_kernel<<<(cs->N + 255) / 256, 256, 0, st>>>(cs->cin(), cs->m, cs->psi_out, cs->bra_out, cs->N,
                                                                  cs->P, cs->scale);
         ones_kernel<<<1, kMaxCols, 0, st>>>(cs->scale, kMaxCols);
@@ -1687,7 +1716,7 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
         if ((rc = cheb_prepare_readout(cs, tr->fac.L))) return rc;
         if ((rc = cheb_plan(tr->plan, one))) return rc;
     }
-    if (!coords && !cs.readout_ready && tr->fac.L) {
+    if (!coords && !cs.readout_ready && tr->fac.L && cs.precision != ELHL_PREC_DF64) {
         // fixed nuclei after moving steps: factor-based read-out matrices for the current L
         if ((rc = cheb_prepare_readout(cs, tr->fac.L))) return rc;
         if ((rc = cheb_plan(tr->plan, one))) return rc;
@@ -1725,7 +1754,7 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
         return ELHL_OK;
     }
     // ---- moving nuclei (or no device read-out): factor-based read-out through cuBLAS
-    const bool renorm = cs.precision != ELHL_PREC_FP64;
+    const bool renorm = reduced_precision(cs.precision);
     double *pops_tmp = nullptr;
     if (!d_pops && renorm) {
         if ((rc = dev_alloc(&pops_tmp, pop_per_step))) return rc;
@@ -2204,7 +2233,7 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
     const bool taylor_p = tr->cfg.nparticles == 2;
     const bool cheb_ok = tr->cfg.method == ELHL_METHOD_CHEBYSHEV &&
                          (tr->cfg.precision == ELHL_PREC_FP64 || tr->cfg.precision == ELHL_PREC_FP32 ||
-                          tr->cfg.precision == ELHL_PREC_BF16X3) &&
+                          tr->cfg.precision == ELHL_PREC_BF16X3 || tr->cfg.precision == ELHL_PREC_DF64) &&
                          tr->cfg.nparticles >= 1 && tr->cfg.nparticles <= 64 &&
                          (tr->cfg.ncols == tr->cfg.nparticles || tr->cfg.ncols == 2 * tr->cfg.nparticles) &&
                          tr->cfg.cheb_tol > 0.0;
@@ -2249,13 +2278,14 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
         if (!rc) rc = dev_alloc(&tr->target, (size_t)tr->P);
         if (!rc && cudaMemset(tr->psi_ao, 0, (size_t)tr->ld * tr->P * sizeof(double2)) != cudaSuccess) rc = ELHL_ERR_CUDA;
         if (!rc && cudaMemset(tr->bra_ao, 0, (size_t)tr->ld * tr->P * sizeof(double2)) != cudaSuccess) rc = ELHL_ERR_CUDA;
-        if (!rc) rc = cheb_rebuild_operator(tr);
+        const bool df = tr->cfg.precision == ELHL_PREC_DF64;  // DF64: implicit operator from the start
+        if (!rc) rc = cheb_rebuild_operator(tr, df);
         ChebState &cs = tr->cs;
         cs.P = tr->P; cs.nfrag = tr->nfrag; cs.psi_out = tr->psi_ao; cs.bra_out = tr->bra_ao;
         cs.ao_frag = tr->basis.ao_frag; cs.target = tr->target;
-        if (!rc) rc = cheb_prepare_readout(cs, tr->fac.L);
+        if (!rc && !df) rc = cheb_prepare_readout(cs, tr->fac.L);
         // GEMM regime: many ket columns in FP32 / BF16X3 -> one GEMM per order
-        if (!rc && cs.precision != ELHL_PREC_FP64 && cs.m == cs.P && cs.P >= kGemmMinCols && cs.N >= kGemmMinN) {
+        if (!rc && reduced_precision(cs.precision) && cs.m == cs.P && cs.P >= kGemmMinCols && cs.N >= kGemmMinN) {
             cs.gemm = true;
             if (cudaMalloc(&cs.Y, (size_t)cs.ld * cs.m * sizeof(float2)) != cudaSuccess ||
                 cudaMalloc(&cs.Vf, (size_t)cs.ld * cs.m * sizeof(float2)) != cudaSuccess)
@@ -2612,7 +2642,7 @@ struct elhl_server {
 };
 
 static double request_bytes(const elhl_traj_config &cfg, int nao, int P) {
-    const double ld = (double)round_up(nao, 32), tsz = cfg.precision == ELHL_PREC_FP64 ? 8.0 : 4.0;
+    const double ld = (double)round_up(nao, 32), tsz = wide_storage(cfg.precision) ? 8.0 : 4.0;
     // set-up peak: S, h, H~, L (FP64) + Hs + vectors
     return ld * nao * (4 * 8.0 + tsz) + ld * cfg.ncols / cfg.nparticles * P * (3 * 2 * tsz + 2 * 16.0) + 1e6;
 }

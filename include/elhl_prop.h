@@ -112,6 +112,10 @@ enum {
     ELHL_PREC_FP32 = 1,   /* Chebyshev: FP32 H~ and series vectors, FP64 coefficients, sums and norms;
                              with >= 16 ket columns (one per particle) and N >= 2048, H~.Psi runs as
                              FP32 GEMMs on the FP32 pipes (cuBLAS, FP32 sums along N) */
+    ELHL_PREC_DF64 = 3,   /* Chebyshev, implicit operator: operator and series vectors as FP32 pairs
+                             hi + lo (48-bit significands) with exact-product / TwoSum arithmetic on the
+                             FP32 pipes, FP64 recurrence and sums: FP64-level accuracy (1e-10 populations)
+                             without the FP64 pipe; read-out through FP64 library products */
     ELHL_PREC_BF16X3 = 2  /* Chebyshev: as FP32, but those GEMMs run on the tensor cores with each
                              FP32 operand split in three bf16 terms: a hand-written tcgen05/TMA kernel
                              for 16, 32 or 64 columns (cuBLAS emulation otherwise); outside the GEMM

@@ -182,3 +182,46 @@ def test_gemm_regime_matches_fp64(elhl, oracle_mod, prec_name):
         ref = oracle_mod.exact_populations(sysm, S, ex.ket(ket0.astype(complex), 4e-4))
         assert np.abs(out[elhl.PREC_FP64][-1, c] - ref).max() < 1e-10
         assert np.abs(out[prec32][-1, c, :-1] - ref[:-1]).max() < tol
+
+
+def test_df64_fixed_nuclei_vs_exact(elhl, oracle_mod, flake):
+    """DF64 (FP32 pairs on the FP32 pipes, implicit operator) on the flake: 20 steps
+    against the exact propagator at the FP64 bar, 1e-10."""
+    S = oracle_mod.overlap(flake)
+    bra, ket = oracle_mod.initial_states(flake, S, 41, 40)
+    pops, b, k, st = _cheb(elhl, flake, 20, elhl.PREC_DF64, 2)
+    ref = _exact(oracle_mod, flake, ket, 20 * 1e-4)
+    assert np.abs(pops[-1] - ref).max() < 1e-10
+    assert st.phases == 3
+
+
+def test_df64_moving_nuclei_vs_taylor_oracle(elhl, oracle_mod):
+    """DF64 with moving nuclei, bra and ket carried (ncols = 4): the reference's
+    Taylor step driver at tolerance 1e-12, populations to 1e-9."""
+    sysm = systems.cubic_cluster(n_atoms=64, seed=7)
+    coords = np.stack([systems.perturbed_coords(sysm.coords, i, seed=3) for i in range(4)])
+    S0 = oracle_mod.overlap(sysm, coords[1])
+    bra, ket = oracle_mod.initial_states(sysm, S0, 41, 40)
+    ref = oracle_mod.ReferenceStep(sysm, bra, ket, dt=5e-4, tol=1e-12, norm_tol=1e-12, nthreads=4)
+    rp = np.stack([ref.step(coords[1 + i]).T for i in range(3)])
+    tr = elhl.Trajectory(sysm, coords=coords[1], dt=5e-4, method=elhl.METHOD_CHEBYSHEV, precision=elhl.PREC_DF64,
+                         ncols=4, cheb_tol=1e-14)
+    tr.set_psi(bra, ket)
+    pops = tr.step(coords[1:], nsteps=3)
+    tr.close()
+    assert np.abs(pops - rp).max() < 1e-9
+
+
+def test_df64_cluster_vs_exact(elhl, oracle_mod):
+    """DF64 at N = 1860 (two row chunks per CTA) against the exact propagator, 1e-9."""
+    sysm = systems.cubic_cluster(n_atoms=600, seed=11)
+    homo = systems.fermi_state(sysm, sysm.fragment_atoms("E"))
+    tr = elhl.Trajectory(sysm, coords=sysm.coords, dt=2e-4, method=elhl.METHOD_CHEBYSHEV,
+                         precision=elhl.PREC_DF64, ncols=4, cheb_tol=1e-14)
+    tr.init_fmo(homo + 1, homo)
+    pops = tr.step(np.stack([sysm.coords] * 2), nsteps=2)
+    tr.close()
+    ket0, _ = oracle_mod.fragment_mo(sysm, "E", homo + 1)
+    ref = _exact(oracle_mod, sysm, np.column_stack([ket0, oracle_mod.fragment_mo(sysm, "H", homo)[0]]).astype(complex),
+                 4e-4)
+    assert np.abs(pops[-1] - ref).max() < 1e-9
