@@ -307,6 +307,55 @@ def run_ours(args, rank, world):
     return line
 
 
+def run_variant(args, precision_name: str):
+    """The same workload and coordinates with another precision (device-resident
+    steps, CUDA events on the library's stream, L2 flushed between steps): the
+    DF64 variant of the default FP64 run."""
+    import torch
+    from dynemol_gb300 import api, systems
+    dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    api.set_stream(stream.cuda_stream)
+    sysm, dt, moving = workload(args.workload)
+    homo = systems.fermi_state(sysm, np.arange(20))
+    W, K = args.warmup, args.steps
+    coords = step_coords(sysm, moving, W + K + 1)
+    prec = {"fp64": api.PREC_FP64, "fp32": api.PREC_FP32, "df64": api.PREC_DF64}[precision_name]
+    tr = api.Trajectory(sysm, coords=None if coords is None else coords[0], dt=dt, method=api.METHOD_CHEBYSHEV,
+                        precision=prec, ncols=4 if moving else 2, cheb_tol=1e-12)
+    tr.init_fmo(homo + 1, homo)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    d_coords = None if coords is None else torch.from_numpy(coords[1:]).to(dev).contiguous()
+    nf1 = sysm.nfrag + 1
+    d_pops = torch.zeros((W + K) * 2 * nf1, dtype=torch.float64, device=dev)
+    nc = sysm.natoms * 3
+
+    def dev_step(i):
+        if d_coords is None:
+            tr.step(None, nsteps=1, want_pops=False)
+        else:
+            tr.step_device(d_coords.data_ptr() + i * nc * 8, 1, d_pops.data_ptr() + i * 2 * nf1 * 8)
+
+    for i in range(W):
+        dev_step(i)
+    torch.cuda.synchronize(dev)
+    ms = prop = 0.0
+    for i in range(K):
+        flush.fill_(float(i))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        dev_step(W + i)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+        ms += e0.elapsed_time(e1)
+        prop += tr.stats().prop_ms
+    tr.close()
+    api.set_stream(None)
+    return {"precision": precision_name, "value": K / (ms / 1e3), "unit": "steps/s", "ms_per_step": ms / K,
+            "propagation_ms_per_step": prop / K}
+
+
 def run_dropin(args, steps: int = 2):
     """The reference-semantics FP64 Taylor path (the propagationelhl_gpucaller_
     algorithm) on the same workload and coordinates, device-resident, CUDA events."""
@@ -550,6 +599,10 @@ def main():
         import torch
         torch.distributed.init_process_group("nccl")
     line = run_ours(args, rank, world)
+    if rank == 0 and args.method == "chebyshev" and args.precision == "fp64" and args.workload != "flake":
+        # the same moving-nuclei workload with the operator in DF64 (FP32 pairs): FP64-level
+        # populations (tested to 1e-9 against the oracle) without the FP64 pipe
+        line["df64_variant"] = run_variant(args, "df64")
     if rank == 0 and args.method == "chebyshev" and not args.no_dropin:
         line["dropin_taylor_fp64"] = run_dropin(args)
     if rank == 0 and args.mix:

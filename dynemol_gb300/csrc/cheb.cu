@@ -470,14 +470,53 @@ __device__ __forceinline__ void df_fma(float &sh, float &sl, float ah, float al,
     sh = t;
 }
 
+// (ah, al) + (bh, bl) in FP32 pairs (TwoSum of the high parts, low parts added)
+__device__ __forceinline__ void df_add(float &ah, float &al, float bh, float bl) {
+    const float t = __fadd_rn(ah, bh);
+    const float z = __fsub_rn(t, ah);
+    const float y = __fadd_rn(__fsub_rn(ah, __fsub_rn(t, z)), __fsub_rn(bh, z));
+    al = __fadd_rn(al, __fadd_rn(y, bl));
+    ah = t;
+}
+
+// warp sums of NV FP32-pair values (NV = 4 ... 32), all on the FP32 pipe: plain
+// butterflies over the lane bits >= log2(NV), then a transposed butterfly; lane l
+// returns the warp sum of value l % NV
+template <int NV>
+__device__ __forceinline__ float2 df_warp_sums(float (&h)[NV], float (&l)[NV], int lane) {
+#pragma unroll
+    for (int o = 16; o >= NV; o >>= 1)
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            const float oh = __shfl_xor_sync(0xffffffffu, h[i], o), ol = __shfl_xor_sync(0xffffffffu, l[i], o);
+            df_add(h[i], l[i], oh, ol);
+        }
+#pragma unroll
+    for (int o = NV / 2; o > 0; o >>= 1) {
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < o; ++i) {
+            const float sh = upper ? h[i] : h[i + o], sl = upper ? l[i] : l[i + o];
+            float kh = upper ? h[i + o] : h[i], kl = upper ? l[i + o] : l[i];
+            const float rh = __shfl_xor_sync(0xffffffffu, sh, o), rl = __shfl_xor_sync(0xffffffffu, sl, o);
+            df_add(kh, kl, rh, rl);
+            h[i] = kh;
+            l[i] = kl;
+        }
+    }
+    return make_float2(h[0], l[0]);
+}
+
 // rows_gemv for DF64: y_i = sum_j M(j, i) x_j, M float2 (hi, lo) column-major,
 // x staged as float4 (re hi, re lo, im hi, im lo); calls epi(i, c, yr, yi) with
 // FP64 sums.  Same tiling, triangular ranges and warp sums as rows_gemv.
 template <int MG, int TRI, typename Epi>
-__device__ void rows_gemv_df(const float2 *M, int ld, const float4 *s_v, int row0, int row1, double *s_part,
+__device__ void rows_gemv_df(const float2 *M, int ld, const float4 *s_v, int row0, int row1, float2 *s_part,
                              Epi &epi) {
-    constexpr int kRT = 4;             // rows per warp tile
-    constexpr int NV = kRT * MG * 2;   // sums per lane (8 ... 32)
+    // rows per warp tile: 8 for one staged column (4 KB of matrix loads in flight per
+    // warp), 4 for two or four (register budget of the hi/lo accumulators)
+    constexpr int kRT = MG == 1 ? 8 : 4;
+    constexpr int NV = kRT * MG * 2;      // sums per lane (16 ... 32)
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int rows = row1 - row0;
     int WR = 1;
@@ -531,14 +570,18 @@ __device__ void rows_gemv_df(const float2 *M, int ld, const float4 *s_v, int row
             sweep(std::true_type{});
         else if (nr > 0)
             sweep(std::false_type{});
-        // FP64 warp sums, then the fixed-order sum over the WJ slices
+        // warp sums in FP32 pairs (no FP64 instruction in the tile), then the
+        // fixed-order sum over the WJ slices; FP64 only for the tile's outputs
         constexpr int NW = NV < 32 ? NV : 32;
 #pragma unroll
         for (int b = 0; b < NV / NW; ++b) {
-            double tmp[NW];
+            float th[NW], tl[NW];
 #pragma unroll
-            for (int q = 0; q < NW; ++q) tmp[q] = (double)ah[b * NW + q] + (double)al[b * NW + q];
-            const double sm = warp_sums<double, NW>(tmp, lane);
+            for (int q = 0; q < NW; ++q) {
+                th[q] = ah[b * NW + q];
+                tl[q] = al[b * NW + q];
+            }
+            const float2 sm = df_warp_sums<NW>(th, tl, lane);
             if (lane < NW) s_part[((size_t)wj * WR + wr) * NV + b * NW + lane] = sm;
         }
         __syncthreads();
@@ -547,12 +590,14 @@ __device__ void rows_gemv_df(const float2 *M, int ld, const float4 *s_v, int row
             const int r = rem / MG, c = rem % MG;
             const int i = base + kRT * wrr + r;
             if (i >= row1) continue;
-            double yr = 0.0, yi = 0.0;
+            float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
             for (int w = 0; w < WJ; ++w) {
-                yr += s_part[((size_t)w * WR + wrr) * NV + (r * MG + c) * 2 + 0];
-                yi += s_part[((size_t)w * WR + wrr) * NV + (r * MG + c) * 2 + 1];
+                const float2 a = s_part[((size_t)w * WR + wrr) * NV + (r * MG + c) * 2 + 0];
+                const float2 b = s_part[((size_t)w * WR + wrr) * NV + (r * MG + c) * 2 + 1];
+                df_add(rh, rl, a.x, a.y);
+                df_add(ih, il, b.x, b.y);
             }
-            epi(i, c, yr, yi);
+            epi(i, c, (double)rh + (double)rl, (double)ih + (double)il);
         }
         __syncthreads();
     }
@@ -619,7 +664,7 @@ __device__ void order_zero_df(const ChebProblem &pb, const ChebSegment &sg, int 
 
 template <int MG>
 __device__ void implicit_phase_df(const ChebLaunch &L, const ChebProblem &pb, int s0, int s1, int k, int ph, int g,
-                                  float4 *s_v, double *s_part, double cre, double cim) {
+                                  float4 *s_v, float2 *s_part, double cre, double cim) {
     const int ld = pb.ld, m = pb.m;
     float4 *vbuf = reinterpret_cast<float4 *>(pb.vbuf);
     float4 *wb = reinterpret_cast<float4 *>(pb.wb);
@@ -651,7 +696,7 @@ __device__ void implicit_phase_df(const ChebLaunch &L, const ChebProblem &pb, in
 template <int MG>
 __global__ void __launch_bounds__(kBlock, 1) cheb_df_kernel(ChebLaunch L) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    double *s_part = reinterpret_cast<double *>(smem_raw);
+    float2 *s_part = reinterpret_cast<float2 *>(smem_raw);
     float4 *s_v = reinterpret_cast<float4 *>(smem_raw + kCheb_part_bytes);
     const int G = gridDim.x;
     const int s0 = L.seg_begin[blockIdx.x], s1 = L.seg_begin[blockIdx.x + 1];
