@@ -836,7 +836,7 @@ constexpr int kTrmmBase = ELHL_TRMM_BASE;  // triangular products left to cuBLAS
 // large blocks become DGEMMs (cuBLAS DTRMM at these sizes runs on 32 x 32
 // tiles), blocks of at most kTrmmBase rows use DTRMM.
 //   right: X (m x n) <- alpha X T,  T n x n:  [X1 X2] T = [X1 T11 + X2 T21, X2 T22]
-int trmm_right(double alpha, const double *T, int ldt, double *X, int ldx, int m, int n) {
+int trmm_right(double alpha, const double *T, int ldt, double *X, int ldx, int m, int n, bool df) {
     if (n <= kTrmmBase) {
         BLAS_TRY(cublasDtrmm(g_ctx.blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT,
                              m, n, &alpha, T, ldt, X, ldx, X, ldx));
@@ -844,14 +844,17 @@ int trmm_right(double alpha, const double *T, int ldt, double *X, int ldx, int m
     }
     const int n1 = (n / 2 + 63) / 64 * 64, n2 = n - n1;
     const double one = 1.0;
-    if (int rc = trmm_right(alpha, T, ldt, X, ldx, m, n1)) return rc;  // X1 T11
-    BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, m, n1, n2, &alpha, X + (size_t)n1 * ldx, ldx, T + n1,
-                         ldt, &one, X, ldx));                            // + X2 T21
-    return trmm_right(alpha, T + (size_t)n1 * ldt + n1, ldt, X + (size_t)n1 * ldx, ldx, m, n2);  // X2 T22
+    if (int rc = trmm_right(alpha, T, ldt, X, ldx, m, n1, df)) return rc;  // X1 T11
+    if (df)                                                                // + X2 T21
+        CU_TRY(dfgemm(m, n1, n2, alpha, X + (size_t)n1 * ldx, ldx, T + n1, ldt, 1.0, X, ldx, g_ctx.stream));
+    else
+        BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, m, n1, n2, &alpha, X + (size_t)n1 * ldx, ldx,
+                             T + n1, ldt, &one, X, ldx));
+    return trmm_right(alpha, T + (size_t)n1 * ldt + n1, ldt, X + (size_t)n1 * ldx, ldx, m, n2, df);  // X2 T22
 }
 
 //   left: X (m x n) <- alpha T X,  T m x m:  T [X1; X2] = [T11 X1; T21 X1 + T22 X2]
-int trmm_left(double alpha, const double *T, int ldt, double *X, int ldx, int m, int n) {
+int trmm_left(double alpha, const double *T, int ldt, double *X, int ldx, int m, int n, bool df) {
     if (m <= kTrmmBase) {
         BLAS_TRY(cublasDtrmm(g_ctx.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT,
                              m, n, &alpha, T, ldt, X, ldx, X, ldx));
@@ -859,10 +862,13 @@ int trmm_left(double alpha, const double *T, int ldt, double *X, int ldx, int m,
     }
     const int m1 = (m / 2 + 63) / 64 * 64, m2 = m - m1;
     const double one = 1.0;
-    if (int rc = trmm_left(alpha, T + (size_t)m1 * ldt + m1, ldt, X + m1, ldx, m2, n)) return rc;  // T22 X2
-    BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, m2, n, m1, &alpha, T + m1, ldt, X, ldx, &one, X + m1,
-                         ldx));                                          // + T21 X1
-    return trmm_left(alpha, T, ldt, X, ldx, m1, n);                     // T11 X1
+    if (int rc = trmm_left(alpha, T + (size_t)m1 * ldt + m1, ldt, X + m1, ldx, m2, n, df)) return rc;  // T22 X2
+    if (df)                                                                                         // + T21 X1
+        CU_TRY(dfgemm(m2, n, m1, alpha, T + m1, ldt, X, ldx, 1.0, X + m1, ldx, g_ctx.stream));
+    else
+        BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, m2, n, m1, &alpha, T + m1, ldt, X, ldx, &one,
+                             X + m1, ldx));
+    return trmm_left(alpha, T, ldt, X, ldx, m1, n, df);                 // T11 X1
 }
 
 int tri_inverse(ChebState &cs, double *A, int n, int ld) {
@@ -889,8 +895,9 @@ int tri_inverse(ChebState &cs, double *A, int n, int ld) {
     double *A11 = A, *A21 = A + n1, *A22 = A + (size_t)n1 * ld + n1;
     if (int rc = tri_inverse(cs, A11, n1, ld)) return rc;
     if (int rc = tri_inverse(cs, A22, n2, ld)) return rc;
-    if (int rc = trmm_right(-1.0, A11, ld, A21, ld, n2, n1)) return rc;  // -L21 G11
-    return trmm_left(1.0, A22, ld, A21, ld, n2, n1);                     // G22 (.)
+    const bool df = cs.precision == ELHL_PREC_DF64;  // DF64: the GEMMs in double-float on the FP32 pipes
+    if (int rc = trmm_right(-1.0, A11, ld, A21, ld, n2, n1, df)) return rc;  // -L21 G11
+    return trmm_left(1.0, A22, ld, A21, ld, n2, n1, df);                     // G22 (.)
 }
 
 // G = L^-1 (FP64, lower; the upper triangle keeps what dst held) from a copy of

@@ -142,6 +142,11 @@ int split3_bf16(const float *src, int rows, int cols, int lds, __nv_bfloat16 *co
 int umma_bf16x3_gemm(const __nv_bfloat16 *const A[3], int lda, const __nv_bfloat16 *const B[3], int ldb, int rows,
                      int K, int n2, int splits, float *Y, int *d_error, cudaStream_t st);
 
+// C = alpha A B + beta C in double-float arithmetic on the FP32 pipes (dfgemm.cu),
+// column-major FP64 operands, no transposes
+cudaError_t dfgemm(int m, int n, int k, double alpha, const double *A, int lda, const double *B, int ldb, double beta,
+                   double *C, int ldc, cudaStream_t st);
+
 int bessel_j_sequence(double beta, int kmax, double *J);
 int chebyshev_coefficients(double dt, double emin, double emax, double tol, int kcap, std::vector<double> &cre,
                            std::vector<double> &cim, int *K_out);
