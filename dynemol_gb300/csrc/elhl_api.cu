@@ -578,10 +578,8 @@ struct ChebState {
     bool implicit = false;
     void *Gt = nullptr;
     void *wb = nullptr;      // [2][ld][m] launch precision (phase intermediates)
-    void *tri_ws = nullptr;  // trtri device workspace
-    size_t tri_dev = 0, tri_host = 0;
-    std::vector<unsigned char> tri_hbuf;
-    int *tinfo = nullptr;
+    double *fws = nullptr;   // workspace of the recursive factorisations
+    size_t fws_n = 0;
     double *cscratch = nullptr;  // [2m][ld] column-transform output
     int alloc(int N_, int m_, int prec) {
         N = N_;
@@ -619,10 +617,9 @@ struct ChebState {
         umma = false;
         if (Gt) cudaFree(Gt);
         if (wb) cudaFree(wb);
-        if (tri_ws) cudaFree(tri_ws);
-        Gt = wb = tri_ws = nullptr;
-        tri_dev = tri_host = 0;
-        dev_free(tinfo);
+        Gt = wb = nullptr;
+        dev_free(fws);
+        fws_n = 0;
         dev_free(cscratch);
         implicit = false;
         dev_free(gpops);
@@ -817,101 +814,153 @@ __global__ void convert_kernel(const double *__restrict__ src, T *__restrict__ d
     dst[(size_t)j * ld + i] = (T)v;
 }
 
-// In-place inverse of the lower-triangular n x n block A (leading dimension ld):
-// [L11 0; L21 L22]^-1 = [G11 0; -G22 L21 G11  G22], recursively.  Blocks of at
-// most kTriBase rows go to cuSOLVER trtri; the off-diagonal blocks are two
-// in-place cuBLAS DTRMMs, so almost all of the N^3/3 flops run in large
-// triangular-times-square products (cuSOLVER's own trtri at N = 3720 spends
-// most of its time in 32 x 32 tiles).
-#ifndef ELHL_TRI_BASE
-#define ELHL_TRI_BASE 256
-#endif
-#ifndef ELHL_TRMM_BASE
-#define ELHL_TRMM_BASE 256
-#endif
-constexpr int kTriBase = ELHL_TRI_BASE;    // blocks inverted by cuSOLVER trtri
-constexpr int kTrmmBase = ELHL_TRMM_BASE;  // triangular products left to cuBLAS DTRMM
-
-// In-place triangular products with the lower-triangular T (ld), recursively:
-// large blocks become DGEMMs (cuBLAS DTRMM at these sizes runs on 32 x 32
-// tiles), blocks of at most kTrmmBase rows use DTRMM.
-//   right: X (m x n) <- alpha X T,  T n x n:  [X1 X2] T = [X1 T11 + X2 T21, X2 T22]
-int trmm_right(double alpha, const double *T, int ldt, double *X, int ldx, int m, int n, bool df) {
-    if (n <= kTrmmBase) {
-        BLAS_TRY(cublasDtrmm(g_ctx.blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT,
-                             m, n, &alpha, T, ldt, X, ldx, X, ldx));
-        return ELHL_OK;
-    }
-    const int n1 = (n / 2 + 63) / 64 * 64, n2 = n - n1;
-    const double one = 1.0;
-    if (int rc = trmm_right(alpha, T, ldt, X, ldx, m, n1, df)) return rc;  // X1 T11
-    if (df)                                                                // + X2 T21
-        CU_TRY(dfgemm(m, n1, n2, alpha, X + (size_t)n1 * ldx, ldx, T + n1, ldt, 1.0, X, ldx, g_ctx.stream));
-    else
-        BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, m, n1, n2, &alpha, X + (size_t)n1 * ldx, ldx,
-                             T + n1, ldt, &one, X, ldx));
-    return trmm_right(alpha, T + (size_t)n1 * ldt + n1, ldt, X + (size_t)n1 * ldx, ldx, m, n2, df);  // X2 T22
+// zero the strictly upper triangle and the padding rows of an ld x n matrix
+__global__ void lower_only_kernel(double *A, int n, int ld) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i < ld && j < n && (i < j || i >= n)) A[(size_t)j * ld + i] = 0.0;
 }
 
-//   left: X (m x n) <- alpha T X,  T m x m:  T [X1; X2] = [T11 X1; T21 X1 + T22 X2]
-int trmm_left(double alpha, const double *T, int ldt, double *X, int ldx, int m, int n, bool df) {
-    if (m <= kTrmmBase) {
-        BLAS_TRY(cublasDtrmm(g_ctx.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT,
-                             m, n, &alpha, T, ldt, X, ldx, X, ldx));
-        return ELHL_OK;
+// ---- inverse of the Cholesky factor --------------------------------------------
+// Workspace of the recursive factorisations: ld x (ld / 2 + 256) doubles, enough
+// for the off-diagonal block of the top split and for every batched level.
+int factor_workspace(ChebState &cs, double **W) {
+    const size_t need = (size_t)cs.ld * (cs.ld / 2 + 256);
+    if (cs.fws_n < need) {
+        dev_free(cs.fws);
+        cs.fws_n = 0;
+        if (int rc = dev_alloc(&cs.fws, need)) return rc;
+        cs.fws_n = need;
     }
-    const int m1 = (m / 2 + 63) / 64 * 64, m2 = m - m1;
-    const double one = 1.0;
-    if (int rc = trmm_left(alpha, T + (size_t)m1 * ldt + m1, ldt, X + m1, ldx, m2, n, df)) return rc;  // T22 X2
-    if (df)                                                                                         // + T21 X1
-        CU_TRY(dfgemm(m2, n, m1, alpha, T + m1, ldt, X, ldx, 1.0, X + m1, ldx, g_ctx.stream));
-    else
-        BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, m2, n, m1, &alpha, T + m1, ldt, X, ldx, &one,
-                             X + m1, ldx));
-    return trmm_left(alpha, T, ldt, X, ldx, m1, n, df);                 // T11 X1
+    *W = cs.fws;
+    return ELHL_OK;
 }
 
-int tri_inverse(ChebState &cs, double *A, int n, int ld) {
-    if (n <= kTriBase) {
-        size_t dev = 0, host = 0;
-        SOLVER_TRY(cusolverDnXtrtri_bufferSize(g_ctx.solver, CUBLAS_FILL_MODE_LOWER, CUBLAS_DIAG_NON_UNIT, n,
-                                               CUDA_R_64F, A, ld, &dev, &host));
-        if (dev > cs.tri_dev || !cs.tri_ws) {
-            CU_TRY(cudaStreamSynchronize(g_ctx.stream));
-            if (cs.tri_ws) cudaFree(cs.tri_ws);
-            cs.tri_ws = nullptr;
-            cs.tri_dev = std::max<size_t>(dev, 16);
-            CU_TRY(cudaMalloc(&cs.tri_ws, cs.tri_dev));
-        }
-        if (host > cs.tri_host || cs.tri_hbuf.empty()) {
-            cs.tri_host = std::max<size_t>(host, 16);
-            cs.tri_hbuf.assign(cs.tri_host, 0);
-        }
-        SOLVER_TRY(cusolverDnXtrtri(g_ctx.solver, CUBLAS_FILL_MODE_LOWER, CUBLAS_DIAG_NON_UNIT, n, CUDA_R_64F, A, ld,
-                                    cs.tri_ws, cs.tri_dev, cs.tri_hbuf.data(), cs.tri_host, cs.tinfo));
+constexpr int kTriBlock = 256;   // diagonal blocks finished by the batched bottom-up levels
+constexpr int kTrmmLeaf = 256;   // triangular products of at most this order run as one full DGEMM
+
+// Y (m x n, ldy) = alpha X T for the lower-triangular T (n x n, zero upper
+// triangle), out of place, recursively:
+//   [X1 X2] [T11 0; T21 T22] = [X1 T11 + X2 T21, X2 T22].
+// Blocks of order <= kTrmmLeaf are one DGEMM over the full square (twice the
+// triangular flops on under an eighth of the work; cuBLAS DTRMM at these
+// sizes runs on a few CTAs for 65 us a call).
+int trmm_right_oop(double alpha, const double *X, int ldx, const double *T, int ldt, double *Y, int ldy, int m, int n) {
+    const double zero = 0.0, one = 1.0;
+    if (n <= kTrmmLeaf) {
+        BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, m, n, n, &alpha, X, ldx, T, ldt, &zero, Y, ldy));
         return ELHL_OK;
     }
-    const int n1 = std::min(n - 1, (n / 2 + 63) / 64 * 64), n2 = n - n1;
+    const int n1 = round_up(n / 2, 64), n2 = n - n1;
+    if (int rc = trmm_right_oop(alpha, X, ldx, T, ldt, Y, ldy, m, n1)) return rc;  // Y1 = X1 T11
+    BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, m, n1, n2, &alpha, X + (size_t)n1 * ldx, ldx, T + n1,
+                         ldt, &one, Y, ldy));                                     // Y1 += X2 T21
+    return trmm_right_oop(alpha, X + (size_t)n1 * ldx, ldx, T + (size_t)n1 * ldt + n1, ldt, Y + (size_t)n1 * ldy, ldy,
+                          m, n2);                                                  // Y2 = X2 T22
+}
+
+// Y (m x n, ldy) = alpha T X for the lower-triangular T (m x m), out of place:
+//   [T11 0; T21 T22] [X1; X2] = [T11 X1; T21 X1 + T22 X2].
+int trmm_left_oop(double alpha, const double *T, int ldt, const double *X, int ldx, double *Y, int ldy, int m, int n) {
+    const double zero = 0.0, one = 1.0;
+    if (m <= kTrmmLeaf) {
+        BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, m, n, m, &alpha, T, ldt, X, ldx, &zero, Y, ldy));
+        return ELHL_OK;
+    }
+    const int m1 = round_up(m / 2, 64), m2 = m - m1;
+    if (int rc = trmm_left_oop(alpha, T, ldt, X, ldx, Y, ldy, m1, n)) return rc;  // Y1 = T11 X1
+    if (int rc = trmm_left_oop(alpha, T + (size_t)m1 * ldt + m1, ldt, X + m1, ldx, Y + m1, ldy, m2, n)) return rc;
+    BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, m2, n, m1, &alpha, T + m1, ldt, X, ldx, &one, Y + m1,
+                         ldy));                                                    // Y2 += T21 X1
+    return ELHL_OK;
+}
+
+// Above kTriBlock rows: [L11 0; L21 L22]^-1 = [G11 0; -G22 L21 G11  G22], the
+// splits on multiples of kTriBlock so that the leaves are the blocks the
+// bottom-up levels finished.
+int tri_inverse_top(double *A, int n, int ld, double *W) {
+    if (n <= kTriBlock) return ELHL_OK;
+    const int n1 = round_up(n / 2, kTriBlock), n2 = n - n1;
     double *A11 = A, *A21 = A + n1, *A22 = A + (size_t)n1 * ld + n1;
-    if (int rc = tri_inverse(cs, A11, n1, ld)) return rc;
-    if (int rc = tri_inverse(cs, A22, n2, ld)) return rc;
-    const bool df = cs.precision == ELHL_PREC_DF64;  // DF64: the GEMMs in double-float on the FP32 pipes
-    if (int rc = trmm_right(-1.0, A11, ld, A21, ld, n2, n1, df)) return rc;  // -L21 G11
-    return trmm_left(1.0, A22, ld, A21, ld, n2, n1, df);                     // G22 (.)
+    if (int rc = tri_inverse_top(A11, n1, ld, W)) return rc;
+    if (int rc = tri_inverse_top(A22, n2, ld, W)) return rc;
+    if (int rc = trmm_right_oop(1.0, A21, ld, A11, ld, W, ld, n2, n1)) return rc;  // W = L21 G11
+    return trmm_left_oop(-1.0, A22, ld, W, ld, A21, ld, n2, n1);                   // A21 = -G22 W
 }
 
-// G = L^-1 (FP64, lower; the upper triangle keeps what dst held) from a copy of
-// the Cholesky factor: N^3/3 flops.
+// G = L^-1 in place for the n x n lower-triangular A (zero upper triangle), FP64:
+//  1. every 64-row diagonal block by leaf_inverse, one launch;
+//  2. bottom-up, s = 64 and 128: pairs of inverted s-blocks become inverted
+//     2s-blocks, G21 = -G22 (L21 G11), as two strided-batched DGEMMs over all
+//     complete pairs and two plain ones for a short last pair (full products
+//     of triangular blocks; these levels hold about 2 % of the flops);
+//  3. top-down above 256 rows (tri_inverse_top), N^3/3 flops in large DGEMMs.
+int tri_inverse(ChebState &cs, double *A, int n, int ld) {
+    cudaStream_t st = g_ctx.stream;
+    double *W = nullptr;
+    if (int rc = factor_workspace(cs, &W)) return rc;
+    CU_TRY(leaf_inverse(A, n, ld, st));
+    const double one = 1.0, mone = -1.0, zero = 0.0;
+    for (int s = leaf_rows(); s < kTriBlock; s *= 2) {
+        const int np = n / (2 * s), rem = n - 2 * s * np;
+        const long long stride = (long long)2 * s * (ld + 1), ws = (long long)s * s;
+        if (np > 0) {
+            BLAS_TRY(cublasDgemmStridedBatched(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, s, s, s, &one, A + s, ld, stride,
+                                               A, ld, stride, &zero, W, s, ws, np));  // W_p = L21 G11
+            BLAS_TRY(cublasDgemmStridedBatched(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, s, s, s, &mone,
+                                               A + (size_t)s * (ld + 1), ld, stride, W, s, ws, &zero, A + s, ld,
+                                               stride, np));                           // G21 = -G22 W_p
+        }
+        if (rem > s) {  // short last pair: s rows over rem - s rows
+            const int n2 = rem - s;
+            double *P = A + (size_t)2 * s * np * (ld + 1);
+            BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n2, s, s, &one, P + s, ld, P, ld, &zero, W,
+                                 n2));
+            BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n2, s, n2, &mone, P + (size_t)s * (ld + 1), ld,
+                                 W, n2, &zero, P + s, ld));
+        }
+    }
+    return tri_inverse_top(A, n, ld, W);
+}
+
+// G = L^-1 (FP64, lower, zero upper triangle) from a copy of the Cholesky factor:
+// N^3/3 flops.
 int invert_factor(ChebState &cs, const double *Lfac, double *dst) {
     cudaStream_t st = g_ctx.stream;
     const int n = cs.N, ld = cs.ld;
     CU_TRY(cudaMemcpy2DAsync(dst, ld * sizeof(double), Lfac, ld * sizeof(double), n * sizeof(double), n,
                              cudaMemcpyDeviceToDevice, st));
-    if (!cs.tinfo) {
-        if (int rc = dev_alloc(&cs.tinfo, 1)) return rc;
-        CU_TRY(cudaMemset(cs.tinfo, 0, sizeof(int)));
-    }
+    lower_only_kernel<<<dim3((ld + 127) / 128, n), 128, 0, st>>>(dst, n, ld);  // potrf leaves S above the diagonal
+    CU_TRY(cudaGetLastError());
     return tri_inverse(cs, dst, n, ld);
+}
+
+// Cholesky factor and its inverse together, in place, for the DF64 rebuild:
+// A (n x n, lower) <- L, G <- L^-1, recursively with every product in
+// double-float arithmetic on the FP32 pipes (dfgemm, triangular operands at
+// half cost):
+//   L11, G11 = chol_inv(A11);   L21 = A21 G11^T;   A22 -= L21 L21^T;
+//   L22, G22 = chol_inv(A22);   G21 = -G22 (L21 G11),
+// N^3/3 + N^3/3 flops, the 64-row diagonal blocks in FP64 (leaf_chol_inv).
+// The upper triangles of A and G are left undefined.
+int chol_inv_df(double *A, double *G, int n, int ld, int row0, double *W, int *info) {
+    cudaStream_t st = g_ctx.stream;
+    const int leaf = leaf_rows();
+    if (n <= leaf) {
+        CU_TRY(leaf_chol_inv(A, G, n, ld, row0, info, st));
+        return ELHL_OK;
+    }
+    const int n1 = round_up(n / 2, leaf), n2 = n - n1;
+    double *A21 = A + n1, *A22 = A + (size_t)n1 * ld + n1;
+    double *G21 = G + n1, *G22 = G + (size_t)n1 * ld + n1;
+    if (int rc = chol_inv_df(A, G, n1, ld, row0, W, info)) return rc;
+    CU_TRY(cudaMemcpy2DAsync(W, ld * sizeof(double), A21, ld * sizeof(double), n2 * sizeof(double), n1,
+                             cudaMemcpyDeviceToDevice, st));
+    CU_TRY(dfgemm(n2, n1, n1, 1.0, W, ld, G, ld, 0.0, A21, ld, st, true, kTriBt));              // L21
+    CU_TRY(dfgemm(n2, n2, n1, -1.0, A21, ld, A21, ld, 1.0, A22, ld, st, true, kTriLowerC));    // Schur
+    if (int rc = chol_inv_df(A22, G22, n2, ld, row0 + n1, W, info)) return rc;
+    CU_TRY(dfgemm(n2, n1, n1, 1.0, A21, ld, G, ld, 0.0, W, ld, st, false, kTriB));             // L21 G11
+    CU_TRY(dfgemm(n2, n1, n2, -1.0, G22, ld, W, ld, 0.0, G21, ld, st, false, kTriA));          // G21
+    return ELHL_OK;
 }
 
 // A = L^-1 and B = L^T (launch precision) for the device read-out of fixed nuclei.
@@ -941,16 +990,12 @@ int cheb_prepare_readout(ChebState &cs, const double *Lfac) {
     return rc;
 }
 
-// zero the strictly upper triangle and the padding rows of an ld x n matrix
-__global__ void lower_only_kernel(double *A, int n, int ld) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-    if (i < ld && j < n && (i < j || i >= n)) A[(size_t)j * ld + i] = 0.0;
-}
-
-// Implicit operator for the current factor and h: G = L^-1 (FP64, in cs.Ht),
-// bounds by Lanczos on G h G^T, Hs = h/b, and A = G, Gt = G^T, B = L^T in the
-// launch precision.  N^3/3 flops (trtri) instead of the 2 N^3 of forming H~.
-int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, double dt, double tol) {
+// Implicit operator for the current factor and h: G = L^-1 (FP64, in cs.Ht;
+// already there when have_inverse), bounds by Lanczos on G h G^T, Hs = h/b,
+// and A = G, Gt = G^T, B = L^T in the launch precision.  N^3/3 flops for the
+// inverse instead of the 2 N^3 of forming H~.
+int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, double dt, double tol,
+                          bool have_inverse = false) {
     cudaStream_t st = g_ctx.stream;
     const int n = cs.N, ld = cs.ld;
     const size_t tsz = wide_storage(cs.precision) ? sizeof(double) : sizeof(float);
@@ -966,7 +1011,8 @@ int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, do
     // L with a zero upper triangle (potrf leaves S there): the dense column transforms read all of it
     lower_only_kernel<<<dim3((ld + 127) / 128, n), 128, 0, st>>>(const_cast<double *>(Lfac), n, ld);
     CU_TRY(cudaGetLastError());
-    if (int rc = invert_factor(cs, Lfac, cs.Ht)) return rc;
+    if (!have_inverse)
+        if (int rc = invert_factor(cs, Lfac, cs.Ht)) return rc;
     CU_TRY(cudaEventRecord(g_ctx.ev[6], st));
     lower_only_kernel<<<dim3((ld + 127) / 128, n), 128, 0, st>>>(cs.Ht, n, ld);
     CU_TRY(cudaGetLastError());
@@ -1647,12 +1693,21 @@ int cheb_rebuild_operator(elhl_traj *tr, bool implicit = false) {
     cudaStream_t st = g_ctx.stream;
     CU_TRY(cudaMemcpy2DAsync(tr->fac.L, tr->ld * sizeof(double), tr->S, tr->ld * sizeof(double), tr->N * sizeof(double),
                              tr->N, cudaMemcpyDeviceToDevice, st));
-    SOLVER_TRY(cusolverDnDpotrf(g_ctx.solver, CUBLAS_FILL_MODE_LOWER, tr->N, tr->fac.L, tr->ld, tr->fac.work,
-                                tr->fac.lwork, tr->fac.info));
+    const bool together = implicit && tr->cs.precision == ELHL_PREC_DF64;  // factor and inverse in one recursion
+    if (together) {
+        double *W = nullptr;
+        if (int rc = factor_workspace(tr->cs, &W)) return rc;
+        CU_TRY(cudaMemsetAsync(tr->fac.info, 0, sizeof(int), st));
+        if (int rc = chol_inv_df(tr->fac.L, tr->cs.Ht, tr->N, tr->ld, 0, W, tr->fac.info)) return rc;
+    } else {
+        SOLVER_TRY(cusolverDnDpotrf(g_ctx.solver, CUBLAS_FILL_MODE_LOWER, tr->N, tr->fac.L, tr->ld, tr->fac.work,
+                                    tr->fac.lwork, tr->fac.info));
+    }
     CU_TRY(cudaEventRecord(g_ctx.ev[5], st));
     if (int rc = tr->fac.check_info(false)) return rc;
     if (implicit)
-        return cheb_prepare_implicit(tr->cs, tr->fac.L, tr->h, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol);
+        return cheb_prepare_implicit(tr->cs, tr->fac.L, tr->h, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol,
+                                     together);
     tr->cs.implicit = false;
     if (int rc = form_htilde(tr->cs, tr->fac.L, tr->h, tr->ld)) return rc;
     if (int rc = lanczos_bounds(tr->cs, 40)) return rc;
