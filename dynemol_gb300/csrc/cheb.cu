@@ -22,6 +22,7 @@
 //   FP64 coefficients and accumulation.
 #include <type_traits>
 
+#include "df64.cuh"
 #include "elhl_internal.cuh"
 #include "grid_sync.cuh"
 
@@ -442,41 +443,13 @@ __global__ void reduce_pops_kernel(ChebLaunch L, int nprob) {
 // operator and the series vectors as unevaluated sums hi + lo of two FP32
 // numbers (48-bit significands, about 4e-15 relative) and evaluates the
 // products on the FP32 pipes: Dekker's exact product error by FMA and Knuth's
-// TwoSum for the running sums, with round-to-nearest intrinsics so that no
-// operation is contracted.  Sums leave the row loop in FP64; the recurrence and
+// TwoSum for the running sums (df64.cuh).  Sums leave the row loop in FP64; the recurrence and
 // the accumulation of c_k v_k are FP64 as in the other precisions.  Implicit
 // operator only (G, h/b and G^T stored as float2 = (hi, lo)).
-
-__device__ __forceinline__ float2 df_split(double x) {
-    const float h = __double2float_rn(x);
-    return make_float2(h, __double2float_rn(x - (double)h));
-}
 
 __device__ __forceinline__ float4 df_split2(double re, double im) {
     const float2 a = df_split(re), b = df_split(im);
     return make_float4(a.x, a.y, b.x, b.y);
-}
-
-// (sh, sl) += (ah + al)(bh + bl), dropping al bl (2^-48 relative)
-__device__ __forceinline__ void df_fma(float &sh, float &sl, float ah, float al, float bh, float bl) {
-    const float p = __fmul_rn(ah, bh);
-    float e = __fmaf_rn(ah, bh, -p);
-    e = __fmaf_rn(ah, bl, e);
-    e = __fmaf_rn(al, bh, e);
-    const float t = __fadd_rn(sh, p);
-    const float z = __fsub_rn(t, sh);
-    const float y = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, z)), __fsub_rn(p, z));
-    sl = __fadd_rn(sl, __fadd_rn(y, e));
-    sh = t;
-}
-
-// (ah, al) + (bh, bl) in FP32 pairs (TwoSum of the high parts, low parts added)
-__device__ __forceinline__ void df_add(float &ah, float &al, float bh, float bl) {
-    const float t = __fadd_rn(ah, bh);
-    const float z = __fsub_rn(t, ah);
-    const float y = __fadd_rn(__fsub_rn(ah, __fsub_rn(t, z)), __fsub_rn(bh, z));
-    al = __fadd_rn(al, __fadd_rn(y, bl));
-    ah = t;
 }
 
 // warp sums of NV FP32-pair values (NV = 4 ... 32), all on the FP32 pipe: plain

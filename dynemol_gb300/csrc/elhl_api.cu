@@ -935,31 +935,47 @@ int invert_factor(ChebState &cs, const double *Lfac, double *dst) {
 }
 
 // Cholesky factor and its inverse together, in place, for the DF64 rebuild:
-// A (n x n, lower) <- L, G <- L^-1, recursively with every product in
-// double-float arithmetic on the FP32 pipes (dfgemm, triangular operands at
-// half cost):
+// A (n x n, lower) <- L, G <- L^-1, all three matrices (and the workspace W)
+// held as DF64 pairs and every product in double-float arithmetic on the FP32
+// pipes (dfgemm, triangular operands at half cost):
 //   L11, G11 = chol_inv(A11);   L21 = A21 G11^T;   A22 -= L21 L21^T;
 //   L22, G22 = chol_inv(A22);   G21 = -G22 (L21 G11),
-// N^3/3 + N^3/3 flops, the 64-row diagonal blocks in FP64 (leaf_chol_inv).
+// N^3/3 + N^3/3 flops, with 64-row diagonal blocks as leaves (leaf_chol_inv_df).
 // The upper triangles of A and G are left undefined.
-int chol_inv_df(double *A, double *G, int n, int ld, int row0, double *W, int *info) {
+int chol_inv_df(float2 *A, float2 *G, int n, int ld, int row0, float2 *W, int *info) {
     cudaStream_t st = g_ctx.stream;
     const int leaf = leaf_rows();
     if (n <= leaf) {
-        CU_TRY(leaf_chol_inv(A, G, n, ld, row0, info, st));
+        CU_TRY(leaf_chol_inv_df(A, G, n, ld, row0, info, st));
         return ELHL_OK;
     }
     const int n1 = round_up(n / 2, leaf), n2 = n - n1;
-    double *A21 = A + n1, *A22 = A + (size_t)n1 * ld + n1;
-    double *G21 = G + n1, *G22 = G + (size_t)n1 * ld + n1;
+    float2 *A21 = A + n1, *A22 = A + (size_t)n1 * ld + n1;
+    float2 *G21 = G + n1, *G22 = G + (size_t)n1 * ld + n1;
     if (int rc = chol_inv_df(A, G, n1, ld, row0, W, info)) return rc;
-    CU_TRY(cudaMemcpy2DAsync(W, ld * sizeof(double), A21, ld * sizeof(double), n2 * sizeof(double), n1,
+    CU_TRY(cudaMemcpy2DAsync(W, ld * sizeof(float2), A21, ld * sizeof(float2), n2 * sizeof(float2), n1,
                              cudaMemcpyDeviceToDevice, st));
     CU_TRY(dfgemm(n2, n1, n1, 1.0, W, ld, G, ld, 0.0, A21, ld, st, true, kTriBt));              // L21
     CU_TRY(dfgemm(n2, n2, n1, -1.0, A21, ld, A21, ld, 1.0, A22, ld, st, true, kTriLowerC));    // Schur
     if (int rc = chol_inv_df(A22, G22, n2, ld, row0 + n1, W, info)) return rc;
     CU_TRY(dfgemm(n2, n1, n1, 1.0, A21, ld, G, ld, 0.0, W, ld, st, false, kTriB));             // L21 G11
     CU_TRY(dfgemm(n2, n1, n2, -1.0, G22, ld, W, ld, 0.0, G21, ld, st, false, kTriA));          // G21
+    return ELHL_OK;
+}
+
+// L = chol(S) in Lfac and G = L^-1 in G, both FP64 on return, by chol_inv_df
+// on DF64 pairs converted in place.
+int chol_inv_pairs(ChebState &cs, double *Lfac, double *G, int *info) {
+    cudaStream_t st = g_ctx.stream;
+    double *W = nullptr;
+    if (int rc = factor_workspace(cs, &W)) return rc;
+    CU_TRY(cudaMemsetAsync(info, 0, sizeof(int), st));
+    CU_TRY(df_convert(Lfac, cs.N, cs.N, cs.ld, true, st));
+    if (int rc = chol_inv_df(reinterpret_cast<float2 *>(Lfac), reinterpret_cast<float2 *>(G), cs.N, cs.ld, 0,
+                             reinterpret_cast<float2 *>(W), info))
+        return rc;
+    CU_TRY(df_convert(Lfac, cs.N, cs.N, cs.ld, false, st));
+    CU_TRY(df_convert(G, cs.N, cs.N, cs.ld, false, st));
     return ELHL_OK;
 }
 
@@ -1695,10 +1711,7 @@ int cheb_rebuild_operator(elhl_traj *tr, bool implicit = false) {
                              tr->N, cudaMemcpyDeviceToDevice, st));
     const bool together = implicit && tr->cs.precision == ELHL_PREC_DF64;  // factor and inverse in one recursion
     if (together) {
-        double *W = nullptr;
-        if (int rc = factor_workspace(tr->cs, &W)) return rc;
-        CU_TRY(cudaMemsetAsync(tr->fac.info, 0, sizeof(int), st));
-        if (int rc = chol_inv_df(tr->fac.L, tr->cs.Ht, tr->N, tr->ld, 0, W, tr->fac.info)) return rc;
+        if (int rc = chol_inv_pairs(tr->cs, tr->fac.L, tr->cs.Ht, tr->fac.info)) return rc;
     } else {
         SOLVER_TRY(cusolverDnDpotrf(g_ctx.solver, CUBLAS_FILL_MODE_LOWER, tr->N, tr->fac.L, tr->ld, tr->fac.work,
                                     tr->fac.lwork, tr->fac.info));

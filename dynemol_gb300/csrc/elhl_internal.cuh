@@ -143,23 +143,28 @@ int umma_bf16x3_gemm(const __nv_bfloat16 *const A[3], int lda, const __nv_bfloat
                      int K, int n2, int splits, float *Y, int *d_error, cudaStream_t st);
 
 // C = alpha A op(B) + beta C in double-float arithmetic on the FP32 pipes (dfgemm.cu),
-// column-major FP64 operands, op(B) = B^T when transB.  `tri` marks lower-
+// column-major operands stored as DF64 pairs (float2 = hi + lo), op(B) = B^T
+// when transB.  `tri` marks lower-
 // triangular operands (kTriA: A; kTriB: B; kTriBt: op(B) = B^T of a lower B)
 // and kTriLowerC a symmetric update that writes only the tiles on or below
 // the diagonal.
 constexpr int kTriA = 1, kTriB = 2, kTriBt = 4, kTriLowerC = 8;
-cudaError_t dfgemm(int m, int n, int k, double alpha, const double *A, int lda, const double *B, int ldb, double beta,
-                   double *C, int ldc, cudaStream_t st, bool transB = false, int tri = 0);
+cudaError_t dfgemm(int m, int n, int k, double alpha, const float2 *A, int lda, const float2 *B, int ldb, double beta,
+                   float2 *C, int ldc, cudaStream_t st, bool transB = false, int tri = 0);
+// rows x n block of an FP64 matrix (leading dimension ld) to DF64 pairs in
+// place (to_pairs) or back
+cudaError_t df_convert(double *x, int rows, int n, int ld, bool to_pairs, cudaStream_t st);
 
-// Diagonal-block leaves of the recursive factorisations (factor.cu), FP64 in
+// Diagonal-block leaves of the recursive factorisations (factor.cu), in
 // shared memory, blocks of leaf_rows() = 64 rows:
-//   leaf_inverse:  every diagonal block of the n x n lower-triangular A
-//                  replaced by its inverse, one CTA per block;
-//   leaf_chol_inv: A (nb x nb, nb <= 64) <- chol(A), G <- its inverse; a
-//                  non-positive pivot sets *info (if still 0) to row0 + column + 1.
+//   leaf_inverse:     every diagonal block of the n x n lower-triangular A
+//                     replaced by its inverse, one CTA per block (FP64);
+//   leaf_chol_inv_df: A (nb x nb, nb <= 64, DF64 pairs) <- chol(A), G <- its
+//                     inverse; a non-positive pivot sets *info (if still 0)
+//                     to row0 + column + 1.
 int leaf_rows();
 cudaError_t leaf_inverse(double *A, int n, int ld, cudaStream_t st);
-cudaError_t leaf_chol_inv(double *A, double *G, int nb, int ld, int row0, int *info, cudaStream_t st);
+cudaError_t leaf_chol_inv_df(float2 *A, float2 *G, int nb, int ld, int row0, int *info, cudaStream_t st);
 
 int bessel_j_sequence(double beta, int kmax, double *J);
 int chebyshev_coefficients(double dt, double emin, double emax, double tol, int kcap, std::vector<double> &cre,
