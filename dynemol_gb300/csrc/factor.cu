@@ -6,23 +6,17 @@
 //                             once (FP64);
 //   leaf_chol_inv_df_kernel:  L = chol(A) and G = L^-1 for one diagonal block,
 //                             in DF64 pairs on the FP32 pipes (the DF64
-//                             rebuild), pivots' 1/sqrt included.
+//                             rebuild), pivots' 1/sqrt included, blocked by 8.
 // Library triangular kernels at these sizes (cuSOLVER trtri on 256 rows,
-// cuBLAS DTRMM/DTRSM panels) run on a handful of CTAs for 65-106 us per call;
-// one leaf here is one barrier per column and little more FP64 work than
-// the flops themselves: the FP64 pipe of one SM retires about two FMAs per
-// clock, so a warp instruction with idle lanes costs as much as a full one.
-// Work is therefore laid out by rows: warp w takes rows i = w (mod 8) of the
-// active part and its lanes the active columns of the row, and the pivot's
-// reciprocal square root is taken once, by the thread that finished the pivot.
+// cuBLAS DTRMM/DTRSM panels) run on a handful of CTAs for 65-106 us per call.
 //
-// Both are column sweeps.  Cholesky, step k (right-looking):
-//   r = 1/sqrt(a_kk);  a_ij -= (a_ik r)(a_jk r)   for i >= j > k,
-// leaving column k unscaled (L(i, k) = a_ik r), so that a step only writes
-// columns right of the ones it reads and needs one barrier.  Inverse, step k:
-// row k of X holds L(k, k) G(k, :) and, for rows i > k,
+// The FP64 leaf is a column sweep, one barrier per column.  Row k of X holds
+// L(k, k) G(k, :) after step k and, for rows i > k,
 //   x_ij -= L(i, k) / L(k, k) * x_kj   for j <= k;
-// at the end G(i, j) = x_ij / L(i, i).
+// at the end G(i, j) = x_ij / L(i, i).  The FP64 pipe of one SM retires about
+// two FMAs per clock, so a warp instruction with idle lanes costs as much as a
+// full one: warp w takes rows i = w (mod 8) and its lanes the active columns.
+// The DF64 leaf is blocked to need few barriers (see its comment).
 #include "df64.cuh"
 #include "elhl_internal.cuh"
 
@@ -109,71 +103,150 @@ __global__ void __launch_bounds__(kThreads) leaf_inverse_kernel(double *A, int n
 
 // L = chol(A) in place and G = L^-1 for the nb x nb diagonal block at offset r
 // (global row of its first column, for the status word), A and G as DF64
-// pairs.  A non-positive pivot sets *info to its 1-based global column (the
-// first one found) and the factorisation carries on with a zero scale, so the
-// launch always ends.
+// pairs, blocked so that few steps wait at a block-wide barrier:
+//   Cholesky, for each 8-column block b (rows past nb padded with identity):
+//     (1) warp 0 factors and inverts the 8 x 8 diagonal block (column sweeps
+//         under __syncwarp only);
+//     (2) panel L_rb = A_rb G_bb^T for the rows below;
+//     (3) trailing update A_rr -= L_rb L_rb^T;
+//   inverse by doubling, s = 8, 16, 32: G21 = -G22 (L21 G11) for all pairs.
+// About 30 barriers instead of one per column.  A non-positive pivot sets
+// *info to its 1-based global column (the first one found) and the
+// factorisation carries on with a zero scale, so the launch always ends.
+constexpr int kDiag = 8, kPPitch = kDiag + 1;
+constexpr size_t kLeafDfSmem =
+    (size_t)(2 * kLeaf * kPitch + kLeaf * kPPitch + 32 * kLeaf + 2 * kDiag) * sizeof(float2);
+
 __global__ void __launch_bounds__(kThreads) leaf_chol_inv_df_kernel(float2 *A, float2 *G, int nb, int ld, int r,
                                                                     int *info) {
     extern __shared__ double smem[];
-    float2 *As = reinterpret_cast<float2 *>(smem), *X = As + kLeaf * kPitch;
-    float2 *rd = X + kLeaf * kPitch, *sc = rd + kLeaf;
-    const int j = own_col(), r0 = own_row0(), lane = threadIdx.x % 32;
-    const float2 zero = make_float2(0.f, 0.f);
-#pragma unroll
-    for (int q = 0; q < kRowsPerThread; ++q) {
-        const int i = r0 + 4 * q;
-        As[i * kPitch + j] = (i < nb && j < nb && i >= j) ? A[(size_t)j * ld + i] : zero;
-        X[i * kPitch + j] = (i == j && i < nb) ? make_float2(1.f, 0.f) : zero;
+    float2 *As = reinterpret_cast<float2 *>(smem);  // [64][kPitch]: A, then L
+    float2 *Gs = As + kLeaf * kPitch;               // [64][kPitch]: G
+    float2 *P = Gs + kLeaf * kPitch;                // [64][kPPitch]: panel of the current block
+    float2 *Wm = P + kLeaf * kPPitch;               // [32 * 64]: products of a doubling level
+    float2 *rb = Wm + 32 * kLeaf, *sb = rb + kDiag;  // 1/L(k, k) and its square, current block
+    const int tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
+    const float2 zero = make_float2(0.f, 0.f), one = make_float2(1.f, 0.f);
+    for (int e = tid; e < kLeaf * kLeaf; e += kThreads) {
+        const int i = e % kLeaf, j = e / kLeaf;
+        float2 v = zero;
+        if (i < nb && j < nb) {
+            if (i >= j) v = A[(size_t)j * ld + i];
+        } else if (i == j) {
+            v = one;
+        }
+        As[i * kPitch + j] = v;
+        Gs[i * kPitch + j] = zero;
     }
     __syncthreads();
-    // the pivot of column k is final once step k - 1 has updated it; its owner
-    // (row k, lane 0) records r = 1 / sqrt(pivot) and r^2
-    auto pivot = [&](int k) {
-        const float2 d = As[k * kPitch + k];
-        const bool ok = d.x > 0.f;
-        const float2 rk = ok ? df_rsqrt(d) : zero;
-        rd[k] = rk;
-        sc[k] = df_mul(rk, rk);
-        if (!ok) atomicCAS(info, 0, r + k + 1);
-    };
-    if (threadIdx.x == 0) pivot(0);
-    for (int k = 0; k < nb - 1; ++k) {  // Cholesky: a_ij -= (a_ik r^2) a_jk
-        __syncthreads();
-        const float2 s = sc[k];
-        for (int i = first_row(k + 1); i < nb; i += kWarps) {
-            const float2 lik = df_mul(As[i * kPitch + k], s);
-            for (int c = k + 1 + lane; c <= i; c += 32) {
-                float2 a = As[i * kPitch + c];
-                const float2 b = As[c * kPitch + k];
-                df_fma(a.x, a.y, -lik.x, -lik.y, b.x, b.y);
-                As[i * kPitch + c] = df_renorm(a.x, a.y);
+    for (int b0 = 0; b0 < kLeaf; b0 += kDiag) {
+        float2 *Ab = As + b0 * kPitch + b0, *Gb = Gs + b0 * kPitch + b0;
+        if (warp == 0) {  // (1)
+            for (int kk = 0; kk < kDiag; ++kk) {
+                __syncwarp();
+                const float2 d = Ab[kk * kPitch + kk];
+                const bool ok = d.x > 0.f;
+                const float2 rr = ok ? df_rsqrt(d) : zero, sq = df_mul(rr, rr);
+                if (lane == 0) {
+                    rb[kk] = rr;
+                    sb[kk] = sq;
+                    if (!ok && b0 + kk < nb) atomicCAS(info, 0, r + b0 + kk + 1);
+                }
+                for (int e = lane; e < kDiag * kDiag; e += 32) {
+                    const int i = e / kDiag, j = e % kDiag;
+                    if (j > kk && i >= j) {
+                        float2 a = Ab[i * kPitch + j];
+                        const float2 l = df_mul(Ab[i * kPitch + kk], sq), c = Ab[j * kPitch + kk];
+                        df_fma(a.x, a.y, -l.x, -l.y, c.x, c.y);
+                        Ab[i * kPitch + j] = df_renorm(a.x, a.y);
+                    }
+                }
             }
-            if (i == k + 1 && lane == 0) pivot(i);
-        }
-    }
-    for (int k = 0; k < nb - 1; ++k) {  // inverse: x_ij -= (a_ik r^2) x_kj, j <= k
-        __syncthreads();
-        const float2 s = sc[k];
-        for (int i = first_row(k + 1); i < nb; i += kWarps) {
-            const float2 mik = df_mul(As[i * kPitch + k], s);
-            for (int c = lane; c <= k; c += 32) {
-                float2 x = X[i * kPitch + c];
-                const float2 b = X[k * kPitch + c];
-                df_fma(x.x, x.y, -mik.x, -mik.y, b.x, b.y);
-                X[i * kPitch + c] = df_renorm(x.x, x.y);
+            for (int e = lane; e < kDiag * kDiag; e += 32) {
+                const int i = e / kDiag, j = e % kDiag;
+                Gb[i * kPitch + j] = i == j ? one : zero;
+            }
+            for (int kk = 0; kk < kDiag - 1; ++kk) {
+                __syncwarp();
+                for (int e = lane; e < kDiag * kDiag; e += 32) {
+                    const int i = e / kDiag, j = e % kDiag;
+                    if (i > kk && j <= kk) {
+                        const float2 m = df_mul(Ab[i * kPitch + kk], sb[kk]), xk = Gb[kk * kPitch + j];
+                        float2 x = Gb[i * kPitch + j];
+                        df_fma(x.x, x.y, -m.x, -m.y, xk.x, xk.y);
+                        Gb[i * kPitch + j] = df_renorm(x.x, x.y);
+                    }
+                }
+            }
+            __syncwarp();
+            for (int e = lane; e < kDiag * kDiag; e += 32) {  // G = x_ij / L(i, i), L = a_ij / L(j, j)
+                const int i = e / kDiag, j = e % kDiag;
+                if (i >= j) {
+                    Gb[i * kPitch + j] = df_mul(Gb[i * kPitch + j], rb[i]);
+                    Ab[i * kPitch + j] = df_mul(Ab[i * kPitch + j], rb[j]);
+                }
             }
         }
-    }
-    __syncthreads();
-    // G(i, j) = x_ij / L(i, i) and L(i, j) = a_ij r_j on and below the diagonal
-    if (j < nb) {
+        __syncthreads();
+        const int r0 = b0 + kDiag, nr = kLeaf - r0;
+        for (int e = tid; e < nr * kDiag; e += kThreads) {  // (2) L(i, b0 + j) = sum_t A(i, b0 + t) G_bb(j, t)
+            const int i = r0 + e / kDiag, j = e % kDiag;
+            float h = 0.f, l = 0.f;
+            for (int t = 0; t <= j; ++t) {
+                const float2 a = As[i * kPitch + b0 + t], g = Gb[j * kPitch + t];
+                df_fma(h, l, a.x, a.y, g.x, g.y);
+            }
+            P[i * kPPitch + j] = df_renorm(h, l);
+        }
+        __syncthreads();
+        for (int e = tid; e < nr * kDiag; e += kThreads) {
+            const int i = r0 + e / kDiag, j = e % kDiag;
+            As[i * kPitch + b0 + j] = P[i * kPPitch + j];
+        }
+        for (int e = tid; e < kLeaf * kLeaf; e += kThreads) {  // (3), a warp on one row
+            const int i = e / kLeaf, j = e % kLeaf;
+            if (j < r0 || j > i) continue;
+            float2 a = As[i * kPitch + j];
 #pragma unroll
-        for (int q = 0; q < kRowsPerThread; ++q) {
-            const int i = r0 + 4 * q;
-            if (i >= nb) continue;
+            for (int t = 0; t < kDiag; ++t) {
+                const float2 p = P[i * kPPitch + t], q = P[j * kPPitch + t];
+                df_fma(a.x, a.y, -p.x, -p.y, q.x, q.y);
+            }
+            As[i * kPitch + j] = df_renorm(a.x, a.y);
+        }
+        __syncthreads();
+    }
+    for (int s = kDiag; s < kLeaf; s *= 2) {  // inverse by doubling
+        const int per = s * s, count = (kLeaf / (2 * s)) * per;
+        for (int e = tid; e < count; e += kThreads) {  // W = L21 G11 (G11 lower: t >= j)
+            const int o = 2 * s * (e / per), i = (e % per) / s, j = e % s;
+            float h = 0.f, l = 0.f;
+            for (int t = j; t < s; ++t) {
+                const float2 a = As[(o + s + i) * kPitch + o + t], g = Gs[(o + t) * kPitch + o + j];
+                df_fma(h, l, a.x, a.y, g.x, g.y);
+            }
+            Wm[e] = df_renorm(h, l);
+        }
+        __syncthreads();
+        for (int e = tid; e < count; e += kThreads) {  // G21 = -G22 W (G22 lower: t <= i)
+            const int o = 2 * s * (e / per), i = (e % per) / s, j = e % s;
+            const float2 *W = Wm + (e / per) * per;
+            float h = 0.f, l = 0.f;
+            for (int t = 0; t <= i; ++t) {
+                const float2 g = Gs[(o + s + i) * kPitch + o + s + t], w = W[t * s + j];
+                df_fma(h, l, g.x, g.y, w.x, w.y);
+            }
+            const float2 v = df_renorm(h, l);
+            Gs[(o + s + i) * kPitch + o + j] = make_float2(-v.x, -v.y);
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < kLeaf * kLeaf; e += kThreads) {
+        const int i = e % kLeaf, j = e / kLeaf;
+        if (i < nb && j < nb) {
             const bool low = i >= j;
-            G[(size_t)j * ld + i] = low ? df_mul(X[i * kPitch + j], rd[i]) : zero;
-            A[(size_t)j * ld + i] = low ? df_mul(As[i * kPitch + j], rd[j]) : zero;
+            G[(size_t)j * ld + i] = low ? Gs[i * kPitch + j] : zero;
+            A[(size_t)j * ld + i] = low ? As[i * kPitch + j] : zero;
         }
     }
 }
@@ -199,12 +272,12 @@ cudaError_t leaf_chol_inv_df(float2 *A, float2 *G, int nb, int ld, int row0, int
     static bool attr = false;
     if (!attr) {
         cudaError_t e = cudaFuncSetAttribute(leaf_chol_inv_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kLeafSmem);
+                                             (int)kLeafDfSmem);
         if (e != cudaSuccess) return e;
         attr = true;
     }
     if (nb <= 0 || nb > kLeaf) return cudaErrorInvalidValue;
-    leaf_chol_inv_df_kernel<<<1, kThreads, kLeafSmem, st>>>(A, G, nb, ld, row0, info);
+    leaf_chol_inv_df_kernel<<<1, kThreads, kLeafDfSmem, st>>>(A, G, nb, ld, row0, info);
     return cudaGetLastError();
 }
 
