@@ -650,9 +650,10 @@ int form_htilde(ChebState &cs, const double *Lfac, const double *h, int ld) {
     return ELHL_OK;
 }
 
-__global__ void lanczos_start(double *v, int n) {
+template <typename T>
+__global__ void lanczos_start(T *v, int n) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) v[i] = 1.0 + 0.5 * sin(1.37 * i + 0.2);  // deterministic, every component present
+    if (i < n) v[i] = (T)(1.0 + 0.5 * sin(1.37 * i + 0.2));  // deterministic, every component present
 }
 
 constexpr int kLzBlock = 1024;
@@ -671,32 +672,34 @@ __device__ double lz_block_sum(double x, double *s) {
     return r;
 }
 
-// v <- v / |v| (one block)
-__global__ void __launch_bounds__(kLzBlock) lanczos_normalize_kernel(double *v, int n) {
+// v <- v / |v| (one block; sums in FP64)
+template <typename T>
+__global__ void __launch_bounds__(kLzBlock) lanczos_normalize_kernel(T *v, int n) {
     __shared__ double s[kLzBlock];
     double a = 0.0;
-    for (int i = threadIdx.x; i < n; i += kLzBlock) a += v[i] * v[i];
+    for (int i = threadIdx.x; i < n; i += kLzBlock) a += (double)v[i] * v[i];
     const double inv = 1.0 / sqrt(lz_block_sum(a, s));
-    for (int i = threadIdx.x; i < n; i += kLzBlock) v[i] *= inv;
+    for (int i = threadIdx.x; i < n; i += kLzBlock) v[i] = (T)(v[i] * inv);
 }
 
-// One Lanczos update after w = H v (one block, fixed-order sums):
+// One Lanczos update after w = H v (one block, fixed-order FP64 sums):
 //   alpha_j = w.v, w <- w - alpha_j v - beta_{j-1} vp, beta_j = |w|,
 //   vp <- v, v <- w / beta_j.
 // rec[0..k) alpha, rec[k..2k) beta, rec[2k] = steps used once the recursion
 // breaks down (beta ~ 0), after which later updates do nothing.
-__global__ void __launch_bounds__(kLzBlock) lanczos_update_kernel(double *v, double *vp, double *w, int n,
-                                                                  double *rec, int k, int j) {
+template <typename T>
+__global__ void __launch_bounds__(kLzBlock) lanczos_update_kernel(T *v, T *vp, T *w, int n, double *rec, int k,
+                                                                  int j) {
     __shared__ double s[kLzBlock];
     if (rec[2 * k] > 0.0) return;
     double a = 0.0;
-    for (int i = threadIdx.x; i < n; i += kLzBlock) a += w[i] * v[i];
+    for (int i = threadIdx.x; i < n; i += kLzBlock) a += (double)w[i] * v[i];
     a = lz_block_sum(a, s);
     const double bprev = j > 0 ? rec[k + j - 1] : 0.0;
     double b = 0.0;
     for (int i = threadIdx.x; i < n; i += kLzBlock) {
         const double x = w[i] - a * v[i] - bprev * vp[i];
-        w[i] = x;
+        w[i] = (T)x;
         b += x * x;
     }
     b = sqrt(lz_block_sum(b, s));
@@ -709,35 +712,57 @@ __global__ void __launch_bounds__(kLzBlock) lanczos_update_kernel(double *v, dou
     const double ib = 1.0 / b;
     for (int i = threadIdx.x; i < n; i += kLzBlock) {
         vp[i] = v[i];
-        v[i] = w[i] * ib;
+        v[i] = (T)(w[i] * ib);
     }
 }
 
-// Spectral bounds of H~ by FP64 Lanczos (k steps, no reorthogonalisation) with
-// a guard of |beta_k s_k| + 1 % of the width around the extreme Ritz values.
-// h == nullptr: H~ is cs.Ht; otherwise H~ v = G h G^T v with G = L^-1 in cs.Ht
-// (zero upper triangle: plain GEMVs).  The recursion runs on the device without
-// host round trips; the tridiagonal matrix is read back once.
+// dst = (float) src for the n x n block of an ld x n matrix (dst leading dimension ld)
+__global__ void to_fp32_kernel(const double *__restrict__ src, float *__restrict__ dst, int n, int ld) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i < n && j < n) dst[(size_t)j * ld + i] = (float)src[(size_t)j * ld + i];
+}
+
+// Spectral bounds of H~ by Lanczos (k steps, no reorthogonalisation) with a
+// guard of |beta_k s_k| + 1 % of the width around the extreme Ritz values.
+// h == nullptr: H~ is cs.Ht (FP64 DSYMV; fixed nuclei, once per trajectory).
+// Otherwise H~ v = G h G^T v with G = L^-1 in cs.Ht (zero upper triangle) on
+// FP32 copies of G and h: FP32 rounding (about 1e-7 of the width) is far
+// inside the 1 % guard, and FP64 GEMVs run on the FP64 pipe at about 37 us
+// each, 120 of them per rebuild.  The copies go to cs.A and cs.Hs, which are
+// written only after the bounds are known.  The recursion runs on the device
+// without host round trips (dot products in FP64); the tridiagonal matrix is
+// read back once.
 int lanczos_bounds(ChebState &cs, int ksteps, const double *h = nullptr) {
-    const int n = cs.N;
+    const int n = cs.N, ld = cs.ld;
     cudaStream_t st = g_ctx.stream;
-    double *v = cs.lz, *vp = cs.lz + cs.ld, *w = cs.lz + 2 * cs.ld, *t = cs.lz + 3 * cs.ld;
     const int k = std::min(std::min(ksteps, n), 63);
-    double *rec = cs.lz + 4 * cs.ld;  // [2k + 1] <= 127 doubles
-    lanczos_start<<<(n + 255) / 256, 256, 0, st>>>(v, n);
-    CU_TRY(cudaMemsetAsync(vp, 0, n * sizeof(double), st));
+    double *rec = cs.lz + 4 * ld;  // [2k + 1] <= 127 doubles
     CU_TRY(cudaMemsetAsync(rec, 0, (2 * k + 1) * sizeof(double), st));
-    lanczos_normalize_kernel<<<1, kLzBlock, 0, st>>>(v, n);
-    const double one = 1.0, zero = 0.0;
-    for (int j = 0; j < k; ++j) {
-        if (h) {
-            BLAS_TRY(cublasDgemv(g_ctx.blas, CUBLAS_OP_T, n, n, &one, cs.Ht, cs.ld, v, 1, &zero, t, 1));  // G^T v
-            BLAS_TRY(cublasDgemv(g_ctx.blas, CUBLAS_OP_N, n, n, &one, h, cs.ld, t, 1, &zero, w, 1));      // h (.)
-            BLAS_TRY(cublasDgemv(g_ctx.blas, CUBLAS_OP_N, n, n, &one, cs.Ht, cs.ld, w, 1, &zero, t, 1));  // G (.)
-            lanczos_update_kernel<<<1, kLzBlock, 0, st>>>(v, vp, t, n, rec, k, j);
-        } else {
-            BLAS_TRY(cublasDsymv(g_ctx.blas, CUBLAS_FILL_MODE_LOWER, n, &one, cs.Ht, cs.ld, v, 1, &zero, w, 1));
-            lanczos_update_kernel<<<1, kLzBlock, 0, st>>>(v, vp, w, n, rec, k, j);
+    if (h) {
+        float *v = reinterpret_cast<float *>(cs.lz), *vp = v + ld, *w = v + 2 * ld, *t = v + 3 * ld;
+        float *G32 = static_cast<float *>(cs.A), *h32 = static_cast<float *>(cs.Hs);
+        dim3 grid((n + 127) / 128, n);
+        to_fp32_kernel<<<grid, 128, 0, st>>>(cs.Ht, G32, n, ld);
+        to_fp32_kernel<<<grid, 128, 0, st>>>(h, h32, n, ld);
+        lanczos_start<float><<<(n + 255) / 256, 256, 0, st>>>(v, n);
+        CU_TRY(cudaMemsetAsync(vp, 0, n * sizeof(float), st));
+        lanczos_normalize_kernel<float><<<1, kLzBlock, 0, st>>>(v, n);
+        const float one = 1.f, zero = 0.f;
+        for (int j = 0; j < k; ++j) {
+            BLAS_TRY(cublasSgemv(g_ctx.blas, CUBLAS_OP_T, n, n, &one, G32, ld, v, 1, &zero, t, 1));  // G^T v
+            BLAS_TRY(cublasSgemv(g_ctx.blas, CUBLAS_OP_N, n, n, &one, h32, ld, t, 1, &zero, w, 1));  // h (.)
+            BLAS_TRY(cublasSgemv(g_ctx.blas, CUBLAS_OP_N, n, n, &one, G32, ld, w, 1, &zero, t, 1));  // G (.)
+            lanczos_update_kernel<float><<<1, kLzBlock, 0, st>>>(v, vp, t, n, rec, k, j);
+        }
+    } else {
+        double *v = cs.lz, *vp = cs.lz + ld, *w = cs.lz + 2 * ld;
+        lanczos_start<double><<<(n + 255) / 256, 256, 0, st>>>(v, n);
+        CU_TRY(cudaMemsetAsync(vp, 0, n * sizeof(double), st));
+        lanczos_normalize_kernel<double><<<1, kLzBlock, 0, st>>>(v, n);
+        const double one = 1.0, zero = 0.0;
+        for (int j = 0; j < k; ++j) {
+            BLAS_TRY(cublasDsymv(g_ctx.blas, CUBLAS_FILL_MODE_LOWER, n, &one, cs.Ht, ld, v, 1, &zero, w, 1));
+            lanczos_update_kernel<double><<<1, kLzBlock, 0, st>>>(v, vp, w, n, rec, k, j);
         }
     }
     CU_TRY(cudaGetLastError());
@@ -821,10 +846,16 @@ __global__ void lower_only_kernel(double *A, int n, int ld) {
 }
 
 // ---- inverse of the Cholesky factor --------------------------------------------
-// Workspace of the recursive factorisations: ld x (ld / 2 + 256) doubles, enough
-// for the off-diagonal block of the top split and for every batched level.
+constexpr int kTriBlock = 512;   // diagonal blocks finished by the batched bottom-up levels
+constexpr int kTrmmLeaf = 256;   // triangular products of at most this order run as one full DGEMM
+
+// Workspace of the recursive factorisations: ld x (ld / 2 + kTriBlock) doubles.
+// The widest block it holds is the off-diagonal block of the top split,
+// n2 x n1 with n1 = round_up(n / 2, kTriBlock) <= n / 2 + kTriBlock - 1 (the
+// Cholesky-with-inverse splits on multiples of 64); the batched levels need at
+// most n x kTriBlock / 4.
 int factor_workspace(ChebState &cs, double **W) {
-    const size_t need = (size_t)cs.ld * (cs.ld / 2 + 256);
+    const size_t need = (size_t)cs.ld * (cs.ld / 2 + kTriBlock);
     if (cs.fws_n < need) {
         dev_free(cs.fws);
         cs.fws_n = 0;
@@ -834,9 +865,6 @@ int factor_workspace(ChebState &cs, double **W) {
     *W = cs.fws;
     return ELHL_OK;
 }
-
-constexpr int kTriBlock = 256;   // diagonal blocks finished by the batched bottom-up levels
-constexpr int kTrmmLeaf = 256;   // triangular products of at most this order run as one full DGEMM
 
 // Y (m x n, ldy) = alpha X T for the lower-triangular T (n x n, zero upper
 // triangle), out of place, recursively:
@@ -889,11 +917,13 @@ int tri_inverse_top(double *A, int n, int ld, double *W) {
 
 // G = L^-1 in place for the n x n lower-triangular A (zero upper triangle), FP64:
 //  1. every 64-row diagonal block by leaf_inverse, one launch;
-//  2. bottom-up, s = 64 and 128: pairs of inverted s-blocks become inverted
-//     2s-blocks, G21 = -G22 (L21 G11), as two strided-batched DGEMMs over all
-//     complete pairs and two plain ones for a short last pair (full products
-//     of triangular blocks; these levels hold about 2 % of the flops);
-//  3. top-down above 256 rows (tri_inverse_top), N^3/3 flops in large DGEMMs.
+//  2. bottom-up, s = 64, 128 and 256: pairs of inverted s-blocks become
+//     inverted 2s-blocks, G21 = -G22 (L21 G11), as two strided-batched DGEMMs
+//     over all complete pairs and two plain ones for a short last pair (full
+//     products of triangular blocks; these levels hold about 4 % of the flops);
+//  3. top-down above 512 rows (tri_inverse_top), N^3/3 flops in large DGEMMs.
+// Block sizes measured at N = 3720: 256 / 512 for the leaf products / the
+// bottom-up blocks gave 23.7 ms, 256 / 256 24.2, 128 / 256 24.8, 512 / 256 25.7.
 int tri_inverse(ChebState &cs, double *A, int n, int ld) {
     cudaStream_t st = g_ctx.stream;
     double *W = nullptr;
