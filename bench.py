@@ -187,9 +187,11 @@ def run_ours(args, rank, world):
     torch.cuda.synchronize(dev)
     for i in range(K):
         flush.fill_(float(i))
+        n0 = api.kernel_launches()
         ev[i][0].record(stream)
         dev_step(W + i)
         ev[i][1].record(stream)
+        launches += api.kernel_launches() - n0  # this library's kernels in the timed region
         st = tr.stats()
         prop_ms += st.prop_ms
         rebuild_ms += st.rebuild_ms
@@ -197,7 +199,6 @@ def run_ours(args, rank, world):
         factor_ms += st.factor_ms
         inverse_ms += st.inverse_ms
         orders += st.orders
-        launches += st.prop_launches + st.rebuild_count
     tile = {"tile_cols": st.tile_cols, "phases": st.phases} if method == api.METHOD_CHEBYSHEV else {}
     torch.cuda.synchronize(dev)
     clk = clocks.stop()
@@ -340,7 +341,7 @@ def run_variant(args, precision_name: str):
     for i in range(W):
         dev_step(i)
     torch.cuda.synchronize(dev)
-    ms = prop = 0.0
+    ms = prop = rebuild = sh = factor = 0.0
     for i in range(K):
         flush.fill_(float(i))
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -349,11 +350,17 @@ def run_variant(args, precision_name: str):
         e1.record(stream)
         torch.cuda.synchronize(dev)
         ms += e0.elapsed_time(e1)
-        prop += tr.stats().prop_ms
+        st = tr.stats()
+        prop += st.prop_ms
+        rebuild += st.rebuild_ms
+        sh += st.sh_ms
+        factor += st.factor_ms + st.inverse_ms
     tr.close()
     api.set_stream(None)
     return {"precision": precision_name, "value": K / (ms / 1e3), "unit": "steps/s", "ms_per_step": ms / K,
-            "propagation_ms_per_step": prop / K}
+            "propagation_ms_per_step": prop / K,
+            "rebuild_parts_ms_per_step": {"S_h_build": sh / K, "cholesky_and_inverse": factor / K,
+                                          "bounds_columns_other": (rebuild - sh - factor) / K}}
 
 
 def run_dropin(args, steps: int = 2):

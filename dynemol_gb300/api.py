@@ -33,7 +33,7 @@ EXPORTED_SYMBOLS = (
     "propagationelhl_gpucaller_", "elhl_last_status", "elhl_status_string", "elhl_traj_config_default",
     "elhl_traj_create", "elhl_traj_destroy", "elhl_traj_init_fmo", "elhl_traj_init_fmo_states", "elhl_traj_set_psi", "elhl_traj_get_psi", "elhl_traj_step",
     "elhl_traj_step_device", "elhl_traj_energies", "elhl_traj_get_matrices", "elhl_traj_get_stats", "elhl_device_count",
-    "elhl_sm_count", "elhl_set_stream", "elhl_propagate_fixed_scratch", "elhl_bessel_j",
+    "elhl_sm_count", "elhl_set_stream", "elhl_kernel_launches", "elhl_propagate_fixed_scratch", "elhl_bessel_j",
     "elhl_chebyshev_coefficients", "elhl_batch_create", "elhl_batch_size", "elhl_batch_member",
     "elhl_batch_compact", "elhl_batch_step", "elhl_batch_get_stats", "elhl_batch_destroy",
     "elhl_server_create", "elhl_server_submit", "elhl_server_step", "elhl_server_poll", "elhl_server_result",
@@ -126,6 +126,8 @@ def load(path: str = LIB_PATH):
     L.elhl_device_count.restype = ci
     L.elhl_sm_count.restype = ci
     L.elhl_set_stream.argtypes = [vp]
+    L.elhl_kernel_launches.argtypes = []
+    L.elhl_kernel_launches.restype = ctypes.c_longlong
     L.elhl_propagate_fixed_scratch.argtypes = [ci, vp, ci, vp, vp, ctypes.c_double, ctypes.c_double,
                                                ctypes.c_double, dp, vp]
     L.elhl_bessel_j.argtypes = [ctypes.c_double, ci, vp]
@@ -404,6 +406,11 @@ def chebyshev_coefficients(dt: float, emin: float, emax: float, tol: float = 1e-
     _check(load().elhl_chebyshev_coefficients(dt, emin, emax, tol, kcap, _p(cre), _p(cim), ctypes.byref(K)),
            "elhl_chebyshev_coefficients")
     return cre[: K.value + 1] + 1j * cim[: K.value + 1]
+
+
+def kernel_launches() -> int:
+    """Kernels of this library launched so far in this process (library calls such as cuBLAS not counted)."""
+    return int(load().elhl_kernel_launches())
 
 
 def set_stream(stream_handle: int | None):

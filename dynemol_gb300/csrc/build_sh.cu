@@ -476,6 +476,7 @@ __global__ void pulay_reduce_kernel(const double *__restrict__ F, int nat, doubl
 
 cudaError_t init_build_tables() {
     init_tables_kernel<<<(1001 + 255) / 256, 256>>>();
+    count_launch();
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     return e;
@@ -488,7 +489,9 @@ cudaError_t launch_pulay_forces(const DevBasis &b, const double *d_coords, doubl
     dim3 block(16, 8);
     dim3 grid((b.natoms + block.x - 1) / block.x, (b.natoms + block.y - 1) / block.y);
     pulay_pairs_kernel<<<grid, block, 0, st>>>(b, d_coords, cutoff, delta, d_kernel, ldk, d_F);
+    count_launch();
     pulay_reduce_kernel<<<(3 * b.natoms + 127) / 128, 128, 0, st>>>(d_F, b.natoms, scale, d_force);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -498,6 +501,7 @@ cudaError_t launch_huckel_fields(const DevBasis &b, const double *d_coords, doub
     dim3 block(16, 8);
     dim3 grid((b.natoms + block.x - 1) / block.x, (b.natoms + block.y - 1) / block.y);
     huckel_fields_kernel<<<grid, block, 0, st>>>(b, d_coords, cutoff, d_S, lds, d_dp_ao, d_dp4, d_h, ldh);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -507,6 +511,7 @@ cudaError_t launch_build_sh(const DevBasis &b, const double *d_coords, double cu
     dim3 block(16, 8);
     dim3 grid((b.natoms + block.x - 1) / block.x, (b.natoms + block.y - 1) / block.y);
     build_sh_kernel<<<grid, block, 0, st>>>(b, d_coords, cutoff, d_S, d_h, ld);
+    count_launch();
     return cudaGetLastError();
 }
 

@@ -699,7 +699,9 @@ cudaError_t launch_df(const ChebLaunch &L, cudaStream_t st) {
     if (e != cudaSuccess) return e;
     ChebLaunch copy = L;
     void *args[] = {&copy};
-    return cudaLaunchCooperativeKernel((const void *)kern, dim3(L.grid), dim3(kBlock), args, smem, st);
+    e = cudaLaunchCooperativeKernel((const void *)kern, dim3(L.grid), dim3(kBlock), args, smem, st);
+    count_launch();
+    return e;
 }
 
 template <typename T, int MG>
@@ -711,7 +713,9 @@ cudaError_t launch_t(const ChebLaunch &L, cudaStream_t st) {
     if (e != cudaSuccess) return e;
     ChebLaunch copy = L;
     void *args[] = {&copy};
-    return cudaLaunchCooperativeKernel((const void *)kern, dim3(L.grid), dim3(kBlock), args, smem, st);
+    e = cudaLaunchCooperativeKernel((const void *)kern, dim3(L.grid), dim3(kBlock), args, smem, st);
+    count_launch();
+    return e;
 }
 
 template <typename T, int MG>
@@ -722,9 +726,11 @@ cudaError_t launch_readout_t(const ChebLaunch &L, int nprob, cudaStream_t st) {
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     kern<<<L.grid, kBlock, smem, st>>>(L);
+    count_launch();
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     reduce_pops_kernel<<<nprob, 128, 0, st>>>(L, nprob);
+    count_launch();
     return cudaGetLastError();
 }
 

@@ -153,6 +153,7 @@ __global__ void df_convert_kernel(double *x, int rows, int n, int ld, bool to_pa
 cudaError_t df_convert(double *x, int rows, int n, int ld, bool to_pairs, cudaStream_t st) {
     if (rows <= 0 || n <= 0) return cudaSuccess;
     df_convert_kernel<<<dim3((rows + 127) / 128, n), 128, 0, st>>>(x, rows, n, ld, to_pairs);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -174,10 +175,13 @@ cudaError_t dfgemm(int m, int n, int k, double alpha, const float2 *A, int lda, 
     grid.z = splits;
     const float ah = (float)alpha, bh = (float)beta;  // alpha and beta as pairs
     const float2 a2 = make_float2(ah, (float)(alpha - ah)), b2 = make_float2(bh, (float)(beta - bh));
-    if (transB)
+    if (transB) {
         dfgemm_kernel<true><<<grid, kThreads, 0, st>>>(m, n, k, a2, A, lda, B, ldb, b2, C, ldc, tri, g_part, g_count);
-    else
+        count_launch();
+    } else {
         dfgemm_kernel<false><<<grid, kThreads, 0, st>>>(m, n, k, a2, A, lda, B, ldb, b2, C, ldc, tri, g_part, g_count);
+        count_launch();
+    }
     return cudaGetLastError();
 }
 

@@ -11,6 +11,7 @@
 #include <cusolverDn.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -21,6 +22,12 @@
 #include "elhl_internal.cuh"
 
 using namespace elhl;
+
+namespace elhl {
+std::atomic<long long> g_own_launches{0};
+void count_launch(long long n) { g_own_launches.fetch_add(n, std::memory_order_relaxed); }
+long long own_launches() { return g_own_launches.load(std::memory_order_relaxed); }
+}  // namespace elhl
 
 namespace {
 
@@ -243,8 +250,10 @@ struct Factor {
         cudaStream_t st = g_ctx.stream;
         const int tb = 256, nb = (n + tb - 1) / tb;
         split_complex<<<nb, tb, 0, st>>>(z, cols, n, ld);
+        count_launch();
         SOLVER_TRY(cusolverDnDpotrs(g_ctx.solver, CUBLAS_FILL_MODE_LOWER, n, 2, L, ld, cols, ld, info + 1));
         join_complex<<<nb, tb, 0, st>>>(cols, out, n, ld);
+        count_launch();
         CU_TRY(cudaGetLastError());
         return ELHL_OK;
     }
@@ -559,6 +568,7 @@ struct ChebState {
     float *Vf = nullptr;       // [ld][m] complex FP32 copy of the propagated columns (read-out input)
     double *gpops = nullptr;   // [P][nfrag+1] populations of the last step
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    long long graph_kernels = 0;  // kernels of this library in one step graph
     // BF16X3 on the hand-written tcgen05 GEMM: Hs and the order's block split in three BF16 terms
     bool umma = false;
     int usplits = 1;           // K split of the tensor-core GEMM (partial tiles in Y)
@@ -646,6 +656,7 @@ int form_htilde(ChebState &cs, const double *Lfac, const double *h, int ld) {
     BLAS_TRY(cublasDtrsm(g_ctx.blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n,
                          n, &one, Lfac, ld, cs.Ht, cs.ld));
     symmetrize_kernel<<<dim3((n + 127) / 128, n), 128, 0, st>>>(cs.Ht, n, cs.ld);
+    count_launch();
     CU_TRY(cudaGetLastError());
     return ELHL_OK;
 }
@@ -743,26 +754,34 @@ int lanczos_bounds(ChebState &cs, int ksteps, const double *h = nullptr) {
         float *G32 = static_cast<float *>(cs.A), *h32 = static_cast<float *>(cs.Hs);
         dim3 grid((n + 127) / 128, n);
         to_fp32_kernel<<<grid, 128, 0, st>>>(cs.Ht, G32, n, ld);
+        count_launch();
         to_fp32_kernel<<<grid, 128, 0, st>>>(h, h32, n, ld);
+        count_launch();
         lanczos_start<float><<<(n + 255) / 256, 256, 0, st>>>(v, n);
+        count_launch();
         CU_TRY(cudaMemsetAsync(vp, 0, n * sizeof(float), st));
         lanczos_normalize_kernel<float><<<1, kLzBlock, 0, st>>>(v, n);
+        count_launch();
         const float one = 1.f, zero = 0.f;
         for (int j = 0; j < k; ++j) {
             BLAS_TRY(cublasSgemv(g_ctx.blas, CUBLAS_OP_T, n, n, &one, G32, ld, v, 1, &zero, t, 1));  // G^T v
             BLAS_TRY(cublasSgemv(g_ctx.blas, CUBLAS_OP_N, n, n, &one, h32, ld, t, 1, &zero, w, 1));  // h (.)
             BLAS_TRY(cublasSgemv(g_ctx.blas, CUBLAS_OP_N, n, n, &one, G32, ld, w, 1, &zero, t, 1));  // G (.)
             lanczos_update_kernel<float><<<1, kLzBlock, 0, st>>>(v, vp, t, n, rec, k, j);
+            count_launch();
         }
     } else {
         double *v = cs.lz, *vp = cs.lz + ld, *w = cs.lz + 2 * ld;
         lanczos_start<double><<<(n + 255) / 256, 256, 0, st>>>(v, n);
+        count_launch();
         CU_TRY(cudaMemsetAsync(vp, 0, n * sizeof(double), st));
         lanczos_normalize_kernel<double><<<1, kLzBlock, 0, st>>>(v, n);
+        count_launch();
         const double one = 1.0, zero = 0.0;
         for (int j = 0; j < k; ++j) {
             BLAS_TRY(cublasDsymv(g_ctx.blas, CUBLAS_FILL_MODE_LOWER, n, &one, cs.Ht, ld, v, 1, &zero, w, 1));
             lanczos_update_kernel<double><<<1, kLzBlock, 0, st>>>(v, vp, w, n, rec, k, j);
+            count_launch();
         }
     }
     CU_TRY(cudaGetLastError());
@@ -793,12 +812,16 @@ int cheb_prepare(ChebState &cs, double dt, double tol, const double *h = nullptr
     dim3 grid((cs.ld + 127) / 128, cs.N);
     const double *src = h ? h : cs.Ht;
     const double a = h ? 0.0 : cs.a;
-    if (cs.precision == ELHL_PREC_DF64)
+    if (cs.precision == ELHL_PREC_DF64) {
         split_df_kernel<<<grid, 128, 0, st>>>(src, (float2 *)cs.Hs, cs.N, cs.ld, a, binv, false);
-    else if (cs.precision == ELHL_PREC_FP64)
+        count_launch();
+    } else if (cs.precision == ELHL_PREC_FP64) {
         scale_kernel<double><<<grid, 128, 0, st>>>(src, (double *)cs.Hs, cs.N, cs.ld, a, binv);
-    else
+        count_launch();
+    } else {
         scale_kernel<float><<<grid, 128, 0, st>>>(src, (float *)cs.Hs, cs.N, cs.ld, a, binv);
+        count_launch();
+    }
     CU_TRY(cudaGetLastError());
     std::vector<double> cre, cim;
     int K = 0;
@@ -960,6 +983,7 @@ int invert_factor(ChebState &cs, const double *Lfac, double *dst) {
     CU_TRY(cudaMemcpy2DAsync(dst, ld * sizeof(double), Lfac, ld * sizeof(double), n * sizeof(double), n,
                              cudaMemcpyDeviceToDevice, st));
     lower_only_kernel<<<dim3((ld + 127) / 128, n), 128, 0, st>>>(dst, n, ld);  // potrf leaves S above the diagonal
+    count_launch();
     CU_TRY(cudaGetLastError());
     return tri_inverse(cs, dst, n, ld);
 }
@@ -1023,10 +1047,14 @@ int cheb_prepare_readout(ChebState &cs, const double *Lfac) {
     if (!rc) {
         if (cs.precision == ELHL_PREC_FP64) {
             convert_kernel<double><<<grid, 128, 0, st>>>(tmp, (double *)cs.A, n, ld, false);
+            count_launch();
             convert_kernel<double><<<grid, 128, 0, st>>>(Lfac, (double *)cs.B, n, ld, true);
+            count_launch();
         } else {
             convert_kernel<float><<<grid, 128, 0, st>>>(tmp, (float *)cs.A, n, ld, false);
+            count_launch();
             convert_kernel<float><<<grid, 128, 0, st>>>(Lfac, (float *)cs.B, n, ld, true);
+            count_launch();
         }
         if (cudaGetLastError() != cudaSuccess) rc = ELHL_ERR_CUDA;
     }
@@ -1056,18 +1084,22 @@ int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, do
         if (int rc = dev_alloc(&cs.cscratch, (size_t)2 * cs.m * ld)) return rc;
     // L with a zero upper triangle (potrf leaves S there): the dense column transforms read all of it
     lower_only_kernel<<<dim3((ld + 127) / 128, n), 128, 0, st>>>(const_cast<double *>(Lfac), n, ld);
+    count_launch();
     CU_TRY(cudaGetLastError());
     if (!have_inverse)
         if (int rc = invert_factor(cs, Lfac, cs.Ht)) return rc;
     CU_TRY(cudaEventRecord(g_ctx.ev[6], st));
     lower_only_kernel<<<dim3((ld + 127) / 128, n), 128, 0, st>>>(cs.Ht, n, ld);
+    count_launch();
     CU_TRY(cudaGetLastError());
     if (int rc = lanczos_bounds(cs, 40, h)) return rc;
     if (int rc = cheb_prepare(cs, dt, tol, h)) return rc;
     dim3 grid((ld + 127) / 128, n);
     if (cs.precision == ELHL_PREC_DF64) {  // G and G^T as (hi, lo) pairs; no device read-out matrices
         split_df_kernel<<<grid, 128, 0, st>>>(cs.Ht, (float2 *)cs.A, n, ld, 0.0, 1.0, false);
+        count_launch();
         split_df_kernel<<<grid, 128, 0, st>>>(cs.Ht, (float2 *)cs.Gt, n, ld, 0.0, 1.0, true);
+        count_launch();
         CU_TRY(cudaGetLastError());
         cs.implicit = true;
         cs.readout_ready = false;  // read-out through the FP64 dense transforms
@@ -1075,12 +1107,18 @@ int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, do
     }
     if (cs.precision == ELHL_PREC_FP64) {
         convert_kernel<double><<<grid, 128, 0, st>>>(cs.Ht, (double *)cs.A, n, ld, false);
+        count_launch();
         convert_kernel<double><<<grid, 128, 0, st>>>(cs.Ht, (double *)cs.Gt, n, ld, true);
+        count_launch();
         convert_kernel<double><<<grid, 128, 0, st>>>(Lfac, (double *)cs.B, n, ld, true);
+        count_launch();
     } else {
         convert_kernel<float><<<grid, 128, 0, st>>>(cs.Ht, (float *)cs.A, n, ld, false);
+        count_launch();
         convert_kernel<float><<<grid, 128, 0, st>>>(cs.Ht, (float *)cs.Gt, n, ld, true);
+        count_launch();
         convert_kernel<float><<<grid, 128, 0, st>>>(Lfac, (float *)cs.B, n, ld, true);
+        count_launch();
     }
     CU_TRY(cudaGetLastError());
     cs.implicit = true;
@@ -1171,6 +1209,7 @@ int cheb_gemm_enqueue(ChebState &cs, int parity) {
     double2 *out = parity ? cs.phi : cs.acc;
     const bool renorm = true;
     gemm_order0_kernel<<<nb, tb, 0, st>>>(in, renorm ? cs.scale : nullptr, cs.P, n, m, cs.c0, vb, out);
+    count_launch();
     for (int k = 1; k <= cs.K; ++k) {
         const float *vprev = reinterpret_cast<const float *>(vb + ((k + 2) % 3) * vs);
         if (cs.umma) {  // Y (N x 2m) = Hs V^T on the tensor cores (Hs symmetric), three BF16 terms each
@@ -1185,18 +1224,24 @@ int cheb_gemm_enqueue(ChebState &cs, int parity) {
         gemm_epilogue_kernel<<<nb, tb, 0, st>>>(reinterpret_cast<const float2 *>(cs.Y), cs.umma ? cs.usplits : 1,
                                                 (size_t)n * m, vb + ((k + 1) % 3) * vs,
                                                 vb + (k % 3) * vs, out, cs.coef, k, nm);
+        count_launch();
     }
     to_float2_kernel<<<nb, tb, 0, st>>>(out, reinterpret_cast<float2 *>(cs.Vf), nm);
+    count_launch();
     if (int rc = gemm_vt(g_ctx.blas_tc, cs.precision, 2 * m, n, cs.Vf, reinterpret_cast<const float *>(cs.A), cs.ld,
                          cs.Y))
         return rc;
     to_double2_kernel<<<nb, tb, 0, st>>>(reinterpret_cast<const float2 *>(cs.Y), cs.psi_out, nm);
+    count_launch();
     if (int rc = gemm_vt(g_ctx.blas_tc, cs.precision, 2 * m, n, cs.Vf, reinterpret_cast<const float *>(cs.B), cs.ld,
                          cs.Y))
         return rc;
     to_double2_kernel<<<nb, tb, 0, st>>>(reinterpret_cast<const float2 *>(cs.Y), cs.bra_out, nm);
+    count_launch();
     populations_kernel<<<cs.P, 256, 0, st>>>(cs.psi_out, cs.bra_out, n, cs.P, cs.ao_frag, cs.nfrag, cs.gpops);
+    count_launch();
     scale_from_pops_kernel<<<1, kMaxCols, 0, st>>>(cs.gpops, cs.P, cs.nfrag, cs.target, cs.scale);
+    count_launch();
     CU_TRY(cudaGetLastError());
     return ELHL_OK;
 }
@@ -1208,7 +1253,10 @@ int cheb_gemm_step(ChebState &cs) {
     if (!ge) {
         cudaGraph_t g = nullptr;
         CU_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        const long long before = own_launches();
         int rc = cheb_gemm_enqueue(cs, cs.parity);
+        cs.graph_kernels = own_launches() - before;  // recorded, not launched: counted at each replay
+        count_launch(-cs.graph_kernels);
         cudaError_t e = cudaStreamEndCapture(st, &g);
         if (rc) {
             if (g) cudaGraphDestroy(g);
@@ -1221,6 +1269,7 @@ int cheb_gemm_step(ChebState &cs) {
     }
     CU_TRY(cudaEventRecord(g_ctx.ev[0], st));
     CU_TRY(cudaGraphLaunch(ge, st));
+    count_launch(cs.graph_kernels);
     CU_TRY(cudaEventRecord(g_ctx.ev[1], st));
     cs.parity ^= 1;
     return ELHL_OK;
@@ -1523,7 +1572,9 @@ int cheb_settle(const std::vector<ChebState *> &states) {
         if (!reduced_precision(cs->precision)) continue;
         settle_scale_kernel<<<(cs->N + 255) / 256, 256, 0, st>>>(cs->cin(), cs->m, cs->psi_out, cs->bra_out, cs->N,
                                                                  cs->P, cs->scale);
+        count_launch();
         ones_kernel<<<1, kMaxCols, 0, st>>>(cs->scale, kMaxCols);
+        count_launch();
     }
     CU_TRY(cudaGetLastError());
     return ELHL_OK;
@@ -1625,8 +1676,10 @@ int ehrenfest_impl(int n, const double *hH, const double *hA, const elhl_zcomple
         CU_TRY(cudaMemcpyAsync(g_ehr.bk, hbra, 2 * n * sizeof(double2), cudaMemcpyHostToDevice, st));
         CU_TRY(cudaMemcpyAsync(g_ehr.bk + 2 * n, hket, 2 * n * sizeof(double2), cudaMemcpyHostToDevice, st));
         ehrenfest_a_kernel<<<grid, 128, 0, st>>>(g_ehr.bk, g_ehr.bk + 2 * n, g_ehr.A, n, ld);
+        count_launch();
     }
     hadamard_kernel<<<grid, 128, 0, st>>>(g_ehr.X, g_ehr.A, g_ehr.K, n, ld);
+    count_launch();
     CU_TRY(cudaGetLastError());
     const double m1 = -1.0, one = 1.0;
     BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &m1, g_ehr.H, ld, g_ehr.A, ld, &one, g_ehr.K,
@@ -1802,6 +1855,7 @@ int cheb_readout(elhl_traj *tr, const double2 *cols, double *d_pops) {
     }
     if (d_pops) {
         populations_kernel<<<P, 256, 0, st>>>(tr->psi_ao, tr->bra_ao, n, P, tr->basis.ao_frag, tr->nfrag, d_pops);
+        count_launch();
         CU_TRY(cudaGetLastError());
     }
     return ELHL_OK;
@@ -1893,6 +1947,7 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
         if ((rc = cheb_readout(tr, out, pp))) break;
         if (renorm) {
             renormalize_kernel<<<(tr->N + 255) / 256, 256, 0, st>>>(out, tr->N, cs.m, P, pp, nf, tr->target);
+            count_launch();
             if (cudaGetLastError() != cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
             if ((rc = cheb_readout(tr, out, nullptr))) break;  // AO state follows the renormalised columns
         }
@@ -2084,8 +2139,11 @@ int fmo_particle(elhl_traj *tr, int nat, const int *atoms, int state, double2 *k
         rc = ELHL_ERR_CUDA;
     if (!rc) {
         zero_strided<<<(tr->N + 255) / 256, 256, 0, st>>>(ket, tr->N, stride);
+        count_launch();
         embed_fmo<<<1, 256, 0, st>>>(hf, ldf, nf, state - 1, daos, ket, stride);
+        count_launch();
         s_times_sparse<<<(tr->N + 127) / 128, 128, 0, st>>>(tr->S, tr->ld, tr->N, daos, nf, ket, bra, stride);
+        count_launch();
         if (cudaGetLastError() != cudaSuccess) rc = ELHL_ERR_CUDA;
     }
     int hinfo = 0;
@@ -2126,6 +2184,7 @@ int cheb_set_target(elhl_traj *tr) {
     double *pops = nullptr;
     if (int rc = dev_alloc(&pops, (size_t)P * (tr->nfrag + 1))) return rc;
     populations_kernel<<<P, 256, 0, g_ctx.stream>>>(tr->psi_ao, tr->bra_ao, n, P, tr->basis.ao_frag, tr->nfrag, pops);
+    count_launch();
     std::vector<double> h((size_t)P * (tr->nfrag + 1)), tgt(P);
     cudaError_t ce = cudaMemcpyAsync(h.data(), pops, h.size() * sizeof(double), cudaMemcpyDeviceToHost, g_ctx.stream);
     if (ce == cudaSuccess) ce = cudaStreamSynchronize(g_ctx.stream);
@@ -2174,6 +2233,8 @@ int elhl_set_stream(void *stream) {
     if (cublasSetStream(g_ctx.blas_tc, g_ctx.stream) != CUBLAS_STATUS_SUCCESS) return ELHL_ERR_CUDA;
     return ELHL_OK;
 }
+
+long long elhl_kernel_launches(void) { return own_launches(); }
 
 int elhl_sm_count(void) {
     if (ensure_context()) return 0;

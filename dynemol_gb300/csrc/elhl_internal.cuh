@@ -11,6 +11,12 @@
 
 namespace elhl {
 
+// Kernels of this library launched so far (graph replays counted per kernel
+// node), for the launch accounting of benchmarks: count_launch() follows every
+// launch site.
+void count_launch(long long n = 1);
+long long own_launches();
+
 constexpr double kHbar = 6.58264e-4;  // eV ps (constants_m.f:23)
 constexpr int kOrder = 25;            // Taylor order cap (Taylor.f:20)
 constexpr int kMaxFrag = 8;           // fragments tracked by the population reduction

@@ -265,6 +265,7 @@ cudaError_t leaf_inverse(double *A, int n, int ld, cudaStream_t st) {
     }
     if (n <= 0) return cudaSuccess;
     leaf_inverse_kernel<<<(n + kLeaf - 1) / kLeaf, kThreads, kLeafSmem, st>>>(A, n, ld);
+    count_launch();
     return cudaGetLastError();
 }
 
@@ -278,6 +279,7 @@ cudaError_t leaf_chol_inv_df(float2 *A, float2 *G, int nb, int ld, int row0, int
     }
     if (nb <= 0 || nb > kLeaf) return cudaErrorInvalidValue;
     leaf_chol_inv_df_kernel<<<1, kThreads, kLeafDfSmem, st>>>(A, G, nb, ld, row0, info);
+    count_launch();
     return cudaGetLastError();
 }
 

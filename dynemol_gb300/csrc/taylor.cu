@@ -525,7 +525,9 @@ int taylor_grid_size(int block, int *grid_out) {
 cudaError_t launch_taylor(const TaylorLaunch &L, int grid, int block, cudaStream_t st) {
     TaylorLaunch copy = L;
     void *args[] = {&copy};
-    return cudaLaunchCooperativeKernel((const void *)taylor_kernel, dim3(grid), dim3(block), args, 0, st);
+    const cudaError_t e = cudaLaunchCooperativeKernel((const void *)taylor_kernel, dim3(grid), dim3(block), args, 0, st);
+    count_launch();
+    return e;
 }
 
 }  // namespace elhl

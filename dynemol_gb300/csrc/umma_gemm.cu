@@ -376,10 +376,12 @@ int split3_bf16(const float *src, int rows, int cols, int lds, __nv_bfloat16 *co
     if (transpose) {
         dim3 grid((cols + 31) / 32, (rows + 31) / 32);
         split3_t_kernel<<<grid, dim3(32, 8), 0, st>>>(src, rows, cols, lds, dst[0], dst[1], dst[2], ldd);
+        count_launch();
         return cudaGetLastError() == cudaSuccess ? ELHL_OK : ELHL_ERR_CUDA;
     }
     dim3 grid((cols + 255) / 256, rows);
     split3_kernel<<<grid, 256, 0, st>>>(src, rows, cols, lds, dst[0], dst[1], dst[2], ldd, false);
+    count_launch();
     return cudaGetLastError() == cudaSuccess ? ELHL_OK : ELHL_ERR_CUDA;
 }
 
@@ -409,6 +411,7 @@ int umma_bf16x3_gemm(const __nv_bfloat16 *const A[3], int lda, const __nv_bfloat
     UmmaParams p{rows, K, n2, splits, Y, d_error};
     dim3 grid((rows + kBM - 1) / kBM, splits);
     umma_bf16x3_kernel<<<grid, kThreads, smem, st>>>(m[0], m[1], m[2], m[3], m[4], m[5], p);
+    count_launch();
     return cudaGetLastError() == cudaSuccess ? ELHL_OK : ELHL_ERR_CUDA;
 }
 

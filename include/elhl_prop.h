@@ -311,6 +311,11 @@ int elhl_server_destroy(elhl_server *sv);
  * events on that stream; NULL restores the library's own stream. */
 int elhl_set_stream(void *stream);
 
+/* Kernels of this library launched so far in this process (each kernel node
+ * of a replayed step graph counted; library calls such as cuBLAS not
+ * counted): benchmarks read it before and after a timed region. */
+long long elhl_kernel_launches(void);
+
 /*
  * Allocation-free propagation of one particle (no counterpart in the
  * reference).  Same computation and thresholds as propagation_gpucaller_
