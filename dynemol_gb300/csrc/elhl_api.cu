@@ -1792,7 +1792,9 @@ int cheb_rebuild_operator(elhl_traj *tr, bool implicit = false) {
     cudaStream_t st = g_ctx.stream;
     CU_TRY(cudaMemcpy2DAsync(tr->fac.L, tr->ld * sizeof(double), tr->S, tr->ld * sizeof(double), tr->N * sizeof(double),
                              tr->N, cudaMemcpyDeviceToDevice, st));
-    const bool together = implicit && tr->cs.precision == ELHL_PREC_DF64;  // factor and inverse in one recursion
+    // factor and inverse in one double-float recursion (about 1e-14 relative): DF64, and the FP32 / BF16X3
+    // propagations, whose own rounding is near 1e-7; FP64 keeps cuSOLVER potrf and the FP64 inverse
+    const bool together = implicit && tr->cs.precision != ELHL_PREC_FP64;
     if (together) {
         if (int rc = chol_inv_pairs(tr->cs, tr->fac.L, tr->cs.Ht, tr->fac.info)) return rc;
     } else {
