@@ -32,7 +32,7 @@ EXPORTED_SYMBOLS = (
     "ehrenfestkernel2_gpu_", "elhl_ehrenfest_forces", "elhl_huckel_with_fields",
     "propagationelhl_gpucaller_", "elhl_last_status", "elhl_status_string", "elhl_traj_config_default",
     "elhl_traj_create", "elhl_traj_destroy", "elhl_traj_init_fmo", "elhl_traj_init_fmo_states", "elhl_traj_set_psi", "elhl_traj_get_psi", "elhl_traj_step",
-    "elhl_traj_step_device", "elhl_traj_energies", "elhl_traj_get_matrices", "elhl_traj_get_stats", "elhl_device_count",
+    "elhl_traj_step_device", "elhl_traj_energies", "elhl_traj_get_matrices", "elhl_traj_get_factor", "elhl_traj_get_stats", "elhl_device_count",
     "elhl_sm_count", "elhl_set_stream", "elhl_kernel_launches", "elhl_propagate_fixed_scratch", "elhl_bessel_j",
     "elhl_chebyshev_coefficients", "elhl_batch_create", "elhl_batch_size", "elhl_batch_member",
     "elhl_batch_compact", "elhl_batch_step", "elhl_batch_get_stats", "elhl_batch_destroy",
@@ -121,6 +121,7 @@ def load(path: str = LIB_PATH):
     L.elhl_traj_step.argtypes = [vp, vp, ci, vp]
     L.elhl_traj_step_device.argtypes = [vp, vp, ci, vp]
     L.elhl_traj_get_matrices.argtypes = [vp, vp, vp, vp]
+    L.elhl_traj_get_factor.argtypes = [vp, vp, vp]
     L.elhl_traj_energies.argtypes = [vp, vp]
     L.elhl_traj_get_stats.argtypes = [vp, ctypes.POINTER(TrajStats)]
     L.elhl_device_count.restype = ci
@@ -370,6 +371,15 @@ class Trajectory:
         S, h, Hp = (np.zeros((N, N), order="F") for _ in range(3))
         _check(load().elhl_traj_get_matrices(self.handle, _p(S), _p(h), _p(Hp)), "elhl_traj_get_matrices")
         return S, h, Hp
+
+    def factor(self, with_inverse: bool = True):
+        """Cholesky factor L of S and (after a step with coordinates) G = L^-1, host copies."""
+        N = self.N
+        L = np.zeros((N, N), order="F")
+        G = np.zeros((N, N), order="F") if with_inverse else None
+        _check(load().elhl_traj_get_factor(self.handle, _p(L), _p(G) if G is not None else None),
+               "elhl_traj_get_factor")
+        return L, G
 
     def stats(self) -> TrajStats:
         st = TrajStats()

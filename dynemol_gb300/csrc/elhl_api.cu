@@ -2630,6 +2630,21 @@ int elhl_traj_get_matrices(elhl_traj *tr, double *S, double *h, double *Hp) {
     return ELHL_OK;
 }
 
+int elhl_traj_get_factor(elhl_traj *tr, double *L, double *G) {
+    if (!tr) return ELHL_ERR_BAD_ARG;
+    if (!tr->cheb() || (G && !tr->cs.implicit)) return ELHL_ERR_UNSUPPORTED;
+    std::lock_guard<std::mutex> lk(g_ctx.mu);
+    CU_TRY(cudaStreamSynchronize(g_ctx.stream));
+    const size_t col = tr->N * sizeof(double), ldb = tr->ld * sizeof(double);
+    if (L) {
+        CU_TRY(cudaMemcpy2D(L, col, tr->fac.L, ldb, col, tr->N, cudaMemcpyDeviceToHost));
+        for (int j = 1; j < tr->N; ++j)  // the explicit operator's factor keeps S above the diagonal
+            std::memset(L + (size_t)j * tr->N, 0, j * sizeof(double));
+    }
+    if (G) CU_TRY(cudaMemcpy2D(G, col, tr->cs.Ht, ldb, col, tr->N, cudaMemcpyDeviceToHost));
+    return ELHL_OK;
+}
+
 int elhl_traj_get_stats(elhl_traj *tr, elhl_traj_stats *st) {
     if (!tr || !st) return ELHL_ERR_BAD_ARG;
     *st = tr->stats;

@@ -236,6 +236,12 @@ int elhl_traj_energies(elhl_traj *tr, elhl_zcomplex *E);
 /* Copies of the device matrices (host, N x N, ld = N); any pointer may be NULL. */
 int elhl_traj_get_matrices(elhl_traj *tr, double *S, double *h, double *Hp);
 
+/* The Chebyshev propagator's current Cholesky factor L (S = L L^T, lower, zero
+ * above the diagonal) and, once a step with coordinates has run (implicit
+ * operator), G = L^-1; host, N x N, ld = N; either pointer may be NULL.
+ * ELHL_ERR_UNSUPPORTED for G before the first such step or on the Taylor path. */
+int elhl_traj_get_factor(elhl_traj *tr, double *L, double *G);
+
 /* Counters of the last elhl_traj_step call. */
 typedef struct {
     long long orders;     /* expansion orders executed, summed over particles */

@@ -75,7 +75,8 @@ def test_cheb_fp64_moving_nuclei_vs_taylor_oracle(elhl, oracle_mod):
 @pytest.mark.parametrize("prec_name,tol", [("fp64", 1e-11), ("fp32", 5e-6)])
 def test_implicit_operator_matches_explicit(elhl, flake, prec_name, tol):
     """Steps given coordinates run the implicit operator G (h/b) G^T (three phases
-    per order, G = L^-1 by trtri); fixed-nuclei steps run the explicit H~.  Same
+    per order; G = L^-1 by the recursive inverse in FP64, by the double-float
+    Cholesky-with-inverse in FP32); fixed-nuclei steps run the explicit H~.  Same
     geometry, same result; fixed steps after moving ones keep the implicit form."""
     prec = {"fp64": elhl.PREC_FP64, "fp32": elhl.PREC_FP32}[prec_name]
     kw = dict(dt=1e-4, method=elhl.METHOD_CHEBYSHEV, precision=prec, ncols=4, cheb_tol=1e-14)
@@ -225,3 +226,40 @@ def test_df64_cluster_vs_exact(elhl, oracle_mod):
     ref = _exact(oracle_mod, sysm, np.column_stack([ket0, oracle_mod.fragment_mo(sysm, "H", homo)[0]]).astype(complex),
                  4e-4)
     assert np.abs(pops[-1] - ref).max() < 1e-9
+
+
+@pytest.mark.parametrize("prec_name,tol", [("fp64", 1e-12), ("df64", 1e-11), ("fp32", 1e-11)])
+def test_rebuild_factor_and_inverse(elhl, prec_name, tol):
+    """The moving-nuclei rebuild's factorisations at N = 1860 (a short last 64-row
+    leaf; short pairs in the batched levels of the FP64 inverse): FP64 runs potrf
+    and the recursive inverse of L, DF64 and FP32 the double-float
+    Cholesky-with-inverse.  L L^T = S, G L = I, L against numpy's Cholesky of the
+    same S, both factors lower triangular."""
+    prec = {"fp64": elhl.PREC_FP64, "df64": elhl.PREC_DF64, "fp32": elhl.PREC_FP32}[prec_name]
+    sysm = systems.cubic_cluster(n_atoms=600, seed=11)
+    homo = systems.fermi_state(sysm, sysm.fragment_atoms("E"))
+    coords = np.stack([systems.perturbed_coords(sysm.coords, i, seed=5) for i in range(2)])
+    tr = elhl.Trajectory(sysm, coords=coords[0], dt=2e-4, method=elhl.METHOD_CHEBYSHEV, precision=prec, ncols=4,
+                         cheb_tol=1e-12)
+    tr.init_fmo(homo + 1, homo)
+    tr.step(coords[1:], nsteps=1)
+    S, _, _ = tr.matrices()
+    L, G = tr.factor()
+    tr.close()
+    assert S.shape == (1860, 1860)
+    assert np.abs(np.triu(L, 1)).max() == 0.0 and np.abs(np.triu(G, 1)).max() == 0.0
+    assert np.abs(L @ L.T - S).max() < tol
+    assert np.abs(G @ L - np.eye(S.shape[0])).max() < 10 * tol
+    assert np.abs(L - np.linalg.cholesky(S)).max() < 10 * tol
+
+
+def test_kernel_launch_counter(elhl, flake):
+    """The library counts its own kernel launches (bench.py's gpu_launches)."""
+    n0 = elhl.kernel_launches()
+    tr = elhl.Trajectory(flake, dt=1e-4, method=elhl.METHOD_CHEBYSHEV, precision=elhl.PREC_FP64, ncols=2)
+    tr.init_fmo(41, 40)
+    n1 = elhl.kernel_launches()
+    tr.step(None, nsteps=3)
+    n2 = elhl.kernel_launches()
+    tr.close()
+    assert n1 > n0 and n2 > n1
