@@ -336,11 +336,21 @@ __device__ void pair_overlap_block(const DevBasis &b, int ia, int ib, double xab
     }
 }
 
+// One thread per atom pair.  Threads walk the pairs in b.atom_order (atoms
+// grouped by kind), so that the lanes of a warp mostly take the same shell and
+// zeta loops; each pair is computed as (ia, ib) with ia >= ib in the input order,
+// the same arithmetic whatever the walk.
 __global__ void build_sh_kernel(DevBasis b, const double *__restrict__ coords, double cutoff,
                                 double *__restrict__ S, double *__restrict__ h, int ld) {
-    const int ia = blockIdx.y * blockDim.y + threadIdx.y;
-    const int ib = blockIdx.x * blockDim.x + threadIdx.x;
-    if (ia >= b.natoms || ib >= b.natoms || ib > ia) return;
+    const int py = blockIdx.y * blockDim.y + threadIdx.y;
+    const int px = blockIdx.x * blockDim.x + threadIdx.x;
+    if (py >= b.natoms || px >= b.natoms || px > py) return;
+    int ia = b.atom_order ? b.atom_order[py] : py, ib = b.atom_order ? b.atom_order[px] : px;
+    if (ib > ia) {
+        const int t = ia;
+        ia = ib;
+        ib = t;
+    }
     const int a0 = b.atom_ao0[ia], na_ao = b.atom_nao[ia];
     const int b0 = b.atom_ao0[ib], nb_ao = b.atom_nao[ib];
 

@@ -1746,13 +1746,31 @@ int upload_basis(DevBasis &d, const elhl_basis_desc *b) {
     rc |= up_d(&d.ao_kwh, b->ao_kwh, b->nao);
     rc |= up_d(&d.ao_vshift, b->ao_vshift, b->nao);
     if (b->ao_frag) rc |= up_i(&d.ao_frag, b->ao_frag, b->nao);
+    // atoms grouped by kind: AO count, then each AO's (n, l, zetas), so that the
+    // S/h build's warps see few distinct pair kinds
+    std::vector<int> order(b->natoms);
+    for (int a = 0; a < b->natoms; ++a) order[a] = a;
+    auto key = [&](int a) {
+        std::vector<double> k{(double)b->atom_nao[a]};
+        for (int i = b->atom_ao0[a]; i < b->atom_ao0[a] + b->atom_nao[a]; ++i) {
+            k.push_back(b->ao_n[i]);
+            k.push_back(b->ao_l[i]);
+            k.push_back(b->ao_nzeta[i]);
+            for (int z = 0; z < b->ao_nzeta[i]; ++z) k.push_back(b->ao_zeta[2 * i + z]);
+        }
+        return k;
+    };
+    std::vector<std::vector<double>> keys(b->natoms);
+    for (int a = 0; a < b->natoms; ++a) keys[a] = key(a);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return keys[x] < keys[y]; });
+    rc |= up_i(&d.atom_order, order.data(), b->natoms);
     return rc ? ELHL_ERR_CUDA : ELHL_OK;
 }
 
 void free_basis(DevBasis &d) {
     dev_free(d.atom_ao0); dev_free(d.atom_nao); dev_free(d.ao_n); dev_free(d.ao_l); dev_free(d.ao_m);
     dev_free(d.ao_nzeta); dev_free(d.ao_zeta); dev_free(d.ao_coef); dev_free(d.ao_ip); dev_free(d.ao_kwh);
-    dev_free(d.ao_vshift); dev_free(d.ao_frag);
+    dev_free(d.ao_vshift); dev_free(d.ao_frag); dev_free(d.atom_order);
 }
 
 int validate_basis(const elhl_basis_desc *b) {

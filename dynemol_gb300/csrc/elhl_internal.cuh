@@ -27,6 +27,7 @@ struct DevBasis {
     int *atom_ao0 = nullptr, *atom_nao = nullptr;
     int *ao_n = nullptr, *ao_l = nullptr, *ao_m = nullptr, *ao_nzeta = nullptr, *ao_frag = nullptr;
     double *ao_zeta = nullptr, *ao_coef = nullptr, *ao_ip = nullptr, *ao_kwh = nullptr, *ao_vshift = nullptr;
+    int *atom_order = nullptr;  // atoms grouped by kind (same AO signature): the S/h build's pair order
 };
 
 // One-time per-device fill of the overlap kernel's constant tables.
