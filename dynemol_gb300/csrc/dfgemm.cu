@@ -17,7 +17,8 @@
 // tiles that reach the diagonal or below it are written (a symmetric update).
 //
 // Tiling: 64 x 64 output tile per CTA of 256 threads, 4 x 4 outputs per thread,
-// K in steps of 16 staged in shared memory.  Products with fewer tiles than SMs
+// K in steps of 16 staged in shared memory, two stages: cp.async fetches the
+// next k tile (zero-filling masked elements) while the current one is used.  Products with fewer tiles than SMs
 // (the lower levels of the recursive factorisations) split K over gridDim.z
 // CTAs per tile: each writes its partial tile (pairs) to a workspace, and the
 // CTA that arrives last at the tile's counter sums the partials in split order
@@ -36,6 +37,15 @@ constexpr int kSplitBelowTiles = 152;  // one tile per SM
 float2 *g_part = nullptr;              // [tile][split][kBM * kBN]
 int *g_count = nullptr;                // [tile] arrivals, back to 0 after each fix-up
 
+// 8-byte global -> shared copy, asynchronous; src_bytes = 0 writes zeros
+__device__ __forceinline__ void cp_async8(float2 *dst, const float2 *src, int src_bytes) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
 // c <- alpha v + beta c (beta = 0: c not read)
 __device__ __forceinline__ void store_df(float2 *c, float2 v, float2 alpha, float2 beta) {
     v = df_mul(v, alpha);
@@ -48,8 +58,8 @@ __global__ void __launch_bounds__(kThreads) dfgemm_kernel(int m, int n, int k, f
                                                           int lda, const float2 *__restrict__ B, int ldb, float2 beta,
                                                           float2 *__restrict__ C, int ldc, int tri,
                                                           float2 *__restrict__ part, int *__restrict__ count) {
-    __shared__ float2 As[kBK][kBM + 1];
-    __shared__ float2 Bs[kBK][kBN + 1];
+    __shared__ float2 As[2][kBK][kBM + 1];
+    __shared__ float2 Bs[2][kBK][kBN + 1];
     const int tid = threadIdx.x;
     const int i0 = blockIdx.x * kBM, j0 = blockIdx.y * kBN;
     if ((tri & kTriLowerC) && i0 + kBM <= j0) return;  // tile strictly above the diagonal
@@ -71,36 +81,48 @@ __global__ void __launch_bounds__(kThreads) dfgemm_kernel(int m, int n, int k, f
     for (int q = 0; q < 4; ++q)
 #pragma unroll
         for (int p = 0; p < 4; ++p) sh[q][p] = sl[q][p] = 0.f;
-    const float2 zero = make_float2(0.f, 0.f);
-    for (int k0 = klo; k0 < khi; k0 += kBK) {
-        // A tile kBM x kBK: consecutive threads on consecutive rows (coalesced)
+    // stage s <- the k tile at k0: A tile kBM x kBK with consecutive threads on
+    // consecutive rows, op(B) tile kBK x kBN along its contiguous index (both
+    // coalesced); masked elements are zero-filled from an in-bounds address
+    auto fetch = [&](int s, int k0) {
         for (int t = tid; t < kBM * kBK; t += kThreads) {
             const int ii = t % kBM, kk = t / kBM;
             const int gi = i0 + ii, gk = k0 + kk;
             const bool nz = gi < m && gk < k && !((tri & kTriA) && gk > gi);
-            As[kk][ii] = nz ? A[(size_t)gk * lda + gi] : zero;
+            cp_async8(&As[s][kk][ii], nz ? A + (size_t)gk * lda + gi : A, nz ? 8 : 0);
         }
-        // op(B) tile kBK x kBN, consecutive threads along the contiguous index
         for (int t = tid; t < kBK * kBN; t += kThreads) {
             const int kk = TB ? t / kBN : t % kBK, jj = TB ? t % kBN : t / kBK;
             const int gk = k0 + kk, gj = j0 + jj;
             const bool nz = gk < k && gj < n && !((tri & kTriB) && gk < gj) && !((tri & kTriBt) && gk > gj);
-            Bs[kk][jj] = nz ? (TB ? B[(size_t)gk * ldb + gj] : B[(size_t)gj * ldb + gk]) : zero;
+            const float2 *src = TB ? B + (size_t)gk * ldb + gj : B + (size_t)gj * ldb + gk;
+            cp_async8(&Bs[s][kk][jj], nz ? src : B, nz ? 8 : 0);
+        }
+        cp_async_commit();
+    };
+    if (klo < khi) fetch(0, klo);
+    int s = 0;
+    for (int k0 = klo; k0 < khi; k0 += kBK, s ^= 1) {
+        if (k0 + kBK < khi) {
+            fetch(s ^ 1, k0 + kBK);
+            cp_async_wait<1>();  // this tile's group is complete, the next one may be in flight
+        } else {
+            cp_async_wait<0>();
         }
         __syncthreads();
 #pragma unroll 4
         for (int kk = 0; kk < kBK; ++kk) {
             float2 a[4], b[4];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) a[q] = As[kk][tr + 16 * q];
+            for (int q = 0; q < 4; ++q) a[q] = As[s][kk][tr + 16 * q];
 #pragma unroll
-            for (int p = 0; p < 4; ++p) b[p] = Bs[kk][tc + 16 * p];
+            for (int p = 0; p < 4; ++p) b[p] = Bs[s][kk][tc + 16 * p];
 #pragma unroll
             for (int q = 0; q < 4; ++q)
 #pragma unroll
                 for (int p = 0; p < 4; ++p) df_fma(sh[q][p], sl[q][p], a[q].x, a[q].y, b[p].x, b[p].y);
         }
-        __syncthreads();
+        __syncthreads();  // stage s is refilled by the next iteration's fetch
     }
     if (gridDim.z == 1) {
 #pragma unroll
