@@ -1600,18 +1600,68 @@ int cols_apply(const double *Lfac, int ld, int n, double2 *cols, int m, int col0
     return ELHL_OK;
 }
 
+// Y (R x n) = X M for an R x n X (column k at X + k ldx) and a triangular FP64
+// M: Y(r, j) = sum_k X(r, k) M(k, j) over the non-zero part of column j of M
+// (k >= j for a lower M, k <= j for an upper one).  One warp per column j:
+// coalesced reads of the column, the R <= kMaxTransformRows values of X(., k)
+// from L1/L2, FP64 FMAs, then fixed-order warp sums.  The DGEMM it replaces,
+// with 4 rows, ran at about 0.9 ms at N = 3720.
+constexpr int kMaxTransformRows = 8;
+template <bool LOWER>
+__global__ void cols_mt_kernel(const double *__restrict__ M, int ld, int n, const double *__restrict__ X, int ldx,
+                               int R, double *__restrict__ Y) {
+    const int j = (blockIdx.x * blockDim.x + threadIdx.x) / 32, lane = threadIdx.x % 32;
+    if (j >= n) return;
+    const int k0 = LOWER ? j : 0, k1 = LOWER ? n : j + 1;
+    const double *col = M + (size_t)j * ld;
+    double acc[kMaxTransformRows];
+#pragma unroll
+    for (int r = 0; r < kMaxTransformRows; ++r) acc[r] = 0.0;
+    for (int k = k0 + lane; k < k1; k += 32) {
+        const double mk = col[k];
+        const double *x = X + (size_t)k * ldx;
+#pragma unroll
+        for (int r = 0; r < kMaxTransformRows; ++r)
+            if (r < R) acc[r] = fma(mk, x[r], acc[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < kMaxTransformRows; ++r)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[r] += __shfl_xor_sync(0xffffffffu, acc[r], o);
+#pragma unroll
+    for (int r = 0; r < kMaxTransformRows; ++r)
+        if (r < R && lane == r) Y[(size_t)j * R + r] = acc[r];
+}
+
 // The same four transforms with dense FP64 factors (zeros above the diagonal):
-// M = G = L^-1 for the inverse ones, M = L otherwise; one DGEMM X op(M) into
-// scratch (2 ncols x n) and a strided copy back.  The implicit operator keeps
-// both factors, and a DGEMM over a few rows costs one read of M, where a
-// right-side TRSM with 4 rows runs as a long chain of small launches.
+// M = G = L^-1 for the inverse ones, M = L otherwise, X op(M) into scratch
+// (2 ncols x n) and a strided copy back.  op(M) = M, and op(M) = M^T when the
+// FP64 transpose Mt (Lt for L, Gt for G) is resident, run as cols_mt_kernel;
+// otherwise one DGEMM.  The implicit operator keeps both factors, and either
+// costs one read of M, where a right-side TRSM with 4 rows runs as a long
+// chain of small launches.
 int cols_apply_dense(const double *L, const double *G, int ld, int n, double2 *cols, int m, int col0, int ncols,
-                     bool transpose, bool inverse, double *scratch) {
+                     bool transpose, bool inverse, double *scratch, const double *Lt = nullptr,
+                     const double *Gt = nullptr) {
     const double one = 1.0, zero = 0.0;
     double *X = reinterpret_cast<double *>(cols) + 2 * col0;
     const int rows = 2 * ncols, ldx = 2 * m;
-    BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, transpose ? CUBLAS_OP_T : CUBLAS_OP_N, rows, n, n, &one, X, ldx,
-                         inverse ? G : L, ld, &zero, scratch, rows));
+    const double *Mt = inverse ? Gt : Lt;
+    if (rows <= kMaxTransformRows && (!transpose || Mt)) {
+        const int warps_per_block = 8, grid = (n + warps_per_block - 1) / warps_per_block;
+        if (!transpose) {
+            cols_mt_kernel<true><<<grid, 32 * warps_per_block, 0, g_ctx.stream>>>(inverse ? G : L, ld, n, X, ldx, rows,
+                                                                                   scratch);
+            count_launch();
+        } else {  // X M^T = X (Mt)^T with Mt upper triangular
+            cols_mt_kernel<false><<<grid, 32 * warps_per_block, 0, g_ctx.stream>>>(Mt, ld, n, X, ldx, rows, scratch);
+            count_launch();
+        }
+        CU_TRY(cudaGetLastError());
+    } else {
+        BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, transpose ? CUBLAS_OP_T : CUBLAS_OP_N, rows, n, n, &one, X, ldx,
+                             inverse ? G : L, ld, &zero, scratch, rows));
+    }
     CU_TRY(cudaMemcpy2DAsync(X, ldx * sizeof(double), scratch, rows * sizeof(double), rows * sizeof(double), n,
                              cudaMemcpyDeviceToDevice, g_ctx.stream));
     return ELHL_OK;
@@ -1841,9 +1891,14 @@ int cheb_load_columns(elhl_traj *tr) {
     if (cs.m == 2 * P)
         CU_TRY(cudaMemcpy2DAsync(in + P, cs.m * e, tr->bra_ao, P * e, P * e, n, cudaMemcpyDeviceToDevice, st));
     if (cs.implicit) {  // dense L (zeroed upper triangle) and G = L^-1
-        if (int rc = cols_apply_dense(tr->fac.L, cs.Ht, tr->ld, n, in, cs.m, 0, P, false, false, cs.cscratch)) return rc;
+        // FP64 L^T (B) and G^T (Gt) are resident on the FP64 path
+        const bool t64 = cs.precision == ELHL_PREC_FP64;
+        const double *Lt = t64 ? static_cast<const double *>(cs.B) : nullptr;
+        const double *Gt = t64 ? static_cast<const double *>(cs.Gt) : nullptr;
+        if (int rc = cols_apply_dense(tr->fac.L, cs.Ht, tr->ld, n, in, cs.m, 0, P, false, false, cs.cscratch, Lt, Gt))
+            return rc;
         if (cs.m == 2 * P)
-            if (int rc = cols_apply_dense(tr->fac.L, cs.Ht, tr->ld, n, in, cs.m, P, P, true, true, cs.cscratch))
+            if (int rc = cols_apply_dense(tr->fac.L, cs.Ht, tr->ld, n, in, cs.m, P, P, true, true, cs.cscratch, Lt, Gt))
                 return rc;
         cs.cols_current = true;
         return ELHL_OK;
