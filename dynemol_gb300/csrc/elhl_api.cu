@@ -590,6 +590,11 @@ struct ChebState {
     void *wb = nullptr;      // [2][ld][m] launch precision (phase intermediates)
     double *fws = nullptr;   // workspace of the recursive factorisations
     size_t fws_n = 0;
+    // FP64 L^T and G^T for the column transforms of the implicit operator: B and
+    // Gt on the FP64 path, own copies in the other precisions
+    double *Lt64 = nullptr, *Gt64 = nullptr;
+    const double *lt64() const { return precision == ELHL_PREC_FP64 ? static_cast<const double *>(B) : Lt64; }
+    const double *gt64() const { return precision == ELHL_PREC_FP64 ? static_cast<const double *>(Gt) : Gt64; }
     double *cscratch = nullptr;  // [2m][ld] column-transform output
     int alloc(int N_, int m_, int prec) {
         N = N_;
@@ -630,6 +635,8 @@ struct ChebState {
         Gt = wb = nullptr;
         dev_free(fws);
         fws_n = 0;
+        dev_free(Lt64);
+        dev_free(Gt64);
         dev_free(cscratch);
         implicit = false;
         dev_free(gpops);
@@ -1095,6 +1102,16 @@ int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, do
     if (int rc = lanczos_bounds(cs, 40, h)) return rc;
     if (int rc = cheb_prepare(cs, dt, tol, h)) return rc;
     dim3 grid((ld + 127) / 128, n);
+    if (cs.precision != ELHL_PREC_FP64) {  // FP64 L^T and G^T for the column transforms
+        if (!cs.Lt64)
+            if (int rc = dev_alloc(&cs.Lt64, (size_t)ld * n)) return rc;
+        if (!cs.Gt64)
+            if (int rc = dev_alloc(&cs.Gt64, (size_t)ld * n)) return rc;
+        convert_kernel<double><<<grid, 128, 0, st>>>(Lfac, cs.Lt64, n, ld, true);
+        count_launch();
+        convert_kernel<double><<<grid, 128, 0, st>>>(cs.Ht, cs.Gt64, n, ld, true);
+        count_launch();
+    }
     if (cs.precision == ELHL_PREC_DF64) {  // G and G^T as (hi, lo) pairs; no device read-out matrices
         split_df_kernel<<<grid, 128, 0, st>>>(cs.Ht, (float2 *)cs.A, n, ld, 0.0, 1.0, false);
         count_launch();
@@ -1891,10 +1908,7 @@ int cheb_load_columns(elhl_traj *tr) {
     if (cs.m == 2 * P)
         CU_TRY(cudaMemcpy2DAsync(in + P, cs.m * e, tr->bra_ao, P * e, P * e, n, cudaMemcpyDeviceToDevice, st));
     if (cs.implicit) {  // dense L (zeroed upper triangle) and G = L^-1
-        // FP64 L^T (B) and G^T (Gt) are resident on the FP64 path
-        const bool t64 = cs.precision == ELHL_PREC_FP64;
-        const double *Lt = t64 ? static_cast<const double *>(cs.B) : nullptr;
-        const double *Gt = t64 ? static_cast<const double *>(cs.Gt) : nullptr;
+        const double *Lt = cs.lt64(), *Gt = cs.gt64();
         if (int rc = cols_apply_dense(tr->fac.L, cs.Ht, tr->ld, n, in, cs.m, 0, P, false, false, cs.cscratch, Lt, Gt))
             return rc;
         if (cs.m == 2 * P)
@@ -1920,9 +1934,11 @@ int cheb_readout(elhl_traj *tr, const double2 *cols, double *d_pops) {
     const double2 *bsrc = (cs.m == 2 * P) ? cols + P : cols;
     CU_TRY(cudaMemcpy2DAsync(tr->bra_ao, P * e, bsrc, cs.m * e, P * e, n, cudaMemcpyDeviceToDevice, st));
     if (cs.implicit) {
-        if (int rc = cols_apply_dense(tr->fac.L, cs.Ht, tr->ld, n, tr->psi_ao, P, 0, P, false, true, cs.cscratch))
+        if (int rc = cols_apply_dense(tr->fac.L, cs.Ht, tr->ld, n, tr->psi_ao, P, 0, P, false, true, cs.cscratch,
+                                      cs.lt64(), cs.gt64()))
             return rc;  // L^-T phi
-        if (int rc = cols_apply_dense(tr->fac.L, cs.Ht, tr->ld, n, tr->bra_ao, P, 0, P, true, false, cs.cscratch))
+        if (int rc = cols_apply_dense(tr->fac.L, cs.Ht, tr->ld, n, tr->bra_ao, P, 0, P, true, false, cs.cscratch,
+                                      cs.lt64(), cs.gt64()))
             return rc;  // L chi
     } else {
         if (int rc = cols_apply(tr->fac.L, tr->ld, n, tr->psi_ao, P, 0, P, false, true)) return rc;   // L^-T phi
