@@ -228,25 +228,29 @@ def test_df64_cluster_vs_exact(elhl, oracle_mod):
     assert np.abs(pops[-1] - ref).max() < 1e-9
 
 
+@pytest.mark.parametrize("n_atoms,nao", [(20, 62), (64, 199), (150, 465), (600, 1860)])
 @pytest.mark.parametrize("prec_name,tol", [("fp64", 1e-12), ("df64", 1e-11), ("fp32", 1e-11)])
-def test_rebuild_factor_and_inverse(elhl, prec_name, tol):
-    """The moving-nuclei rebuild's factorisations at N = 1860 (a short last 64-row
-    leaf; short pairs in the batched levels of the FP64 inverse): FP64 runs potrf
-    and the recursive inverse of L, DF64 and FP32 the double-float
-    Cholesky-with-inverse.  L L^T = S, G L = I, L against numpy's Cholesky of the
-    same S, both factors lower triangular."""
+def test_rebuild_factor_and_inverse(elhl, prec_name, tol, n_atoms, nao):
+    """The moving-nuclei rebuild's factorisations: FP64 runs potrf and the
+    recursive inverse of L, DF64 and FP32 the double-float Cholesky-with-inverse.
+    N = 62 is one leaf, 199 and 465 stay below the 512-row bottom-up block, 1860
+    has a short last 64-row leaf and short pairs in the batched levels.
+    L L^T = S, G L = I, L against numpy's Cholesky of the same S, both factors
+    lower triangular."""
     prec = {"fp64": elhl.PREC_FP64, "df64": elhl.PREC_DF64, "fp32": elhl.PREC_FP32}[prec_name]
-    sysm = systems.cubic_cluster(n_atoms=600, seed=11)
-    homo = systems.fermi_state(sysm, sysm.fragment_atoms("E"))
+    sysm = systems.cubic_cluster(n_atoms=n_atoms, seed=11)
     coords = np.stack([systems.perturbed_coords(sysm.coords, i, seed=5) for i in range(2)])
     tr = elhl.Trajectory(sysm, coords=coords[0], dt=2e-4, method=elhl.METHOD_CHEBYSHEV, precision=prec, ncols=4,
                          cheb_tol=1e-12)
-    tr.init_fmo(homo + 1, homo)
+    rng = np.random.default_rng(n_atoms)
+    psi = rng.standard_normal((nao, 2)) + 1j * rng.standard_normal((nao, 2))
+    psi /= np.linalg.norm(psi, axis=0)
+    tr.set_psi(psi, psi)  # any state: only the factors are checked
     tr.step(coords[1:], nsteps=1)
     S, _, _ = tr.matrices()
     L, G = tr.factor()
     tr.close()
-    assert S.shape == (1860, 1860)
+    assert S.shape == (nao, nao)
     assert np.abs(np.triu(L, 1)).max() == 0.0 and np.abs(np.triu(G, 1)).max() == 0.0
     assert np.abs(L @ L.T - S).max() < tol
     assert np.abs(G @ L - np.eye(S.shape[0])).max() < 10 * tol
