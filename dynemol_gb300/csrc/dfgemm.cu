@@ -16,7 +16,7 @@
 // triangular product costs half a square one.  With kTriLowerC only output
 // tiles that reach the diagonal or below it are written (a symmetric update).
 //
-// Tiling: 64 x 64 output tile per CTA of 256 threads, 4 x 4 outputs per thread,
+// Tiling: 64 x 64 output tile per CTA of 256 threads, kTM x kTN = 4 x 4 outputs per thread,
 // K in steps of 16 staged in shared memory, two stages: cp.async fetches the
 // next k tile (zero-filling masked elements) while the current one is used.  Products with fewer tiles than SMs
 // (the lower levels of the recursive factorisations) split K over gridDim.z
@@ -31,7 +31,12 @@
 namespace elhl {
 namespace {
 
-constexpr int kBM = 64, kBN = 64, kBK = 16, kThreads = 256;
+constexpr int kBM = 64, kBN = 64, kBK = 16;
+// outputs per thread (rows x columns); measured on the N = 3720 DF64 factorisation:
+// 4 x 4 (64 registers) 23.2 ms, 8 x 4 24.9 ms, 4 x 8 25.4 ms (124-128 registers)
+constexpr int kTM = 4, kTN = 4;
+constexpr int kRT = kBM / kTM, kCT = kBN / kTN;      // threads along rows and columns
+constexpr int kThreads = kRT * kCT;
 constexpr int kMaxPartials = 1024;     // tiles x splits held by the split-K workspace
 constexpr int kSplitBelowTiles = 152;  // one tile per SM
 float2 *g_part = nullptr;              // [tile][split][kBM * kBN]
@@ -75,12 +80,12 @@ __global__ void __launch_bounds__(kThreads) dfgemm_kernel(int m, int n, int k, f
         khi = min(khi, klo + kt1 * kBK);
         klo += kt0 * kBK;
     }
-    const int tr = tid % 16, tc = tid / 16;  // 4 x 4 outputs: rows i0 + tr + 16 q, columns j0 + tc + 16 p
-    float sh[4][4], sl[4][4];
+    const int tr = tid % kRT, tc = tid / kRT;  // outputs: rows i0 + tr + kRT q, columns j0 + tc + kCT p
+    float sh[kTM][kTN], sl[kTM][kTN];
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
+    for (int q = 0; q < kTM; ++q)
 #pragma unroll
-        for (int p = 0; p < 4; ++p) sh[q][p] = sl[q][p] = 0.f;
+        for (int p = 0; p < kTN; ++p) sh[q][p] = sl[q][p] = 0.f;
     // stage s <- the k tile at k0: A tile kBM x kBK with consecutive threads on
     // consecutive rows, op(B) tile kBK x kBN along its contiguous index (both
     // coalesced); masked elements are zero-filled from an in-bounds address
@@ -112,24 +117,24 @@ __global__ void __launch_bounds__(kThreads) dfgemm_kernel(int m, int n, int k, f
         __syncthreads();
 #pragma unroll 4
         for (int kk = 0; kk < kBK; ++kk) {
-            float2 a[4], b[4];
+            float2 a[kTM], b[kTN];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) a[q] = As[s][kk][tr + 16 * q];
+            for (int q = 0; q < kTM; ++q) a[q] = As[s][kk][tr + kRT * q];
 #pragma unroll
-            for (int p = 0; p < 4; ++p) b[p] = Bs[s][kk][tc + 16 * p];
+            for (int p = 0; p < kTN; ++p) b[p] = Bs[s][kk][tc + kCT * p];
 #pragma unroll
-            for (int q = 0; q < 4; ++q)
+            for (int q = 0; q < kTM; ++q)
 #pragma unroll
-                for (int p = 0; p < 4; ++p) df_fma(sh[q][p], sl[q][p], a[q].x, a[q].y, b[p].x, b[p].y);
+                for (int p = 0; p < kTN; ++p) df_fma(sh[q][p], sl[q][p], a[q].x, a[q].y, b[p].x, b[p].y);
         }
         __syncthreads();  // stage s is refilled by the next iteration's fetch
     }
     if (gridDim.z == 1) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
+        for (int q = 0; q < kTM; ++q)
 #pragma unroll
-            for (int p = 0; p < 4; ++p) {
-                const int gi = i0 + tr + 16 * q, gj = j0 + tc + 16 * p;
+            for (int p = 0; p < kTN; ++p) {
+                const int gi = i0 + tr + kRT * q, gj = j0 + tc + kCT * p;
                 if (gi < m && gj < n) store_df(C + (size_t)gj * ldc + gi, df_renorm(sh[q][p], sl[q][p]), alpha, beta);
             }
         return;
@@ -138,9 +143,9 @@ __global__ void __launch_bounds__(kThreads) dfgemm_kernel(int m, int n, int k, f
     const int S = gridDim.z, tile = blockIdx.y * gridDim.x + blockIdx.x;
     float2 *mine = part + ((size_t)tile * S + blockIdx.z) * (kBM * kBN);
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
+    for (int q = 0; q < kTM; ++q)
 #pragma unroll
-        for (int p = 0; p < 4; ++p) mine[(tc + 16 * p) * kBM + tr + 16 * q] = df_renorm(sh[q][p], sl[q][p]);
+        for (int p = 0; p < kTN; ++p) mine[(tc + kCT * p) * kBM + tr + kRT * q] = df_renorm(sh[q][p], sl[q][p]);
     __threadfence();
     __syncthreads();
     __shared__ int last;
@@ -150,10 +155,10 @@ __global__ void __launch_bounds__(kThreads) dfgemm_kernel(int m, int n, int k, f
     __threadfence();
     const float2 *all = part + (size_t)tile * S * (kBM * kBN);
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
+    for (int q = 0; q < kTM; ++q)
 #pragma unroll
-        for (int p = 0; p < 4; ++p) {
-            const int gi = i0 + tr + 16 * q, gj = j0 + tc + 16 * p, e = (tc + 16 * p) * kBM + tr + 16 * q;
+        for (int p = 0; p < kTN; ++p) {
+            const int gi = i0 + tr + kRT * q, gj = j0 + tc + kCT * p, e = (tc + kCT * p) * kBM + tr + kRT * q;
             float2 sum = __ldcg(all + e);
             for (int z = 1; z < S; ++z) sum = df_sum(sum, __ldcg(all + (size_t)z * (kBM * kBN) + e));
             if (gi < m && gj < n) store_df(C + (size_t)gj * ldc + gi, sum, alpha, beta);
