@@ -614,7 +614,7 @@ def main():
         line["dropin_taylor_fp64"] = run_dropin(args)
     if rank == 0 and args.mix:
         from dynemol_gb300 import api
-        line["north_star_mix"] = run_mix(args, args.mix, steps=5, warm=2, precision=api.PREC_FP32,
+        line["trajectory_mix"] = run_mix(args, args.mix, steps=5, warm=2, precision=api.PREC_FP32,
                                          dropin_sample=4)
     if rank == 0 and args.precision_study:
         line["precision_study"] = run_precision_study(args)
