@@ -230,7 +230,7 @@ def run_ours(args, rank, world):
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
     hbm_peak = peaks.get("hbm_gbs", 6800.0)
-    FP64_PEAK = 1.20  # TFLOP/s, FMA probe measured on this machine's GB300 (profiles/gb300_peaks_probe.md)
+    FP64_PEAK = 1.20  # TFLOP/s: FP64 FMA throughput of a GB300 measured by a DFMA loop
     prop_launch_ms = prop_ms / K
     traffic_per_launch = None
     if args.method == "taylor":
@@ -256,9 +256,9 @@ def run_ours(args, rank, world):
         flops_per_launch = per_launch_orders * 4.0 * elems * m
         if moving and args.precision in ("fp64", "df64"):
             # DRAM traffic per matrix element and order measured by ncu on the same
-            # kernel at N = 2790 (profiles/cheb_kernel_implicit_cluster900_fp64_ncu.md:
-            # 18.68 GB read + 0.11 GB written over 149 orders of 2 N^2 elements);
-            # traffic grows with N^2 and the orders, so it is scaled to this launch
+            # kernel at N = 2790 (18.68 GB read + 0.11 GB written over 149 orders of
+            # 2 N^2 elements); traffic grows with N^2 and the orders, so it is scaled
+            # to this launch
             traffic_per_launch = 8.10 * elems * per_launch_orders
     achieved_gbs = bytes_per_launch / (prop_launch_ms * 1e-3) / 1e9
     # ALU bound: FP64 FMA pipe; FP32 FMA pipe; DF64 = FP32 pipe at 12 FP32
@@ -296,7 +296,7 @@ def run_ours(args, rank, world):
                              "peak_tflops": alu_peak,
                              "frac": tflops / alu_peak,
                              "pipe": alu_pipe,
-                             "peak_source": "of measured (FMA probe, profiles/gb300_peaks_probe.md)"},
+                             "peak_source": "of measured (FP64/FP32 FMA probe on a GB300)"},
                      "orders_per_launch": per_launch_orders, "launch_ms": prop_launch_ms},
         "breakdown_ms_per_step": {"propagation": prop_ms / K, "rebuild_S_h_operator": rebuild_ms / K,
                                   "rebuild_parts": {"S_h_build": sh_ms / K, "cholesky": factor_ms / K,
