@@ -934,13 +934,15 @@ int trmm_left_oop(double alpha, const double *T, int ldt, const double *X, int l
 
 // Above kTriBlock rows: [L11 0; L21 L22]^-1 = [G11 0; -G22 L21 G11  G22], the
 // splits on multiples of kTriBlock so that the leaves are the blocks the
-// bottom-up levels finished.
-int tri_inverse_top(double *A, int n, int ld, double *W) {
+// bottom-up levels finished.  wcap: elements of W; a block that would not fit
+// is refused before any launch.
+int tri_inverse_top(double *A, int n, int ld, double *W, size_t wcap) {
     if (n <= kTriBlock) return ELHL_OK;
     const int n1 = round_up(n / 2, kTriBlock), n2 = n - n1;
     double *A11 = A, *A21 = A + n1, *A22 = A + (size_t)n1 * ld + n1;
-    if (int rc = tri_inverse_top(A11, n1, ld, W)) return rc;
-    if (int rc = tri_inverse_top(A22, n2, ld, W)) return rc;
+    if ((size_t)ld * n1 > wcap) return ELHL_ERR_OOM;  // W holds n2 x n1 at leading dimension ld
+    if (int rc = tri_inverse_top(A11, n1, ld, W, wcap)) return rc;
+    if (int rc = tri_inverse_top(A22, n2, ld, W, wcap)) return rc;
     if (int rc = trmm_right_oop(1.0, A21, ld, A11, ld, W, ld, n2, n1)) return rc;  // W = L21 G11
     return trmm_left_oop(-1.0, A22, ld, W, ld, A21, ld, n2, n1);                   // A21 = -G22 W
 }
@@ -963,6 +965,7 @@ int tri_inverse(ChebState &cs, double *A, int n, int ld) {
     for (int s = leaf_rows(); s < kTriBlock; s *= 2) {
         const int np = n / (2 * s), rem = n - 2 * s * np;
         const long long stride = (long long)2 * s * (ld + 1), ws = (long long)s * s;
+        if ((size_t)np * ws > cs.fws_n || (rem > s && (size_t)(rem - s) * s > cs.fws_n)) return ELHL_ERR_OOM;
         if (np > 0) {
             BLAS_TRY(cublasDgemmStridedBatched(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, s, s, s, &one, A + s, ld, stride,
                                                A, ld, stride, &zero, W, s, ws, np));  // W_p = L21 G11
@@ -979,7 +982,7 @@ int tri_inverse(ChebState &cs, double *A, int n, int ld) {
                                  W, n2, &zero, P + s, ld));
         }
     }
-    return tri_inverse_top(A, n, ld, W);
+    return tri_inverse_top(A, n, ld, W, cs.fws_n);
 }
 
 // G = L^-1 (FP64, lower, zero upper triangle) from a copy of the Cholesky factor:
@@ -1003,7 +1006,7 @@ int invert_factor(ChebState &cs, const double *Lfac, double *dst) {
 //   L22, G22 = chol_inv(A22);   G21 = -G22 (L21 G11),
 // N^3/3 + N^3/3 flops, with 64-row diagonal blocks as leaves (leaf_chol_inv_df).
 // The upper triangles of A and G are left undefined.
-int chol_inv_df(float2 *A, float2 *G, int n, int ld, int row0, float2 *W, int *info) {
+int chol_inv_df(float2 *A, float2 *G, int n, int ld, int row0, float2 *W, size_t wcap, int *info) {
     cudaStream_t st = g_ctx.stream;
     const int leaf = leaf_rows();
     if (n <= leaf) {
@@ -1011,14 +1014,15 @@ int chol_inv_df(float2 *A, float2 *G, int n, int ld, int row0, float2 *W, int *i
         return ELHL_OK;
     }
     const int n1 = round_up(n / 2, leaf), n2 = n - n1;
+    if ((size_t)ld * n1 > wcap) return ELHL_ERR_OOM;  // W holds n2 x n1 at leading dimension ld
     float2 *A21 = A + n1, *A22 = A + (size_t)n1 * ld + n1;
     float2 *G21 = G + n1, *G22 = G + (size_t)n1 * ld + n1;
-    if (int rc = chol_inv_df(A, G, n1, ld, row0, W, info)) return rc;
+    if (int rc = chol_inv_df(A, G, n1, ld, row0, W, wcap, info)) return rc;
     CU_TRY(cudaMemcpy2DAsync(W, ld * sizeof(float2), A21, ld * sizeof(float2), n2 * sizeof(float2), n1,
                              cudaMemcpyDeviceToDevice, st));
     CU_TRY(dfgemm(n2, n1, n1, 1.0, W, ld, G, ld, 0.0, A21, ld, st, true, kTriBt));              // L21
     CU_TRY(dfgemm(n2, n2, n1, -1.0, A21, ld, A21, ld, 1.0, A22, ld, st, true, kTriLowerC));    // Schur
-    if (int rc = chol_inv_df(A22, G22, n2, ld, row0 + n1, W, info)) return rc;
+    if (int rc = chol_inv_df(A22, G22, n2, ld, row0 + n1, W, wcap, info)) return rc;
     CU_TRY(dfgemm(n2, n1, n1, 1.0, A21, ld, G, ld, 0.0, W, ld, st, false, kTriB));             // L21 G11
     CU_TRY(dfgemm(n2, n1, n2, -1.0, G22, ld, W, ld, 0.0, G21, ld, st, false, kTriA));          // G21
     return ELHL_OK;
@@ -1033,7 +1037,7 @@ int chol_inv_pairs(ChebState &cs, double *Lfac, double *G, int *info) {
     CU_TRY(cudaMemsetAsync(info, 0, sizeof(int), st));
     CU_TRY(df_convert(Lfac, cs.N, cs.N, cs.ld, true, st));
     if (int rc = chol_inv_df(reinterpret_cast<float2 *>(Lfac), reinterpret_cast<float2 *>(G), cs.N, cs.ld, 0,
-                             reinterpret_cast<float2 *>(W), info))
+                             reinterpret_cast<float2 *>(W), cs.fws_n, info))
         return rc;
     CU_TRY(df_convert(Lfac, cs.N, cs.N, cs.ld, false, st));
     CU_TRY(df_convert(G, cs.N, cs.N, cs.ld, false, st));
