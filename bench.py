@@ -235,11 +235,11 @@ def run_ours(args, rank, world):
     traffic_per_launch = None
     if args.method == "taylor":
         # dominant kernel: taylor_kernel.  Unit = one expansion order of one
-        # particle: H' read once for bra (H'^T) and ket (H'), 2 complex columns:
-        # bytes = 8 N^2 + 160 N, flops = 8 N^2
+        # particle: H' read twice, by rows for the ket (H') and by columns for the
+        # bra (H'^T), 2 complex columns: bytes = 16 N^2 + 160 N, flops = 8 N^2
         kernel = "taylor_kernel"
         per_launch_orders = orders / max(1, K)
-        bytes_per_launch = per_launch_orders * (8.0 * N * N + 160.0 * N)
+        bytes_per_launch = per_launch_orders * (16.0 * N * N + 160.0 * N)
         flops_per_launch = per_launch_orders * 8.0 * N * N
     else:
         # dominant kernel: cheb_kernel.  Unit = one Chebyshev order over m complex

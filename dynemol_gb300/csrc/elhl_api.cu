@@ -134,6 +134,9 @@ int ensure_context_locked(int device) {
     CU_TRY(cudaMemset(g_ctx.bar, 0, 2 * sizeof(unsigned)));
     CU_TRY(cudaMemset(g_ctx.err, 0, sizeof(int)));
     for (auto &e : g_ctx.ev) CU_TRY(cudaEventCreate(&e));
+    // make the allocation-free entry point's fixed array resident now, before
+    // a caller's pool allocator or stream capture can start
+    if (int rc = fixed_scratch_prepare()) return rc;
     g_ctx.ready = true;
     return ELHL_OK;
 }
@@ -366,28 +369,39 @@ struct DropIn {
     Factor fac;
     TaylorBuffers tb;
     double2 *ao = nullptr;
+    cudaEvent_t hp_ready = nullptr;  // H' formed: the copy stream may read it
     int reserve(int N_) {
         const int ld_ = round_up(N_, 32);
-        if (S && N_ <= N && ld_ == ld) return ELHL_OK;
-        release();
-        N = N_;
-        ld = ld_;
-        if (int rc = dev_alloc(&S, (size_t)ld * N)) return rc;
-        if (int rc = dev_alloc(&h, (size_t)ld * N)) return rc;
-        if (int rc = dev_alloc(&Hp, (size_t)ld * N)) return rc;
-        if (int rc = dev_alloc(&ao, (size_t)ld)) return rc;
-        if (int rc = fac.reserve(N, ld)) return rc;
-        if (int rc = tb.reserve(N, 1)) return rc;
+        if (!(S && N_ <= N && ld_ == ld)) {
+            release();
+            N = N_;
+            ld = ld_;
+            if (int rc = dev_alloc(&S, (size_t)ld * N)) return rc;
+            if (int rc = dev_alloc(&h, (size_t)ld * N)) return rc;
+            if (int rc = dev_alloc(&Hp, (size_t)ld * N)) return rc;
+            if (int rc = dev_alloc(&ao, (size_t)ld)) return rc;
+            if (int rc = fac.reserve(N, ld)) return rc;
+            if (int rc = tb.reserve(N, 1)) return rc;
+        }
+        if (!hp_ready) CU_TRY(cudaEventCreateWithFlags(&hp_ready, cudaEventDisableTiming));
         return ELHL_OK;
     }
     void release() {
         dev_free(S); dev_free(h); dev_free(Hp); dev_free(ao);
         fac.release();
         tb.release();
+        if (hp_ready) cudaEventDestroy(hp_ready);
+        hp_ready = nullptr;
         N = 0;
     }
 };
 DropIn g_drop;
+
+// Waits for the copy stream when it goes out of scope, so that no return path
+// leaves a copy into the caller's host buffer in flight.
+struct CopyStreamJoin {
+    ~CopyStreamJoin() { cudaStreamSynchronize(g_ctx.copy_stream); }
+};
 
 int dropin_elhl(int n, const double *hS, const double *hh, double *hH, elhl_zcomplex *hAO_bra, elhl_zcomplex *hbra,
                 elhl_zcomplex *hket, double t_init, double t_max, double tau, double *save_tau) {
@@ -403,11 +417,13 @@ int dropin_elhl(int n, const double *hS, const double *hh, double *hH, elhl_zcom
     CU_TRY(cudaMemcpyAsync(d.tb.bra(0), hbra, n * sizeof(double2), cudaMemcpyHostToDevice, st));
     CU_TRY(cudaMemcpyAsync(d.tb.ket(0), hket, n * sizeof(double2), cudaMemcpyHostToDevice, st));
     if (int rc = d.fac.form_hprime(d.S, d.h, d.Hp, n)) return rc;
+    // A factorisation that failed (S not positive definite) ends the call here,
+    // before anything is propagated or copied back.
+    if (int frc = d.fac.check_info()) return frc;
     // H' back to the host on a second stream, overlapped with the propagation (Taylor_gpu.cpp:700)
-    cudaEvent_t ev;
-    CU_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
-    CU_TRY(cudaEventRecord(ev, st));
-    CU_TRY(cudaStreamWaitEvent(g_ctx.copy_stream, ev, 0));
+    CopyStreamJoin join;
+    CU_TRY(cudaEventRecord(d.hp_ready, st));
+    CU_TRY(cudaStreamWaitEvent(g_ctx.copy_stream, d.hp_ready, 0));
     if (hH) CU_TRY(cudaMemcpy2DAsync(hH, col, d.Hp, ldb, col, n, cudaMemcpyDeviceToHost, g_ctx.copy_stream));
     const double tau_in[1] = {tau};
     const double dt = t_max - t_init;
@@ -424,7 +440,6 @@ int dropin_elhl(int n, const double *hS, const double *hh, double *hH, elhl_zcom
     std::vector<TaylorParticle> res;
     int rc = collect_taylor(d.tb, 1, res, nullptr);
     CU_TRY(cudaStreamSynchronize(g_ctx.copy_stream));
-    cudaEventDestroy(ev);
     if (int frc = d.fac.check_info()) return frc;
     if (save_tau) *save_tau = res[0].save_tau;
     return rc;

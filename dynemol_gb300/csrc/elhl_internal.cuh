@@ -88,6 +88,9 @@ constexpr int kSlots = 6;
 
 cudaError_t launch_taylor(const TaylorLaunch &L, int grid, int block, cudaStream_t st);
 int taylor_grid_size(int block, int *grid_out);
+// Loads the allocation-free entry point's module on the current device and
+// resolves its fixed scratch (noalloc.cu); ELHL_OK or an error status.
+int fixed_scratch_prepare();
 constexpr int kTaylorBlock = 256;
 
 // ---- Chebyshev engine (cheb.cu, chebcoef.cu) ---------------------------------

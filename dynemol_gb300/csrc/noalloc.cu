@@ -11,10 +11,16 @@
 // file-scope device array of fixed size, so the call allocates nothing.  The
 // caller passes device pointers for H' and Psi and a stream.
 //
-// The array is module-scope device memory: every GPU that loads this library
-// holds it (about 0.9 MB) until the process exits.  All calls on a device
-// share it and it keeps the contents of the last call; the barrier counters
-// and the error flag are cleared at the start of every call.  Calls whose work
+// The array belongs to this file's device module (about 0.9 MB).  With CUDA's
+// lazy module loading (the default since CUDA 12.2) the driver places it in
+// device memory when the module is first loaded on a device: by gpu_init_ /
+// the library's context set-up (which call fixed_scratch_prepare), or
+// else by the first call of this entry point on that device.  From then on the
+// device holds it until the process exits.  A caller whose pool allocator
+// takes the device memory should therefore call gpu_init_ (or this entry point
+// once) first, and before any stream capture.  All calls on a device share the
+// array and it keeps the contents of the last call; the barrier counters and
+// the error flag are cleared at the start of every call.  Calls whose work
 // overlaps on the GPU (for example on two streams) race on the array.
 #include <mutex>
 
@@ -123,14 +129,28 @@ extern "C" int elhl_propagate_fixed_scratch(int n, const double *d_H, int ld, el
     L.bar_gen = fs->bar + 1;
     L.error = &fs->err;
     FX_TRY(launch_taylor(L, grid, kTaylorBlock, st));
-    FX_TRY(cudaMemcpyAsync(d_psi_bra, bra0, vb, cudaMemcpyDeviceToDevice, st));
-    FX_TRY(cudaMemcpyAsync(d_psi_ket, ket0, vb, cudaMemcpyDeviceToDevice, st));
+    // Status first: the caller's Psi is overwritten only by a converged step,
+    // so a call that fails (timeout, no convergence) can be retried.
     TaylorParticle res{};
     int err = 0;
     FX_TRY(cudaMemcpyAsync(&res, fs->part, sizeof(TaylorParticle), cudaMemcpyDeviceToHost, st));
     FX_TRY(cudaMemcpyAsync(&err, &fs->err, sizeof(int), cudaMemcpyDeviceToHost, st));
     FX_TRY(cudaStreamSynchronize(st));
     if (err) return err;
+    if (res.status) return res.status;
+    FX_TRY(cudaMemcpyAsync(d_psi_bra, bra0, vb, cudaMemcpyDeviceToDevice, st));
+    FX_TRY(cudaMemcpyAsync(d_psi_ket, ket0, vb, cudaMemcpyDeviceToDevice, st));
+    FX_TRY(cudaStreamSynchronize(st));
     if (save_tau) *save_tau = res.save_tau;
-    return res.status;
+    return ELHL_OK;
 }
+
+// Loads this module on the current device and resolves the array's address,
+// so that the array is resident before a caller's pool allocator or stream
+// capture starts.  Called from the library's context set-up (gpu_init_).
+namespace elhl {
+int fixed_scratch_prepare() {
+    FixedScratch *fs = nullptr;
+    return fixed_scratch(&fs);
+}
+}  // namespace elhl

@@ -330,16 +330,22 @@ long long elhl_kernel_launches(void);
  * while a CUDA graph capture is in progress elsewhere, or code that must not
  * risk the device synchronisation cudaMalloc/cudaFree can trigger.  It calls
  * no cudaMalloc, cudaFree or allocating library routine: all scratch lives in
- * a fixed device array inside the library (about 0.9 MB, held by every GPU that
- * loads the library until the process exits).
+ * a fixed device array inside the library (about 0.9 MB).
  *   d_H         device, n x n column-major H', leading dimension ld >= n
- *   d_psi_bra/d_psi_ket  device, length n, propagated in place
+ *   d_psi_bra/d_psi_ket  device, length n, propagated in place; left
+ *               unchanged when the call returns an error status
  *   save_tau    host, receives the tau accepted by the first convergence
  *   stream      cudaStream_t as void* (NULL = legacy default stream)
  * Limit: n <= 4096 (larger n returns ELHL_ERR_BAD_ARG).  The call is
- * synchronous.  The first call on a device looks up the array's device address
- * (cudaGetSymbolAddress) and should come before any stream capture.  All calls
- * share the array; calls that overlap on the GPU race.
+ * synchronous.  The array is device memory of the library's module: with
+ * CUDA's lazy module loading the driver allocates it when that module is
+ * first loaded on a device -- by gpu_init_ (and any other call that sets up
+ * the library's context), or else by the first call of this function on that
+ * device, which also looks up the array's address (cudaGetSymbolAddress) --
+ * and the device holds it until the process exits.  Call gpu_init_ (or this
+ * function once) before a pool allocator takes the device memory and before
+ * any stream capture.  All calls share the array; calls that overlap on the
+ * GPU race.
  */
 int elhl_propagate_fixed_scratch(int n, const double *d_H, int ld, elhl_zcomplex *d_psi_bra,
                                  elhl_zcomplex *d_psi_ket, double t_init, double t_max, double tau,

@@ -4,9 +4,11 @@ It is meant for callers that cannot allocate device memory (a pool allocator
 owns the device, a graph capture is in progress elsewhere, or allocation's
 implicit synchronisation is not acceptable).  The test calls it through the C
 ABI on device buffers and checks it against the existing
-propagation_gpucaller_ entry point on the same inputs, for two calls in a row
-(the second continues from the first, so it also sees the array's leftover
-contents from the first call).  This file sorts last so that a stop-at-first-
+propagation_gpucaller_ entry point on the same inputs, for three calls in a
+row.  Each continues from the last, so it also sees the array's leftover
+contents from the previous call.  The second call runs on a non-default
+stream, and the third checks that the device's free memory does not change.
+This file sorts last so that a stop-at-first-
 failure run has already run every other test."""
 import numpy as np
 import pytest
@@ -31,12 +33,22 @@ def test_fixed_scratch_matches_gpucaller(elhl, oracle_mod, flake):
     d_b = torch.from_numpy(ref_b.view(np.float64).copy()).to(dev)
     d_k = torch.from_numpy(ref_k.view(np.float64).copy()).to(dev)
     tau_max = 1e-4 / oracle_mod.H_BAR
+    side = torch.cuda.Stream(dev)
     t = 0.0
-    for call in range(2):
+    for call in range(3):
         t_max = t + 1e-4
         ref_b, ref_k, ref_st = elhl.propagation_gpucaller(Hp, ref_b, ref_k, t, t_max, tau_max)
+        # call 1 runs on a stream of its own; calls 0 and 2 on torch's current stream
+        stream = side if call == 1 else torch.cuda.current_stream(dev)
+        stream.wait_stream(torch.cuda.current_stream(dev))
+        torch.cuda.synchronize(dev)
+        free_before = torch.cuda.mem_get_info(dev)[0]
         st = elhl.propagate_fixed_scratch(N, d_H.data_ptr(), ld, d_b.data_ptr(), d_k.data_ptr(), t, t_max, tau_max,
-                                          torch.cuda.current_stream(dev).cuda_stream)
+                                          stream.cuda_stream)
+        free_after = torch.cuda.mem_get_info(dev)[0]
+        if call == 2:
+            # the module and its array are resident after the first calls: no device memory is taken
+            assert free_after == free_before
         got_b = d_b.cpu().numpy().view(np.complex128)
         got_k = d_k.cpu().numpy().view(np.complex128)
         assert st == pytest.approx(ref_st, rel=1e-12)
