@@ -496,6 +496,169 @@ def run_mix(args, ntraj, steps, warm, precision, dropin_sample):
     return res
 
 
+def serve_all(sv_factory, mix, steps, submit_at=None):
+    """Submit every system of `mix` (fragment LUMO/HOMO pair, `steps` steps) to a
+    fresh server and step it until all are done.  submit_at: per-request arrival
+    offsets in seconds (None: all at t = 0).  Returns (wall s, populations
+    [request][P][nfrag+1], latencies s, statuses)."""
+    from dynemol_gb300 import systems
+    sv = sv_factory()
+    n = len(mix)
+    order = list(range(n)) if submit_at is None else sorted(range(n), key=lambda i: submit_at[i])
+    ids, pops, lat, status = {}, [None] * n, [0.0] * n, [0] * n
+    t0 = time.perf_counter()
+    nxt, done = 0, 0
+    while done < n:
+        now = time.perf_counter() - t0
+        while nxt < n and (submit_at is None or submit_at[order[nxt]] <= now):
+            i = order[nxt]
+            sysm = mix[i]
+            homo = systems.fermi_state(sysm, sysm.fragment_atoms("E"))
+            ids[sv.submit(sysm, steps if np.isscalar(steps) else steps[i], [homo + 1, homo])] = i
+            nxt += 1
+        active, pending = sv.step()
+        for rid in sv.poll():
+            i = ids.pop(rid)
+            try:
+                p, _, times = sv.result(rid)
+                pops[i] = p
+                lat[i] = times[2] - times[0]
+            except Exception as e:  # a failed request keeps its status; the caller reports it
+                status[i] = getattr(e, "status", -1)
+            done += 1
+        if active == 0 and pending == 0 and nxt < n and submit_at is not None:
+            time.sleep(max(0.0, submit_at[order[nxt]] - (time.perf_counter() - t0)))
+    wall = time.perf_counter() - t0
+    sv.close()
+    return wall, pops, np.array(lat), status
+
+
+def run_served_mix(args, ntraj=512, steps=200, sample=32):
+    """The batching workload through the continuous-batching server: every
+    trajectory of the uneven mix (N uniform in [200, 3000], dt 0.1 fs, electron
+    and hole) submitted at t = 0, served in FP32 and, on the same path, in FP64
+    (the reference for the population error of every member).  The plain FP64
+    drop-in (propagationelhl_gpucaller_ with host S, h, H', Psi buffers, one
+    particle per call, the reference's Taylor semantics) and the solo FP64
+    Chebyshev trajectory are timed on a stratified sample of the mix (every
+    (ntraj/sample)-th member by N), whose mean cost per trajectory-step stands
+    for the mix's.  The speed-up splits into method (Taylor drop-in -> solo
+    Chebyshev), batching (solo -> served, FP64) and precision (FP64 -> FP32)."""
+    import torch
+    from dynemol_gb300 import api, systems
+    mix = trajectory_mix(ntraj)
+    dt = 1e-4
+    res = {"ntraj": ntraj, "steps": steps, "dt_ps": dt, "N_range": [min(s.nao for s in mix), max(s.nao for s in mix)],
+           "N_mean": float(np.mean([s.nao for s in mix])), "hbm_budget_GB": 150.0,
+           "arrivals": "all requests submitted at t = 0"}
+    out = {}
+    for name, prec in (("fp32", api.PREC_FP32), ("fp64", api.PREC_FP64)):
+        wall, pops, lat, status = serve_all(lambda: api.Server(150e9, dt=dt, precision=prec, cheb_tol=1e-12),
+                                            mix, steps)
+        out[name] = (wall, pops, lat, status)
+        res[f"served_{name}"] = {"trajectory_steps_per_s": ntraj * steps / wall, "wall_s": wall,
+                                 "latency_p50_s": float(np.percentile(lat, 50)),
+                                 "latency_p99_s": float(np.percentile(lat, 99)),
+                                 "failed": int(sum(1 for x in status if x))}
+    ok = [i for i in range(ntraj) if not out["fp32"][3][i] and not out["fp64"][3][i]]
+    err = [float(np.abs(out["fp32"][1][i] - out["fp64"][1][i]).max()) for i in ok]
+    res["pop_err_vs_fp64"] = {"max": max(err), "members_compared": len(ok),
+                              "note": "every member's final populations (fragments and totals), FP32 served vs "
+                                      "FP64 served"}
+    # stratified sample by N: drop-in (host buffers) and solo Chebyshev FP64 (device resident)
+    by_n = sorted(range(ntraj), key=lambda i: mix[i].nao)
+    stride = max(1, ntraj // sample)
+    picks = [by_n[stride // 2 + k * stride] for k in range(min(sample, ntraj // stride))]
+    t_drop = t_solo = 0.0
+    nstep_s = 2
+    for i in picks:
+        sysm = mix[i]
+        homo = systems.fermi_state(sysm, sysm.fragment_atoms("E"))
+        tr = api.Trajectory(sysm, dt=dt)  # host S and h for the drop-in calls
+        tr.init_fmo(homo + 1, homo)
+        S, h, _ = tr.matrices()
+        bra, ket = tr.get_psi()
+        tr.close()
+        bra = [np.ascontiguousarray(bra[:, p]) for p in range(2)]
+        ket = [np.ascontiguousarray(ket[:, p]) for p in range(2)]
+        save = [dt / H_BAR, dt / H_BAR]
+        for s in range(1 + nstep_s):  # one untimed step, then nstep_s timed ones; el and hl one call each
+            t0 = time.perf_counter()
+            for p in range(2):
+                tau = dt / H_BAR if s == 0 else min(1.15 * save[p], dt / H_BAR)
+                *_, save[p] = api.propagationelhl_gpucaller(S, h, bra[p], ket[p], s * dt, (s + 1) * dt, tau)
+            if s:
+                t_drop += time.perf_counter() - t0
+        tr = api.Trajectory(sysm, dt=dt, method=api.METHOD_CHEBYSHEV, precision=api.PREC_FP64, ncols=2,
+                            cheb_tol=1e-12)
+        tr.init_fmo(homo + 1, homo)
+        tr.step(None, nsteps=1, want_pops=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tr.step(None, nsteps=nstep_s, want_pops=True)
+        t_solo += time.perf_counter() - t0
+        tr.close()
+    n_s = len(picks) * nstep_s
+    r_drop, r_solo = n_s / t_drop, n_s / t_solo
+    r64, r32 = res["served_fp64"]["trajectory_steps_per_s"], res["served_fp32"]["trajectory_steps_per_s"]
+    res["dropin_fp64"] = {"trajectory_steps_per_s": r_drop,
+                          "sample": f"{len(picks)} members, every {stride}th by N (N {mix[picks[0]].nao}-"
+                                    f"{mix[picks[-1]].nao}), {nstep_s} timed steps each after one untimed; "
+                                    "two propagationelhl_gpucaller_ calls (electron, hole) per step, host buffers"}
+    res["solo_chebyshev_fp64"] = {"trajectory_steps_per_s": r_solo, "sample": "the same members and steps"}
+    res["speedup_served_fp32_vs_dropin_fp64"] = r32 / r_drop
+    res["speedup_factors"] = {"method": r_solo / r_drop, "batching": r64 / r_solo, "precision": r32 / r64}
+    return res
+
+
+def run_config5(args, nreq=12, rate=200.0, nmax=16384, precision=None):
+    """Bounded sample of the serving workload at its stated ranges: Poisson
+    arrivals (200 / s), N log-uniform in [256, 16384], 50-5,000 steps, 2-32
+    even complex columns, 150 GB budget; fewer requests than a long stream."""
+    from dynemol_gb300 import api, systems
+    precision = api.PREC_FP32 if precision is None else precision
+    rng = systems.SplitMix64(5)
+    mix, steps, cols, arrive = [], [], [], []
+    t = 0.0
+    for i in range(nreq):
+        u = ((rng.next_u64() >> 11) + 0.5) / 9007199254740992.0
+        t += -np.log(u) / rate
+        u = ((rng.next_u64() >> 11) + 0.5) / 9007199254740992.0
+        N = 256.0 * (nmax / 256.0) ** u
+        mix.append(systems.cubic_cluster(n_atoms=max(8, int(round(N / 3.1))), seed=500 + i))
+        steps.append(int(50 + rng.next_u64() % 4951))
+        cols.append(2 * (1 + int(rng.next_u64() % 16)))
+        arrive.append(t)
+    sv = api.Server(150e9, dt=1e-4, precision=precision, cheb_tol=1e-12)
+    t0 = time.perf_counter()
+    ids, lat, done, nxt = {}, [], 0, 0
+    while done < nreq:
+        now = time.perf_counter() - t0
+        while nxt < nreq and arrive[nxt] <= now:
+            sysm = mix[nxt]
+            homo = systems.fermi_state(sysm, sysm.fragment_atoms("E"))
+            nf = int(sum(sysm.atom_nao[a] for a in sysm.fragment_atoms("E")))
+            states = [int(1 + (homo - cols[nxt] // 2 + c) % nf) for c in range(cols[nxt])]
+            ids[sv.submit(sysm, steps[nxt], states)] = nxt
+            nxt += 1
+        active, pending = sv.step()
+        for rid in sv.poll():
+            ids.pop(rid)
+            _, _, times = sv.result(rid)
+            lat.append(times[2] - times[0])
+            done += 1
+        if active == 0 and pending == 0 and nxt < nreq:
+            time.sleep(max(0.0, arrive[nxt] - (time.perf_counter() - t0)))
+    wall = time.perf_counter() - t0
+    sv.close()
+    lat = np.array(lat)
+    col_steps = sum(s * c for s, c in zip(steps, cols))
+    return {"requests": nreq, "arrival_rate_per_s": rate, "N": sorted(s.nao for s in mix), "steps": steps,
+            "columns": cols, "hbm_budget_GB": 150.0, "precision": "fp32", "wall_s": wall,
+            "request_steps_per_s": sum(steps) / wall, "column_steps_per_s": col_steps / wall,
+            "latency_p50_s": float(np.percentile(lat, 50)), "latency_p99_s": float(np.percentile(lat, 99))}
+
+
 def run_precision_study(args, steps=5, ncols=64, nao=8192):
     """Config 3: C/H honeycomb sheet with N = 8192 AOs, 64 complex columns
     (seeded random fragment MOs), fixed nuclei, dt 0.1 fs.  FP32 runs H.Psi as
@@ -587,8 +750,11 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--method", default="chebyshev", choices=["taylor", "chebyshev"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "bf16x3", "df64"])
-    ap.add_argument("--mix", type=int, default=64, help="also run the batched-vs-drop-in comparison on a mix "
+    ap.add_argument("--mix", type=int, default=0, help="also run the batched-vs-drop-in comparison on a mix "
                     "of this many trajectories (0 = skip)")
+    ap.add_argument("--served-mix", type=int, default=512, help="trajectories of the served mix (0 = skip)")
+    ap.add_argument("--served-steps", type=int, default=200, help="steps of each served-mix trajectory")
+    ap.add_argument("--config5", type=int, default=12, help="requests of the bounded serving sample (0 = skip)")
     ap.add_argument("--no-dropin", action="store_true", help="skip the Taylor drop-in measurement")
     ap.add_argument("--serve", type=int, default=0, help="also run a serving stream of this many requests")
     ap.add_argument("--precision-study", action="store_true", help="also run the N = 8192, 64-column study")
@@ -616,6 +782,10 @@ def main():
         from dynemol_gb300 import api
         line["trajectory_mix"] = run_mix(args, args.mix, steps=5, warm=2, precision=api.PREC_FP32,
                                          dropin_sample=4)
+    if rank == 0 and args.served_mix:
+        line["served_mix"] = run_served_mix(args, args.served_mix, args.served_steps)
+    if rank == 0 and args.config5:
+        line["serving_config5"] = run_config5(args, args.config5)
     if rank == 0 and args.precision_study:
         line["precision_study"] = run_precision_study(args)
     if rank == 0 and args.serve:

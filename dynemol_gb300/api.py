@@ -57,7 +57,8 @@ class TrajConfig(ctypes.Structure):
     _fields_ = [("method", ctypes.c_int), ("precision", ctypes.c_int), ("dt", ctypes.c_double),
                 ("frame_step", ctypes.c_int), ("tol", ctypes.c_double), ("norm_tol", ctypes.c_double),
                 ("cheb_tol", ctypes.c_double), ("cutoff", ctypes.c_double), ("max_conv_calls", ctypes.c_int),
-                ("ncols", ctypes.c_int), ("nparticles", ctypes.c_int)]
+                ("ncols", ctypes.c_int), ("nparticles", ctypes.c_int), ("cheb_norm_tol", ctypes.c_double),
+                ("cheb_max_retries", ctypes.c_int), ("lanczos_guard", ctypes.c_double)]
 
 
 class TrajStats(ctypes.Structure):
@@ -66,7 +67,7 @@ class TrajStats(ctypes.Structure):
                 ("status", ctypes.c_int), ("prop_ms", ctypes.c_double), ("rebuild_ms", ctypes.c_double),
                 ("prop_launches", ctypes.c_int), ("rebuild_count", ctypes.c_int), ("tile_cols", ctypes.c_int),
                 ("phases", ctypes.c_int), ("sh_ms", ctypes.c_double), ("factor_ms", ctypes.c_double),
-                ("inverse_ms", ctypes.c_double)]
+                ("inverse_ms", ctypes.c_double), ("cheb_retries", ctypes.c_int), ("norm_drift", ctypes.c_double)]
 
 
 class Request(ctypes.Structure):

@@ -571,6 +571,9 @@ struct ChebState {
     void *A = nullptr, *B = nullptr;   // L^-1, L^T in the launch precision (fixed nuclei read-out)
     bool readout_ready = false, cols_current = false;
     double *scale = nullptr;   // [P] pending renormalisation factor (reduced precision), 1 otherwise
+    double *drift = nullptr;   // norm drift word of the GEMM-regime step (plans keep their own)
+    double2 *saved = nullptr;  // [ld][m] input columns at the start of a call, for redone steps
+    double guard = 0.01;       // Lanczos interval guard, fraction of the width
     // read-out outputs, owned by the trajectory
     int P = 0, nfrag = 0;
     double2 *psi_out = nullptr, *bra_out = nullptr;
@@ -627,6 +630,8 @@ struct ChebState {
         CU_TRY(cudaMemset(acc, 0, (size_t)ld * m * sizeof(double2)));
         if (int rc = dev_alloc(&lz, (size_t)4 * ld + 128)) return rc;  // 4 vectors + the tridiagonal record
         if (int rc = dev_alloc(&scale, (size_t)kMaxCols)) return rc;
+        if (int rc = dev_alloc(&drift, 1)) return rc;
+        CU_TRY(cudaMemset(drift, 0, sizeof(double)));
         std::vector<double> ones(kMaxCols, 1.0);
         CU_TRY(copy_h2d(scale, ones.data(), kMaxCols * sizeof(double)));
         return ELHL_OK;
@@ -656,6 +661,7 @@ struct ChebState {
         implicit = false;
         dev_free(gpops);
         dev_free(Ht); dev_free(phi); dev_free(acc); dev_free(coef); dev_free(lz); dev_free(scale);
+        dev_free(drift); dev_free(saved);
         if (Hs) cudaFree(Hs);
         if (vbuf) cudaFree(vbuf);
         if (A) cudaFree(A);
@@ -817,8 +823,8 @@ int lanczos_bounds(ChebState &cs, int ksteps, const double *h = nullptr) {
     const double rlo = bk * tridiagonal_last_component(alpha, beta, used, lo);
     const double rhi = bk * tridiagonal_last_component(alpha, beta, used, hi);
     const double width = hi - lo;
-    cs.emin = lo - rlo - 0.01 * width;
-    cs.emax = hi + rhi + 0.01 * width;
+    cs.emin = lo - rlo - cs.guard * width;
+    cs.emax = hi + rhi + cs.guard * width;
     if (!(cs.emax > cs.emin) || !std::isfinite(cs.emin) || !std::isfinite(cs.emax)) return ELHL_ERR_NO_CONVERGENCE;
     return ELHL_OK;
 }
@@ -1162,6 +1168,62 @@ int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, do
     return ELHL_OK;
 }
 
+// ---- norm control ------------------------------------------------------------
+// In the symmetrised basis the exact step exp(-i H~ dt / hbar) is unitary, so
+// each propagated column keeps its squared norm.  For column c: n_in = s^2
+// |col_in|^2 (s: the pending renormalisation factor applied to the input, 1
+// without) and n_out = |col_out|^2 before any renormalisation; the relative
+// drift |n_out / n_in - 1| is the counterpart of the Taylor path's test
+// |<bra|ket>| - norm_ref (Taylor.f:103-104).  One block of kDriftBlock threads
+// per column, fixed-order FP64 sums; the largest drift is kept in *drift by an
+// integer max on the bits of the non-negative double (exact, independent of
+// the order in which blocks finish).  A non-finite norm counts as 1e300.
+constexpr int kDriftBlock = 256;
+
+__device__ void drift_column(const double2 *__restrict__ in, const double2 *__restrict__ out, int n, int m, int c,
+                             double s2, double *drift) {
+    __shared__ double ra[kDriftBlock], rb[kDriftBlock];
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < n; i += kDriftBlock) {
+        const double2 x = in[(size_t)i * m + c], y = out[(size_t)i * m + c];
+        a += x.x * x.x + x.y * x.y;
+        b += y.x * y.x + y.y * y.y;
+    }
+    ra[threadIdx.x] = a;
+    rb[threadIdx.x] = b;
+    __syncthreads();
+    for (int o = kDriftBlock / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            ra[threadIdx.x] += ra[threadIdx.x + o];
+            rb[threadIdx.x] += rb[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double nin = ra[0] * s2, nout = rb[0];
+        double d = nin > 0.0 ? fabs(nout / nin - 1.0) : (nout > 0.0 ? 1.0e300 : 0.0);
+        if (!(d <= 1.0e300)) d = 1.0e300;
+        atomicMax(reinterpret_cast<unsigned long long *>(drift), (unsigned long long)__double_as_longlong(d));
+    }
+}
+
+// every problem of a plan after a propagation launch of this parity (block (q, c))
+__global__ void __launch_bounds__(kDriftBlock) norm_drift_kernel(const ChebProblem *probs, int parity) {
+    const ChebProblem &pb = probs[blockIdx.x];
+    const int c = blockIdx.y;
+    if (!pb.drift || c >= pb.m) return;
+    const double s = pb.scale ? pb.scale[c % pb.P] : 1.0;
+    drift_column(pb.col[parity], pb.col[parity ^ 1], pb.N, pb.m, c, s * s, pb.drift);
+}
+
+// one problem's columns (GEMM regime), block c
+__global__ void __launch_bounds__(kDriftBlock) norm_drift_cols_kernel(const double2 *in, const double2 *out, int n,
+                                                                      int m, int P, const double *scale, double *drift) {
+    const int c = blockIdx.x;
+    const double s = scale ? scale[c % P] : 1.0;
+    drift_column(in, out, n, m, c, s * s, drift);
+}
+
 // ---- GEMM regime kernels (complex columns [ld][m], element-wise) -------------
 __global__ void gemm_order0_kernel(const double2 *__restrict__ phi, const double *__restrict__ scale, int P, int n,
                                    int m, double2 c0, float2 *__restrict__ v0, double2 *__restrict__ acc) {
@@ -1262,6 +1324,8 @@ int cheb_gemm_enqueue(ChebState &cs, int parity) {
                                                 vb + (k % 3) * vs, out, cs.coef, k, nm);
         count_launch();
     }
+    norm_drift_cols_kernel<<<m, kDriftBlock, 0, st>>>(in, out, n, m, cs.P, renorm ? cs.scale : nullptr, cs.drift);
+    count_launch();
     to_float2_kernel<<<nb, tb, 0, st>>>(out, reinterpret_cast<float2 *>(cs.Vf), nm);
     count_launch();
     if (int rc = gemm_vt(g_ctx.blas_tc, cs.precision, 2 * m, n, cs.Vf, reinterpret_cast<const float *>(cs.A), cs.ld,
@@ -1321,6 +1385,7 @@ struct ChebPlan {
     ChebSegment *d_segs = nullptr;
     int *d_seg_begin = nullptr, *d_prob_seg0 = nullptr;
     double *d_seg_pops = nullptr;
+    double *d_drift = nullptr;  // [problem] norm drift of the steps since the last reset
     int grid = 0, max_ld = 0, kmax = 0, mg = 0, mg_read = 0, precision = 0, parity = 0;
     int nphase = 1;            // 3: one implicit problem
     int mgcd = 0;              // gcd of the problems' column counts
@@ -1328,6 +1393,7 @@ struct ChebPlan {
     size_t pops_per_step = 0;  // populations of all problems in one step
     void release() {
         dev_free(d_probs); dev_free(d_segs); dev_free(d_seg_begin); dev_free(d_prob_seg0); dev_free(d_seg_pops);
+        dev_free(d_drift);
     }
 };
 
@@ -1339,6 +1405,8 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
     pl.segs.clear();
     if (states.empty()) return ELHL_ERR_BAD_ARG;
     if (cheb_grid_size(&pl.grid)) return ELHL_ERR_CUDA;
+    if (int rc = dev_alloc(&pl.d_drift, states.size())) return rc;
+    CU_TRY(cudaMemsetAsync(pl.d_drift, 0, states.size() * sizeof(double), g_ctx.stream));
     pl.max_ld = 0;
     pl.kmax = 0;
     pl.precision = states[0]->precision;
@@ -1386,6 +1454,7 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
             p.wb = cs->wb;
             p.shift = cs->a / cs->b;
         }
+        p.drift = pl.d_drift + pl.probs.size();
         pl.pops_per_step += (size_t)cs->P * (cs->nfrag + 1);
         pl.probs.push_back(p);
         pl.kmax = std::max(pl.kmax, cs->K);
@@ -1558,10 +1627,27 @@ int cheb_run(ChebPlan &pl) {
     return ELHL_OK;
 }
 
-// One fixed-nuclei step with the device read-out: propagation launch, read-out
-// launch (+ population reduction), then the columns swap roles.  No host sync.
+int launch_norm_drift(const ChebPlan &pl) {
+    int mmax = 0;
+    for (const auto &p : pl.probs) mmax = std::max(mmax, p.m);
+    norm_drift_kernel<<<dim3((unsigned)pl.probs.size(), mmax), kDriftBlock, 0, g_ctx.stream>>>(pl.d_probs, pl.parity);
+    count_launch();
+    CU_TRY(cudaGetLastError());
+    return ELHL_OK;
+}
+
+// drift tolerance of a configuration: <= 0 selects the precision's default
+double cheb_norm_tolerance(const elhl_traj_config &c) {
+    if (c.cheb_norm_tol > 0.0) return c.cheb_norm_tol;
+    return reduced_precision(c.precision) ? 1.0e-4 : 1.0e-8;
+}
+
+// One fixed-nuclei step with the device read-out: propagation launch, norm
+// drift of the step, read-out launch (+ population reduction), then the
+// columns swap roles.  No host sync.
 int cheb_dev_step(ChebPlan &pl, const std::vector<ChebState *> &states, double *d_pops_step) {
     if (int rc = cheb_run(pl)) return rc;
+    if (int rc = launch_norm_drift(pl)) return rc;
     ChebLaunch L{};
     L.probs = pl.d_probs;
     L.segs = pl.d_segs;
@@ -1971,6 +2057,70 @@ int cheb_readout(elhl_traj *tr, const double2 *cols, double *d_pops) {
     return ELHL_OK;
 }
 
+// ---- norm control of the trajectory's steps ----------------------------------
+// Widen the spectral interval by half its width (a quarter on each side) and
+// redo the scaled operator, the coefficients and the plan's order counts.
+int cheb_widen(elhl_traj *tr) {
+    ChebState &cs = tr->cs;
+    const double w = cs.emax - cs.emin;
+    cs.emin -= 0.25 * w;
+    cs.emax += 0.25 * w;
+    if (int rc = cheb_prepare(cs, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol, cs.implicit ? tr->h : nullptr))
+        return rc;
+    if (tr->plan.probs.empty()) return ELHL_OK;  // GEMM regime: no row-kernel plan
+    std::vector<ChebState *> one{&cs};
+    return cheb_plan_refresh(tr->plan, one);
+}
+
+// Input columns and pending renormalisation factors at the start of a
+// multi-step call (column roles: the caller keeps the parity), so that the
+// whole call can be redone.
+int cheb_save_state(ChebState &cs) {
+    cudaStream_t st = g_ctx.stream;
+    if (!cs.saved)
+        if (int rc = dev_alloc(&cs.saved, (size_t)cs.ld * cs.m + kMaxCols / 2)) return rc;
+    CU_TRY(cudaMemcpyAsync(cs.saved, cs.cin(), (size_t)cs.ld * cs.m * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    CU_TRY(cudaMemcpyAsync(cs.saved + (size_t)cs.ld * cs.m, cs.scale, kMaxCols * sizeof(double),
+                           cudaMemcpyDeviceToDevice, st));
+    return ELHL_OK;
+}
+
+int cheb_restore_state(elhl_traj *tr, int parity) {
+    cudaStream_t st = g_ctx.stream;
+    ChebState &cs = tr->cs;
+    cs.parity = parity;
+    tr->plan.parity = parity;
+    CU_TRY(cudaMemcpyAsync(cs.cin(), cs.saved, (size_t)cs.ld * cs.m * sizeof(double2), cudaMemcpyDeviceToDevice, st));
+    CU_TRY(cudaMemcpyAsync(cs.scale, cs.saved + (size_t)cs.ld * cs.m, kMaxCols * sizeof(double),
+                           cudaMemcpyDeviceToDevice, st));
+    return ELHL_OK;
+}
+
+// One propagation launch of the trajectory's plan with the norm check: redone
+// from its input columns (which the launch does not write) on a widened
+// interval while the drift exceeds the tolerance, at most cheb_max_retries
+// times.  Synchronises with the stream; *drift receives the accepted drift.
+int cheb_run_checked(elhl_traj *tr, double *drift) {
+    cudaStream_t st = g_ctx.stream;
+    const double ntol = cheb_norm_tolerance(tr->cfg);
+    for (int attempt = 0;; ++attempt) {
+        CU_TRY(cudaMemsetAsync(tr->plan.d_drift, 0, sizeof(double), st));
+        if (int rc = cheb_run(tr->plan)) return rc;
+        if (int rc = launch_norm_drift(tr->plan)) return rc;
+        int err = 0;
+        double d = 0.0;
+        CU_TRY(cudaMemcpyAsync(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaMemcpyAsync(&d, tr->plan.d_drift, sizeof(double), cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaStreamSynchronize(st));
+        if (err) return err;
+        *drift = d;
+        if (d <= ntol) return ELHL_OK;
+        if (attempt >= tr->cfg.cheb_max_retries) return ELHL_ERR_NO_CONVERGENCE;
+        if (int rc = cheb_widen(tr)) return rc;
+        tr->stats.cheb_retries += 1;
+    }
+}
+
 int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, int nsteps, double *d_pops) {
     cudaStream_t st = g_ctx.stream;
     ChebState &cs = tr->cs;
@@ -1991,26 +2141,44 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
         if ((rc = cheb_plan(tr->plan, one))) return rc;
     }
     if (!coords && cs.readout_ready && (tr->plan.mg_read || cs.gemm)) {
-        // ---- fixed nuclei, device read-out: two launches (or one graph) per step, no host sync
+        // ---- fixed nuclei, device read-out: two launches (or one graph) per step, no host sync;
+        // the norm drift of every step is kept on the device and read once at the end
         if (!cs.cols_current && (rc = cheb_load_columns(tr))) return rc;
-        CU_TRY(cudaEventRecord(g_ctx.ev[2], st));
-        for (int s = 0; s < nsteps; ++s) {
-            if (cs.gemm) {
-                if ((rc = cheb_gemm_step(cs))) return rc;
-                tr->plan.parity = cs.parity;
-                if (d_pops)
-                    CU_TRY(cudaMemcpyAsync(d_pops + s * pop_per_step, cs.gpops, pop_per_step * sizeof(double),
-                                           cudaMemcpyDeviceToDevice, st));
-                continue;
+        if ((rc = cheb_save_state(cs))) return rc;
+        const int parity0 = cs.parity;
+        const double ntol = cheb_norm_tolerance(tr->cfg);
+        double *d_drift = cs.gemm ? cs.drift : tr->plan.d_drift;
+        double drift = 0.0;
+        for (int attempt = 0;; ++attempt) {
+            CU_TRY(cudaMemsetAsync(d_drift, 0, sizeof(double), st));
+            CU_TRY(cudaEventRecord(g_ctx.ev[2], st));
+            for (int s = 0; s < nsteps; ++s) {
+                if (cs.gemm) {
+                    if ((rc = cheb_gemm_step(cs))) return rc;
+                    tr->plan.parity = cs.parity;
+                    if (d_pops)
+                        CU_TRY(cudaMemcpyAsync(d_pops + s * pop_per_step, cs.gpops, pop_per_step * sizeof(double),
+                                               cudaMemcpyDeviceToDevice, st));
+                    continue;
+                }
+                if ((rc = cheb_dev_step(tr->plan, one, d_pops ? d_pops + s * pop_per_step : nullptr))) return rc;
             }
-            if ((rc = cheb_dev_step(tr->plan, one, d_pops ? d_pops + s * pop_per_step : nullptr))) return rc;
+            CU_TRY(cudaEventRecord(g_ctx.ev[3], st));
+            if ((rc = cheb_settle(one))) return rc;
+            int err = 0;
+            CU_TRY(cudaMemcpyAsync(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CU_TRY(cudaMemcpyAsync(&drift, d_drift, sizeof(double), cudaMemcpyDeviceToHost, st));
+            CU_TRY(cudaStreamSynchronize(st));
+            if (err) return err;
+            if (drift <= ntol) break;
+            tr->stats.norm_drift = drift;
+            if (attempt >= tr->cfg.cheb_max_retries) return ELHL_ERR_NO_CONVERGENCE;
+            // redo the whole call from its saved input on a widened interval
+            if ((rc = cheb_restore_state(tr, parity0))) return rc;
+            if ((rc = cheb_widen(tr))) return rc;
+            tr->stats.cheb_retries += 1;
         }
-        CU_TRY(cudaEventRecord(g_ctx.ev[3], st));
-        if ((rc = cheb_settle(one))) return rc;
-        int err = 0;
-        CU_TRY(cudaMemcpyAsync(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost, st));
-        CU_TRY(cudaStreamSynchronize(st));
-        if (err) return err;
+        tr->stats.norm_drift = drift;
         tr->stats.prop_ms += event_ms(0, 1) * nsteps;  // last launch x launches
         tr->stats.rebuild_ms += 0.0;
         tr->stats.prop_launches += nsteps;
@@ -2051,7 +2219,9 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
             if (cudaEventRecord(g_ctx.ev[3], st) != cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
             if ((rc = cheb_plan_refresh(tr->plan, one))) break;
         }
-        if ((rc = cheb_run(tr->plan))) break;
+        double drift = 0.0;
+        if ((rc = cheb_run_checked(tr, &drift))) break;
+        tr->stats.norm_drift = std::max(tr->stats.norm_drift, drift);
         double2 *out = cs.parity ? cs.phi : cs.acc;
         double *pp = d_pops ? d_pops + s * pop_per_step : pops_tmp;
         if ((rc = cheb_readout(tr, out, pp))) break;
@@ -2063,11 +2233,7 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
         }
         tr->plan.parity ^= 1;
         cs.parity = tr->plan.parity;
-        int err = 0;
-        if (cudaMemcpyAsync(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-            cudaStreamSynchronize(st) != cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
-        if (err) { rc = err; break; }
-        tr->stats.prop_ms += event_ms(0, 1);
+        tr->stats.prop_ms += event_ms(0, 1);  // the events completed before the checked run returned
         tr->stats.prop_launches += 1;
         tr->stats.orders += (long long)cs.K * cs.m;
         if (coords) {
@@ -2435,6 +2601,9 @@ void elhl_traj_config_default(elhl_traj_config *c) {
     c->max_conv_calls = 2000;
     c->ncols = 2;
     c->nparticles = 2;
+    c->cheb_norm_tol = 0.0;  // by precision
+    c->cheb_max_retries = 3;
+    c->lanczos_guard = 0.01;
 }
 
 int elhl_ehrenfest_forces(const elhl_basis_desc *basis, const double *coords, const double *kernel, double delta,
@@ -2513,7 +2682,10 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
                          tr->cfg.nparticles >= 1 && tr->cfg.nparticles <= 64 &&
                          (tr->cfg.ncols == tr->cfg.nparticles || tr->cfg.ncols == 2 * tr->cfg.nparticles) &&
                          tr->cfg.cheb_tol > 0.0;
-    if (!((taylor_ok && taylor_p) || cheb_ok) || tr->cfg.dt <= 0 || tr->cfg.frame_step <= 0 || tr->cfg.max_conv_calls <= 0) {
+    const bool control_ok = tr->cfg.cheb_max_retries >= 0 && tr->cfg.lanczos_guard > -0.45 &&
+                            tr->cfg.lanczos_guard < 10.0 && !(tr->cfg.cheb_norm_tol < 0.0);
+    if (!((taylor_ok && taylor_p) || cheb_ok) || !control_ok || tr->cfg.dt <= 0 || tr->cfg.frame_step <= 0 ||
+        tr->cfg.max_conv_calls <= 0) {
         delete tr;
         return ELHL_ERR_UNSUPPORTED;
     }
@@ -2549,6 +2721,7 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
     if (!rc && !tr->cheb()) rc = tr->fac.check_info();  // the Chebyshev set-up factors S below
     if (!rc && tr->cheb()) {
         rc = tr->cs.alloc(tr->N, tr->cfg.ncols, tr->cfg.precision);
+        tr->cs.guard = tr->cfg.lanczos_guard;
         if (!rc) rc = dev_alloc(&tr->psi_ao, (size_t)tr->ld * tr->P);
         if (!rc) rc = dev_alloc(&tr->bra_ao, (size_t)tr->ld * tr->P);
         if (!rc) rc = dev_alloc(&tr->target, (size_t)tr->P);
@@ -2848,6 +3021,7 @@ int elhl_batch_step(elhl_batch *b, int nsteps, double *pops) {
         if (!tr->cs.cols_current)
             if (int rc = cheb_load_columns(tr)) return rc;
     (void)per_traj;
+    CU_TRY(cudaMemsetAsync(b->plan.d_drift, 0, nt * sizeof(double), st));
     for (int s = 0; s < nsteps; ++s) {
         if (int rc = cheb_dev_step(b->plan, b->states, b->pops + s * per_step)) return rc;
         for (auto *tr : b->members) {
@@ -2858,9 +3032,20 @@ int elhl_batch_step(elhl_batch *b, int nsteps, double *pops) {
     }
     if (int rc = cheb_settle(b->states)) return rc;
     int err = 0;
+    std::vector<double> drift(nt, 0.0);
     CU_TRY(cudaMemcpyAsync(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CU_TRY(cudaMemcpyAsync(drift.data(), b->plan.d_drift, nt * sizeof(double), cudaMemcpyDeviceToHost, st));
     CU_TRY(cudaStreamSynchronize(st));
     if (err) return err;
+    // norm control: a member whose step changed a column's norm beyond the
+    // tolerance fails the call (its stats carry the drift)
+    bool diverged = false;
+    for (int i = 0; i < nt; ++i) {
+        b->members[i]->stats.norm_drift = drift[i];
+        b->stats.norm_drift = std::max(b->stats.norm_drift, drift[i]);
+        diverged |= !(drift[i] <= cheb_norm_tolerance(b->members[i]->cfg));
+    }
+    if (diverged) return ELHL_ERR_NO_CONVERGENCE;
     b->stats.prop_ms += event_ms(0, 1) * nsteps;
     b->stats.prop_launches += nsteps;
     b->stats.tile_cols = b->plan.mg;
@@ -3045,6 +3230,7 @@ int elhl_server_step(elhl_server *sv, int *n_active, int *n_pending) {
         std::vector<ChebState *> states;
         for (auto *r : sv->active) states.push_back(&r->tr->cs);
         if (!sv->plan.mg_read) return ELHL_ERR_UNSUPPORTED;
+        CU_TRY(cudaMemsetAsync(sv->plan.d_drift, 0, sv->active.size() * sizeof(double), st));
         if (int rc = cheb_dev_step(sv->plan, states, sv->pops)) return rc;
         sv->parity = sv->plan.parity;
         std::vector<ChebState *> leaving;
@@ -3054,17 +3240,23 @@ int elhl_server_step(elhl_server *sv, int *n_active, int *n_pending) {
             if (int rc = cheb_settle(leaving)) return rc;
         size_t off = 0;
         int err = 0;
+        std::vector<double> drift(sv->active.size(), 0.0);
         CU_TRY(cudaMemcpyAsync(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CU_TRY(cudaMemcpyAsync(drift.data(), sv->plan.d_drift, drift.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                               st));
         CU_TRY(cudaStreamSynchronize(st));
         if (err) return err;
         sv->steps_done += (long long)sv->active.size();
-        // retire finished requests
+        // retire finished requests, and requests whose step failed the norm control
+        // (status ELHL_ERR_NO_CONVERGENCE, results as of that step)
         off = 0;
         std::vector<ServerRequest *> keep;
-        for (auto *r : sv->active) {
+        for (size_t q = 0; q < sv->active.size(); ++q) {
+            ServerRequest *r = sv->active[q];
             r->done_steps += 1;
             const size_t np = (size_t)r->P * (r->nfrag + 1);
-            if (r->done_steps >= r->nsteps) {
+            if (!(drift[q] <= cheb_norm_tolerance(r->tr->cfg))) r->status = ELHL_ERR_NO_CONVERGENCE;
+            if (r->done_steps >= r->nsteps || r->status) {
                 r->pops.resize(np);
                 CU_TRY(copy_d2h(r->pops.data(), sv->pops + off, np * sizeof(double)));
                 r->psi.resize((size_t)r->nao * r->P);

@@ -116,6 +116,7 @@ struct ChebProblem {
     const void *G, *Gt;
     void *wb;               // [2][m/MG][ldv][MG] launch precision: w = G^T v, y = (h/b) w
     double shift;           // a / b
+    double *drift;          // largest relative change of a column's squared norm over a step (norm control)
 };
 struct ChebSegment {
     int prob, row0, row1;   // rows [row0, row1) of problem `prob` owned by one CTA

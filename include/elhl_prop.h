@@ -155,6 +155,20 @@ typedef struct {
                             or 2 * nparticles (bra carried as the reference does) */
     int nparticles;      /* wavefunctions per trajectory: 2 (electron, hole) for the Taylor method;
                             1..64 for Chebyshev (ensembles) */
+    /* Chebyshev norm and convergence control, the counterpart of the Taylor
+     * path's per-sub-step test |<bra|ket>| - norm_ref (Taylor.f:103-114): the
+     * exact step is unitary in the symmetrised basis, so after every step each
+     * propagated column's squared norm is compared with its value before the
+     * step (before any reduced-precision renormalisation).  A relative change
+     * above cheb_norm_tol means the expansion did not converge (for example a
+     * spectral interval that misses part of the spectrum): the step is redone
+     * from its saved input on an interval widened by half its width each time,
+     * at most cheb_max_retries times, and then the call returns
+     * ELHL_ERR_NO_CONVERGENCE (batch and server members: the member fails). */
+    double cheb_norm_tol;  /* <= 0: 1e-8 for FP64 / DF64 (the reference's norm_error), 1e-4 for FP32 / BF16X3 */
+    int cheb_max_retries;  /* redone steps per step (default 3) */
+    double lanczos_guard;  /* spectral interval = Lanczos extremes + residual bounds, widened on each side by
+                              this fraction of the width (default 0.01) */
 } elhl_traj_config;
 
 typedef struct elhl_traj elhl_traj;
@@ -260,6 +274,9 @@ typedef struct {
     double sh_ms;         /* moving nuclei: device time of the S, h build */
     double factor_ms;     /* ... of the Cholesky factorisation of S */
     double inverse_ms;    /* ... of G = L^-1 (implicit operator) */
+    int cheb_retries;     /* Chebyshev steps redone on a widened spectral interval */
+    double norm_drift;    /* Chebyshev: largest relative change of a column's squared norm in one step
+                             (before renormalisation), over the call's accepted steps */
 } elhl_traj_stats;
 int elhl_traj_get_stats(elhl_traj *tr, elhl_traj_stats *st);
 
