@@ -33,7 +33,7 @@ EXPORTED_SYMBOLS = (
     "propagationelhl_gpucaller_", "elhl_last_status", "elhl_status_string", "elhl_traj_config_default",
     "elhl_traj_create", "elhl_traj_destroy", "elhl_traj_init_fmo", "elhl_traj_init_fmo_states", "elhl_traj_set_psi", "elhl_traj_get_psi", "elhl_traj_step",
     "elhl_traj_step_device", "elhl_traj_energies", "elhl_traj_get_matrices", "elhl_traj_get_factor", "elhl_traj_get_stats", "elhl_device_count",
-    "elhl_sm_count", "elhl_set_stream", "elhl_kernel_launches", "elhl_propagate_fixed_scratch", "elhl_bessel_j",
+    "elhl_sm_count", "elhl_set_stream", "elhl_debug_barrier", "elhl_kernel_launches", "elhl_propagate_fixed_scratch", "elhl_bessel_j",
     "elhl_chebyshev_coefficients", "elhl_batch_create", "elhl_batch_size", "elhl_batch_member",
     "elhl_batch_compact", "elhl_batch_step", "elhl_batch_get_stats", "elhl_batch_destroy",
     "elhl_server_create", "elhl_server_submit", "elhl_server_step", "elhl_server_poll", "elhl_server_result",
@@ -128,6 +128,7 @@ def load(path: str = LIB_PATH):
     L.elhl_device_count.restype = ci
     L.elhl_sm_count.restype = ci
     L.elhl_set_stream.argtypes = [vp]
+    L.elhl_debug_barrier.argtypes = [ctypes.c_double, ci]
     L.elhl_kernel_launches.argtypes = []
     L.elhl_kernel_launches.restype = ctypes.c_longlong
     L.elhl_propagate_fixed_scratch.argtypes = [ci, vp, ci, vp, vp, ctypes.c_double, ctypes.c_double,
@@ -427,6 +428,12 @@ def kernel_launches() -> int:
 def set_stream(stream_handle: int | None):
     """Route library work to a caller stream (integer cudaStream_t) or back to its own (None)."""
     _check(load().elhl_set_stream(ctypes.c_void_p(stream_handle) if stream_handle else None), "elhl_set_stream")
+
+
+def debug_barrier(limit_s: float = 0.0, exit_cta: int = -1):
+    """Failure-detection test hook: grid-barrier limit (s, <= 0: default) and a
+    CTA of the next propagation launch that leaves before its first barrier."""
+    _check(load().elhl_debug_barrier(float(limit_s), int(exit_cta)), "elhl_debug_barrier")
 
 
 class Batch:

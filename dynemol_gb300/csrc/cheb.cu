@@ -312,6 +312,8 @@ __global__ void __launch_bounds__(kBlock, 1) cheb_kernel(ChebLaunch L) {
     T2 *s_v = reinterpret_cast<T2 *>(smem_raw + kCheb_part_bytes);
     const int G = gridDim.x;
     const int s0 = L.seg_begin[blockIdx.x], s1 = L.seg_begin[blockIdx.x + 1];
+    const unsigned long long bar_ns = L.barrier_ns ? L.barrier_ns : kBarrierNs;
+    if ((int)blockIdx.x + 1 == L.exit_cta1) return;  // test hook: the other CTAs' barrier waits run out
     for (int k = 0; k <= L.kmax; ++k) {
         const int nph = k == 0 ? 1 : L.nphase;
         for (int ph = 0; ph < nph; ++ph) {
@@ -338,7 +340,7 @@ __global__ void __launch_bounds__(kBlock, 1) cheb_kernel(ChebLaunch L) {
                     }
                 }
             }
-            if (!grid_barrier(L.bar_count, L.bar_gen, G, L.error)) return;
+            if (!grid_barrier(L.bar_count, L.bar_gen, G, L.error, bar_ns)) return;
         }
     }
 }
@@ -674,6 +676,8 @@ __global__ void __launch_bounds__(kBlock, 1) cheb_df_kernel(ChebLaunch L) {
     const int G = gridDim.x;
     const int s0 = L.seg_begin[blockIdx.x], s1 = L.seg_begin[blockIdx.x + 1];
     const ChebProblem &pb = L.probs[0];
+    const unsigned long long bar_ns = L.barrier_ns ? L.barrier_ns : kBarrierNs;
+    if ((int)blockIdx.x + 1 == L.exit_cta1) return;  // test hook: the other CTAs' barrier waits run out
     for (int k = 0; k <= L.kmax; ++k) {
         const int nph = k == 0 ? 1 : 3;
         for (int ph = 0; ph < nph; ++ph) {
@@ -684,7 +688,7 @@ __global__ void __launch_bounds__(kBlock, 1) cheb_df_kernel(ChebLaunch L) {
                 for (int g = 0; g < pb.m / MG; ++g)
                     implicit_phase_df<MG>(L, pb, s0, s1, k, ph, g, s_v, s_part, cre, cim);
             }
-            if (!grid_barrier(L.bar_count, L.bar_gen, G, L.error)) return;
+            if (!grid_barrier(L.bar_count, L.bar_gen, G, L.error, bar_ns)) return;
         }
     }
 }

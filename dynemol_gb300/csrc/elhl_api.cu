@@ -3,10 +3,10 @@
 //
 // Per nuclear step (ElHl_Chebyshev, ElHl_Chebyshev.f:148-291) everything stays
 // on the device: S and h from coordinates (build_sh.cu), the Cholesky factor
-// S = L L^T and H' = S^-1 h by two triangular solves (cuSOLVER potrf/potrs,
-// replacing the reference's LU inverse + dsymm, Taylor_gpu.cpp:686-697), the
-// propagation (taylor.cu) and the populations.  Host traffic per step is the
-// coordinates in and the populations out.
+// S = L L^T with its inverse G = L^-1 and H' = S^-1 h = G^T (G h) (factor.cu,
+// dgemm.cu; replacing the reference's LU inverse + dsymm, Taylor_gpu.cpp:686-697),
+// the propagation (taylor.cu, cheb.cu) and the populations.  Host traffic per
+// step is the coordinates in and the populations out.
 #include <cublas_v2.h>
 #include <cusolverDn.h>
 
@@ -211,62 +211,124 @@ __global__ void zero_strided(double2 *v, int n, int stride) {
     if (i < n) v[(size_t)i * stride] = make_double2(0.0, 0.0);
 }
 
-// ---- H' = S^-1 h via Cholesky ------------------------------------------------
+// ---- S = L L^T and G = L^-1 in FP64 (hand-written) ------------------------------
+// zero the strictly upper triangle and the padding rows of an ld x n matrix
+__global__ void lower_only_kernel(double *A, int n, int ld) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i < ld && j < n && (i < j || i >= n)) A[(size_t)j * ld + i] = 0.0;
+}
+
+// Cholesky factor and its inverse together, in place, FP64 on the FP64 pipe:
+//   L11, G11 = chol_inv(A11);   L21 = A21 G11^T;   A22 -= L21 L21^T;
+//   L22, G22 = chol_inv(A22);   G21 = -G22 (L21 G11),
+// N^3/3 + N^3/3 flops in dgemm64 products (triangular operands at half cost),
+// 64-row diagonal blocks as leaves (leaf_chol_inv64), splits on multiples of 64.
+// It replaces the reference's LU inverse of S (MAGMA dgetrf + dgetri,
+// GPU_Interface.cpp:910-928; CPU dsytrf + dsytri, :936-947): S is symmetric
+// positive definite, so its Cholesky factor gives S^-1 = G^T G.  W holds the
+// n2 x n1 off-diagonal block of each split (leading dimension ld).  The upper
+// triangles of A and G are left undefined.
+bool chol_inv_fits(int n, int ld, size_t wcap) {
+    const int leaf = leaf_rows();
+    if (n <= leaf) return true;
+    const int n1 = round_up(n / 2, leaf), n2 = n - n1;
+    return (size_t)ld * n1 <= wcap && chol_inv_fits(n1, ld, wcap) && chol_inv_fits(n2, ld, wcap);
+}
+
+int chol_inv64(double *A, double *G, int n, int ld, int row0, double *W, int *info) {
+    cudaStream_t st = g_ctx.stream;
+    const int leaf = leaf_rows();
+    if (n <= leaf) {
+        CU_TRY(leaf_chol_inv64(A, G, n, ld, row0, info, st));
+        return ELHL_OK;
+    }
+    const int n1 = round_up(n / 2, leaf), n2 = n - n1;
+    double *A21 = A + n1, *A22 = A + (size_t)n1 * ld + n1;
+    double *G21 = G + n1, *G22 = G + (size_t)n1 * ld + n1;
+    if (int rc = chol_inv64(A, G, n1, ld, row0, W, info)) return rc;
+    CU_TRY(cudaMemcpy2DAsync(W, ld * sizeof(double), A21, ld * sizeof(double), n2 * sizeof(double), n1,
+                             cudaMemcpyDeviceToDevice, st));
+    CU_TRY(dgemm64(n2, n1, n1, 1.0, W, ld, false, G, ld, true, 0.0, A21, ld, st, kTriBt));       // L21
+    CU_TRY(dgemm64(n2, n2, n1, -1.0, A21, ld, false, A21, ld, true, 1.0, A22, ld, st, kTriLowerC));  // Schur
+    if (int rc = chol_inv64(A22, G22, n2, ld, row0 + n1, W, info)) return rc;
+    CU_TRY(dgemm64(n2, n1, n1, 1.0, A21, ld, false, G, ld, false, 0.0, W, ld, st, kTriB));      // L21 G11
+    CU_TRY(dgemm64(n2, n1, n2, -1.0, G22, ld, false, W, ld, false, 0.0, G21, ld, st, kTriA));   // G21
+    return ELHL_OK;
+}
+
+// ---- H' = S^-1 h = G^T (G h) ---------------------------------------------------
 struct Factor {
-    int N = 0, ld = 0, lwork = 0;
-    double *L = nullptr;     // Cholesky factor (lower), N x N, ld
-    double *work = nullptr;
-    int *info = nullptr;
-    double *cols = nullptr;  // N x 2 scratch (S^-1 applied to a complex vector)
+    int N = 0, ld = 0;
+    double *L = nullptr;     // Cholesky factor (lower, zero above the diagonal), N x N, ld
+    double *G = nullptr;     // G = L^-1 (lower, zero above the diagonal), unless factor() put it elsewhere
+    double *W = nullptr;     // ld x N workspace: the factorisation's off-diagonal blocks, then G h
+    int *info = nullptr;     // [2]: first non-positive pivot (1-based global column), 0 = positive definite
+    double *cols = nullptr;  // 2 x (N x 2) scratch (S^-1 applied to a complex vector)
     int reserve(int N_, int ld_) {
         if (N_ <= N && ld_ == ld && L) return ELHL_OK;
         release();
         N = N_;
         ld = ld_;
         if (int rc = dev_alloc(&L, (size_t)ld * N)) return rc;
-        if (cusolverDnDpotrf_bufferSize(g_ctx.solver, CUBLAS_FILL_MODE_LOWER, N, L, ld, &lwork) !=
-            CUSOLVER_STATUS_SUCCESS)
-            return ELHL_ERR_CUDA;
-        if (int rc = dev_alloc(&work, (size_t)lwork + 1)) return rc;
+        if (int rc = dev_alloc(&G, (size_t)ld * N)) return rc;
+        if (int rc = dev_alloc(&W, (size_t)ld * N)) return rc;
         if (int rc = dev_alloc(&info, 2)) return rc;
         CU_TRY(cudaMemset(info, 0, 2 * sizeof(int)));
-        if (int rc = dev_alloc(&cols, (size_t)2 * ld)) return rc;
+        if (int rc = dev_alloc(&cols, (size_t)4 * ld)) return rc;
         return ELHL_OK;
     }
     void release() {
-        dev_free(L); dev_free(work); dev_free(info); dev_free(cols);
+        dev_free(L); dev_free(G); dev_free(W); dev_free(info); dev_free(cols);
         N = 0;
     }
-    // L <- chol(S); Hp <- S^-1 h.  Asynchronous on the context stream.
-    int form_hprime(const double *S, const double *h, double *Hp, int n) {
+    // L <- chol(S) and Gdst (this->G when null) <- L^-1, both with zero upper
+    // triangles and padding rows.  Every block of the recursion is checked
+    // against the workspace before the first launch.  Asynchronous.
+    int factor(const double *S, int n, double *Gdst = nullptr) {
         cudaStream_t st = g_ctx.stream;
+        double *g = Gdst ? Gdst : G;
+        if (!chol_inv_fits(n, ld, (size_t)ld * N)) return ELHL_ERR_OOM;
+        CU_TRY(cudaMemsetAsync(info, 0, 2 * sizeof(int), st));
         CU_TRY(cudaMemcpy2DAsync(L, ld * sizeof(double), S, ld * sizeof(double), n * sizeof(double), n,
                                  cudaMemcpyDeviceToDevice, st));
-        SOLVER_TRY(cusolverDnDpotrf(g_ctx.solver, CUBLAS_FILL_MODE_LOWER, n, L, ld, work, lwork, info));
-        CU_TRY(cudaMemcpy2DAsync(Hp, ld * sizeof(double), h, ld * sizeof(double), n * sizeof(double), n,
-                                 cudaMemcpyDeviceToDevice, st));
-        SOLVER_TRY(cusolverDnDpotrs(g_ctx.solver, CUBLAS_FILL_MODE_LOWER, n, n, L, ld, Hp, ld, info + 1));
+        if (int rc = chol_inv64(L, g, n, ld, 0, W, info)) return rc;
+        const dim3 grid((ld + 127) / 128, n);
+        lower_only_kernel<<<grid, 128, 0, st>>>(L, n, ld);
+        count_launch();
+        lower_only_kernel<<<grid, 128, 0, st>>>(g, n, ld);
+        count_launch();
+        CU_TRY(cudaGetLastError());
         return ELHL_OK;
     }
-    // out = S^-1 z for a complex vector z (device), using the factor.
+    // L, G from S; Hp <- G^T (G h) = S^-1 h, 2 N^3 flops with triangular G.  Asynchronous.
+    int form_hprime(const double *S, const double *h, double *Hp, int n) {
+        cudaStream_t st = g_ctx.stream;
+        if (int rc = factor(S, n)) return rc;
+        CU_TRY(dgemm64(n, n, n, 1.0, G, ld, false, h, ld, false, 0.0, W, ld, st, kTriA));    // G h
+        CU_TRY(dgemm64(n, n, n, 1.0, G, ld, true, W, ld, false, 0.0, Hp, ld, st, kTriAt));   // G^T (G h)
+        return ELHL_OK;
+    }
+    // out = S^-1 z = G^T (G z) for a complex vector z (device), using the factor.
     int apply_sinv(const double2 *z, double2 *out, int n) {
         cudaStream_t st = g_ctx.stream;
         const int tb = 256, nb = (n + tb - 1) / tb;
+        double *c2 = cols + 2 * ld;
         split_complex<<<nb, tb, 0, st>>>(z, cols, n, ld);
         count_launch();
-        SOLVER_TRY(cusolverDnDpotrs(g_ctx.solver, CUBLAS_FILL_MODE_LOWER, n, 2, L, ld, cols, ld, info + 1));
+        CU_TRY(dgemm64(n, 2, n, 1.0, G, ld, false, cols, ld, false, 0.0, c2, ld, st, kTriA));
+        CU_TRY(dgemm64(n, 2, n, 1.0, G, ld, true, c2, ld, false, 0.0, cols, ld, st, kTriAt));
         join_complex<<<nb, tb, 0, st>>>(cols, out, n, ld);
         count_launch();
         CU_TRY(cudaGetLastError());
         return ELHL_OK;
     }
-    // status words of the last potrf (info[0]) and, with solves, potrs (info[1])
-    int check_info(bool with_solve = true) {  // waits for the factorisation on the library stream
+    // status of the last factorisation; waits for it on the library stream
+    int check_info(bool = true) {
         int h[2] = {0, 0};
         CU_TRY(cudaMemcpyAsync(h, info, 2 * sizeof(int), cudaMemcpyDeviceToHost, g_ctx.stream));
         CU_TRY(cudaStreamSynchronize(g_ctx.stream));
         if (h[0] > 0) return ELHL_ERR_NOT_POSITIVE_DEFINITE;
-        if (h[0] < 0 || (with_solve && h[1] != 0)) return ELHL_ERR_BAD_ARG;
+        if (h[0] < 0) return ELHL_ERR_BAD_ARG;
         return ELHL_OK;
     }
 };
@@ -481,14 +543,6 @@ int dropin_single(int n, double tau, double *save_tau, double t_init, double t_m
 // ---- Chebyshev state of one problem ------------------------------------------
 // H~ = L^-1 h L^-T (FP64), its scaled copy Hs = (H~ - a)/b in the launch
 // precision, the expansion coefficients and the column buffers.
-__global__ void symmetrize_kernel(double *A, int n, int ld) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-    if (i >= n || j >= n || i <= j) return;
-    const double v = 0.5 * (A[(size_t)j * ld + i] + A[(size_t)i * ld + j]);
-    A[(size_t)j * ld + i] = v;
-    A[(size_t)i * ld + j] = v;
-}
-
 template <typename T>
 __global__ void scale_kernel(const double *__restrict__ Ht, T *__restrict__ Hs, int n, int ld, double a, double binv) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
@@ -606,8 +660,6 @@ struct ChebState {
     bool implicit = false;
     void *Gt = nullptr;
     void *wb = nullptr;      // [2][ld][m] launch precision (phase intermediates)
-    double *fws = nullptr;   // workspace of the recursive factorisations
-    size_t fws_n = 0;
     // FP64 L^T and G^T for the column transforms of the implicit operator: B and
     // Gt on the FP64 path, own copies in the other precisions
     double *Lt64 = nullptr, *Gt64 = nullptr;
@@ -629,6 +681,7 @@ struct ChebState {
         CU_TRY(cudaMemset(phi, 0, (size_t)ld * m * sizeof(double2)));
         CU_TRY(cudaMemset(acc, 0, (size_t)ld * m * sizeof(double2)));
         if (int rc = dev_alloc(&lz, (size_t)4 * ld + 128)) return rc;  // 4 vectors + the tridiagonal record
+        if (int rc = dev_alloc(&cscratch, (size_t)2 * m * ld)) return rc;
         if (int rc = dev_alloc(&scale, (size_t)kMaxCols)) return rc;
         if (int rc = dev_alloc(&drift, 1)) return rc;
         CU_TRY(cudaMemset(drift, 0, sizeof(double)));
@@ -653,8 +706,6 @@ struct ChebState {
         if (Gt) cudaFree(Gt);
         if (wb) cudaFree(wb);
         Gt = wb = nullptr;
-        dev_free(fws);
-        fws_n = 0;
         dev_free(Lt64);
         dev_free(Gt64);
         dev_free(cscratch);
@@ -672,18 +723,20 @@ struct ChebState {
     }
 };
 
-// H~ = L^-1 h L^-T from the Cholesky factor (lower) and h, then symmetrised.
-int form_htilde(ChebState &cs, const double *Lfac, const double *h, int ld) {
+// A(j, i) = A(i, j) for i > j: the upper triangle from the lower one
+__global__ void mirror_lower_kernel(double *A, int n, int ld) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+    if (i < n && j < n && i > j) A[(size_t)i * ld + j] = A[(size_t)j * ld + i];
+}
+
+// H~ = G h G^T with G = L^-1 (lower, zero upper triangle): W = G h, then the
+// lower triangle of W G^T (symmetric result, N^3 + N^3/2 flops), mirrored.
+int form_htilde(ChebState &cs, const double *G, const double *h, int ld, double *W) {
     cudaStream_t st = g_ctx.stream;
     const int n = cs.N;
-    const double one = 1.0;
-    CU_TRY(cudaMemcpy2DAsync(cs.Ht, cs.ld * sizeof(double), h, ld * sizeof(double), n * sizeof(double), n,
-                             cudaMemcpyDeviceToDevice, st));
-    BLAS_TRY(cublasDtrsm(g_ctx.blas, CUBLAS_SIDE_LEFT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, n,
-                         n, &one, Lfac, ld, cs.Ht, cs.ld));
-    BLAS_TRY(cublasDtrsm(g_ctx.blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, CUBLAS_DIAG_NON_UNIT, n,
-                         n, &one, Lfac, ld, cs.Ht, cs.ld));
-    symmetrize_kernel<<<dim3((n + 127) / 128, n), 128, 0, st>>>(cs.Ht, n, cs.ld);
+    CU_TRY(dgemm64(n, n, n, 1.0, G, ld, false, h, ld, false, 0.0, W, ld, st, kTriA));
+    CU_TRY(dgemm64(n, n, n, 1.0, W, ld, false, G, ld, true, 0.0, cs.Ht, cs.ld, st, kTriBt | kTriLowerC));
+    mirror_lower_kernel<<<dim3((n + 127) / 128, n), 128, 0, st>>>(cs.Ht, n, cs.ld);
     count_launch();
     CU_TRY(cudaGetLastError());
     return ELHL_OK;
@@ -877,7 +930,7 @@ int cheb_prepare(ChebState &cs, double dt, double tol, const double *h = nullptr
 }
 
 // dst(i, j) = src(j, i) if transpose else src(i, j), in T, keeping only the
-// lower triangle of src (potrf leaves the other triangle untouched); rows >= n are zero
+// lower triangle of src (the factorisations leave the other triangle undefined); rows >= n are zero
 template <typename T>
 __global__ void convert_kernel(const double *__restrict__ src, T *__restrict__ dst, int n, int ld, bool transpose) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
@@ -890,135 +943,6 @@ __global__ void convert_kernel(const double *__restrict__ src, T *__restrict__ d
     dst[(size_t)j * ld + i] = (T)v;
 }
 
-// zero the strictly upper triangle and the padding rows of an ld x n matrix
-__global__ void lower_only_kernel(double *A, int n, int ld) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-    if (i < ld && j < n && (i < j || i >= n)) A[(size_t)j * ld + i] = 0.0;
-}
-
-// ---- inverse of the Cholesky factor --------------------------------------------
-constexpr int kTriBlock = 512;   // diagonal blocks finished by the batched bottom-up levels
-constexpr int kTrmmLeaf = 256;   // triangular products of at most this order run as one full DGEMM
-
-// Workspace of the recursive factorisations: ld x (ld / 2 + kTriBlock) doubles.
-// The widest block it holds is the off-diagonal block of the top split,
-// n2 x n1 with n1 = round_up(n / 2, kTriBlock) <= n / 2 + kTriBlock - 1 (the
-// Cholesky-with-inverse splits on multiples of 64); the batched levels need at
-// most n x kTriBlock / 4.
-int factor_workspace(ChebState &cs, double **W) {
-    const size_t need = (size_t)cs.ld * (cs.ld / 2 + kTriBlock);
-    if (cs.fws_n < need) {
-        dev_free(cs.fws);
-        cs.fws_n = 0;
-        if (int rc = dev_alloc(&cs.fws, need)) return rc;
-        cs.fws_n = need;
-    }
-    *W = cs.fws;
-    return ELHL_OK;
-}
-
-// Y (m x n, ldy) = alpha X T for the lower-triangular T (n x n, zero upper
-// triangle), out of place, recursively:
-//   [X1 X2] [T11 0; T21 T22] = [X1 T11 + X2 T21, X2 T22].
-// Blocks of order <= kTrmmLeaf are one DGEMM over the full square (twice the
-// triangular flops on under an eighth of the work; cuBLAS DTRMM at these
-// sizes runs on a few CTAs for 65 us a call).
-int trmm_right_oop(double alpha, const double *X, int ldx, const double *T, int ldt, double *Y, int ldy, int m, int n) {
-    const double zero = 0.0, one = 1.0;
-    if (n <= kTrmmLeaf) {
-        BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, m, n, n, &alpha, X, ldx, T, ldt, &zero, Y, ldy));
-        return ELHL_OK;
-    }
-    const int n1 = round_up(n / 2, 64), n2 = n - n1;
-    if (int rc = trmm_right_oop(alpha, X, ldx, T, ldt, Y, ldy, m, n1)) return rc;  // Y1 = X1 T11
-    BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, m, n1, n2, &alpha, X + (size_t)n1 * ldx, ldx, T + n1,
-                         ldt, &one, Y, ldy));                                     // Y1 += X2 T21
-    return trmm_right_oop(alpha, X + (size_t)n1 * ldx, ldx, T + (size_t)n1 * ldt + n1, ldt, Y + (size_t)n1 * ldy, ldy,
-                          m, n2);                                                  // Y2 = X2 T22
-}
-
-// Y (m x n, ldy) = alpha T X for the lower-triangular T (m x m), out of place:
-//   [T11 0; T21 T22] [X1; X2] = [T11 X1; T21 X1 + T22 X2].
-int trmm_left_oop(double alpha, const double *T, int ldt, const double *X, int ldx, double *Y, int ldy, int m, int n) {
-    const double zero = 0.0, one = 1.0;
-    if (m <= kTrmmLeaf) {
-        BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, m, n, m, &alpha, T, ldt, X, ldx, &zero, Y, ldy));
-        return ELHL_OK;
-    }
-    const int m1 = round_up(m / 2, 64), m2 = m - m1;
-    if (int rc = trmm_left_oop(alpha, T, ldt, X, ldx, Y, ldy, m1, n)) return rc;  // Y1 = T11 X1
-    if (int rc = trmm_left_oop(alpha, T + (size_t)m1 * ldt + m1, ldt, X + m1, ldx, Y + m1, ldy, m2, n)) return rc;
-    BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, m2, n, m1, &alpha, T + m1, ldt, X, ldx, &one, Y + m1,
-                         ldy));                                                    // Y2 += T21 X1
-    return ELHL_OK;
-}
-
-// Above kTriBlock rows: [L11 0; L21 L22]^-1 = [G11 0; -G22 L21 G11  G22], the
-// splits on multiples of kTriBlock so that the leaves are the blocks the
-// bottom-up levels finished.  wcap: elements of W; a block that would not fit
-// is refused before any launch.
-int tri_inverse_top(double *A, int n, int ld, double *W, size_t wcap) {
-    if (n <= kTriBlock) return ELHL_OK;
-    const int n1 = round_up(n / 2, kTriBlock), n2 = n - n1;
-    double *A11 = A, *A21 = A + n1, *A22 = A + (size_t)n1 * ld + n1;
-    if ((size_t)ld * n1 > wcap) return ELHL_ERR_OOM;  // W holds n2 x n1 at leading dimension ld
-    if (int rc = tri_inverse_top(A11, n1, ld, W, wcap)) return rc;
-    if (int rc = tri_inverse_top(A22, n2, ld, W, wcap)) return rc;
-    if (int rc = trmm_right_oop(1.0, A21, ld, A11, ld, W, ld, n2, n1)) return rc;  // W = L21 G11
-    return trmm_left_oop(-1.0, A22, ld, W, ld, A21, ld, n2, n1);                   // A21 = -G22 W
-}
-
-// G = L^-1 in place for the n x n lower-triangular A (zero upper triangle), FP64:
-//  1. every 64-row diagonal block by leaf_inverse, one launch;
-//  2. bottom-up, s = 64, 128 and 256: pairs of inverted s-blocks become
-//     inverted 2s-blocks, G21 = -G22 (L21 G11), as two strided-batched DGEMMs
-//     over all complete pairs and two plain ones for a short last pair (full
-//     products of triangular blocks; these levels hold about 4 % of the flops);
-//  3. top-down above 512 rows (tri_inverse_top), N^3/3 flops in large DGEMMs.
-// Block sizes measured at N = 3720: 256 / 512 for the leaf products / the
-// bottom-up blocks gave 23.7 ms, 256 / 256 24.2, 128 / 256 24.8, 512 / 256 25.7.
-int tri_inverse(ChebState &cs, double *A, int n, int ld) {
-    cudaStream_t st = g_ctx.stream;
-    double *W = nullptr;
-    if (int rc = factor_workspace(cs, &W)) return rc;
-    CU_TRY(leaf_inverse(A, n, ld, st));
-    const double one = 1.0, mone = -1.0, zero = 0.0;
-    for (int s = leaf_rows(); s < kTriBlock; s *= 2) {
-        const int np = n / (2 * s), rem = n - 2 * s * np;
-        const long long stride = (long long)2 * s * (ld + 1), ws = (long long)s * s;
-        if ((size_t)np * ws > cs.fws_n || (rem > s && (size_t)(rem - s) * s > cs.fws_n)) return ELHL_ERR_OOM;
-        if (np > 0) {
-            BLAS_TRY(cublasDgemmStridedBatched(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, s, s, s, &one, A + s, ld, stride,
-                                               A, ld, stride, &zero, W, s, ws, np));  // W_p = L21 G11
-            BLAS_TRY(cublasDgemmStridedBatched(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, s, s, s, &mone,
-                                               A + (size_t)s * (ld + 1), ld, stride, W, s, ws, &zero, A + s, ld,
-                                               stride, np));                           // G21 = -G22 W_p
-        }
-        if (rem > s) {  // short last pair: s rows over rem - s rows
-            const int n2 = rem - s;
-            double *P = A + (size_t)2 * s * np * (ld + 1);
-            BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n2, s, s, &one, P + s, ld, P, ld, &zero, W,
-                                 n2));
-            BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n2, s, n2, &mone, P + (size_t)s * (ld + 1), ld,
-                                 W, n2, &zero, P + s, ld));
-        }
-    }
-    return tri_inverse_top(A, n, ld, W, cs.fws_n);
-}
-
-// G = L^-1 (FP64, lower, zero upper triangle) from a copy of the Cholesky factor:
-// N^3/3 flops.
-int invert_factor(ChebState &cs, const double *Lfac, double *dst) {
-    cudaStream_t st = g_ctx.stream;
-    const int n = cs.N, ld = cs.ld;
-    CU_TRY(cudaMemcpy2DAsync(dst, ld * sizeof(double), Lfac, ld * sizeof(double), n * sizeof(double), n,
-                             cudaMemcpyDeviceToDevice, st));
-    lower_only_kernel<<<dim3((ld + 127) / 128, n), 128, 0, st>>>(dst, n, ld);  // potrf leaves S above the diagonal
-    count_launch();
-    CU_TRY(cudaGetLastError());
-    return tri_inverse(cs, dst, n, ld);
-}
-
 // Cholesky factor and its inverse together, in place, for the DF64 rebuild:
 // A (n x n, lower) <- L, G <- L^-1, all three matrices (and the workspace W)
 // held as DF64 pairs and every product in double-float arithmetic on the FP32
@@ -1027,7 +951,7 @@ int invert_factor(ChebState &cs, const double *Lfac, double *dst) {
 //   L22, G22 = chol_inv(A22);   G21 = -G22 (L21 G11),
 // N^3/3 + N^3/3 flops, with 64-row diagonal blocks as leaves (leaf_chol_inv_df).
 // The upper triangles of A and G are left undefined.
-int chol_inv_df(float2 *A, float2 *G, int n, int ld, int row0, float2 *W, size_t wcap, int *info) {
+int chol_inv_df(float2 *A, float2 *G, int n, int ld, int row0, float2 *W, int *info) {
     cudaStream_t st = g_ctx.stream;
     const int leaf = leaf_rows();
     if (n <= leaf) {
@@ -1035,30 +959,29 @@ int chol_inv_df(float2 *A, float2 *G, int n, int ld, int row0, float2 *W, size_t
         return ELHL_OK;
     }
     const int n1 = round_up(n / 2, leaf), n2 = n - n1;
-    if ((size_t)ld * n1 > wcap) return ELHL_ERR_OOM;  // W holds n2 x n1 at leading dimension ld
     float2 *A21 = A + n1, *A22 = A + (size_t)n1 * ld + n1;
     float2 *G21 = G + n1, *G22 = G + (size_t)n1 * ld + n1;
-    if (int rc = chol_inv_df(A, G, n1, ld, row0, W, wcap, info)) return rc;
+    if (int rc = chol_inv_df(A, G, n1, ld, row0, W, info)) return rc;
     CU_TRY(cudaMemcpy2DAsync(W, ld * sizeof(float2), A21, ld * sizeof(float2), n2 * sizeof(float2), n1,
                              cudaMemcpyDeviceToDevice, st));
     CU_TRY(dfgemm(n2, n1, n1, 1.0, W, ld, G, ld, 0.0, A21, ld, st, true, kTriBt));              // L21
     CU_TRY(dfgemm(n2, n2, n1, -1.0, A21, ld, A21, ld, 1.0, A22, ld, st, true, kTriLowerC));    // Schur
-    if (int rc = chol_inv_df(A22, G22, n2, ld, row0 + n1, W, wcap, info)) return rc;
+    if (int rc = chol_inv_df(A22, G22, n2, ld, row0 + n1, W, info)) return rc;
     CU_TRY(dfgemm(n2, n1, n1, 1.0, A21, ld, G, ld, 0.0, W, ld, st, false, kTriB));             // L21 G11
     CU_TRY(dfgemm(n2, n1, n2, -1.0, G22, ld, W, ld, 0.0, G21, ld, st, false, kTriA));          // G21
     return ELHL_OK;
 }
 
 // L = chol(S) in Lfac and G = L^-1 in G, both FP64 on return, by chol_inv_df
-// on DF64 pairs converted in place.
-int chol_inv_pairs(ChebState &cs, double *Lfac, double *G, int *info) {
+// on DF64 pairs converted in place; W: ld x N workspace (held as pairs).  The
+// blocks of the recursion are checked against W before the first launch.
+int chol_inv_pairs(ChebState &cs, double *Lfac, double *G, int *info, double *W) {
     cudaStream_t st = g_ctx.stream;
-    double *W = nullptr;
-    if (int rc = factor_workspace(cs, &W)) return rc;
+    if (!chol_inv_fits(cs.N, cs.ld, (size_t)cs.ld * cs.N)) return ELHL_ERR_OOM;
     CU_TRY(cudaMemsetAsync(info, 0, sizeof(int), st));
     CU_TRY(df_convert(Lfac, cs.N, cs.N, cs.ld, true, st));
     if (int rc = chol_inv_df(reinterpret_cast<float2 *>(Lfac), reinterpret_cast<float2 *>(G), cs.N, cs.ld, 0,
-                             reinterpret_cast<float2 *>(W), cs.fws_n, info))
+                             reinterpret_cast<float2 *>(W), info))
         return rc;
     CU_TRY(df_convert(Lfac, cs.N, cs.N, cs.ld, false, st));
     CU_TRY(df_convert(G, cs.N, cs.N, cs.ld, false, st));
@@ -1066,42 +989,36 @@ int chol_inv_pairs(ChebState &cs, double *Lfac, double *G, int *info) {
 }
 
 // A = L^-1 and B = L^T (launch precision) for the device read-out of fixed nuclei.
-int cheb_prepare_readout(ChebState &cs, const double *Lfac) {
+// L and G = L^-1 both FP64 with zero upper triangles.
+int cheb_prepare_readout(ChebState &cs, const double *Lfac, const double *G) {
     cudaStream_t st = g_ctx.stream;
     const int n = cs.N, ld = cs.ld;
     const size_t tsz = cs.precision == ELHL_PREC_FP64 ? sizeof(double) : sizeof(float);
     if (!cs.A) CU_TRY(cudaMalloc(&cs.A, (size_t)ld * n * tsz));
     if (!cs.B) CU_TRY(cudaMalloc(&cs.B, (size_t)ld * n * tsz));
-    double *tmp = nullptr;
-    if (int rc = dev_alloc(&tmp, (size_t)ld * n)) return rc;
     dim3 grid((ld + 127) / 128, n);
-    int rc = invert_factor(cs, Lfac, tmp);
-    if (!rc) {
-        if (cs.precision == ELHL_PREC_FP64) {
-            convert_kernel<double><<<grid, 128, 0, st>>>(tmp, (double *)cs.A, n, ld, false);
-            count_launch();
-            convert_kernel<double><<<grid, 128, 0, st>>>(Lfac, (double *)cs.B, n, ld, true);
-            count_launch();
-        } else {
-            convert_kernel<float><<<grid, 128, 0, st>>>(tmp, (float *)cs.A, n, ld, false);
-            count_launch();
-            convert_kernel<float><<<grid, 128, 0, st>>>(Lfac, (float *)cs.B, n, ld, true);
-            count_launch();
-        }
-        if (cudaGetLastError() != cudaSuccess) rc = ELHL_ERR_CUDA;
+    if (cs.precision == ELHL_PREC_FP64) {
+        convert_kernel<double><<<grid, 128, 0, st>>>(G, (double *)cs.A, n, ld, false);
+        count_launch();
+        convert_kernel<double><<<grid, 128, 0, st>>>(Lfac, (double *)cs.B, n, ld, true);
+        count_launch();
+    } else {
+        convert_kernel<float><<<grid, 128, 0, st>>>(G, (float *)cs.A, n, ld, false);
+        count_launch();
+        convert_kernel<float><<<grid, 128, 0, st>>>(Lfac, (float *)cs.B, n, ld, true);
+        count_launch();
     }
-    if (cudaStreamSynchronize(st) != cudaSuccess && !rc) rc = ELHL_ERR_CUDA;
-    dev_free(tmp);
-    if (!rc) cs.readout_ready = true;
-    return rc;
+    CU_TRY(cudaGetLastError());
+    CU_TRY(cudaStreamSynchronize(st));
+    cs.readout_ready = true;
+    return ELHL_OK;
 }
 
-// Implicit operator for the current factor and h: G = L^-1 (FP64, in cs.Ht;
-// already there when have_inverse), bounds by Lanczos on G h G^T, Hs = h/b,
-// and A = G, Gt = G^T, B = L^T in the launch precision.  N^3/3 flops for the
-// inverse instead of the 2 N^3 of forming H~.
-int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, double dt, double tol,
-                          bool have_inverse = false) {
+// Implicit operator for the current factor and h: G = L^-1 (FP64, in cs.Ht,
+// formed with L at N^3/3 flops instead of the 2 N^3 of forming H~), bounds by
+// Lanczos on G h G^T, Hs = h/b, and A = G, Gt = G^T, B = L^T in the launch
+// precision.
+int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, double dt, double tol) {
     cudaStream_t st = g_ctx.stream;
     const int n = cs.N, ld = cs.ld;
     const size_t tsz = wide_storage(cs.precision) ? sizeof(double) : sizeof(float);
@@ -1112,14 +1029,10 @@ int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, do
         CU_TRY(cudaMalloc(&cs.wb, (size_t)2 * ld * cs.m * 2 * tsz));
         CU_TRY(cudaMemset(cs.wb, 0, (size_t)2 * ld * cs.m * 2 * tsz));
     }
-    if (!cs.cscratch)
-        if (int rc = dev_alloc(&cs.cscratch, (size_t)2 * cs.m * ld)) return rc;
-    // L with a zero upper triangle (potrf leaves S there): the dense column transforms read all of it
+    // L with a zero upper triangle (the recursion leaves S's there): the dense column transforms read all of it
     lower_only_kernel<<<dim3((ld + 127) / 128, n), 128, 0, st>>>(const_cast<double *>(Lfac), n, ld);
     count_launch();
     CU_TRY(cudaGetLastError());
-    if (!have_inverse)
-        if (int rc = invert_factor(cs, Lfac, cs.Ht)) return rc;
     CU_TRY(cudaEventRecord(g_ctx.ev[6], st));
     lower_only_kernel<<<dim3((ld + 127) / 128, n), 128, 0, st>>>(cs.Ht, n, ld);
     count_launch();
@@ -1599,6 +1512,11 @@ int tune_plan(ChebPlan &pl, int mgcd) {
     return ELHL_OK;
 }
 
+// Failure-detection test hook (elhl_debug_barrier): the grid-barrier limit of
+// the propagation launches and a one-shot early exit of one CTA.
+unsigned long long g_dbg_barrier_ns = 0;
+int g_dbg_exit_cta1 = 0;
+
 int cheb_run(ChebPlan &pl) {
     cudaStream_t st = g_ctx.stream;
     if (!pl.tuned) {
@@ -1621,6 +1539,9 @@ int cheb_run(ChebPlan &pl) {
     L.parity = pl.parity;
     L.seg_pops = pl.d_seg_pops;
     L.nphase = pl.nphase;
+    L.barrier_ns = g_dbg_barrier_ns;
+    L.exit_cta1 = g_dbg_exit_cta1;
+    g_dbg_exit_cta1 = 0;  // one launch only
     CU_TRY(cudaEventRecord(g_ctx.ev[0], st));
     CU_TRY(launch_cheb(L, pl.precision, pl.mg, st));
     CU_TRY(cudaEventRecord(g_ctx.ev[1], st));
@@ -1706,22 +1627,6 @@ int cheb_settle(const std::vector<ChebState *> &states) {
 // column-major real matrix X; right-side triangular operations act on every
 // column at once:  X L  = (L^T x)^T,  X L^-1 = (L^-T x)^T,
 //                  X L^T = (L x)^T,   X L^-T = (L^-1 x)^T.
-int cols_apply(const double *Lfac, int ld, int n, double2 *cols, int m, int col0, int ncols, bool transpose,
-               bool inverse) {
-    const double one = 1.0;
-    double *X = reinterpret_cast<double *>(cols) + 2 * col0;
-    const int rows = 2 * ncols, ldx = 2 * m;
-    const cublasOperation_t op = transpose ? CUBLAS_OP_T : CUBLAS_OP_N;
-    if (inverse) {
-        BLAS_TRY(cublasDtrsm(g_ctx.blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, op, CUBLAS_DIAG_NON_UNIT, rows, n,
-                             &one, Lfac, ld, X, ldx));
-    } else {
-        BLAS_TRY(cublasDtrmm(g_ctx.blas, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_LOWER, op, CUBLAS_DIAG_NON_UNIT, rows, n,
-                             &one, Lfac, ld, X, ldx, X, ldx));
-    }
-    return ELHL_OK;
-}
-
 // Y (R x n) = X M for an R x n X (column k at X + k ldx) and a triangular FP64
 // M: Y(r, j) = sum_k X(r, k) M(k, j) over the non-zero part of column j of M
 // (k >= j for a lower M, k <= j for an upper one).  One warp per column j:
@@ -1765,7 +1670,6 @@ __global__ void cols_mt_kernel(const double *__restrict__ M, int ld, int n, cons
 int cols_apply_dense(const double *L, const double *G, int ld, int n, double2 *cols, int m, int col0, int ncols,
                      bool transpose, bool inverse, double *scratch, const double *Lt = nullptr,
                      const double *Gt = nullptr) {
-    const double one = 1.0, zero = 0.0;
     double *X = reinterpret_cast<double *>(cols) + 2 * col0;
     const int rows = 2 * ncols, ldx = 2 * m;
     const double *Mt = inverse ? Gt : Lt;
@@ -1781,8 +1685,8 @@ int cols_apply_dense(const double *L, const double *G, int ld, int n, double2 *c
         }
         CU_TRY(cudaGetLastError());
     } else {
-        BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, transpose ? CUBLAS_OP_T : CUBLAS_OP_N, rows, n, n, &one, X, ldx,
-                             inverse ? G : L, ld, &zero, scratch, rows));
+        CU_TRY(dgemm64(rows, n, n, 1.0, X, ldx, false, inverse ? G : L, ld, transpose, 0.0, scratch, rows, g_ctx.stream,
+                       transpose ? kTriBt : kTriB));
     }
     CU_TRY(cudaMemcpy2DAsync(X, ldx * sizeof(double), scratch, rows * sizeof(double), rows * sizeof(double), n,
                              cudaMemcpyDeviceToDevice, g_ctx.stream));
@@ -1790,7 +1694,7 @@ int cols_apply_dense(const double *L, const double *G, int ld, int n, double2 *c
 }
 
 // ---- Ehrenfest force kernel pieces ---------------------------------------------
-// K = X o A (Hadamard), then K -= H A by one DGEMM (alpha = -1, beta = 1):
+// K = X o A (Hadamard), then K -= H A by one FP64 product (dgemm64, beta = 1):
 // the K = X o A - H A of hadamard_minus (Chebyshev_gpu_kernels.cu:358-389) with
 // ehrenfestkernel_gpu_ (Taylor_gpu.cpp:743-791).
 __global__ void hadamard_kernel(const double *__restrict__ X, const double *__restrict__ A, double *__restrict__ K,
@@ -1853,9 +1757,7 @@ int ehrenfest_impl(int n, const double *hH, const double *hA, const elhl_zcomple
     hadamard_kernel<<<grid, 128, 0, st>>>(g_ehr.X, g_ehr.A, g_ehr.K, n, ld);
     count_launch();
     CU_TRY(cudaGetLastError());
-    const double m1 = -1.0, one = 1.0;
-    BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, n, n, n, &m1, g_ehr.H, ld, g_ehr.A, ld, &one, g_ehr.K,
-                         ld));
+    CU_TRY(dgemm64(n, n, n, -1.0, g_ehr.H, ld, false, g_ehr.A, ld, false, 1.0, g_ehr.K, ld, st));  // K -= H' A
     CU_TRY(cudaMemcpy2DAsync(hK, col, g_ehr.K, ldb, col, n, cudaMemcpyDeviceToHost, st));
     CU_TRY(cudaStreamSynchronize(st));
     return ELHL_OK;
@@ -1980,27 +1882,31 @@ int rebuild(elhl_traj *tr, const double *d_coords) {
 // changes every step, N^3/3 flops); bounds and coefficients.
 int cheb_rebuild_operator(elhl_traj *tr, bool implicit = false) {
     cudaStream_t st = g_ctx.stream;
-    CU_TRY(cudaMemcpy2DAsync(tr->fac.L, tr->ld * sizeof(double), tr->S, tr->ld * sizeof(double), tr->N * sizeof(double),
-                             tr->N, cudaMemcpyDeviceToDevice, st));
-    // factor and inverse in one double-float recursion (about 1e-14 relative): DF64, and the FP32 / BF16X3
-    // propagations, whose own rounding is near 1e-7; FP64 keeps cuSOLVER potrf and the FP64 inverse
-    const bool together = implicit && tr->cs.precision != ELHL_PREC_FP64;
-    if (together) {
-        if (int rc = chol_inv_pairs(tr->cs, tr->fac.L, tr->cs.Ht, tr->fac.info)) return rc;
-    } else {
-        SOLVER_TRY(cusolverDnDpotrf(g_ctx.solver, CUBLAS_FILL_MODE_LOWER, tr->N, tr->fac.L, tr->ld, tr->fac.work,
-                                    tr->fac.lwork, tr->fac.info));
+    ChebState &cs = tr->cs;
+    // S = L L^T and G = L^-1 in one recursion: FP64 for FP64 propagation and for every
+    // fixed-nuclei set-up; double-float pairs (about 1e-14 relative) for the moving-nuclei
+    // DF64, FP32 and BF16X3 propagations, whose own rounding is near 1e-14 or 1e-7.
+    // The implicit operator keeps G in cs.Ht, the explicit one in the factor's G.
+    const bool pairs = implicit && cs.precision != ELHL_PREC_FP64;
+    if (pairs) {
+        CU_TRY(cudaMemcpy2DAsync(tr->fac.L, tr->ld * sizeof(double), tr->S, tr->ld * sizeof(double),
+                                 tr->N * sizeof(double), tr->N, cudaMemcpyDeviceToDevice, st));
+        if (int rc = chol_inv_pairs(cs, tr->fac.L, cs.Ht, tr->fac.info, tr->fac.W)) return rc;
+    } else if (int rc = tr->fac.factor(tr->S, tr->N, implicit ? cs.Ht : nullptr)) {
+        return rc;
     }
     CU_TRY(cudaEventRecord(g_ctx.ev[5], st));
     if (int rc = tr->fac.check_info(false)) return rc;
-    if (implicit)
-        return cheb_prepare_implicit(tr->cs, tr->fac.L, tr->h, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol,
-                                     together);
-    tr->cs.implicit = false;
-    if (int rc = form_htilde(tr->cs, tr->fac.L, tr->h, tr->ld)) return rc;
-    if (int rc = lanczos_bounds(tr->cs, 40)) return rc;
-    return cheb_prepare(tr->cs, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol);
+    if (implicit) return cheb_prepare_implicit(cs, tr->fac.L, tr->h, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol);
+    cs.implicit = false;
+    if (int rc = form_htilde(cs, tr->fac.G, tr->h, tr->ld, tr->fac.W)) return rc;
+    if (int rc = lanczos_bounds(cs, 40)) return rc;
+    return cheb_prepare(cs, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol);
 }
+
+// G = L^-1 of the trajectory's current factor: in cs.Ht for the implicit
+// operator, in the factor's own buffer otherwise
+const double *traj_inverse(const elhl_traj *tr) { return tr->cs.implicit ? tr->cs.Ht : tr->fac.G; }
 
 // phi <- transformed columns of (psi_ao, bra_ao) with the current factor
 int cheb_load_columns(elhl_traj *tr) {
@@ -2022,9 +1928,12 @@ int cheb_load_columns(elhl_traj *tr) {
         cs.cols_current = true;
         return ELHL_OK;
     }
-    if (int rc = cols_apply(tr->fac.L, tr->ld, n, in, cs.m, 0, P, false, false)) return rc;       // L^T psi
+    const double *G = traj_inverse(tr);
+    if (int rc = cols_apply_dense(tr->fac.L, G, tr->ld, n, in, cs.m, 0, P, false, false, cs.cscratch))
+        return rc;  // L^T psi
     if (cs.m == 2 * P)
-        if (int rc = cols_apply(tr->fac.L, tr->ld, n, in, cs.m, P, P, true, true)) return rc;    // L^-1 bra
+        if (int rc = cols_apply_dense(tr->fac.L, G, tr->ld, n, in, cs.m, P, P, true, true, cs.cscratch))
+            return rc;  // L^-1 bra
     cs.cols_current = true;
     return ELHL_OK;
 }
@@ -2046,8 +1955,11 @@ int cheb_readout(elhl_traj *tr, const double2 *cols, double *d_pops) {
                                       cs.lt64(), cs.gt64()))
             return rc;  // L chi
     } else {
-        if (int rc = cols_apply(tr->fac.L, tr->ld, n, tr->psi_ao, P, 0, P, false, true)) return rc;   // L^-T phi
-        if (int rc = cols_apply(tr->fac.L, tr->ld, n, tr->bra_ao, P, 0, P, true, false)) return rc;   // L chi
+        const double *G = traj_inverse(tr);
+        if (int rc = cols_apply_dense(tr->fac.L, G, tr->ld, n, tr->psi_ao, P, 0, P, false, true, cs.cscratch))
+            return rc;  // L^-T phi
+        if (int rc = cols_apply_dense(tr->fac.L, G, tr->ld, n, tr->bra_ao, P, 0, P, true, false, cs.cscratch))
+            return rc;  // L chi
     }
     if (d_pops) {
         populations_kernel<<<P, 256, 0, st>>>(tr->psi_ao, tr->bra_ao, n, P, tr->basis.ao_frag, tr->nfrag, d_pops);
@@ -2132,12 +2044,12 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
     if (!coords && cs.implicit && cs.gemm) {
         // GEMM regime after moving steps: form H~ for the current geometry
         if ((rc = cheb_rebuild_operator(tr, false))) return rc;
-        if ((rc = cheb_prepare_readout(cs, tr->fac.L))) return rc;
+        if ((rc = cheb_prepare_readout(cs, tr->fac.L, traj_inverse(tr)))) return rc;
         if ((rc = cheb_plan(tr->plan, one))) return rc;
     }
     if (!coords && !cs.readout_ready && tr->fac.L && cs.precision != ELHL_PREC_DF64) {
         // fixed nuclei after moving steps: factor-based read-out matrices for the current L
-        if ((rc = cheb_prepare_readout(cs, tr->fac.L))) return rc;
+        if ((rc = cheb_prepare_readout(cs, tr->fac.L, traj_inverse(tr)))) return rc;
         if ((rc = cheb_plan(tr->plan, one))) return rc;
     }
     if (!coords && cs.readout_ready && (tr->plan.mg_read || cs.gemm)) {
@@ -2446,9 +2358,8 @@ int cheb_set_psi(elhl_traj *tr, const elhl_zcomplex *bra, const elhl_zcomplex *k
             CU_TRY(cudaMemcpy2D(tr->bra_ao + p, P * e, bra + (size_t)p * n, e, e, n, cudaMemcpyHostToDevice));
     } else {
         // bra = S ket: the complex columns as a 2P x N real matrix times S (symmetric)
-        const double one = 1.0, zero = 0.0;
-        BLAS_TRY(cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * P, n, n, &one, (const double *)tr->psi_ao, 2 * P,
-                             tr->S, tr->ld, &zero, (double *)tr->bra_ao, 2 * P));
+        CU_TRY(dgemm64(2 * P, n, n, 1.0, (const double *)tr->psi_ao, 2 * P, false, tr->S, tr->ld, false, 0.0,
+                       (double *)tr->bra_ao, 2 * P, g_ctx.stream));
     }
     return cheb_set_target(tr);
 }
@@ -2497,6 +2408,14 @@ int elhl_device_count(void) {
     int n = 0;
     if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
     return n;
+}
+
+int elhl_debug_barrier(double limit_s, int exit_cta) {
+    std::lock_guard<std::mutex> lk(g_ctx.mu);
+    if (limit_s > 10.0 || exit_cta < -1 || exit_cta >= 1 << 20) return ELHL_ERR_BAD_ARG;
+    g_dbg_barrier_ns = limit_s > 0.0 ? (unsigned long long)(limit_s * 1e9) : 0ULL;
+    g_dbg_exit_cta1 = exit_cta + 1;
+    return ELHL_OK;
 }
 
 int elhl_set_stream(void *stream) {
@@ -2732,7 +2651,7 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
         ChebState &cs = tr->cs;
         cs.P = tr->P; cs.nfrag = tr->nfrag; cs.psi_out = tr->psi_ao; cs.bra_out = tr->bra_ao;
         cs.ao_frag = tr->basis.ao_frag; cs.target = tr->target;
-        if (!rc && !df) rc = cheb_prepare_readout(cs, tr->fac.L);
+        if (!rc && !df) rc = cheb_prepare_readout(cs, tr->fac.L, traj_inverse(tr));
         // GEMM regime: many ket columns in FP32 / BF16X3 -> one GEMM per order
         if (!rc && reduced_precision(cs.precision) && cs.m == cs.P && cs.P >= kGemmMinCols && cs.N >= kGemmMinN) {
             cs.gemm = true;
@@ -2821,9 +2740,11 @@ int elhl_traj_energies(elhl_traj *tr, elhl_zcomplex *E) {
     cudaStream_t st = g_ctx.stream;
     const int P = tr->P, n = tr->N;
     double2 *ket = nullptr, *bra = nullptr, *hk = nullptr;  // [n][P] each
+    double *scr = nullptr;                                  // 2P x n transform output
     int rc = dev_alloc(&ket, (size_t)n * P);
     if (!rc) rc = dev_alloc(&bra, (size_t)n * P);
     if (!rc) rc = dev_alloc(&hk, (size_t)n * P);
+    if (!rc) rc = dev_alloc(&scr, (size_t)2 * n * P);
     const size_t e = sizeof(double2);
     for (int p = 0; p < P && !rc; ++p) {
         const double2 *k = tr->cheb() ? tr->psi_ao + p : tr->tb.ket(p);
@@ -2833,21 +2754,19 @@ int elhl_traj_energies(elhl_traj *tr, elhl_zcomplex *E) {
             cudaMemcpy2DAsync(bra + p, P * e, b, sp, e, n, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
             rc = ELHL_ERR_CUDA;
     }
-    // S^-1 bra = L^-T L^-1 bra: rows of the 2P x n real view times L^-T then L^-1
-    if (!rc) rc = cols_apply(tr->fac.L, tr->ld, n, bra, P, 0, P, true, true);
-    if (!rc) rc = cols_apply(tr->fac.L, tr->ld, n, bra, P, 0, P, false, true);
-    if (!rc) {
-        const double one = 1.0, zero = 0.0;
-        if (cublasDgemm(g_ctx.blas, CUBLAS_OP_N, CUBLAS_OP_N, 2 * P, n, n, &one, (const double *)ket, 2 * P, tr->h,
-                        tr->ld, &zero, (double *)hk, 2 * P) != CUBLAS_STATUS_SUCCESS)
-            rc = ELHL_ERR_CUDA;  // (h ket)^T = ket^T h, h symmetric
-    }
+    // S^-1 bra = G^T G bra: rows of the 2P x n real view times G^T, then times G
+    const double *G = tr->cheb() ? traj_inverse(tr) : tr->fac.G;
+    if (!rc) rc = cols_apply_dense(tr->fac.L, G, tr->ld, n, bra, P, 0, P, true, true, scr);
+    if (!rc) rc = cols_apply_dense(tr->fac.L, G, tr->ld, n, bra, P, 0, P, false, true, scr);
+    if (!rc && dgemm64(2 * P, n, n, 1.0, (const double *)ket, 2 * P, false, tr->h, tr->ld, false, 0.0, (double *)hk,
+                       2 * P, st) != cudaSuccess)
+        rc = ELHL_ERR_CUDA;  // (h ket)^T = ket^T h, h symmetric
     std::vector<double2> hb((size_t)n * P), hh((size_t)n * P);
     if (!rc && (cudaMemcpyAsync(hb.data(), bra, hb.size() * e, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
                 cudaMemcpyAsync(hh.data(), hk, hh.size() * e, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
                 cudaStreamSynchronize(st) != cudaSuccess))
         rc = ELHL_ERR_CUDA;
-    dev_free(ket); dev_free(bra); dev_free(hk);
+    dev_free(ket); dev_free(bra); dev_free(hk); dev_free(scr);
     if (rc) return rc;
     for (int p = 0; p < P; ++p) {
         double er = 0.0, ei = 0.0;

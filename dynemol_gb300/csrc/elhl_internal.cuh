@@ -132,6 +132,11 @@ struct ChebLaunch {
     double *seg_pops;       // [nseg][kMaxCols][kMaxFrag+1] read-out partials
     double *pops;           // this step's populations block, or nullptr
     int nphase;             // grid phases per order: 1 (explicit Hs) or 3 (one implicit problem)
+    // failure-detection test hook (elhl_debug_barrier): grid-barrier limit in ns
+    // (0: the default 5 s) and 1 + the CTA that leaves before its first grid
+    // barrier (0: none, so a zero-initialised launch has no hook)
+    unsigned long long barrier_ns;
+    int exit_cta1;
 };
 constexpr size_t kCheb_part_bytes = 16 * 64 * sizeof(double);  // cross-warp partial sums
 constexpr size_t kCheb_smem_limit = 200 * 1024;
@@ -159,23 +164,27 @@ int umma_bf16x3_gemm(const __nv_bfloat16 *const A[3], int lda, const __nv_bfloat
 // triangular operands (kTriA: A; kTriB: B; kTriBt: op(B) = B^T of a lower B)
 // and kTriLowerC a symmetric update that writes only the tiles on or below
 // the diagonal.
-constexpr int kTriA = 1, kTriB = 2, kTriBt = 4, kTriLowerC = 8;
+constexpr int kTriA = 1, kTriB = 2, kTriBt = 4, kTriLowerC = 8, kTriAt = 16;
 cudaError_t dfgemm(int m, int n, int k, double alpha, const float2 *A, int lda, const float2 *B, int ldb, double beta,
                    float2 *C, int ldc, cudaStream_t st, bool transB = false, int tri = 0);
+// C = alpha op(A) op(B) + beta C in FP64 on the FP64 pipe (dgemm.cu), op = the
+// transpose when transA / transB; `tri` as for dfgemm, plus kTriAt: op(A) = A^T
+// of a lower A.
+cudaError_t dgemm64(int m, int n, int k, double alpha, const double *A, int lda, bool transA, const double *B, int ldb,
+                    bool transB, double beta, double *C, int ldc, cudaStream_t st, int tri = 0);
 // rows x n block of an FP64 matrix (leading dimension ld) to DF64 pairs in
 // place (to_pairs) or back
 cudaError_t df_convert(double *x, int rows, int n, int ld, bool to_pairs, cudaStream_t st);
 
 // Diagonal-block leaves of the recursive factorisations (factor.cu), in
 // shared memory, blocks of leaf_rows() = 64 rows:
-//   leaf_inverse:     every diagonal block of the n x n lower-triangular A
-//                     replaced by its inverse, one CTA per block (FP64);
 //   leaf_chol_inv_df: A (nb x nb, nb <= 64, DF64 pairs) <- chol(A), G <- its
 //                     inverse; a non-positive pivot sets *info (if still 0)
-//                     to row0 + column + 1.
+//                     to row0 + column + 1;
+//   leaf_chol_inv64:  the same in FP64.
 int leaf_rows();
-cudaError_t leaf_inverse(double *A, int n, int ld, cudaStream_t st);
 cudaError_t leaf_chol_inv_df(float2 *A, float2 *G, int nb, int ld, int row0, int *info, cudaStream_t st);
+cudaError_t leaf_chol_inv64(double *A, double *G, int nb, int ld, int row0, int *info, cudaStream_t st);
 
 int bessel_j_sequence(double beta, int kmax, double *J);
 int chebyshev_coefficients(double dt, double emin, double emax, double tol, int kcap, std::vector<double> &cre,

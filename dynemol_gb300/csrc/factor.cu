@@ -1,22 +1,14 @@
-// Dense factorisations of the diagonal blocks of a lower-triangular matrix,
-// one CTA of 256 threads per block of at most kLeaf = 64 rows, entirely in
-// shared memory.  They are the leaves of the rebuild's recursive inverse of
-// the Cholesky factor and of the recursive Cholesky-with-inverse:
-//   leaf_inverse_kernel:      G_cc = L_cc^-1 for every diagonal block c at
-//                             once (FP64);
-//   leaf_chol_inv_df_kernel:  L = chol(A) and G = L^-1 for one diagonal block,
-//                             in DF64 pairs on the FP32 pipes (the DF64
-//                             rebuild), pivots' 1/sqrt included, blocked by 8.
-// Library triangular kernels at these sizes (cuSOLVER trtri on 256 rows,
-// cuBLAS DTRMM/DTRSM panels) run on a handful of CTAs for 65-106 us per call.
-//
-// The FP64 leaf is a column sweep, one barrier per column.  Row k of X holds
-// L(k, k) G(k, :) after step k and, for rows i > k,
-//   x_ij -= L(i, k) / L(k, k) * x_kj   for j <= k;
-// at the end G(i, j) = x_ij / L(i, i).  The FP64 pipe of one SM retires about
-// two FMAs per clock, so a warp instruction with idle lanes costs as much as a
-// full one: warp w takes rows i = w (mod 8) and its lanes the active columns.
-// The DF64 leaf is blocked to need few barriers (see its comment).
+// Dense Cholesky-with-inverse of one diagonal block of at most kLeaf = 64
+// rows, one CTA of 256 threads, entirely in shared memory: the leaves of the
+// rebuild's recursive factorisations (S = L L^T with G = L^-1).
+//   leaf_chol_inv_df_kernel:  in DF64 pairs on the FP32 pipes (the DF64,
+//                             FP32 and BF16X3 moving-nuclei rebuilds);
+//   leaf_chol_inv64_kernel:   in FP64 (the FP64 rebuild, every fixed-nuclei
+//                             set-up and the drop-in's H' = S^-1 h).
+// Both are blocked by 8 columns so that few steps wait at a block-wide
+// barrier; library triangular kernels at these sizes (cuSOLVER trtri on 256
+// rows, cuBLAS DTRMM/DTRSM panels) ran on a handful of CTAs for 65-106 us per
+// call.
 #include "df64.cuh"
 #include "elhl_internal.cuh"
 
@@ -24,83 +16,6 @@ namespace elhl {
 namespace {
 
 constexpr int kLeaf = 64, kPitch = kLeaf + 1, kThreads = 256;
-constexpr int kRowsPerThread = kLeaf * kLeaf / kThreads;  // 16
-constexpr size_t kLeafSmem = (size_t)(2 * kLeaf * kPitch + 2 * kLeaf) * sizeof(double);
-
-constexpr int kWarps = kThreads / 32;
-
-// For whole-block loads and stores: thread t owns column j = t % 64 and rows
-// r0 + 4 q (r0 = t / 64, q < 16).
-__device__ __forceinline__ int own_col() { return threadIdx.x % kLeaf; }
-__device__ __forceinline__ int own_row0() { return threadIdx.x / kLeaf; }
-// first row >= lo owned by this warp in the row layout (rows = warp mod 8)
-__device__ __forceinline__ int first_row(int lo) {
-    const int w = threadIdx.x / 32;
-    return lo + ((w - lo) % kWarps + kWarps) % kWarps;
-}
-
-// X <- L(k, k) L^-1 row by row (see above).  As holds L's columns unscaled by
-// sc: L(i, k) / L(k, k) = As[i][k] * sc[k].  On return X holds G up to the row
-// scale rd (G(i, j) = X[i][j] * rd[i]).
-__device__ void sweep_inverse(const double *As, const double *sc, double *X, int nb) {
-    const int j0 = own_col(), r0 = own_row0(), lane = threadIdx.x % 32;
-#pragma unroll
-    for (int q = 0; q < kRowsPerThread; ++q) {
-        const int i = r0 + 4 * q;
-        X[i * kPitch + j0] = (i == j0 && i < nb) ? 1.0 : 0.0;
-    }
-    for (int k = 0; k < nb - 1; ++k) {
-        __syncthreads();
-        const double s = sc[k];
-        for (int i = first_row(k + 1); i < nb; i += kWarps) {
-            const double mik = As[i * kPitch + k] * s;
-            for (int j = lane; j <= k; j += 32) X[i * kPitch + j] = fma(-mik, X[k * kPitch + j], X[i * kPitch + j]);
-        }
-    }
-    __syncthreads();
-}
-
-// Load the lower triangle of the nb x nb block at src (leading dimension ld)
-// into As (row-major, pitch kPitch); the rest of As is zero.
-__device__ void load_lower(const double *__restrict__ src, int ld, int nb, double *As) {
-    const int j = own_col(), r0 = own_row0();
-#pragma unroll
-    for (int q = 0; q < kRowsPerThread; ++q) {
-        const int i = r0 + 4 * q;
-        As[i * kPitch + j] = (i < nb && j < nb && i >= j) ? src[(size_t)j * ld + i] : 0.0;
-    }
-}
-
-// dst(i, j) = X[i][j] * rd[i] * scale on and below the diagonal, 0 above
-__device__ void store_lower(const double *X, const double *rd, double scale, int nb, double *__restrict__ dst, int ld) {
-    const int j = own_col(), r0 = own_row0();
-    if (j >= nb) return;
-#pragma unroll
-    for (int q = 0; q < kRowsPerThread; ++q) {
-        const int i = r0 + 4 * q;
-        if (i < nb) dst[(size_t)j * ld + i] = (i >= j) ? X[i * kPitch + j] * rd[i] * scale : 0.0;
-    }
-}
-
-// G_cc = L_cc^-1 for the diagonal blocks c of the n x n lower-triangular L, in
-// place (blockIdx.x = c; the last block may be short).
-__global__ void __launch_bounds__(kThreads) leaf_inverse_kernel(double *A, int n, int ld) {
-    extern __shared__ double smem[];
-    double *As = smem, *X = smem + kLeaf * kPitch, *rd = X + kLeaf * kPitch, *sc = rd + kLeaf;
-    const int r = blockIdx.x * kLeaf, nb = min(kLeaf, n - r);
-    double *blk = A + (size_t)r * ld + r;
-    load_lower(blk, ld, nb, As);
-    __syncthreads();
-    if (threadIdx.x < nb) {
-        const double d = As[threadIdx.x * kPitch + threadIdx.x];
-        rd[threadIdx.x] = 1.0 / d;
-        sc[threadIdx.x] = 1.0 / d;
-    }
-    __syncthreads();
-    sweep_inverse(As, sc, X, nb);
-    store_lower(X, rd, 1.0, nb, blk, ld);
-}
-
 // L = chol(A) in place and G = L^-1 for the nb x nb diagonal block at offset r
 // (global row of its first column, for the status word), A and G as DF64
 // pairs, blocked so that few steps wait at a block-wide barrier:
@@ -251,20 +166,139 @@ __global__ void __launch_bounds__(kThreads) leaf_chol_inv_df_kernel(float2 *A, f
     }
 }
 
+// The same blocked Cholesky-with-inverse in FP64 for the FP64 rebuild: L =
+// chol(A) in place and G = L^-1 for the nb x nb diagonal block at offset r,
+// pivots' 1/sqrt by rsqrt.  Steps as leaf_chol_inv_df_kernel; a non-positive
+// pivot sets *info to its 1-based global column (the first one found) and the
+// factorisation carries on with a zero scale, so the launch always ends.
+constexpr size_t kLeaf64Smem = (size_t)(2 * kLeaf * kPitch + kLeaf * kPPitch + 32 * kLeaf + 2 * kDiag) * sizeof(double);
+
+__global__ void __launch_bounds__(kThreads) leaf_chol_inv64_kernel(double *A, double *G, int nb, int ld, int r,
+                                                                   int *info) {
+    extern __shared__ double smem[];
+    double *As = smem;                 // [64][kPitch]: A, then L
+    double *Gs = As + kLeaf * kPitch;  // [64][kPitch]: G
+    double *P = Gs + kLeaf * kPitch;   // [64][kPPitch]: panel of the current block
+    double *Wm = P + kLeaf * kPPitch;  // [32 * 64]: products of a doubling level
+    double *rb = Wm + 32 * kLeaf, *sb = rb + kDiag;  // 1/L(k, k) and its square, current block
+    const int tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
+    for (int e = tid; e < kLeaf * kLeaf; e += kThreads) {
+        const int i = e % kLeaf, j = e / kLeaf;
+        double v = 0.0;
+        if (i < nb && j < nb) {
+            if (i >= j) v = A[(size_t)j * ld + i];
+        } else if (i == j) {
+            v = 1.0;
+        }
+        As[i * kPitch + j] = v;
+        Gs[i * kPitch + j] = 0.0;
+    }
+    __syncthreads();
+    for (int b0 = 0; b0 < kLeaf; b0 += kDiag) {
+        double *Ab = As + b0 * kPitch + b0, *Gb = Gs + b0 * kPitch + b0;
+        if (warp == 0) {  // (1) factor and invert the 8 x 8 diagonal block
+            for (int kk = 0; kk < kDiag; ++kk) {
+                __syncwarp();
+                const double d = Ab[kk * kPitch + kk];
+                const bool ok = d > 0.0;
+                const double rr = ok ? rsqrt(d) : 0.0, sq = rr * rr;
+                if (lane == 0) {
+                    rb[kk] = rr;
+                    sb[kk] = sq;
+                    if (!ok && b0 + kk < nb) atomicCAS(info, 0, r + b0 + kk + 1);
+                }
+                for (int e = lane; e < kDiag * kDiag; e += 32) {
+                    const int i = e / kDiag, j = e % kDiag;
+                    if (j > kk && i >= j)
+                        Ab[i * kPitch + j] = fma(-Ab[i * kPitch + kk] * sq, Ab[j * kPitch + kk], Ab[i * kPitch + j]);
+                }
+            }
+            for (int e = lane; e < kDiag * kDiag; e += 32) {
+                const int i = e / kDiag, j = e % kDiag;
+                Gb[i * kPitch + j] = i == j ? 1.0 : 0.0;
+            }
+            for (int kk = 0; kk < kDiag - 1; ++kk) {
+                __syncwarp();
+                for (int e = lane; e < kDiag * kDiag; e += 32) {
+                    const int i = e / kDiag, j = e % kDiag;
+                    if (i > kk && j <= kk)
+                        Gb[i * kPitch + j] = fma(-Ab[i * kPitch + kk] * sb[kk], Gb[kk * kPitch + j], Gb[i * kPitch + j]);
+                }
+            }
+            __syncwarp();
+            for (int e = lane; e < kDiag * kDiag; e += 32) {  // G = x_ij / L(i, i), L = a_ij / L(j, j)
+                const int i = e / kDiag, j = e % kDiag;
+                if (i >= j) {
+                    Gb[i * kPitch + j] *= rb[i];
+                    Ab[i * kPitch + j] *= rb[j];
+                }
+            }
+        }
+        __syncthreads();
+        const int r0 = b0 + kDiag, nr = kLeaf - r0;
+        for (int e = tid; e < nr * kDiag; e += kThreads) {  // (2) L(i, b0 + j) = sum_t A(i, b0 + t) G_bb(j, t)
+            const int i = r0 + e / kDiag, j = e % kDiag;
+            double a = 0.0;
+            for (int t = 0; t <= j; ++t) a = fma(As[i * kPitch + b0 + t], Gb[j * kPitch + t], a);
+            P[i * kPPitch + j] = a;
+        }
+        __syncthreads();
+        for (int e = tid; e < nr * kDiag; e += kThreads) {
+            const int i = r0 + e / kDiag, j = e % kDiag;
+            As[i * kPitch + b0 + j] = P[i * kPPitch + j];
+        }
+        for (int e = tid; e < kLeaf * kLeaf; e += kThreads) {  // (3) trailing update, a warp on one row
+            const int i = e / kLeaf, j = e % kLeaf;
+            if (j < r0 || j > i) continue;
+            double a = As[i * kPitch + j];
+#pragma unroll
+            for (int t = 0; t < kDiag; ++t) a = fma(-P[i * kPPitch + t], P[j * kPPitch + t], a);
+            As[i * kPitch + j] = a;
+        }
+        __syncthreads();
+    }
+    for (int s = kDiag; s < kLeaf; s *= 2) {  // inverse by doubling
+        const int per = s * s, count = (kLeaf / (2 * s)) * per;
+        for (int e = tid; e < count; e += kThreads) {  // W = L21 G11 (G11 lower: t >= j)
+            const int o = 2 * s * (e / per), i = (e % per) / s, j = e % s;
+            double a = 0.0;
+            for (int t = j; t < s; ++t) a = fma(As[(o + s + i) * kPitch + o + t], Gs[(o + t) * kPitch + o + j], a);
+            Wm[e] = a;
+        }
+        __syncthreads();
+        for (int e = tid; e < count; e += kThreads) {  // G21 = -G22 W (G22 lower: t <= i)
+            const int o = 2 * s * (e / per), i = (e % per) / s, j = e % s;
+            const double *W = Wm + (e / per) * per;
+            double a = 0.0;
+            for (int t = 0; t <= i; ++t) a = fma(Gs[(o + s + i) * kPitch + o + s + t], W[t * s + j], a);
+            Gs[(o + s + i) * kPitch + o + j] = -a;
+        }
+        __syncthreads();
+    }
+    for (int e = tid; e < kLeaf * kLeaf; e += kThreads) {
+        const int i = e % kLeaf, j = e / kLeaf;
+        if (i < nb && j < nb) {
+            const bool low = i >= j;
+            G[(size_t)j * ld + i] = low ? Gs[i * kPitch + j] : 0.0;
+            A[(size_t)j * ld + i] = low ? As[i * kPitch + j] : 0.0;
+        }
+    }
+}
+
 }  // namespace
 
 int leaf_rows() { return kLeaf; }
 
-cudaError_t leaf_inverse(double *A, int n, int ld, cudaStream_t st) {
+cudaError_t leaf_chol_inv64(double *A, double *G, int nb, int ld, int row0, int *info, cudaStream_t st) {
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(leaf_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kLeafSmem);
+        cudaError_t e = cudaFuncSetAttribute(leaf_chol_inv64_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kLeaf64Smem);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    if (n <= 0) return cudaSuccess;
-    leaf_inverse_kernel<<<(n + kLeaf - 1) / kLeaf, kThreads, kLeafSmem, st>>>(A, n, ld);
+    if (nb <= 0 || nb > kLeaf) return cudaErrorInvalidValue;
+    leaf_chol_inv64_kernel<<<1, kThreads, kLeaf64Smem, st>>>(A, G, nb, ld, row0, info);
     count_launch();
     return cudaGetLastError();
 }

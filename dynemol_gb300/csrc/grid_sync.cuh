@@ -17,8 +17,10 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 
 // Sense-reversing barrier over all CTAs of a cooperative launch.  Returns
 // false (and sets *err = ELHL_ERR_TIMEOUT) if the other CTAs do not arrive
-// within kBarrierNs, so a stuck launch ends with an error instead of hanging.
-__device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned *gen, unsigned nblocks, int *err) {
+// within limit_ns (kBarrierNs unless the launch sets a shorter limit), so a
+// stuck launch ends with an error instead of hanging.
+__device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned *gen, unsigned nblocks, int *err,
+                                             unsigned long long limit_ns = kBarrierNs) {
     __syncthreads();
     if (threadIdx.x == 0) {
         volatile unsigned *vgen = gen;
@@ -32,7 +34,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned *gen, uns
         } else {
             const unsigned long long t0 = globaltimer_ns();
             while (*vgen == g) {
-                if (globaltimer_ns() - t0 > kBarrierNs) {
+                if (globaltimer_ns() - t0 > limit_ns) {
                     atomicExch(err, ELHL_ERR_TIMEOUT);
                     break;
                 }

@@ -334,6 +334,15 @@ int elhl_server_destroy(elhl_server *sv);
  * events on that stream; NULL restores the library's own stream. */
 int elhl_set_stream(void *stream);
 
+/* Test hook for failure detection (no counterpart in the reference): the
+ * grid-barrier wait limit of the Chebyshev propagation launches (limit_s <= 0
+ * restores the default 5 s; at most 10 s) and, when exit_cta >= 0, one CTA of
+ * the next propagation launch that leaves before its first grid barrier, so
+ * that the other CTAs' waits run out and the call returns ELHL_ERR_TIMEOUT
+ * with the device context intact.  No fault or hang is involved: every wait
+ * is bounded. */
+int elhl_debug_barrier(double limit_s, int exit_cta);
+
 /* Kernels of this library launched so far in this process (each kernel node
  * of a replayed step graph counted; library calls such as cuBLAS not
  * counted): benchmarks read it before and after a timed region. */

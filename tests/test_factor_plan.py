@@ -1,10 +1,15 @@
-"""The block plans of the rebuild's recursive factorisations
-(dynemol_gb300/csrc/elhl_api.cu: tri_inverse / tri_inverse_top / trmm_*_oop,
-chol_inv_df), replayed on the host with the block constants read from the
-source: every leaf is a diagonal block of the expected size, the leaves tile
-the matrix, and no block exceeds the workspace factor_workspace allocates
-(ld x (ld / 2 + kTriBlock) elements).  A numpy replay of the same splits
-checks the algorithms on small matrices."""
+"""Host replays of the rebuild's index arithmetic, checked on the CPU before any
+GPU run:
+
+* the block plan of the recursive Cholesky-with-inverse (chol_inv64 and
+  chol_inv_df in dynemol_gb300/csrc/elhl_api.cu, both checked up front by
+  chol_inv_fits): every leaf is a diagonal block of at most 64 rows, the leaves
+  tile the matrix, and no off-diagonal block exceeds the ld x N workspace the
+  factor allocates; a numpy replay of the same splits reproduces L and L^-1;
+* dgemm64's tiling (dynemol_gb300/csrc/dgemm.cu): the k range each output tile
+  and split reads, for every triangular flag, with the constants read from the
+  source; the replayed masked product must equal the triangular product, and
+  the splits must cover the tile's k tiles exactly once."""
 import os
 import re
 
@@ -12,52 +17,25 @@ import numpy as np
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-SRC = open(os.path.join(ROOT, "dynemol_gb300", "csrc", "elhl_api.cu")).read()
-LEAF = 64       # leaf_rows(): 64-row diagonal blocks (factor.cu)
-CHOL_SPLIT = 64  # chol_inv_df splits on multiples of 64
+API = open(os.path.join(ROOT, "dynemol_gb300", "csrc", "elhl_api.cu")).read()
+DG = open(os.path.join(ROOT, "dynemol_gb300", "csrc", "dgemm.cu")).read()
+HDR = open(os.path.join(ROOT, "dynemol_gb300", "csrc", "elhl_internal.cuh")).read()
+LEAF = 64  # leaf_rows(): 64-row diagonal blocks (factor.cu)
 
 
-def _const(name):
-    m = re.search(r"constexpr int %s = (\d+);" % name, SRC)
+def _const(src, name):
+    m = re.search(r"\b%s = (\d+)" % name, src)
     assert m, name
     return int(m.group(1))
 
 
-TRI_BLOCK, TRMM_LEAF = _const("kTriBlock"), _const("kTrmmLeaf")
+BM, BN, BK = _const(DG, "kBM"), _const(DG, "kBN"), _const(DG, "kBK")
+MAX_PARTIALS, SPLIT_BELOW = _const(DG, "kMaxPartials"), _const(DG, "kSplitBelowTiles")
+TRI_A, TRI_B, TRI_BT, TRI_LC, TRI_AT = (_const(HDR, n) for n in ("kTriA", "kTriB", "kTriBt", "kTriLowerC", "kTriAt"))
 
 
 def ru(x, m):
     return (x + m - 1) // m * m
-
-
-def workspace(ld):
-    assert "cs.ld * (cs.ld / 2 + kTriBlock)" in SRC
-    return ld * (ld // 2 + TRI_BLOCK)
-
-
-def tri_plan(n, ld):
-    """Largest workspace use of tri_inverse, and the top-down leaves."""
-    need = 0
-    s = LEAF
-    while s < TRI_BLOCK:
-        npairs, rem = n // (2 * s), n - 2 * s * (n // (2 * s))
-        need = max(need, npairs * s * s, (rem - s) * s if rem > s else 0)
-        s *= 2
-    leaves = []
-
-    def top(a, m):
-        nonlocal need
-        if m <= TRI_BLOCK:
-            leaves.append((a, m))
-            return
-        n1 = ru(m // 2, TRI_BLOCK)
-        assert 0 < n1 < m
-        need = max(need, ld * n1)
-        top(a, n1)
-        top(a + n1, m - n1)
-
-    top(0, n)
-    return need, leaves
 
 
 def chol_plan(n, ld):
@@ -68,7 +46,7 @@ def chol_plan(n, ld):
         if m <= LEAF:
             leaves.append((a, m))
             return
-        n1 = ru(m // 2, CHOL_SPLIT)
+        n1 = ru(m // 2, LEAF)
         assert 0 < n1 < m
         need = max(need, ld * n1)
         rec(a, n1)
@@ -79,47 +57,17 @@ def chol_plan(n, ld):
 
 
 @pytest.mark.parametrize("n", list(range(1, 600)) + list(range(600, 4097, 7)) + [2170, 3720, 8192, 16384])
-def test_plans_fit_the_workspace(n):
+def test_plan_fits_the_workspace(n):
+    assert "chol_inv_fits(n, ld, (size_t)ld * N)" in API  # the FP64 factor's check, workspace ld x N
+    assert "chol_inv_fits(cs.N, cs.ld, (size_t)cs.ld * cs.N)" in API  # the double-float one
     ld = ru(n, 32)
-    w = workspace(ld)
-    for plan, block in ((tri_plan, TRI_BLOCK), (chol_plan, LEAF)):
-        need, leaves = plan(n, ld)
-        assert need <= w, (plan.__name__, n, need, w)
-        # leaves tile [0, n) with aligned blocks of at most `block` rows
-        pos = 0
-        for a, m in leaves:
-            assert a == pos and a % block == 0 and 0 < m <= block
-            pos += m
-        assert pos == n
-
-
-def _tri_inverse(L):
-    """G = L^-1 by the splits of tri_inverse (bottom-up batched pairs, then
-    top-down with both triangular products as full products of the blocks)."""
-    n = L.shape[0]
-    A = L.copy()
-    for r in range(0, n, LEAF):
-        b = slice(r, min(n, r + LEAF))
-        A[b, b] = np.linalg.inv(A[b, b])
-    s = LEAF
-    while s < TRI_BLOCK:
-        for o in range(0, n - s, 2 * s):
-            e = min(n, o + 2 * s)
-            i1, i2 = slice(o, o + s), slice(o + s, e)
-            A[i2, i1] = -A[i2, i2] @ (A[i2, i1] @ A[i1, i1])
-        s *= 2
-
-    def top(a, m):
-        if m <= TRI_BLOCK:
-            return
-        n1 = ru(m // 2, TRI_BLOCK)
-        top(a, n1)
-        top(a + n1, m - n1)
-        i1, i2 = slice(a, a + n1), slice(a + n1, a + m)
-        A[i2, i1] = -A[i2, i2] @ (A[i2, i1] @ A[i1, i1])
-
-    top(0, n)
-    return A
+    need, leaves = chol_plan(n, ld)
+    assert need <= ld * n, (n, need)
+    pos = 0
+    for a, m in leaves:  # leaves tile [0, n) with aligned blocks of at most 64 rows
+        assert a == pos and a % LEAF == 0 and 0 < m <= LEAF
+        pos += m
+    assert pos == n
 
 
 def _chol_inv(S):
@@ -132,7 +80,7 @@ def _chol_inv(S):
             Lb = np.linalg.cholesky(A[i, i] + np.tril(A[i, i], -1).T)
             A[i, i], G[i, i] = Lb, np.linalg.inv(Lb)
             return
-        n1 = ru(m // 2, CHOL_SPLIT)
+        n1 = ru(m // 2, LEAF)
         i1, i2 = slice(a, a + n1), slice(a + n1, a + m)
         rec(a, n1)
         A[i2, i1] = A[i2, i1] @ G[i1, i1].T
@@ -145,13 +93,100 @@ def _chol_inv(S):
 
 
 @pytest.mark.parametrize("n", [1, 63, 64, 65, 130, 300, 513, 700, 1100])
-def test_plans_compute_the_factors(n):
+def test_plan_computes_the_factors(n):
     rng = np.random.default_rng(n)
     X = rng.standard_normal((n, n))
     S = X @ X.T / n + np.eye(n)
     L = np.linalg.cholesky(S)
-    G = _tri_inverse(L)
-    assert np.abs(np.tril(G) - np.linalg.inv(L)).max() < 1e-12
     L2, G2 = _chol_inv(S)
     assert np.abs(L2 - L).max() < 1e-12
     assert np.abs(G2 - np.linalg.inv(L)).max() < 1e-12
+
+
+def _splits(tiles, ktiles):
+    """dgemm64's split-K count for a grid of `tiles` output tiles."""
+    if tiles < SPLIT_BELOW and ktiles > 0:
+        return max(1, min((2 * SPLIT_BELOW + tiles - 1) // tiles, ktiles, 16, MAX_PARTIALS // tiles))
+    return 1
+
+
+def _dgemm_replay(m, n, k, A, B, ta, tb, tri):
+    """C = op(A) op(B) accumulated tile by tile over the k ranges the kernel reads."""
+    opA = A.T if ta else A
+    opB = B.T if tb else B
+    gx, gy = (m + BM - 1) // BM, (n + BN - 1) // BN
+    S = _splits(gx * gy, (k + BK - 1) // BK)
+    assert gx * gy * S <= MAX_PARTIALS or S == 1
+    C = np.zeros((m, n))
+    for bx in range(gx):
+        for by in range(gy):
+            i0, j0 = bx * BM, by * BN
+            if (tri & TRI_LC) and i0 + BM <= j0:
+                continue
+            klo, khi = 0, k
+            if tri & TRI_A:
+                khi = min(khi, i0 + BM)
+            if tri & TRI_AT:
+                klo = max(klo, i0)
+            if tri & TRI_B:
+                klo = max(klo, j0)
+            if tri & TRI_BT:
+                khi = min(khi, j0 + BN)
+            nkt = (khi - klo + BK - 1) // BK if khi > klo else 0
+            covered = []
+            for z in range(S):
+                kt0, kt1 = z * nkt // S, (z + 1) * nkt // S
+                lo, hi = klo + kt0 * BK, min(khi, klo + kt1 * BK)
+                for k0 in range(lo, hi, BK):
+                    kk = np.arange(k0, min(k0 + BK, k))  # whole k tiles, masked only at k (as the kernel loads)
+                    covered += list(kk)
+                    ii = np.arange(i0, min(i0 + BM, m))
+                    jj = np.arange(j0, min(j0 + BN, n))
+                    a = opA[np.ix_(ii, kk)].copy()
+                    b = opB[np.ix_(kk, jj)].copy()
+                    gi, gk = np.meshgrid(ii, kk, indexing="ij")
+                    if tri & TRI_A:
+                        a[gk > gi] = 0.0
+                    if tri & TRI_AT:
+                        a[gk < gi] = 0.0
+                    gk2, gj = np.meshgrid(kk, jj, indexing="ij")
+                    if tri & TRI_B:
+                        b[gk2 < gj] = 0.0
+                    if tri & TRI_BT:
+                        b[gk2 > gj] = 0.0
+                    C[np.ix_(ii, jj)] += a @ b
+            assert len(covered) == len(set(covered))  # no k index twice in one tile
+            assert set(range(klo, khi)) <= set(covered)
+    return C
+
+
+@pytest.mark.parametrize("m,n,k", [(200, 200, 200), (130, 70, 130), (64, 2, 64), (3, 5, 7), (190, 190, 61)])
+@pytest.mark.parametrize("case", ["none", "A", "At", "B", "Bt", "Bt_lowerC"])
+def test_dgemm_tiles_cover_the_triangular_products(m, n, k, case):
+    rng = np.random.default_rng(m * 7 + n + k)
+    ta = case == "At"
+    tb = case.startswith("Bt")
+    A = rng.standard_normal((k, m) if ta else (m, k))
+    B = rng.standard_normal((n, k) if tb else (k, n))
+    tri = {"none": 0, "A": TRI_A, "At": TRI_AT, "B": TRI_B, "Bt": TRI_BT, "Bt_lowerC": TRI_BT | TRI_LC}[case]
+    # the triangular operand's stored zero side holds garbage, which the kernel must ignore
+    opA, opB = (A.T if ta else A), (B.T if tb else B)
+    if tri & TRI_A:
+        ref_a = np.tril(opA)
+    elif tri & TRI_AT:
+        ref_a = np.triu(opA)
+    else:
+        ref_a = opA
+    if tri & TRI_B:
+        ref_b = np.tril(opB)
+    elif tri & TRI_BT:
+        ref_b = np.triu(opB)
+    else:
+        ref_b = opB
+    C = _dgemm_replay(m, n, k, A, B, ta, tb, tri)
+    ref = ref_a @ ref_b
+    if tri & TRI_LC:  # only tiles reaching the diagonal are written; compare the lower triangle
+        mask = np.tril(np.ones((m, n), bool))
+        assert np.abs((C - ref)[mask]).max() < 1e-10
+    else:
+        assert np.abs(C - ref).max() < 1e-10

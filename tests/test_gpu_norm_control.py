@@ -114,3 +114,23 @@ def test_server_request_divergence_is_reported(elhl):
         sv.result(rid)
     sv.close()
     assert e.value.status == elhl.ERR_NO_CONVERGENCE
+
+
+def test_grid_barrier_timeout_is_reported(elhl, flake):
+    """A CTA that leaves the propagation launch before its first grid barrier
+    (the test hook) leaves the others waiting until their limit (0.2 s here):
+    the call returns ELHL_ERR_TIMEOUT, and the device stays usable."""
+    tr = _traj(elhl, flake, elhl.PREC_FP64)
+    tr.step(None, nsteps=1)
+    elhl.debug_barrier(0.2, 5)
+    try:
+        with pytest.raises(elhl.ElhlError) as e:
+            tr.step(None, nsteps=1)
+    finally:
+        elhl.debug_barrier(0.0, -1)
+    tr.close()
+    assert e.value.status == elhl.ERR_TIMEOUT
+    tr = _traj(elhl, flake, elhl.PREC_FP64)  # a fresh launch on the same context succeeds
+    pops = tr.step(None, nsteps=2)
+    tr.close()
+    assert np.isfinite(pops).all() and abs(pops[-1, 0, -1] - 1.0) < 1e-10
