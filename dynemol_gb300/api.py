@@ -32,12 +32,12 @@ EXPORTED_SYMBOLS = (
     "ehrenfestkernel2_gpu_", "elhl_ehrenfest_forces", "elhl_huckel_with_fields",
     "propagationelhl_gpucaller_", "elhl_last_status", "elhl_status_string", "elhl_traj_config_default",
     "elhl_traj_create", "elhl_traj_destroy", "elhl_traj_init_fmo", "elhl_traj_init_fmo_states", "elhl_traj_set_psi", "elhl_traj_get_psi", "elhl_traj_step",
-    "elhl_traj_step_device", "elhl_traj_energies", "elhl_traj_get_matrices", "elhl_traj_get_factor", "elhl_traj_get_stats", "elhl_device_count",
+    "elhl_traj_step_device", "elhl_traj_energies", "elhl_traj_get_matrices", "elhl_traj_get_factor", "elhl_traj_get_stats", "elhl_traj_snapshot", "elhl_traj_restore", "elhl_device_count",
     "elhl_sm_count", "elhl_set_stream", "elhl_debug_barrier", "elhl_kernel_launches", "elhl_propagate_fixed_scratch", "elhl_bessel_j",
     "elhl_chebyshev_coefficients", "elhl_batch_create", "elhl_batch_size", "elhl_batch_member",
     "elhl_batch_compact", "elhl_batch_step", "elhl_batch_get_stats", "elhl_batch_destroy",
     "elhl_server_create", "elhl_server_submit", "elhl_server_step", "elhl_server_poll", "elhl_server_result",
-    "elhl_server_destroy",
+    "elhl_server_destroy", "elhl_server_snapshot", "elhl_server_submit_restart",
 )
 
 
@@ -125,6 +125,8 @@ def load(path: str = LIB_PATH):
     L.elhl_traj_get_factor.argtypes = [vp, vp, vp]
     L.elhl_traj_energies.argtypes = [vp, vp]
     L.elhl_traj_get_stats.argtypes = [vp, ctypes.POINTER(TrajStats)]
+    L.elhl_traj_snapshot.argtypes = [vp, ctypes.c_char_p]
+    L.elhl_traj_restore.argtypes = [vp, ctypes.c_char_p]
     L.elhl_device_count.restype = ci
     L.elhl_sm_count.restype = ci
     L.elhl_set_stream.argtypes = [vp]
@@ -149,6 +151,9 @@ def load(path: str = LIB_PATH):
     L.elhl_server_step.argtypes = [vp, ip, ip]
     L.elhl_server_poll.argtypes = [vp, vp, ci, ip]
     L.elhl_server_result.argtypes = [vp, ctypes.c_longlong, vp, vp, vp]
+    L.elhl_server_snapshot.argtypes = [vp, ctypes.c_longlong, ctypes.c_char_p]
+    L.elhl_server_submit_restart.argtypes = [vp, ctypes.POINTER(Request), ctypes.c_char_p,
+                                             ctypes.POINTER(ctypes.c_longlong)]
     L.elhl_server_destroy.argtypes = [vp]
     for s in EXPORTED_SYMBOLS:
         getattr(L, s)
@@ -388,6 +393,14 @@ class Trajectory:
         _check(load().elhl_traj_get_stats(self.handle, ctypes.byref(st)), "elhl_traj_get_stats")
         return st
 
+    def snapshot(self, path: str):
+        """Checkpoint in the reference's Security_copy.dat layout (plus the resume record)."""
+        _check(load().elhl_traj_snapshot(self.handle, os.fsencode(path)), "elhl_traj_snapshot")
+
+    def restore(self, path: str):
+        """Resume from a checkpoint written by snapshot() (or by the reference)."""
+        _check(load().elhl_traj_restore(self.handle, os.fsencode(path)), "elhl_traj_restore")
+
 
 FIXED_SCRATCH_MAX_N = 4096
 
@@ -507,16 +520,25 @@ class Server:
         self.handle = h
         self.meta = {}
 
-    def submit(self, system, nsteps: int, states, which: str = "E", coords=None) -> int:
+    def submit(self, system, nsteps: int, states, which: str = "E", coords=None, restart: str | None = None) -> int:
+        """Queue a request; `restart`: resume from a checkpoint (snapshot()) and run nsteps more steps."""
         desc, keep = _basis_desc(system)
         c = np.ascontiguousarray(system.coords if coords is None else coords, np.float64)
         at = np.ascontiguousarray(system.fragment_atoms(which), np.int32)
         st = np.ascontiguousarray(states, np.int32)
         req = Request(ctypes.pointer(desc), _p(c), nsteps, len(st), len(at), _p(at), _p(st))
         rid = ctypes.c_longlong(0)
-        _check(load().elhl_server_submit(self.handle, ctypes.byref(req), ctypes.byref(rid)), "elhl_server_submit")
+        if restart is None:
+            _check(load().elhl_server_submit(self.handle, ctypes.byref(req), ctypes.byref(rid)), "elhl_server_submit")
+        else:
+            _check(load().elhl_server_submit_restart(self.handle, ctypes.byref(req), os.fsencode(restart),
+                                                     ctypes.byref(rid)), "elhl_server_submit_restart")
         self.meta[rid.value] = (system, len(st))
         return rid.value
+
+    def snapshot(self, rid: int, path: str):
+        """Checkpoint of an admitted request."""
+        _check(load().elhl_server_snapshot(self.handle, rid, os.fsencode(path)), "elhl_server_snapshot")
 
     def step(self):
         a, p = ctypes.c_int(0), ctypes.c_int(0)

@@ -256,11 +256,18 @@ __device__ void implicit_phase(const ChebLaunch &L, const ChebProblem &pb, int s
     const size_t bstride = gstride * (m / MG);
     const T2 *vprev = vbuf + (size_t)((k + 2) % 3) * bstride + g * gstride;  // v_{k-1}
     const T2 *src = ph == 0 ? vprev : wb + (size_t)(ph - 1) * bstride + g * gstride;
+    const ChebSegment *segs = L.segs;
+    if (ph == 1 && L.segs_full) {  // the full phase has its own even row split
+        segs = L.segs_full;
+        s0 = L.seg_full_begin[blockIdx.x];
+        s1 = L.seg_full_begin[blockIdx.x + 1];
+    }
+    if (s0 >= s1) return;
     __syncthreads();
     for (int q = threadIdx.x; q < ld * MG; q += kBlock) s_v[q] = ldcg2(src + q);  // padding rows are zero
     __syncthreads();
     for (int s = s0; s < s1; ++s) {
-        const ChebSegment sg = L.segs[s];
+        const ChebSegment sg = segs[s];
         if (ph == 0) {
             StoreEpi<T, MG> epi{wb + g * gstride};
             rows_gemv<T, MG, 1>(reinterpret_cast<const T *>(pb.G), ld, s_v, sg.row0, sg.row1, s_part, epi);
@@ -321,7 +328,7 @@ __global__ void __launch_bounds__(kBlock, 1) cheb_kernel(ChebLaunch L) {
                 const ChebProblem &pb = L.probs[0];
                 if (k == 0) {
                     for (int s = s0; s < s1; ++s) order_zero<T, MG>(pb, L.segs[s], L.parity);
-                } else if (k <= pb.K && s0 < s1) {
+                } else if (k <= pb.K) {
                     const double cre = pb.coef[k].x, cim = pb.coef[k].y;
                     for (int g = 0; g < pb.m / MG; ++g)
                         implicit_phase<T, MG>(L, pb, s0, s1, k, ph, g, s_v, s_part, cre, cim);
@@ -647,11 +654,18 @@ __device__ void implicit_phase_df(const ChebLaunch &L, const ChebProblem &pb, in
     const size_t bstride = gstride * (m / MG);
     const float4 *vprev = vbuf + (size_t)((k + 2) % 3) * bstride + g * gstride;
     const float4 *src = ph == 0 ? vprev : wb + (size_t)(ph - 1) * bstride + g * gstride;
+    const ChebSegment *segs = L.segs;
+    if (ph == 1 && L.segs_full) {  // the full phase has its own even row split
+        segs = L.segs_full;
+        s0 = L.seg_full_begin[blockIdx.x];
+        s1 = L.seg_full_begin[blockIdx.x + 1];
+    }
+    if (s0 >= s1) return;
     __syncthreads();
     for (int q = threadIdx.x; q < ld * MG; q += kBlock) s_v[q] = __ldcg(src + q);
     __syncthreads();
     for (int s = s0; s < s1; ++s) {
-        const ChebSegment sg = L.segs[s];
+        const ChebSegment sg = segs[s];
         if (ph == 0) {
             StoreEpiDF<MG> epi{wb + g * gstride};
             rows_gemv_df<MG, 1>(reinterpret_cast<const float2 *>(pb.G), ld, s_v, sg.row0, sg.row1, s_part, epi);
@@ -683,7 +697,7 @@ __global__ void __launch_bounds__(kBlock, 1) cheb_df_kernel(ChebLaunch L) {
         for (int ph = 0; ph < nph; ++ph) {
             if (k == 0) {
                 for (int s = s0; s < s1; ++s) order_zero_df<MG>(pb, L.segs[s], L.parity);
-            } else if (k <= pb.K && s0 < s1) {
+            } else if (k <= pb.K) {
                 const double cre = pb.coef[k].x, cim = pb.coef[k].y;
                 for (int g = 0; g < pb.m / MG; ++g)
                     implicit_phase_df<MG>(L, pb, s0, s1, k, ph, g, s_v, s_part, cre, cim);

@@ -14,6 +14,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <string>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -1294,9 +1295,11 @@ struct ChebPlan {
     std::vector<ChebSegment> segs;
     std::vector<int> seg_begin;
     std::vector<int> prob_seg0;
+    std::vector<ChebSegment> segs_full;  // implicit operator: even row split of the full phase
+    std::vector<int> seg_full_begin;
     ChebProblem *d_probs = nullptr;
-    ChebSegment *d_segs = nullptr;
-    int *d_seg_begin = nullptr, *d_prob_seg0 = nullptr;
+    ChebSegment *d_segs = nullptr, *d_segs_full = nullptr;
+    int *d_seg_begin = nullptr, *d_prob_seg0 = nullptr, *d_seg_full_begin = nullptr;
     double *d_seg_pops = nullptr;
     double *d_drift = nullptr;  // [problem] norm drift of the steps since the last reset
     int grid = 0, max_ld = 0, kmax = 0, mg = 0, mg_read = 0, precision = 0, parity = 0;
@@ -1306,7 +1309,7 @@ struct ChebPlan {
     size_t pops_per_step = 0;  // populations of all problems in one step
     void release() {
         dev_free(d_probs); dev_free(d_segs); dev_free(d_seg_begin); dev_free(d_prob_seg0); dev_free(d_seg_pops);
-        dev_free(d_drift);
+        dev_free(d_drift); dev_free(d_segs_full); dev_free(d_seg_full_begin);
     }
 };
 
@@ -1374,6 +1377,18 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
         if (cs->parity != pl.parity) return ELHL_ERR_BAD_ARG;
     }
     pl.seg_begin.assign(pl.grid + 1, 0);
+    pl.segs_full.clear();
+    pl.seg_full_begin.clear();
+    if (implicit) {
+        // the full phase: CTA c owns rows [N c / grid, N (c + 1) / grid), 24 or 25 rows at N = 3720
+        const int N = states[0]->N;
+        pl.seg_full_begin.assign(pl.grid + 1, 0);
+        for (int c = 0; c < pl.grid; ++c) {
+            const int r0 = (int)((long long)N * c / pl.grid), r1 = (int)((long long)N * (c + 1) / pl.grid);
+            if (r1 > r0) pl.segs_full.push_back({0, r0, r1});
+            pl.seg_full_begin[c + 1] = (int)pl.segs_full.size();
+        }
+    }
     if (implicit) {
         // 2 x grid equal row chunks, CTA c owning chunks c and 2 grid - 1 - c: the
         // triangular phases (G^T: j >= i, G: j <= i) then cost every CTA the same
@@ -1423,6 +1438,12 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
     CU_TRY(copy_h2d(pl.d_probs, pl.probs.data(), pl.probs.size() * sizeof(ChebProblem)));
     CU_TRY(copy_h2d(pl.d_segs, pl.segs.data(), pl.segs.size() * sizeof(ChebSegment)));
     CU_TRY(copy_h2d(pl.d_seg_begin, pl.seg_begin.data(), pl.seg_begin.size() * sizeof(int)));
+    if (!pl.segs_full.empty()) {
+        if (int rc = dev_alloc(&pl.d_segs_full, pl.segs_full.size())) return rc;
+        if (int rc = dev_alloc(&pl.d_seg_full_begin, pl.seg_full_begin.size())) return rc;
+        CU_TRY(copy_h2d(pl.d_segs_full, pl.segs_full.data(), pl.segs_full.size() * sizeof(ChebSegment)));
+        CU_TRY(copy_h2d(pl.d_seg_full_begin, pl.seg_full_begin.data(), pl.seg_full_begin.size() * sizeof(int)));
+    }
     pl.mgcd = mgcd;
     pl.tuned = false;  // measured on the first run (plans of batch members never run)
     return ELHL_OK;
@@ -1457,6 +1478,8 @@ ChebLaunch plan_launch(const ChebPlan &pl) {
     L.parity = pl.parity;
     L.seg_pops = pl.d_seg_pops;
     L.nphase = pl.nphase;
+    L.segs_full = pl.d_segs_full;
+    L.seg_full_begin = pl.d_seg_full_begin;
     return L;
 }
 
@@ -1539,6 +1562,8 @@ int cheb_run(ChebPlan &pl) {
     L.parity = pl.parity;
     L.seg_pops = pl.d_seg_pops;
     L.nphase = pl.nphase;
+    L.segs_full = pl.d_segs_full;
+    L.seg_full_begin = pl.d_seg_full_begin;
     L.barrier_ns = g_dbg_barrier_ns;
     L.exit_cta1 = g_dbg_exit_cta1;
     g_dbg_exit_cta1 = 0;  // one launch only
@@ -2099,7 +2124,7 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
         for (int s = 0; s < nsteps; ++s) tr->t = tr->t + tr->cfg.dt * tr->cfg.frame_step;
         tr->it += nsteps;
         tr->first_call = false;
-        for (int p = 0; p < P; ++p) tr->save_tau[p] = tr->cfg.dt / kHbar;
+        for (int p = 0; p < P && p < 2; ++p) tr->save_tau[p] = tr->cfg.dt / kHbar;  // electron, hole
         return ELHL_OK;
     }
     // ---- moving nuclei (or no device read-out): factor-based read-out through cuBLAS
@@ -2161,7 +2186,7 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
         tr->first_call = false;
     }
     dev_free(pops_tmp);
-    for (int p = 0; p < P; ++p) tr->save_tau[p] = tr->cfg.dt / kHbar;
+    for (int p = 0; p < P && p < 2; ++p) tr->save_tau[p] = tr->cfg.dt / kHbar;  // electron, hole
     tr->stats.status = rc;
     return rc;
 }
@@ -2857,6 +2882,269 @@ int elhl_traj_get_stats(elhl_traj *tr, elhl_traj_stats *st) {
 
 }  // extern "C"
 
+// =============================== checkpoints ====================================
+// Security_Copy_Cheb / Restart_State_Cheb (backup.f:329-445): a Fortran
+// sequential unformatted file (4-byte record lengths around each record) with
+// it, t, the basis size, the particle count, the particle tags, per particle
+// the interleaved (DUAL_bra, DUAL_ket) and (AO_bra, AO_ket) pairs, and the
+// Net_Charge record (the reference writes the whole array once per atom).  The
+// reference's reader stops there; one more record, which it never reads,
+// carries what a bit-exact resume of this library's trajectory needs: the
+// method and precision, first_call and save_tau (the next step's tau), the
+// norm targets, the Chebyshev interval and the symmetrised columns.
+namespace {
+
+constexpr char kResumeMagic[8] = {'E', 'L', 'H', 'L', 'R', 'S', 'M', '1'};
+
+struct ResumeHead {
+    char magic[8];
+    int method, precision, N, P, ncols, first_call, has_cols, pad;
+    double save_tau[2], emin, emax;
+};
+
+bool put_record(FILE *f, const void *p, size_t n) {
+    const uint32_t m = (uint32_t)n;
+    return fwrite(&m, 4, 1, f) == 1 && (n == 0 || fwrite(p, 1, n, f) == n) && fwrite(&m, 4, 1, f) == 1;
+}
+
+bool get_record(FILE *f, std::vector<char> &buf) {
+    uint32_t m = 0, m2 = 0;
+    if (fread(&m, 4, 1, f) != 1) return false;
+    buf.resize(m);
+    if (m && fread(buf.data(), 1, m, f) != m) return false;
+    return fread(&m2, 4, 1, f) == 1 && m2 == m;
+}
+
+struct FileCloser {
+    FILE *f;
+    ~FileCloser() { if (f) fclose(f); }
+};
+
+// Psi_bra, Psi_ket of every particle (host, column-major N x P)
+int traj_psi_host(elhl_traj *tr, std::vector<double2> &bra, std::vector<double2> &ket) {
+    const int N = tr->N, P = tr->P;
+    bra.resize((size_t)N * P);
+    ket.resize((size_t)N * P);
+    const size_t e = sizeof(double2);
+    CU_TRY(cudaStreamSynchronize(g_ctx.stream));
+    for (int p = 0; p < P; ++p) {
+        if (tr->cheb()) {
+            CU_TRY(cudaMemcpy2D(ket.data() + (size_t)p * N, e, tr->psi_ao + p, P * e, e, N, cudaMemcpyDeviceToHost));
+            CU_TRY(cudaMemcpy2D(bra.data() + (size_t)p * N, e, tr->bra_ao + p, P * e, e, N, cudaMemcpyDeviceToHost));
+        } else {
+            CU_TRY(cudaMemcpy(bra.data() + (size_t)p * N, tr->tb.bra(p), N * e, cudaMemcpyDeviceToHost));
+            CU_TRY(cudaMemcpy(ket.data() + (size_t)p * N, tr->tb.ket(p), N * e, cudaMemcpyDeviceToHost));
+        }
+    }
+    return ELHL_OK;
+}
+
+// AO_bra = conj(S^-1 Psi_bra) (ElHl_Chebyshev.f:274-275), S^-1 = G^T G on the device
+int traj_ao_bra(elhl_traj *tr, const std::vector<double2> &bra, std::vector<double2> &ao) {
+    const int N = tr->N, P = tr->P;
+    const size_t e = sizeof(double2);
+    double2 *d = nullptr;
+    double *scr = nullptr;
+    int rc = dev_alloc(&d, (size_t)N * P);
+    if (!rc) rc = dev_alloc(&scr, (size_t)2 * N * P);
+    for (int p = 0; p < P && !rc; ++p)  // [N][P] row-interleaved: the 2P x N real view
+        if (cudaMemcpy2DAsync(d + p, P * e, bra.data() + (size_t)p * N, e, e, N, cudaMemcpyHostToDevice,
+                              g_ctx.stream) != cudaSuccess)
+            rc = ELHL_ERR_CUDA;
+    const double *G = tr->cheb() ? traj_inverse(tr) : tr->fac.G;
+    if (!rc) rc = cols_apply_dense(tr->fac.L, G, tr->ld, N, d, P, 0, P, true, true, scr);
+    if (!rc) rc = cols_apply_dense(tr->fac.L, G, tr->ld, N, d, P, 0, P, false, true, scr);
+    ao.resize((size_t)N * P);
+    for (int p = 0; p < P && !rc; ++p)
+        if (cudaMemcpy2DAsync(ao.data() + (size_t)p * N, e, d + p, P * e, e, N, cudaMemcpyDeviceToHost,
+                              g_ctx.stream) != cudaSuccess)
+            rc = ELHL_ERR_CUDA;
+    if (!rc && cudaStreamSynchronize(g_ctx.stream) != cudaSuccess) rc = ELHL_ERR_CUDA;
+    dev_free(d);
+    dev_free(scr);
+    for (auto &z : ao) z.y = -z.y;
+    return rc;
+}
+
+int traj_snapshot_impl(elhl_traj *tr, const char *path) {
+    const int N = tr->N, P = tr->P;
+    std::vector<double2> bra, ket, ao_bra;
+    if (int rc = traj_psi_host(tr, bra, ket)) return rc;
+    if (int rc = traj_ao_bra(tr, bra, ao_bra)) return rc;
+    ResumeHead rh{};
+    memcpy(rh.magic, kResumeMagic, 8);
+    rh.method = tr->cfg.method;
+    rh.precision = tr->cfg.precision;
+    rh.N = N;
+    rh.P = P;
+    rh.ncols = tr->cfg.ncols;
+    rh.first_call = tr->first_call;
+    rh.save_tau[0] = tr->save_tau[0];
+    rh.save_tau[1] = tr->save_tau[1];
+    std::vector<double> target(P, 0.0);
+    std::vector<double2> cols;
+    if (tr->cheb()) {
+        ChebState &cs = tr->cs;
+        rh.emin = cs.emin;
+        rh.emax = cs.emax;
+        CU_TRY(cudaMemcpy(target.data(), tr->target, P * sizeof(double), cudaMemcpyDeviceToHost));
+        if (cs.cols_current) {  // fixed-nuclei steps continue from them (moving ones reload them from Psi)
+            rh.has_cols = 1;
+            cols.resize((size_t)N * cs.m);
+            CU_TRY(cudaMemcpy(cols.data(), cs.cin(), cols.size() * sizeof(double2), cudaMemcpyDeviceToHost));
+        }
+    }
+    // Net_Charge(atom) = sum_n sign_n |sum_{i in atom} DUAL_bra_i DUAL_ket_i|, sign -1 el / +1 hl
+    // (Populations_mtx, data_output.f:129-134), DUAL_bra = conj(Psi_ket), DUAL_ket = Psi_bra
+    std::vector<double> q(tr->natoms, 0.0);
+    for (int p = 0; p < P; ++p) {
+        const double sg = p % 2 == 0 ? -1.0 : 1.0;
+        for (int a = 0; a < tr->natoms; ++a) {
+            double re = 0.0, im = 0.0;
+            for (int j = 0; j < tr->h_nao[a]; ++j) {
+                const size_t i = (size_t)p * N + tr->h_ao0[a] + j;
+                const double2 x = make_double2(ket[i].x, -ket[i].y), y = bra[i];
+                re += x.x * y.x - x.y * y.y;
+                im += x.x * y.y + x.y * y.x;
+            }
+            q[a] += sg * std::sqrt(re * re + im * im);
+        }
+    }
+    FILE *f = fopen(path, "wb");
+    if (!f) return ELHL_ERR_BAD_ARG;
+    FileCloser fc{f};
+    const int it = tr->it, ntag = P;
+    const double t = tr->t;
+    bool ok = put_record(f, &it, 4) && put_record(f, &t, 8) && put_record(f, &N, 4) && put_record(f, &P, 4) &&
+              put_record(f, &ntag, 4);
+    std::string tags;
+    for (int p = 0; p < P; ++p) tags += p == 0 ? "el" : p == 1 ? "hl" : "  ";
+    ok = ok && put_record(f, tags.data(), tags.size());
+    std::vector<double2> pair(2 * (size_t)N);
+    for (int p = 0; p < P && ok; ++p) {
+        for (int i = 0; i < N; ++i) {  // (DUAL_bra, DUAL_ket) = (conj Psi_ket, Psi_bra)
+            const double2 k = ket[(size_t)p * N + i];
+            pair[2 * i] = make_double2(k.x, -k.y);
+            pair[2 * i + 1] = bra[(size_t)p * N + i];
+        }
+        ok = put_record(f, pair.data(), pair.size() * sizeof(double2));
+        for (int i = 0; i < N; ++i) {  // (AO_bra, AO_ket) = (conj S^-1 Psi_bra, Psi_ket)
+            pair[2 * i] = ao_bra[(size_t)p * N + i];
+            pair[2 * i + 1] = ket[(size_t)p * N + i];
+        }
+        ok = ok && put_record(f, pair.data(), pair.size() * sizeof(double2));
+    }
+    std::vector<double> qrep;
+    for (int a = 0; a < tr->natoms; ++a) qrep.insert(qrep.end(), q.begin(), q.end());
+    ok = ok && put_record(f, qrep.data(), qrep.size() * sizeof(double));
+    std::vector<char> resume(sizeof(ResumeHead) + P * sizeof(double) + cols.size() * sizeof(double2));
+    memcpy(resume.data(), &rh, sizeof(rh));
+    memcpy(resume.data() + sizeof(rh), target.data(), P * sizeof(double));
+    if (!cols.empty()) memcpy(resume.data() + sizeof(rh) + P * sizeof(double), cols.data(), cols.size() * sizeof(double2));
+    ok = ok && put_record(f, resume.data(), resume.size());
+    return ok ? ELHL_OK : ELHL_ERR_CUDA;
+}
+
+int traj_restore_impl(elhl_traj *tr, const char *path) {
+    FILE *f = fopen(path, "rb");
+    if (!f) return ELHL_ERR_BAD_ARG;
+    FileCloser fc{f};
+    std::vector<char> r;
+    int it = 0, N = 0, P = 0, ntag = 0;
+    double t = 0.0;
+    auto get_int = [&](int &v) { return get_record(f, r) && r.size() == 4 && (memcpy(&v, r.data(), 4), true); };
+    if (!get_int(it) || !(get_record(f, r) && r.size() == 8)) return ELHL_ERR_BAD_ARG;
+    memcpy(&t, r.data(), 8);
+    if (!get_int(N) || !get_int(P) || !get_int(ntag) || !get_record(f, r)) return ELHL_ERR_BAD_ARG;
+    if (N != tr->N || P != tr->P) return ELHL_ERR_BAD_ARG;
+    std::vector<double2> bra((size_t)N * P), ket((size_t)N * P);
+    for (int p = 0; p < P; ++p) {
+        if (!get_record(f, r) || r.size() != 2 * (size_t)N * sizeof(double2)) return ELHL_ERR_BAD_ARG;
+        const double2 *d = reinterpret_cast<const double2 *>(r.data());
+        for (int i = 0; i < N; ++i) bra[(size_t)p * N + i] = d[2 * i + 1];  // Psi_bra = DUAL_ket
+        if (!get_record(f, r) || r.size() != 2 * (size_t)N * sizeof(double2)) return ELHL_ERR_BAD_ARG;
+        d = reinterpret_cast<const double2 *>(r.data());
+        for (int i = 0; i < N; ++i) ket[(size_t)p * N + i] = d[2 * i + 1];  // Psi_ket = AO_ket
+    }
+    if (!get_record(f, r)) return ELHL_ERR_BAD_ARG;  // Net_Charge
+    ResumeHead rh{};
+    std::vector<double> target;
+    std::vector<char> res;
+    if (get_record(f, res) && res.size() >= sizeof(ResumeHead)) {
+        memcpy(&rh, res.data(), sizeof(rh));
+        if (memcmp(rh.magic, kResumeMagic, 8) || rh.method != tr->cfg.method || rh.precision != tr->cfg.precision ||
+            rh.N != N || rh.P != P || rh.ncols != tr->cfg.ncols)
+            return ELHL_ERR_BAD_ARG;
+        const size_t need = sizeof(rh) + P * sizeof(double) + (rh.has_cols ? (size_t)N * tr->cfg.ncols * 16 : 0);
+        if (res.size() != need) return ELHL_ERR_BAD_ARG;
+        target.assign(reinterpret_cast<const double *>(res.data() + sizeof(rh)),
+                      reinterpret_cast<const double *>(res.data() + sizeof(rh)) + P);
+    } else {
+        res.clear();  // a checkpoint of the reference itself: Psi, t and it only
+    }
+    const size_t e = sizeof(double2);
+    if (tr->cheb()) {
+        ChebState &cs = tr->cs;
+        for (int p = 0; p < P; ++p) {
+            CU_TRY(cudaMemcpy2D(tr->psi_ao + p, P * e, ket.data() + (size_t)p * N, e, e, N, cudaMemcpyHostToDevice));
+            CU_TRY(cudaMemcpy2D(tr->bra_ao + p, P * e, bra.data() + (size_t)p * N, e, e, N, cudaMemcpyHostToDevice));
+        }
+        if (res.empty()) {
+            if (int rc = cheb_set_target(tr)) return rc;
+        } else {
+            CU_TRY(cudaMemcpy(tr->target, target.data(), P * sizeof(double), cudaMemcpyHostToDevice));
+            cs.cols_current = false;
+            if (!cs.implicit && (rh.emin != cs.emin || rh.emax != cs.emax)) {  // an interval widened by norm control
+                cs.emin = rh.emin;
+                cs.emax = rh.emax;
+                if (int rc = cheb_prepare(cs, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol)) return rc;
+                if (!tr->plan.probs.empty()) {
+                    std::vector<ChebState *> one{&cs};
+                    if (int rc = cheb_plan_refresh(tr->plan, one)) return rc;
+                }
+            }
+            if (rh.has_cols) {
+                CU_TRY(cudaMemcpy(cs.cin(), res.data() + sizeof(rh) + P * sizeof(double), (size_t)N * cs.m * e,
+                                  cudaMemcpyHostToDevice));
+                cs.cols_current = true;
+            }
+        }
+    } else {
+        for (int p = 0; p < P; ++p) {
+            CU_TRY(cudaMemcpy(tr->tb.bra(p), bra.data() + (size_t)p * N, N * e, cudaMemcpyHostToDevice));
+            CU_TRY(cudaMemcpy(tr->tb.ket(p), ket.data() + (size_t)p * N, N * e, cudaMemcpyHostToDevice));
+        }
+    }
+    tr->t = t;
+    tr->it = it;
+    if (!res.empty()) {
+        tr->first_call = rh.first_call != 0;
+        tr->save_tau[0] = rh.save_tau[0];
+        tr->save_tau[1] = rh.save_tau[1];
+    } else {
+        tr->first_call = true;  // the reference's checkpoint has no tau: restart at tau_max
+    }
+    return ELHL_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int elhl_traj_snapshot(elhl_traj *tr, const char *path) {
+    if (!tr || !path) return ELHL_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(g_ctx.mu);
+    return traj_snapshot_impl(tr, path);
+}
+
+int elhl_traj_restore(elhl_traj *tr, const char *path) {
+    if (!tr || !path) return ELHL_ERR_BAD_ARG;
+    std::lock_guard<std::mutex> lk(g_ctx.mu);
+    return traj_restore_impl(tr, path);
+}
+
+}  // extern "C"
+
 // =============================== batches ========================================
 // Many Chebyshev trajectories (fixed nuclei) advanced together: one cooperative
 // launch per nuclear step covers every member's orders (persistent kernel over
@@ -3014,6 +3302,7 @@ struct ServerRequest {
     std::vector<double2> psi;          // final ket, N x P (column-major)
     int status = ELHL_OK;
     double t_submit = 0.0, t_admit = 0.0, t_done = 0.0;  // seconds, host steady clock
+    std::string restart;               // checkpoint to resume from at admission (empty: initial states)
 };
 
 static double now_s() {
@@ -3059,7 +3348,10 @@ static int server_admit(elhl_server *sv, ServerRequest *r) {
     std::lock_guard<std::mutex> lk(g_ctx.mu);
     elhl_traj *tr = r->tr;
     tr->cs.parity = sv->parity;  // join the running batch's column roles
-    if (int rc = cheb_load_columns(tr)) return rc;
+    if (!r->restart.empty())
+        if (int rc = traj_restore_impl(tr, r->restart.c_str())) return rc;
+    if (!tr->cs.cols_current)
+        if (int rc = cheb_load_columns(tr)) return rc;
     CU_TRY(cudaStreamSynchronize(g_ctx.stream));
     dev_free(tr->S); dev_free(tr->h); dev_free(tr->cs.Ht); dev_free(tr->cs.lz);
     return ELHL_OK;
@@ -3078,7 +3370,30 @@ int elhl_server_create(double hbm_budget_bytes, const elhl_traj_config *cfg, elh
     return ELHL_OK;
 }
 
+static int server_submit(elhl_server *sv, const elhl_request *q, const char *restart, long long *id);
+
 int elhl_server_submit(elhl_server *sv, const elhl_request *q, long long *id) {
+    return server_submit(sv, q, nullptr, id);
+}
+
+int elhl_server_submit_restart(elhl_server *sv, const elhl_request *q, const char *path, long long *id) {
+    if (!path) return ELHL_ERR_BAD_ARG;
+    return server_submit(sv, q, path, id);
+}
+
+int elhl_server_snapshot(elhl_server *sv, long long id, const char *path) {
+    if (!sv || !path) return ELHL_ERR_BAD_ARG;
+    for (auto *r : sv->active) {
+        if (r->id != id) continue;
+        std::lock_guard<std::mutex> lk(g_ctx.mu);
+        std::vector<ChebState *> one{&r->tr->cs};
+        if (int rc = cheb_settle(one)) return rc;  // apply the pending renormalisation (bit-neutral)
+        return traj_snapshot_impl(r->tr, path);
+    }
+    return ELHL_ERR_BAD_ARG;  // not admitted yet, or finished
+}
+
+static int server_submit(elhl_server *sv, const elhl_request *q, const char *restart, long long *id) {
     if (!sv || !q || !q->basis || !q->coords || q->nsteps <= 0 || q->nparticles < 1 || q->nparticles > 64 ||
         !q->frag_atoms || q->n_frag_atoms <= 0 || !q->states)
         return ELHL_ERR_BAD_ARG;
@@ -3097,6 +3412,7 @@ int elhl_server_submit(elhl_server *sv, const elhl_request *q, long long *id) {
     r->coords.assign(q->coords, q->coords + 3 * b->natoms);
     r->frag_atoms.assign(q->frag_atoms, q->frag_atoms + q->n_frag_atoms);
     r->states.assign(q->states, q->states + q->nparticles);
+    if (restart) r->restart = restart;
     r->bytes = request_bytes(sv->cfg, b->nao, r->P);
     if (r->bytes > sv->budget) {
         delete r;
@@ -3173,6 +3489,9 @@ int elhl_server_step(elhl_server *sv, int *n_active, int *n_pending) {
         for (size_t q = 0; q < sv->active.size(); ++q) {
             ServerRequest *r = sv->active[q];
             r->done_steps += 1;
+            r->tr->t += r->tr->cfg.dt * r->tr->cfg.frame_step;
+            r->tr->it += 1;
+            r->tr->first_call = false;
             const size_t np = (size_t)r->P * (r->nfrag + 1);
             if (!(drift[q] <= cheb_norm_tolerance(r->tr->cfg))) r->status = ELHL_ERR_NO_CONVERGENCE;
             if (r->done_steps >= r->nsteps || r->status) {

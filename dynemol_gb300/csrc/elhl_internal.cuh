@@ -132,6 +132,10 @@ struct ChebLaunch {
     double *seg_pops;       // [nseg][kMaxCols][kMaxFrag+1] read-out partials
     double *pops;           // this step's populations block, or nullptr
     int nphase;             // grid phases per order: 1 (explicit Hs) or 3 (one implicit problem)
+    // implicit operator: row ranges of the full phase y = (h/b) w, an even split of
+    // the rows over the CTAs (the triangular phases use segs: mirrored chunk pairs)
+    const ChebSegment *segs_full;
+    const int *seg_full_begin;  // [grid + 1]
     // failure-detection test hook (elhl_debug_barrier): grid-barrier limit in ns
     // (0: the default 5 s) and 1 + the CTA that leaves before its first grid
     // barrier (0: none, so a zero-initialised launch has no hook)

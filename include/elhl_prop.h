@@ -247,6 +247,25 @@ int elhl_traj_step_device(elhl_traj *tr, const double *d_coords, int nsteps, dou
  * ElHl_Chebyshev.f:329-371, evaluated with the Hueckel h).  E: [nparticles]. */
 int elhl_traj_energies(elhl_traj *tr, elhl_zcomplex *E);
 
+/*
+ * Checkpoint and resume (Security_Copy_Cheb / Restart_State_Cheb,
+ * backup.f:329-445).  elhl_traj_snapshot writes the trajectory's state to
+ * `path` in the reference's layout -- a Fortran sequential unformatted file
+ * with it, t, the basis size, the particle count and tags, per particle the
+ * (DUAL_bra, DUAL_ket) and (AO_bra, AO_ket) pairs, and the Net_Charge record
+ * -- followed by one record the reference does not read, holding what an exact
+ * resume needs (tau continuation, norm targets, the Chebyshev interval and the
+ * symmetrised columns).  elhl_traj_restore reads such a file into a trajectory
+ * created with the same basis, configuration and coordinates (Psi_bra =
+ * DUAL_ket, Psi_ket = AO_ket as in preprocess_from_restart,
+ * ElHl_Chebyshev.f:396-397); the next steps then reproduce the uninterrupted
+ * run bit for bit within one process.  A file written by the reference itself
+ * (no trailing record) restores Psi, t and it, and the next step restarts at
+ * tau_max.  ELHL_ERR_BAD_ARG for an unreadable or mismatched file.
+ */
+int elhl_traj_snapshot(elhl_traj *tr, const char *path);
+int elhl_traj_restore(elhl_traj *tr, const char *path);
+
 /* Copies of the device matrices (host, N x N, ld = N); any pointer may be NULL. */
 int elhl_traj_get_matrices(elhl_traj *tr, double *S, double *h, double *Hp);
 
@@ -327,6 +346,13 @@ int elhl_server_poll(elhl_server *sv, long long *ids, int max, int *n);
  * column-major) and times {submit, admit, done} (s, host steady clock); frees
  * the request; returns its status. */
 int elhl_server_result(elhl_server *sv, long long id, double *pops, elhl_zcomplex *psi_ket, double *times);
+/* Checkpoint of an admitted request (elhl_traj_snapshot's file layout; its it
+ * and t count the server steps done), and a request that resumes from such a
+ * file at admission: the trajectory is set up as for elhl_server_submit, its
+ * state restored, and q->nsteps more steps run.  ELHL_ERR_BAD_ARG for a request
+ * that is not active. */
+int elhl_server_snapshot(elhl_server *sv, long long id, const char *path);
+int elhl_server_submit_restart(elhl_server *sv, const elhl_request *q, const char *path, long long *id);
 int elhl_server_destroy(elhl_server *sv);
 
 /* Run all library work on the caller's CUDA stream (a cudaStream_t passed as
