@@ -427,23 +427,32 @@ __global__ void __launch_bounds__(kBlock, 1) readout_kernel(ChebLaunch L) {
 }
 
 // one block per problem: sum its segments' partials in order -> populations of
-// this step; renormalisation factor for the next step (reduced precision)
+// this step.  Reduced precision: the renormalisation factor s = sqrt(target /
+// total) for the next step, and the populations reported are those of the
+// renormalised state the trajectory carries on with (each times s^2).
 __global__ void reduce_pops_kernel(ChebLaunch L, int nprob) {
     const int q = blockIdx.x;
     if (q >= nprob) return;
     const ChebProblem &pb = L.probs[q];
     if (!pb.A) return;
     const int nf = min(pb.nfrag, kMaxFrag), P = pb.P;
+    __shared__ double s2[kMaxCols];  // population factor s^2 per particle
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+        double tot = 0.0;
+        for (int s = L.prob_seg0[q]; s < L.prob_seg0[q + 1]; ++s)
+            tot += L.seg_pops[(size_t)s * kMaxCols * (kMaxFrag + 1) + p * (kMaxFrag + 1) + nf];
+        const double tgt = pb.target ? pb.target[p] : 0.0;
+        const bool rn = pb.scale_out && tot > 0.0 && tgt > 0.0;
+        if (pb.scale_out) pb.scale_out[p] = rn ? sqrt(tgt / tot) : 1.0;
+        s2[p] = rn ? tgt / tot : 1.0;
+    }
+    __syncthreads();
     for (int t = threadIdx.x; t < P * (nf + 1); t += blockDim.x) {
         const int p = t / (nf + 1), f = t % (nf + 1);
         double a = 0.0;
         for (int s = L.prob_seg0[q]; s < L.prob_seg0[q + 1]; ++s)
             a += L.seg_pops[(size_t)s * kMaxCols * (kMaxFrag + 1) + p * (kMaxFrag + 1) + f];
-        if (L.pops) L.pops[pb.pops_off + p * (pb.nfrag + 1) + (f == nf ? pb.nfrag : f)] = a;
-        if (f == nf && pb.scale_out) {
-            const double tot = a, tgt = pb.target ? pb.target[p] : 0.0;
-            pb.scale_out[p] = (tot > 0.0 && tgt > 0.0) ? sqrt(tgt / tot) : 1.0;
-        }
+        if (L.pops) L.pops[pb.pops_off + p * (pb.nfrag + 1) + (f == nf ? pb.nfrag : f)] = a * s2[p];
     }
 }
 

@@ -1189,11 +1189,16 @@ __global__ void to_double2_kernel(const float2 *__restrict__ src, double2 *__res
     if (q < nm) dst[q] = make_double2((double)src[q].x, (double)src[q].y);
 }
 
-__global__ void scale_from_pops_kernel(const double *pops, int P, int nfrag, const double *target, double *scale) {
+// renormalisation factor s = sqrt(target / total) for the next step; the
+// populations become those of the renormalised state (each times s^2)
+__global__ void scale_from_pops_kernel(double *pops, int P, int nfrag, const double *target, double *scale) {
     const int p = threadIdx.x;
     if (p < P) {
         const double tot = pops[(size_t)p * (nfrag + 1) + nfrag];
-        scale[p] = (tot > 0.0 && target[p] > 0.0) ? sqrt(target[p] / tot) : 1.0;
+        const bool rn = tot > 0.0 && target[p] > 0.0;
+        scale[p] = rn ? sqrt(target[p] / tot) : 1.0;
+        if (rn)
+            for (int f = 0; f <= nfrag; ++f) pops[(size_t)p * (nfrag + 1) + f] *= target[p] / tot;
     }
 }
 
@@ -2166,7 +2171,7 @@ int cheb_step_impl(elhl_traj *tr, const double *coords, bool coords_on_device, i
             renormalize_kernel<<<(tr->N + 255) / 256, 256, 0, st>>>(out, tr->N, cs.m, P, pp, nf, tr->target);
             count_launch();
             if (cudaGetLastError() != cudaSuccess) { rc = ELHL_ERR_CUDA; break; }
-            if ((rc = cheb_readout(tr, out, nullptr))) break;  // AO state follows the renormalised columns
+            if ((rc = cheb_readout(tr, out, pp))) break;  // AO state and populations of the renormalised columns
         }
         tr->plan.parity ^= 1;
         cs.parity = tr->plan.parity;
