@@ -35,6 +35,7 @@ template <> struct Vec2<float> { using type = float2; };
 
 constexpr int kBlock = 512;
 constexpr int kWarps = kBlock / 32;
+constexpr int kYRows = 512;  // rows per block of window partial sums (explicit Hs, large bases)
 // rows per warp tile: FP32 reuses each staged x over 8 rows (shared-memory
 // bandwidth); FP64 is bound by its FMA pipe, so 2-row tiles keep the per-CTA
 // row counts (about N / 152) from wasting FMAs on partial tiles
@@ -85,7 +86,7 @@ __device__ __forceinline__ T warp_sums(T (&v)[NV], int lane) {
 // 8-row tile issue no loads and no FMAs.
 template <typename T, int MG, int TRI, typename Epi>
 __device__ void rows_gemv(const T *M, int ld, const typename Vec2<T>::type *s_v, int row0, int row1, T *s_part,
-                          Epi &epi) {
+                          Epi &epi, int jw0 = 0, int jw1 = 1 << 30) {
     using T2 = typename Vec2<T>::type;
     constexpr int kRT = RowTile<T>::value;
     constexpr int NV = kRT * MG * 2;   // accumulators per lane (4 ... 64)
@@ -99,8 +100,9 @@ __device__ void rows_gemv(const T *M, int ld, const typename Vec2<T>::type *s_v,
     const int wr = warp / WJ, wj = warp % WJ;
     for (int base = row0; base < row1; base += kRT * WR) {
         const int tile_end = min(row1, base + kRT * WR);
-        const int jlo = TRI == 1 ? (base & ~31) : 0;
-        const int jhi = TRI == 2 ? min(ld, (tile_end + 31) & ~31) : ld;
+        // j window [jw0, jw1) (multiples of 32; s_v holds x from row jw0 on)
+        const int jlo = max(jw0, TRI == 1 ? (base & ~31) : 0);
+        const int jhi = min(jw1, TRI == 2 ? min(ld, (tile_end + 31) & ~31) : ld);
         const int jchunk = ((jhi - jlo + WJ - 1) / WJ + 31) / 32 * 32;
         const int j0 = jlo + wj * jchunk, j1 = min(jhi, j0 + jchunk);
         const int r0 = base + kRT * wr;
@@ -128,7 +130,7 @@ __device__ void rows_gemv(const T *M, int ld, const typename Vec2<T>::type *s_v,
                 for (int u = 0; u < VE; ++u) {
                     T2 x[MG];
 #pragma unroll
-                    for (int c = 0; c < MG; ++c) x[c] = s_v[(jv + u) * MG + c];
+                    for (int c = 0; c < MG; ++c) x[c] = s_v[(jv - jw0 + u) * MG + c];
 #pragma unroll
                     for (int r = 0; r < kRT; ++r) {
                         if (kFull || r < nr) {
@@ -210,10 +212,24 @@ struct OrderEpi {
     }
 };
 
-// one order k >= 1 for the rows of segment sg, column group g (MG columns)
+// partial sums of a j window: s_y[(i - r0) * MG + c] += (yr, yi)
+template <typename T, int MG>
+struct AccEpi {
+    typename Vec2<T>::type *s_y;
+    int r0;
+    __device__ void operator()(int i, int c, T yr, T yi) {
+        auto &y = s_y[(size_t)(i - r0) * MG + c];
+        y.x += yr;
+        y.y += yi;
+    }
+};
+
+// one order k >= 1 for the rows of segment sg, column group g (MG columns);
+// jwin > 0: the previous vector is staged in windows of jwin rows
 template <typename T, int MG>
 __device__ void order_rows(const ChebProblem &pb, const ChebSegment &sg, int k, int g, int parity,
-                           typename Vec2<T>::type *s_v, T *s_part, double cre, double cim) {
+                           typename Vec2<T>::type *s_v, T *s_part, double cre, double cim, int jwin,
+                           typename Vec2<T>::type *s_y) {
     using T2 = typename Vec2<T>::type;
     const int tid = threadIdx.x;
     const int ld = pb.ld, m = pb.m;
@@ -221,13 +237,35 @@ __device__ void order_rows(const ChebProblem &pb, const ChebSegment &sg, int k, 
     const size_t gstride = (size_t)pb.ldv * MG;         // one column group
     const size_t bstride = gstride * (m / MG);          // one of the three vector buffers
     const T2 *vprev = vbuf + (size_t)((k + 2) % 3) * bstride + g * gstride;   // v_{k-1}
-    __syncthreads();
-    for (int q = tid; q < ld * MG; q += kBlock) s_v[q] = ldcg2(vprev + q);  // padding rows are zero
-    __syncthreads();
     OrderEpi<T, MG> epi{vbuf + (size_t)((k + 1) % 3) * bstride + g * gstride,
                         vbuf + (size_t)(k % 3) * bstride + g * gstride,
                         pb.col[parity ^ 1], k, m, g, cre, cim, nullptr, T(0)};
-    rows_gemv<T, MG, 0>(reinterpret_cast<const T *>(pb.H), ld, s_v, sg.row0, sg.row1, s_part, epi);
+    if (jwin == 0 || ld <= jwin) {  // the whole previous vector in shared memory
+        __syncthreads();
+        for (int q = tid; q < ld * MG; q += kBlock) s_v[q] = ldcg2(vprev + q);  // padding rows are zero
+        __syncthreads();
+        rows_gemv<T, MG, 0>(reinterpret_cast<const T *>(pb.H), ld, s_v, sg.row0, sg.row1, s_part, epi);
+        return;
+    }
+    // A basis too large for the whole vector: stage it in windows of jwin rows;
+    // each row's partial sums accumulate over the windows in shared memory (s_y,
+    // one writer per entry per window), and the order's epilogue runs once after
+    // the last window, in row blocks of kYRows.
+    for (int r0 = sg.row0; r0 < sg.row1; r0 += kYRows) {
+        const int r1 = min(sg.row1, r0 + kYRows);
+        __syncthreads();
+        for (int q = tid; q < (r1 - r0) * MG; q += kBlock) s_y[q] = T2{T(0), T(0)};
+        for (int jw0 = 0; jw0 < ld; jw0 += jwin) {
+            const int jw1 = min(ld, jw0 + jwin);
+            __syncthreads();
+            for (int q = tid; q < (jw1 - jw0) * MG; q += kBlock) s_v[q] = ldcg2(vprev + (size_t)jw0 * MG + q);
+            __syncthreads();
+            AccEpi<T, MG> acc_epi{s_y, r0};
+            rows_gemv<T, MG, 0>(reinterpret_cast<const T *>(pb.H), ld, s_v, r0, r1, s_part, acc_epi, jw0, jw1);
+        }
+        __syncthreads();
+        for (int q = tid; q < (r1 - r0) * MG; q += kBlock) epi(r0 + q / MG, q % MG, s_y[q].x, s_y[q].y);
+    }
 }
 
 template <typename T, int MG>
@@ -343,7 +381,8 @@ __global__ void __launch_bounds__(kBlock, 1) cheb_kernel(ChebLaunch L) {
                     } else {
                         const double cre = pb.coef[k].x, cim = pb.coef[k].y;
                         for (int g = 0; g < pb.m / MG; ++g)
-                            order_rows<T, MG>(pb, sg, k, g, L.parity, s_v, s_part, cre, cim);
+                            order_rows<T, MG>(pb, sg, k, g, L.parity, s_v, s_part, cre, cim, L.jwin,
+                                              s_v + (size_t)L.jwin * MG);
                     }
                 }
             }
@@ -734,11 +773,18 @@ cudaError_t launch_df(const ChebLaunch &L, cudaStream_t st) {
 template <typename T, int MG>
 cudaError_t launch_t(const ChebLaunch &L, cudaStream_t st) {
     auto kern = cheb_kernel<T, MG>;
-    const size_t smem = kCheb_part_bytes + (size_t)L.max_ld * MG * sizeof(typename Vec2<T>::type);
+    constexpr size_t c2 = sizeof(typename Vec2<T>::type);
+    size_t smem = kCheb_part_bytes + (size_t)L.max_ld * MG * c2;
+    ChebLaunch copy = L;
+    copy.jwin = 0;
+    if (smem > kCheb_smem_limit && L.nphase == 1) {  // explicit Hs: stage the vector in windows
+        const size_t ybytes = (size_t)kYRows * MG * c2;
+        copy.jwin = (int)(((kCheb_smem_limit - kCheb_part_bytes - ybytes) / (MG * c2)) & ~(size_t)31);
+        smem = kCheb_part_bytes + (size_t)copy.jwin * MG * c2 + ybytes;
+    }
     if (smem > kCheb_smem_limit) return cudaErrorInvalidValue;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    ChebLaunch copy = L;
     void *args[] = {&copy};
     e = cudaLaunchCooperativeKernel((const void *)kern, dim3(L.grid), dim3(kBlock), args, smem, st);
     count_launch();
@@ -782,11 +828,12 @@ cudaError_t launch_readout(const ChebLaunch &L, int nprob, int precision, int mg
 
 int cheb_block() { return kBlock; }
 
-int cheb_group_size(int precision, int m, int max_ld) {
-    // the largest of 4, 2, 1 staged columns that divides m and fits in shared memory
+int cheb_group_size(int precision, int m, int max_ld, bool windowed) {
+    // the largest of 4, 2, 1 staged columns that divides m and fits in shared
+    // memory (windowed: the explicit propagation stages the vector in windows)
     const size_t c2 = (precision == ELHL_PREC_FP64 || precision == ELHL_PREC_DF64) ? sizeof(double2) : sizeof(float2);
     for (int mg : {4, 2, 1})
-        if (m % mg == 0 && kCheb_part_bytes + (size_t)max_ld * mg * c2 <= kCheb_smem_limit) return mg;
+        if (m % mg == 0 && (windowed || kCheb_part_bytes + (size_t)max_ld * mg * c2 <= kCheb_smem_limit)) return mg;
     return 0;
 }
 

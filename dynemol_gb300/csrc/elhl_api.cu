@@ -1341,7 +1341,8 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
         while (b) { const int t = a % b; a = b; b = t; }
         mgcd = a;
     }
-    pl.mg = cheb_group_size(pl.precision, mgcd, pl.max_ld);
+    const bool implicit_plan = states[0]->implicit;
+    pl.mg = cheb_group_size(pl.precision, mgcd, pl.max_ld, !implicit_plan);
     if (!pl.mg) return ELHL_ERR_UNSUPPORTED;
     int pgcd = 0;  // read-out groups must divide every problem's ket columns
     for (auto *cs : states) {
@@ -1501,7 +1502,7 @@ std::map<std::tuple<int, int, int, int, int>, int> g_tile_cache;
 int tune_plan(ChebPlan &pl, int mgcd) {
     std::vector<int> cand;
     for (int mg : {4, 2, 1})
-        if (mgcd % mg == 0 && cheb_group_size(pl.precision, mg, pl.max_ld) == mg) cand.push_back(mg);
+        if (mgcd % mg == 0 && cheb_group_size(pl.precision, mg, pl.max_ld, pl.nphase == 1) == mg) cand.push_back(mg);
     if (cand.size() < 2 || pl.kmax < 1) return ELHL_OK;
     double elems = 0.0;
     for (const auto &p : pl.probs) elems += (double)p.N * p.ld;
@@ -3308,7 +3309,23 @@ struct ServerRequest {
     int status = ELHL_OK;
     double t_submit = 0.0, t_admit = 0.0, t_done = 0.0;  // seconds, host steady clock
     std::string restart;               // checkpoint to resume from at admission (empty: initial states)
+    int group = -1;                    // row-kernel group index, or -1: GEMM regime (own step graph)
+    size_t pops_off = 0;               // offset of its populations in the group's block
 };
+
+// Requests whose bases allow the same staged column-group size (4, 2 or 1:
+// the whole previous vector of a group sits in shared memory) share one plan
+// and one cooperative launch per server step, so that one large basis does
+// not force single columns on every other request.
+struct ServerGroup {
+    std::vector<ServerRequest *> reqs;
+    ChebPlan plan;
+    bool dirty = true;
+    int parity = 0;
+    double *pops = nullptr;
+    size_t pops_cap = 0;
+};
+constexpr int kServerGroups = 3;  // column-group size 4, 2, 1
 
 static double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -3318,15 +3335,11 @@ struct elhl_server {
     elhl_traj_config cfg;
     double budget = 0.0, used = 0.0;
     std::deque<ServerRequest *> pending;
-    std::vector<ServerRequest *> active;
+    std::vector<ServerRequest *> active;  // admission order
     std::map<long long, ServerRequest *> finished;
     std::vector<long long> newly_done;
-    ChebPlan plan;
-    bool plan_dirty = true;
-    int parity = 0;
+    ServerGroup groups[kServerGroups];
     long long next_id = 1;
-    double *pops = nullptr;
-    size_t pops_cap = 0;
     long long steps_done = 0;
 };
 
@@ -3352,7 +3365,14 @@ static int server_admit(elhl_server *sv, ServerRequest *r) {
         return rc;
     std::lock_guard<std::mutex> lk(g_ctx.mu);
     elhl_traj *tr = r->tr;
-    tr->cs.parity = sv->parity;  // join the running batch's column roles
+    if (tr->cs.gemm) {
+        r->group = -1;  // many columns on a large basis: one GEMM per order, its own step graph
+    } else {
+        const int mg = cheb_group_size(tr->cfg.precision, 4, tr->ld);
+        if (!mg) return ELHL_ERR_UNSUPPORTED;  // the vector does not fit in shared memory
+        r->group = mg == 4 ? 0 : mg == 2 ? 1 : 2;
+        tr->cs.parity = sv->groups[r->group].parity;  // join the running group's column roles
+    }
     if (!r->restart.empty())
         if (int rc = traj_restore_impl(tr, r->restart.c_str())) return rc;
     if (!tr->cs.cols_current)
@@ -3449,47 +3469,65 @@ int elhl_server_step(elhl_server *sv, int *n_active, int *n_pending) {
         }
         sv->used += r->bytes;
         sv->active.push_back(r);
-        sv->plan_dirty = true;
+        if (r->group >= 0) {
+            sv->groups[r->group].reqs.push_back(r);
+            sv->groups[r->group].dirty = true;
+        }
     }
     if (!sv->active.empty()) {
         std::lock_guard<std::mutex> lk(g_ctx.mu);
         cudaStream_t st = g_ctx.stream;
-        if (sv->plan_dirty) {
+        // one cooperative launch per non-empty group, one step graph per GEMM-regime request
+        for (auto &g : sv->groups) {
+            if (g.reqs.empty()) continue;
             std::vector<ChebState *> states;
-            for (auto *r : sv->active) states.push_back(&r->tr->cs);
-            if (int rc = cheb_plan(sv->plan, states)) return rc;
-            sv->plan_dirty = false;
+            for (auto *r : g.reqs) states.push_back(&r->tr->cs);
+            if (g.dirty) {
+                if (int rc = cheb_plan(g.plan, states)) return rc;
+                if (!g.plan.mg_read) return ELHL_ERR_UNSUPPORTED;
+                g.dirty = false;
+            }
+            size_t need = 0;
+            for (auto *r : g.reqs) {
+                r->pops_off = need;
+                need += (size_t)r->P * (r->nfrag + 1);
+            }
+            if (need > g.pops_cap) {
+                dev_free(g.pops);
+                if (int rc = dev_alloc(&g.pops, need)) return rc;
+                g.pops_cap = need;
+            }
+            CU_TRY(cudaMemsetAsync(g.plan.d_drift, 0, g.reqs.size() * sizeof(double), st));
+            if (int rc = cheb_dev_step(g.plan, states, g.pops)) return rc;
+            g.parity = g.plan.parity;
         }
-        size_t need = 0;
-        for (auto *r : sv->active) need += (size_t)r->P * (r->nfrag + 1);
-        if (need > sv->pops_cap) {
-            dev_free(sv->pops);
-            if (int rc = dev_alloc(&sv->pops, need)) return rc;
-            sv->pops_cap = need;
+        for (auto *r : sv->active) {
+            if (r->group >= 0) continue;
+            CU_TRY(cudaMemsetAsync(r->tr->cs.drift, 0, sizeof(double), st));
+            if (int rc = cheb_gemm_step(r->tr->cs)) return rc;
         }
-        std::vector<ChebState *> states;
-        for (auto *r : sv->active) states.push_back(&r->tr->cs);
-        if (!sv->plan.mg_read) return ELHL_ERR_UNSUPPORTED;
-        CU_TRY(cudaMemsetAsync(sv->plan.d_drift, 0, sv->active.size() * sizeof(double), st));
-        if (int rc = cheb_dev_step(sv->plan, states, sv->pops)) return rc;
-        sv->parity = sv->plan.parity;
         std::vector<ChebState *> leaving;
         for (auto *r : sv->active)
             if (r->done_steps + 1 >= r->nsteps) leaving.push_back(&r->tr->cs);
         if (!leaving.empty())
             if (int rc = cheb_settle(leaving)) return rc;
-        size_t off = 0;
         int err = 0;
         std::vector<double> drift(sv->active.size(), 0.0);
         CU_TRY(cudaMemcpyAsync(&err, g_ctx.err, sizeof(int), cudaMemcpyDeviceToHost, st));
-        CU_TRY(cudaMemcpyAsync(drift.data(), sv->plan.d_drift, drift.size() * sizeof(double), cudaMemcpyDeviceToHost,
-                               st));
+        for (size_t q = 0; q < sv->active.size(); ++q) {
+            const ServerRequest *r = sv->active[q];
+            const double *d = r->group < 0 ? r->tr->cs.drift : sv->groups[r->group].plan.d_drift;
+            if (r->group >= 0) {
+                const auto &reqs = sv->groups[r->group].reqs;
+                d += std::find(reqs.begin(), reqs.end(), r) - reqs.begin();
+            }
+            CU_TRY(cudaMemcpyAsync(&drift[q], d, sizeof(double), cudaMemcpyDeviceToHost, st));
+        }
         CU_TRY(cudaStreamSynchronize(st));
         if (err) return err;
         sv->steps_done += (long long)sv->active.size();
         // retire finished requests, and requests whose step failed the norm control
         // (status ELHL_ERR_NO_CONVERGENCE, results as of that step)
-        off = 0;
         std::vector<ServerRequest *> keep;
         for (size_t q = 0; q < sv->active.size(); ++q) {
             ServerRequest *r = sv->active[q];
@@ -3501,7 +3539,8 @@ int elhl_server_step(elhl_server *sv, int *n_active, int *n_pending) {
             if (!(drift[q] <= cheb_norm_tolerance(r->tr->cfg))) r->status = ELHL_ERR_NO_CONVERGENCE;
             if (r->done_steps >= r->nsteps || r->status) {
                 r->pops.resize(np);
-                CU_TRY(copy_d2h(r->pops.data(), sv->pops + off, np * sizeof(double)));
+                const double *src = r->group < 0 ? r->tr->cs.gpops : sv->groups[r->group].pops + r->pops_off;
+                CU_TRY(copy_d2h(r->pops.data(), src, np * sizeof(double)));
                 r->psi.resize((size_t)r->nao * r->P);
                 const size_t e = sizeof(double2);
                 for (int p = 0; p < r->P; ++p)
@@ -3509,13 +3548,16 @@ int elhl_server_step(elhl_server *sv, int *n_active, int *n_pending) {
                                         cudaMemcpyDeviceToHost));
                 r->t_done = now_s();
                 sv->used -= r->bytes;
-                sv->plan_dirty = true;
+                if (r->group >= 0) {
+                    auto &g = sv->groups[r->group];
+                    g.reqs.erase(std::find(g.reqs.begin(), g.reqs.end(), r));
+                    g.dirty = true;
+                }
                 sv->finished[r->id] = r;
                 sv->newly_done.push_back(r->id);
             } else {
                 keep.push_back(r);
             }
-            off += np;
         }
         sv->active.swap(keep);
     }
@@ -3574,8 +3616,10 @@ int elhl_server_destroy(elhl_server *sv) {
     }
     {
         std::lock_guard<std::mutex> lk(g_ctx.mu);
-        sv->plan.release();
-        dev_free(sv->pops);
+        for (auto &g : sv->groups) {
+            g.plan.release();
+            dev_free(g.pops);
+        }
     }
     delete sv;
     return ELHL_OK;

@@ -136,6 +136,7 @@ struct ChebLaunch {
     // the rows over the CTAs (the triangular phases use segs: mirrored chunk pairs)
     const ChebSegment *segs_full;
     const int *seg_full_begin;  // [grid + 1]
+    int jwin;                   // explicit Hs: vector window in rows (0: the whole vector); set by the launcher
     // failure-detection test hook (elhl_debug_barrier): grid-barrier limit in ns
     // (0: the default 5 s) and 1 + the CTA that leaves before its first grid
     // barrier (0: none, so a zero-initialised launch has no hook)
@@ -146,7 +147,9 @@ constexpr size_t kCheb_part_bytes = 16 * 64 * sizeof(double);  // cross-warp par
 constexpr size_t kCheb_smem_limit = 200 * 1024;
 int cheb_block();
 int cheb_grid_size(int *grid_out);
-int cheb_group_size(int precision, int m, int max_ld);  // columns staged per pass, 0 = unsupported
+// columns staged per pass, 0 = unsupported; windowed: the explicit propagation,
+// which stages the vector in windows when it does not fit in shared memory
+int cheb_group_size(int precision, int m, int max_ld, bool windowed = false);
 cudaError_t launch_cheb(const ChebLaunch &L, int precision, int mg, cudaStream_t st);
 cudaError_t launch_readout(const ChebLaunch &L, int nprob, int precision, int mg, cudaStream_t st);
 

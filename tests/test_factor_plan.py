@@ -190,3 +190,60 @@ def test_dgemm_tiles_cover_the_triangular_products(m, n, k, case):
         assert np.abs((C - ref)[mask]).max() < 1e-10
     else:
         assert np.abs(C - ref).max() < 1e-10
+
+
+CHEB = open(os.path.join(ROOT, "dynemol_gb300", "csrc", "cheb.cu")).read()
+CBLOCK, YROWS = _const(CHEB, "kBlock"), _const(CHEB, "kYRows")
+SMEM_LIMIT = 200 * 1024
+PART_BYTES = 16 * 64 * 8
+
+
+def _jwin(ld, mg, c2):
+    """The launcher's window (explicit Hs) when the whole vector does not fit."""
+    if PART_BYTES + ld * mg * c2 <= SMEM_LIMIT:
+        return 0
+    return ((SMEM_LIMIT - PART_BYTES - YROWS * mg * c2) // (mg * c2)) & ~31
+
+
+@pytest.mark.parametrize("n,mg,c2,krt", [(15553, 4, 8, 8), (15553, 1, 8, 8), (9000, 2, 8, 8), (4000, 4, 16, 2),
+                                          (12001, 4, 16, 2), (3000, 4, 8, 8)])
+def test_windowed_rows_cover_the_matrix_once(n, mg, c2, krt):
+    """order_rows + rows_gemv (cheb.cu) with the vector staged in windows: every
+    (row, j) of a segment is summed exactly once, every 16-byte vector stays in
+    its window, and the window and partial-sum arrays fit the shared memory."""
+    assert "rows_gemv<T, MG, 0>(reinterpret_cast<const T *>(pb.H), ld, s_v, r0, r1, s_part, acc_epi, jw0, jw1)" in CHEB
+    ld = ru(n, 32)
+    jwin = _jwin(ld, mg, c2)
+    warps = CBLOCK // 32
+    ve = 16 // (c2 // 2)  # elements per 16-byte load
+    if jwin:
+        assert PART_BYTES + jwin * mg * c2 + YROWS * mg * c2 <= SMEM_LIMIT and jwin % 32 == 0
+    for row0, row1 in [(0, 37), (n - 700, n), (1000, 1000 + YROWS + 5)]:
+        row1 = min(row1, n)
+        count = np.zeros((row1 - row0, ld), np.int32)
+        blocks = [(r, min(row1, r + YROWS)) for r in range(row0, row1, YROWS)] if jwin else [(row0, row1)]
+        for r0, r1 in blocks:
+            assert r1 - r0 <= YROWS or not jwin
+            windows = [(w, min(ld, w + jwin)) for w in range(0, ld, jwin)] if jwin else [(0, ld)]
+            for jw0, jw1 in windows:
+                rows = r1 - r0
+                WR = 1
+                while WR < warps and WR * krt < rows:
+                    WR <<= 1
+                WJ = warps // WR
+                for base in range(r0, r1, krt * WR):
+                    jlo, jhi = max(jw0, 0), min(jw1, ld)
+                    jchunk = ((jhi - jlo + WJ - 1) // WJ + 31) // 32 * 32
+                    for wr in range(WR):
+                        rr0 = base + krt * wr
+                        nr = min(krt, r1 - rr0)
+                        if nr <= 0:
+                            continue
+                        for wj in range(WJ):
+                            j0 = jlo + wj * jchunk
+                            j1 = min(jhi, j0 + jchunk)
+                            for jv in range(j0, j1, ve):  # one lane's vector: [jv, jv + ve)
+                                assert jv + ve <= j1 and jv - jw0 >= 0 and jv + ve - jw0 <= jwin + (0 if jwin else ld)
+                            if j1 > j0:
+                                count[rr0 - row0:rr0 - row0 + nr, j0:j1] += 1
+        assert (count == 1).all(), (n, mg, row0, row1)
