@@ -467,8 +467,11 @@ __global__ void __launch_bounds__(kBlock, 1) readout_kernel(ChebLaunch L) {
 
 // one block per problem: sum its segments' partials in order -> populations of
 // this step.  Reduced precision: the renormalisation factor s = sqrt(target /
-// total) for the next step, and the populations reported are those of the
-// renormalised state the trajectory carries on with (each times s^2).
+// total) for the next step, with the total from the propagated columns in FP64
+// (pb.ntot; a total from the read-out, whose matrices are in the launch
+// precision, carries about 1e-7 of noise that renormalising every step would
+// turn into a random walk of the norm), and the populations reported are those
+// of the renormalised state the trajectory carries on with (each times s^2).
 __global__ void reduce_pops_kernel(ChebLaunch L, int nprob) {
     const int q = blockIdx.x;
     if (q >= nprob) return;
@@ -478,8 +481,12 @@ __global__ void reduce_pops_kernel(ChebLaunch L, int nprob) {
     __shared__ double s2[kMaxCols];  // population factor s^2 per particle
     for (int p = threadIdx.x; p < P; p += blockDim.x) {
         double tot = 0.0;
-        for (int s = L.prob_seg0[q]; s < L.prob_seg0[q + 1]; ++s)
-            tot += L.seg_pops[(size_t)s * kMaxCols * (kMaxFrag + 1) + p * (kMaxFrag + 1) + nf];
+        if (pb.ntot) {
+            tot = pb.ntot[p];  // FP64 from the propagated columns, not the read-out in the launch precision
+        } else {
+            for (int s = L.prob_seg0[q]; s < L.prob_seg0[q + 1]; ++s)
+                tot += L.seg_pops[(size_t)s * kMaxCols * (kMaxFrag + 1) + p * (kMaxFrag + 1) + nf];
+        }
         const double tgt = pb.target ? pb.target[p] : 0.0;
         const bool rn = pb.scale_out && tot > 0.0 && tgt > 0.0;
         if (pb.scale_out) pb.scale_out[p] = rn ? sqrt(tgt / tot) : 1.0;

@@ -627,6 +627,7 @@ struct ChebState {
     bool readout_ready = false, cols_current = false;
     double *scale = nullptr;   // [P] pending renormalisation factor (reduced precision), 1 otherwise
     double *drift = nullptr;   // norm drift word of the GEMM-regime step (plans keep their own)
+    double *ntot = nullptr;    // [kMaxCols] FP64 totals of the last step's columns (renormalisation)
     double2 *saved = nullptr;  // [ld][m] input columns at the start of a call, for redone steps
     double guard = 0.01;       // Lanczos interval guard, fraction of the width
     // read-out outputs, owned by the trajectory
@@ -685,6 +686,7 @@ struct ChebState {
         if (int rc = dev_alloc(&cscratch, (size_t)2 * m * ld)) return rc;
         if (int rc = dev_alloc(&scale, (size_t)kMaxCols)) return rc;
         if (int rc = dev_alloc(&drift, 1)) return rc;
+        if (int rc = dev_alloc(&ntot, (size_t)kMaxCols)) return rc;
         CU_TRY(cudaMemset(drift, 0, sizeof(double)));
         std::vector<double> ones(kMaxCols, 1.0);
         CU_TRY(copy_h2d(scale, ones.data(), kMaxCols * sizeof(double)));
@@ -713,7 +715,7 @@ struct ChebState {
         implicit = false;
         dev_free(gpops);
         dev_free(Ht); dev_free(phi); dev_free(acc); dev_free(coef); dev_free(lz); dev_free(scale);
-        dev_free(drift); dev_free(saved);
+        dev_free(drift); dev_free(saved); dev_free(ntot);
         if (Hs) cudaFree(Hs);
         if (vbuf) cudaFree(vbuf);
         if (A) cudaFree(A);
@@ -1138,6 +1140,38 @@ __global__ void __launch_bounds__(kDriftBlock) norm_drift_cols_kernel(const doub
     drift_column(in, out, n, m, c, s * s, drift);
 }
 
+// Total population of particle p after a step, in FP64 from the propagated
+// columns of the symmetrised basis: |phi_p|^2 for ket-only problems (m = P),
+// Re <phi_p|chi_p> with bra columns (m = 2P); one block per (problem, particle),
+// fixed-order sums.
+__device__ void total_column(const double2 *__restrict__ out, int n, int m, int P, int p, double *dst) {
+    __shared__ double r[kDriftBlock];
+    double a = 0.0;
+    for (int i = threadIdx.x; i < n; i += kDriftBlock) {
+        const double2 x = out[(size_t)i * m + p];
+        const double2 y = m == 2 * P ? out[(size_t)i * m + P + p] : x;
+        a += x.x * y.x + x.y * y.y;
+    }
+    r[threadIdx.x] = a;
+    __syncthreads();
+    for (int o = kDriftBlock / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) r[threadIdx.x] += r[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *dst = r[0];
+}
+
+__global__ void __launch_bounds__(kDriftBlock) norm_total_kernel(const ChebProblem *probs, int parity) {
+    const ChebProblem &pb = probs[blockIdx.x];
+    if (!pb.ntot || (int)blockIdx.y >= pb.P) return;
+    total_column(pb.col[parity ^ 1], pb.N, pb.m, pb.P, blockIdx.y, pb.ntot + blockIdx.y);
+}
+
+__global__ void __launch_bounds__(kDriftBlock) norm_total_cols_kernel(const double2 *out, int n, int m, int P,
+                                                                      double *ntot) {
+    total_column(out, n, m, P, blockIdx.x, ntot + blockIdx.x);
+}
+
 // ---- GEMM regime kernels (complex columns [ld][m], element-wise) -------------
 __global__ void gemm_order0_kernel(const double2 *__restrict__ phi, const double *__restrict__ scale, int P, int n,
                                    int m, double2 c0, float2 *__restrict__ v0, double2 *__restrict__ acc) {
@@ -1189,12 +1223,14 @@ __global__ void to_double2_kernel(const float2 *__restrict__ src, double2 *__res
     if (q < nm) dst[q] = make_double2((double)src[q].x, (double)src[q].y);
 }
 
-// renormalisation factor s = sqrt(target / total) for the next step; the
-// populations become those of the renormalised state (each times s^2)
-__global__ void scale_from_pops_kernel(double *pops, int P, int nfrag, const double *target, double *scale) {
+// renormalisation factor s = sqrt(target / total) for the next step, the total
+// in FP64 from the propagated columns (ntot); the populations become those of
+// the renormalised state (each times s^2)
+__global__ void scale_from_pops_kernel(double *pops, int P, int nfrag, const double *target, const double *ntot,
+                                       double *scale) {
     const int p = threadIdx.x;
     if (p < P) {
-        const double tot = pops[(size_t)p * (nfrag + 1) + nfrag];
+        const double tot = ntot[p];
         const bool rn = tot > 0.0 && target[p] > 0.0;
         scale[p] = rn ? sqrt(target[p] / tot) : 1.0;
         if (rn)
@@ -1245,6 +1281,8 @@ int cheb_gemm_enqueue(ChebState &cs, int parity) {
     }
     norm_drift_cols_kernel<<<m, kDriftBlock, 0, st>>>(in, out, n, m, cs.P, renorm ? cs.scale : nullptr, cs.drift);
     count_launch();
+    norm_total_cols_kernel<<<cs.P, kDriftBlock, 0, st>>>(out, n, m, cs.P, cs.ntot);
+    count_launch();
     to_float2_kernel<<<nb, tb, 0, st>>>(out, reinterpret_cast<float2 *>(cs.Vf), nm);
     count_launch();
     if (int rc = gemm_vt(g_ctx.blas_tc, cs.precision, 2 * m, n, cs.Vf, reinterpret_cast<const float *>(cs.A), cs.ld,
@@ -1259,7 +1297,7 @@ int cheb_gemm_enqueue(ChebState &cs, int parity) {
     count_launch();
     populations_kernel<<<cs.P, 256, 0, st>>>(cs.psi_out, cs.bra_out, n, cs.P, cs.ao_frag, cs.nfrag, cs.gpops);
     count_launch();
-    scale_from_pops_kernel<<<1, kMaxCols, 0, st>>>(cs.gpops, cs.P, cs.nfrag, cs.target, cs.scale);
+    scale_from_pops_kernel<<<1, kMaxCols, 0, st>>>(cs.gpops, cs.P, cs.nfrag, cs.target, cs.ntot, cs.scale);
     count_launch();
     CU_TRY(cudaGetLastError());
     return ELHL_OK;
@@ -1370,6 +1408,7 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
         p.scale = renorm ? cs->scale : nullptr;
         p.scale_out = renorm ? cs->scale : nullptr;
         p.target = renorm ? cs->target : nullptr;
+        p.ntot = renorm ? cs->ntot : nullptr;
         if (cs->implicit) {
             p.G = cs->A;
             p.Gt = cs->Gt;
@@ -1584,6 +1623,17 @@ int launch_norm_drift(const ChebPlan &pl) {
     for (const auto &p : pl.probs) mmax = std::max(mmax, p.m);
     norm_drift_kernel<<<dim3((unsigned)pl.probs.size(), mmax), kDriftBlock, 0, g_ctx.stream>>>(pl.d_probs, pl.parity);
     count_launch();
+    bool totals = false;
+    int pmax = 0;
+    for (const auto &p : pl.probs) {
+        totals |= p.ntot != nullptr;
+        pmax = std::max(pmax, p.P);
+    }
+    if (totals) {
+        norm_total_kernel<<<dim3((unsigned)pl.probs.size(), pmax), kDriftBlock, 0, g_ctx.stream>>>(pl.d_probs,
+                                                                                                    pl.parity);
+        count_launch();
+    }
     CU_TRY(cudaGetLastError());
     return ELHL_OK;
 }

@@ -117,6 +117,8 @@ struct ChebProblem {
     void *wb;               // [2][m/MG][ldv][MG] launch precision: w = G^T v, y = (h/b) w
     double shift;           // a / b
     double *drift;          // largest relative change of a column's squared norm over a step (norm control)
+    double *ntot;           // [P] total population of each particle after the step, in FP64 from the
+                            // propagated columns (reduced precision: the renormalisation divides by it)
 };
 struct ChebSegment {
     int prob, row0, row1;   // rows [row0, row1) of problem `prob` owned by one CTA
