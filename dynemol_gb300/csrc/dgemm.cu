@@ -53,7 +53,12 @@ __global__ void __launch_bounds__(kThreads) dgemm_kernel(int m, int n, int k, do
     __shared__ double As[2][kBK][kBM + 1];
     __shared__ double Bs[2][kBK][kBN + 1];
     const int tid = threadIdx.x;
-    const int i0 = blockIdx.x * kBM, j0 = blockIdx.y * kBN;
+    // blocks start roughly in index order: the tiles with the longest k range
+    // (kTriA: the last row tiles; kTriBt: the last column tiles) go first, so
+    // that the last wave holds the short ones
+    const int bx = (tri & kTriA) ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+    const int by = (tri & kTriBt) ? gridDim.y - 1 - blockIdx.y : blockIdx.y;
+    const int i0 = bx * kBM, j0 = by * kBN;
     if ((tri & kTriLowerC) && i0 + kBM <= j0) return;  // tile strictly above the diagonal
     // k range holding non-zero products for this tile
     int klo = 0, khi = k;
@@ -131,7 +136,7 @@ __global__ void __launch_bounds__(kThreads) dgemm_kernel(int m, int n, int k, do
         return;
     }
     // split K: partial tile out, then the last CTA of the tile sums the splits in order
-    const int S = gridDim.z, tile = blockIdx.y * gridDim.x + blockIdx.x;
+    const int S = gridDim.z, tile = by * gridDim.x + bx;
     double *mine = part + ((size_t)tile * S + blockIdx.z) * (kBM * kBN);
 #pragma unroll
     for (int q = 0; q < kTM; ++q)
