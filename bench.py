@@ -390,6 +390,49 @@ def run_dropin(args, steps: int = 2):
             "propagation_ms_per_step": st.prop_ms / steps, "rebuild_ms_per_step": st.rebuild_ms / steps}
 
 
+def run_dropin_host(args, steps: int = 3):
+    """The drop-in as the reference's Fortran host calls it: per nuclear step one
+    propagationelhl_gpucaller_ call per particle (electron, hole) with host S, h
+    (column-major N x N), H' out and Psi in/out (Taylor_gpu.cpp:634-736;
+    ElHl_Chebyshev_GPU.f:269-272), on the workload's geometries.  S and h of each
+    step come from the library's own device build at that geometry, outside the
+    timed region, as the reference builds them on the host before the call."""
+    from dynemol_gb300 import api, systems
+    sysm, dt, moving = workload(args.workload)
+    homo = systems.fermi_state(sysm, np.arange(20))
+    coords = step_coords(sysm, moving, steps + 2)
+    tr = api.Trajectory(sysm, coords=None if coords is None else coords[0], dt=dt, method=api.METHOD_CHEBYSHEV,
+                        precision=api.PREC_FP64, ncols=4, cheb_tol=1e-12)
+    tr.init_fmo(homo + 1, homo)
+    bra, ket = tr.get_psi()
+    mats = []
+    for i in range(steps + 1):
+        if coords is not None:
+            tr.step(coords[1 + i: 2 + i], nsteps=1, want_pops=False)
+        S, h, _ = tr.matrices()
+        mats.append((np.asfortranarray(S), np.asfortranarray(h)))
+    tr.close()
+    N = sysm.nao
+    bra = [np.ascontiguousarray(bra[:, p]) for p in range(2)]
+    ket = [np.ascontiguousarray(ket[:, p]) for p in range(2)]
+    tau_max = dt / H_BAR
+    save = [tau_max, tau_max]
+    t_timed = 0.0
+    for s in range(steps + 1):  # one untimed step, then `steps` timed
+        S, h = mats[s]
+        t0 = time.perf_counter()
+        for p in range(2):
+            tau = tau_max if s == 0 else min(1.15 * save[p], tau_max)
+            *_, save[p] = api.propagationelhl_gpucaller(S, h, bra[p], ket[p], s * dt, (s + 1) * dt, tau)
+        if s:
+            t_timed += time.perf_counter() - t0
+    return {"steps_per_s": steps / t_timed, "steps": steps, "N_ao": N,
+            "h2d_bytes_per_step": 2 * (2 * N * N * 8 + 2 * N * 16),
+            "d2h_bytes_per_step": 2 * (N * N * 8 + 3 * N * 16),
+            "path": "propagationelhl_gpucaller_ with host buffers, electron and hole one call each per step "
+                    "(S^-1 h by the library's FP64 Cholesky with inverse, adaptive-tau Taylor)"}
+
+
 # ----------------------------------------------------------------- CPU sample
 def cpu_sample(args, sysm, dt, moving, nsteps, nthreads):
     """Oracle port timed on the host cores: `nsteps` nuclear steps after one untimed step."""
@@ -754,10 +797,10 @@ def main():
                     "of this many trajectories (0 = skip)")
     ap.add_argument("--served-mix", type=int, default=512, help="trajectories of the served mix (0 = skip)")
     ap.add_argument("--served-steps", type=int, default=200, help="steps of each served-mix trajectory")
-    ap.add_argument("--config5", type=int, default=12, help="requests of the bounded serving sample (0 = skip)")
+    ap.add_argument("--config5", type=int, default=6, help="requests of the bounded serving sample (0 = skip)")
     ap.add_argument("--no-dropin", action="store_true", help="skip the Taylor drop-in measurement")
     ap.add_argument("--serve", type=int, default=0, help="also run a serving stream of this many requests")
-    ap.add_argument("--precision-study", action="store_true", help="also run the N = 8192, 64-column study")
+    ap.add_argument("--no-precision-study", action="store_true", help="skip the N = 8192, 64-column study")
     args = ap.parse_args()
     if args.warmup < 3 and args.impl == "ours":
         args.warmup = 3
@@ -778,6 +821,7 @@ def main():
         line["df64_variant"] = run_variant(args, "df64")
     if rank == 0 and args.method == "chebyshev" and not args.no_dropin:
         line["dropin_taylor_fp64"] = run_dropin(args)
+        line["dropin_host_fp64"] = run_dropin_host(args)
     if rank == 0 and args.mix:
         from dynemol_gb300 import api
         line["trajectory_mix"] = run_mix(args, args.mix, steps=5, warm=2, precision=api.PREC_FP32,
@@ -786,7 +830,7 @@ def main():
         line["served_mix"] = run_served_mix(args, args.served_mix, args.served_steps)
     if rank == 0 and args.config5:
         line["serving_config5"] = run_config5(args, args.config5)
-    if rank == 0 and args.precision_study:
+    if rank == 0 and not args.no_precision_study:
         line["precision_study"] = run_precision_study(args)
     if rank == 0 and args.serve:
         from dynemol_gb300 import api
