@@ -16,10 +16,13 @@
 // there, and k tiles that are zero for the whole output tile are skipped, so a
 // triangular product costs half a square one.  With kTriLowerC only output
 // tiles that reach the diagonal or below it are written (a symmetric update).
-// Products with fewer tiles than SMs split K over gridDim.z CTAs per tile: each
-// writes its partial tile to a workspace, and the CTA that arrives last at the
-// tile's counter sums the partials in split order (deterministic) and writes C;
-// no CTA waits.
+// Work is scheduled dynamically: the FP64 pipe is saturated while a CTA runs
+// (ncu: 99.6 % of its active cycles on the top-level product of an N = 2790
+// factorisation), so what costs time is SMs left idle when the tiles of a
+// triangular product (k ranges from one k tile to all of them) are dealt out
+// statically.  Persistent CTAs pull (tile, k-chunk) units from a counter; a
+// tile split into chunks is summed by its last arriving unit in chunk order
+// (deterministic); no CTA waits.
 #include <algorithm>
 
 #include "elhl_internal.cuh"
@@ -31,10 +34,12 @@ constexpr int kBM = 64, kBN = 64, kBK = 16;
 constexpr int kTM = 4, kTN = 4;
 constexpr int kRT = kBM / kTM, kCT = kBN / kTN;  // threads along rows and columns
 constexpr int kThreads = kRT * kCT;
-constexpr int kMaxPartials = 1024;     // tiles x splits held by the split-K workspace
-constexpr int kSplitBelowTiles = 152;  // one tile per SM
-double *g_part = nullptr;              // [tile][split][kBM * kBN]
+constexpr int kMaxPartials = 4096;     // partial tiles held by the workspace (128 MB)
+constexpr int kUnitsPerSlot = 6;       // work units per resident CTA the chunk length aims at
+double *g_part = nullptr;              // [tile * chunks + chunk][kBM * kBN]
 int *g_count = nullptr;                // [tile] arrivals, back to 0 after each fix-up
+int *g_sched = nullptr;                // [2]: next unit, CTAs finished; back to 0 after each launch
+int g_slots = 0;                       // resident CTAs of the whole GPU
 
 __device__ __forceinline__ void cp_async8(double *dst, const double *src, int src_bytes) {
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -44,125 +49,158 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
+struct DgemmArgs {
+    int m, n, k;
+    double alpha, beta;
+    const double *A, *B;
+    double *C;
+    int lda, ldb, ldc, tri;
+    int gx, gy;        // output tiles along rows and columns
+    int chunk;         // k tiles per work unit
+    int nchunk;        // chunks of the longest k range (units per tile)
+    long long units;   // gx * gy * nchunk
+    double *part;
+    int *count, *sched;
+};
+
+// Persistent CTAs pull work units u = (tile, k-chunk) from an atomic counter:
+// the FP64 pipe of every SM stays busy until the last units, whatever the
+// mix of long and short (triangular) k ranges.  A tile with one chunk writes C
+// directly; otherwise each chunk writes its partial tile and the unit arriving
+// last at the tile's counter sums the partials in chunk order (deterministic)
+// and writes C.  The last CTA to finish resets the counter for the next launch.
 template <bool TA, bool TB>
-__global__ void __launch_bounds__(kThreads) dgemm_kernel(int m, int n, int k, double alpha,
-                                                         const double *__restrict__ A, int lda,
-                                                         const double *__restrict__ B, int ldb, double beta,
-                                                         double *__restrict__ C, int ldc, int tri,
-                                                         double *__restrict__ part, int *__restrict__ count) {
+__global__ void __launch_bounds__(kThreads) dgemm_kernel(const DgemmArgs g) {
     __shared__ double As[2][kBK][kBM + 1];
     __shared__ double Bs[2][kBK][kBN + 1];
-    const int tid = threadIdx.x;
-    // blocks start roughly in index order: the tiles with the longest k range
-    // (kTriA: the last row tiles; kTriBt: the last column tiles) go first, so
-    // that the last wave holds the short ones
-    const int bx = (tri & kTriA) ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
-    const int by = (tri & kTriBt) ? gridDim.y - 1 - blockIdx.y : blockIdx.y;
-    const int i0 = bx * kBM, j0 = by * kBN;
-    if ((tri & kTriLowerC) && i0 + kBM <= j0) return;  // tile strictly above the diagonal
-    // k range holding non-zero products for this tile
-    int klo = 0, khi = k;
-    if (tri & kTriA) khi = min(khi, i0 + kBM);   // op(A)(i, l) = A(i, l) = 0 for l > i
-    if (tri & kTriAt) klo = max(klo, i0);        // op(A)(i, l) = A(l, i) = 0 for l < i
-    if (tri & kTriB) klo = max(klo, j0);         // op(B)(l, j) = B(l, j) = 0 for l < j
-    if (tri & kTriBt) khi = min(khi, j0 + kBN);  // op(B)(l, j) = B(j, l) = 0 for l > j
-    {  // this split's share of the tile's k tiles
-        const int S = gridDim.z, z = blockIdx.z;
-        const int nkt = khi > klo ? (khi - klo + kBK - 1) / kBK : 0;
-        const int kt0 = z * nkt / S, kt1 = (z + 1) * nkt / S;
-        khi = min(khi, klo + kt1 * kBK);
-        klo += kt0 * kBK;
-    }
+    __shared__ long long s_unit;
+    __shared__ int s_last;
+    const int tid = threadIdx.x, tri = g.tri, m = g.m, n = g.n, k = g.k;
+    const double *__restrict__ A = g.A;
+    const double *__restrict__ B = g.B;
     const int tr = tid % kRT, tc = tid / kRT;  // outputs: rows i0 + tr + kRT q, columns j0 + tc + kCT p
-    double acc[kTM][kTN];
-#pragma unroll
-    for (int q = 0; q < kTM; ++q)
-#pragma unroll
-        for (int p = 0; p < kTN; ++p) acc[q][p] = 0.0;
-    // stage s <- the k tile at k0, threads along each operand's contiguous index;
-    // masked elements are zero-filled from an in-bounds address
-    auto fetch = [&](int s, int k0) {
-        for (int t = tid; t < kBM * kBK; t += kThreads) {
-            const int ii = TA ? t / kBK : t % kBM, kk = TA ? t % kBK : t / kBM;
-            const int gi = i0 + ii, gk = k0 + kk;
-            const bool nz = gi < m && gk < k && !((tri & kTriA) && gk > gi) && !((tri & kTriAt) && gk < gi);
-            const double *src = TA ? A + (size_t)gi * lda + gk : A + (size_t)gk * lda + gi;
-            cp_async8(&As[s][kk][ii], nz ? src : A, nz ? 8 : 0);
-        }
-        for (int t = tid; t < kBK * kBN; t += kThreads) {
-            const int kk = TB ? t / kBN : t % kBK, jj = TB ? t % kBN : t / kBK;
-            const int gk = k0 + kk, gj = j0 + jj;
-            const bool nz = gk < k && gj < n && !((tri & kTriB) && gk < gj) && !((tri & kTriBt) && gk > gj);
-            const double *src = TB ? B + (size_t)gk * ldb + gj : B + (size_t)gj * ldb + gk;
-            cp_async8(&Bs[s][kk][jj], nz ? src : B, nz ? 8 : 0);
-        }
-        cp_async_commit();
-    };
-    if (klo < khi) fetch(0, klo);
-    int s = 0;
-    for (int k0 = klo; k0 < khi; k0 += kBK, s ^= 1) {
-        if (k0 + kBK < khi) {
-            fetch(s ^ 1, k0 + kBK);
-            cp_async_wait<1>();  // this tile's group is complete, the next one may be in flight
-        } else {
-            cp_async_wait<0>();
-        }
+    for (;;) {
+        if (tid == 0) s_unit = atomicAdd(reinterpret_cast<unsigned long long *>(g.sched), 1ull);
         __syncthreads();
+        const long long u = s_unit;
+        __syncthreads();  // s_unit is rewritten by the next fetch
+        if (u >= g.units) break;
+        const int t = (int)(u / g.nchunk), ch = (int)(u % g.nchunk);
+        // tiles with the longest k range (kTriA: the last row tiles; kTriBt: the last
+        // column tiles) come first
+        const int bx0 = t % g.gx, by0 = t / g.gx;
+        const int bx = (tri & kTriA) ? g.gx - 1 - bx0 : bx0;
+        const int by = (tri & kTriBt) ? g.gy - 1 - by0 : by0;
+        const int i0 = bx * kBM, j0 = by * kBN;
+        if ((tri & kTriLowerC) && i0 + kBM <= j0) continue;  // tile strictly above the diagonal
+        // k range holding non-zero products for this tile
+        int klo = 0, khi = k;
+        if (tri & kTriA) khi = min(khi, i0 + kBM);   // op(A)(i, l) = A(i, l) = 0 for l > i
+        if (tri & kTriAt) klo = max(klo, i0);        // op(A)(i, l) = A(l, i) = 0 for l < i
+        if (tri & kTriB) klo = max(klo, j0);         // op(B)(l, j) = B(l, j) = 0 for l < j
+        if (tri & kTriBt) khi = min(khi, j0 + kBN);  // op(B)(l, j) = B(j, l) = 0 for l > j
+        const int nkt = khi > klo ? (khi - klo + kBK - 1) / kBK : 0;
+        const int nch = max(1, (nkt + g.chunk - 1) / g.chunk);  // chunks of this tile
+        if (ch >= nch) continue;
+        {  // this chunk's k tiles
+            const int kt0 = ch * g.chunk, kt1 = min(nkt, kt0 + g.chunk);
+            khi = min(khi, klo + kt1 * kBK);
+            klo += kt0 * kBK;
+        }
+        double acc[kTM][kTN];
+#pragma unroll
+        for (int q = 0; q < kTM; ++q)
+#pragma unroll
+            for (int p = 0; p < kTN; ++p) acc[q][p] = 0.0;
+        // stage s <- the k tile at k0, threads along each operand's contiguous index;
+        // masked elements are zero-filled from an in-bounds address
+        auto fetch = [&](int s, int k0) {
+            for (int e = tid; e < kBM * kBK; e += kThreads) {
+                const int ii = TA ? e / kBK : e % kBM, kk = TA ? e % kBK : e / kBM;
+                const int gi = i0 + ii, gk = k0 + kk;
+                const bool nz = gi < m && gk < k && !((tri & kTriA) && gk > gi) && !((tri & kTriAt) && gk < gi);
+                const double *src = TA ? A + (size_t)gi * g.lda + gk : A + (size_t)gk * g.lda + gi;
+                cp_async8(&As[s][kk][ii], nz ? src : A, nz ? 8 : 0);
+            }
+            for (int e = tid; e < kBK * kBN; e += kThreads) {
+                const int kk = TB ? e / kBN : e % kBK, jj = TB ? e % kBN : e / kBK;
+                const int gk = k0 + kk, gj = j0 + jj;
+                const bool nz = gk < k && gj < n && !((tri & kTriB) && gk < gj) && !((tri & kTriBt) && gk > gj);
+                const double *src = TB ? B + (size_t)gk * g.ldb + gj : B + (size_t)gj * g.ldb + gk;
+                cp_async8(&Bs[s][kk][jj], nz ? src : B, nz ? 8 : 0);
+            }
+            cp_async_commit();
+        };
+        if (klo < khi) fetch(0, klo);
+        int s = 0;
+        for (int k0 = klo; k0 < khi; k0 += kBK, s ^= 1) {
+            if (k0 + kBK < khi) {
+                fetch(s ^ 1, k0 + kBK);
+                cp_async_wait<1>();  // this tile's group is complete, the next one may be in flight
+            } else {
+                cp_async_wait<0>();
+            }
+            __syncthreads();
 #pragma unroll 4
-        for (int kk = 0; kk < kBK; ++kk) {
-            double a[kTM], b[kTN];
+            for (int kk = 0; kk < kBK; ++kk) {
+                double a[kTM], b[kTN];
 #pragma unroll
-            for (int q = 0; q < kTM; ++q) a[q] = As[s][kk][tr + kRT * q];
+                for (int q = 0; q < kTM; ++q) a[q] = As[s][kk][tr + kRT * q];
 #pragma unroll
-            for (int p = 0; p < kTN; ++p) b[p] = Bs[s][kk][tc + kCT * p];
+                for (int p = 0; p < kTN; ++p) b[p] = Bs[s][kk][tc + kCT * p];
+#pragma unroll
+                for (int q = 0; q < kTM; ++q)
+#pragma unroll
+                    for (int p = 0; p < kTN; ++p) acc[q][p] = fma(a[q], b[p], acc[q][p]);
+            }
+            __syncthreads();  // stage s is refilled by the next iteration's fetch
+        }
+        if (nch == 1) {
 #pragma unroll
             for (int q = 0; q < kTM; ++q)
 #pragma unroll
-                for (int p = 0; p < kTN; ++p) acc[q][p] = fma(a[q], b[p], acc[q][p]);
+                for (int p = 0; p < kTN; ++p) {
+                    const int gi = i0 + tr + kRT * q, gj = j0 + tc + kCT * p;
+                    if (gi < m && gj < n) {
+                        double *c = g.C + (size_t)gj * g.ldc + gi;
+                        *c = g.beta == 0.0 ? g.alpha * acc[q][p] : fma(g.alpha, acc[q][p], g.beta * *c);
+                    }
+                }
+            continue;
         }
-        __syncthreads();  // stage s is refilled by the next iteration's fetch
-    }
-    if (gridDim.z == 1) {
+        // partial tile out, then the last unit of the tile sums the chunks in order
+        const int tile = by * g.gx + bx;
+        double *mine = g.part + ((size_t)tile * g.nchunk + ch) * (kBM * kBN);
+#pragma unroll
+        for (int q = 0; q < kTM; ++q)
+#pragma unroll
+            for (int p = 0; p < kTN; ++p) mine[(tc + kCT * p) * kBM + tr + kRT * q] = acc[q][p];
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) s_last = atomicAdd(g.count + tile, 1) == nch - 1;
+        __syncthreads();
+        if (!s_last) continue;
+        __threadfence();
+        const double *all = g.part + (size_t)tile * g.nchunk * (kBM * kBN);
 #pragma unroll
         for (int q = 0; q < kTM; ++q)
 #pragma unroll
             for (int p = 0; p < kTN; ++p) {
-                const int gi = i0 + tr + kRT * q, gj = j0 + tc + kCT * p;
+                const int gi = i0 + tr + kRT * q, gj = j0 + tc + kCT * p, e = (tc + kCT * p) * kBM + tr + kRT * q;
+                double sum = __ldcg(all + e);
+                for (int z = 1; z < nch; ++z) sum += __ldcg(all + (size_t)z * (kBM * kBN) + e);
                 if (gi < m && gj < n) {
-                    double *c = C + (size_t)gj * ldc + gi;
-                    *c = beta == 0.0 ? alpha * acc[q][p] : fma(alpha, acc[q][p], beta * *c);
+                    double *c = g.C + (size_t)gj * g.ldc + gi;
+                    *c = g.beta == 0.0 ? g.alpha * sum : fma(g.alpha, sum, g.beta * *c);
                 }
             }
-        return;
+        if (tid == 0) g.count[tile] = 0;
     }
-    // split K: partial tile out, then the last CTA of the tile sums the splits in order
-    const int S = gridDim.z, tile = by * gridDim.x + bx;
-    double *mine = part + ((size_t)tile * S + blockIdx.z) * (kBM * kBN);
-#pragma unroll
-    for (int q = 0; q < kTM; ++q)
-#pragma unroll
-        for (int p = 0; p < kTN; ++p) mine[(tc + kCT * p) * kBM + tr + kRT * q] = acc[q][p];
-    __threadfence();
-    __syncthreads();
-    __shared__ int last;
-    if (tid == 0) last = atomicAdd(count + tile, 1) == S - 1;
-    __syncthreads();
-    if (!last) return;
-    __threadfence();
-    const double *all = part + (size_t)tile * S * (kBM * kBN);
-#pragma unroll
-    for (int q = 0; q < kTM; ++q)
-#pragma unroll
-        for (int p = 0; p < kTN; ++p) {
-            const int gi = i0 + tr + kRT * q, gj = j0 + tc + kCT * p, e = (tc + kCT * p) * kBM + tr + kRT * q;
-            double sum = __ldcg(all + e);
-            for (int z = 1; z < S; ++z) sum += __ldcg(all + (size_t)z * (kBM * kBN) + e);
-            if (gi < m && gj < n) {
-                double *c = C + (size_t)gj * ldc + gi;
-                *c = beta == 0.0 ? alpha * sum : fma(alpha, sum, beta * *c);
-            }
-        }
-    if (tid == 0) count[tile] = 0;
+    // the last CTA out resets the scheduler for the next launch (stream order)
+    if (tid == 0 && atomicAdd(g.sched + 2, 1) == (int)gridDim.x - 1) {
+        *reinterpret_cast<unsigned long long *>(g.sched) = 0ull;
+        g.sched[2] = 0;
+    }
 }
 
 }  // namespace
@@ -171,21 +209,35 @@ cudaError_t dgemm64(int m, int n, int k, double alpha, const double *A, int lda,
                     bool transB, double beta, double *C, int ldc, cudaStream_t st, int tri) {
     if (m <= 0 || n <= 0) return cudaSuccess;
     if (!g_part) {
-        cudaError_t e = cudaMalloc(&g_part, (size_t)kMaxPartials * kBM * kBN * sizeof(double));
-        if (e == cudaSuccess) e = cudaMalloc(&g_count, kMaxPartials * sizeof(int));
-        if (e == cudaSuccess) e = cudaMemset(g_count, 0, kMaxPartials * sizeof(int));
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dgemm_kernel<false, false>, kThreads, 0);
+        if (e == cudaSuccess) e = cudaMalloc(&g_part, (size_t)kMaxPartials * kBM * kBN * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&g_count, (size_t)kMaxPartials * sizeof(int));
+        if (e == cudaSuccess) e = cudaMemset(g_count, 0, (size_t)kMaxPartials * sizeof(int));
+        if (e == cudaSuccess) e = cudaMalloc(&g_sched, 4 * sizeof(int));
+        if (e == cudaSuccess) e = cudaMemset(g_sched, 0, 4 * sizeof(int));
         if (e != cudaSuccess) return e;
+        g_slots = std::max(1, per_sm) * sms;
     }
-    dim3 grid((m + kBM - 1) / kBM, (n + kBN - 1) / kBN);
-    // split K until about two CTAs per SM, at least one k tile per split
-    const int tiles = grid.x * grid.y, ktiles = (k + kBK - 1) / kBK;
-    int splits = 1;
-    if (tiles < kSplitBelowTiles && k > 0)
-        splits = std::max(1, std::min({(2 * kSplitBelowTiles + tiles - 1) / tiles, ktiles, 16, kMaxPartials / tiles}));
-    grid.z = splits;
-#define ELHL_DGEMM(TA_, TB_)                                                                                     \
-    dgemm_kernel<TA_, TB_><<<grid, kThreads, 0, st>>>(m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, g_part, \
-                                                      g_count)
+    DgemmArgs g{m, n, k, alpha, beta, A, B, C, lda, ldb, ldc, tri, (m + kBM - 1) / kBM, (n + kBN - 1) / kBN,
+                1, 1, 0, g_part, g_count, g_sched};
+    const long long tiles = (long long)g.gx * g.gy;
+    const int kt = std::max(1, (k + kBK - 1) / kBK);
+    // chunk length: about kUnitsPerSlot units per resident CTA, whole k ranges when
+    // the tiles alone are enough, and no more partial tiles than the workspace holds
+    long long chunk = (tiles * kt + (long long)kUnitsPerSlot * g_slots - 1) / ((long long)kUnitsPerSlot * g_slots);
+    chunk = std::max(1ll, std::min<long long>(chunk, kt));
+    while (chunk < kt && tiles * ((kt + chunk - 1) / chunk) > kMaxPartials) chunk *= 2;
+    if (chunk >= kt) chunk = kt;
+    g.chunk = (int)chunk;
+    g.nchunk = (kt + g.chunk - 1) / g.chunk;
+    if (g.nchunk > 1 && tiles > kMaxPartials) return cudaErrorInvalidValue;  // never: chunk = kt above
+    g.units = tiles * g.nchunk;
+    const int grid = (int)std::min<long long>(g.units, g_slots);
+#define ELHL_DGEMM(TA_, TB_) dgemm_kernel<TA_, TB_><<<grid, kThreads, 0, st>>>(g)
     if (transA && transB) ELHL_DGEMM(true, true);
     else if (transA) ELHL_DGEMM(true, false);
     else if (transB) ELHL_DGEMM(false, true);

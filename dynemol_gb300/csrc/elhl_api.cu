@@ -991,6 +991,39 @@ int chol_inv_pairs(ChebState &cs, double *Lfac, double *G, int *info, double *W)
     return ELHL_OK;
 }
 
+// Fixed-nuclei set-up of the reduced precisions (FP32, BF16X3), whose operator
+// is rounded to FP32 anyway: L, G = L^-1 and H~ = G h G^T (lower triangle,
+// mirrored) all in double-float pairs on the FP32 pipes (about 1e-14 relative,
+// 2.4x the FP64 pipe's rate), converted back to FP64 with zero upper triangles.
+// Lfac holds S on entry; Ht receives H~; W: ld x N workspace.
+int chol_htilde_pairs(ChebState &cs, double *Lfac, double *G, const double *h, int *info, double *W) {
+    cudaStream_t st = g_ctx.stream;
+    const int n = cs.N, ld = cs.ld;
+    if (!chol_inv_fits(cs.N, cs.ld, (size_t)cs.ld * cs.N)) return ELHL_ERR_OOM;
+    CU_TRY(cudaMemsetAsync(info, 0, sizeof(int), st));
+    CU_TRY(df_convert(Lfac, n, n, ld, true, st));
+    float2 *Lp = reinterpret_cast<float2 *>(Lfac), *Gp = reinterpret_cast<float2 *>(G);
+    float2 *Wp = reinterpret_cast<float2 *>(W), *Hp = reinterpret_cast<float2 *>(cs.Ht);
+    if (int rc = chol_inv_df(Lp, Gp, n, ld, 0, Wp, info)) return rc;
+    CU_TRY(cudaMemcpy2DAsync(cs.Ht, ld * sizeof(double), h, ld * sizeof(double), n * sizeof(double), n,
+                             cudaMemcpyDeviceToDevice, st));
+    CU_TRY(df_convert(cs.Ht, n, n, ld, true, st));
+    CU_TRY(dfgemm(n, n, n, 1.0, Gp, ld, Hp, ld, 0.0, Wp, ld, st, false, kTriA));                // G h
+    CU_TRY(dfgemm(n, n, n, 1.0, Wp, ld, Gp, ld, 0.0, Hp, ld, st, true, kTriBt | kTriLowerC));   // (G h) G^T
+    CU_TRY(df_convert(cs.Ht, n, n, ld, false, st));
+    CU_TRY(df_convert(Lfac, n, n, ld, false, st));
+    CU_TRY(df_convert(G, n, n, ld, false, st));
+    const dim3 grid((ld + 127) / 128, n);
+    mirror_lower_kernel<<<grid, 128, 0, st>>>(cs.Ht, n, ld);
+    count_launch();
+    lower_only_kernel<<<grid, 128, 0, st>>>(Lfac, n, ld);
+    count_launch();
+    lower_only_kernel<<<grid, 128, 0, st>>>(G, n, ld);
+    count_launch();
+    CU_TRY(cudaGetLastError());
+    return ELHL_OK;
+}
+
 // A = L^-1 and B = L^T (launch precision) for the device read-out of fixed nuclei.
 // L and G = L^-1 both FP64 with zero upper triangles.
 int cheb_prepare_readout(ChebState &cs, const double *Lfac, const double *G) {
@@ -1964,11 +1997,22 @@ int rebuild(elhl_traj *tr, const double *d_coords) {
 int cheb_rebuild_operator(elhl_traj *tr, bool implicit = false) {
     cudaStream_t st = g_ctx.stream;
     ChebState &cs = tr->cs;
-    // S = L L^T and G = L^-1 in one recursion: FP64 for FP64 propagation and for every
-    // fixed-nuclei set-up; double-float pairs (about 1e-14 relative) for the moving-nuclei
-    // DF64, FP32 and BF16X3 propagations, whose own rounding is near 1e-14 or 1e-7.
+    // S = L L^T and G = L^-1 in one recursion: FP64 for FP64 propagation (and the DF64
+    // fixed-nuclei set-up); double-float pairs (about 1e-14 relative) for the DF64, FP32
+    // and BF16X3 moving-nuclei propagations and, with H~, the FP32 / BF16X3 fixed-nuclei
+    // set-ups, whose own rounding is near 1e-14 or 1e-7.
     // The implicit operator keeps G in cs.Ht, the explicit one in the factor's G.
     const bool pairs = implicit && cs.precision != ELHL_PREC_FP64;
+    if (!implicit && reduced_precision(cs.precision)) {
+        CU_TRY(cudaMemcpy2DAsync(tr->fac.L, tr->ld * sizeof(double), tr->S, tr->ld * sizeof(double),
+                                 tr->N * sizeof(double), tr->N, cudaMemcpyDeviceToDevice, st));
+        if (int rc = chol_htilde_pairs(cs, tr->fac.L, tr->fac.G, tr->h, tr->fac.info, tr->fac.W)) return rc;
+        CU_TRY(cudaEventRecord(g_ctx.ev[5], st));
+        if (int rc = tr->fac.check_info(false)) return rc;
+        cs.implicit = false;
+        if (int rc = lanczos_bounds(cs, 40)) return rc;
+        return cheb_prepare(cs, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol);
+    }
     if (pairs) {
         CU_TRY(cudaMemcpy2DAsync(tr->fac.L, tr->ld * sizeof(double), tr->S, tr->ld * sizeof(double),
                                  tr->N * sizeof(double), tr->N, cudaMemcpyDeviceToDevice, st));

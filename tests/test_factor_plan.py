@@ -6,10 +6,12 @@ GPU run:
   chol_inv_fits): every leaf is a diagonal block of at most 64 rows, the leaves
   tile the matrix, and no off-diagonal block exceeds the ld x N workspace the
   factor allocates; a numpy replay of the same splits reproduces L and L^-1;
-* dgemm64's tiling (dynemol_gb300/csrc/dgemm.cu): the k range each output tile
-  and split reads, for every triangular flag, with the constants read from the
-  source; the replayed masked product must equal the triangular product, and
-  the splits must cover the tile's k tiles exactly once."""
+* dgemm64's work units (dynemol_gb300/csrc/dgemm.cu): the k range each (tile,
+  k-chunk) unit reads, for every triangular flag, with the constants read from
+  the source; the replayed masked product must equal the triangular product,
+  the chunks must cover each tile's k tiles exactly once, and every partial
+  tile must have its slot in the workspace."""
+
 import os
 import re
 
@@ -30,7 +32,8 @@ def _const(src, name):
 
 
 BM, BN, BK = _const(DG, "kBM"), _const(DG, "kBN"), _const(DG, "kBK")
-MAX_PARTIALS, SPLIT_BELOW = _const(DG, "kMaxPartials"), _const(DG, "kSplitBelowTiles")
+MAX_PARTIALS, UNITS_PER_SLOT = _const(DG, "kMaxPartials"), _const(DG, "kUnitsPerSlot")
+SLOTS = 4 * 152  # resident CTAs on a GB300 (4 per SM at 256 threads, 55 registers, 33 KB)
 TRI_A, TRI_B, TRI_BT, TRI_LC, TRI_AT = (_const(HDR, n) for n in ("kTriA", "kTriB", "kTriBt", "kTriLowerC", "kTriAt"))
 
 
@@ -103,64 +106,76 @@ def test_plan_computes_the_factors(n):
     assert np.abs(G2 - np.linalg.inv(L)).max() < 1e-12
 
 
-def _splits(tiles, ktiles):
-    """dgemm64's split-K count for a grid of `tiles` output tiles."""
-    if tiles < SPLIT_BELOW and ktiles > 0:
-        return max(1, min((2 * SPLIT_BELOW + tiles - 1) // tiles, ktiles, 16, MAX_PARTIALS // tiles))
-    return 1
+def _chunking(tiles, k, slots=SLOTS):
+    """dgemm64's k tiles per work unit and units per tile (dgemm.cu, host side)."""
+    kt = max(1, (k + BK - 1) // BK)
+    chunk = (tiles * kt + UNITS_PER_SLOT * slots - 1) // (UNITS_PER_SLOT * slots)
+    chunk = max(1, min(chunk, kt))
+    while chunk < kt and tiles * ((kt + chunk - 1) // chunk) > MAX_PARTIALS:
+        chunk *= 2
+    chunk = min(chunk, kt)
+    nchunk = (kt + chunk - 1) // chunk
+    assert nchunk == 1 or tiles * nchunk <= MAX_PARTIALS
+    return chunk, nchunk
 
 
-def _dgemm_replay(m, n, k, A, B, ta, tb, tri):
-    """C = op(A) op(B) accumulated tile by tile over the k ranges the kernel reads."""
+def _dgemm_replay(m, n, k, A, B, ta, tb, tri, slots=SLOTS):
+    """C = op(A) op(B) accumulated unit by unit over the k ranges the kernel reads."""
     opA = A.T if ta else A
     opB = B.T if tb else B
     gx, gy = (m + BM - 1) // BM, (n + BN - 1) // BN
-    S = _splits(gx * gy, (k + BK - 1) // BK)
-    assert gx * gy * S <= MAX_PARTIALS or S == 1
+    chunk, nchunk = _chunking(gx * gy, k, slots)
     C = np.zeros((m, n))
-    for bx in range(gx):
-        for by in range(gy):
-            i0, j0 = bx * BM, by * BN
-            if (tri & TRI_LC) and i0 + BM <= j0:
-                continue
-            klo, khi = 0, k
+    seen = set()
+    for u in range(gx * gy * nchunk):
+        t, ch = divmod(u, nchunk)
+        bx0, by0 = t % gx, t // gx
+        bx = gx - 1 - bx0 if tri & TRI_A else bx0
+        by = gy - 1 - by0 if tri & TRI_BT else by0
+        i0, j0 = bx * BM, by * BN
+        if (tri & TRI_LC) and i0 + BM <= j0:
+            continue
+        klo, khi = 0, k
+        if tri & TRI_A:
+            khi = min(khi, i0 + BM)
+        if tri & TRI_AT:
+            klo = max(klo, i0)
+        if tri & TRI_B:
+            klo = max(klo, j0)
+        if tri & TRI_BT:
+            khi = min(khi, j0 + BN)
+        nkt = (khi - klo + BK - 1) // BK if khi > klo else 0
+        nch = max(1, (nkt + chunk - 1) // chunk)
+        if ch >= nch:
+            continue
+        assert nch == 1 or (by * gx + bx) * nchunk + ch < MAX_PARTIALS  # partial slot in the workspace
+        kt0, kt1 = ch * chunk, min(nkt, ch * chunk + chunk)
+        lo, hi = klo + kt0 * BK, min(khi, klo + kt1 * BK)
+        for k0 in range(lo, hi, BK):
+            kk = np.arange(k0, min(k0 + BK, k))  # whole k tiles, masked only at k (as the kernel loads)
+            for x in kk:
+                assert (bx, by, x) not in seen  # no k index twice in one tile
+                seen.add((bx, by, x))
+            ii = np.arange(i0, min(i0 + BM, m))
+            jj = np.arange(j0, min(j0 + BN, n))
+            a = opA[np.ix_(ii, kk)].copy()
+            b = opB[np.ix_(kk, jj)].copy()
+            gi, gk = np.meshgrid(ii, kk, indexing="ij")
             if tri & TRI_A:
-                khi = min(khi, i0 + BM)
+                a[gk > gi] = 0.0
             if tri & TRI_AT:
-                klo = max(klo, i0)
+                a[gk < gi] = 0.0
+            gk2, gj = np.meshgrid(kk, jj, indexing="ij")
             if tri & TRI_B:
-                klo = max(klo, j0)
+                b[gk2 < gj] = 0.0
             if tri & TRI_BT:
-                khi = min(khi, j0 + BN)
-            nkt = (khi - klo + BK - 1) // BK if khi > klo else 0
-            covered = []
-            for z in range(S):
-                kt0, kt1 = z * nkt // S, (z + 1) * nkt // S
-                lo, hi = klo + kt0 * BK, min(khi, klo + kt1 * BK)
-                for k0 in range(lo, hi, BK):
-                    kk = np.arange(k0, min(k0 + BK, k))  # whole k tiles, masked only at k (as the kernel loads)
-                    covered += list(kk)
-                    ii = np.arange(i0, min(i0 + BM, m))
-                    jj = np.arange(j0, min(j0 + BN, n))
-                    a = opA[np.ix_(ii, kk)].copy()
-                    b = opB[np.ix_(kk, jj)].copy()
-                    gi, gk = np.meshgrid(ii, kk, indexing="ij")
-                    if tri & TRI_A:
-                        a[gk > gi] = 0.0
-                    if tri & TRI_AT:
-                        a[gk < gi] = 0.0
-                    gk2, gj = np.meshgrid(kk, jj, indexing="ij")
-                    if tri & TRI_B:
-                        b[gk2 < gj] = 0.0
-                    if tri & TRI_BT:
-                        b[gk2 > gj] = 0.0
-                    C[np.ix_(ii, jj)] += a @ b
-            assert len(covered) == len(set(covered))  # no k index twice in one tile
-            assert set(range(klo, khi)) <= set(covered)
+                b[gk2 > gj] = 0.0
+            C[np.ix_(ii, jj)] += a @ b
     return C
 
 
-@pytest.mark.parametrize("m,n,k", [(200, 200, 200), (130, 70, 130), (64, 2, 64), (3, 5, 7), (190, 190, 61)])
+@pytest.mark.parametrize("m,n,k", [(200, 200, 200), (130, 70, 130), (64, 2, 64), (3, 5, 7), (190, 190, 61),
+                                   (700, 640, 900)])
 @pytest.mark.parametrize("case", ["none", "A", "At", "B", "Bt", "Bt_lowerC"])
 def test_dgemm_tiles_cover_the_triangular_products(m, n, k, case):
     rng = np.random.default_rng(m * 7 + n + k)
@@ -183,7 +198,7 @@ def test_dgemm_tiles_cover_the_triangular_products(m, n, k, case):
         ref_b = np.triu(opB)
     else:
         ref_b = opB
-    C = _dgemm_replay(m, n, k, A, B, ta, tb, tri)
+    C = _dgemm_replay(m, n, k, A, B, ta, tb, tri, slots=8)  # few slots: many chunks per tile
     ref = ref_a @ ref_b
     if tri & TRI_LC:  # only tiles reaching the diagonal are written; compare the lower triangle
         mask = np.tril(np.ones((m, n), bool))
@@ -247,3 +262,9 @@ def test_windowed_rows_cover_the_matrix_once(n, mg, c2, krt):
                             if j1 > j0:
                                 count[rr0 - row0:rr0 - row0 + nr, j0:j1] += 1
         assert (count == 1).all(), (n, mg, row0, row1)
+
+
+@pytest.mark.parametrize("tiles,k", [(484, 1408), (841, 1920), (16384, 8192), (4, 64), (64, 480), (3000, 16384)])
+def test_dgemm_chunking_bounds(tiles, k):
+    chunk, nchunk = _chunking(tiles, k)
+    assert chunk >= 1 and nchunk >= 1 and (nchunk == 1 or tiles * nchunk <= MAX_PARTIALS)
