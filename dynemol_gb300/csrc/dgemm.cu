@@ -36,9 +36,13 @@ constexpr int kRT = kBM / kTM, kCT = kBN / kTN;  // threads along rows and colum
 constexpr int kThreads = kRT * kCT;
 constexpr int kMaxPartials = 4096;     // partial tiles held by the workspace (128 MB)
 constexpr int kUnitsPerSlot = 6;       // work units per resident CTA the chunk length aims at
-double *g_part = nullptr;              // [tile * chunks + chunk][kBM * kBN]
-int *g_count = nullptr;                // [tile] arrivals, back to 0 after each fix-up
-int *g_sched = nullptr;                // [2]: next unit, CTAs finished; back to 0 after each launch
+constexpr int kLanes = 2;              // products that may run concurrently (streams), each with its own state
+struct Lane {
+    double *part = nullptr;            // [tile * chunks + chunk][kBM * kBN]
+    int *count = nullptr;              // [tile] arrivals, back to 0 after each fix-up
+    int *sched = nullptr;              // next unit (64-bit), CTAs finished; back to 0 after each launch
+};
+Lane g_lane[kLanes];
 int g_slots = 0;                       // resident CTAs of the whole GPU
 
 __device__ __forceinline__ void cp_async8(double *dst, const double *src, int src_bytes) {
@@ -206,29 +210,37 @@ __global__ void __launch_bounds__(kThreads) dgemm_kernel(const DgemmArgs g) {
 }  // namespace
 
 cudaError_t dgemm64(int m, int n, int k, double alpha, const double *A, int lda, bool transA, const double *B, int ldb,
-                    bool transB, double beta, double *C, int ldc, cudaStream_t st, int tri) {
+                    bool transB, double beta, double *C, int ldc, cudaStream_t st, int tri, int lane) {
     if (m <= 0 || n <= 0) return cudaSuccess;
-    if (!g_part) {
+    if (lane < 0 || lane >= kLanes) return cudaErrorInvalidValue;
+    if (!g_slots) {
         int dev = 0, sms = 0, per_sm = 0;
         cudaError_t e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess)
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dgemm_kernel<false, false>, kThreads, 0);
-        if (e == cudaSuccess) e = cudaMalloc(&g_part, (size_t)kMaxPartials * kBM * kBN * sizeof(double));
-        if (e == cudaSuccess) e = cudaMalloc(&g_count, (size_t)kMaxPartials * sizeof(int));
-        if (e == cudaSuccess) e = cudaMemset(g_count, 0, (size_t)kMaxPartials * sizeof(int));
-        if (e == cudaSuccess) e = cudaMalloc(&g_sched, 4 * sizeof(int));
-        if (e == cudaSuccess) e = cudaMemset(g_sched, 0, 4 * sizeof(int));
         if (e != cudaSuccess) return e;
         g_slots = std::max(1, per_sm) * sms;
     }
+    Lane &ln = g_lane[lane];
+    if (!ln.part) {
+        cudaError_t e = cudaMalloc(&ln.part, (size_t)kMaxPartials * kBM * kBN * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&ln.count, (size_t)kMaxPartials * sizeof(int));
+        if (e == cudaSuccess) e = cudaMemset(ln.count, 0, (size_t)kMaxPartials * sizeof(int));
+        if (e == cudaSuccess) e = cudaMalloc(&ln.sched, 4 * sizeof(int));
+        if (e == cudaSuccess) e = cudaMemset(ln.sched, 0, 4 * sizeof(int));
+        if (e != cudaSuccess) return e;
+    }
+    // lane 1 runs beside lane 0's work (single-CTA leaves, small products): it leaves
+    // a quarter of the resident CTA slots free
+    const int slots = lane == 0 ? g_slots : std::max(1, g_slots * 3 / 4);
     DgemmArgs g{m, n, k, alpha, beta, A, B, C, lda, ldb, ldc, tri, (m + kBM - 1) / kBM, (n + kBN - 1) / kBN,
-                1, 1, 0, g_part, g_count, g_sched};
+                1, 1, 0, ln.part, ln.count, ln.sched};
     const long long tiles = (long long)g.gx * g.gy;
     const int kt = std::max(1, (k + kBK - 1) / kBK);
     // chunk length: about kUnitsPerSlot units per resident CTA, whole k ranges when
     // the tiles alone are enough, and no more partial tiles than the workspace holds
-    long long chunk = (tiles * kt + (long long)kUnitsPerSlot * g_slots - 1) / ((long long)kUnitsPerSlot * g_slots);
+    long long chunk = (tiles * kt + (long long)kUnitsPerSlot * slots - 1) / ((long long)kUnitsPerSlot * slots);
     chunk = std::max(1ll, std::min<long long>(chunk, kt));
     while (chunk < kt && tiles * ((kt + chunk - 1) / chunk) > kMaxPartials) chunk *= 2;
     if (chunk >= kt) chunk = kt;
@@ -236,7 +248,7 @@ cudaError_t dgemm64(int m, int n, int k, double alpha, const double *A, int lda,
     g.nchunk = (kt + g.chunk - 1) / g.chunk;
     if (g.nchunk > 1 && tiles > kMaxPartials) return cudaErrorInvalidValue;  // never: chunk = kt above
     g.units = tiles * g.nchunk;
-    const int grid = (int)std::min<long long>(g.units, g_slots);
+    const int grid = (int)std::min<long long>(g.units, slots);
 #define ELHL_DGEMM(TA_, TB_) dgemm_kernel<TA_, TB_><<<grid, kThreads, 0, st>>>(g)
     if (transA && transB) ELHL_DGEMM(true, true);
     else if (transA) ELHL_DGEMM(true, false);

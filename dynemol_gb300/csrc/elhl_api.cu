@@ -90,6 +90,10 @@ struct Context {
     double *partials = nullptr;
     // 0/1 propagation begin/end, 2/3 rebuild begin/end, 4 S/h built, 5 factorised, 6 inverse formed
     cudaEvent_t ev[7] = {};
+    // the factorisation's second stream: G11^T L21^T of a split runs there while the
+    // main stream factors the trailing block (ev_l21: L21 ready, ev_side: side work done)
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t ev_l21 = nullptr, ev_side = nullptr;
     std::mutex mu;
 };
 Context g_ctx;
@@ -119,6 +123,9 @@ int ensure_context_locked(int device) {
     CU_TRY(cudaStreamCreateWithFlags(&g_ctx.own_stream, cudaStreamNonBlocking));
     g_ctx.stream = g_ctx.own_stream;
     CU_TRY(cudaStreamCreateWithFlags(&g_ctx.copy_stream, cudaStreamNonBlocking));
+    CU_TRY(cudaStreamCreateWithFlags(&g_ctx.aux_stream, cudaStreamNonBlocking));
+    CU_TRY(cudaEventCreateWithFlags(&g_ctx.ev_l21, cudaEventDisableTiming));
+    CU_TRY(cudaEventCreateWithFlags(&g_ctx.ev_side, cudaEventDisableTiming));
     SOLVER_TRY(cusolverDnCreate(&g_ctx.solver));
     SOLVER_TRY(cusolverDnSetStream(g_ctx.solver, g_ctx.stream));
     if (cublasCreate(&g_ctx.blas) != CUBLAS_STATUS_SUCCESS) return ELHL_ERR_CUDA;
@@ -224,6 +231,9 @@ __global__ void lower_only_kernel(double *A, int n, int ld) {
 //   L22, G22 = chol_inv(A22);   G21 = -G22 (L21 G11),
 // N^3/3 + N^3/3 flops in dgemm64 products (triangular operands at half cost),
 // 64-row diagonal blocks as leaves (leaf_chol_inv64), splits on multiples of 64.
+// G11^T L21^T, the first factor of G21 = -G22 (L21 G11) stored transposed in the
+// unused upper block G12, runs on a second stream while the main stream does the
+// Schur update and factors A22 (whose single-CTA leaves leave most SMs free).
 // It replaces the reference's LU inverse of S (MAGMA dgetrf + dgetri,
 // GPU_Interface.cpp:910-928; CPU dsytrf + dsytri, :936-947): S is symmetric
 // positive definite, so its Cholesky factor gives S^-1 = G^T G.  W holds the
@@ -246,14 +256,21 @@ int chol_inv64(double *A, double *G, int n, int ld, int row0, double *W, int *in
     const int n1 = round_up(n / 2, leaf), n2 = n - n1;
     double *A21 = A + n1, *A22 = A + (size_t)n1 * ld + n1;
     double *G21 = G + n1, *G22 = G + (size_t)n1 * ld + n1;
+    double *G12 = G + (size_t)n1 * ld;  // n1 x n2, above the diagonal: free until lower_only
+    cudaStream_t side = g_ctx.aux_stream;
     if (int rc = chol_inv64(A, G, n1, ld, row0, W, info)) return rc;
     CU_TRY(cudaMemcpy2DAsync(W, ld * sizeof(double), A21, ld * sizeof(double), n2 * sizeof(double), n1,
                              cudaMemcpyDeviceToDevice, st));
     CU_TRY(dgemm64(n2, n1, n1, 1.0, W, ld, false, G, ld, true, 0.0, A21, ld, st, kTriBt));       // L21
+    CU_TRY(cudaEventRecord(g_ctx.ev_l21, st));
+    CU_TRY(cudaStreamWaitEvent(side, g_ctx.ev_l21, 0));
+    CU_TRY(dgemm64(n1, n2, n1, 1.0, G, ld, true, A21, ld, true, 0.0, G12, ld, side, kTriAt, 1));  // (L21 G11)^T
+    CU_TRY(cudaEventRecord(g_ctx.ev_side, side));
     CU_TRY(dgemm64(n2, n2, n1, -1.0, A21, ld, false, A21, ld, true, 1.0, A22, ld, st, kTriLowerC));  // Schur
     if (int rc = chol_inv64(A22, G22, n2, ld, row0 + n1, W, info)) return rc;
-    CU_TRY(dgemm64(n2, n1, n1, 1.0, A21, ld, false, G, ld, false, 0.0, W, ld, st, kTriB));      // L21 G11
-    CU_TRY(dgemm64(n2, n1, n2, -1.0, G22, ld, false, W, ld, false, 0.0, G21, ld, st, kTriA));   // G21
+    // the side stream is serial: its last recorded event covers this split's product
+    CU_TRY(cudaStreamWaitEvent(st, g_ctx.ev_side, 0));
+    CU_TRY(dgemm64(n2, n1, n2, -1.0, G22, ld, false, G12, ld, true, 0.0, G21, ld, st, kTriA));  // G21
     return ELHL_OK;
 }
 
@@ -630,6 +647,8 @@ struct ChebState {
     double *ntot = nullptr;    // [kMaxCols] FP64 totals of the last step's columns (renormalisation)
     double2 *saved = nullptr;  // [ld][m] input columns at the start of a call, for redone steps
     double guard = 0.01;       // Lanczos interval guard, fraction of the width
+    bool ro64 = false;         // read-out matrices A, B in FP64 (else the launch precision)
+    size_t ab_tsz = 0;         // element size A and B were allocated with
     // read-out outputs, owned by the trajectory
     int P = 0, nfrag = 0;
     double2 *psi_out = nullptr, *bra_out = nullptr;
@@ -1024,16 +1043,39 @@ int chol_htilde_pairs(ChebState &cs, double *Lfac, double *G, const double *h, i
     return ELHL_OK;
 }
 
-// A = L^-1 and B = L^T (launch precision) for the device read-out of fixed nuclei.
-// L and G = L^-1 both FP64 with zero upper triangles.
+// Read-out matrices in FP64 for the reduced precisions too: the populations
+// of an FP32 read-out carry about 1e-7 of noise (up to 1e-6 on some members of
+// the 512-trajectory mix), while the FP32 propagation itself stays within 5e-8
+// of FP64 over 200 steps.  Exceptions: the GEMM regime, whose read-out is two
+// tensor-core GEMMs of the FP32 block, and bases whose FP64 vector would not fit
+// in shared memory for the read-out kernel.
+bool gemm_eligible(const ChebState &cs) {
+    return reduced_precision(cs.precision) && cs.m == cs.P && cs.P >= kGemmMinCols && cs.N >= kGemmMinN;
+}
+bool readout_fp64(const ChebState &cs) {
+    if (cs.precision == ELHL_PREC_FP64) return true;
+    return reduced_precision(cs.precision) && !gemm_eligible(cs) && cheb_group_size(ELHL_PREC_FP64, 1, cs.ld) > 0;
+}
+
+// A = L^-1 and B = L^T for the device read-out of fixed nuclei, in FP64
+// (readout_fp64) or the launch precision.  L and G = L^-1 both FP64 with zero
+// upper triangles.
 int cheb_prepare_readout(ChebState &cs, const double *Lfac, const double *G) {
     cudaStream_t st = g_ctx.stream;
     const int n = cs.N, ld = cs.ld;
-    const size_t tsz = cs.precision == ELHL_PREC_FP64 ? sizeof(double) : sizeof(float);
+    const bool wide = readout_fp64(cs);
+    const size_t tsz = wide ? sizeof(double) : sizeof(float);
+    if (cs.A && cs.ab_tsz != tsz) {  // allocated by the implicit operator in the launch precision
+        cudaFree(cs.A);
+        cudaFree(cs.B);
+        cs.A = cs.B = nullptr;
+    }
     if (!cs.A) CU_TRY(cudaMalloc(&cs.A, (size_t)ld * n * tsz));
     if (!cs.B) CU_TRY(cudaMalloc(&cs.B, (size_t)ld * n * tsz));
+    cs.ab_tsz = tsz;
+    cs.ro64 = wide;
     dim3 grid((ld + 127) / 128, n);
-    if (cs.precision == ELHL_PREC_FP64) {
+    if (wide) {
         convert_kernel<double><<<grid, 128, 0, st>>>(G, (double *)cs.A, n, ld, false);
         count_launch();
         convert_kernel<double><<<grid, 128, 0, st>>>(Lfac, (double *)cs.B, n, ld, true);
@@ -1058,8 +1100,15 @@ int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, do
     cudaStream_t st = g_ctx.stream;
     const int n = cs.N, ld = cs.ld;
     const size_t tsz = wide_storage(cs.precision) ? sizeof(double) : sizeof(float);
+    if (cs.A && cs.ab_tsz != tsz) {  // FP64 read-out matrices of an earlier fixed-nuclei set-up
+        cudaFree(cs.A);
+        cudaFree(cs.B);
+        cs.A = cs.B = nullptr;
+    }
     if (!cs.A) CU_TRY(cudaMalloc(&cs.A, (size_t)ld * n * tsz));
     if (!cs.B) CU_TRY(cudaMalloc(&cs.B, (size_t)ld * n * tsz));
+    cs.ab_tsz = tsz;
+    cs.ro64 = cs.precision == ELHL_PREC_FP64;
     if (!cs.Gt) CU_TRY(cudaMalloc(&cs.Gt, (size_t)ld * n * tsz));
     if (!cs.wb) {
         CU_TRY(cudaMalloc(&cs.wb, (size_t)2 * ld * cs.m * 2 * tsz));
@@ -1379,6 +1428,7 @@ struct ChebPlan {
     double *d_seg_pops = nullptr;
     double *d_drift = nullptr;  // [problem] norm drift of the steps since the last reset
     int grid = 0, max_ld = 0, kmax = 0, mg = 0, mg_read = 0, precision = 0, parity = 0;
+    int ro_precision = 0;      // element type of the read-out matrices (FP64 or the launch precision)
     int nphase = 1;            // 3: one implicit problem
     int mgcd = 0;              // gcd of the problems' column counts
     bool tuned = false;        // tile measured (on the plan's first run)
@@ -1421,7 +1471,10 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
         while (b) { const int t = a % b; a = b; b = t; }
         pgcd = a;
     }
-    pl.mg_read = cheb_group_size(pl.precision, pgcd, pl.max_ld);
+    pl.ro_precision = states[0]->ro64 ? ELHL_PREC_FP64 : pl.precision;
+    for (auto *cs : states)
+        if (cs->readout_ready && cs->ro64 != states[0]->ro64) return ELHL_ERR_UNSUPPORTED;  // one read-out type
+    pl.mg_read = cheb_group_size(pl.ro_precision, pgcd, pl.max_ld);
     pl.pops_per_step = 0;
     pl.parity = states[0]->parity;
     const bool implicit = states[0]->implicit;
@@ -1693,7 +1746,7 @@ int cheb_dev_step(ChebPlan &pl, const std::vector<ChebState *> &states, double *
     L.parity = pl.parity;
     L.seg_pops = pl.d_seg_pops;
     L.pops = d_pops_step;
-    CU_TRY(launch_readout(L, (int)pl.probs.size(), pl.precision, pl.mg_read, g_ctx.stream));
+    CU_TRY(launch_readout(L, (int)pl.probs.size(), pl.ro_precision, pl.mg_read, g_ctx.stream));
     pl.parity ^= 1;
     for (auto *cs : states) cs->parity = pl.parity;
     return ELHL_OK;
@@ -2585,6 +2638,11 @@ void gpu_finalize_(void) {
     g_ctx.tc_ws = nullptr;
     if (g_ctx.own_stream) cudaStreamDestroy(g_ctx.own_stream);
     if (g_ctx.copy_stream) cudaStreamDestroy(g_ctx.copy_stream);
+    if (g_ctx.aux_stream) cudaStreamDestroy(g_ctx.aux_stream);
+    if (g_ctx.ev_l21) cudaEventDestroy(g_ctx.ev_l21);
+    if (g_ctx.ev_side) cudaEventDestroy(g_ctx.ev_side);
+    g_ctx.aux_stream = nullptr;
+    g_ctx.ev_l21 = g_ctx.ev_side = nullptr;
     g_ctx.solver = nullptr;
     g_ctx.stream = g_ctx.copy_stream = g_ctx.own_stream = nullptr;
     g_ctx.ready = false;
@@ -2778,7 +2836,7 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
         cs.ao_frag = tr->basis.ao_frag; cs.target = tr->target;
         if (!rc && !df) rc = cheb_prepare_readout(cs, tr->fac.L, traj_inverse(tr));
         // GEMM regime: many ket columns in FP32 / BF16X3 -> one GEMM per order
-        if (!rc && reduced_precision(cs.precision) && cs.m == cs.P && cs.P >= kGemmMinCols && cs.N >= kGemmMinN) {
+        if (!rc && gemm_eligible(cs)) {
             cs.gemm = true;
             if (cudaMalloc(&cs.Y, (size_t)cs.ld * cs.m * sizeof(float2)) != cudaSuccess ||
                 cudaMalloc(&cs.Vf, (size_t)cs.ld * cs.m * sizeof(float2)) != cudaSuccess)
@@ -3419,7 +3477,7 @@ struct ServerGroup {
     double *pops = nullptr;
     size_t pops_cap = 0;
 };
-constexpr int kServerGroups = 3;  // column-group size 4, 2, 1
+constexpr int kServerGroups = 4;  // FP64 read-out with column-group size 4, 2, 1; read-out in the launch precision
 
 static double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
@@ -3439,8 +3497,8 @@ struct elhl_server {
 
 static double request_bytes(const elhl_traj_config &cfg, int nao, int P) {
     const double ld = (double)round_up(nao, 32), tsz = wide_storage(cfg.precision) ? 8.0 : 4.0;
-    // set-up peak: S, h, H~, L (FP64) + Hs + vectors
-    return ld * nao * (4 * 8.0 + tsz) + ld * cfg.ncols / cfg.nparticles * P * (3 * 2 * tsz + 2 * 16.0) + 1e6;
+    // set-up peak: S, h, H~, L, G (FP64) + Hs + read-out matrices (FP64) + vectors
+    return ld * nao * (5 * 8.0 + tsz + 2 * 8.0) + ld * cfg.ncols / cfg.nparticles * P * (3 * 2 * tsz + 2 * 16.0) + 1e6;
 }
 
 static int server_admit(elhl_server *sv, ServerRequest *r) {
@@ -3462,9 +3520,10 @@ static int server_admit(elhl_server *sv, ServerRequest *r) {
     if (tr->cs.gemm) {
         r->group = -1;  // many columns on a large basis: one GEMM per order, its own step graph
     } else {
-        const int mg = cheb_group_size(tr->cfg.precision, 4, tr->ld);
+        const ChebState &cs = tr->cs;
+        const int mg = cheb_group_size(cs.ro64 ? ELHL_PREC_FP64 : tr->cfg.precision, 4, tr->ld);
         if (!mg) return ELHL_ERR_UNSUPPORTED;  // the vector does not fit in shared memory
-        r->group = mg == 4 ? 0 : mg == 2 ? 1 : 2;
+        r->group = !cs.ro64 ? 3 : mg == 4 ? 0 : mg == 2 ? 1 : 2;
         tr->cs.parity = sv->groups[r->group].parity;  // join the running group's column roles
     }
     if (!r->restart.empty())

@@ -178,9 +178,11 @@ cudaError_t dfgemm(int m, int n, int k, double alpha, const float2 *A, int lda, 
                    float2 *C, int ldc, cudaStream_t st, bool transB = false, int tri = 0);
 // C = alpha op(A) op(B) + beta C in FP64 on the FP64 pipe (dgemm.cu), op = the
 // transpose when transA / transB; `tri` as for dfgemm, plus kTriAt: op(A) = A^T
-// of a lower A.
+// of a lower A.  lane 0 or 1: products that run concurrently (on two streams)
+// use different lanes, each with its own scheduler and workspace; lane 1 takes
+// three quarters of the resident CTA slots.
 cudaError_t dgemm64(int m, int n, int k, double alpha, const double *A, int lda, bool transA, const double *B, int ldb,
-                    bool transB, double beta, double *C, int ldc, cudaStream_t st, int tri = 0);
+                    bool transB, double beta, double *C, int ldc, cudaStream_t st, int tri = 0, int lane = 0);
 // rows x n block of an FP64 matrix (leading dimension ld) to DF64 pairs in
 // place (to_pairs) or back
 cudaError_t df_convert(double *x, int rows, int n, int ld, bool to_pairs, cudaStream_t st);
