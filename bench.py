@@ -153,7 +153,7 @@ def run_ours(args, rank, world):
     coords = step_coords(sysm, moving, W + K + 1, offset=1000 * rank)
     method = api.METHOD_CHEBYSHEV if args.method == "chebyshev" else api.METHOD_TAYLOR_REF
     prec = {"fp64": api.PREC_FP64, "fp32": api.PREC_FP32, "bf16x3": api.PREC_BF16X3,
-            "df64": api.PREC_DF64}[args.precision]
+            "df64": api.PREC_DF64, "oz64": api.PREC_OZ64}[args.precision]
     tr = api.Trajectory(sysm, coords=None if coords is None else coords[0], dt=dt, method=method, precision=prec,
                         ncols=4 if moving else 2, cheb_tol=1e-12)
     tr.init_fmo(homo + 1, homo)
@@ -247,9 +247,10 @@ def run_ours(args, rank, world):
         # vector bytes, flops 4 N^2 m.  Moving nuclei (implicit G (h/b) G^T, three
         # phases): N^2/2 + N^2 + N^2/2 matrix elements (b_H 2 N^2) + 9 x 16 N m vector
         # bytes, flops 8 N^2 m
-        kernel = "cheb_kernel"
+        kernel = "oz_cheb_kernel" if args.precision == "oz64" else "cheb_kernel"
         m = 4 if moving else 2
-        bH = 8.0 if args.precision in ("fp64", "df64") else 4.0
+        # bytes per matrix element: FP64 / DF64 pairs 8, FP32 4, OZ64 seven BF16 slices 14
+        bH = {"fp64": 8.0, "df64": 8.0, "oz64": 14.0}.get(args.precision, 4.0)
         elems, vec = (2.0 * N * N, 144.0) if moving else (1.0 * N * N, 80.0)
         per_launch_orders = orders / max(1, K) / m
         bytes_per_launch = per_launch_orders * (bH * elems + vec * N * m)
@@ -266,6 +267,13 @@ def run_ours(args, rank, world):
     alu_peak, alu_pipe = {"fp64": (FP64_PEAK, "fp64 FMA"),
                           "df64": (70.1 / 12.0, "fp32 FMA, 12 instructions per df64 FMA")}.get(
         args.precision, (70.1, "fp32 FMA"))
+    alu_src = "of measured (FP64/FP32 FMA probe on a GB300)"
+    if args.precision == "oz64":
+        # tensor pipe: per matrix element and order, 2 x 256 BF16 MMA flops (the 7 slice
+        # products against 8, 6, 6, 4, 4, 2, 2 vector slice columns of 8 real columns)
+        flops_per_launch = per_launch_orders * 512.0 * elems
+        alu_peak, alu_pipe = peaks.get("bf16_tflops", 1900.0), "bf16 tensor (tcgen05.mma, FP32 accumulation)"
+        alu_src = "of measured (MEASURED_PEAKS.json bf16_tflops)"
     tflops = flops_per_launch / (prop_launch_ms * 1e-3) / 1e12
 
     line = {
@@ -279,7 +287,9 @@ def run_ours(args, rank, world):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": {"fp64": "f64", "df64": "f64-accurate FP32 pairs (df64), f64 recurrence"}.get(
+        "dtype": {"fp64": "f64", "df64": "f64-accurate FP32 pairs (df64), f64 recurrence",
+                  "oz64": "f64 (operator products exact on bf16 tensor cores from 8-bit slices, "
+                          "rounded once to f64; f64 vectors and recurrence)"}.get(
             args.precision, "f32 products, f64 accumulation"),
         "data": "synthetic (seeded geometry, no external dataset)",
         "config": {"workload": WORKLOAD_DESC[args.workload], "N_ao": N, "natoms": sysm.natoms,
@@ -296,7 +306,7 @@ def run_ours(args, rank, world):
                              "peak_tflops": alu_peak,
                              "frac": tflops / alu_peak,
                              "pipe": alu_pipe,
-                             "peak_source": "of measured (FP64/FP32 FMA probe on a GB300)"},
+                             "peak_source": alu_src},
                      "orders_per_launch": per_launch_orders, "launch_ms": prop_launch_ms},
         "breakdown_ms_per_step": {"propagation": prop_ms / K, "rebuild_S_h_operator": rebuild_ms / K,
                                   "rebuild_parts": {"S_h_build": sh_ms / K, "cholesky": factor_ms / K,
@@ -311,7 +321,7 @@ def run_ours(args, rank, world):
 def run_variant(args, precision_name: str):
     """The same workload and coordinates with another precision (device-resident
     steps, CUDA events on the library's stream, L2 flushed between steps): the
-    DF64 variant of the default FP64 run."""
+    DF64 and OZ64 variants of the default FP64 run."""
     import torch
     from dynemol_gb300 import api, systems
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
@@ -322,7 +332,8 @@ def run_variant(args, precision_name: str):
     homo = systems.fermi_state(sysm, np.arange(20))
     W, K = args.warmup, args.steps
     coords = step_coords(sysm, moving, W + K + 1)
-    prec = {"fp64": api.PREC_FP64, "fp32": api.PREC_FP32, "df64": api.PREC_DF64}[precision_name]
+    prec = {"fp64": api.PREC_FP64, "fp32": api.PREC_FP32, "df64": api.PREC_DF64, "oz64": api.PREC_OZ64}[
+        precision_name]
     tr = api.Trajectory(sysm, coords=None if coords is None else coords[0], dt=dt, method=api.METHOD_CHEBYSHEV,
                         precision=prec, ncols=4 if moving else 2, cheb_tol=1e-12)
     tr.init_fmo(homo + 1, homo)
@@ -792,7 +803,7 @@ def main():
     ap.add_argument("--workload", default="ehrenfest", choices=sorted(WORKLOAD_DESC))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--method", default="chebyshev", choices=["taylor", "chebyshev"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "bf16x3", "df64"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "bf16x3", "df64", "oz64"])
     ap.add_argument("--mix", type=int, default=0, help="also run the batched-vs-drop-in comparison on a mix "
                     "of this many trajectories (0 = skip)")
     ap.add_argument("--served-mix", type=int, default=512, help="trajectories of the served mix (0 = skip)")
@@ -819,6 +830,8 @@ def main():
         # the same moving-nuclei workload with the operator in DF64 (FP32 pairs): FP64-level
         # populations (tested to 1e-9 against the oracle) without the FP64 pipe
         line["df64_variant"] = run_variant(args, "df64")
+        # and with every operator product exact on the tensor cores (FP64 results, 1e-10 tested)
+        line["oz64_variant"] = run_variant(args, "oz64")
     if rank == 0 and args.method == "chebyshev" and not args.no_dropin:
         line["dropin_taylor_fp64"] = run_dropin(args)
         line["dropin_host_fp64"] = run_dropin_host(args)

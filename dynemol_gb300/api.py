@@ -25,7 +25,7 @@ LIB_PATH = os.path.join(HERE, "libelhlprop.so")
 # status codes (elhl_prop.h)
 OK, ERR_BAD_ARG, ERR_NO_CONVERGENCE, ERR_TIMEOUT, ERR_OOM, ERR_CUDA, ERR_NOT_PD, ERR_NO_DEVICE, ERR_UNSUPPORTED = range(9)
 METHOD_TAYLOR_REF, METHOD_CHEBYSHEV = 0, 1
-PREC_FP64, PREC_FP32, PREC_BF16X3, PREC_DF64 = 0, 1, 2, 3
+PREC_FP64, PREC_FP32, PREC_BF16X3, PREC_DF64, PREC_OZ64 = 0, 1, 2, 3, 4
 
 EXPORTED_SYMBOLS = (
     "gpu_init_", "gpu_finalize_", "gpu_pin_", "gpu_unpin_", "propagation_gpucaller_", "ehrenfestkernel_gpu_",

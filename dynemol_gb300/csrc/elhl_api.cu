@@ -246,7 +246,33 @@ bool chol_inv_fits(int n, int ld, size_t wcap) {
     return (size_t)ld * n1 <= wcap && chol_inv_fits(n1, ld, wcap) && chol_inv_fits(n2, ld, wcap);
 }
 
-int chol_inv64(double *A, double *G, int n, int ld, int row0, double *W, int *info) {
+// An FP64 product of the factorisations: on the tensor cores from exact slices
+// (ozgemm) when tc is set and the product is large enough to fill the GPU, else
+// on the FP64 pipe (dgemm64).
+constexpr int kOzGemmMin = 128;
+cudaError_t fgemm(bool tc, int m, int n, int k, double alpha, const double *A, int lda, bool transA, const double *B,
+                  int ldb, bool transB, double beta, double *C, int ldc, cudaStream_t st, int tri = 0, int lane = 0) {
+    if (tc && m >= kOzGemmMin && n >= kOzGemmMin && k >= kOzGemmMin)
+        return ozgemm(m, n, k, alpha, A, lda, transA, B, ldb, transB, beta, C, ldc, st, tri, lane);
+    return dgemm64(m, n, k, alpha, A, lda, transA, B, ldb, transB, beta, C, ldc, st, tri, lane);
+}
+
+// ELHL_ERR_TIMEOUT if a tensor-core product gave up a wait since the last check (then cleared)
+int ozgemm_status() {
+    for (int lane = 0; lane < 2; ++lane) {
+        int *e = ozgemm_error(lane);
+        if (!e) continue;
+        int h = 0;
+        CU_TRY(cudaMemcpy(&h, e, sizeof(int), cudaMemcpyDeviceToHost));
+        if (h) {
+            CU_TRY(cudaMemset(e, 0, sizeof(int)));
+            return h;
+        }
+    }
+    return ELHL_OK;
+}
+
+int chol_inv64(double *A, double *G, int n, int ld, int row0, double *W, int *info, bool tc = false) {
     cudaStream_t st = g_ctx.stream;
     const int leaf = leaf_rows();
     if (n <= leaf) {
@@ -258,19 +284,19 @@ int chol_inv64(double *A, double *G, int n, int ld, int row0, double *W, int *in
     double *G21 = G + n1, *G22 = G + (size_t)n1 * ld + n1;
     double *G12 = G + (size_t)n1 * ld;  // n1 x n2, above the diagonal: free until lower_only
     cudaStream_t side = g_ctx.aux_stream;
-    if (int rc = chol_inv64(A, G, n1, ld, row0, W, info)) return rc;
+    if (int rc = chol_inv64(A, G, n1, ld, row0, W, info, tc)) return rc;
     CU_TRY(cudaMemcpy2DAsync(W, ld * sizeof(double), A21, ld * sizeof(double), n2 * sizeof(double), n1,
                              cudaMemcpyDeviceToDevice, st));
-    CU_TRY(dgemm64(n2, n1, n1, 1.0, W, ld, false, G, ld, true, 0.0, A21, ld, st, kTriBt));       // L21
+    CU_TRY(fgemm(tc, n2, n1, n1, 1.0, W, ld, false, G, ld, true, 0.0, A21, ld, st, kTriBt));       // L21
     CU_TRY(cudaEventRecord(g_ctx.ev_l21, st));
     CU_TRY(cudaStreamWaitEvent(side, g_ctx.ev_l21, 0));
-    CU_TRY(dgemm64(n1, n2, n1, 1.0, G, ld, true, A21, ld, true, 0.0, G12, ld, side, kTriAt, 1));  // (L21 G11)^T
+    CU_TRY(fgemm(tc, n1, n2, n1, 1.0, G, ld, true, A21, ld, true, 0.0, G12, ld, side, kTriAt, 1));  // (L21 G11)^T
     CU_TRY(cudaEventRecord(g_ctx.ev_side, side));
-    CU_TRY(dgemm64(n2, n2, n1, -1.0, A21, ld, false, A21, ld, true, 1.0, A22, ld, st, kTriLowerC));  // Schur
-    if (int rc = chol_inv64(A22, G22, n2, ld, row0 + n1, W, info)) return rc;
+    CU_TRY(fgemm(tc, n2, n2, n1, -1.0, A21, ld, false, A21, ld, true, 1.0, A22, ld, st, kTriLowerC));  // Schur
+    if (int rc = chol_inv64(A22, G22, n2, ld, row0 + n1, W, info, tc)) return rc;
     // the side stream is serial: its last recorded event covers this split's product
     CU_TRY(cudaStreamWaitEvent(st, g_ctx.ev_side, 0));
-    CU_TRY(dgemm64(n2, n1, n2, -1.0, G22, ld, false, G12, ld, true, 0.0, G21, ld, st, kTriA));  // G21
+    CU_TRY(fgemm(tc, n2, n1, n2, -1.0, G22, ld, false, G12, ld, true, 0.0, G21, ld, st, kTriA));  // G21
     return ELHL_OK;
 }
 
@@ -282,6 +308,7 @@ struct Factor {
     double *W = nullptr;     // ld x N workspace: the factorisation's off-diagonal blocks, then G h
     int *info = nullptr;     // [2]: first non-positive pivot (1-based global column), 0 = positive definite
     double *cols = nullptr;  // 2 x (N x 2) scratch (S^-1 applied to a complex vector)
+    bool tc = false;         // large products on the tensor cores from exact slices (ELHL_PREC_OZ64)
     int reserve(int N_, int ld_) {
         if (N_ <= N && ld_ == ld && L) return ELHL_OK;
         release();
@@ -309,7 +336,7 @@ struct Factor {
         CU_TRY(cudaMemsetAsync(info, 0, 2 * sizeof(int), st));
         CU_TRY(cudaMemcpy2DAsync(L, ld * sizeof(double), S, ld * sizeof(double), n * sizeof(double), n,
                                  cudaMemcpyDeviceToDevice, st));
-        if (int rc = chol_inv64(L, g, n, ld, 0, W, info)) return rc;
+        if (int rc = chol_inv64(L, g, n, ld, 0, W, info, tc)) return rc;
         const dim3 grid((ld + 127) / 128, n);
         lower_only_kernel<<<grid, 128, 0, st>>>(L, n, ld);
         count_launch();
@@ -322,8 +349,8 @@ struct Factor {
     int form_hprime(const double *S, const double *h, double *Hp, int n) {
         cudaStream_t st = g_ctx.stream;
         if (int rc = factor(S, n)) return rc;
-        CU_TRY(dgemm64(n, n, n, 1.0, G, ld, false, h, ld, false, 0.0, W, ld, st, kTriA));    // G h
-        CU_TRY(dgemm64(n, n, n, 1.0, G, ld, true, W, ld, false, 0.0, Hp, ld, st, kTriAt));   // G^T (G h)
+        CU_TRY(fgemm(tc, n, n, n, 1.0, G, ld, false, h, ld, false, 0.0, W, ld, st, kTriA));    // G h
+        CU_TRY(fgemm(tc, n, n, n, 1.0, G, ld, true, W, ld, false, 0.0, Hp, ld, st, kTriAt));   // G^T (G h)
         return ELHL_OK;
     }
     // out = S^-1 z = G^T (G z) for a complex vector z (device), using the factor.
@@ -345,6 +372,8 @@ struct Factor {
         int h[2] = {0, 0};
         CU_TRY(cudaMemcpyAsync(h, info, 2 * sizeof(int), cudaMemcpyDeviceToHost, g_ctx.stream));
         CU_TRY(cudaStreamSynchronize(g_ctx.stream));
+        if (tc)
+            if (int rc = ozgemm_status()) return rc;
         if (h[0] > 0) return ELHL_ERR_NOT_POSITIVE_DEFINITE;
         if (h[0] < 0) return ELHL_ERR_BAD_ARG;
         return ELHL_OK;
@@ -637,6 +666,75 @@ __global__ void split_df_kernel(const double *__restrict__ src, float2 *__restri
     dst[(size_t)j * ld + i] = make_float2(h, __double2float_rn(v - (double)h));
 }
 
+// Resources of ELHL_PREC_OZ64 (ozaki.cu): BF16 slices of the operator's
+// matrices with their row scales, the FP64 series vectors in [ld][8] rows, the
+// per-phase block schedules and the launch's partial tiles and counters.
+// Matrix 0: G = L^-1 (storage column i = row i of G^T), 1: Hs, 2: G^T.
+struct OzRes {
+    int N = 0, ld = 0, ntiles = 0, grid = 0;
+    __nv_bfloat16 *s[3] = {nullptr, nullptr, nullptr};
+    double *r[3] = {nullptr, nullptr, nullptr};
+    double *v = nullptr, *w = nullptr, *part = nullptr;
+    unsigned *cnt = nullptr;
+    unsigned long long *cmax = nullptr;
+    OzSeg *segs[3] = {nullptr, nullptr, nullptr};
+    int *begin[3] = {nullptr, nullptr, nullptr}, *base[3] = {nullptr, nullptr, nullptr};
+    int *count[3] = {nullptr, nullptr, nullptr};
+    int init(int N_, int ld_, int grid_) {
+        N = N_;
+        ld = ld_;
+        grid = grid_;
+        ntiles = (N + oz_tile_rows() - 1) / oz_tile_rows();
+        if (int rc = dev_alloc(&v, (size_t)3 * ld * 8)) return rc;
+        if (int rc = dev_alloc(&w, (size_t)2 * ld * 8)) return rc;
+        CU_TRY(cudaMemset(v, 0, (size_t)3 * ld * 8 * sizeof(double)));
+        CU_TRY(cudaMemset(w, 0, (size_t)2 * ld * 8 * sizeof(double)));
+        CU_TRY(cudaMalloc(&cnt, (size_t)ntiles * sizeof(unsigned)));
+        CU_TRY(cudaMalloc(&cmax, 3 * 8 * sizeof(unsigned long long)));
+        size_t max_segs = 0;
+        for (int t = 0; t < 3; ++t) {
+            std::vector<OzSeg> sg;
+            std::vector<int> b, pb, pc;
+            oz_schedule(N, grid, t, sg, b, pb, pc);
+            max_segs = std::max(max_segs, sg.size());
+            CU_TRY(cudaMalloc(&segs[t], std::max<size_t>(sg.size(), 1) * sizeof(OzSeg)));
+            if (int rc = dev_alloc(&begin[t], b.size())) return rc;
+            if (int rc = dev_alloc(&base[t], pb.size())) return rc;
+            if (int rc = dev_alloc(&count[t], pc.size())) return rc;
+            if (!sg.empty()) CU_TRY(copy_h2d(segs[t], sg.data(), sg.size() * sizeof(OzSeg)));
+            CU_TRY(copy_h2d(begin[t], b.data(), b.size() * sizeof(int)));
+            CU_TRY(copy_h2d(base[t], pb.data(), pb.size() * sizeof(int)));
+            CU_TRY(copy_h2d(count[t], pc.data(), pc.size() * sizeof(int)));
+        }
+        return dev_alloc(&part, std::max<size_t>(max_segs, 1) * oz_tile_rows() * 8);
+    }
+    // slices and row scales of matrix t, allocated on first use
+    int slice(int t, const double *M, cudaStream_t st) {
+        if (!s[t]) {
+            CU_TRY(cudaMalloc(&s[t], (size_t)oz_slices() * N * ld * sizeof(__nv_bfloat16)));
+            const size_t nr = (size_t)ntiles * oz_tile_rows();
+            if (int rc = dev_alloc(&r[t], nr)) return rc;
+            CU_TRY(cudaMemset(r[t], 0, nr * sizeof(double)));  // rows past N: scale 0
+        }
+        CU_TRY(oz_slice_matrix(M, N, ld, s[t], r[t], st));
+        return ELHL_OK;
+    }
+    void release() {
+        for (int t = 0; t < 3; ++t) {
+            if (s[t]) cudaFree(s[t]);
+            if (segs[t]) cudaFree(segs[t]);
+            s[t] = nullptr;
+            segs[t] = nullptr;
+            dev_free(r[t]); dev_free(begin[t]); dev_free(base[t]); dev_free(count[t]);
+        }
+        dev_free(v); dev_free(w); dev_free(part);
+        if (cnt) cudaFree(cnt);
+        if (cmax) cudaFree(cmax);
+        cnt = nullptr;
+        cmax = nullptr;
+    }
+};
+
 struct ChebState {
     int N = 0, ld = 0, m = 0, precision = ELHL_PREC_FP64, K = 0;
     int parity = 0;            // phi/acc role of col[0], col[1] for the device read-out path
@@ -647,6 +745,7 @@ struct ChebState {
     double *ntot = nullptr;    // [kMaxCols] FP64 totals of the last step's columns (renormalisation)
     double2 *saved = nullptr;  // [ld][m] input columns at the start of a call, for redone steps
     double guard = 0.01;       // Lanczos interval guard, fraction of the width
+    OzRes *oz = nullptr;       // ELHL_PREC_OZ64: operator products on the tensor cores (FP64 otherwise)
     bool ro64 = false;         // read-out matrices A, B in FP64 (else the launch precision)
     size_t ab_tsz = 0;         // element size A and B were allocated with
     // read-out outputs, owned by the trajectory
@@ -725,6 +824,11 @@ struct ChebState {
             hsplit[t] = vsplit[t] = nullptr;
         }
         umma = false;
+        if (oz) {
+            oz->release();
+            delete oz;
+            oz = nullptr;
+        }
         if (Gt) cudaFree(Gt);
         if (wb) cudaFree(wb);
         Gt = wb = nullptr;
@@ -756,8 +860,9 @@ __global__ void mirror_lower_kernel(double *A, int n, int ld) {
 int form_htilde(ChebState &cs, const double *G, const double *h, int ld, double *W) {
     cudaStream_t st = g_ctx.stream;
     const int n = cs.N;
-    CU_TRY(dgemm64(n, n, n, 1.0, G, ld, false, h, ld, false, 0.0, W, ld, st, kTriA));
-    CU_TRY(dgemm64(n, n, n, 1.0, W, ld, false, G, ld, true, 0.0, cs.Ht, cs.ld, st, kTriBt | kTriLowerC));
+    const bool tc = cs.oz != nullptr;  // ELHL_PREC_OZ64: large products on the tensor cores
+    CU_TRY(fgemm(tc, n, n, n, 1.0, G, ld, false, h, ld, false, 0.0, W, ld, st, kTriA));
+    CU_TRY(fgemm(tc, n, n, n, 1.0, W, ld, false, G, ld, true, 0.0, cs.Ht, cs.ld, st, kTriBt | kTriLowerC));
     mirror_lower_kernel<<<dim3((n + 127) / 128, n), 128, 0, st>>>(cs.Ht, n, cs.ld);
     count_launch();
     CU_TRY(cudaGetLastError());
@@ -944,6 +1049,8 @@ int cheb_prepare(ChebState &cs, double dt, double tol, const double *h = nullptr
     CU_TRY(cudaMemcpyAsync(cs.coef, c.data(), (K + 1) * sizeof(double2), cudaMemcpyHostToDevice, st));
     CU_TRY(cudaStreamSynchronize(st));  // c is a host temporary
     cs.K = K;
+    if (cs.oz)  // the tensor-core propagation reads Hs as BF16 slices
+        if (int rc = cs.oz->slice(1, static_cast<const double *>(cs.Hs), st)) return rc;
     if (cs.umma && !h) {  // the tensor-core GEMM reads Hs as three BF16 terms
         if (int rc = split3_bf16(reinterpret_cast<const float *>(cs.Hs), cs.N, cs.N, cs.ld, cs.hsplit, cs.ld, false, st))
             return rc;
@@ -1152,6 +1259,11 @@ int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, do
         count_launch();
         convert_kernel<double><<<grid, 128, 0, st>>>(Lfac, (double *)cs.B, n, ld, true);
         count_launch();
+        CU_TRY(cudaGetLastError());
+        if (cs.oz) {  // G^T v and G y on the tensor cores: slices of G's columns and of G^T's
+            if (int rc = cs.oz->slice(0, static_cast<const double *>(cs.A), st)) return rc;
+            if (int rc = cs.oz->slice(2, static_cast<const double *>(cs.Gt), st)) return rc;
+        }
     } else {
         convert_kernel<float><<<grid, 128, 0, st>>>(cs.Ht, (float *)cs.A, n, ld, false);
         count_launch();
@@ -1432,6 +1544,7 @@ struct ChebPlan {
     int nphase = 1;            // 3: one implicit problem
     int mgcd = 0;              // gcd of the problems' column counts
     bool tuned = false;        // tile measured (on the plan's first run)
+    OzRes *oz = nullptr;       // one ELHL_PREC_OZ64 trajectory: the tensor-core propagation
     size_t pops_per_step = 0;  // populations of all problems in one step
     void release() {
         dev_free(d_probs); dev_free(d_segs); dev_free(d_seg_begin); dev_free(d_prob_seg0); dev_free(d_seg_pops);
@@ -1577,6 +1690,7 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
     }
     pl.mgcd = mgcd;
     pl.tuned = false;  // measured on the first run (plans of batch members never run)
+    pl.oz = states.size() == 1 ? states[0]->oz : nullptr;
     return ELHL_OK;
 }
 
@@ -1671,8 +1785,52 @@ int tune_plan(ChebPlan &pl, int mgcd) {
 unsigned long long g_dbg_barrier_ns = 0;
 int g_dbg_exit_cta1 = 0;
 
+// The propagation launch of an ELHL_PREC_OZ64 plan (one problem, m <= 4).
+int oz_run(ChebPlan &pl) {
+    cudaStream_t st = g_ctx.stream;
+    OzRes &oz = *pl.oz;
+    const ChebProblem &p = pl.probs[0];
+    OzLaunch L{};
+    L.N = p.N; L.ld = p.ld; L.K = p.K; L.m = p.m; L.P = p.P;
+    L.nphase = pl.nphase;
+    L.coef = p.coef;
+    L.phi = p.col[pl.parity];
+    L.acc = p.col[pl.parity ^ 1];
+    L.scale = p.scale;
+    L.v = oz.v;
+    L.w = oz.w;
+    L.shift = p.shift;
+    for (int t = 0; t < 3; ++t) {
+        L.rscale[t] = oz.r[t] ? oz.r[t] : oz.r[1];
+        L.segs[t] = oz.segs[t];
+        L.seg_begin[t] = oz.begin[t];
+        L.part_base[t] = oz.base[t];
+        L.part_count[t] = oz.count[t];
+    }
+    L.part = oz.part;
+    L.tile_cnt = oz.cnt;
+    L.colmax = oz.cmax;
+    L.bar_count = g_ctx.bar;
+    L.bar_gen = g_ctx.bar + 1;
+    L.error = g_ctx.err;
+    L.barrier_ns = g_dbg_barrier_ns;
+    L.exit_cta1 = g_dbg_exit_cta1;
+    g_dbg_exit_cta1 = 0;  // one launch only
+    if (p.m > 4 || !oz.s[1] || (pl.nphase == 3 && (!oz.s[0] || !oz.s[2]))) return ELHL_ERR_UNSUPPORTED;
+    CU_TRY(cudaMemsetAsync(g_ctx.err, 0, sizeof(int), st));
+    CU_TRY(cudaMemsetAsync(g_ctx.bar, 0, 2 * sizeof(unsigned), st));
+    CU_TRY(cudaMemsetAsync(oz.cnt, 0, (size_t)oz.ntiles * sizeof(unsigned), st));
+    CU_TRY(cudaMemsetAsync(oz.cmax, 0, 3 * 8 * sizeof(unsigned long long), st));
+    const __nv_bfloat16 *sl[3] = {oz.s[0], oz.s[1], oz.s[2]};
+    CU_TRY(cudaEventRecord(g_ctx.ev[0], st));
+    CU_TRY(launch_oz_cheb(L, sl, oz.grid, st));
+    CU_TRY(cudaEventRecord(g_ctx.ev[1], st));
+    return ELHL_OK;
+}
+
 int cheb_run(ChebPlan &pl) {
     cudaStream_t st = g_ctx.stream;
+    if (pl.oz) return oz_run(pl);
     if (!pl.tuned) {
         if (int rc = tune_plan(pl, pl.mgcd)) return rc;
         pl.tuned = true;
@@ -2780,7 +2938,8 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
     const bool taylor_p = tr->cfg.nparticles == 2;
     const bool cheb_ok = tr->cfg.method == ELHL_METHOD_CHEBYSHEV &&
                          (tr->cfg.precision == ELHL_PREC_FP64 || tr->cfg.precision == ELHL_PREC_FP32 ||
-                          tr->cfg.precision == ELHL_PREC_BF16X3 || tr->cfg.precision == ELHL_PREC_DF64) &&
+                          tr->cfg.precision == ELHL_PREC_BF16X3 || tr->cfg.precision == ELHL_PREC_DF64 ||
+                          (tr->cfg.precision == ELHL_PREC_OZ64 && tr->cfg.ncols <= 4)) &&
                          tr->cfg.nparticles >= 1 && tr->cfg.nparticles <= 64 &&
                          (tr->cfg.ncols == tr->cfg.nparticles || tr->cfg.ncols == 2 * tr->cfg.nparticles) &&
                          tr->cfg.cheb_tol > 0.0;
@@ -2822,7 +2981,14 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
     if (!rc && cudaStreamSynchronize(g_ctx.stream) != cudaSuccess) rc = ELHL_ERR_CUDA;
     if (!rc && !tr->cheb()) rc = tr->fac.check_info();  // the Chebyshev set-up factors S below
     if (!rc && tr->cheb()) {
-        rc = tr->cs.alloc(tr->N, tr->cfg.ncols, tr->cfg.precision);
+        const bool oz = tr->cfg.precision == ELHL_PREC_OZ64;  // FP64 state, tensor-core propagation
+        rc = tr->cs.alloc(tr->N, tr->cfg.ncols, oz ? ELHL_PREC_FP64 : tr->cfg.precision);
+        if (!rc && oz) {
+            int grid = 0;
+            tr->fac.tc = true;
+            tr->cs.oz = new OzRes();
+            rc = cheb_grid_size(&grid) ? ELHL_ERR_CUDA : tr->cs.oz->init(tr->N, tr->ld, grid);
+        }
         tr->cs.guard = tr->cfg.lanczos_guard;
         if (!rc) rc = dev_alloc(&tr->psi_ao, (size_t)tr->ld * tr->P);
         if (!rc) rc = dev_alloc(&tr->bra_ao, (size_t)tr->ld * tr->P);
@@ -3323,7 +3489,7 @@ extern "C" {
 int elhl_batch_create(int ntraj, const elhl_basis_desc *bases, const double *const *coords,
                       const elhl_traj_config *cfg, elhl_batch **out) {
     if (!out || ntraj <= 0 || !bases || !coords || !cfg) return ELHL_ERR_BAD_ARG;
-    if (cfg->method != ELHL_METHOD_CHEBYSHEV) return ELHL_ERR_UNSUPPORTED;
+    if (cfg->method != ELHL_METHOD_CHEBYSHEV || cfg->precision == ELHL_PREC_OZ64) return ELHL_ERR_UNSUPPORTED;
     *out = nullptr;
     elhl_batch *b = new elhl_batch();
     int rc = ELHL_OK;
@@ -3539,7 +3705,7 @@ extern "C" {
 
 int elhl_server_create(double hbm_budget_bytes, const elhl_traj_config *cfg, elhl_server **out) {
     if (!out || !cfg || !(hbm_budget_bytes > 0.0)) return ELHL_ERR_BAD_ARG;
-    if (cfg->method != ELHL_METHOD_CHEBYSHEV) return ELHL_ERR_UNSUPPORTED;
+    if (cfg->method != ELHL_METHOD_CHEBYSHEV || cfg->precision == ELHL_PREC_OZ64) return ELHL_ERR_UNSUPPORTED;
     if (int rc = ensure_context()) return rc;
     elhl_server *sv = new elhl_server();
     sv->cfg = *cfg;

@@ -167,6 +167,46 @@ int split3_bf16(const float *src, int rows, int cols, int lds, __nv_bfloat16 *co
 int umma_bf16x3_gemm(const __nv_bfloat16 *const A[3], int lda, const __nv_bfloat16 *const B[3], int ldb, int rows,
                      int K, int n2, int splits, float *Y, int *d_error, cudaStream_t st);
 
+// FP64 Chebyshev propagation by exact BF16 slices on the tensor cores
+// (ozaki.cu).  A phase's work: 64-K blocks of 128-row tiles; OzSeg is one CTA's
+// run of blocks [kb0, kb1) in row tile rt, the slot-th segment of that tile.
+struct OzSeg {
+    int rt, kb0, kb1, slot;
+};
+struct OzLaunch {
+    int N, ld, K, m, P;          // size, padded rows, last order, complex columns (<= 4), particles
+    int nphase;                  // 1: explicit Hs (matrix 1); 3: G^T (matrix 0), h/b (1), G (2)
+    const double2 *coef;         // [K+1] expansion coefficients
+    const double2 *phi;          // [ld][m] input columns
+    double2 *acc;                // [ld][m] output columns (sum of c_k v_k)
+    const double *scale;         // [P] renormalisation factor of the input, or nullptr
+    double *v;                   // [3][ld][8] Chebyshev vectors (re, im of 4 columns; padding rows zero)
+    double *w;                   // [2][ld][8] implicit phase outputs
+    double shift;                // a / b (implicit)
+    const double *rscale[3];     // [tiles * 128] power-of-two row scales of the sliced matrices
+    const OzSeg *segs[3];        // per schedule: 0 upper (G^T), 1 full, 2 lower (G)
+    const int *seg_begin[3];     // [grid + 1]
+    const int *part_base[3];     // [tiles] first partial slot of a row tile
+    const int *part_count[3];    // [tiles] segments of a row tile
+    double *part;                // partial tiles [slot][128][8]
+    unsigned *tile_cnt;          // [tiles] segments finished (reset by the last)
+    unsigned long long *colmax;  // [3][8] bits of the largest |x| per real column, by phase sequence
+    unsigned *bar_count, *bar_gen;
+    int *error;
+    unsigned long long barrier_ns;  // grid-barrier limit (0: default)
+    int exit_cta1;                  // test hook: 1 + the CTA that leaves before its first barrier
+};
+int oz_slices();
+int oz_tile_rows();
+int oz_block_k();
+size_t oz_smem_bytes();
+// slices [oz_slices()][n][ld] of the n storage columns of M (ld rows), scale per column
+cudaError_t oz_slice_matrix(const double *M, int n, int ld, __nv_bfloat16 *out, double *rscale, cudaStream_t st);
+// schedule type 0 (upper), 1 (full) or 2 (lower) of an n x n operator over grid CTAs
+void oz_schedule(int n, int grid, int type, std::vector<OzSeg> &segs, std::vector<int> &seg_begin,
+                 std::vector<int> &part_base, std::vector<int> &part_count);
+cudaError_t launch_oz_cheb(const OzLaunch &L, const __nv_bfloat16 *const slices[3], int grid, cudaStream_t st);
+
 // C = alpha A op(B) + beta C in double-float arithmetic on the FP32 pipes (dfgemm.cu),
 // column-major operands stored as DF64 pairs (float2 = hi + lo), op(B) = B^T
 // when transB.  `tri` marks lower-
@@ -183,6 +223,14 @@ cudaError_t dfgemm(int m, int n, int k, double alpha, const float2 *A, int lda, 
 // three quarters of the resident CTA slots.
 cudaError_t dgemm64(int m, int n, int k, double alpha, const double *A, int lda, bool transA, const double *B, int ldb,
                     bool transB, double beta, double *C, int ldc, cudaStream_t st, int tri = 0, int lane = 0);
+// The same product on the tensor cores from exact BF16 slices (ozgemm.cu):
+// FP64-accurate (each output exact until one rounding, products below 2^-64 of
+// the row and column scales dropped), for large products; lane as for dgemm64.
+// A timeout of its bounded waits sets *ozgemm_error(lane) to ELHL_ERR_TIMEOUT.
+cudaError_t ozgemm(int m, int n, int k, double alpha, const double *A, int lda, bool transA, const double *B, int ldb,
+                   bool transB, double beta, double *C, int ldc, cudaStream_t st, int tri = 0, int lane = 0);
+int *ozgemm_error(int lane);
+size_t ozgemm_smem_bytes();
 // rows x n block of an FP64 matrix (leading dimension ld) to DF64 pairs in
 // place (to_pairs) or back
 cudaError_t df_convert(double *x, int rows, int n, int ld, bool to_pairs, cudaStream_t st);

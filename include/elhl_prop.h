@@ -116,10 +116,15 @@ enum {
                              hi + lo (48-bit significands) with exact-product / TwoSum arithmetic on the
                              FP32 pipes, FP64 recurrence and sums: FP64-level accuracy (1e-10 populations)
                              without the FP64 pipe; read-out through FP64 library products */
-    ELHL_PREC_BF16X3 = 2  /* Chebyshev: as FP32, but those GEMMs run on the tensor cores with each
+    ELHL_PREC_BF16X3 = 2, /* Chebyshev: as FP32, but those GEMMs run on the tensor cores with each
                              FP32 operand split in three bf16 terms: a hand-written tcgen05/TMA kernel
                              for 16, 32 or 64 columns (cuBLAS emulation otherwise); outside the GEMM
                              regime it runs as FP32 */
+    ELHL_PREC_OZ64 = 4    /* Chebyshev, trajectories with ncols <= 4: FP64 operator, vectors and
+                             recurrence, with every operator product computed exactly on the tensor
+                             cores from 7 bf16 slices of 8 bits per operand (Ozaki scheme I, products
+                             below 2^-64 of a row's scale dropped) and rounded once to FP64; set-up
+                             (factorisation, bounds, read-out) as ELHL_PREC_FP64 */
 };
 
 /* STO basis of one system (the STO_basis fields the path reads, types_EHT.f:135-165). */

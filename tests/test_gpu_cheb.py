@@ -229,15 +229,17 @@ def test_df64_cluster_vs_exact(elhl, oracle_mod):
 
 
 @pytest.mark.parametrize("n_atoms,nao", [(20, 62), (64, 199), (150, 465), (600, 1860)])
-@pytest.mark.parametrize("prec_name,tol", [("fp64", 1e-12), ("df64", 1e-11), ("fp32", 1e-11)])
+@pytest.mark.parametrize("prec_name,tol", [("fp64", 1e-12), ("df64", 1e-11), ("fp32", 1e-11), ("oz64", 1e-12)])
 def test_rebuild_factor_and_inverse(elhl, prec_name, tol, n_atoms, nao):
-    """The moving-nuclei rebuild's factorisations: FP64 runs potrf and the
-    recursive inverse of L, DF64 and FP32 the double-float Cholesky-with-inverse.
+    """The moving-nuclei rebuild's factorisations: FP64 the recursive
+    Cholesky-with-inverse on the FP64 pipe, OZ64 the same recursion with its
+    products of 128 or more rows on the tensor cores (exact slices), DF64 and
+    FP32 the double-float Cholesky-with-inverse.
     N = 62 is one leaf, 199 and 465 stay below the 512-row bottom-up block, 1860
     has a short last 64-row leaf and short pairs in the batched levels.
     L L^T = S, G L = I, L against numpy's Cholesky of the same S, both factors
     lower triangular."""
-    prec = {"fp64": elhl.PREC_FP64, "df64": elhl.PREC_DF64, "fp32": elhl.PREC_FP32}[prec_name]
+    prec = {"fp64": elhl.PREC_FP64, "df64": elhl.PREC_DF64, "fp32": elhl.PREC_FP32, "oz64": elhl.PREC_OZ64}[prec_name]
     sysm = systems.cubic_cluster(n_atoms=n_atoms, seed=11)
     coords = np.stack([systems.perturbed_coords(sysm.coords, i, seed=5) for i in range(2)])
     tr = elhl.Trajectory(sysm, coords=coords[0], dt=2e-4, method=elhl.METHOD_CHEBYSHEV, precision=prec, ncols=4,

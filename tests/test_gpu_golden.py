@@ -4,7 +4,7 @@ config-2 cluster (N = 3720) with moving nuclei.  The fixtures hold the oracle's
 outputs (Taylor restatement of Taylor.f at tolerance 1e-12, and the exact
 generalized-eigenbasis propagator of ElHl_schroedinger.f:131-147), so these
 tests compare the CUDA path with the oracle without running the oracle here.
-Bar: populations within 1e-10 (FP64 and DF64)."""
+Bar: populations within 1e-10 (FP64, DF64 and OZ64)."""
 import os
 
 import numpy as np
@@ -33,7 +33,7 @@ def test_small_matrices_vs_golden(elhl):
     assert np.abs(Hp - g["Hp"]).max() < 1e-10 * np.abs(g["Hp"]).max()
 
 
-@pytest.mark.parametrize("method,prec", [("taylor", "fp64"), ("cheb", "fp64"), ("cheb", "df64")])
+@pytest.mark.parametrize("method,prec", [("taylor", "fp64"), ("cheb", "fp64"), ("cheb", "df64"), ("cheb", "oz64")])
 def test_small_moving_nuclei_vs_golden(elhl, method, prec):
     g = _load("small16.npz")
     cl = systems.cubic_cluster(n_atoms=16, seed=11, frag_atoms=6)
@@ -41,7 +41,8 @@ def test_small_moving_nuclei_vs_golden(elhl, method, prec):
     homo = int(g["homo"])
     kw = dict(dt=float(g["dt"]), tol=1e-12, norm_tol=1e-12)
     if method == "cheb":
-        kw.update(method=elhl.METHOD_CHEBYSHEV, precision={"fp64": elhl.PREC_FP64, "df64": elhl.PREC_DF64}[prec],
+        kw.update(method=elhl.METHOD_CHEBYSHEV,
+                  precision={"fp64": elhl.PREC_FP64, "df64": elhl.PREC_DF64, "oz64": elhl.PREC_OZ64}[prec],
                   ncols=4, cheb_tol=1e-14)
     tr = elhl.Trajectory(cl, coords=coords[0], **kw)
     tr.init_fmo(homo + 1, homo)
@@ -63,14 +64,15 @@ def test_flake_taylor_200_steps_vs_golden(elhl, flake):
     assert np.abs(pops[199] - g["taylor200"]).max() < 1e-10
 
 
-@pytest.mark.parametrize("prec", ["fp64", "df64"])
+@pytest.mark.parametrize("prec", ["fp64", "df64", "oz64"])
 def test_flake_chebyshev_2000_steps_vs_golden(elhl, flake, prec):
     """Config 1 in full: 2,000 fixed-nuclei steps at dt 0.1 fs against the exact
     propagator (and the Taylor oracle at step 200).  DF64 runs the implicit
-    operator G (h/b) G^T, FP64 the explicit H~."""
+    operator G (h/b) G^T, FP64 and OZ64 (products on the tensor cores) the
+    explicit H~."""
     g = _load("flake.npz")
     homo = int(g["homo"])
-    p = {"fp64": elhl.PREC_FP64, "df64": elhl.PREC_DF64}[prec]
+    p = {"fp64": elhl.PREC_FP64, "df64": elhl.PREC_DF64, "oz64": elhl.PREC_OZ64}[prec]
     tr = elhl.Trajectory(flake, dt=1e-4, method=elhl.METHOD_CHEBYSHEV, precision=p, ncols=4, cheb_tol=1e-14)
     tr.init_fmo(homo + 1, homo)
     pops = tr.step(None, nsteps=2000)
@@ -82,7 +84,7 @@ def test_flake_chebyshev_2000_steps_vs_golden(elhl, flake, prec):
     assert st.norm_drift < 1e-10  # per-step unitarity held throughout
 
 
-@pytest.mark.parametrize("prec", ["fp64", "df64"])
+@pytest.mark.parametrize("prec", ["fp64", "df64", "oz64"])
 def test_cluster1200_moving_nuclei_vs_golden(elhl, prec):
     """Config 2 at its size (1,200 atoms, N = 3720): two moving-nuclei steps
     (S, h, the factor and its inverse rebuilt each step) against the Taylor
@@ -92,7 +94,7 @@ def test_cluster1200_moving_nuclei_vs_golden(elhl, prec):
     assert cl.nao == 3720
     coords = np.stack([systems.perturbed_coords(cl.coords, i, sigma=0.02, seed=2) for i in range(3)])
     homo = int(g["homo"])
-    p = {"fp64": elhl.PREC_FP64, "df64": elhl.PREC_DF64}[prec]
+    p = {"fp64": elhl.PREC_FP64, "df64": elhl.PREC_DF64, "oz64": elhl.PREC_OZ64}[prec]
     tr = elhl.Trajectory(cl, coords=coords[0], dt=float(g["dt"]), method=elhl.METHOD_CHEBYSHEV, precision=p,
                          ncols=4, cheb_tol=1e-14)
     tr.init_fmo(homo + 1, homo)

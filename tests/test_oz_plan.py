@@ -1,0 +1,231 @@
+"""Host replays of the tensor-core FP64 arithmetic of ELHL_PREC_OZ64 (the
+propagation in dynemol_gb300/csrc/ozaki.cu, the factorisation products in
+dynemol_gb300/csrc/ozgemm.cu), checked on the CPU before any GPU run:
+
+* the block schedules (oz_schedule): for the full, upper (A = G^T) and lower
+  (A = G) operators every non-zero 128 x 64 block of the operator is given to
+  exactly one CTA, CTAs differ by at most one block, a row tile's segments are
+  numbered in K order and their partial slots fit the partial buffer;
+* the arithmetic: operands cut into 7 slices of 8 bits on a power-of-two row
+  (column) scale exactly as the kernels do (slice7: one rounding to a 64-bit
+  integer, then balanced base-256 digits),
+  products of slices accumulated over 256-K groups, where every sum of
+  absolute products must stay at or below 2^24 (so that the tensor cores' FP32
+  accumulation is exact), and the pairs with s_a + s_b <= 6 combined in one
+  exact integer per row and column; the result must agree with the exact
+  (rational) product to within an FP64 dot product's rounding bound plus the
+  slices' own truncation (2^-54.5 of the row and column scales per k),
+  including rows and columns of very different scales;
+* the products' weight sums (ozgemm: all slice pairs of one weight share an
+  accumulator over a 64-K block) against the same 2^24 bound, and their fold
+  into two 64-bit integers.
+The constants are read from the kernel sources."""
+
+import os
+import re
+from fractions import Fraction
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+OZ = open(os.path.join(ROOT, "dynemol_gb300", "csrc", "ozaki.cu")).read()
+
+
+def _const(name):
+    m = re.search(r"\b%s = (\d+)" % name, OZ)
+    assert m, name
+    return int(m.group(1))
+
+
+S, TILE, KB, GROUP = _const("kS"), _const("kTileM"), _const("kKB"), _const("kGroupBlocks")
+GRID = 152
+
+
+def schedule(n, grid, typ):
+    """oz_schedule: (segments, seg_begin, part_base, part_count); a segment is (rt, kb0, kb1, slot)."""
+    nkb, ntiles = -(-n // KB), -(-n // TILE)
+    lo, hi = [], []
+    for rt in range(ntiles):
+        h = min(nkb, 2 * rt + 2) if typ == 2 else nkb
+        lo.append(min(2 * rt if typ == 0 else 0, h))
+        hi.append(h)
+    total = sum(h - l for l, h in zip(lo, hi))
+    segs, begin, count = [], [0], [0] * ntiles
+    rt, pos = 0, 0
+    for b in range(grid):
+        u0, u1 = total * b // grid, total * (b + 1) // grid
+        while u0 < u1:
+            while rt < ntiles and u0 >= pos + (hi[rt] - lo[rt]):
+                pos += hi[rt] - lo[rt]
+                rt += 1
+            end = min(u1, pos + (hi[rt] - lo[rt]))
+            segs.append((rt, lo[rt] + u0 - pos, lo[rt] + end - pos, count[rt]))
+            count[rt] += 1
+            u0 = end
+        begin.append(len(segs))
+    base = [0] * ntiles
+    for t in range(1, ntiles):
+        base[t] = base[t - 1] + count[t - 1]
+    return segs, begin, base, count
+
+
+def test_schedule_source_matches_replay():
+    """The replay follows the source's block ranges (guard against drift)."""
+    assert "lo[rt] = type == 0 ? 2 * rt : 0;" in OZ
+    assert "hi[rt] = type == 2 ? std::min(nkb, 2 * rt + 2) : nkb;" in OZ
+    assert "long long u0 = total * b / grid;" in OZ
+
+
+@pytest.mark.parametrize("n", [1, 2, 8, 63, 64, 65, 127, 128, 129, 450, 1000, 1860, 2170, 3720, 4096, 8192, 16384])
+@pytest.mark.parametrize("typ", [0, 1, 2])
+def test_schedule_covers_nonzero_blocks_once(n, typ):
+    segs, begin, base, count = schedule(n, GRID, typ)
+    nkb, ntiles = -(-n // KB), -(-n // TILE)
+    seen = np.zeros((ntiles, nkb), dtype=int)
+    for rt, k0, k1, slot in segs:
+        assert 0 <= rt < ntiles and 0 <= k0 < k1 <= nkb
+        seen[rt, k0:k1] += 1
+    # a block is needed iff some (row, k) inside it with row, k < n lies in the operator's triangle
+    for rt in range(ntiles):
+        for kb in range(nkb):
+            r0, r1 = rt * TILE, min(n, rt * TILE + TILE) - 1
+            k0, k1 = kb * KB, min(n, kb * KB + KB) - 1
+            need = {0: k1 >= r0, 1: True, 2: k0 <= r1}[typ]
+            assert seen[rt, kb] == (1 if need else 0), (rt, kb)
+    per_cta = [sum(s[2] - s[1] for s in segs[begin[b]:begin[b + 1]]) for b in range(GRID)]
+    assert max(per_cta) - min(per_cta) <= 1
+    # segments of a row tile: slots 0.. in K order; partial slots within the buffer
+    for rt in range(ntiles):
+        mine = sorted([s for s in segs if s[0] == rt], key=lambda s: s[3])
+        assert [s[3] for s in mine] == list(range(count[rt]))
+        assert all(mine[i][2] == mine[i + 1][1] for i in range(len(mine) - 1))
+        assert base[rt] + count[rt] <= len(segs)
+    assert len(segs) <= GRID + ntiles
+
+
+def scale_exp(mx):
+    """The kernel's scale_exp: e with |x| < 2^e from the biased exponent (0 for 0)."""
+    if not mx > 0.0:
+        return 0
+    return int((np.float64(mx).view(np.int64) >> 52) & 0x7FF) - 1022
+
+
+def slices(x, e):
+    """x (1-D) on scale 2^e cut as slice7 (tc_ptx.cuh) does: T = rint(x 2^-e 2^56) as a
+    64-bit integer, then balanced base-256 digits from the bottom."""
+    T = np.rint(x * np.ldexp(1.0, -e) * 2.0 ** 56).astype(np.int64)
+    out = [None] * S
+    for s in range(S - 1, 0, -1):
+        d = ((T + 128) & 255) - 128
+        out[s] = d
+        T = (T - d) >> 8
+    out[0] = T
+    return np.array(out, dtype=np.float64)  # [S][len]
+
+
+def test_slice7_source_matches_replay():
+    src = open(os.path.join(ROOT, "dynemol_gb300", "csrc", "tc_ptx.cuh")).read()
+    assert "long long T = __double2ll_rn(xs * 0x1p56);" in src
+    assert "const int d = (int)(((T + 128) & 255) - 128);" in src
+    assert "T = (T - d) >> 8;" in src
+
+
+def oz_product(A, X):
+    """y = A X as the kernel computes it (one CTA segment over all of K)."""
+    m, K = A.shape
+    er = [scale_exp(np.abs(A[i]).max()) for i in range(m)]
+    ec = [scale_exp(np.abs(X[:, c]).max()) for c in range(X.shape[1])]
+    As = np.stack([slices(A[i], er[i]) for i in range(m)], axis=1)      # [S][m][K]
+    Xs = np.stack([slices(X[:, c], ec[c]) for c in range(X.shape[1])], axis=2)  # [S][K][c]
+    assert np.abs(As[0]).max() <= 256 and np.abs(As[1:]).max() <= 128
+    assert np.abs(Xs[0]).max() <= 256 and np.abs(Xs[1:]).max() <= 128
+    ai, xi = As.astype(np.int64), Xs.astype(np.int64)
+    y = np.zeros((m, X.shape[1]))
+    for i in range(m):
+        for c in range(X.shape[1]):
+            T = 0
+            for g0 in range(0, K, GROUP * KB):
+                g = slice(g0, g0 + GROUP * KB)
+                for a in range(S):
+                    for b in range(S - a):
+                        pa, pb = ai[a, i, g], xi[b, g, c]
+                        assert int(np.abs(pa * pb).sum()) <= 1 << 24  # exact FP32 accumulation
+                        T += int((pa * pb).sum()) << (8 * (S - 1 - a - b))
+            y[i, c] = float(Fraction(T, 1 << 64) * Fraction(2) ** (er[i] + ec[c]))
+    return y
+
+
+def oz_bound(A, X):
+    """An FP64 dot product's rounding bound 2^-53 sum |a| |x|, plus what the slices
+    leave out: per k at most 2^-54.5 of the row and column scales 2^(e_r + e_c)
+    (residuals below 2^-57 of each scale, dropped products of weight d >= 7)."""
+    er = np.array([scale_exp(np.abs(A[i]).max()) for i in range(A.shape[0])], dtype=float)
+    ec = np.array([scale_exp(np.abs(X[:, c]).max()) for c in range(X.shape[1])], dtype=float)
+    return (np.abs(A) @ np.abs(X)) * 2.0 ** -53 + A.shape[1] * 2.0 ** (er[:, None] + ec[None, :] - 54) + 1e-300
+
+
+def exact_product(A, X):
+    return np.array([[float(sum(Fraction(float(A[i, k])) * Fraction(float(X[k, c])) for k in range(A.shape[1])))
+                      for c in range(X.shape[1])] for i in range(A.shape[0])])
+
+
+def test_slice_product_matches_exact_product():
+    rng = np.random.default_rng(7)
+    m, K = 6, 700  # three 256-K groups, the last partial
+    A = rng.standard_normal((m, K)) * np.exp(rng.uniform(-12, 2, (m, K)))  # wide dynamic range per row
+    A[1] *= 1e-9   # a tiny row
+    A[2, ::7] = 0.0
+    X = rng.standard_normal((K, 8))
+    X[:, 3] *= 1e-12  # a tiny column
+    X[:, 5] = 0.0     # an unused column
+    y = oz_product(A, X)
+    ref = exact_product(A, X)
+    assert np.all(np.abs(y - ref) <= oz_bound(A, X))
+    assert np.all(y[:, 5] == 0.0)
+
+
+OZG = open(os.path.join(ROOT, "dynemol_gb300", "csrc", "ozgemm.cu")).read()
+
+
+def test_gemm_constants_match_source():
+    assert re.search(r"\bkS = (\d+)", OZG).group(1) == str(S)
+    assert "constexpr int kTM = 128, kTN = 32, kKB = 64;" in OZG
+    assert "if (d <= 2) H[c] += x * (1ll << (8 * (2 - d)));" in OZG
+    assert "else L[c] += x * (1ll << (8 * (kS - 1 - d)));" in OZG
+
+
+def test_gemm_weight_sums_are_exact_and_fold_to_the_product():
+    """ozgemm: per 64-K block the products of equal weight d = a + b share one FP32
+    accumulator; every such sum of absolute products must stay at or below 2^24,
+    the folds H (d <= 2) and L (d >= 3) must stay inside int64 over all blocks, and
+    2^-64 (2^32 H + L) times the scales must agree with the exact product.  The
+    lower-triangular masks of kTriA / kTriBt are applied as the slicing does."""
+    rng = np.random.default_rng(11)
+    m, n, k = 5, 4, 300
+    A = rng.standard_normal((m, k)) * np.exp(rng.uniform(-10, 3, (m, k)))
+    B = rng.standard_normal((k, n))
+    B[:, 2] *= 1e-7
+    A[np.arange(m)[:, None] < np.arange(k)[None, :] - 200] = 0.0  # zero upper band, as a triangular operand
+    er = [scale_exp(np.abs(A[i]).max()) for i in range(m)]
+    ec = [scale_exp(np.abs(B[:, j]).max()) for j in range(n)]
+    As = np.stack([slices(A[i], er[i]) for i in range(m)], axis=1).astype(np.int64)     # [S][m][k]
+    Bs = np.stack([slices(B[:, j], ec[j]) for j in range(n)], axis=2).astype(np.int64)  # [S][k][n]
+    out = np.zeros((m, n))
+    for i in range(m):
+        for j in range(n):
+            H = L = 0
+            for k0 in range(0, k, KB):
+                g = slice(k0, k0 + KB)
+                for d in range(S):
+                    terms = [As[a, i, g] * Bs[d - a, g, j] for a in range(d + 1)]
+                    assert sum(int(np.abs(t).sum()) for t in terms) <= 1 << 24
+                    acc = sum(int(t.sum()) for t in terms)
+                    if d <= 2:
+                        H += acc << (8 * (2 - d))
+                    else:
+                        L += acc << (8 * (S - 1 - d))
+                assert abs(H) < 1 << 62 and abs(L) < 1 << 62
+            out[i, j] = float(Fraction((H << 32) + L, 1 << 64) * Fraction(2) ** (er[i] + ec[j]))
+    ref = exact_product(A, B)
+    assert np.all(np.abs(out - ref) <= oz_bound(A, B))
