@@ -242,20 +242,23 @@ def run_ours(args, rank, world):
         bytes_per_launch = per_launch_orders * (16.0 * N * N + 160.0 * N)
         flops_per_launch = per_launch_orders * 8.0 * N * N
     else:
-        # dominant kernel: cheb_kernel.  Unit = one Chebyshev order over m complex
-        # columns.  Fixed nuclei (explicit Hs): Hs read once (b_H N^2) + 5 x 16 N m
-        # vector bytes, flops 4 N^2 m.  Moving nuclei (implicit G (h/b) G^T, three
+        # dominant kernel: cheb_kernel (oz_cheb_kernel for OZ64).  Unit = one Chebyshev
+        # order over m complex columns.  Explicit Hs: Hs read once (b_H N^2) + 5 x 16 N m
+        # vector bytes, flops 4 N^2 m.  Implicit G (h/b) G^T (moving nuclei, three
         # phases): N^2/2 + N^2 + N^2/2 matrix elements (b_H 2 N^2) + 9 x 16 N m vector
         # bytes, flops 8 N^2 m
         kernel = "oz_cheb_kernel" if args.precision == "oz64" else "cheb_kernel"
         m = 4 if moving else 2
         # bytes per matrix element: FP64 / DF64 pairs 8, FP32 4, OZ64 seven BF16 slices 14
         bH = {"fp64": 8.0, "df64": 8.0, "oz64": 14.0}.get(args.precision, 4.0)
-        elems, vec = (2.0 * N * N, 144.0) if moving else (1.0 * N * N, 80.0)
+        # the implicit operator (three grid phases) reads 2 N^2 elements per order, an
+        # explicit H~ (one phase: fixed nuclei, and OZ64 moving nuclei) N^2
+        implicit = st.phases == 3 if method == api.METHOD_CHEBYSHEV else False
+        elems, vec = (2.0 * N * N, 144.0) if implicit else (1.0 * N * N, 80.0)
         per_launch_orders = orders / max(1, K) / m
         bytes_per_launch = per_launch_orders * (bH * elems + vec * N * m)
         flops_per_launch = per_launch_orders * 4.0 * elems * m
-        if moving and args.precision in ("fp64", "df64"):
+        if implicit and args.precision in ("fp64", "df64"):
             # DRAM traffic per matrix element and order measured by ncu on the same
             # kernel at N = 2790 (18.68 GB read + 0.11 GB written over 149 orders of
             # 2 N^2 elements); traffic grows with N^2 and the orders, so it is scaled
@@ -310,7 +313,7 @@ def run_ours(args, rank, world):
                      "orders_per_launch": per_launch_orders, "launch_ms": prop_launch_ms},
         "breakdown_ms_per_step": {"propagation": prop_ms / K, "rebuild_S_h_operator": rebuild_ms / K,
                                   "rebuild_parts": {"S_h_build": sh_ms / K, "cholesky": factor_ms / K,
-                                                    "inverse_L": inverse_ms / K,
+                                                    "operator_form": inverse_ms / K,
                                                     "bounds_columns_other": (rebuild_ms - sh_ms - factor_ms
                                                                              - inverse_ms) / K}},
         "clocks": clk,

@@ -249,7 +249,7 @@ bool chol_inv_fits(int n, int ld, size_t wcap) {
 // An FP64 product of the factorisations: on the tensor cores from exact slices
 // (ozgemm) when tc is set and the product is large enough to fill the GPU, else
 // on the FP64 pipe (dgemm64).
-constexpr int kOzGemmMin = 128;
+constexpr int kOzGemmMin = 64;  // one 64 x 64 x 64 tile takes 67 us on one SM's FP64 pipe
 cudaError_t fgemm(bool tc, int m, int n, int k, double alpha, const double *A, int lda, bool transA, const double *B,
                   int ldb, bool transB, double beta, double *C, int ldc, cudaStream_t st, int tri = 0, int lane = 0) {
     if (tc && m >= kOzGemmMin && n >= kOzGemmMin && k >= kOzGemmMin)
@@ -674,9 +674,10 @@ struct OzRes {
     int N = 0, ld = 0, ntiles = 0, grid = 0;
     __nv_bfloat16 *s[3] = {nullptr, nullptr, nullptr};
     double *r[3] = {nullptr, nullptr, nullptr};
-    double *v = nullptr, *w = nullptr, *part = nullptr;
+    double *v = nullptr, *part = nullptr;
+    unsigned char *xs = nullptr;  // [3][2 tiles] sliced phase vectors (oz_vector_tile_bytes each)
+    int *xe = nullptr;            // [3][tiles][8] their scale exponents, then [3][8] column maxima
     unsigned *cnt = nullptr;
-    unsigned long long *cmax = nullptr;
     OzSeg *segs[3] = {nullptr, nullptr, nullptr};
     int *begin[3] = {nullptr, nullptr, nullptr}, *base[3] = {nullptr, nullptr, nullptr};
     int *count[3] = {nullptr, nullptr, nullptr};
@@ -686,11 +687,11 @@ struct OzRes {
         grid = grid_;
         ntiles = (N + oz_tile_rows() - 1) / oz_tile_rows();
         if (int rc = dev_alloc(&v, (size_t)3 * ld * 8)) return rc;
-        if (int rc = dev_alloc(&w, (size_t)2 * ld * 8)) return rc;
         CU_TRY(cudaMemset(v, 0, (size_t)3 * ld * 8 * sizeof(double)));
-        CU_TRY(cudaMemset(w, 0, (size_t)2 * ld * 8 * sizeof(double)));
+        CU_TRY(cudaMalloc(&xs, xs_bytes()));
+        CU_TRY(cudaMemset(xs, 0, xs_bytes()));  // the zero slots of every tile stay zero
+        if (int rc = dev_alloc(&xe, (size_t)3 * ntiles * 8 + 3 * 8)) return rc;
         CU_TRY(cudaMalloc(&cnt, (size_t)ntiles * sizeof(unsigned)));
-        CU_TRY(cudaMalloc(&cmax, 3 * 8 * sizeof(unsigned long long)));
         size_t max_segs = 0;
         for (int t = 0; t < 3; ++t) {
             std::vector<OzSeg> sg;
@@ -706,8 +707,9 @@ struct OzRes {
             CU_TRY(copy_h2d(base[t], pb.data(), pb.size() * sizeof(int)));
             CU_TRY(copy_h2d(count[t], pc.data(), pc.size() * sizeof(int)));
         }
-        return dev_alloc(&part, std::max<size_t>(max_segs, 1) * oz_tile_rows() * 8);
+        return dev_alloc(&part, std::max<size_t>(max_segs, 1) * oz_tile_rows() * 16);  // 128-bit partials
     }
+    size_t xs_bytes() const { return (size_t)3 * 2 * ntiles * oz_vector_tile_bytes(); }
     // slices and row scales of matrix t, allocated on first use
     int slice(int t, const double *M, cudaStream_t st) {
         if (!s[t]) {
@@ -727,11 +729,11 @@ struct OzRes {
             segs[t] = nullptr;
             dev_free(r[t]); dev_free(begin[t]); dev_free(base[t]); dev_free(count[t]);
         }
-        dev_free(v); dev_free(w); dev_free(part);
+        dev_free(v); dev_free(xe); dev_free(part);
+        if (xs) cudaFree(xs);
         if (cnt) cudaFree(cnt);
-        if (cmax) cudaFree(cmax);
+        xs = nullptr;
         cnt = nullptr;
-        cmax = nullptr;
     }
 };
 
@@ -1798,7 +1800,11 @@ int oz_run(ChebPlan &pl) {
     L.acc = p.col[pl.parity ^ 1];
     L.scale = p.scale;
     L.v = oz.v;
-    L.w = oz.w;
+    for (int b = 0; b < 3; ++b) {
+        L.xs[b] = oz.xs + (size_t)b * 2 * oz.ntiles * oz_vector_tile_bytes();
+        L.xe[b] = oz.xe + (size_t)b * oz.ntiles * 8;
+        L.emax[b] = oz.xe + (size_t)3 * oz.ntiles * 8 + b * 8;
+    }
     L.shift = p.shift;
     for (int t = 0; t < 3; ++t) {
         L.rscale[t] = oz.r[t] ? oz.r[t] : oz.r[1];
@@ -1809,7 +1815,6 @@ int oz_run(ChebPlan &pl) {
     }
     L.part = oz.part;
     L.tile_cnt = oz.cnt;
-    L.colmax = oz.cmax;
     L.bar_count = g_ctx.bar;
     L.bar_gen = g_ctx.bar + 1;
     L.error = g_ctx.err;
@@ -1820,7 +1825,7 @@ int oz_run(ChebPlan &pl) {
     CU_TRY(cudaMemsetAsync(g_ctx.err, 0, sizeof(int), st));
     CU_TRY(cudaMemsetAsync(g_ctx.bar, 0, 2 * sizeof(unsigned), st));
     CU_TRY(cudaMemsetAsync(oz.cnt, 0, (size_t)oz.ntiles * sizeof(unsigned), st));
-    CU_TRY(cudaMemsetAsync(oz.cmax, 0, 3 * 8 * sizeof(unsigned long long), st));
+    CU_TRY(cudaMemsetAsync(oz.xe + (size_t)3 * oz.ntiles * 8, 0x80, 3 * 8 * sizeof(int), st));  // column maxima
     const __nv_bfloat16 *sl[3] = {oz.s[0], oz.s[1], oz.s[2]};
     CU_TRY(cudaEventRecord(g_ctx.ev[0], st));
     CU_TRY(launch_oz_cheb(L, sl, oz.grid, st));
@@ -2214,6 +2219,27 @@ int cheb_rebuild_operator(elhl_traj *tr, bool implicit = false) {
     // set-ups, whose own rounding is near 1e-14 or 1e-7.
     // The implicit operator keeps G in cs.Ht, the explicit one in the factor's G.
     const bool pairs = implicit && cs.precision != ELHL_PREC_FP64;
+    if (implicit && cs.oz) {
+        // ELHL_PREC_OZ64: with every product on the tensor cores, forming H~ = G h G^T
+        // (1.5 N^3 flops) costs less than the implicit operator's extra phases (2 N^2
+        // elements and three grid phases per order instead of N^2 and one), so moving
+        // nuclei use the explicit operator too.  FP64 L^T and G^T serve the column transforms.
+        if (int rc = tr->fac.factor(tr->S, tr->N)) return rc;
+        CU_TRY(cudaEventRecord(g_ctx.ev[5], st));
+        if (int rc = tr->fac.check_info(false)) return rc;
+        cs.implicit = false;
+        if (int rc = form_htilde(cs, tr->fac.G, tr->h, tr->ld, tr->fac.W)) return rc;
+        CU_TRY(cudaEventRecord(g_ctx.ev[6], st));
+        if (int rc = lanczos_bounds(cs, 40)) return rc;
+        if (int rc = cheb_prepare(cs, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol)) return rc;
+        if (int rc = cheb_prepare_readout(cs, tr->fac.L, tr->fac.G)) return rc;  // A = G, B = L^T in FP64
+        if (!cs.Gt) CU_TRY(cudaMalloc(&cs.Gt, (size_t)cs.ld * cs.N * sizeof(double)));
+        convert_kernel<double><<<dim3((cs.ld + 127) / 128, cs.N), 128, 0, st>>>(tr->fac.G, (double *)cs.Gt, cs.N,
+                                                                                cs.ld, true);
+        count_launch();
+        CU_TRY(cudaGetLastError());
+        return ELHL_OK;
+    }
     if (!implicit && reduced_precision(cs.precision)) {
         CU_TRY(cudaMemcpy2DAsync(tr->fac.L, tr->ld * sizeof(double), tr->S, tr->ld * sizeof(double),
                                  tr->N * sizeof(double), tr->N, cudaMemcpyDeviceToDevice, st));
@@ -2265,10 +2291,11 @@ int cheb_load_columns(elhl_traj *tr) {
         return ELHL_OK;
     }
     const double *G = traj_inverse(tr);
-    if (int rc = cols_apply_dense(tr->fac.L, G, tr->ld, n, in, cs.m, 0, P, false, false, cs.cscratch))
+    const double *Lt = cs.oz ? cs.lt64() : nullptr, *Gt = cs.oz ? cs.gt64() : nullptr;  // FP64 transposes
+    if (int rc = cols_apply_dense(tr->fac.L, G, tr->ld, n, in, cs.m, 0, P, false, false, cs.cscratch, Lt, Gt))
         return rc;  // L^T psi
     if (cs.m == 2 * P)
-        if (int rc = cols_apply_dense(tr->fac.L, G, tr->ld, n, in, cs.m, P, P, true, true, cs.cscratch))
+        if (int rc = cols_apply_dense(tr->fac.L, G, tr->ld, n, in, cs.m, P, P, true, true, cs.cscratch, Lt, Gt))
             return rc;  // L^-1 bra
     cs.cols_current = true;
     return ELHL_OK;
@@ -2292,9 +2319,10 @@ int cheb_readout(elhl_traj *tr, const double2 *cols, double *d_pops) {
             return rc;  // L chi
     } else {
         const double *G = traj_inverse(tr);
-        if (int rc = cols_apply_dense(tr->fac.L, G, tr->ld, n, tr->psi_ao, P, 0, P, false, true, cs.cscratch))
+        const double *Lt = cs.oz ? cs.lt64() : nullptr, *Gt = cs.oz ? cs.gt64() : nullptr;  // FP64 transposes
+        if (int rc = cols_apply_dense(tr->fac.L, G, tr->ld, n, tr->psi_ao, P, 0, P, false, true, cs.cscratch, Lt, Gt))
             return rc;  // L^-T phi
-        if (int rc = cols_apply_dense(tr->fac.L, G, tr->ld, n, tr->bra_ao, P, 0, P, true, false, cs.cscratch))
+        if (int rc = cols_apply_dense(tr->fac.L, G, tr->ld, n, tr->bra_ao, P, 0, P, true, false, cs.cscratch, Lt, Gt))
             return rc;  // L chi
     }
     if (d_pops) {
@@ -3181,7 +3209,7 @@ int elhl_traj_get_matrices(elhl_traj *tr, double *S, double *h, double *Hp) {
 
 int elhl_traj_get_factor(elhl_traj *tr, double *L, double *G) {
     if (!tr) return ELHL_ERR_BAD_ARG;
-    if (!tr->cheb() || (G && !tr->cs.implicit)) return ELHL_ERR_UNSUPPORTED;
+    if (!tr->cheb()) return ELHL_ERR_UNSUPPORTED;
     std::lock_guard<std::mutex> lk(g_ctx.mu);
     CU_TRY(cudaStreamSynchronize(g_ctx.stream));
     const size_t col = tr->N * sizeof(double), ldb = tr->ld * sizeof(double);
@@ -3190,7 +3218,11 @@ int elhl_traj_get_factor(elhl_traj *tr, double *L, double *G) {
         for (int j = 1; j < tr->N; ++j)  // the explicit operator's factor keeps S above the diagonal
             std::memset(L + (size_t)j * tr->N, 0, j * sizeof(double));
     }
-    if (G) CU_TRY(cudaMemcpy2D(G, col, tr->cs.Ht, ldb, col, tr->N, cudaMemcpyDeviceToHost));
+    if (G) {
+        CU_TRY(cudaMemcpy2D(G, col, traj_inverse(tr), ldb, col, tr->N, cudaMemcpyDeviceToHost));
+        for (int j = 1; j < tr->N; ++j)  // zero above the diagonal, whatever the recursion left there
+            std::memset(G + (size_t)j * tr->N, 0, j * sizeof(double));
+    }
     return ELHL_OK;
 }
 

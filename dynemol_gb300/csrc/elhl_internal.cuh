@@ -181,16 +181,17 @@ struct OzLaunch {
     double2 *acc;                // [ld][m] output columns (sum of c_k v_k)
     const double *scale;         // [P] renormalisation factor of the input, or nullptr
     double *v;                   // [3][ld][8] Chebyshev vectors (re, im of 4 columns; padding rows zero)
-    double *w;                   // [2][ld][8] implicit phase outputs
+    unsigned char *xs[3];        // phase vectors as BF16 slices: [2 tiles] tiles of 64 rows (zero slots 0, 8)
+    int *xe[3];                  // [tiles][8] exponents e of their scales 2^e, one per 128-row chunk and column
+    int *emax[3];                // [8] the largest chunk exponent of each column (integer max)
     double shift;                // a / b (implicit)
     const double *rscale[3];     // [tiles * 128] power-of-two row scales of the sliced matrices
     const OzSeg *segs[3];        // per schedule: 0 upper (G^T), 1 full, 2 lower (G)
     const int *seg_begin[3];     // [grid + 1]
     const int *part_base[3];     // [tiles] first partial slot of a row tile
     const int *part_count[3];    // [tiles] segments of a row tile
-    double *part;                // partial tiles [slot][128][8]
+    double *part;                // partial tiles [slot][128][8] as 128-bit integers (16 bytes each)
     unsigned *tile_cnt;          // [tiles] segments finished (reset by the last)
-    unsigned long long *colmax;  // [3][8] bits of the largest |x| per real column, by phase sequence
     unsigned *bar_count, *bar_gen;
     int *error;
     unsigned long long barrier_ns;  // grid-barrier limit (0: default)
@@ -199,6 +200,7 @@ struct OzLaunch {
 int oz_slices();
 int oz_tile_rows();
 int oz_block_k();
+size_t oz_vector_tile_bytes();  // bytes of one sliced 64-row tile of a phase vector
 size_t oz_smem_bytes();
 // slices [oz_slices()][n][ld] of the n storage columns of M (ld rows), scale per column
 cudaError_t oz_slice_matrix(const double *M, int n, int ld, __nv_bfloat16 *out, double *rscale, cudaStream_t st);

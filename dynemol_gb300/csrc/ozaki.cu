@@ -4,43 +4,50 @@
 // GB300 runs FP64 FMAs at 1/58 of its FP32 rate, so the FP64 propagation on
 // the FP64 pipe is bound by that pipe (1.2 TFLOP/s), not by HBM.  Here every
 // FP64 operand is cut into kS = 7 slices of 8 bits each on a power-of-two
-// scale shared by a matrix row or a vector column (slice7):
+// scale (slice7):
 //
-//   a = 2^e_row  sum_{s<7} n_s 2^(-8(s+1)),   n_s integers, |n_0| <= 256, |n_s| <= 128,
+//   a = 2^e  sum_{s<7} n_s 2^(-8(s+1)),   n_s integers, |n_0| <= 256, |n_s| <= 128,
 //
-// which represents a to 2^-57 relative to its row's largest element.  Each
-// n_s is exact in BF16, each product of two slices is an integer below 2^16,
-// and a sum of 256 of them is an integer below 2^24: a BF16 tcgen05.mma with
-// FP32 accumulation therefore computes every slice product exactly, as long
-// as no accumulation runs over more than K = 256.  The products with
-// s_a + s_b <= 6 (28 of the 49; the rest lie below 2^-64) are taken from TMEM
-// after every 256-K group, converted to integers and added, shifted by their
-// weight 2^-8(s_a+s_b+2), into one 128-bit integer per row and column: a CTA's
-// partial product is exact until its single rounding to FP64.  The operator is
-// read as 14 bytes per element (7 BF16 slices) instead of 8, but the work
-// moves from the FP64 pipe to the tensor pipe, which leaves HBM as the bound.
+// which represents a to 2^-57 relative to the scale.  An operator row has one
+// scale; a vector column has one per 128-row chunk.  Each n_s is exact in BF16,
+// each product of two slices is an integer below 2^16, and a sum of 256 of them
+// an integer below 2^24: a BF16 tcgen05.mma with FP32 accumulation computes
+// slice products exactly as long as the sums stay below 2^24.  The products with s_a + s_b <= 6
+// (28 of the 49; the rest lie below 2^-64 of the scales) are summed per weight
+// s_a + s_b in TMEM over one 64-K block (each sum below 2^23.2: exact), folded
+// exactly into two 64-bit integers per row and column, and added as integers in the
+// frame of the column's largest chunk scale (exact to 2^-64 of it): a row
+// tile's product is one exact 128-bit integer per column until its single
+// rounding to FP64, whatever the order its partial sums arrive in.  The
+// operator is read as 14 bytes per element (7 BF16 slices) instead of 8, but
+// the work moves from the FP64 pipe to the tensor pipe, which leaves HBM as
+// the bound.
 //
 // One cooperative launch runs every order of one nuclear step.  An order is 1
 // (explicit Hs) or 3 (implicit G (h/b) G^T) grid phases y = A x, A a row-scaled
-// sliced matrix and x the FP64 output of the previous phase.  A phase's work
-// is a list of 64-K blocks of 128-row tiles (the non-zero ones of a triangular
-// A), split evenly over the CTAs; a CTA's blocks form segments (runs within a
-// row tile).  Per CTA:
+// sliced matrix.  A phase's work is a list of 64-K blocks of 128-row tiles (the
+// non-zero ones of a triangular A), split evenly over the CTAs; a CTA's blocks
+// form segments (runs within a row tile).  Per CTA:
 //   warp 0     TMA producer: the 7 slices of each block (128 x 64 BF16, 16 KB,
-//              128B swizzle) into a ring of kAStages stages;
+//              128B swizzle) into a ring of kAStages stages, through every phase
+//              without waiting for grid barriers (the operator does not change);
 //   warp 1     allocates TMEM; one thread issues tcgen05.mma (M = 128, K = 16,
 //              N = 64 ... 16: slice s_a against the vector slices s_b <= 6 - s_a)
-//              into one of two 256-column accumulator buffers;
-//   warps 2-3  build the vector operand of each block: 64 rows x 8 real columns
-//              of x cut into 7 slices, written in the swizzled K-major layout;
-//   warps 4-7  flush each 256-K group from TMEM (one thread per row), and at
-//              the end of a segment store the 128 x 8 FP64 partial; the last
-//              segment of a row tile to finish sums the partials in segment
-//              order (deterministic) and applies the phase epilogue: store w or
-//              y, or the Chebyshev recurrence and c_k v_k accumulation.
-// The column scales of x come from an integer max over the bits of |x| taken
-// by the producing epilogue.  Every wait is bounded: on a timeout the CTA sets
-// ELHL_ERR_TIMEOUT, stops, waits for its own copies and MMAs, and frees TMEM.
+//              into one of two 64-column accumulator buffers, one 8-column sum
+//              per weight s_a + s_b, also through every phase (it waits for
+//              each block's vector operand);
+//   warp 2     one thread loads each block's vector operand (9 KB, already sliced
+//              and swizzled by the producing phase) with one bulk copy, after
+//              the phase's grid barrier;
+//   warps 4-7  fold each block from TMEM (one thread per row); at the end of a
+//              segment they store its partial (exact 128-bit integers); a CTA
+//              designated per row tile sums the tile's partials once all are
+//              counted (exact, in any order), applies the phase epilogue (the
+//              Chebyshev recurrence and c_k v_k accumulation in FP64 after the
+//              last phase) and slices the 128 output rows for the next phase.
+// Warps 2-7 meet the grid barrier of every phase.  Every wait is bounded: on a
+// timeout the CTA sets ELHL_ERR_TIMEOUT, stops, waits for its own copies and
+// MMAs, and frees TMEM.
 #include <cuda.h>
 
 #include <algorithm>
@@ -57,63 +64,77 @@ using namespace tc;
 constexpr int kS = 7;                 // slices per operand
 constexpr int kTileM = 128;           // rows per tile (MMA M)
 constexpr int kKB = 64;               // K per block: 64 BF16 = one 128-byte swizzled row
-constexpr int kGroupBlocks = 4;       // blocks per exact accumulation (K = 256)
 constexpr int kAStages = 10;
 constexpr int kBStages = 4;
 constexpr int kThreads = 256;
 constexpr int kATile = kTileM * kKB * 2;  // 16 KB
-constexpr int kBTile = 64 * kKB * 2;      // 8 KB: 8 slots of 8 real columns (slot 7 stays zero)
-constexpr int kAccCols = 256;             // TMEM columns per accumulator buffer
+// vector operand tile: 9 slots of 8 rows (one per real column) x 128 bytes:
+// a zero slot, the slices 0-6, a zero slot
+constexpr int kBSlots = kS + 2;
+constexpr int kBTile = kBSlots * 8 * 128;     // 9 KB
+constexpr int kAccCols = 64;                  // TMEM columns per accumulator buffer: weights d = 0..7 x 8
 constexpr unsigned long long kWaitNs = 2000000000ull;
 
-// TMEM column offset and MMA N of matrix slice a: its valid columns are the
-// 8 (7 - a) real columns of the vector slices b <= 6 - a, rounded up to 16
-__host__ __device__ constexpr int acc_n(int a) { return ((8 * (kS - a) + 15) / 16) * 16; }
-__host__ __device__ constexpr int acc_off(int a) {  // sum of acc_n(t) for t < a, written out so it folds
-    return a <= 0 ? 0 : a == 1 ? 64 : a == 2 ? 112 : a == 3 ? 160 : a == 4 ? 192 : a == 5 ? 224 : a == 6 ? 240 : 256;
-}
+// Every slice product of weight d = a + b accumulates into the 8 TMEM columns
+// [8 d, 8 d + 8) of the buffer.  Slice a's MMA writes column block j of its D
+// region from B block j: for even a the region starts at column 8 a and B at
+// slice 0 (block j = slice j, weight a + j); for odd a both start one block
+// earlier, at column 8 (a - 1) and at the leading zero slot (block j = slice
+// j - 1, weight a + j - 1), so that every D region starts on a multiple of 16
+// columns.  N covers the slices b <= 6 - a, rounded up to 16 (the extra block
+// reads a zero slot or lands in columns [56, 64), weight 7, never read).
+__host__ __device__ constexpr int mma_col(int a) { return 8 * (a & ~1); }
+__host__ __device__ constexpr int mma_n(int a) { return ((8 * (kS - a) + 8 * (a & 1) + 15) / 16) * 16; }
+__host__ __device__ constexpr int mma_brow(int a) { return (a & 1) ? 0 : 8; }  // first B row (slot) read
 constexpr bool acc_layout_ok() {
-    for (int a = 0, off = 0; a <= kS; off += a < kS ? acc_n(a) : 0, ++a)
-        if (acc_off(a) != off) return false;
+    for (int a = 0; a < kS; ++a)
+        if (mma_col(a) % 16 || mma_col(a) + mma_n(a) > kAccCols || mma_brow(a) + mma_n(a) > 8 * kBSlots ||
+            mma_col(a) - 8 * (mma_brow(a) / 8 - 1) != 8 * a)  // column block j holds weight a + b, b = block - brow/8
+            return false;
     return true;
 }
-static_assert(kS == 7 && acc_layout_ok() && acc_off(kS) == kAccCols, "accumulator layout");
-// matrix slice whose accumulator holds TMEM column col of a buffer
-__host__ __device__ constexpr int acc_slice(int col) {
-    return col >= 240 ? 6 : col >= 224 ? 5 : col >= 192 ? 4 : col >= 160 ? 3 : col >= 112 ? 2 : col >= 64 ? 1 : 0;
-}
+static_assert(kS == 7 && acc_layout_ok(), "accumulator layout");
 
 __device__ __forceinline__ double pow2(int e) {  // 2^e for |e| < 1000
     return __longlong_as_double((long long)(1023 + e) << 52);
 }
-// column maximum written by atomics of other CTAs (read past L1)
-__device__ __forceinline__ double col_max(const unsigned long long *cmax, int c) {
-    return __longlong_as_double(__ldcg(reinterpret_cast<const long long *>(cmax) + c));
-}
-// exponent e with |x| < 2^e for the non-zero finite x = max |column| (0 for x = 0)
+// exponent e with |x| < 2^e for the non-zero finite x (0 for x = 0)
 __device__ __forceinline__ int scale_exp(double x) {
     if (!(x > 0.0)) return 0;
     return (int)((__double_as_longlong(x) >> 52) & 0x7ff) - 1022;
 }
+// byte offset of (row R, K index kk) in a 128B-swizzled K-major tile of 128-byte rows
+__device__ __forceinline__ int swz_off(int R, int kk) { return R * 128 + (((kk >> 3) ^ (R & 7)) << 4) + ((kk & 7) << 1); }
+
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+// generic-proxy global writes made visible to (and ordered with) the async proxy
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
 
 struct SmemLayout {
     static constexpr size_t a_off = 0;
     static constexpr size_t b_off = a_off + (size_t)kAStages * kATile;
     static constexpr size_t bar_off = b_off + (size_t)kBStages * kBTile;
     static constexpr size_t n_bars = 2 * kAStages + 2 * kBStages + 2 + 2 + 1;
-    static constexpr size_t misc_off = bar_off + n_bars * 8;
+    static constexpr size_t red_off = bar_off + n_bars * 8;        // [4][8] doubles: column maxima of the warps
+    static constexpr size_t misc_off = red_off + 4 * 8 * 8;
     static constexpr size_t bytes = misc_off + 64;
 };
 
 struct Roles {  // counters every role advances in the same order
     unsigned acnt = 0;   // A stages
     unsigned bcnt = 0;   // B stages
-    unsigned gcnt = 0;   // 256-K groups
+    unsigned gcnt = 0;   // groups
 };
 
 struct Ctx {
     unsigned char *smem;
     uint64_t *full, *empty, *bfull, *bempty, *accfull, *accempty, *done;
+    double *red;
     uint32_t tmem;
     int *abort_flag;
     unsigned *last_flag;
@@ -178,15 +199,15 @@ __device__ void produce(const Ctx &c, const OzLaunch &L, const CUtensorMap *map,
     }
 }
 
+// One block per accumulator buffer: over 64 K every weight's sum of slice
+// products stays below 2^23.2, exact in FP32.
 __device__ void issue_mma(const Ctx &c, const OzLaunch &L, int sched, Roles &r) {
     const int s0 = L.seg_begin[sched][blockIdx.x], s1 = L.seg_begin[sched][blockIdx.x + 1];
     for (int q = s0; q < s1; ++q) {
         const OzSeg sg = L.segs[sched][q];
         for (int kb = sg.kb0; kb < sg.kb1; ++kb) {
-            const int kin = (kb - sg.kb0) % kGroupBlocks;
-            const bool first = kin == 0, last = kin == kGroupBlocks - 1 || kb == sg.kb1 - 1;
             const unsigned tb = r.gcnt & 1;
-            if (first && r.gcnt >= 2 && !mbar_wait(&c.accempty[tb], ((r.gcnt >> 1) - 1) & 1, now_ns(), kWaitNs)) {
+            if (r.gcnt >= 2 && !mbar_wait(&c.accempty[tb], ((r.gcnt >> 1) - 1) & 1, now_ns(), kWaitNs)) {
                 set_abort(c, L.error);
                 return;
             }
@@ -196,7 +217,7 @@ __device__ void issue_mma(const Ctx &c, const OzLaunch &L, int sched, Roles &r) 
                 return;
             }
             asm volatile("tcgen05.fence::after_thread_sync;");
-            const uint64_t db = smem_desc_sw128(c.smem + SmemLayout::b_off + (size_t)sb * kBTile);
+            const unsigned char *btile = c.smem + SmemLayout::b_off + (size_t)sb * kBTile;
 #pragma unroll
             for (int a = 0; a < kS; ++a) {
                 const unsigned s = r.acnt % kAStages;
@@ -206,32 +227,26 @@ __device__ void issue_mma(const Ctx &c, const OzLaunch &L, int sched, Roles &r) 
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;");
                 const uint64_t da = smem_desc_sw128(c.smem + SmemLayout::a_off + (size_t)s * kATile);
-                const uint32_t acc = c.tmem + tb * kAccCols + (uint32_t)acc_off(a);
-                const uint32_t idesc = idesc_bf16(kTileM, acc_n(a));
+                const uint64_t db = smem_desc_sw128(btile + mma_brow(a) * 128);
+                const uint32_t acc = c.tmem + tb * kAccCols + (uint32_t)mma_col(a);
+                const uint32_t idesc = idesc_bf16(kTileM, mma_n(a));
 #pragma unroll
                 for (int k = 0; k < kKB / 16; ++k)  // K = 16 per MMA: +32 bytes along the swizzled row
-                    umma_bf16(acc, da + (uint64_t)(k * 2), db + (uint64_t)(k * 2), idesc, !(first && k == 0));
+                    umma_bf16(acc, da + (uint64_t)(k * 2), db + (uint64_t)(k * 2), idesc, !(a == 0 && k == 0));
                 umma_commit(&c.empty[s]);  // the A stage is free once these MMAs have read it
                 ++r.acnt;
             }
             umma_commit(&c.bempty[sb]);
             ++r.bcnt;
-            if (last) {
-                umma_commit(&c.accfull[tb]);
-                ++r.gcnt;
-            }
+            umma_commit(&c.accfull[tb]);
+            ++r.gcnt;
         }
     }
 }
 
-// vector operand of one block: rows kb*64 .. +64 of x ([ld][8] FP64), column c
-// cut into slices b on the scale 2^e_c; slice b, column c is row 8 b + c of the
-// K-major tile (128 B per row, 16-byte chunk j stored at j ^ (row & 7))
-__device__ void build(const Ctx &c, const OzLaunch &L, int sched, const double *x, const unsigned long long *cmax,
-                      Roles &r) {
-    const int t = threadIdx.x - 64;  // 0 .. 63
-    const int col = t & 7, chunk = t >> 3;
-    const double inv = pow2(-scale_exp(col_max(cmax, col)));
+// vector operand of each block: the 9 KB tile the producing phase wrote
+__device__ void load_vectors(const Ctx &c, const OzLaunch &L, int sched, const unsigned char *xs, Roles &r) {
+    fence_proxy_async_global();  // the tiles were written by generic stores before the grid barrier
     const int s0 = L.seg_begin[sched][blockIdx.x], s1 = L.seg_begin[sched][blockIdx.x + 1];
     for (int q = s0; q < s1; ++q) {
         const OzSeg sg = L.segs[sched][q];
@@ -243,95 +258,213 @@ __device__ void build(const Ctx &c, const OzLaunch &L, int sched, const double *
                 return;
             }
             if (aborted(c)) return;
-            int dig[8][kS];
-            const int k0 = kb * kKB + chunk * 8;
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int k = k0 + u;
-                slice7(k < L.ld ? __ldcg(x + (size_t)k * 8 + col) * inv : 0.0, dig[u]);
-            }
-            unsigned char *tile = c.smem + SmemLayout::b_off + (size_t)sb * kBTile;
-#pragma unroll
-            for (int b = 0; b < kS; ++b) {
-                uint32_t w[4];
-#pragma unroll
-                for (int u = 0; u < 8; u += 2) {
-                    const __nv_bfloat162 p = __floats2bfloat162_rn((float)dig[u][b], (float)dig[u + 1][b]);
-                    w[u / 2] = *reinterpret_cast<const uint32_t *>(&p);
-                }
-                const int row = 8 * b + col;
-                *reinterpret_cast<uint4 *>(tile + row * 128 + ((chunk ^ col) * 16)) = make_uint4(w[0], w[1], w[2], w[3]);
-            }
-            fence_proxy_async_smem();
-            mbar_arrive(&c.bfull[sb]);
+            mbar_expect_tx(&c.bfull[sb], (unsigned)kBTile);
+            bulk_load(c.smem + SmemLayout::b_off + (size_t)sb * kBTile, xs + (size_t)kb * kBTile, (unsigned)kBTile,
+                      &c.bfull[sb]);
             ++r.bcnt;
         }
     }
 }
 
-// One row of a group's accumulators, added exactly into the 128-bit integer
-// T = (Th, Tl) = sum over the segment of acc(a, b) 2^(8 (6 - a - b)), so that
-// the row's product is 2^-64 T: every accumulator is an integer below 2^24 and
-// the shift is at most 48 bits, so T stays far inside 128 bits.  Columns of
-// pairs with a + b > 6 (pad columns and products below 2^-64) are skipped.
-__device__ __forceinline__ void flush_group(uint32_t taddr, long long (&Th)[8], unsigned long long (&Tl)[8]) {
-#pragma unroll 1
-    for (int ch = 0; ch < kAccCols / 16; ch += 2) {  // two 16-column loads per wait
-        uint32_t v[32];
-        tmem_ld16(taddr + (uint32_t)(16 * ch), *reinterpret_cast<uint32_t(*)[16]>(&v[0]));
-        tmem_ld16(taddr + (uint32_t)(16 * ch + 16), *reinterpret_cast<uint32_t(*)[16]>(&v[16]));
-        tmem_wait_ld();
+// One row of a block's weight sums acc_d (TMEM columns 8 d + q, d <= 6) added
+// exactly into H += sum_{d<=2} acc_d 2^(8 (2 - d)) and L += sum_{d>=3} acc_d
+// 2^(8 (6 - d)) per column q: every acc_d is an integer below 2^23.2, so over
+// the two blocks of a chunk H < 2^40.2 and L < 2^48.2.
+__device__ __forceinline__ void flush_block(uint32_t taddr, long long (&H)[8], long long (&Lo)[8]) {
+    uint32_t v[64];
+    tmem_ld32(taddr, *reinterpret_cast<uint32_t(*)[32]>(&v[0]));
+    tmem_ld32(taddr + 32u, *reinterpret_cast<uint32_t(*)[32]>(&v[32]));
+    tmem_wait_ld();
 #pragma unroll
-        for (int h = 0; h < 4; ++h) {
-            const int col = 16 * ch + 8 * h;
-            const int a = acc_slice(col);
-            const int d = a + (col - acc_off(a)) / 8;
-            if (d >= kS) continue;
-            const int sh = 8 * (kS - 1 - d);
+    for (int d = 0; d < kS; ++d)
 #pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const long long x = (long long)__float2int_rn(__uint_as_float(v[8 * h + q]));
-                const unsigned long long lo = (unsigned long long)x << sh;
-                const long long hi = sh ? (x >> (64 - sh)) : (x >> 63);
-                const unsigned long long t = Tl[q] + lo;
-                Th[q] += hi + (t < lo ? 1ll : 0ll);
-                Tl[q] = t;
-            }
+        for (int q = 0; q < 8; ++q) {
+            const long long x = (long long)__float2int_rn(__uint_as_float(v[8 * d + q]));
+            if (d <= 2) H[q] += x * (1ll << (8 * (2 - d)));
+            else Lo[q] += x * (1ll << (8 * (kS - 1 - d)));
         }
-    }
 }
 
 struct PhaseIO {
-    const double *x;     // input vector [ld][8]
-    double *y;           // output vector [ld][8]
-    int kind;            // 0: store y; 1: Chebyshev order epilogue
-    int k;               // order
-    double cre, cim;     // c_k
-    const double *vm1;   // v_{k-1} (shift term of the implicit operator; nullptr: none)
-    const double *vm2;   // v_{k-2} (k >= 2)
+    int kind;                 // 0: y = A x; 1: Chebyshev order epilogue (recurrence, acc, v_k)
+    int k;                    // order
+    double cre, cim;          // c_k
+    const double *vm1;        // v_{k-1} FP64 (shift term of the implicit operator; nullptr: none)
+    const double *vm2;        // v_{k-2} FP64 (k >= 2)
+    double *vk;               // v_k FP64 out (kind 1)
+    const int *xe_in;         // [chunks][8] exponents e of the input vector's chunk scales 2^e
+    const int *emax_in;       // [8] the largest of them per column
+    unsigned char *xs_out;    // sliced output tiles
+    int *xe_out;              // [chunks][8] their exponents
+    int *emax_out;            // [8] their maxima (integer max)
 };
 
-__device__ void flush_and_epilogue(const Ctx &c, const OzLaunch &L, int sched, int mat, const PhaseIO &io,
-                                   const unsigned long long *cmax, unsigned long long *colmax_out, Roles &r) {
-    const int t = threadIdx.x - 128;  // 0 .. 127: TMEM lane / row in the tile
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double cs[8];
+// 128-bit two's complement integers (hi, lo) for the exact sums of slice products
+struct I128 {
+    long long hi;
+    unsigned long long lo;
+};
+__device__ __forceinline__ void add128(I128 &a, const I128 &b) {
+    const unsigned long long t = a.lo + b.lo;
+    a.hi += b.hi + (t < b.lo ? 1ll : 0ll);
+    a.lo = t;
+}
+// (H 2^32 + L) 2^-sft, rounded toward minus infinity (sft >= 0): |H 2^32 + L| < 2^76
+__device__ __forceinline__ I128 group_term(long long H, long long L, int sft) {
+    long long th = H >> 32;
+    unsigned long long tl = (unsigned long long)H << 32;
+    const unsigned long long t2 = tl + (unsigned long long)L;
+    th += (L >> 63) + (t2 < tl ? 1ll : 0ll);
+    tl = t2;
+    I128 r;
+    if (sft >= 127) {
+        r.hi = th >> 63;
+        r.lo = (unsigned long long)(th >> 63);
+    } else if (sft >= 64) {
+        r.lo = (unsigned long long)(th >> (sft - 64));
+        r.hi = th >> 63;
+    } else if (sft > 0) {
+        r.lo = (tl >> sft) | ((unsigned long long)th << (64 - sft));
+        r.hi = th >> sft;
+    } else {
+        r.lo = tl;
+        r.hi = th;
+    }
+    return r;
+}
+constexpr int kNoExp = (int)0x80808080;  // the column maximum before any chunk (bytes 0x80: a memset)
+
+// 128 output rows of row tile rt (thread t = row, y = 0 past N) cut into slices
+// on one scale 2^e per column for the tile: tiles 2 rt, 2 rt + 1 of xs, the
+// exponents at xe[rt], their maximum over the tiles in emax (non-zero columns);
+// slice b goes to slot b + 1, slots 0 and 8 stay zero.  Named barrier 1.
+__device__ void slice_rows_out(const Ctx &c, int rt, int t, const double (&y)[8], unsigned char *xs, int *xe,
+                               int *emax) {
+    const int w = t >> 5, lane = t & 31;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) cs[q] = pow2(scale_exp(col_max(cmax, q)));
-    const int s0 = L.seg_begin[sched][blockIdx.x], s1 = L.seg_begin[sched][blockIdx.x + 1];
-    for (int q = s0; q < s1; ++q) {
-        const OzSeg sg = L.segs[sched][q];
-        long long Th[8];
-        unsigned long long Tl[8];
+    for (int u = 0; u < 8; ++u) {
+        double mx = fabs(y[u]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        if (lane == 0) c.red[w * 8 + u] = mx;
+    }
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    double inv[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        const double mx = fmax(fmax(c.red[u], c.red[8 + u]), fmax(c.red[16 + u], c.red[24 + u]));
+        const int e = scale_exp(mx);
+        inv[u] = pow2(-e);
+        if (t == u) {
+            xe[rt * 8 + u] = e;
+            if (mx > 0.0) atomicMax(emax + u, e);
+        }
+    }
+    asm volatile("bar.sync 1, 128;" ::: "memory");  // c.red is rewritten by the next tile
+    unsigned char *tile = xs + (size_t)(2 * rt + (t >> 6)) * kBTile;
+    const int kk = t & 63;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+        int dig[kS];
+        slice7(y[u] * inv[u], dig);
+#pragma unroll
+        for (int b = 0; b < kS; ++b)
+            *reinterpret_cast<__nv_bfloat16 *>(tile + swz_off(8 * (b + 1) + u, kk)) = __float2bfloat16_rn((float)dig[b]);
+    }
+    fence_proxy_async_global();  // read by bulk copies after the next grid barrier
+}
+
+// bounded wait until *cnt reaches target (segments of a row tile written)
+__device__ __forceinline__ bool wait_count(const unsigned *cnt, unsigned target) {
+    const unsigned long long t0 = now_ns();
+    while (*(volatile const unsigned *)cnt < target) {
+        if (now_ns() - t0 > kWaitNs) return false;
+        __nanosleep(32);
+    }
+    return true;
+}
+
+// Epilogue of row tile rt once its np partials are written: their exact sum,
+// the output row (thread t) in FP64, the phase's epilogue and the slices of the
+// output for the next phase.
+__device__ void tile_epilogue(const Ctx &c, const OzLaunch &L, int sched, int mat, const PhaseIO &io, int rt, int np,
+                              const int (&E)[8], int t) {
+    const int row = rt * kTileM + t;
+    I128 S[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) S[u] = I128{0, 0ull};
+    const long long *p0 = reinterpret_cast<const long long *>(L.part) + ((size_t)L.part_base[sched][rt] * kTileM + t) * 16;
+    for (int s = 0; s < np; ++s) {
+        const longlong2 *pp = reinterpret_cast<const longlong2 *>(p0 + (size_t)s * kTileM * 16);
 #pragma unroll
         for (int u = 0; u < 8; ++u) {
-            Th[u] = 0;
-            Tl[u] = 0ull;
+            const longlong2 v = __ldcg(pp + u);
+            add128(S[u], I128{v.x, (unsigned long long)v.y});
         }
-        for (int g0 = sg.kb0; g0 < sg.kb1; g0 += kGroupBlocks) {
+    }
+    const double rs = L.rscale[mat][row];
+    double y[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u)
+        y[u] = ((double)S[u].hi * 0x1p64 + (double)S[u].lo) * (pow2(max(E[u], -900) - 64) * rs);
+    if (io.kind == 1) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            double v = 0.0;
+            if (row < L.N) {
+                double yv = y[u];
+                if (io.vm1) yv -= L.shift * __ldcg(io.vm1 + (size_t)row * 8 + u);
+                v = io.k == 1 ? yv : 2.0 * yv - __ldcg(io.vm2 + (size_t)row * 8 + u);
+                io.vk[(size_t)row * 8 + u] = v;
+            }
+            y[u] = v;
+        }
+        if (row < L.N)
+            for (int col = 0; col < L.m; ++col) {  // acc += c_k v_k, complex column col
+                double2 *ap = L.acc + (size_t)row * L.m + col;
+                double2 a = __ldcg(ap);  // the row's last writer may have been another CTA
+                const double vr = y[2 * col], vi = y[2 * col + 1];
+                a.x += io.cre * vr - io.cim * vi;
+                a.y += io.cre * vi + io.cim * vr;
+                *ap = a;
+            }
+    } else if (row >= L.N) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) y[u] = 0.0;
+    }
+    slice_rows_out(c, rt, t, y, io.xs_out, io.xe_out, io.emax_out);
+}
+
+// The CTA's segments: each 64-K block's weight sums folded per chunk into one
+// exact 128-bit integer per row and column, written as the segment's partial
+// and counted at its row tile.  Then the epilogues of the row tiles this CTA
+// is designated for (tile rt by CTA floor(rt grid / tiles): spread over the
+// grid, at most one per CTA while tiles <= grid), each once all of its
+// segments are counted.
+__device__ void flush_and_epilogue(const Ctx &c, const OzLaunch &L, int sched, int mat, const PhaseIO &io, Roles &r) {
+    const int t = threadIdx.x - 128;  // 0 .. 127: TMEM lane / row in the tile
+    const int warp = threadIdx.x >> 5;
+    const int s0 = L.seg_begin[sched][blockIdx.x], s1 = L.seg_begin[sched][blockIdx.x + 1];
+    // every group of this phase is added exactly in the frame 2^(E - 64) of its
+    // column's largest chunk scale 2^E
+    int E[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) E[u] = __ldcg(io.emax_in + u);
+    for (int q = s0; q < s1; ++q) {
+        const OzSeg sg = L.segs[sched][q];
+        I128 A[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) A[u] = I128{0, 0ull};
+        long long H[8], Lo[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            H[u] = 0;
+            Lo[u] = 0;
+        }
+        for (int kb = sg.kb0; kb < sg.kb1; ++kb) {
             const unsigned tb = r.gcnt & 1;
             // one thread waits and all 128 follow its outcome, so that none is left
-            // alone at the named barriers below
+            // alone at the named barriers
             if (t == 0) *c.last_flag = mbar_wait(&c.accfull[tb], (r.gcnt >> 1) & 1, now_ns(), kWaitNs) ? 1u : 0u;
             asm volatile("bar.sync 1, 128;" ::: "memory");
             const bool ready = *(volatile unsigned *)c.last_flag != 0;
@@ -341,111 +474,73 @@ __device__ void flush_and_epilogue(const Ctx &c, const OzLaunch &L, int sched, i
                 return;
             }
             asm volatile("tcgen05.fence::after_thread_sync;");
-            flush_group(c.tmem + ((uint32_t)((warp & 3) * 32) << 16) + tb * kAccCols, Th, Tl);
+            flush_block(c.tmem + ((uint32_t)((warp & 3) * 32) << 16) + tb * kAccCols, H, Lo);
             asm volatile("tcgen05.fence::before_thread_sync;");
             mbar_arrive(&c.accempty[tb]);
             ++r.gcnt;
-        }
-        const int row = sg.rt * kTileM + t;
-        const double rs = L.rscale[mat][row] * pow2(-64);
-        double R[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) R[u] = ((double)Th[u] * 0x1p64 + (double)Tl[u]) * rs * cs[u];
-        double *part = L.part + ((size_t)(L.part_base[sched][sg.rt] + sg.slot) * kTileM + t) * 8;
-#pragma unroll
-        for (int u = 0; u < 8; u += 2) *reinterpret_cast<double2 *>(part + u) = make_double2(R[u], R[u + 1]);
-        __threadfence();
-        asm volatile("bar.sync 1, 128;" ::: "memory");
-        const int np = L.part_count[sched][sg.rt];
-        if (t == 0) *c.last_flag = atomicAdd(&L.tile_cnt[sg.rt], 1u) == (unsigned)(np - 1);
-        asm volatile("bar.sync 1, 128;" ::: "memory");
-        if (!*(volatile unsigned *)c.last_flag) continue;
-        // last segment of this row tile: partials in segment order, then the epilogue
-        __threadfence();
-        double y[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) y[u] = 0.0;
-        const double *p0 = L.part + ((size_t)L.part_base[sched][sg.rt] * kTileM + t) * 8;
-        for (int s = 0; s < np; ++s) {
-            const double2 *pp = reinterpret_cast<const double2 *>(p0 + (size_t)s * kTileM * 8);
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const double2 v = __ldcg(pp + u);
-                y[2 * u] += v.x;
-                y[2 * u + 1] += v.y;
-            }
-        }
-        if (t == 0) L.tile_cnt[sg.rt] = 0u;  // next used after a grid barrier
-        double amax[8];
-        if (row < L.N) {
-            if (io.kind == 0) {
-#pragma unroll
-                for (int u = 0; u < 8; ++u) io.y[(size_t)row * 8 + u] = y[u];
-            } else {
-                double v[8];
+            if ((kb & 1) == 1 || kb == sg.kb1 - 1) {  // end of a 128-row chunk of the vector: its scale
+                const int *eg = io.xe_in + (size_t)(kb >> 1) * 8;
 #pragma unroll
                 for (int u = 0; u < 8; ++u) {
-                    double yv = y[u];
-                    if (io.vm1) yv -= L.shift * __ldcg(io.vm1 + (size_t)row * 8 + u);
-                    v[u] = io.k == 1 ? yv : 2.0 * yv - __ldcg(io.vm2 + (size_t)row * 8 + u);
-                    io.y[(size_t)row * 8 + u] = v[u];
+                    add128(A[u], group_term(H[u], Lo[u], max(0, E[u] - __ldcg(eg + u))));
+                    H[u] = 0;
+                    Lo[u] = 0;
                 }
-                for (int col = 0; col < L.m; ++col) {  // acc += c_k v_k, complex column col
-                    double2 *ap = L.acc + (size_t)row * L.m + col;
-                    double2 a = __ldcg(ap);  // the row's last writer may have been another CTA
-                    const double vr = v[2 * col], vi = v[2 * col + 1];
-                    a.x += io.cre * vr - io.cim * vi;
-                    a.y += io.cre * vi + io.cim * vr;
-                    *ap = a;
-                }
-#pragma unroll
-                for (int u = 0; u < 8; ++u) y[u] = v[u];
             }
-#pragma unroll
-            for (int u = 0; u < 8; ++u) amax[u] = fabs(y[u]);
-        } else {
-#pragma unroll
-            for (int u = 0; u < 8; ++u) amax[u] = 0.0;
         }
+        long long *part = reinterpret_cast<long long *>(L.part) +
+                          ((size_t)(L.part_base[sched][sg.rt] + sg.slot) * kTileM + t) * 16;
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            double mx = amax[u];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-            if (lane == 0 && mx > 0.0) atomicMax(colmax_out + u, (unsigned long long)__double_as_longlong(mx));
+        for (int u = 0; u < 8; ++u)
+            *reinterpret_cast<longlong2 *>(part + 2 * u) = make_longlong2(A[u].hi, (long long)A[u].lo);
+        __threadfence();
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        if (t == 0) atomicAdd(&L.tile_cnt[sg.rt], 1u);
+    }
+    const int ntiles = (L.N + kTileM - 1) / kTileM, G = gridDim.x;
+    const int rt1 = (int)(((long long)(blockIdx.x + 1) * ntiles + G - 1) / G);
+    for (int rt = (int)(((long long)blockIdx.x * ntiles + G - 1) / G); rt < rt1; ++rt) {
+        const int np = L.part_count[sched][rt];
+        if (t == 0) *c.last_flag = wait_count(&L.tile_cnt[rt], (unsigned)np) ? 1u : 0u;
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        const bool ready = *(volatile unsigned *)c.last_flag != 0;
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        if (!ready) {
+            if (t == 0) set_abort(c, L.error);
+            return;
         }
+        __threadfence();
+        tile_epilogue(c, L, sched, mat, io, rt, np, E, t);
+        if (t == 0) L.tile_cnt[rt] = 0u;  // next used after a grid barrier
     }
 }
 
-// order 0: v_0 = s phi (s: pending renormalisation factor), acc = c_0 v_0, column maxima
-__device__ void order_zero(const OzLaunch &L, double *v0, unsigned long long *colmax_out) {
-    const int lane = threadIdx.x & 31;
-    double amax[8];
-#pragma unroll
-    for (int u = 0; u < 8; ++u) amax[u] = 0.0;
+// order 0: v_0 = s phi (s: pending renormalisation factor), acc = c_0 v_0, and
+// the slices of v_0; row tiles rt = blockIdx.x, + grid, ... by warps 4-7
+__device__ void order_zero(const Ctx &c, const OzLaunch &L) {
+    const int t = threadIdx.x - 128;
+    const int ntiles = (L.N + kTileM - 1) / kTileM;
     const double2 c0 = L.coef[0];
-    const int stride = gridDim.x * blockDim.x;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < L.N; i += stride) {
-        for (int col = 0; col < L.m; ++col) {
-            double2 p = L.phi[(size_t)i * L.m + col];
-            if (L.scale) {
-                const double sc = L.scale[col % L.P];
-                p.x *= sc;
-                p.y *= sc;
+    for (int rt = blockIdx.x; rt < ntiles; rt += gridDim.x) {
+        const int i = rt * kTileM + t;
+        double y[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) y[u] = 0.0;
+        if (i < L.N)
+            for (int col = 0; col < L.m; ++col) {
+                double2 p = L.phi[(size_t)i * L.m + col];
+                if (L.scale) {
+                    const double sc = L.scale[col % L.P];
+                    p.x *= sc;
+                    p.y *= sc;
+                }
+                L.v[(size_t)i * 8 + 2 * col] = p.x;
+                L.v[(size_t)i * 8 + 2 * col + 1] = p.y;
+                L.acc[(size_t)i * L.m + col] = make_double2(c0.x * p.x - c0.y * p.y, c0.x * p.y + c0.y * p.x);
+                y[2 * col] = p.x;
+                y[2 * col + 1] = p.y;
             }
-            v0[(size_t)i * 8 + 2 * col] = p.x;
-            v0[(size_t)i * 8 + 2 * col + 1] = p.y;
-            L.acc[(size_t)i * L.m + col] = make_double2(c0.x * p.x - c0.y * p.y, c0.x * p.y + c0.y * p.x);
-            amax[2 * col] = fmax(amax[2 * col], fabs(p.x));
-            amax[2 * col + 1] = fmax(amax[2 * col + 1], fabs(p.y));
-        }
-    }
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-        double mx = amax[u];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (lane == 0 && mx > 0.0) atomicMax(colmax_out + u, (unsigned long long)__double_as_longlong(mx));
+        slice_rows_out(c, rt, t, y, L.xs[0], L.xe[0], L.emax[0]);
     }
 }
 
@@ -465,6 +560,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     c.accfull = c.bempty + kBStages;
     c.accempty = c.accfull + 2;
     c.done = c.accempty + 2;
+    c.red = reinterpret_cast<double *>(c.smem + SmemLayout::red_off);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(c.smem + SmemLayout::misc_off);
     c.abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
     c.last_flag = reinterpret_cast<unsigned *>(tmem_slot + 2);
@@ -476,7 +572,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             mbar_init(&c.empty[s], 1);
         }
         for (int s = 0; s < kBStages; ++s) {
-            mbar_init(&c.bfull[s], 64);
+            mbar_init(&c.bfull[s], 1);
             mbar_init(&c.bempty[s], 1);
         }
         for (int s = 0; s < 2; ++s) {
@@ -487,13 +583,6 @@ __global__ void __launch_bounds__(kThreads, 1)
         *c.abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    // slot 7 (rows 56-63) of every B stage stays zero: the MMA of slice 0 reads 64 rows
-    for (int q = threadIdx.x; q < kBStages * 8 * 128 / 16; q += kThreads) {
-        const int s = q / (8 * 8), o = q % (8 * 8);
-        *reinterpret_cast<uint4 *>(c.smem + SmemLayout::b_off + (size_t)s * kBTile + 56 * 128 + o * 16) =
-            make_uint4(0u, 0u, 0u, 0u);
-    }
-    fence_proxy_async_smem();
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                      "r"(2 * kAccCols));
@@ -507,26 +596,23 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int G = gridDim.x;
     Roles r;
 
-    // order 0 (phase sequence 0 writes column-max slot 0)
-    order_zero(L, L.v, L.colmax);
-    const bool ok0 = grid_barrier(L.bar_count, L.bar_gen, G, L.error, bar_ns);
+    if (warp >= 4) order_zero(c, L);  // slices of v_0 into vector buffer 0
     // The producer and the MMA issuer run through every phase without grid
     // barriers: the operator tiles do not depend on the previous phase, and the
-    // MMAs wait for the vector operand, which the builders form only after the
-    // phase's grid barrier.  So the next phase's loads and MMAs overlap the
-    // barrier.  The builders and the flush warps (192 threads) meet every phase's
-    // grid barrier on named barrier 2.
-    int seq = 0;
-    bool ok = ok0;
+    // MMAs wait for each block's vector operand, which thread 64 loads only
+    // after the phase's grid barrier.  So the next phase's loads and MMAs
+    // overlap the barrier.  Warps 2-7 meet every grid barrier on named barrier 2.
+    bool ok = true;
+    if (warp >= 2) ok = grid_barrier_sub(L.bar_count, L.bar_gen, G, L.error, bar_ns);
+    int seq = 0;  // phases so far; the vector of phase seq is in buffer seq % 3
     for (int k = 1; ok && k <= L.K; ++k) {
         const double2 ck = L.coef[k];
-        double *vk = L.v + (size_t)(k % 3) * L.ld * 8;
-        const double *vm1 = L.v + (size_t)((k + 2) % 3) * L.ld * 8, *vm2 = L.v + (size_t)((k + 1) % 3) * L.ld * 8;
         for (int ph = 0; ph < L.nphase && ok; ++ph) {
             ++seq;
             // implicit: 0: w = G^T v (sched upper, matrix 0), 1: y = (h/b) w (full, 1),
             // 2: G y (lower, 2) + recurrence;  explicit: Hs v (full, 1) + recurrence
             const int sched = L.nphase == 3 ? ph : 1, mat = sched;
+            const int bin = (seq + 2) % 3, bout = seq % 3;
             if (warp == 0) {
                 if ((threadIdx.x & 31) == 0) produce(c, L, maps[mat], sched, r);
                 ok = !aborted(c) && *(volatile int *)L.error == 0;
@@ -537,28 +623,27 @@ __global__ void __launch_bounds__(kThreads, 1)
                 ok = !aborted(c) && *(volatile int *)L.error == 0;
                 continue;
             }
-            const unsigned long long *cm_in = L.colmax + (size_t)((seq + 2) % 3) * 8;
-            unsigned long long *cm_out = L.colmax + (size_t)(seq % 3) * 8;
-            if (blockIdx.x == 0 && threadIdx.x >= 64 && threadIdx.x < 72)
-                L.colmax[(size_t)((seq + 1) % 3) * 8 + threadIdx.x - 64] = 0ull;
-            PhaseIO io{};
-            io.k = k;
-            io.cre = ck.x;
-            io.cim = ck.y;
-            io.vm2 = vm2;
-            if (L.nphase == 3) {
-                io.x = ph == 0 ? vm1 : L.w + (size_t)(ph - 1) * L.ld * 8;
-                io.y = ph == 2 ? vk : L.w + (size_t)ph * L.ld * 8;
-                io.kind = ph == 2 ? 1 : 0;
-                io.vm1 = ph == 2 ? vm1 : nullptr;
+            if (warp < 4) {
+                // buffer (seq + 1) % 3 was written two phases ago and read in the last one
+                if (blockIdx.x == 0 && threadIdx.x >= 96 && threadIdx.x < 104)
+                    L.emax[(seq + 1) % 3][threadIdx.x - 96] = kNoExp;
+                if (threadIdx.x == 64) load_vectors(c, L, sched, L.xs[bin], r);
             } else {
-                io.x = vm1;
-                io.y = vk;
-                io.kind = 1;
-                io.vm1 = nullptr;
+                PhaseIO io{};
+                io.kind = ph == L.nphase - 1 ? 1 : 0;
+                io.k = k;
+                io.cre = ck.x;
+                io.cim = ck.y;
+                io.vm1 = L.nphase == 3 ? L.v + (size_t)((k + 2) % 3) * L.ld * 8 : nullptr;
+                io.vm2 = L.v + (size_t)((k + 1) % 3) * L.ld * 8;
+                io.vk = L.v + (size_t)(k % 3) * L.ld * 8;
+                io.xe_in = L.xe[bin];
+                io.emax_in = L.emax[bin];
+                io.xs_out = L.xs[bout];
+                io.xe_out = L.xe[bout];
+                io.emax_out = L.emax[bout];
+                flush_and_epilogue(c, L, sched, mat, io, r);
             }
-            if (warp < 4) build(c, L, sched, io.x, cm_in, r);
-            else flush_and_epilogue(c, L, sched, mat, io, cm_in, cm_out, r);
             ok = grid_barrier_sub(L.bar_count, L.bar_gen, G, L.error, bar_ns) && !aborted(c);
             if (!ok && threadIdx.x == 64) atomicExch(c.abort_flag, 1);  // stops this CTA's producer and MMA issuer
         }
@@ -569,6 +654,11 @@ __global__ void __launch_bounds__(kThreads, 1)
         const unsigned n = min(r.acnt, (unsigned)kAStages);
         for (unsigned q = r.acnt - n; q < r.acnt; ++q)
             mbar_wait(&c.full[q % kAStages], (q / kAStages) & 1, now_ns(), kWaitNs);
+    }
+    if (threadIdx.x == 64) {  // the vector loads of stages not consumed
+        const unsigned n = min(r.bcnt, (unsigned)kBStages);
+        for (unsigned q = r.bcnt - n; q < r.bcnt; ++q)
+            mbar_wait(&c.bfull[q % kBStages], (q / kBStages) & 1, now_ns(), kWaitNs);
     }
     if (threadIdx.x == 32) {
         umma_commit(c.done);
@@ -649,6 +739,7 @@ int make_slice_map(CUtensorMap *m, const __nv_bfloat16 *base, int n, int ld) {
 int oz_slices() { return kS; }
 int oz_tile_rows() { return kTileM; }
 int oz_block_k() { return kKB; }
+size_t oz_vector_tile_bytes() { return kBTile; }
 size_t oz_smem_bytes() { return 1024 + SmemLayout::bytes; }
 
 cudaError_t oz_slice_matrix(const double *M, int n, int ld, __nv_bfloat16 *out, double *rscale, cudaStream_t st) {

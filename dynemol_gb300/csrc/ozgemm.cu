@@ -25,8 +25,8 @@
 //              accumulator a + b of one of two 224-column buffers;
 //   warps 2-5  fold each block's accumulators into H and L (one thread per row)
 //              and write C.
-// Operands are sliced by oz_slice_rows_kernel beforehand (K-major, zero outside
-// the triangle a flag names).  Every wait is bounded (ELHL_ERR_TIMEOUT).
+// Operands are sliced by oz_partmax_kernel and oz_slice_kernel beforehand
+// (K-major, zero outside the triangle a flag names).  Every wait is bounded (ELHL_ERR_TIMEOUT).
 #include <cuda.h>
 
 #include <algorithm>
@@ -94,39 +94,60 @@ __device__ __forceinline__ void load_tile(const OperandView &v, int r0, int j0, 
     }
 }
 
-// Slices of 32 operand rows per CTA (blockIdx.y: 0 = op(A), 1 = op(B)^T): a
-// first pass over K takes each row's largest |element| (the tiles load along
-// X's contiguous index; 8 warps each keep partial maxima of all 32 rows), a
-// second pass cuts every element with slice7 and writes out[s][r][j] along K
-// (row stride kp, zero for k <= j < kp); scale[r] = 2^e_r.
-__global__ void __launch_bounds__(256) oz_slice_rows_kernel(OperandView va, OperandView vb, __nv_bfloat16 *outA,
-                                                            __nv_bfloat16 *outB, int kp, double *scA, double *scB) {
+// Slicing of both operands in two passes over pieces of 32 operand rows x
+// kChunk K (blockIdx.z: 0 = op(A), 1 = op(B)^T), tiles of 32 x 32 loaded along
+// X's contiguous index: oz_partmax_kernel writes each row's largest |element|
+// of the piece to pm[r][piece]; oz_slice_kernel reduces a row's pieces to its
+// scale 2^e_r (scale[r], written by the pieces at K = 0) and cuts every element
+// of its piece with slice7 into out[s][r][j] (row stride kp, zero for k <= j < kp).
+constexpr int kChunk = 256;
+
+__global__ void __launch_bounds__(256) oz_partmax_kernel(OperandView va, OperandView vb, double *pmA, double *pmB,
+                                                         int npiece) {
     __shared__ double t[32][33];
-    __shared__ double s_max[8][32];
-    const bool isB = blockIdx.y == 1;
+    const bool isB = blockIdx.z == 1;
     const OperandView &v = isB ? vb : va;
-    __nv_bfloat16 *out = isB ? outB : outA;
-    double *scale = isB ? scB : scA;
-    const int r0 = blockIdx.x * 32;
+    const int r0 = blockIdx.y * 32, j00 = blockIdx.x * kChunk;
     if (r0 >= v.rows) return;
-    double mx = 0.0;  // thread (x, y): row r0 + x over the K columns y, y + 8, ... of each tile
-    for (int j0 = 0; j0 < v.k; j0 += 32) {
+    double mx = 0.0;  // thread (x, y): row r0 + x over K columns y, y + 8, ... of each tile
+    for (int j0 = j00; j0 < min(v.k, j00 + kChunk); j0 += 32) {
         __syncthreads();
         load_tile(v, r0, j0, t);
         __syncthreads();
         for (int q = threadIdx.y; q < 32; q += 8) mx = fmax(mx, fabs(t[threadIdx.x][q]));
     }
+    __shared__ double s_max[8][32];
     s_max[threadIdx.y][threadIdx.x] = mx;
     __syncthreads();
-    if (threadIdx.y == 0) {
+    if (threadIdx.y == 0 && r0 + threadIdx.x < v.rows) {
         double m = s_max[0][threadIdx.x];
         for (int q = 1; q < 8; ++q) m = fmax(m, s_max[q][threadIdx.x]);
-        s_max[0][threadIdx.x] = m;
-        if (r0 + threadIdx.x < v.rows) scale[r0 + threadIdx.x] = pow2(scale_exp(m));
+        (isB ? pmB : pmA)[(size_t)(r0 + threadIdx.x) * npiece + blockIdx.x] = m;
     }
-    __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) oz_slice_kernel(OperandView va, OperandView vb, const double *pmA,
+                                                       const double *pmB, int npiece, __nv_bfloat16 *outA,
+                                                       __nv_bfloat16 *outB, int kp, double *scA, double *scB) {
+    __shared__ double t[32][33];
+    __shared__ int s_e[32];
+    const bool isB = blockIdx.z == 1;
+    const OperandView &v = isB ? vb : va;
+    const double *pm = isB ? pmB : pmA;
+    __nv_bfloat16 *out = isB ? outB : outA;
+    const int r0 = blockIdx.y * 32, j00 = blockIdx.x * kChunk;
+    if (r0 >= v.rows) return;
+    if (threadIdx.y == 0) {
+        const int r = r0 + threadIdx.x;
+        double m = 0.0;
+        if (r < v.rows)
+            for (int q = 0; q < npiece; ++q) m = fmax(m, pm[(size_t)r * npiece + q]);
+        const int e = scale_exp(m);
+        s_e[threadIdx.x] = e;
+        if (blockIdx.x == 0 && r < v.rows) (isB ? scB : scA)[r] = pow2(e);
+    }
     const size_t sstride = (size_t)v.rows * kp;
-    for (int j0 = 0; j0 < kp; j0 += 32) {
+    for (int j0 = j00; j0 < min(kp, j00 + kChunk); j0 += 32) {
         __syncthreads();
         load_tile(v, r0, j0, t);
         __syncthreads();
@@ -134,7 +155,7 @@ __global__ void __launch_bounds__(256) oz_slice_rows_kernel(OperandView va, Oper
             const int r = r0 + rr, j = j0 + threadIdx.x;
             if (r >= v.rows || j >= kp) continue;
             int dig[kS];
-            slice7(t[rr][threadIdx.x] * pow2(-scale_exp(s_max[0][rr])), dig);
+            slice7(t[rr][threadIdx.x] * pow2(-s_e[rr]), dig);
 #pragma unroll
             for (int sl = 0; sl < kS; ++sl) out[sl * sstride + (size_t)r * kp + j] = __float2bfloat16_rn((float)dig[sl]);
         }
@@ -377,6 +398,8 @@ struct Lane {
     size_t sl_elems = 0;
     double *sc = nullptr;
     size_t rows_cap = 0;
+    double *pm = nullptr;    // row maxima per K piece of both operands
+    size_t pm_cap = 0;
     int *err = nullptr;
 };
 Lane g_lane[2];
@@ -406,6 +429,16 @@ cudaError_t ensure(Lane &ln, size_t sl_elems, size_t rows) {
     return cudaSuccess;
 }
 
+cudaError_t ensure_pm(Lane &ln, size_t n) {
+    if (n <= ln.pm_cap) return cudaSuccess;
+    if (ln.pm) cudaFree(ln.pm);
+    ln.pm = nullptr;
+    ln.pm_cap = 0;
+    cudaError_t e = cudaMalloc(&ln.pm, n * sizeof(double));
+    if (e == cudaSuccess) ln.pm_cap = n;
+    return e;
+}
+
 }  // namespace
 
 size_t ozgemm_smem_bytes() { return 1024 + Smem::bytes; }
@@ -423,8 +456,13 @@ cudaError_t ozgemm(int m, int n, int k, double alpha, const double *A, int lda, 
     const OperandView va{A, lda, transA, m, k, (tri & kTriA) ? 1 : (tri & kTriAt) ? 2 : 0};
     // op(B) columns: B(l, j) (K along B's columns) or B^T: B(j, l) (K along B's rows)
     const OperandView vb{B, ldb, !transB, n, k, (tri & kTriB) ? 2 : (tri & kTriBt) ? 1 : 0};
-    oz_slice_rows_kernel<<<dim3((std::max(m, n) + 31) / 32, 2), dim3(32, 8), 0, st>>>(va, vb, slA, slB, kp, ln.sc,
-                                                                                      ln.sc + m);
+    const int npiece = (kp + kChunk - 1) / kChunk;
+    if (cudaError_t e = ensure_pm(ln, (size_t)(m + n) * npiece)) return e;
+    const dim3 grid(npiece, (std::max(m, n) + 31) / 32, 2), blk(32, 8);
+    oz_partmax_kernel<<<grid, blk, 0, st>>>(va, vb, ln.pm, ln.pm + (size_t)m * npiece, npiece);
+    count_launch();
+    oz_slice_kernel<<<grid, blk, 0, st>>>(va, vb, ln.pm, ln.pm + (size_t)m * npiece, npiece, slA, slB, kp, ln.sc,
+                                          ln.sc + m);
     count_launch();
     CUtensorMap ma, mb;
     if (!make_map(&ma, slA, m, kp, kTM) || !make_map(&mb, slB, n, kp, kTN)) return cudaErrorInvalidValue;

@@ -275,9 +275,9 @@ int elhl_traj_restore(elhl_traj *tr, const char *path);
 int elhl_traj_get_matrices(elhl_traj *tr, double *S, double *h, double *Hp);
 
 /* The Chebyshev propagator's current Cholesky factor L (S = L L^T, lower, zero
- * above the diagonal) and, once a step with coordinates has run (implicit
- * operator), G = L^-1; host, N x N, ld = N; either pointer may be NULL.
- * ELHL_ERR_UNSUPPORTED for G before the first such step or on the Taylor path. */
+ * above the diagonal) and G = L^-1 (lower, zero above the diagonal); host,
+ * N x N, ld = N; either pointer may be NULL.  ELHL_ERR_UNSUPPORTED on the
+ * Taylor path. */
 int elhl_traj_get_factor(elhl_traj *tr, double *L, double *G);
 
 /* Counters of the last elhl_traj_step call. */
@@ -296,8 +296,9 @@ typedef struct {
     int tile_cols;        /* Chebyshev: complex columns per matrix pass chosen by the autotuner (0: GEMM regime) */
     int phases;           /* Chebyshev: grid phases per order (1 explicit H~, 3 implicit G h G^T) */
     double sh_ms;         /* moving nuclei: device time of the S, h build */
-    double factor_ms;     /* ... of the Cholesky factorisation of S */
-    double inverse_ms;    /* ... of G = L^-1 (implicit operator) */
+    double factor_ms;     /* ... of the Cholesky factorisation of S with G = L^-1 */
+    double inverse_ms;    /* ... of the operator formed from them: H~ = G h G^T (ELHL_PREC_OZ64),
+                             the zeroed upper triangles of L and G (implicit operator) */
     int cheb_retries;     /* Chebyshev steps redone on a widened spectral interval */
     double norm_drift;    /* Chebyshev: largest relative change of a column's squared norm in one step
                              (before renormalisation), over the call's accepted steps */

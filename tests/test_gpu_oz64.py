@@ -50,9 +50,9 @@ def test_oz64_fixed_nuclei_matches_fp64(elhl, flake):
 
 
 def test_oz64_moving_nuclei_vs_taylor_oracle(elhl, oracle_mod):
-    """Implicit operator G (h/b) G^T (three grid phases per order), bra and ket
-    carried through geometry changes, against the reference's Taylor step driver
-    at tolerance 1e-12."""
+    """Moving nuclei with H~ = G h G^T formed every step on the tensor cores (one
+    grid phase per order), bra and ket carried through geometry changes, against
+    the reference's Taylor step driver at tolerance 1e-12."""
     sysm = systems.cubic_cluster(n_atoms=64, seed=7)
     coords = np.stack([systems.perturbed_coords(sysm.coords, i, seed=3) for i in range(4)])
     S0 = oracle_mod.overlap(sysm, coords[1])
@@ -66,7 +66,7 @@ def test_oz64_moving_nuclei_vs_taylor_oracle(elhl, oracle_mod):
     st = tr.stats()
     tr.close()
     assert np.abs(pops - rp).max() < 1e-10
-    assert st.phases == 3
+    assert st.phases == 1
 
 
 def test_oz64_moving_nuclei_matches_fp64_n1860(elhl):

@@ -6,13 +6,14 @@ dynemol_gb300/csrc/ozgemm.cu), checked on the CPU before any GPU run:
   (A = G) operators every non-zero 128 x 64 block of the operator is given to
   exactly one CTA, CTAs differ by at most one block, a row tile's segments are
   numbered in K order and their partial slots fit the partial buffer;
-* the arithmetic: operands cut into 7 slices of 8 bits on a power-of-two row
-  (column) scale exactly as the kernels do (slice7: one rounding to a 64-bit
-  integer, then balanced base-256 digits),
-  products of slices accumulated over 256-K groups, where every sum of
-  absolute products must stay at or below 2^24 (so that the tensor cores' FP32
-  accumulation is exact), and the pairs with s_a + s_b <= 6 combined in one
-  exact integer per row and column; the result must agree with the exact
+* the arithmetic: operands cut into 7 slices of 8 bits on power-of-two scales
+  exactly as the kernels do (slice7: one rounding to a 64-bit integer, then
+  balanced base-256 digits; operator rows one scale each, vector columns one
+  per 128-row chunk), the slice products of one weight s_a + s_b accumulated
+  together per 64-K block, where every sum of absolute products must stay at or
+  below 2^24 (so that the tensor cores' FP32 accumulation is exact), the weights <= 6 folded exactly into
+  two 64-bit integers and the chunks added as integers in the frame of the
+  column's largest chunk scale; the result must agree with the exact
   (rational) product to within an FP64 dot product's rounding bound plus the
   slices' own truncation (2^-54.5 of the row and column scales per k),
   including rows and columns of very different scales;
@@ -38,7 +39,8 @@ def _const(name):
     return int(m.group(1))
 
 
-S, TILE, KB, GROUP = _const("kS"), _const("kTileM"), _const("kKB"), _const("kGroupBlocks")
+S, TILE, KB = _const("kS"), _const("kTileM"), _const("kKB")
+CHUNK = 128  # rows of a vector sharing one scale per column (one output row tile)
 GRID = 152
 
 
@@ -132,37 +134,60 @@ def test_slice7_source_matches_replay():
 
 
 def oz_product(A, X):
-    """y = A X as the kernel computes it (one CTA segment over all of K)."""
+    """y = A X as oz_cheb_kernel computes it: row scales for A, one scale per
+    128-row chunk and column for X (the producing epilogue's tile); per 64-K block
+    all pairs of weight d = a + b <= 6 share one accumulator, folded exactly into
+    H (weights d <= 2) and L (d >= 3) over the chunk's blocks; T = 2^32 H + L is
+    added, shifted down to the frame of the column's
+    largest chunk exponent E (floor), into one integer; y = 2^(E - 64) x that
+    integer x the row scale."""
     m, K = A.shape
+    nc = X.shape[1]
     er = [scale_exp(np.abs(A[i]).max()) for i in range(m)]
-    ec = [scale_exp(np.abs(X[:, c]).max()) for c in range(X.shape[1])]
-    As = np.stack([slices(A[i], er[i]) for i in range(m)], axis=1)      # [S][m][K]
-    Xs = np.stack([slices(X[:, c], ec[c]) for c in range(X.shape[1])], axis=2)  # [S][K][c]
+    As = np.stack([slices(A[i], er[i]) for i in range(m)], axis=1).astype(np.int64)  # [S][m][K]
     assert np.abs(As[0]).max() <= 256 and np.abs(As[1:]).max() <= 128
-    assert np.abs(Xs[0]).max() <= 256 and np.abs(Xs[1:]).max() <= 128
-    ai, xi = As.astype(np.int64), Xs.astype(np.int64)
-    y = np.zeros((m, X.shape[1]))
+    chunks = []
+    for g0 in range(0, K, CHUNK):
+        g = slice(g0, min(K, g0 + CHUNK))
+        mx = [np.abs(X[g, c]).max() for c in range(nc)]
+        ec = [scale_exp(v) for v in mx]
+        Xs = np.stack([slices(X[g, c], ec[c]) for c in range(nc)], axis=2).astype(np.int64)  # [S][chunk][c]
+        assert np.abs(Xs[0]).max() <= 256 and np.abs(Xs[1:]).max() <= 128
+        chunks.append((g, ec, mx, Xs))
+    E = [max([ch[1][c] for ch in chunks if ch[2][c] > 0], default=0) for c in range(nc)]
+    y = np.zeros((m, nc))
     for i in range(m):
-        for c in range(X.shape[1]):
-            T = 0
-            for g0 in range(0, K, GROUP * KB):
-                g = slice(g0, g0 + GROUP * KB)
-                for a in range(S):
-                    for b in range(S - a):
-                        pa, pb = ai[a, i, g], xi[b, g, c]
-                        assert int(np.abs(pa * pb).sum()) <= 1 << 24  # exact FP32 accumulation
-                        T += int((pa * pb).sum()) << (8 * (S - 1 - a - b))
-            y[i, c] = float(Fraction(T, 1 << 64) * Fraction(2) ** (er[i] + ec[c]))
+        for c in range(nc):
+            acc128 = 0
+            for g, ec, mx, Xs in chunks:
+                H = Lo = 0
+                for b0 in range(0, g.stop - g.start, KB):  # one TMEM accumulation per 64-K block
+                    kk = slice(b0, b0 + KB)
+                    for d in range(S):  # all pairs of weight d share one accumulator
+                        terms = [As[a, i, g][kk] * Xs[d - a, kk, c] for a in range(d + 1)]
+                        assert sum(int(np.abs(t).sum()) for t in terms) <= 1 << 24  # exact FP32 accumulation
+                        acc = sum(int(t.sum()) for t in terms)
+                        if d <= 2:
+                            H += acc << (8 * (2 - d))
+                        else:
+                            Lo += acc << (8 * (S - 1 - d))
+                assert abs(H) < 1 << 62 and abs(Lo) < 1 << 62
+                T = (H << 32) + Lo
+                assert abs(T) < 1 << 76
+                acc128 += T >> max(0, E[c] - ec[c])
+            assert abs(acc128) < 1 << 126
+            y[i, c] = float(Fraction(acc128) * Fraction(2) ** (E[c] - 64 + er[i]))
     return y
 
 
-def oz_bound(A, X):
-    """An FP64 dot product's rounding bound 2^-53 sum |a| |x|, plus what the slices
-    leave out: per k at most 2^-54.5 of the row and column scales 2^(e_r + e_c)
-    (residuals below 2^-57 of each scale, dropped products of weight d >= 7)."""
+def oz_bound(A, X, groups=1):
+    """FP64 rounding of the group sums, (groups + 1) 2^-53 sum |a| |x|, plus what the
+    slices leave out: per k at most 2^-54.5 of the row and column scales 2^(e_r +
+    e_c) (residuals below 2^-57 of each scale, dropped products of weight d >= 7)."""
     er = np.array([scale_exp(np.abs(A[i]).max()) for i in range(A.shape[0])], dtype=float)
     ec = np.array([scale_exp(np.abs(X[:, c]).max()) for c in range(X.shape[1])], dtype=float)
-    return (np.abs(A) @ np.abs(X)) * 2.0 ** -53 + A.shape[1] * 2.0 ** (er[:, None] + ec[None, :] - 54) + 1e-300
+    return ((np.abs(A) @ np.abs(X)) * (groups + 1) * 2.0 ** -53 + A.shape[1] * 2.0 ** (er[:, None] + ec[None, :] - 54)
+            + 1e-300)
 
 
 def exact_product(A, X):
@@ -172,7 +197,7 @@ def exact_product(A, X):
 
 def test_slice_product_matches_exact_product():
     rng = np.random.default_rng(7)
-    m, K = 6, 700  # three 256-K groups, the last partial
+    m, K = 6, 700  # six 128-row chunks of X, the last partial
     A = rng.standard_normal((m, K)) * np.exp(rng.uniform(-12, 2, (m, K)))  # wide dynamic range per row
     A[1] *= 1e-9   # a tiny row
     A[2, ::7] = 0.0
@@ -181,7 +206,7 @@ def test_slice_product_matches_exact_product():
     X[:, 5] = 0.0     # an unused column
     y = oz_product(A, X)
     ref = exact_product(A, X)
-    assert np.all(np.abs(y - ref) <= oz_bound(A, X))
+    assert np.all(np.abs(y - ref) <= oz_bound(A, X, groups=-(-K // CHUNK)))
     assert np.all(y[:, 5] == 0.0)
 
 
