@@ -666,21 +666,20 @@ __global__ void split_df_kernel(const double *__restrict__ src, float2 *__restri
     dst[(size_t)j * ld + i] = make_float2(h, __double2float_rn(v - (double)h));
 }
 
-// Resources of ELHL_PREC_OZ64 (ozaki.cu): BF16 slices of the operator's
-// matrices with their row scales, the FP64 series vectors in [ld][8] rows, the
-// per-phase block schedules and the launch's partial tiles and counters.
-// Matrix 0: G = L^-1 (storage column i = row i of G^T), 1: Hs, 2: G^T.
+// Resources of ELHL_PREC_OZ64 (ozaki.cu): the BF16 slices of Hs with their row
+// scales, the FP64 series vectors in [ld][8] rows, their sliced copies, the
+// block schedule and the launch's partial tiles and counters.
 struct OzRes {
     int N = 0, ld = 0, ntiles = 0, grid = 0;
-    __nv_bfloat16 *s[3] = {nullptr, nullptr, nullptr};
-    double *r[3] = {nullptr, nullptr, nullptr};
+    __nv_bfloat16 *s = nullptr;   // [slices][N][ld]
+    double *r = nullptr;          // [tiles * 128] row scales (0 past N)
     double *v = nullptr, *part = nullptr;
-    unsigned char *xs = nullptr;  // [3][2 tiles] sliced phase vectors (oz_vector_tile_bytes each)
-    int *xe = nullptr;            // [3][tiles][8] their scale exponents, then [3][8] column maxima
+    unsigned char *xs = nullptr;  // [3][2 tiles] sliced vectors (oz_vector_tile_bytes each)
+    int *xe = nullptr;            // [3][2 tiles][8] their scale exponents, then [3][8] column maxima
     unsigned *cnt = nullptr;
-    OzSeg *segs[3] = {nullptr, nullptr, nullptr};
-    int *begin[3] = {nullptr, nullptr, nullptr}, *base[3] = {nullptr, nullptr, nullptr};
-    int *count[3] = {nullptr, nullptr, nullptr};
+    OzSeg *segs = nullptr;
+    int *begin = nullptr, *base = nullptr, *count = nullptr;
+    size_t xs_bytes() const { return (size_t)3 * 2 * ntiles * oz_vector_tile_bytes(); }
     int init(int N_, int ld_, int grid_) {
         N = N_;
         ld = ld_;
@@ -690,50 +689,43 @@ struct OzRes {
         CU_TRY(cudaMemset(v, 0, (size_t)3 * ld * 8 * sizeof(double)));
         CU_TRY(cudaMalloc(&xs, xs_bytes()));
         CU_TRY(cudaMemset(xs, 0, xs_bytes()));  // the zero slots of every tile stay zero
-        if (int rc = dev_alloc(&xe, (size_t)3 * ntiles * 8 + 3 * 8)) return rc;
+        if (int rc = dev_alloc(&xe, (size_t)3 * 2 * ntiles * 8 + 3 * 8)) return rc;
         CU_TRY(cudaMalloc(&cnt, (size_t)ntiles * sizeof(unsigned)));
-        size_t max_segs = 0;
-        for (int t = 0; t < 3; ++t) {
-            std::vector<OzSeg> sg;
-            std::vector<int> b, pb, pc;
-            oz_schedule(N, grid, t, sg, b, pb, pc);
-            max_segs = std::max(max_segs, sg.size());
-            CU_TRY(cudaMalloc(&segs[t], std::max<size_t>(sg.size(), 1) * sizeof(OzSeg)));
-            if (int rc = dev_alloc(&begin[t], b.size())) return rc;
-            if (int rc = dev_alloc(&base[t], pb.size())) return rc;
-            if (int rc = dev_alloc(&count[t], pc.size())) return rc;
-            if (!sg.empty()) CU_TRY(copy_h2d(segs[t], sg.data(), sg.size() * sizeof(OzSeg)));
-            CU_TRY(copy_h2d(begin[t], b.data(), b.size() * sizeof(int)));
-            CU_TRY(copy_h2d(base[t], pb.data(), pb.size() * sizeof(int)));
-            CU_TRY(copy_h2d(count[t], pc.data(), pc.size() * sizeof(int)));
-        }
-        return dev_alloc(&part, std::max<size_t>(max_segs, 1) * oz_tile_rows() * 16);  // 128-bit partials
+        std::vector<OzSeg> sg;
+        std::vector<int> b, pb, pc;
+        oz_schedule(N, grid, sg, b, pb, pc);
+        CU_TRY(cudaMalloc(&segs, std::max<size_t>(sg.size(), 1) * sizeof(OzSeg)));
+        if (int rc = dev_alloc(&begin, b.size())) return rc;
+        if (int rc = dev_alloc(&base, pb.size())) return rc;
+        if (int rc = dev_alloc(&count, pc.size())) return rc;
+        if (!sg.empty()) CU_TRY(copy_h2d(segs, sg.data(), sg.size() * sizeof(OzSeg)));
+        CU_TRY(copy_h2d(begin, b.data(), b.size() * sizeof(int)));
+        CU_TRY(copy_h2d(base, pb.data(), pb.size() * sizeof(int)));
+        CU_TRY(copy_h2d(count, pc.data(), pc.size() * sizeof(int)));
+        return dev_alloc(&part, std::max<size_t>(sg.size(), 1) * oz_tile_rows() * 16);  // 128-bit partials
     }
-    size_t xs_bytes() const { return (size_t)3 * 2 * ntiles * oz_vector_tile_bytes(); }
-    // slices and row scales of matrix t, allocated on first use
-    int slice(int t, const double *M, cudaStream_t st) {
-        if (!s[t]) {
-            CU_TRY(cudaMalloc(&s[t], (size_t)oz_slices() * N * ld * sizeof(__nv_bfloat16)));
+    // slices and row scales of Hs (FP64), allocated on first use
+    int slice(const double *Hs, cudaStream_t st) {
+        if (!s) {
+            CU_TRY(cudaMalloc(&s, (size_t)oz_slices() * N * ld * sizeof(__nv_bfloat16)));
             const size_t nr = (size_t)ntiles * oz_tile_rows();
-            if (int rc = dev_alloc(&r[t], nr)) return rc;
-            CU_TRY(cudaMemset(r[t], 0, nr * sizeof(double)));  // rows past N: scale 0
+            if (int rc = dev_alloc(&r, nr)) return rc;
+            CU_TRY(cudaMemset(r, 0, nr * sizeof(double)));  // rows past N: scale 0
         }
-        CU_TRY(oz_slice_matrix(M, N, ld, s[t], r[t], st));
+        CU_TRY(oz_slice_matrix(Hs, N, ld, s, r, st));
         return ELHL_OK;
     }
     void release() {
-        for (int t = 0; t < 3; ++t) {
-            if (s[t]) cudaFree(s[t]);
-            if (segs[t]) cudaFree(segs[t]);
-            s[t] = nullptr;
-            segs[t] = nullptr;
-            dev_free(r[t]); dev_free(begin[t]); dev_free(base[t]); dev_free(count[t]);
-        }
-        dev_free(v); dev_free(xe); dev_free(part);
+        if (s) cudaFree(s);
+        if (segs) cudaFree(segs);
         if (xs) cudaFree(xs);
         if (cnt) cudaFree(cnt);
+        s = nullptr;
+        segs = nullptr;
         xs = nullptr;
         cnt = nullptr;
+        dev_free(r); dev_free(begin); dev_free(base); dev_free(count);
+        dev_free(v); dev_free(xe); dev_free(part);
     }
 };
 
@@ -980,6 +972,25 @@ int lanczos_bounds(ChebState &cs, int ksteps, const double *h = nullptr) {
             lanczos_update_kernel<float><<<1, kLzBlock, 0, st>>>(v, vp, t, n, rec, k, j);
             count_launch();
         }
+    } else if (cs.oz) {
+        // explicit H~ rebuilt every step (ELHL_PREC_OZ64): one FP32 GEMV per Lanczos step on
+        // an FP32 copy in Hs (written by cheb_prepare afterwards); an FP64 DSYMV ran on the
+        // FP64 pipe at 87 us a step.  FP32 rounding (1e-7 of the width) is inside the guard.
+        float *v = reinterpret_cast<float *>(cs.lz), *vp = v + ld, *w = v + 2 * ld;
+        float *H32 = static_cast<float *>(cs.Hs);
+        to_fp32_kernel<<<dim3((n + 127) / 128, n), 128, 0, st>>>(cs.Ht, H32, n, ld);
+        count_launch();
+        lanczos_start<float><<<(n + 255) / 256, 256, 0, st>>>(v, n);
+        count_launch();
+        CU_TRY(cudaMemsetAsync(vp, 0, n * sizeof(float), st));
+        lanczos_normalize_kernel<float><<<1, kLzBlock, 0, st>>>(v, n);
+        count_launch();
+        const float one = 1.f, zero = 0.f;
+        for (int j = 0; j < k; ++j) {
+            BLAS_TRY(cublasSgemv(g_ctx.blas, CUBLAS_OP_N, n, n, &one, H32, ld, v, 1, &zero, w, 1));
+            lanczos_update_kernel<float><<<1, kLzBlock, 0, st>>>(v, vp, w, n, rec, k, j);
+            count_launch();
+        }
     } else {
         double *v = cs.lz, *vp = cs.lz + ld, *w = cs.lz + 2 * ld;
         lanczos_start<double><<<(n + 255) / 256, 256, 0, st>>>(v, n);
@@ -1052,7 +1063,7 @@ int cheb_prepare(ChebState &cs, double dt, double tol, const double *h = nullptr
     CU_TRY(cudaStreamSynchronize(st));  // c is a host temporary
     cs.K = K;
     if (cs.oz)  // the tensor-core propagation reads Hs as BF16 slices
-        if (int rc = cs.oz->slice(1, static_cast<const double *>(cs.Hs), st)) return rc;
+        if (int rc = cs.oz->slice(static_cast<const double *>(cs.Hs), st)) return rc;
     if (cs.umma && !h) {  // the tensor-core GEMM reads Hs as three BF16 terms
         if (int rc = split3_bf16(reinterpret_cast<const float *>(cs.Hs), cs.N, cs.N, cs.ld, cs.hsplit, cs.ld, false, st))
             return rc;
@@ -1261,11 +1272,6 @@ int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, do
         count_launch();
         convert_kernel<double><<<grid, 128, 0, st>>>(Lfac, (double *)cs.B, n, ld, true);
         count_launch();
-        CU_TRY(cudaGetLastError());
-        if (cs.oz) {  // G^T v and G y on the tensor cores: slices of G's columns and of G^T's
-            if (int rc = cs.oz->slice(0, static_cast<const double *>(cs.A), st)) return rc;
-            if (int rc = cs.oz->slice(2, static_cast<const double *>(cs.Gt), st)) return rc;
-        }
     } else {
         convert_kernel<float><<<grid, 128, 0, st>>>(cs.Ht, (float *)cs.A, n, ld, false);
         count_launch();
@@ -1787,14 +1793,14 @@ int tune_plan(ChebPlan &pl, int mgcd) {
 unsigned long long g_dbg_barrier_ns = 0;
 int g_dbg_exit_cta1 = 0;
 
-// The propagation launch of an ELHL_PREC_OZ64 plan (one problem, m <= 4).
+// The propagation launch of an ELHL_PREC_OZ64 plan (one problem, m <= 4, explicit Hs).
 int oz_run(ChebPlan &pl) {
     cudaStream_t st = g_ctx.stream;
     OzRes &oz = *pl.oz;
     const ChebProblem &p = pl.probs[0];
+    if (p.m > 4 || !oz.s || pl.nphase != 1) return ELHL_ERR_UNSUPPORTED;
     OzLaunch L{};
     L.N = p.N; L.ld = p.ld; L.K = p.K; L.m = p.m; L.P = p.P;
-    L.nphase = pl.nphase;
     L.coef = p.coef;
     L.phi = p.col[pl.parity];
     L.acc = p.col[pl.parity ^ 1];
@@ -1802,17 +1808,14 @@ int oz_run(ChebPlan &pl) {
     L.v = oz.v;
     for (int b = 0; b < 3; ++b) {
         L.xs[b] = oz.xs + (size_t)b * 2 * oz.ntiles * oz_vector_tile_bytes();
-        L.xe[b] = oz.xe + (size_t)b * oz.ntiles * 8;
-        L.emax[b] = oz.xe + (size_t)3 * oz.ntiles * 8 + b * 8;
+        L.xe[b] = oz.xe + (size_t)b * 2 * oz.ntiles * 8;
+        L.emax[b] = oz.xe + (size_t)3 * 2 * oz.ntiles * 8 + b * 8;
     }
-    L.shift = p.shift;
-    for (int t = 0; t < 3; ++t) {
-        L.rscale[t] = oz.r[t] ? oz.r[t] : oz.r[1];
-        L.segs[t] = oz.segs[t];
-        L.seg_begin[t] = oz.begin[t];
-        L.part_base[t] = oz.base[t];
-        L.part_count[t] = oz.count[t];
-    }
+    L.rscale = oz.r;
+    L.segs = oz.segs;
+    L.seg_begin = oz.begin;
+    L.part_base = oz.base;
+    L.part_count = oz.count;
     L.part = oz.part;
     L.tile_cnt = oz.cnt;
     L.bar_count = g_ctx.bar;
@@ -1821,14 +1824,12 @@ int oz_run(ChebPlan &pl) {
     L.barrier_ns = g_dbg_barrier_ns;
     L.exit_cta1 = g_dbg_exit_cta1;
     g_dbg_exit_cta1 = 0;  // one launch only
-    if (p.m > 4 || !oz.s[1] || (pl.nphase == 3 && (!oz.s[0] || !oz.s[2]))) return ELHL_ERR_UNSUPPORTED;
     CU_TRY(cudaMemsetAsync(g_ctx.err, 0, sizeof(int), st));
     CU_TRY(cudaMemsetAsync(g_ctx.bar, 0, 2 * sizeof(unsigned), st));
     CU_TRY(cudaMemsetAsync(oz.cnt, 0, (size_t)oz.ntiles * sizeof(unsigned), st));
-    CU_TRY(cudaMemsetAsync(oz.xe + (size_t)3 * oz.ntiles * 8, 0x80, 3 * 8 * sizeof(int), st));  // column maxima
-    const __nv_bfloat16 *sl[3] = {oz.s[0], oz.s[1], oz.s[2]};
+    CU_TRY(cudaMemsetAsync(oz.xe + (size_t)3 * 2 * oz.ntiles * 8, 0x80, 3 * 8 * sizeof(int), st));  // column maxima
     CU_TRY(cudaEventRecord(g_ctx.ev[0], st));
-    CU_TRY(launch_oz_cheb(L, sl, oz.grid, st));
+    CU_TRY(launch_oz_cheb(L, oz.s, oz.grid, st));
     CU_TRY(cudaEventRecord(g_ctx.ev[1], st));
     return ELHL_OK;
 }

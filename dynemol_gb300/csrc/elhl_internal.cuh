@@ -168,30 +168,29 @@ int umma_bf16x3_gemm(const __nv_bfloat16 *const A[3], int lda, const __nv_bfloat
                      int K, int n2, int splits, float *Y, int *d_error, cudaStream_t st);
 
 // FP64 Chebyshev propagation by exact BF16 slices on the tensor cores
-// (ozaki.cu).  A phase's work: 64-K blocks of 128-row tiles; OzSeg is one CTA's
-// run of blocks [kb0, kb1) in row tile rt, the slot-th segment of that tile.
+// (ozaki.cu), one grid phase per order on an explicit Hs.  An order's work:
+// 64-K blocks of 128-row tiles; OzSeg is one CTA's run of blocks [kb0, kb1) in
+// row tile rt, the slot-th segment of that tile.
 struct OzSeg {
     int rt, kb0, kb1, slot;
 };
 struct OzLaunch {
     int N, ld, K, m, P;          // size, padded rows, last order, complex columns (<= 4), particles
-    int nphase;                  // 1: explicit Hs (matrix 1); 3: G^T (matrix 0), h/b (1), G (2)
     const double2 *coef;         // [K+1] expansion coefficients
     const double2 *phi;          // [ld][m] input columns
     double2 *acc;                // [ld][m] output columns (sum of c_k v_k)
     const double *scale;         // [P] renormalisation factor of the input, or nullptr
     double *v;                   // [3][ld][8] Chebyshev vectors (re, im of 4 columns; padding rows zero)
-    unsigned char *xs[3];        // phase vectors as BF16 slices: [2 tiles] tiles of 64 rows (zero slots 0, 8)
-    int *xe[3];                  // [tiles][8] exponents e of their scales 2^e, one per 128-row chunk and column
+    unsigned char *xs[3];        // v_k as BF16 slices: [2 tiles] tiles of 64 rows (zero slots 0, 8)
+    int *xe[3];                  // [2 tiles][8] exponents e of their scales 2^e, one per 64-row chunk and column
     int *emax[3];                // [8] the largest chunk exponent of each column (integer max)
-    double shift;                // a / b (implicit)
-    const double *rscale[3];     // [tiles * 128] power-of-two row scales of the sliced matrices
-    const OzSeg *segs[3];        // per schedule: 0 upper (G^T), 1 full, 2 lower (G)
-    const int *seg_begin[3];     // [grid + 1]
-    const int *part_base[3];     // [tiles] first partial slot of a row tile
-    const int *part_count[3];    // [tiles] segments of a row tile
+    const double *rscale;        // [tiles * 128] power-of-two row scales of the sliced Hs
+    const OzSeg *segs;
+    const int *seg_begin;        // [grid + 1]
+    const int *part_base;        // [tiles] first partial slot of a row tile
+    const int *part_count;       // [tiles] segments of a row tile
     double *part;                // partial tiles [slot][128][8] as 128-bit integers (16 bytes each)
-    unsigned *tile_cnt;          // [tiles] segments finished (reset by the last)
+    unsigned *tile_cnt;          // [tiles] segments written, over all orders of the launch
     unsigned *bar_count, *bar_gen;
     int *error;
     unsigned long long barrier_ns;  // grid-barrier limit (0: default)
@@ -200,14 +199,14 @@ struct OzLaunch {
 int oz_slices();
 int oz_tile_rows();
 int oz_block_k();
-size_t oz_vector_tile_bytes();  // bytes of one sliced 64-row tile of a phase vector
+size_t oz_vector_tile_bytes();  // bytes of one sliced 64-row tile of a vector
 size_t oz_smem_bytes();
 // slices [oz_slices()][n][ld] of the n storage columns of M (ld rows), scale per column
 cudaError_t oz_slice_matrix(const double *M, int n, int ld, __nv_bfloat16 *out, double *rscale, cudaStream_t st);
-// schedule type 0 (upper), 1 (full) or 2 (lower) of an n x n operator over grid CTAs
-void oz_schedule(int n, int grid, int type, std::vector<OzSeg> &segs, std::vector<int> &seg_begin,
-                 std::vector<int> &part_base, std::vector<int> &part_count);
-cudaError_t launch_oz_cheb(const OzLaunch &L, const __nv_bfloat16 *const slices[3], int grid, cudaStream_t st);
+// blocks of an n x n operator over grid CTAs
+void oz_schedule(int n, int grid, std::vector<OzSeg> &segs, std::vector<int> &seg_begin, std::vector<int> &part_base,
+                 std::vector<int> &part_count);
+cudaError_t launch_oz_cheb(const OzLaunch &L, const __nv_bfloat16 *hs_slices, int grid, cudaStream_t st);
 
 // C = alpha A op(B) + beta C in double-float arithmetic on the FP32 pipes (dfgemm.cu),
 // column-major operands stored as DF64 pairs (float2 = hi + lo), op(B) = B^T

@@ -23,29 +23,28 @@
 // the work moves from the FP64 pipe to the tensor pipe, which leaves HBM as
 // the bound.
 //
-// One cooperative launch runs every order of one nuclear step.  An order is 1
-// (explicit Hs) or 3 (implicit G (h/b) G^T) grid phases y = A x, A a row-scaled
-// sliced matrix.  A phase's work is a list of 64-K blocks of 128-row tiles (the
-// non-zero ones of a triangular A), split evenly over the CTAs; a CTA's blocks
-// form segments (runs within a row tile).  Per CTA:
+// One cooperative launch runs every order of one nuclear step: an order is one
+// grid phase y = Hs x with the row-scaled sliced Hs = (H~ - a)/b.  Its work is
+// the 64-K blocks of the 128-row tiles of Hs, split evenly over the CTAs; a
+// CTA's blocks form segments (runs within a row tile).  Per CTA:
 //   warp 0     TMA producer: the 7 slices of each block (128 x 64 BF16, 16 KB,
-//              128B swizzle) into a ring of kAStages stages, through every phase
+//              128B swizzle) into a ring of kAStages stages, through every order
 //              without waiting for grid barriers (the operator does not change);
 //   warp 1     allocates TMEM; one thread issues tcgen05.mma (M = 128, K = 16,
 //              N = 64 ... 16: slice s_a against the vector slices s_b <= 6 - s_a)
 //              into one of two 64-column accumulator buffers, one 8-column sum
-//              per weight s_a + s_b, also through every phase (it waits for
+//              per weight s_a + s_b, also through every order (it waits for
 //              each block's vector operand);
 //   warp 2     one thread loads each block's vector operand (9 KB, already sliced
-//              and swizzled by the producing phase) with one bulk copy, after
-//              the phase's grid barrier;
+//              and swizzled by the previous order) with one bulk copy, after the
+//              order's grid barrier;
 //   warps 4-7  fold each block from TMEM (one thread per row); at the end of a
 //              segment they store its partial (exact 128-bit integers); a CTA
 //              designated per row tile sums the tile's partials once all are
-//              counted (exact, in any order), applies the phase epilogue (the
-//              Chebyshev recurrence and c_k v_k accumulation in FP64 after the
-//              last phase) and slices the 128 output rows for the next phase.
-// Warps 2-7 meet the grid barrier of every phase.  Every wait is bounded: on a
+//              counted (exact, in any order), applies the Chebyshev recurrence
+//              and the c_k v_k accumulation in FP64, and slices the 128 new
+//              rows of v_k for the next order.
+// Warps 2-7 meet the grid barrier of every order.  Every wait is bounded: on a
 // timeout the CTA sets ELHL_ERR_TIMEOUT, stops, waits for its own copies and
 // MMAs, and frees TMEM.
 #include <cuda.h>
@@ -120,8 +119,9 @@ struct SmemLayout {
     static constexpr size_t b_off = a_off + (size_t)kAStages * kATile;
     static constexpr size_t bar_off = b_off + (size_t)kBStages * kBTile;
     static constexpr size_t n_bars = 2 * kAStages + 2 * kBStages + 2 + 2 + 1;
-    static constexpr size_t red_off = bar_off + n_bars * 8;        // [4][8] doubles: column maxima of the warps
-    static constexpr size_t misc_off = red_off + 4 * 8 * 8;
+    static constexpr size_t red_off = bar_off + n_bars * 8;        // [4][8] ints: column maxima of the warps
+    static constexpr size_t out_off = (red_off + 4 * 8 * 4 + 1023) / 1024 * 1024;
+    static constexpr size_t misc_off = out_off + (size_t)kBTile;  // one output tile
     static constexpr size_t bytes = misc_off + 64;
 };
 
@@ -134,7 +134,8 @@ struct Roles {  // counters every role advances in the same order
 struct Ctx {
     unsigned char *smem;
     uint64_t *full, *empty, *bfull, *bempty, *accfull, *accempty, *done;
-    double *red;
+    int *red;
+    unsigned char *out;
     uint32_t tmem;
     int *abort_flag;
     unsigned *last_flag;
@@ -178,10 +179,10 @@ __device__ __forceinline__ bool grid_barrier_sub(unsigned *count, unsigned *gen,
 
 // ---- phase roles ----------------------------------------------------------------
 
-__device__ void produce(const Ctx &c, const OzLaunch &L, const CUtensorMap *map, int sched, Roles &r) {
-    const int s0 = L.seg_begin[sched][blockIdx.x], s1 = L.seg_begin[sched][blockIdx.x + 1];
+__device__ void produce(const Ctx &c, const OzLaunch &L, const CUtensorMap *map, Roles &r) {
+    const int s0 = L.seg_begin[blockIdx.x], s1 = L.seg_begin[blockIdx.x + 1];
     for (int q = s0; q < s1; ++q) {
-        const OzSeg sg = L.segs[sched][q];
+        const OzSeg sg = L.segs[q];
         for (int kb = sg.kb0; kb < sg.kb1; ++kb) {
             for (int a = 0; a < kS; ++a) {
                 const unsigned s = r.acnt % kAStages;
@@ -201,10 +202,10 @@ __device__ void produce(const Ctx &c, const OzLaunch &L, const CUtensorMap *map,
 
 // One block per accumulator buffer: over 64 K every weight's sum of slice
 // products stays below 2^23.2, exact in FP32.
-__device__ void issue_mma(const Ctx &c, const OzLaunch &L, int sched, Roles &r) {
-    const int s0 = L.seg_begin[sched][blockIdx.x], s1 = L.seg_begin[sched][blockIdx.x + 1];
+__device__ void issue_mma(const Ctx &c, const OzLaunch &L, Roles &r) {
+    const int s0 = L.seg_begin[blockIdx.x], s1 = L.seg_begin[blockIdx.x + 1];
     for (int q = s0; q < s1; ++q) {
-        const OzSeg sg = L.segs[sched][q];
+        const OzSeg sg = L.segs[q];
         for (int kb = sg.kb0; kb < sg.kb1; ++kb) {
             const unsigned tb = r.gcnt & 1;
             if (r.gcnt >= 2 && !mbar_wait(&c.accempty[tb], ((r.gcnt >> 1) - 1) & 1, now_ns(), kWaitNs)) {
@@ -244,12 +245,12 @@ __device__ void issue_mma(const Ctx &c, const OzLaunch &L, int sched, Roles &r) 
     }
 }
 
-// vector operand of each block: the 9 KB tile the producing phase wrote
-__device__ void load_vectors(const Ctx &c, const OzLaunch &L, int sched, const unsigned char *xs, Roles &r) {
+// vector operand of each block: the 9 KB tile the previous order wrote
+__device__ void load_vectors(const Ctx &c, const OzLaunch &L, const unsigned char *xs, Roles &r) {
     fence_proxy_async_global();  // the tiles were written by generic stores before the grid barrier
-    const int s0 = L.seg_begin[sched][blockIdx.x], s1 = L.seg_begin[sched][blockIdx.x + 1];
+    const int s0 = L.seg_begin[blockIdx.x], s1 = L.seg_begin[blockIdx.x + 1];
     for (int q = s0; q < s1; ++q) {
-        const OzSeg sg = L.segs[sched][q];
+        const OzSeg sg = L.segs[q];
         for (int kb = sg.kb0; kb < sg.kb1; ++kb) {
             const unsigned sb = r.bcnt % kBStages;
             if (r.bcnt >= kBStages &&
@@ -285,11 +286,9 @@ __device__ __forceinline__ void flush_block(uint32_t taddr, long long (&H)[8], l
         }
 }
 
-struct PhaseIO {
-    int kind;                 // 0: y = A x; 1: Chebyshev order epilogue (recurrence, acc, v_k)
+struct OrderIO {
     int k;                    // order
     double cre, cim;          // c_k
-    const double *vm1;        // v_{k-1} FP64 (shift term of the implicit operator; nullptr: none)
     const double *vm2;        // v_{k-2} FP64 (k >= 2)
     double *vk;               // v_k FP64 out (kind 1)
     const int *xe_in;         // [chunks][8] exponents e of the input vector's chunk scales 2^e
@@ -332,44 +331,73 @@ __device__ __forceinline__ I128 group_term(long long H, long long L, int sft) {
     }
     return r;
 }
+// exact integer -> double for 0 <= x < 2^52 (the bits of 2^52 + x, less 2^52)
+__device__ __forceinline__ double u52_to_double(unsigned long long x) {
+    return __longlong_as_double((long long)(0x4330000000000000ull | x)) - 0x1p52;
+}
+// A 128-bit integer (|s| < 2^116) rounded to FP64 from its magnitude, by exact
+// conversions of three positive parts: no FP64 conversion instructions, no
+// cancellation.
+__device__ __forceinline__ double i128_to_double(I128 s) {
+    const bool neg = s.hi < 0;
+    if (neg) {  // two's complement negation
+        s.lo = ~s.lo + 1ull;
+        s.hi = ~s.hi + (s.lo == 0ull ? 1ll : 0ll);
+    }
+    const double d = fma(u52_to_double((unsigned long long)s.hi), 0x1p64,
+                         fma(u52_to_double(s.lo >> 32), 0x1p32, u52_to_double(s.lo & 0xffffffffull)));
+    return neg ? -d : d;
+}
 constexpr int kNoExp = (int)0x80808080;  // the column maximum before any chunk (bytes 0x80: a memset)
 
-// 128 output rows of row tile rt (thread t = row, y = 0 past N) cut into slices
-// on one scale 2^e per column for the tile: tiles 2 rt, 2 rt + 1 of xs, the
-// exponents at xe[rt], their maximum over the tiles in emax (non-zero columns);
-// slice b goes to slot b + 1, slots 0 and 8 stay zero.  Named barrier 1.
-__device__ void slice_rows_out(const Ctx &c, int rt, int t, const double (&y)[8], unsigned char *xs, int *xe,
-                               int *emax) {
-    const int w = t >> 5, lane = t & 31;
+// The epilogue of one 64-row chunk h of v_k (rows 64 h ...) runs on the 128
+// threads of warps 4-7 of the CTA designated for it: thread t handles row
+// 64 h + (t & 63) and the columns 4 (t >> 6) ... + 3.
+struct EpiThread {
+    int t, r, half, row;  // thread, row in the chunk, column half, global row
+};
+__device__ __forceinline__ EpiThread epi_thread(int h, int t) {
+    return EpiThread{t, t & 63, t >> 6, 64 * h + (t & 63)};
+}
+
+// The chunk's 64 new rows (4 columns per thread, 0 past N) cut into slices on
+// one scale 2^e per column: tile h of xs, the exponents at xe[h], their maximum
+// over the chunks in emax (non-zero columns); slice b goes to slot b + 1, slots
+// 0 and 8 stay zero.  Digits formed in shared memory, copied out in 16-byte
+// stores.  Named barrier 1 (the 128 threads).
+__device__ void slice_chunk_out(const Ctx &c, int h, const EpiThread &et, const double (&y)[4], unsigned char *xs,
+                                int *xe, int *emax) {
+    const int w = et.t >> 5;  // warps 0, 1: columns 0-3; warps 2, 3: columns 4-7
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
-        double mx = fabs(y[u]);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-        if (lane == 0) c.red[w * 8 + u] = mx;
+    for (int u = 0; u < 4; ++u) {  // largest exponent field of the column over the warp's rows
+        const int m = __reduce_max_sync(0xffffffffu, exp_field(y[u]));
+        if ((et.t & 31) == 0) c.red[w * 4 + u] = m;
     }
     asm volatile("bar.sync 1, 128;" ::: "memory");
-    double inv[8];
+    int e[4];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
-        const double mx = fmax(fmax(c.red[u], c.red[8 + u]), fmax(c.red[16 + u], c.red[24 + u]));
-        const int e = scale_exp(mx);
-        inv[u] = pow2(-e);
-        if (t == u) {
-            xe[rt * 8 + u] = e;
-            if (mx > 0.0) atomicMax(emax + u, e);
+    for (int u = 0; u < 4; ++u) {
+        const int be = max(c.red[(2 * et.half) * 4 + u], c.red[(2 * et.half + 1) * 4 + u]);
+        e[u] = be ? be - 1022 : 0;  // |column| < 2^e (0 for a zero column)
+        if (et.r == 0) {
+            xe[h * 8 + 4 * et.half + u] = e[u];
+            if (be) atomicMax(emax + 4 * et.half + u, e[u]);
         }
     }
-    asm volatile("bar.sync 1, 128;" ::: "memory");  // c.red is rewritten by the next tile
-    unsigned char *tile = xs + (size_t)(2 * rt + (t >> 6)) * kBTile;
-    const int kk = t & 63;
 #pragma unroll
-    for (int u = 0; u < 8; ++u) {
+    for (int u = 0; u < 4; ++u) {
         int dig[kS];
-        slice7(y[u] * inv[u], dig);
+        slice7(y[u], e[u], dig);
 #pragma unroll
         for (int b = 0; b < kS; ++b)
-            *reinterpret_cast<__nv_bfloat16 *>(tile + swz_off(8 * (b + 1) + u, kk)) = __float2bfloat16_rn((float)dig[b]);
+            *reinterpret_cast<__nv_bfloat16 *>(c.out + swz_off(8 * (b + 1) + 4 * et.half + u, et.r)) =
+                __float2bfloat16_rn((float)dig[b]);
+    }
+    asm volatile("bar.sync 1, 128;" ::: "memory");  // the tile is complete; c.red is free again
+    constexpr int kChunks = kS * 8 * 128 / 16;  // slots 1-7: 7 KB
+    for (int q = et.t; q < kChunks; q += 128) {
+        const int o = 8 * 128 + q * 16;
+        *reinterpret_cast<uint4 *>(xs + (size_t)h * kBTile + o) = *reinterpret_cast<const uint4 *>(c.out + o);
     }
     fence_proxy_async_global();  // read by bulk copies after the next grid barrier
 }
@@ -384,83 +412,78 @@ __device__ __forceinline__ bool wait_count(const unsigned *cnt, unsigned target)
     return true;
 }
 
-// Epilogue of row tile rt once its np partials are written: their exact sum,
-// the output row (thread t) in FP64, the phase's epilogue and the slices of the
-// output for the next phase.
-__device__ void tile_epilogue(const Ctx &c, const OzLaunch &L, int sched, int mat, const PhaseIO &io, int rt, int np,
-                              const int (&E)[8], int t) {
-    const int row = rt * kTileM + t;
-    I128 S[8];
+// Epilogue of chunk h once its row tile's np segments are written: the exact
+// sum of their partials, the row's product in FP64, the recurrence and
+// accumulation of order k, and the slices of the chunk's rows of v_k for the
+// next order.  The rows of a chunk are only ever touched by this CTA (order 0
+// included), so v and acc use plain (L1) loads.
+__device__ void chunk_epilogue(const Ctx &c, const OzLaunch &L, const OrderIO &io, int h, int np, const int (&E)[8],
+                               int t) {
+    const EpiThread et = epi_thread(h, t);
+    const int rt = h >> 1, trow = (h & 1) * 64 + et.r;  // row tile, row in it
+    I128 S[4];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) S[u] = I128{0, 0ull};
-    const long long *p0 = reinterpret_cast<const long long *>(L.part) + ((size_t)L.part_base[sched][rt] * kTileM + t) * 16;
-    for (int s = 0; s < np; ++s) {
-        const longlong2 *pp = reinterpret_cast<const longlong2 *>(p0 + (size_t)s * kTileM * 16);
+    for (int u = 0; u < 4; ++u) S[u] = I128{0, 0ull};
+    const longlong2 *p0 = reinterpret_cast<const longlong2 *>(L.part) +
+                          ((size_t)L.part_base[rt] * kTileM + trow) * 8 + 4 * et.half;
+    for (int s0 = 0; s0 < np; s0 += 4) {  // up to 16 loads in flight
+        longlong2 v[4][4];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const longlong2 v = __ldcg(pp + u);
-            add128(S[u], I128{v.x, (unsigned long long)v.y});
-        }
+        for (int j = 0; j < 4; ++j)
+            if (s0 + j < np)
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[j][u] = __ldcg(p0 + (size_t)(s0 + j) * kTileM * 8 + u);
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (s0 + j < np)
+#pragma unroll
+                for (int u = 0; u < 4; ++u) add128(S[u], I128{v[j][u].x, (unsigned long long)v[j][u].y});
     }
-    const double rs = L.rscale[mat][row];
-    double y[8];
+    const double rs = L.rscale[et.row];
+    double y[4];
 #pragma unroll
-    for (int u = 0; u < 8; ++u)
-        y[u] = ((double)S[u].hi * 0x1p64 + (double)S[u].lo) * (pow2(max(E[u], -900) - 64) * rs);
-    if (io.kind == 1) {
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            double v = 0.0;
-            if (row < L.N) {
-                double yv = y[u];
-                if (io.vm1) yv -= L.shift * __ldcg(io.vm1 + (size_t)row * 8 + u);
-                v = io.k == 1 ? yv : 2.0 * yv - __ldcg(io.vm2 + (size_t)row * 8 + u);
-                io.vk[(size_t)row * 8 + u] = v;
-            }
-            y[u] = v;
+    for (int u = 0; u < 4; ++u) {
+        const int col = 4 * et.half + u;
+        const double yv = i128_to_double(S[u]) * (pow2(max(E[col], -900) - 64) * rs);
+        double v = 0.0;  // v_k = Hs v_{k-1} (k = 1), 2 Hs v_{k-1} - v_{k-2} after; rows past N stay zero
+        if (et.row < L.N) {
+            v = io.k == 1 ? yv : 2.0 * yv - io.vm2[(size_t)et.row * 8 + col];
+            io.vk[(size_t)et.row * 8 + col] = v;
         }
-        if (row < L.N)
-            for (int col = 0; col < L.m; ++col) {  // acc += c_k v_k, complex column col
-                double2 *ap = L.acc + (size_t)row * L.m + col;
-                double2 a = __ldcg(ap);  // the row's last writer may have been another CTA
-                const double vr = y[2 * col], vi = y[2 * col + 1];
-                a.x += io.cre * vr - io.cim * vi;
-                a.y += io.cre * vi + io.cim * vr;
-                *ap = a;
-            }
-    } else if (row >= L.N) {
-#pragma unroll
-        for (int u = 0; u < 8; ++u) y[u] = 0.0;
+        y[u] = v;
     }
-    slice_rows_out(c, rt, t, y, io.xs_out, io.xe_out, io.emax_out);
+    if (et.row < L.N)
+        for (int cc = 0; cc < 2 && 2 * et.half + cc < L.m; ++cc) {  // acc += c_k v_k, complex column
+            double2 *ap = L.acc + (size_t)et.row * L.m + 2 * et.half + cc;
+            double2 a = *ap;
+            const double vr = y[2 * cc], vi = y[2 * cc + 1];
+            a.x += io.cre * vr - io.cim * vi;
+            a.y += io.cre * vi + io.cim * vr;
+            *ap = a;
+        }
+    slice_chunk_out(c, h, et, y, io.xs_out, io.xe_out, io.emax_out);
 }
 
-// The CTA's segments: each 64-K block's weight sums folded per chunk into one
-// exact 128-bit integer per row and column, written as the segment's partial
-// and counted at its row tile.  Then the epilogues of the row tiles this CTA
-// is designated for (tile rt by CTA floor(rt grid / tiles): spread over the
-// grid, at most one per CTA while tiles <= grid), each once all of its
-// segments are counted.
-__device__ void flush_and_epilogue(const Ctx &c, const OzLaunch &L, int sched, int mat, const PhaseIO &io, Roles &r) {
+// The CTA's segments: each 64-K block's weight sums folded, with that chunk's
+// vector scale, into one exact 128-bit integer per row and column, stored as
+// the segment's partial and counted at its row tile.  Then the epilogues of the
+// 64-row chunks this CTA is designated for (chunk h by CTA floor(h grid /
+// chunks): spread over the grid, at most one per CTA while chunks <= grid),
+// each once its row tile's segments are all counted.
+__device__ void flush_and_epilogue(const Ctx &c, const OzLaunch &L, const OrderIO &io, Roles &r) {
     const int t = threadIdx.x - 128;  // 0 .. 127: TMEM lane / row in the tile
     const int warp = threadIdx.x >> 5;
-    const int s0 = L.seg_begin[sched][blockIdx.x], s1 = L.seg_begin[sched][blockIdx.x + 1];
-    // every group of this phase is added exactly in the frame 2^(E - 64) of its
+    const int s0 = L.seg_begin[blockIdx.x], s1 = L.seg_begin[blockIdx.x + 1];
+    // every block of this order is added exactly in the frame 2^(E - 64) of its
     // column's largest chunk scale 2^E
     int E[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) E[u] = __ldcg(io.emax_in + u);
     for (int q = s0; q < s1; ++q) {
-        const OzSeg sg = L.segs[sched][q];
+        const OzSeg sg = L.segs[q];
         I128 A[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) A[u] = I128{0, 0ull};
-        long long H[8], Lo[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            H[u] = 0;
-            Lo[u] = 0;
-        }
         for (int kb = sg.kb0; kb < sg.kb1; ++kb) {
             const unsigned tb = r.gcnt & 1;
             // one thread waits and all 128 follow its outcome, so that none is left
@@ -474,34 +497,34 @@ __device__ void flush_and_epilogue(const Ctx &c, const OzLaunch &L, int sched, i
                 return;
             }
             asm volatile("tcgen05.fence::after_thread_sync;");
+            long long H[8], Lo[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                H[u] = 0;
+                Lo[u] = 0;
+            }
             flush_block(c.tmem + ((uint32_t)((warp & 3) * 32) << 16) + tb * kAccCols, H, Lo);
             asm volatile("tcgen05.fence::before_thread_sync;");
             mbar_arrive(&c.accempty[tb]);
             ++r.gcnt;
-            if ((kb & 1) == 1 || kb == sg.kb1 - 1) {  // end of a 128-row chunk of the vector: its scale
-                const int *eg = io.xe_in + (size_t)(kb >> 1) * 8;
+            const int *eg = io.xe_in + (size_t)kb * 8;  // the block's vector chunk exponents
 #pragma unroll
-                for (int u = 0; u < 8; ++u) {
-                    add128(A[u], group_term(H[u], Lo[u], max(0, E[u] - __ldcg(eg + u))));
-                    H[u] = 0;
-                    Lo[u] = 0;
-                }
-            }
+            for (int u = 0; u < 8; ++u) add128(A[u], group_term(H[u], Lo[u], max(0, E[u] - __ldcg(eg + u))));
         }
-        long long *part = reinterpret_cast<long long *>(L.part) +
-                          ((size_t)(L.part_base[sched][sg.rt] + sg.slot) * kTileM + t) * 16;
+        longlong2 *part = reinterpret_cast<longlong2 *>(L.part) +
+                          ((size_t)(L.part_base[sg.rt] + sg.slot) * kTileM + t) * 8;
 #pragma unroll
-        for (int u = 0; u < 8; ++u)
-            *reinterpret_cast<longlong2 *>(part + 2 * u) = make_longlong2(A[u].hi, (long long)A[u].lo);
+        for (int u = 0; u < 8; ++u) part[u] = make_longlong2(A[u].hi, (long long)A[u].lo);
         __threadfence();
         asm volatile("bar.sync 1, 128;" ::: "memory");
         if (t == 0) atomicAdd(&L.tile_cnt[sg.rt], 1u);
     }
-    const int ntiles = (L.N + kTileM - 1) / kTileM, G = gridDim.x;
-    const int rt1 = (int)(((long long)(blockIdx.x + 1) * ntiles + G - 1) / G);
-    for (int rt = (int)(((long long)blockIdx.x * ntiles + G - 1) / G); rt < rt1; ++rt) {
-        const int np = L.part_count[sched][rt];
-        if (t == 0) *c.last_flag = wait_count(&L.tile_cnt[rt], (unsigned)np) ? 1u : 0u;
+    const int nch = 2 * ((L.N + kTileM - 1) / kTileM), G = gridDim.x;
+    const int h1 = (int)(((long long)(blockIdx.x + 1) * nch + G - 1) / G);
+    for (int h = (int)(((long long)blockIdx.x * nch + G - 1) / G); h < h1; ++h) {
+        const int np = L.part_count[h >> 1];
+        // the count only grows (np per order, zero at the launch): order k waits for k np
+        if (t == 0) *c.last_flag = wait_count(&L.tile_cnt[h >> 1], (unsigned)(np * io.k)) ? 1u : 0u;
         asm volatile("bar.sync 1, 128;" ::: "memory");
         const bool ready = *(volatile unsigned *)c.last_flag != 0;
         asm volatile("bar.sync 1, 128;" ::: "memory");
@@ -510,43 +533,41 @@ __device__ void flush_and_epilogue(const Ctx &c, const OzLaunch &L, int sched, i
             return;
         }
         __threadfence();
-        tile_epilogue(c, L, sched, mat, io, rt, np, E, t);
-        if (t == 0) L.tile_cnt[rt] = 0u;  // next used after a grid barrier
+        chunk_epilogue(c, L, io, h, np, E, t);
     }
 }
 
 // order 0: v_0 = s phi (s: pending renormalisation factor), acc = c_0 v_0, and
-// the slices of v_0; row tiles rt = blockIdx.x, + grid, ... by warps 4-7
+// the slices of v_0, by warps 4-7 of the CTA designated for each 64-row chunk
 __device__ void order_zero(const Ctx &c, const OzLaunch &L) {
     const int t = threadIdx.x - 128;
-    const int ntiles = (L.N + kTileM - 1) / kTileM;
+    const int nch = 2 * ((L.N + kTileM - 1) / kTileM), G = gridDim.x;
     const double2 c0 = L.coef[0];
-    for (int rt = blockIdx.x; rt < ntiles; rt += gridDim.x) {
-        const int i = rt * kTileM + t;
-        double y[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) y[u] = 0.0;
-        if (i < L.N)
-            for (int col = 0; col < L.m; ++col) {
-                double2 p = L.phi[(size_t)i * L.m + col];
+    const int h1 = (int)(((long long)(blockIdx.x + 1) * nch + G - 1) / G);
+    for (int h = (int)(((long long)blockIdx.x * nch + G - 1) / G); h < h1; ++h) {
+        const EpiThread et = epi_thread(h, t);
+        double y[4] = {0.0, 0.0, 0.0, 0.0};
+        if (et.row < L.N)
+            for (int cc = 0; cc < 2 && 2 * et.half + cc < L.m; ++cc) {
+                const int col = 2 * et.half + cc;
+                double2 p = L.phi[(size_t)et.row * L.m + col];
                 if (L.scale) {
                     const double sc = L.scale[col % L.P];
                     p.x *= sc;
                     p.y *= sc;
                 }
-                L.v[(size_t)i * 8 + 2 * col] = p.x;
-                L.v[(size_t)i * 8 + 2 * col + 1] = p.y;
-                L.acc[(size_t)i * L.m + col] = make_double2(c0.x * p.x - c0.y * p.y, c0.x * p.y + c0.y * p.x);
-                y[2 * col] = p.x;
-                y[2 * col + 1] = p.y;
+                L.v[(size_t)et.row * 8 + 2 * col] = p.x;
+                L.v[(size_t)et.row * 8 + 2 * col + 1] = p.y;
+                L.acc[(size_t)et.row * L.m + col] = make_double2(c0.x * p.x - c0.y * p.y, c0.x * p.y + c0.y * p.x);
+                y[2 * cc] = p.x;
+                y[2 * cc + 1] = p.y;
             }
-        slice_rows_out(c, rt, t, y, L.xs[0], L.xe[0], L.emax[0]);
+        slice_chunk_out(c, h, et, y, L.xs[0], L.xe[0], L.emax[0]);
     }
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
-    oz_cheb_kernel(const __grid_constant__ CUtensorMap m0, const __grid_constant__ CUtensorMap m1,
-                   const __grid_constant__ CUtensorMap m2, OzLaunch L) {
+    oz_cheb_kernel(const __grid_constant__ CUtensorMap mH, OzLaunch L) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     if ((int)blockIdx.x + 1 == L.exit_cta1) return;  // test hook: the other CTAs' barrier waits run out
     Ctx c;
@@ -560,12 +581,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     c.accfull = c.bempty + kBStages;
     c.accempty = c.accfull + 2;
     c.done = c.accempty + 2;
-    c.red = reinterpret_cast<double *>(c.smem + SmemLayout::red_off);
+    c.red = reinterpret_cast<int *>(c.smem + SmemLayout::red_off);
+    c.out = c.smem + SmemLayout::out_off;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(c.smem + SmemLayout::misc_off);
     c.abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
     c.last_flag = reinterpret_cast<unsigned *>(tmem_slot + 2);
     const int warp = threadIdx.x >> 5;
-    const CUtensorMap *maps[3] = {&m0, &m1, &m2};
     if (threadIdx.x == 0) {
         for (int s = 0; s < kAStages; ++s) {
             mbar_init(&c.full[s], 1);
@@ -597,56 +618,48 @@ __global__ void __launch_bounds__(kThreads, 1)
     Roles r;
 
     if (warp >= 4) order_zero(c, L);  // slices of v_0 into vector buffer 0
-    // The producer and the MMA issuer run through every phase without grid
-    // barriers: the operator tiles do not depend on the previous phase, and the
-    // MMAs wait for each block's vector operand, which thread 64 loads only
-    // after the phase's grid barrier.  So the next phase's loads and MMAs
-    // overlap the barrier.  Warps 2-7 meet every grid barrier on named barrier 2.
+    // The producer and the MMA issuer run through every order without grid
+    // barriers: the operator tiles do not change, and the MMAs wait for each
+    // block's vector operand, which thread 64 loads only after the order's grid
+    // barrier.  So the next order's loads and MMAs overlap the barrier.  Warps
+    // 2-7 meet every grid barrier on named barrier 2.
     bool ok = true;
     if (warp >= 2) ok = grid_barrier_sub(L.bar_count, L.bar_gen, G, L.error, bar_ns);
-    int seq = 0;  // phases so far; the vector of phase seq is in buffer seq % 3
+    // the sliced vector v_k is in buffer k % 3
     for (int k = 1; ok && k <= L.K; ++k) {
-        const double2 ck = L.coef[k];
-        for (int ph = 0; ph < L.nphase && ok; ++ph) {
-            ++seq;
-            // implicit: 0: w = G^T v (sched upper, matrix 0), 1: y = (h/b) w (full, 1),
-            // 2: G y (lower, 2) + recurrence;  explicit: Hs v (full, 1) + recurrence
-            const int sched = L.nphase == 3 ? ph : 1, mat = sched;
-            const int bin = (seq + 2) % 3, bout = seq % 3;
-            if (warp == 0) {
-                if ((threadIdx.x & 31) == 0) produce(c, L, maps[mat], sched, r);
-                ok = !aborted(c) && *(volatile int *)L.error == 0;
-                continue;
-            }
-            if (warp == 1) {
-                if ((threadIdx.x & 31) == 0) issue_mma(c, L, sched, r);
-                ok = !aborted(c) && *(volatile int *)L.error == 0;
-                continue;
-            }
-            if (warp < 4) {
-                // buffer (seq + 1) % 3 was written two phases ago and read in the last one
-                if (blockIdx.x == 0 && threadIdx.x >= 96 && threadIdx.x < 104)
-                    L.emax[(seq + 1) % 3][threadIdx.x - 96] = kNoExp;
-                if (threadIdx.x == 64) load_vectors(c, L, sched, L.xs[bin], r);
-            } else {
-                PhaseIO io{};
-                io.kind = ph == L.nphase - 1 ? 1 : 0;
-                io.k = k;
-                io.cre = ck.x;
-                io.cim = ck.y;
-                io.vm1 = L.nphase == 3 ? L.v + (size_t)((k + 2) % 3) * L.ld * 8 : nullptr;
-                io.vm2 = L.v + (size_t)((k + 1) % 3) * L.ld * 8;
-                io.vk = L.v + (size_t)(k % 3) * L.ld * 8;
-                io.xe_in = L.xe[bin];
-                io.emax_in = L.emax[bin];
-                io.xs_out = L.xs[bout];
-                io.xe_out = L.xe[bout];
-                io.emax_out = L.emax[bout];
-                flush_and_epilogue(c, L, sched, mat, io, r);
-            }
-            ok = grid_barrier_sub(L.bar_count, L.bar_gen, G, L.error, bar_ns) && !aborted(c);
-            if (!ok && threadIdx.x == 64) atomicExch(c.abort_flag, 1);  // stops this CTA's producer and MMA issuer
+        const int bin = (k + 2) % 3, bout = k % 3;
+        if (warp == 0) {
+            if ((threadIdx.x & 31) == 0) produce(c, L, &mH, r);
+            ok = !aborted(c) && *(volatile int *)L.error == 0;
+            continue;
         }
+        if (warp == 1) {
+            if ((threadIdx.x & 31) == 0) issue_mma(c, L, r);
+            ok = !aborted(c) && *(volatile int *)L.error == 0;
+            continue;
+        }
+        if (warp < 4) {
+            // buffer (k + 1) % 3 was written two orders ago and read in the last one
+            if (blockIdx.x == 0 && threadIdx.x >= 96 && threadIdx.x < 104)
+                L.emax[(k + 1) % 3][threadIdx.x - 96] = kNoExp;
+            if (threadIdx.x == 64) load_vectors(c, L, L.xs[bin], r);
+        } else {
+            OrderIO io{};
+            const double2 ck = L.coef[k];
+            io.k = k;
+            io.cre = ck.x;
+            io.cim = ck.y;
+            io.vm2 = L.v + (size_t)((k + 1) % 3) * L.ld * 8;
+            io.vk = L.v + (size_t)(k % 3) * L.ld * 8;
+            io.xe_in = L.xe[bin];
+            io.emax_in = L.emax[bin];
+            io.xs_out = L.xs[bout];
+            io.xe_out = L.xe[bout];
+            io.emax_out = L.emax[bout];
+            flush_and_epilogue(c, L, io, r);
+        }
+        ok = grid_barrier_sub(L.bar_count, L.bar_gen, G, L.error, bar_ns) && !aborted(c);
+        if (!ok && threadIdx.x == 64) atomicExch(c.abort_flag, 1);  // stops this CTA's producer and MMA issuer
     }
     // drain: copies issued into the A ring and every MMA complete before the CTA
     // leaves and frees its TMEM (all consumed already unless a wait gave up)
@@ -672,7 +685,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 }
 
-// matrix slices: storage column j of M (ld rows, the row j of the operand A)
+// operator slices: storage column j of the symmetric Hs (ld rows, its row j)
 // on the scale 2^e_j of its largest element; out[s][j][i], rscale[j] = 2^e_j
 __global__ void oz_slice_kernel(const double *__restrict__ M, int n, int ld, __nv_bfloat16 *__restrict__ out,
                                 double *__restrict__ rscale) {
@@ -691,12 +704,11 @@ __global__ void oz_slice_kernel(const double *__restrict__ M, int n, int ld, __n
     }
     __syncthreads();
     const int e = scale_exp(s_max[0]);
-    const double inv = pow2(-e);
     if (threadIdx.x == 0) rscale[j] = pow2(e);
     const size_t sstride = (size_t)n * ld;
     for (int i = threadIdx.x; i < ld; i += blockDim.x) {
         int dig[kS];
-        slice7(col[i] * inv, dig);
+        slice7(col[i], e, dig);
 #pragma unroll
         for (int s = 0; s < kS; ++s) out[s * sstride + (size_t)j * ld + i] = __float2bfloat16_rn((float)dig[s]);
     }
@@ -748,39 +760,25 @@ cudaError_t oz_slice_matrix(const double *M, int n, int ld, __nv_bfloat16 *out, 
     return cudaGetLastError();
 }
 
-void oz_schedule(int n, int grid, int type, std::vector<OzSeg> &segs, std::vector<int> &seg_begin,
-                 std::vector<int> &part_base, std::vector<int> &part_count) {
+void oz_schedule(int n, int grid, std::vector<OzSeg> &segs, std::vector<int> &seg_begin, std::vector<int> &part_base,
+                 std::vector<int> &part_count) {
     const int nkb = (n + kKB - 1) / kKB, ntiles = (n + kTileM - 1) / kTileM;
-    // blocks of row tile rt: full [0, nkb); upper (A = G^T, k >= row) [2 rt, nkb);
-    // lower (A = G, k <= row) [0, 2 rt + 2)
-    std::vector<int> lo(ntiles), hi(ntiles);
-    long long total = 0;
-    for (int rt = 0; rt < ntiles; ++rt) {
-        lo[rt] = type == 0 ? 2 * rt : 0;
-        hi[rt] = type == 2 ? std::min(nkb, 2 * rt + 2) : nkb;
-        lo[rt] = std::min(lo[rt], hi[rt]);
-        total += hi[rt] - lo[rt];
-    }
+    const long long total = (long long)nkb * ntiles;
     segs.clear();
     seg_begin.assign(grid + 1, 0);
     part_base.assign(ntiles, 0);
     part_count.assign(ntiles, 0);
     // CTA b takes the blocks [total b / grid, total (b + 1) / grid) in (row tile, block) order
-    int rt = 0;
-    long long pos = 0;  // blocks before row tile rt
     for (int b = 0; b < grid; ++b) {
         long long u0 = total * b / grid;
         const long long u1 = total * (b + 1) / grid;
         while (u0 < u1) {
-            while (rt < ntiles && u0 >= pos + (hi[rt] - lo[rt])) {
-                pos += hi[rt] - lo[rt];
-                ++rt;
-            }
-            const long long end = std::min(u1, pos + (hi[rt] - lo[rt]));
+            const int rt = (int)(u0 / nkb);
+            const long long end = std::min(u1, (long long)(rt + 1) * nkb);
             OzSeg s;
             s.rt = rt;
-            s.kb0 = lo[rt] + (int)(u0 - pos);
-            s.kb1 = lo[rt] + (int)(end - pos);
+            s.kb0 = (int)(u0 - (long long)rt * nkb);
+            s.kb1 = (int)(end - (long long)rt * nkb);
             s.slot = part_count[rt]++;
             segs.push_back(s);
             u0 = end;
@@ -790,17 +788,14 @@ void oz_schedule(int n, int grid, int type, std::vector<OzSeg> &segs, std::vecto
     for (int t = 1; t < ntiles; ++t) part_base[t] = part_base[t - 1] + part_count[t - 1];
 }
 
-cudaError_t launch_oz_cheb(const OzLaunch &L, const __nv_bfloat16 *const slices[3], int grid, cudaStream_t st) {
-    CUtensorMap m[3];
-    for (int t = 0; t < 3; ++t) {
-        const __nv_bfloat16 *base = slices[t] ? slices[t] : slices[1];
-        if (make_slice_map(&m[t], base, L.N, L.ld)) return cudaErrorInvalidValue;
-    }
+cudaError_t launch_oz_cheb(const OzLaunch &L, const __nv_bfloat16 *hs_slices, int grid, cudaStream_t st) {
+    CUtensorMap m;
+    if (make_slice_map(&m, hs_slices, L.N, L.ld)) return cudaErrorInvalidValue;
     const size_t smem = oz_smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(oz_cheb_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     OzLaunch copy = L;
-    void *args[] = {&m[0], &m[1], &m[2], &copy};
+    void *args[] = {&m, &copy};
     e = cudaLaunchCooperativeKernel((const void *)oz_cheb_kernel, dim3(grid), dim3(kThreads), args, smem, st);
     count_launch();
     return e;

@@ -20,9 +20,10 @@
 // One CTA computes a 128 x 32 tile of C over the tile's non-zero K blocks:
 //   warp 0     TMA producer: per 64-K block the 7 op(B) slices (32 x 64 each) into
 //              a B stage, then the 7 op(A) slices (128 x 64) into a ring of A stages;
-//   warp 1     allocates TMEM; one thread issues tcgen05.mma (M = 128, N = 32,
-//              K = 16) of A slice a against B slices b <= 6 - a into the weight
-//              accumulator a + b of one of two 224-column buffers;
+//   warp 1     allocates TMEM; one thread issues tcgen05.mma (M = 128, K = 16)
+//              of A slice a against the B slices b <= 6 - a at once (N = 32 (7 - a),
+//              D from column 32 a, so that B slice b lands on the weight
+//              accumulator a + b) in one of two 224-column buffers;
 //   warps 2-5  fold each block's accumulators into H and L (one thread per row)
 //              and write C.
 // Operands are sliced by oz_partmax_kernel and oz_slice_kernel beforehand
@@ -155,7 +156,7 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(OperandView va, OperandVi
             const int r = r0 + rr, j = j0 + threadIdx.x;
             if (r >= v.rows || j >= kp) continue;
             int dig[kS];
-            slice7(t[rr][threadIdx.x] * pow2(-s_e[rr]), dig);
+            slice7(t[rr][threadIdx.x], s_e[rr], dig);
 #pragma unroll
             for (int sl = 0; sl < kS; ++sl) out[sl * sstride + (size_t)r * kp + j] = __float2bfloat16_rn((float)dig[sl]);
         }
@@ -256,7 +257,6 @@ __global__ void __launch_bounds__(kThreads, 1)
         issued = acnt;
     } else if (warp == 1 && lane == 0) {
         // ---- MMA issuer
-        const uint32_t idesc = idesc_bf16(kTM, kTN);
         unsigned acnt = 0;
         for (int kb = kb0, bi = 0; kb < kb1; ++kb, ++bi) {
             const unsigned tb = bi & 1, sb = bi % kBStages;
@@ -278,14 +278,16 @@ __global__ void __launch_bounds__(kThreads, 1)
                     break;
                 }
                 asm volatile("tcgen05.fence::after_thread_sync;");
+                // one MMA of A slice a against the B slices 0 .. 6 - a, which lie one after
+                // another in the stage (32 rows each): column block b of its D lands on
+                // weight a + b at TMEM column 32 (a + b); N = 32 (7 - a)
                 const uint64_t da = smem_desc_sw128(smem + Smem::a_off + (size_t)s * kATile);
-                for (int b = 0; b + a < kS; ++b) {
-                    const uint64_t db = smem_desc_sw128(smem + Smem::b_off + (size_t)sb * kBStage + (size_t)b * kBSlice);
-                    const uint32_t acc = tmem + tb * kAccCols + (uint32_t)((a + b) * kTN);
+                const uint64_t db = smem_desc_sw128(smem + Smem::b_off + (size_t)sb * kBStage);
+                const uint32_t acc = tmem + tb * kAccCols + (uint32_t)(a * kTN);
+                const uint32_t idesc = idesc_bf16(kTM, kTN * (kS - a));
 #pragma unroll
-                    for (int k = 0; k < kKB / 16; ++k)  // the first product of each weight (a = 0) starts it
-                        umma_bf16(acc, da + (uint64_t)(k * 2), db + (uint64_t)(k * 2), idesc, !(a == 0 && k == 0));
-                }
+                for (int k = 0; k < kKB / 16; ++k)  // the first MMA (a = 0: all weights) starts the block
+                    umma_bf16(acc, da + (uint64_t)(k * 2), db + (uint64_t)(k * 2), idesc, !(a == 0 && k == 0));
                 umma_commit(&empty[s]);
                 ++acnt;
             }

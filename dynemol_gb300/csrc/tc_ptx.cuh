@@ -132,14 +132,27 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
 
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// Exact slices of the Ozaki scheme: xs = x 2^-e with |xs| < 1 (the scale of
-// its row or column) as 7 balanced base-256 digits, xs ~ sum_s n_s 2^(-8 (s+1))
-// to the nearest 2^-56: one FP64 multiply and one conversion to a 64-bit
-// integer T = rint(xs 2^56), then the digits in integer arithmetic from the
-// bottom (n_s in [-128, 127] for s >= 1, |n_0| <= 256).  GB300's FP64 pipe
-// runs at 1/64 of its integer rate, so the digits are not formed in FP64.
-__device__ __forceinline__ void slice7(double xs, int (&n)[7]) {
-    long long T = __double2ll_rn(xs * 0x1p56);
+// Exact slices of the Ozaki scheme: x on the scale 2^e (|x| < 2^e) as 7
+// balanced base-256 digits, x 2^-e ~ sum_s n_s 2^(-8 (s+1)) to the nearest
+// 2^-56: T = rint(x 2^(56-e)) (round half to even) taken from the bits of x,
+// then the digits from the bottom (n_s in [-128, 127] for s >= 1, |n_0| <= 256).
+// Integer arithmetic only: GB300's FP64 pipe and its conversions are slow.
+__device__ __forceinline__ void slice7(double x, int e, int (&n)[7]) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int be = (int)((b >> 52) & 0x7ff);
+    const unsigned long long m = (b & 0xfffffffffffffull) | (be ? (1ull << 52) : 0ull);
+    const int sh = (be ? be : 1) - 1075 + 56 - e;  // x = m 2^((be ? be : 1) - 1075), |x 2^(56-e)| < 2^56
+    long long T;
+    if (sh >= 0) {
+        T = (long long)(m << sh);
+    } else if (sh > -64) {
+        const int k = -sh;
+        const unsigned long long q = m >> k, rem = m & ((1ull << k) - 1), half = 1ull << (k - 1);
+        T = (long long)(q + ((rem > half || (rem == half && (q & 1))) ? 1ull : 0ull));
+    } else {
+        T = 0;
+    }
+    if (b >> 63) T = -T;
 #pragma unroll
     for (int s = 6; s >= 1; --s) {
         const int d = (int)(((T + 128) & 255) - 128);
@@ -147,6 +160,12 @@ __device__ __forceinline__ void slice7(double xs, int (&n)[7]) {
         T = (T - d) >> 8;
     }
     n[0] = (int)T;
+}
+
+// exponent e with |x| < 2^e for the finite x != 0 (0 for x = 0), from its bits:
+// the biased exponent field minus 1022 (subnormals: -1021)
+__device__ __forceinline__ int exp_field(double x) {
+    return (int)((__double_as_longlong(x) >> 52) & 0x7ff);
 }
 
 }  // namespace tc

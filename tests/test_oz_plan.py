@@ -2,14 +2,14 @@
 propagation in dynemol_gb300/csrc/ozaki.cu, the factorisation products in
 dynemol_gb300/csrc/ozgemm.cu), checked on the CPU before any GPU run:
 
-* the block schedules (oz_schedule): for the full, upper (A = G^T) and lower
-  (A = G) operators every non-zero 128 x 64 block of the operator is given to
-  exactly one CTA, CTAs differ by at most one block, a row tile's segments are
-  numbered in K order and their partial slots fit the partial buffer;
+* the block schedule (oz_schedule): every 128 x 64 block of the operator is
+  given to exactly one CTA, CTAs differ by at most one block, a row tile's
+  segments are numbered in K order and their partial slots fit the partial
+  buffer, and every row tile has one CTA designated for its epilogue;
 * the arithmetic: operands cut into 7 slices of 8 bits on power-of-two scales
   exactly as the kernels do (slice7: one rounding to a 64-bit integer, then
   balanced base-256 digits; operator rows one scale each, vector columns one
-  per 128-row chunk), the slice products of one weight s_a + s_b accumulated
+  per 64-row chunk), the slice products of one weight s_a + s_b accumulated
   together per 64-K block, where every sum of absolute products must stay at or
   below 2^24 (so that the tensor cores' FP32 accumulation is exact), the weights <= 6 folded exactly into
   two 64-bit integers and the chunks added as integers in the frame of the
@@ -40,29 +40,21 @@ def _const(name):
 
 
 S, TILE, KB = _const("kS"), _const("kTileM"), _const("kKB")
-CHUNK = 128  # rows of a vector sharing one scale per column (one output row tile)
+CHUNK = 64  # rows of a vector sharing one scale per column (one 64-K block)
 GRID = 152
 
 
-def schedule(n, grid, typ):
+def schedule(n, grid):
     """oz_schedule: (segments, seg_begin, part_base, part_count); a segment is (rt, kb0, kb1, slot)."""
     nkb, ntiles = -(-n // KB), -(-n // TILE)
-    lo, hi = [], []
-    for rt in range(ntiles):
-        h = min(nkb, 2 * rt + 2) if typ == 2 else nkb
-        lo.append(min(2 * rt if typ == 0 else 0, h))
-        hi.append(h)
-    total = sum(h - l for l, h in zip(lo, hi))
+    total = nkb * ntiles
     segs, begin, count = [], [0], [0] * ntiles
-    rt, pos = 0, 0
     for b in range(grid):
         u0, u1 = total * b // grid, total * (b + 1) // grid
         while u0 < u1:
-            while rt < ntiles and u0 >= pos + (hi[rt] - lo[rt]):
-                pos += hi[rt] - lo[rt]
-                rt += 1
-            end = min(u1, pos + (hi[rt] - lo[rt]))
-            segs.append((rt, lo[rt] + u0 - pos, lo[rt] + end - pos, count[rt]))
+            rt = u0 // nkb
+            end = min(u1, (rt + 1) * nkb)
+            segs.append((rt, u0 - rt * nkb, end - rt * nkb, count[rt]))
             count[rt] += 1
             u0 = end
         begin.append(len(segs))
@@ -74,36 +66,35 @@ def schedule(n, grid, typ):
 
 def test_schedule_source_matches_replay():
     """The replay follows the source's block ranges (guard against drift)."""
-    assert "lo[rt] = type == 0 ? 2 * rt : 0;" in OZ
-    assert "hi[rt] = type == 2 ? std::min(nkb, 2 * rt + 2) : nkb;" in OZ
+    assert "const long long total = (long long)nkb * ntiles;" in OZ
     assert "long long u0 = total * b / grid;" in OZ
+    assert "const int rt = (int)(u0 / nkb);" in OZ
 
 
 @pytest.mark.parametrize("n", [1, 2, 8, 63, 64, 65, 127, 128, 129, 450, 1000, 1860, 2170, 3720, 4096, 8192, 16384])
-@pytest.mark.parametrize("typ", [0, 1, 2])
-def test_schedule_covers_nonzero_blocks_once(n, typ):
-    segs, begin, base, count = schedule(n, GRID, typ)
+def test_schedule_covers_blocks_once(n):
+    """Every 128 x 64 block of the operator (rows and K below n) goes to exactly
+    one CTA, CTAs differ by at most one block, a row tile's segments are
+    numbered in K order, partial slots fit the buffer, and the epilogue of row
+    tile rt has one designated CTA, floor(rt grid / tiles)."""
+    segs, begin, base, count = schedule(n, GRID)
     nkb, ntiles = -(-n // KB), -(-n // TILE)
     seen = np.zeros((ntiles, nkb), dtype=int)
     for rt, k0, k1, slot in segs:
         assert 0 <= rt < ntiles and 0 <= k0 < k1 <= nkb
         seen[rt, k0:k1] += 1
-    # a block is needed iff some (row, k) inside it with row, k < n lies in the operator's triangle
-    for rt in range(ntiles):
-        for kb in range(nkb):
-            r0, r1 = rt * TILE, min(n, rt * TILE + TILE) - 1
-            k0, k1 = kb * KB, min(n, kb * KB + KB) - 1
-            need = {0: k1 >= r0, 1: True, 2: k0 <= r1}[typ]
-            assert seen[rt, kb] == (1 if need else 0), (rt, kb)
+    assert np.all(seen == 1)
     per_cta = [sum(s[2] - s[1] for s in segs[begin[b]:begin[b + 1]]) for b in range(GRID)]
     assert max(per_cta) - min(per_cta) <= 1
-    # segments of a row tile: slots 0.. in K order; partial slots within the buffer
     for rt in range(ntiles):
         mine = sorted([s for s in segs if s[0] == rt], key=lambda s: s[3])
         assert [s[3] for s in mine] == list(range(count[rt]))
         assert all(mine[i][2] == mine[i + 1][1] for i in range(len(mine) - 1))
         assert base[rt] + count[rt] <= len(segs)
     assert len(segs) <= GRID + ntiles
+    designated = [[rt for rt in range(-(-b * ntiles // GRID), -(-(b + 1) * ntiles // GRID))] for b in range(GRID)]
+    assert sorted(rt for d in designated for rt in d) == list(range(ntiles))
+    assert all(rt * GRID // ntiles == b for b, d in enumerate(designated) for rt in d)
 
 
 def scale_exp(mx):
@@ -115,7 +106,8 @@ def scale_exp(mx):
 
 def slices(x, e):
     """x (1-D) on scale 2^e cut as slice7 (tc_ptx.cuh) does: T = rint(x 2^-e 2^56) as a
-    64-bit integer, then balanced base-256 digits from the bottom."""
+    64-bit integer (the kernel rounds on the bits; test_slice7_bits_round_like_rint),
+    then balanced base-256 digits from the bottom."""
     T = np.rint(x * np.ldexp(1.0, -e) * 2.0 ** 56).astype(np.int64)
     out = [None] * S
     for s in range(S - 1, 0, -1):
@@ -128,14 +120,45 @@ def slices(x, e):
 
 def test_slice7_source_matches_replay():
     src = open(os.path.join(ROOT, "dynemol_gb300", "csrc", "tc_ptx.cuh")).read()
-    assert "long long T = __double2ll_rn(xs * 0x1p56);" in src
+    assert "const int sh = (be ? be : 1) - 1075 + 56 - e;" in src  # T = rint(x 2^(56 - e)) from the bits
+    assert "T = (long long)(q + ((rem > half || (rem == half && (q & 1))) ? 1ull : 0ull));" in src  # half to even
     assert "const int d = (int)(((T + 128) & 255) - 128);" in src
     assert "T = (T - d) >> 8;" in src
 
 
+def slice7_bits(x, e):
+    """slice7's rounding of x 2^(56 - e) done on the bits as the kernel does (Python ints)."""
+    b = int(np.float64(x).view(np.uint64))
+    be = (b >> 52) & 0x7FF
+    m = (b & ((1 << 52) - 1)) | ((1 << 52) if be else 0)
+    sh = (be if be else 1) - 1075 + 56 - e
+    if sh >= 0:
+        T = m << sh
+    elif sh > -64:
+        k = -sh
+        q, rem, half = m >> k, m & ((1 << k) - 1), 1 << (k - 1)
+        T = q + (1 if (rem > half or (rem == half and (q & 1))) else 0)
+    else:
+        T = 0
+    return -T if b >> 63 else T
+
+
+def test_slice7_bits_round_like_rint():
+    """The integer rounding equals rint(x 2^(56 - e)) for normal, tiny and subnormal
+    values, ties included."""
+    rng = np.random.default_rng(3)
+    xs = list(rng.standard_normal(2000) * np.exp(rng.uniform(-40, 3, 2000)))
+    xs += [0.0, -0.0, 5e-324, -7e-320, 2.0 ** -1022, 1.5 * 2.0 ** -60, 2.5 * 2.0 ** -56, 3.5 * 2.0 ** -56]
+    for x in xs:
+        e = scale_exp(abs(x)) if x != 0 else 0
+        for ee in (e, e + 3):
+            want = round(Fraction(float(x)) * Fraction(2) ** (56 - ee))  # half to even
+            assert slice7_bits(x, ee) == want, (x, ee)
+
+
 def oz_product(A, X):
     """y = A X as oz_cheb_kernel computes it: row scales for A, one scale per
-    128-row chunk and column for X (the producing epilogue's tile); per 64-K block
+    64-row chunk and column for X (the producing epilogue's chunk); per 64-K block
     all pairs of weight d = a + b <= 6 share one accumulator, folded exactly into
     H (weights d <= 2) and L (d >= 3) over the chunk's blocks; T = 2^32 H + L is
     added, shifted down to the frame of the column's
@@ -254,3 +277,30 @@ def test_gemm_weight_sums_are_exact_and_fold_to_the_product():
             out[i, j] = float(Fraction((H << 32) + L, 1 << 64) * Fraction(2) ** (er[i] + ec[j]))
     ref = exact_product(A, B)
     assert np.all(np.abs(out - ref) <= oz_bound(A, B))
+
+
+def i128_to_double(v):
+    """The kernel's rounding of a 128-bit integer to FP64: its magnitude from three
+    positive parts (high word, two 32-bit halves of the low word), two roundings."""
+    m = abs(v)
+    hi, lo = m >> 64, m & ((1 << 64) - 1)
+    assert hi < 1 << 52
+    d = float(hi) * 2.0 ** 64 + (float(lo >> 32) * 2.0 ** 32 + float(lo & 0xFFFFFFFF))
+    return -d if v < 0 else d
+
+
+def test_partial_sums_round_to_fp64():
+    """The exact 128-bit sum of a row tile's partials rounds to within 2 ulp,
+    negative sums included (rounding the magnitude avoids the cancellation of a
+    two's complement high word -1 against a large low word)."""
+    src = open(os.path.join(ROOT, "dynemol_gb300", "csrc", "ozaki.cu")).read()
+    assert "fma(u52_to_double(s.lo >> 32), 0x1p32, u52_to_double(s.lo & 0xffffffffull))" in src
+    rng = np.random.default_rng(5)
+    for trial in range(4000):
+        nseg = int(rng.integers(1, 9))
+        parts = [int(rng.integers(-2 ** 62, 2 ** 62)) * int(rng.integers(1, 2 ** 28)) >> int(rng.integers(0, 60))
+                 for _ in range(nseg)]
+        total = sum(parts)
+        assert abs(total) < 2 ** 116
+        d = i128_to_double(total)
+        assert abs(Fraction(d) - total) <= 2 * abs(Fraction(total)) * Fraction(1, 2 ** 53)
