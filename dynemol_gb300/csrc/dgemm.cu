@@ -9,7 +9,11 @@
 // the tile only has to keep that pipe fed: 64 x 64 outputs per CTA of 256
 // threads, 4 x 4 per thread (16 independent FMA chains), K in steps of 16 staged
 // in shared memory by cp.async, double buffered.  Eight shared-memory reads per
-// 16 FMAs are far inside the shared-memory bandwidth.
+// 16 FMAs are far inside the shared-memory bandwidth.  Products too small to
+// give every SM work in 64 x 64 tiles (the 64- to 256-row blocks of the
+// factorisations: one 64^3 product is 4 units of 64 x 64 x 16) take 32 x 32 or
+// 16 x 16 tiles (2 x 2 or 1 x 1 outputs per thread), so that up to 64 times as
+// many SMs share them.
 //
 // Triangular operands (flags in `tri`, local block coordinates): elements on the
 // zero side of a triangular operand are treated as zero whatever is stored
@@ -30,20 +34,21 @@
 namespace elhl {
 namespace {
 
-constexpr int kBM = 64, kBN = 64, kBK = 16;
-constexpr int kTM = 4, kTN = 4;
-constexpr int kRT = kBM / kTM, kCT = kBN / kTN;  // threads along rows and columns
+constexpr int kBK = 16;
+constexpr int kRT = 16, kCT = 16;      // threads along rows and columns
 constexpr int kThreads = kRT * kCT;
-constexpr int kMaxPartials = 4096;     // partial tiles held by the workspace (128 MB)
+constexpr int kMaxTile = 64;           // output tiles of BM x BM, BM = 64, 32 or 16
+constexpr int kMaxPartials = 4096;     // partial 64 x 64 tiles held by the workspace (128 MB)
 constexpr int kUnitsPerSlot = 6;       // work units per resident CTA the chunk length aims at
 constexpr int kLanes = 2;              // products that may run concurrently (streams), each with its own state
 struct Lane {
-    double *part = nullptr;            // [tile * chunks + chunk][kBM * kBN]
+    double *part = nullptr;            // [tile * chunks + chunk][BM * BM]
     int *count = nullptr;              // [tile] arrivals, back to 0 after each fix-up
     int *sched = nullptr;              // next unit (64-bit), CTAs finished; back to 0 after each launch
 };
 Lane g_lane[kLanes];
-int g_slots = 0;                       // resident CTAs of the whole GPU
+int g_sms = 0;
+int g_slots[3] = {0, 0, 0};            // resident CTAs of the whole GPU for BM = 64, 32, 16
 
 __device__ __forceinline__ void cp_async8(double *dst, const double *src, int src_bytes) {
     const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
@@ -73,8 +78,9 @@ struct DgemmArgs {
 // directly; otherwise each chunk writes its partial tile and the unit arriving
 // last at the tile's counter sums the partials in chunk order (deterministic)
 // and writes C.  The last CTA to finish resets the counter for the next launch.
-template <bool TA, bool TB>
+template <bool TA, bool TB, int BM>
 __global__ void __launch_bounds__(kThreads) dgemm_kernel(const DgemmArgs g) {
+    constexpr int kBM = BM, kBN = BM, kTM = BM / kRT, kTN = BM / kCT;
     __shared__ double As[2][kBK][kBM + 1];
     __shared__ double Bs[2][kBK][kBN + 1];
     __shared__ long long s_unit;
@@ -207,56 +213,84 @@ __global__ void __launch_bounds__(kThreads) dgemm_kernel(const DgemmArgs g) {
     }
 }
 
+template <int BM>
+cudaError_t launch_dgemm(const DgemmArgs &g, bool transA, bool transB, int grid, cudaStream_t st) {
+#define ELHL_DGEMM(TA_, TB_) dgemm_kernel<TA_, TB_, BM><<<grid, kThreads, 0, st>>>(g)
+    if (transA && transB) ELHL_DGEMM(true, true);
+    else if (transA) ELHL_DGEMM(true, false);
+    else if (transB) ELHL_DGEMM(false, true);
+    else ELHL_DGEMM(false, false);
+#undef ELHL_DGEMM
+    return cudaGetLastError();
+}
+
+template <int BM>
+cudaError_t resident(int &slots) {
+    int per_sm = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dgemm_kernel<false, false, BM>, kThreads, 0);
+    slots = std::max(1, per_sm) * g_sms;
+    return e;
+}
+
 }  // namespace
 
 cudaError_t dgemm64(int m, int n, int k, double alpha, const double *A, int lda, bool transA, const double *B, int ldb,
                     bool transB, double beta, double *C, int ldc, cudaStream_t st, int tri, int lane) {
     if (m <= 0 || n <= 0) return cudaSuccess;
     if (lane < 0 || lane >= kLanes) return cudaErrorInvalidValue;
-    if (!g_slots) {
-        int dev = 0, sms = 0, per_sm = 0;
+    if (!g_sms) {
+        int dev = 0, sms = 0;
         cudaError_t e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, dgemm_kernel<false, false>, kThreads, 0);
         if (e != cudaSuccess) return e;
-        g_slots = std::max(1, per_sm) * sms;
+        g_sms = sms;
+        if ((e = resident<64>(g_slots[0])) != cudaSuccess) return e;
+        if ((e = resident<32>(g_slots[1])) != cudaSuccess) return e;
+        if ((e = resident<16>(g_slots[2])) != cudaSuccess) return e;
     }
     Lane &ln = g_lane[lane];
     if (!ln.part) {
-        cudaError_t e = cudaMalloc(&ln.part, (size_t)kMaxPartials * kBM * kBN * sizeof(double));
-        if (e == cudaSuccess) e = cudaMalloc(&ln.count, (size_t)kMaxPartials * sizeof(int));
-        if (e == cudaSuccess) e = cudaMemset(ln.count, 0, (size_t)kMaxPartials * sizeof(int));
+        cudaError_t e = cudaMalloc(&ln.part, (size_t)kMaxPartials * kMaxTile * kMaxTile * sizeof(double));
+        if (e == cudaSuccess) e = cudaMalloc(&ln.count, (size_t)kMaxPartials * 16 * sizeof(int));
+        if (e == cudaSuccess) e = cudaMemset(ln.count, 0, (size_t)kMaxPartials * 16 * sizeof(int));
         if (e == cudaSuccess) e = cudaMalloc(&ln.sched, 4 * sizeof(int));
         if (e == cudaSuccess) e = cudaMemset(ln.sched, 0, 4 * sizeof(int));
         if (e != cudaSuccess) return e;
     }
+    const int kt = std::max(1, (k + kBK - 1) / kBK);
+    // the largest tile at most twice the product's narrow side whose (tile, k tile)
+    // units number at least half of kUnitsPerSlot per resident CTA slot; else the
+    // smallest
+    int v = 0;
+    while (v < 2) {
+        const int bm = kMaxTile >> v;
+        const long long units = (long long)((m + bm - 1) / bm) * ((n + bm - 1) / bm) * kt;
+        if (bm <= 2 * std::min(m, n) && 2 * units >= (long long)kUnitsPerSlot * g_slots[v]) break;
+        ++v;
+    }
+    const int bm = kMaxTile >> v, scale = 1 << (2 * v);  // partial tiles per 64 x 64 of workspace
     // lane 1 runs beside lane 0's work (single-CTA leaves, small products): it leaves
     // a quarter of the resident CTA slots free
-    const int slots = lane == 0 ? g_slots : std::max(1, g_slots * 3 / 4);
-    DgemmArgs g{m, n, k, alpha, beta, A, B, C, lda, ldb, ldc, tri, (m + kBM - 1) / kBM, (n + kBN - 1) / kBN,
+    const int slots = lane == 0 ? g_slots[v] : std::max(1, g_slots[v] * 3 / 4);
+    DgemmArgs g{m, n, k, alpha, beta, A, B, C, lda, ldb, ldc, tri, (m + bm - 1) / bm, (n + bm - 1) / bm,
                 1, 1, 0, ln.part, ln.count, ln.sched};
-    const long long tiles = (long long)g.gx * g.gy;
-    const int kt = std::max(1, (k + kBK - 1) / kBK);
+    const long long tiles = (long long)g.gx * g.gy, max_part = (long long)kMaxPartials * scale;
     // chunk length: about kUnitsPerSlot units per resident CTA, whole k ranges when
     // the tiles alone are enough, and no more partial tiles than the workspace holds
     long long chunk = (tiles * kt + (long long)kUnitsPerSlot * slots - 1) / ((long long)kUnitsPerSlot * slots);
     chunk = std::max(1ll, std::min<long long>(chunk, kt));
-    while (chunk < kt && tiles * ((kt + chunk - 1) / chunk) > kMaxPartials) chunk *= 2;
+    while (chunk < kt && tiles * ((kt + chunk - 1) / chunk) > max_part) chunk *= 2;
     if (chunk >= kt) chunk = kt;
     g.chunk = (int)chunk;
     g.nchunk = (kt + g.chunk - 1) / g.chunk;
-    if (g.nchunk > 1 && tiles > kMaxPartials) return cudaErrorInvalidValue;  // never: chunk = kt above
+    if (g.nchunk > 1 && tiles > max_part) return cudaErrorInvalidValue;  // never: chunk = kt above
     g.units = tiles * g.nchunk;
     const int grid = (int)std::min<long long>(g.units, slots);
-#define ELHL_DGEMM(TA_, TB_) dgemm_kernel<TA_, TB_><<<grid, kThreads, 0, st>>>(g)
-    if (transA && transB) ELHL_DGEMM(true, true);
-    else if (transA) ELHL_DGEMM(true, false);
-    else if (transB) ELHL_DGEMM(false, true);
-    else ELHL_DGEMM(false, false);
-#undef ELHL_DGEMM
+    cudaError_t e = v == 0   ? launch_dgemm<64>(g, transA, transB, grid, st)
+                    : v == 1 ? launch_dgemm<32>(g, transA, transB, grid, st)
+                             : launch_dgemm<16>(g, transA, transB, grid, st);
     count_launch();
-    return cudaGetLastError();
+    return e;
 }
 
 }  // namespace elhl

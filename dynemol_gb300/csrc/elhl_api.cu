@@ -249,7 +249,11 @@ bool chol_inv_fits(int n, int ld, size_t wcap) {
 // An FP64 product of the factorisations: on the tensor cores from exact slices
 // (ozgemm) when tc is set and the product is large enough to fill the GPU, else
 // on the FP64 pipe (dgemm64).
-constexpr int kOzGemmMin = 64;  // one 64 x 64 x 64 tile takes 67 us on one SM's FP64 pipe
+// Below 320 rows the FP64 pipe of all SMs (dgemm64's 16- and 32-row tiles) beats
+// the three launches of a sliced product: the factorisation at N = 3720 took
+// 15.7 ms with the cut at 64 rows, 12.4 at 192, 11.7 at 320, 11.8 at 448 and
+// 12.6 at 640.
+constexpr int kOzGemmMin = 320;
 cudaError_t fgemm(bool tc, int m, int n, int k, double alpha, const double *A, int lda, bool transA, const double *B,
                   int ldb, bool transB, double beta, double *C, int ldc, cudaStream_t st, int tri = 0, int lane = 0) {
     if (tc && m >= kOzGemmMin && n >= kOzGemmMin && k >= kOzGemmMin)

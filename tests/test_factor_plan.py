@@ -6,11 +6,12 @@ GPU run:
   chol_inv_fits): every leaf is a diagonal block of at most 64 rows, the leaves
   tile the matrix, and no off-diagonal block exceeds the ld x N workspace the
   factor allocates; a numpy replay of the same splits reproduces L and L^-1;
-* dgemm64's work units (dynemol_gb300/csrc/dgemm.cu): the k range each (tile,
-  k-chunk) unit reads, for every triangular flag, with the constants read from
-  the source; the replayed masked product must equal the triangular product,
-  the chunks must cover each tile's k tiles exactly once, and every partial
-  tile must have its slot in the workspace."""
+* dgemm64's work units (dynemol_gb300/csrc/dgemm.cu): the output tile size it
+  picks (64, 32 or 16 rows) and the k range each (tile, k-chunk) unit reads, for
+  every tile size and triangular flag, with the constants read from the source;
+  the replayed masked product must equal the triangular product, the chunks
+  must cover each tile's k tiles exactly once, and every partial tile must have
+  its slot in the workspace."""
 
 import os
 import re
@@ -31,9 +32,11 @@ def _const(src, name):
     return int(m.group(1))
 
 
-BM, BN, BK = _const(DG, "kBM"), _const(DG, "kBN"), _const(DG, "kBK")
+MAX_TILE, BK = _const(DG, "kMaxTile"), _const(DG, "kBK")
 MAX_PARTIALS, UNITS_PER_SLOT = _const(DG, "kMaxPartials"), _const(DG, "kUnitsPerSlot")
-SLOTS = 4 * 152  # resident CTAs on a GB300 (4 per SM at 256 threads, 55 registers, 33 KB)
+# resident CTAs on a GB300 (152 SMs) for 64-, 32- and 16-row tiles: 3 per SM at 256
+# threads and 64-68 registers, 8 per SM at 32 registers and 9-17 KB
+SLOTS = {64: 3 * 152, 32: 8 * 152, 16: 8 * 152}
 TRI_A, TRI_B, TRI_BT, TRI_LC, TRI_AT = (_const(HDR, n) for n in ("kTriA", "kTriB", "kTriBt", "kTriLowerC", "kTriAt"))
 
 
@@ -106,25 +109,40 @@ def test_plan_computes_the_factors(n):
     assert np.abs(G2 - np.linalg.inv(L)).max() < 1e-12
 
 
-def _chunking(tiles, k, slots=SLOTS):
+def _select(m, n, k):
+    """dgemm64's tile size: the largest at most twice the narrow side whose (tile,
+    k tile) units number at least half of kUnitsPerSlot per resident CTA, else 16
+    rows (dgemm.cu, host side)."""
+    assert "if (bm <= 2 * std::min(m, n) && 2 * units >= (long long)kUnitsPerSlot * g_slots[v]) break;" in DG
+    kt = max(1, (k + BK - 1) // BK)
+    for v, bm in enumerate((64, 32)):
+        units = ((m + bm - 1) // bm) * ((n + bm - 1) // bm) * kt
+        if bm <= 2 * min(m, n) and 2 * units >= UNITS_PER_SLOT * SLOTS[bm]:
+            return bm
+    return 16
+
+
+def _chunking(tiles, k, slots, bm):
     """dgemm64's k tiles per work unit and units per tile (dgemm.cu, host side)."""
+    max_part = MAX_PARTIALS * (MAX_TILE // bm) ** 2  # partial tiles of bm x bm in the workspace
     kt = max(1, (k + BK - 1) // BK)
     chunk = (tiles * kt + UNITS_PER_SLOT * slots - 1) // (UNITS_PER_SLOT * slots)
     chunk = max(1, min(chunk, kt))
-    while chunk < kt and tiles * ((kt + chunk - 1) // chunk) > MAX_PARTIALS:
+    while chunk < kt and tiles * ((kt + chunk - 1) // chunk) > max_part:
         chunk *= 2
     chunk = min(chunk, kt)
     nchunk = (kt + chunk - 1) // chunk
-    assert nchunk == 1 or tiles * nchunk <= MAX_PARTIALS
-    return chunk, nchunk
+    assert nchunk == 1 or tiles * nchunk <= max_part
+    return chunk, nchunk, max_part
 
 
-def _dgemm_replay(m, n, k, A, B, ta, tb, tri, slots=SLOTS):
+def _dgemm_replay(m, n, k, A, B, ta, tb, tri, bm, slots):
     """C = op(A) op(B) accumulated unit by unit over the k ranges the kernel reads."""
+    BM = BN = bm
     opA = A.T if ta else A
     opB = B.T if tb else B
     gx, gy = (m + BM - 1) // BM, (n + BN - 1) // BN
-    chunk, nchunk = _chunking(gx * gy, k, slots)
+    chunk, nchunk, max_part = _chunking(gx * gy, k, slots, bm)
     C = np.zeros((m, n))
     seen = set()
     for u in range(gx * gy * nchunk):
@@ -148,7 +166,8 @@ def _dgemm_replay(m, n, k, A, B, ta, tb, tri, slots=SLOTS):
         nch = max(1, (nkt + chunk - 1) // chunk)
         if ch >= nch:
             continue
-        assert nch == 1 or (by * gx + bx) * nchunk + ch < MAX_PARTIALS  # partial slot in the workspace
+        assert nch == 1 or (by * gx + bx) * nchunk + ch < max_part  # partial slot in the workspace
+        assert nch == 1 or by * gx + bx < MAX_PARTIALS * 16  # arrival counter of the tile
         kt0, kt1 = ch * chunk, min(nkt, ch * chunk + chunk)
         lo, hi = klo + kt0 * BK, min(khi, klo + kt1 * BK)
         for k0 in range(lo, hi, BK):
@@ -177,7 +196,8 @@ def _dgemm_replay(m, n, k, A, B, ta, tb, tri, slots=SLOTS):
 @pytest.mark.parametrize("m,n,k", [(200, 200, 200), (130, 70, 130), (64, 2, 64), (3, 5, 7), (190, 190, 61),
                                    (700, 640, 900)])
 @pytest.mark.parametrize("case", ["none", "A", "At", "B", "Bt", "Bt_lowerC"])
-def test_dgemm_tiles_cover_the_triangular_products(m, n, k, case):
+@pytest.mark.parametrize("bm", [64, 32, 16])
+def test_dgemm_tiles_cover_the_triangular_products(m, n, k, case, bm):
     rng = np.random.default_rng(m * 7 + n + k)
     ta = case == "At"
     tb = case.startswith("Bt")
@@ -198,7 +218,7 @@ def test_dgemm_tiles_cover_the_triangular_products(m, n, k, case):
         ref_b = np.triu(opB)
     else:
         ref_b = opB
-    C = _dgemm_replay(m, n, k, A, B, ta, tb, tri, slots=8)  # few slots: many chunks per tile
+    C = _dgemm_replay(m, n, k, A, B, ta, tb, tri, bm, slots=8)  # few slots: many chunks per tile
     ref = ref_a @ ref_b
     if tri & TRI_LC:  # only tiles reaching the diagonal are written; compare the lower triangle
         mask = np.tril(np.ones((m, n), bool))
@@ -264,7 +284,20 @@ def test_windowed_rows_cover_the_matrix_once(n, mg, c2, krt):
         assert (count == 1).all(), (n, mg, row0, row1)
 
 
-@pytest.mark.parametrize("tiles,k", [(484, 1408), (841, 1920), (16384, 8192), (4, 64), (64, 480), (3000, 16384)])
-def test_dgemm_chunking_bounds(tiles, k):
-    chunk, nchunk = _chunking(tiles, k)
-    assert chunk >= 1 and nchunk >= 1 and (nchunk == 1 or tiles * nchunk <= MAX_PARTIALS)
+@pytest.mark.parametrize("tiles,k", [(484, 1408), (841, 1920), (16384, 8192), (4, 64), (64, 480), (3000, 16384),
+                                     (65536, 4096)])
+@pytest.mark.parametrize("bm", [64, 32, 16])
+def test_dgemm_chunking_bounds(tiles, k, bm):
+    chunk, nchunk, max_part = _chunking(tiles, k, SLOTS[bm], bm)
+    assert chunk >= 1 and nchunk >= 1 and (nchunk == 1 or tiles * nchunk <= max_part)
+
+
+@pytest.mark.parametrize("m,n,k,bm", [(64, 64, 64, 16), (128, 128, 128, 16), (256, 256, 256, 16), (512, 512, 512, 64),
+                                      (3720, 3720, 3720, 64), (3720, 2, 3720, 16), (1920, 24, 1920, 32),
+                                      (3720, 40, 3720, 64)])
+def test_dgemm_tile_choice(m, n, k, bm):
+    """Small products take small tiles so that their units reach most SMs."""
+    assert _select(m, n, k) == bm
+    gx, gy = (m + bm - 1) // bm, (n + bm - 1) // bm
+    _, nchunk, _ = _chunking(gx * gy, k, SLOTS[bm], bm)
+    assert gx * gy * nchunk >= min(152, gx * gy * max(1, (k + BK - 1) // BK))

@@ -233,7 +233,7 @@ def test_df64_cluster_vs_exact(elhl, oracle_mod):
 def test_rebuild_factor_and_inverse(elhl, prec_name, tol, n_atoms, nao):
     """The moving-nuclei rebuild's factorisations: FP64 the recursive
     Cholesky-with-inverse on the FP64 pipe, OZ64 the same recursion with its
-    products of 64 or more rows on the tensor cores (exact slices), DF64 and
+    products of 320 or more rows on the tensor cores (exact slices), DF64 and
     FP32 the double-float Cholesky-with-inverse.
     N = 62 is one leaf, 199 and 465 stay below the 512-row bottom-up block, 1860
     has a short last 64-row leaf and short pairs in the batched levels.
