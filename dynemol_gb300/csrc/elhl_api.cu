@@ -855,10 +855,10 @@ __global__ void mirror_lower_kernel(double *A, int n, int ld) {
 
 // H~ = G h G^T with G = L^-1 (lower, zero upper triangle): W = G h, then the
 // lower triangle of W G^T (symmetric result, N^3 + N^3/2 flops), mirrored.
-int form_htilde(ChebState &cs, const double *G, const double *h, int ld, double *W) {
+// tc: products of 320 or more rows on the tensor cores from exact slices.
+int form_htilde(ChebState &cs, const double *G, const double *h, int ld, double *W, bool tc) {
     cudaStream_t st = g_ctx.stream;
     const int n = cs.N;
-    const bool tc = cs.oz != nullptr;  // ELHL_PREC_OZ64: large products on the tensor cores
     CU_TRY(fgemm(tc, n, n, n, 1.0, G, ld, false, h, ld, false, 0.0, W, ld, st, kTriA));
     CU_TRY(fgemm(tc, n, n, n, 1.0, W, ld, false, G, ld, true, 0.0, cs.Ht, cs.ld, st, kTriBt | kTriLowerC));
     mirror_lower_kernel<<<dim3((n + 127) / 128, n), 128, 0, st>>>(cs.Ht, n, cs.ld);
@@ -1087,84 +1087,6 @@ __global__ void convert_kernel(const double *__restrict__ src, T *__restrict__ d
         else v = (i >= j) ? src[(size_t)j * ld + i] : 0.0;            // src(i, j), i >= j
     }
     dst[(size_t)j * ld + i] = (T)v;
-}
-
-// Cholesky factor and its inverse together, in place, for the DF64 rebuild:
-// A (n x n, lower) <- L, G <- L^-1, all three matrices (and the workspace W)
-// held as DF64 pairs and every product in double-float arithmetic on the FP32
-// pipes (dfgemm, triangular operands at half cost):
-//   L11, G11 = chol_inv(A11);   L21 = A21 G11^T;   A22 -= L21 L21^T;
-//   L22, G22 = chol_inv(A22);   G21 = -G22 (L21 G11),
-// N^3/3 + N^3/3 flops, with 64-row diagonal blocks as leaves (leaf_chol_inv_df).
-// The upper triangles of A and G are left undefined.
-int chol_inv_df(float2 *A, float2 *G, int n, int ld, int row0, float2 *W, int *info) {
-    cudaStream_t st = g_ctx.stream;
-    const int leaf = leaf_rows();
-    if (n <= leaf) {
-        CU_TRY(leaf_chol_inv_df(A, G, n, ld, row0, info, st));
-        return ELHL_OK;
-    }
-    const int n1 = round_up(n / 2, leaf), n2 = n - n1;
-    float2 *A21 = A + n1, *A22 = A + (size_t)n1 * ld + n1;
-    float2 *G21 = G + n1, *G22 = G + (size_t)n1 * ld + n1;
-    if (int rc = chol_inv_df(A, G, n1, ld, row0, W, info)) return rc;
-    CU_TRY(cudaMemcpy2DAsync(W, ld * sizeof(float2), A21, ld * sizeof(float2), n2 * sizeof(float2), n1,
-                             cudaMemcpyDeviceToDevice, st));
-    CU_TRY(dfgemm(n2, n1, n1, 1.0, W, ld, G, ld, 0.0, A21, ld, st, true, kTriBt));              // L21
-    CU_TRY(dfgemm(n2, n2, n1, -1.0, A21, ld, A21, ld, 1.0, A22, ld, st, true, kTriLowerC));    // Schur
-    if (int rc = chol_inv_df(A22, G22, n2, ld, row0 + n1, W, info)) return rc;
-    CU_TRY(dfgemm(n2, n1, n1, 1.0, A21, ld, G, ld, 0.0, W, ld, st, false, kTriB));             // L21 G11
-    CU_TRY(dfgemm(n2, n1, n2, -1.0, G22, ld, W, ld, 0.0, G21, ld, st, false, kTriA));          // G21
-    return ELHL_OK;
-}
-
-// L = chol(S) in Lfac and G = L^-1 in G, both FP64 on return, by chol_inv_df
-// on DF64 pairs converted in place; W: ld x N workspace (held as pairs).  The
-// blocks of the recursion are checked against W before the first launch.
-int chol_inv_pairs(ChebState &cs, double *Lfac, double *G, int *info, double *W) {
-    cudaStream_t st = g_ctx.stream;
-    if (!chol_inv_fits(cs.N, cs.ld, (size_t)cs.ld * cs.N)) return ELHL_ERR_OOM;
-    CU_TRY(cudaMemsetAsync(info, 0, sizeof(int), st));
-    CU_TRY(df_convert(Lfac, cs.N, cs.N, cs.ld, true, st));
-    if (int rc = chol_inv_df(reinterpret_cast<float2 *>(Lfac), reinterpret_cast<float2 *>(G), cs.N, cs.ld, 0,
-                             reinterpret_cast<float2 *>(W), info))
-        return rc;
-    CU_TRY(df_convert(Lfac, cs.N, cs.N, cs.ld, false, st));
-    CU_TRY(df_convert(G, cs.N, cs.N, cs.ld, false, st));
-    return ELHL_OK;
-}
-
-// Fixed-nuclei set-up of the reduced precisions (FP32, BF16X3), whose operator
-// is rounded to FP32 anyway: L, G = L^-1 and H~ = G h G^T (lower triangle,
-// mirrored) all in double-float pairs on the FP32 pipes (about 1e-14 relative,
-// 2.4x the FP64 pipe's rate), converted back to FP64 with zero upper triangles.
-// Lfac holds S on entry; Ht receives H~; W: ld x N workspace.
-int chol_htilde_pairs(ChebState &cs, double *Lfac, double *G, const double *h, int *info, double *W) {
-    cudaStream_t st = g_ctx.stream;
-    const int n = cs.N, ld = cs.ld;
-    if (!chol_inv_fits(cs.N, cs.ld, (size_t)cs.ld * cs.N)) return ELHL_ERR_OOM;
-    CU_TRY(cudaMemsetAsync(info, 0, sizeof(int), st));
-    CU_TRY(df_convert(Lfac, n, n, ld, true, st));
-    float2 *Lp = reinterpret_cast<float2 *>(Lfac), *Gp = reinterpret_cast<float2 *>(G);
-    float2 *Wp = reinterpret_cast<float2 *>(W), *Hp = reinterpret_cast<float2 *>(cs.Ht);
-    if (int rc = chol_inv_df(Lp, Gp, n, ld, 0, Wp, info)) return rc;
-    CU_TRY(cudaMemcpy2DAsync(cs.Ht, ld * sizeof(double), h, ld * sizeof(double), n * sizeof(double), n,
-                             cudaMemcpyDeviceToDevice, st));
-    CU_TRY(df_convert(cs.Ht, n, n, ld, true, st));
-    CU_TRY(dfgemm(n, n, n, 1.0, Gp, ld, Hp, ld, 0.0, Wp, ld, st, false, kTriA));                // G h
-    CU_TRY(dfgemm(n, n, n, 1.0, Wp, ld, Gp, ld, 0.0, Hp, ld, st, true, kTriBt | kTriLowerC));   // (G h) G^T
-    CU_TRY(df_convert(cs.Ht, n, n, ld, false, st));
-    CU_TRY(df_convert(Lfac, n, n, ld, false, st));
-    CU_TRY(df_convert(G, n, n, ld, false, st));
-    const dim3 grid((ld + 127) / 128, n);
-    mirror_lower_kernel<<<grid, 128, 0, st>>>(cs.Ht, n, ld);
-    count_launch();
-    lower_only_kernel<<<grid, 128, 0, st>>>(Lfac, n, ld);
-    count_launch();
-    lower_only_kernel<<<grid, 128, 0, st>>>(G, n, ld);
-    count_launch();
-    CU_TRY(cudaGetLastError());
-    return ELHL_OK;
 }
 
 // Read-out matrices in FP64 for the reduced precisions too: the populations
@@ -2218,12 +2140,10 @@ int rebuild(elhl_traj *tr, const double *d_coords) {
 int cheb_rebuild_operator(elhl_traj *tr, bool implicit = false) {
     cudaStream_t st = g_ctx.stream;
     ChebState &cs = tr->cs;
-    // S = L L^T and G = L^-1 in one recursion: FP64 for FP64 propagation (and the DF64
-    // fixed-nuclei set-up); double-float pairs (about 1e-14 relative) for the DF64, FP32
-    // and BF16X3 moving-nuclei propagations and, with H~, the FP32 / BF16X3 fixed-nuclei
-    // set-ups, whose own rounding is near 1e-14 or 1e-7.
+    // S = L L^T and G = L^-1 in one recursion, in FP64 for every precision: on the
+    // FP64 pipe for FP64 propagation (the plain FP64 path), with the products of
+    // 320 or more rows exact on the tensor cores for the others (Factor::tc).
     // The implicit operator keeps G in cs.Ht, the explicit one in the factor's G.
-    const bool pairs = implicit && cs.precision != ELHL_PREC_FP64;
     if (implicit && cs.oz) {
         // ELHL_PREC_OZ64: with every product on the tensor cores, forming H~ = G h G^T
         // (1.5 N^3 flops) costs less than the implicit operator's extra phases (2 N^2
@@ -2233,7 +2153,7 @@ int cheb_rebuild_operator(elhl_traj *tr, bool implicit = false) {
         CU_TRY(cudaEventRecord(g_ctx.ev[5], st));
         if (int rc = tr->fac.check_info(false)) return rc;
         cs.implicit = false;
-        if (int rc = form_htilde(cs, tr->fac.G, tr->h, tr->ld, tr->fac.W)) return rc;
+        if (int rc = form_htilde(cs, tr->fac.G, tr->h, tr->ld, tr->fac.W, tr->fac.tc)) return rc;
         CU_TRY(cudaEventRecord(g_ctx.ev[6], st));
         if (int rc = lanczos_bounds(cs, 40)) return rc;
         if (int rc = cheb_prepare(cs, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol)) return rc;
@@ -2245,28 +2165,12 @@ int cheb_rebuild_operator(elhl_traj *tr, bool implicit = false) {
         CU_TRY(cudaGetLastError());
         return ELHL_OK;
     }
-    if (!implicit && reduced_precision(cs.precision)) {
-        CU_TRY(cudaMemcpy2DAsync(tr->fac.L, tr->ld * sizeof(double), tr->S, tr->ld * sizeof(double),
-                                 tr->N * sizeof(double), tr->N, cudaMemcpyDeviceToDevice, st));
-        if (int rc = chol_htilde_pairs(cs, tr->fac.L, tr->fac.G, tr->h, tr->fac.info, tr->fac.W)) return rc;
-        CU_TRY(cudaEventRecord(g_ctx.ev[5], st));
-        if (int rc = tr->fac.check_info(false)) return rc;
-        cs.implicit = false;
-        if (int rc = lanczos_bounds(cs, 40)) return rc;
-        return cheb_prepare(cs, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol);
-    }
-    if (pairs) {
-        CU_TRY(cudaMemcpy2DAsync(tr->fac.L, tr->ld * sizeof(double), tr->S, tr->ld * sizeof(double),
-                                 tr->N * sizeof(double), tr->N, cudaMemcpyDeviceToDevice, st));
-        if (int rc = chol_inv_pairs(cs, tr->fac.L, cs.Ht, tr->fac.info, tr->fac.W)) return rc;
-    } else if (int rc = tr->fac.factor(tr->S, tr->N, implicit ? cs.Ht : nullptr)) {
-        return rc;
-    }
+    if (int rc = tr->fac.factor(tr->S, tr->N, implicit ? cs.Ht : nullptr)) return rc;
     CU_TRY(cudaEventRecord(g_ctx.ev[5], st));
     if (int rc = tr->fac.check_info(false)) return rc;
     if (implicit) return cheb_prepare_implicit(cs, tr->fac.L, tr->h, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol);
     cs.implicit = false;
-    if (int rc = form_htilde(cs, tr->fac.G, tr->h, tr->ld, tr->fac.W)) return rc;
+    if (int rc = form_htilde(cs, tr->fac.G, tr->h, tr->ld, tr->fac.W, tr->fac.tc)) return rc;
     if (int rc = lanczos_bounds(cs, 40)) return rc;
     return cheb_prepare(cs, tr->cfg.dt * tr->cfg.frame_step, tr->cfg.cheb_tol);
 }
@@ -3015,10 +2919,10 @@ int elhl_traj_create(const elhl_basis_desc *basis, const double *coords, const e
     if (!rc && !tr->cheb()) rc = tr->fac.check_info();  // the Chebyshev set-up factors S below
     if (!rc && tr->cheb()) {
         const bool oz = tr->cfg.precision == ELHL_PREC_OZ64;  // FP64 state, tensor-core propagation
+        tr->fac.tc = tr->cfg.precision != ELHL_PREC_FP64;      // FP64 factorisation, large products sliced
         rc = tr->cs.alloc(tr->N, tr->cfg.ncols, oz ? ELHL_PREC_FP64 : tr->cfg.precision);
         if (!rc && oz) {
             int grid = 0;
-            tr->fac.tc = true;
             tr->cs.oz = new OzRes();
             rc = cheb_grid_size(&grid) ? ELHL_ERR_CUDA : tr->cs.oz->init(tr->N, tr->ld, grid);
         }
@@ -3700,8 +3604,12 @@ struct elhl_server {
 
 static double request_bytes(const elhl_traj_config &cfg, int nao, int P) {
     const double ld = (double)round_up(nao, 32), tsz = wide_storage(cfg.precision) ? 8.0 : 4.0;
-    // set-up peak: S, h, H~, L, G (FP64) + Hs + read-out matrices (FP64) + vectors
-    return ld * nao * (5 * 8.0 + tsz + 2 * 8.0) + ld * cfg.ncols / cfg.nparticles * P * (3 * 2 * tsz + 2 * 16.0) + 1e6;
+    // set-up peak: S, h, H~, L, G (FP64) + Hs + read-out matrices (FP64) + vectors, and
+    // for the sliced set-up products (every precision but FP64) the slices of both
+    // operands of an N x N x N product: 2 x 7 BF16 slices of N^2 elements
+    const double slices = (cfg.precision != ELHL_PREC_FP64 && nao >= 320) ? 28.0 * nao * nao : 0.0;
+    return ld * nao * (5 * 8.0 + tsz + 2 * 8.0) + ld * cfg.ncols / cfg.nparticles * P * (3 * 2 * tsz + 2 * 16.0) +
+           slices + 1e6;
 }
 
 static int server_admit(elhl_server *sv, ServerRequest *r) {

@@ -208,18 +208,13 @@ void oz_schedule(int n, int grid, std::vector<OzSeg> &segs, std::vector<int> &se
                  std::vector<int> &part_count);
 cudaError_t launch_oz_cheb(const OzLaunch &L, const __nv_bfloat16 *hs_slices, int grid, cudaStream_t st);
 
-// C = alpha A op(B) + beta C in double-float arithmetic on the FP32 pipes (dfgemm.cu),
-// column-major operands stored as DF64 pairs (float2 = hi + lo), op(B) = B^T
-// when transB.  `tri` marks lower-
-// triangular operands (kTriA: A; kTriB: B; kTriBt: op(B) = B^T of a lower B)
-// and kTriLowerC a symmetric update that writes only the tiles on or below
-// the diagonal.
+// Triangular operands of the FP64 products (dgemm64, ozgemm), flags of `tri`:
+// kTriA: op(A) = A lower triangular; kTriAt: op(A) = A^T of a lower A; kTriB:
+// op(B) = B lower; kTriBt: op(B) = B^T of a lower B; kTriLowerC: a symmetric
+// update that writes only the tiles on or below the diagonal.
 constexpr int kTriA = 1, kTriB = 2, kTriBt = 4, kTriLowerC = 8, kTriAt = 16;
-cudaError_t dfgemm(int m, int n, int k, double alpha, const float2 *A, int lda, const float2 *B, int ldb, double beta,
-                   float2 *C, int ldc, cudaStream_t st, bool transB = false, int tri = 0);
 // C = alpha op(A) op(B) + beta C in FP64 on the FP64 pipe (dgemm.cu), op = the
-// transpose when transA / transB; `tri` as for dfgemm, plus kTriAt: op(A) = A^T
-// of a lower A.  lane 0 or 1: products that run concurrently (on two streams)
+// transpose when transA / transB, `tri` the triangular flags above.  lane 0 or 1: products that run concurrently (on two streams)
 // use different lanes, each with its own scheduler and workspace; lane 1 takes
 // three quarters of the resident CTA slots.
 cudaError_t dgemm64(int m, int n, int k, double alpha, const double *A, int lda, bool transA, const double *B, int ldb,
@@ -232,18 +227,11 @@ cudaError_t ozgemm(int m, int n, int k, double alpha, const double *A, int lda, 
                    bool transB, double beta, double *C, int ldc, cudaStream_t st, int tri = 0, int lane = 0);
 int *ozgemm_error(int lane);
 size_t ozgemm_smem_bytes();
-// rows x n block of an FP64 matrix (leading dimension ld) to DF64 pairs in
-// place (to_pairs) or back
-cudaError_t df_convert(double *x, int rows, int n, int ld, bool to_pairs, cudaStream_t st);
-
-// Diagonal-block leaves of the recursive factorisations (factor.cu), in
-// shared memory, blocks of leaf_rows() = 64 rows:
-//   leaf_chol_inv_df: A (nb x nb, nb <= 64, DF64 pairs) <- chol(A), G <- its
-//                     inverse; a non-positive pivot sets *info (if still 0)
-//                     to row0 + column + 1;
-//   leaf_chol_inv64:  the same in FP64.
+// Diagonal-block leaves of the recursive factorisation (factor.cu), in shared
+// memory, blocks of leaf_rows() = 64 rows: leaf_chol_inv64: A (nb x nb,
+// nb <= 64) <- chol(A), G <- its inverse, in FP64; a non-positive pivot sets
+// *info (if still 0) to row0 + column + 1.
 int leaf_rows();
-cudaError_t leaf_chol_inv_df(float2 *A, float2 *G, int nb, int ld, int row0, int *info, cudaStream_t st);
 cudaError_t leaf_chol_inv64(double *A, double *G, int nb, int ld, int row0, int *info, cudaStream_t st);
 
 int bessel_j_sequence(double beta, int kmax, double *J);

@@ -1,24 +1,21 @@
 // Dense Cholesky-with-inverse of one diagonal block of at most kLeaf = 64
-// rows, one CTA of 256 threads, entirely in shared memory: the leaves of the
-// rebuild's recursive factorisations (S = L L^T with G = L^-1).
-//   leaf_chol_inv_df_kernel:  in DF64 pairs on the FP32 pipes (the DF64,
-//                             FP32 and BF16X3 moving-nuclei rebuilds);
-//   leaf_chol_inv64_kernel:   in FP64 (the FP64 rebuild, every fixed-nuclei
-//                             set-up and the drop-in's H' = S^-1 h).
-// Both are blocked by 8 columns so that few steps wait at a block-wide
-// barrier; library triangular kernels at these sizes (cuSOLVER trtri on 256
-// rows, cuBLAS DTRMM/DTRSM panels) ran on a handful of CTAs for 65-106 us per
-// call.
-#include "df64.cuh"
+// rows in FP64, one CTA of 256 threads, entirely in shared memory: the leaves
+// of the rebuild's recursive factorisation (S = L L^T with G = L^-1) for every
+// precision, and of the drop-in's H' = S^-1 h.  Blocked by 8 columns so that
+// few steps wait at a block-wide barrier; library triangular kernels at these
+// sizes (cuSOLVER trtri on 256 rows, cuBLAS DTRMM/DTRSM panels) ran on a
+// handful of CTAs for 65-106 us per call.
 #include "elhl_internal.cuh"
 
 namespace elhl {
 namespace {
 
 constexpr int kLeaf = 64, kPitch = kLeaf + 1, kThreads = 256;
+constexpr int kDiag = 8, kPPitch = kDiag + 1;
+
 // L = chol(A) in place and G = L^-1 for the nb x nb diagonal block at offset r
-// (global row of its first column, for the status word), A and G as DF64
-// pairs, blocked so that few steps wait at a block-wide barrier:
+// (global row of its first column, for the status word), pivots' 1/sqrt by
+// rsqrt, blocked so that few steps wait at a block-wide barrier:
 //   Cholesky, for each 8-column block b (rows past nb padded with identity):
 //     (1) warp 0 factors and inverts the 8 x 8 diagonal block (column sweeps
 //         under __syncwarp only);
@@ -27,149 +24,6 @@ constexpr int kLeaf = 64, kPitch = kLeaf + 1, kThreads = 256;
 //   inverse by doubling, s = 8, 16, 32: G21 = -G22 (L21 G11) for all pairs.
 // About 30 barriers instead of one per column.  A non-positive pivot sets
 // *info to its 1-based global column (the first one found) and the
-// factorisation carries on with a zero scale, so the launch always ends.
-constexpr int kDiag = 8, kPPitch = kDiag + 1;
-constexpr size_t kLeafDfSmem =
-    (size_t)(2 * kLeaf * kPitch + kLeaf * kPPitch + 32 * kLeaf + 2 * kDiag) * sizeof(float2);
-
-__global__ void __launch_bounds__(kThreads) leaf_chol_inv_df_kernel(float2 *A, float2 *G, int nb, int ld, int r,
-                                                                    int *info) {
-    extern __shared__ double smem[];
-    float2 *As = reinterpret_cast<float2 *>(smem);  // [64][kPitch]: A, then L
-    float2 *Gs = As + kLeaf * kPitch;               // [64][kPitch]: G
-    float2 *P = Gs + kLeaf * kPitch;                // [64][kPPitch]: panel of the current block
-    float2 *Wm = P + kLeaf * kPPitch;               // [32 * 64]: products of a doubling level
-    float2 *rb = Wm + 32 * kLeaf, *sb = rb + kDiag;  // 1/L(k, k) and its square, current block
-    const int tid = threadIdx.x, lane = tid % 32, warp = tid / 32;
-    const float2 zero = make_float2(0.f, 0.f), one = make_float2(1.f, 0.f);
-    for (int e = tid; e < kLeaf * kLeaf; e += kThreads) {
-        const int i = e % kLeaf, j = e / kLeaf;
-        float2 v = zero;
-        if (i < nb && j < nb) {
-            if (i >= j) v = A[(size_t)j * ld + i];
-        } else if (i == j) {
-            v = one;
-        }
-        As[i * kPitch + j] = v;
-        Gs[i * kPitch + j] = zero;
-    }
-    __syncthreads();
-    for (int b0 = 0; b0 < kLeaf; b0 += kDiag) {
-        float2 *Ab = As + b0 * kPitch + b0, *Gb = Gs + b0 * kPitch + b0;
-        if (warp == 0) {  // (1)
-            for (int kk = 0; kk < kDiag; ++kk) {
-                __syncwarp();
-                const float2 d = Ab[kk * kPitch + kk];
-                const bool ok = d.x > 0.f;
-                const float2 rr = ok ? df_rsqrt(d) : zero, sq = df_mul(rr, rr);
-                if (lane == 0) {
-                    rb[kk] = rr;
-                    sb[kk] = sq;
-                    if (!ok && b0 + kk < nb) atomicCAS(info, 0, r + b0 + kk + 1);
-                }
-                for (int e = lane; e < kDiag * kDiag; e += 32) {
-                    const int i = e / kDiag, j = e % kDiag;
-                    if (j > kk && i >= j) {
-                        float2 a = Ab[i * kPitch + j];
-                        const float2 l = df_mul(Ab[i * kPitch + kk], sq), c = Ab[j * kPitch + kk];
-                        df_fma(a.x, a.y, -l.x, -l.y, c.x, c.y);
-                        Ab[i * kPitch + j] = df_renorm(a.x, a.y);
-                    }
-                }
-            }
-            for (int e = lane; e < kDiag * kDiag; e += 32) {
-                const int i = e / kDiag, j = e % kDiag;
-                Gb[i * kPitch + j] = i == j ? one : zero;
-            }
-            for (int kk = 0; kk < kDiag - 1; ++kk) {
-                __syncwarp();
-                for (int e = lane; e < kDiag * kDiag; e += 32) {
-                    const int i = e / kDiag, j = e % kDiag;
-                    if (i > kk && j <= kk) {
-                        const float2 m = df_mul(Ab[i * kPitch + kk], sb[kk]), xk = Gb[kk * kPitch + j];
-                        float2 x = Gb[i * kPitch + j];
-                        df_fma(x.x, x.y, -m.x, -m.y, xk.x, xk.y);
-                        Gb[i * kPitch + j] = df_renorm(x.x, x.y);
-                    }
-                }
-            }
-            __syncwarp();
-            for (int e = lane; e < kDiag * kDiag; e += 32) {  // G = x_ij / L(i, i), L = a_ij / L(j, j)
-                const int i = e / kDiag, j = e % kDiag;
-                if (i >= j) {
-                    Gb[i * kPitch + j] = df_mul(Gb[i * kPitch + j], rb[i]);
-                    Ab[i * kPitch + j] = df_mul(Ab[i * kPitch + j], rb[j]);
-                }
-            }
-        }
-        __syncthreads();
-        const int r0 = b0 + kDiag, nr = kLeaf - r0;
-        for (int e = tid; e < nr * kDiag; e += kThreads) {  // (2) L(i, b0 + j) = sum_t A(i, b0 + t) G_bb(j, t)
-            const int i = r0 + e / kDiag, j = e % kDiag;
-            float h = 0.f, l = 0.f;
-            for (int t = 0; t <= j; ++t) {
-                const float2 a = As[i * kPitch + b0 + t], g = Gb[j * kPitch + t];
-                df_fma(h, l, a.x, a.y, g.x, g.y);
-            }
-            P[i * kPPitch + j] = df_renorm(h, l);
-        }
-        __syncthreads();
-        for (int e = tid; e < nr * kDiag; e += kThreads) {
-            const int i = r0 + e / kDiag, j = e % kDiag;
-            As[i * kPitch + b0 + j] = P[i * kPPitch + j];
-        }
-        for (int e = tid; e < kLeaf * kLeaf; e += kThreads) {  // (3), a warp on one row
-            const int i = e / kLeaf, j = e % kLeaf;
-            if (j < r0 || j > i) continue;
-            float2 a = As[i * kPitch + j];
-#pragma unroll
-            for (int t = 0; t < kDiag; ++t) {
-                const float2 p = P[i * kPPitch + t], q = P[j * kPPitch + t];
-                df_fma(a.x, a.y, -p.x, -p.y, q.x, q.y);
-            }
-            As[i * kPitch + j] = df_renorm(a.x, a.y);
-        }
-        __syncthreads();
-    }
-    for (int s = kDiag; s < kLeaf; s *= 2) {  // inverse by doubling
-        const int per = s * s, count = (kLeaf / (2 * s)) * per;
-        for (int e = tid; e < count; e += kThreads) {  // W = L21 G11 (G11 lower: t >= j)
-            const int o = 2 * s * (e / per), i = (e % per) / s, j = e % s;
-            float h = 0.f, l = 0.f;
-            for (int t = j; t < s; ++t) {
-                const float2 a = As[(o + s + i) * kPitch + o + t], g = Gs[(o + t) * kPitch + o + j];
-                df_fma(h, l, a.x, a.y, g.x, g.y);
-            }
-            Wm[e] = df_renorm(h, l);
-        }
-        __syncthreads();
-        for (int e = tid; e < count; e += kThreads) {  // G21 = -G22 W (G22 lower: t <= i)
-            const int o = 2 * s * (e / per), i = (e % per) / s, j = e % s;
-            const float2 *W = Wm + (e / per) * per;
-            float h = 0.f, l = 0.f;
-            for (int t = 0; t <= i; ++t) {
-                const float2 g = Gs[(o + s + i) * kPitch + o + s + t], w = W[t * s + j];
-                df_fma(h, l, g.x, g.y, w.x, w.y);
-            }
-            const float2 v = df_renorm(h, l);
-            Gs[(o + s + i) * kPitch + o + j] = make_float2(-v.x, -v.y);
-        }
-        __syncthreads();
-    }
-    for (int e = tid; e < kLeaf * kLeaf; e += kThreads) {
-        const int i = e % kLeaf, j = e / kLeaf;
-        if (i < nb && j < nb) {
-            const bool low = i >= j;
-            G[(size_t)j * ld + i] = low ? Gs[i * kPitch + j] : zero;
-            A[(size_t)j * ld + i] = low ? As[i * kPitch + j] : zero;
-        }
-    }
-}
-
-// The same blocked Cholesky-with-inverse in FP64 for the FP64 rebuild: L =
-// chol(A) in place and G = L^-1 for the nb x nb diagonal block at offset r,
-// pivots' 1/sqrt by rsqrt.  Steps as leaf_chol_inv_df_kernel; a non-positive
-// pivot sets *info to its 1-based global column (the first one found) and the
 // factorisation carries on with a zero scale, so the launch always ends.
 constexpr size_t kLeaf64Smem = (size_t)(2 * kLeaf * kPitch + kLeaf * kPPitch + 32 * kLeaf + 2 * kDiag) * sizeof(double);
 
@@ -299,20 +153,6 @@ cudaError_t leaf_chol_inv64(double *A, double *G, int nb, int ld, int row0, int 
     }
     if (nb <= 0 || nb > kLeaf) return cudaErrorInvalidValue;
     leaf_chol_inv64_kernel<<<1, kThreads, kLeaf64Smem, st>>>(A, G, nb, ld, row0, info);
-    count_launch();
-    return cudaGetLastError();
-}
-
-cudaError_t leaf_chol_inv_df(float2 *A, float2 *G, int nb, int ld, int row0, int *info, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(leaf_chol_inv_df_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kLeafDfSmem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
-    if (nb <= 0 || nb > kLeaf) return cudaErrorInvalidValue;
-    leaf_chol_inv_df_kernel<<<1, kThreads, kLeafDfSmem, st>>>(A, G, nb, ld, row0, info);
     count_launch();
     return cudaGetLastError();
 }

@@ -1,9 +1,8 @@
 """Host replays of the rebuild's index arithmetic, checked on the CPU before any
 GPU run:
 
-* the block plan of the recursive Cholesky-with-inverse (chol_inv64 and
-  chol_inv_df in dynemol_gb300/csrc/elhl_api.cu, both checked up front by
-  chol_inv_fits): every leaf is a diagonal block of at most 64 rows, the leaves
+* the block plan of the recursive Cholesky-with-inverse (chol_inv64 in
+  dynemol_gb300/csrc/elhl_api.cu, checked up front by chol_inv_fits): every leaf is a diagonal block of at most 64 rows, the leaves
   tile the matrix, and no off-diagonal block exceeds the ld x N workspace the
   factor allocates; a numpy replay of the same splits reproduces L and L^-1;
 * dgemm64's work units (dynemol_gb300/csrc/dgemm.cu): the output tile size it
@@ -65,7 +64,6 @@ def chol_plan(n, ld):
 @pytest.mark.parametrize("n", list(range(1, 600)) + list(range(600, 4097, 7)) + [2170, 3720, 8192, 16384])
 def test_plan_fits_the_workspace(n):
     assert "chol_inv_fits(n, ld, (size_t)ld * N)" in API  # the FP64 factor's check, workspace ld x N
-    assert "chol_inv_fits(cs.N, cs.ld, (size_t)cs.ld * cs.N)" in API  # the double-float one
     ld = ru(n, 32)
     need, leaves = chol_plan(n, ld)
     assert need <= ld * n, (n, need)
