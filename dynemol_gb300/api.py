@@ -67,7 +67,8 @@ class TrajStats(ctypes.Structure):
                 ("status", ctypes.c_int), ("prop_ms", ctypes.c_double), ("rebuild_ms", ctypes.c_double),
                 ("prop_launches", ctypes.c_int), ("rebuild_count", ctypes.c_int), ("tile_cols", ctypes.c_int),
                 ("phases", ctypes.c_int), ("sh_ms", ctypes.c_double), ("factor_ms", ctypes.c_double),
-                ("inverse_ms", ctypes.c_double), ("cheb_retries", ctypes.c_int), ("norm_drift", ctypes.c_double)]
+                ("inverse_ms", ctypes.c_double), ("cheb_retries", ctypes.c_int), ("norm_drift", ctypes.c_double),
+                ("emin", ctypes.c_double), ("emax", ctypes.c_double)]
 
 
 class Request(ctypes.Structure):

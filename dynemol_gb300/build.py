@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libelhlprop.so")
-SOURCES = ["build_sh.cu", "taylor.cu", "cheb.cu", "chebcoef.cu", "elhl_api.cu", "noalloc.cu", "umma_gemm.cu", "dgemm.cu", "factor.cu", "ozaki.cu", "ozgemm.cu"]
+SOURCES = ["build_sh.cu", "taylor.cu", "cheb.cu", "chebcoef.cu", "elhl_api.cu", "noalloc.cu", "umma_gemm.cu", "dgemm.cu", "factor.cu", "ozaki.cu", "ozgemm.cu", "lanczos.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
          "--expt-relaxed-constexpr", "-diag-suppress", "177"]

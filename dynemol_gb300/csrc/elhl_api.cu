@@ -652,6 +652,7 @@ __global__ void renormalize_kernel(double2 *cols, int n, int m, int P, const dou
 }
 
 // 8-byte storage per real element: FP64, or a DF64 (hi, lo) pair of FP32
+constexpr int kLzPart = 1024;  // per-CTA partial sums of the Lanczos launch: 2 per SM, up to 512 SMs
 inline bool wide_storage(int prec) { return prec == ELHL_PREC_FP64 || prec == ELHL_PREC_DF64; }
 // reduced precision: renormalised every step, GEMM regime possible
 inline bool reduced_precision(int prec) { return prec == ELHL_PREC_FP32 || prec == ELHL_PREC_BF16X3; }
@@ -772,7 +773,7 @@ struct ChebState {
     int coef_cap = 0;
     double emin = 0.0, emax = 0.0, a = 0.0, b = 1.0;
     double2 c0{1.0, 0.0};    // host copy of the order-0 coefficient
-    double *lz = nullptr;    // Lanczos vectors [4][ld]
+    double *lz = nullptr;    // Lanczos vectors [6][ld], partial sums [kLzPart], record [128]
     // implicit operator (geometry changing every step): Ht holds G = L^-1 in FP64,
     // Hs = h/b, A = G and Gt = G^T in the launch precision; no H~ is formed
     bool implicit = false;
@@ -798,7 +799,8 @@ struct ChebState {
         if (int rc = dev_alloc(&acc, (size_t)ld * m)) return rc;
         CU_TRY(cudaMemset(phi, 0, (size_t)ld * m * sizeof(double2)));
         CU_TRY(cudaMemset(acc, 0, (size_t)ld * m * sizeof(double2)));
-        if (int rc = dev_alloc(&lz, (size_t)4 * ld + 128)) return rc;  // 4 vectors + the tridiagonal record
+        // 6 Lanczos vectors, per-CTA partial sums, the tridiagonal record
+        if (int rc = dev_alloc(&lz, (size_t)6 * ld + kLzPart + 128)) return rc;
         if (int rc = dev_alloc(&cscratch, (size_t)2 * m * ld)) return rc;
         if (int rc = dev_alloc(&scale, (size_t)kMaxCols)) return rc;
         if (int rc = dev_alloc(&drift, 1)) return rc;
@@ -867,149 +869,25 @@ int form_htilde(ChebState &cs, const double *G, const double *h, int ld, double 
     return ELHL_OK;
 }
 
-template <typename T>
-__global__ void lanczos_start(T *v, int n) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) v[i] = (T)(1.0 + 0.5 * sin(1.37 * i + 0.2));  // deterministic, every component present
-}
-
-constexpr int kLzBlock = 1024;
-
-// sum over the block in a fixed order (every thread returns it)
-__device__ double lz_block_sum(double x, double *s) {
-    const int t = threadIdx.x;
-    s[t] = x;
-    __syncthreads();
-    for (int o = kLzBlock / 2; o > 0; o >>= 1) {
-        if (t < o) s[t] += s[t + o];
-        __syncthreads();
-    }
-    const double r = s[0];
-    __syncthreads();
-    return r;
-}
-
-// v <- v / |v| (one block; sums in FP64)
-template <typename T>
-__global__ void __launch_bounds__(kLzBlock) lanczos_normalize_kernel(T *v, int n) {
-    __shared__ double s[kLzBlock];
-    double a = 0.0;
-    for (int i = threadIdx.x; i < n; i += kLzBlock) a += (double)v[i] * v[i];
-    const double inv = 1.0 / sqrt(lz_block_sum(a, s));
-    for (int i = threadIdx.x; i < n; i += kLzBlock) v[i] = (T)(v[i] * inv);
-}
-
-// One Lanczos update after w = H v (one block, fixed-order FP64 sums):
-//   alpha_j = w.v, w <- w - alpha_j v - beta_{j-1} vp, beta_j = |w|,
-//   vp <- v, v <- w / beta_j.
-// rec[0..k) alpha, rec[k..2k) beta, rec[2k] = steps used once the recursion
-// breaks down (beta ~ 0), after which later updates do nothing.
-template <typename T>
-__global__ void __launch_bounds__(kLzBlock) lanczos_update_kernel(T *v, T *vp, T *w, int n, double *rec, int k,
-                                                                  int j) {
-    __shared__ double s[kLzBlock];
-    if (rec[2 * k] > 0.0) return;
-    double a = 0.0;
-    for (int i = threadIdx.x; i < n; i += kLzBlock) a += (double)w[i] * v[i];
-    a = lz_block_sum(a, s);
-    const double bprev = j > 0 ? rec[k + j - 1] : 0.0;
-    double b = 0.0;
-    for (int i = threadIdx.x; i < n; i += kLzBlock) {
-        const double x = w[i] - a * v[i] - bprev * vp[i];
-        w[i] = (T)x;
-        b += x * x;
-    }
-    b = sqrt(lz_block_sum(b, s));
-    if (threadIdx.x == 0) {
-        rec[j] = a;
-        rec[k + j] = b;
-        if (!(b > 1e-10 * (fabs(a) + 1.0))) rec[2 * k] = j + 1;
-    }
-    if (!(b > 1e-10 * (fabs(a) + 1.0))) return;
-    const double ib = 1.0 / b;
-    for (int i = threadIdx.x; i < n; i += kLzBlock) {
-        vp[i] = v[i];
-        v[i] = (T)(w[i] * ib);
-    }
-}
-
-// dst = (float) src for the n x n block of an ld x n matrix (dst leading dimension ld)
-__global__ void to_fp32_kernel(const double *__restrict__ src, float *__restrict__ dst, int n, int ld) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
-    if (i < n && j < n) dst[(size_t)j * ld + i] = (float)src[(size_t)j * ld + i];
-}
-
 // Spectral bounds of H~ by Lanczos (k steps, no reorthogonalisation) with a
-// guard of |beta_k s_k| + 1 % of the width around the extreme Ritz values.
-// h == nullptr: H~ is cs.Ht (FP64 DSYMV; fixed nuclei, once per trajectory).
-// Otherwise H~ v = G h G^T v with G = L^-1 in cs.Ht (zero upper triangle) on
-// FP32 copies of G and h: FP32 rounding (about 1e-7 of the width) is far
-// inside the 1 % guard, and FP64 GEMVs run on the FP64 pipe at about 37 us
-// each, 120 of them per rebuild.  The copies go to cs.A and cs.Hs, which are
-// written only after the bounds are known.  The recursion runs on the device
-// without host round trips (dot products in FP64); the tridiagonal matrix is
-// read back once.
-int lanczos_bounds(ChebState &cs, int ksteps, const double *h = nullptr) {
+// guard of |beta_k s_k| + cs.guard of the width around the extreme Ritz
+// values, in FP64 on the device in one cooperative launch (lanczos.cu):
+// h == nullptr: H~ is cs.Ht (both triangles stored); otherwise H~ = G h G^T
+// with G = L^-1 in cs.Ht (zero upper triangle) and its transpose Gt (FP64).
+// The tridiagonal matrix is read back once.
+int lanczos_bounds(ChebState &cs, int ksteps, const double *h = nullptr, const double *Gt = nullptr) {
     const int n = cs.N, ld = cs.ld;
     cudaStream_t st = g_ctx.stream;
     const int k = std::min(std::min(ksteps, n), 63);
-    double *rec = cs.lz + 4 * ld;  // [2k + 1] <= 127 doubles
+    double *part = cs.lz + 6 * ld, *rec = part + kLzPart;  // rec: [2k + 1] <= 127 doubles
+    if (h && !Gt) return ELHL_ERR_BAD_ARG;
     CU_TRY(cudaMemsetAsync(rec, 0, (2 * k + 1) * sizeof(double), st));
-    if (h) {
-        float *v = reinterpret_cast<float *>(cs.lz), *vp = v + ld, *w = v + 2 * ld, *t = v + 3 * ld;
-        float *G32 = static_cast<float *>(cs.A), *h32 = static_cast<float *>(cs.Hs);
-        dim3 grid((n + 127) / 128, n);
-        to_fp32_kernel<<<grid, 128, 0, st>>>(cs.Ht, G32, n, ld);
-        count_launch();
-        to_fp32_kernel<<<grid, 128, 0, st>>>(h, h32, n, ld);
-        count_launch();
-        lanczos_start<float><<<(n + 255) / 256, 256, 0, st>>>(v, n);
-        count_launch();
-        CU_TRY(cudaMemsetAsync(vp, 0, n * sizeof(float), st));
-        lanczos_normalize_kernel<float><<<1, kLzBlock, 0, st>>>(v, n);
-        count_launch();
-        const float one = 1.f, zero = 0.f;
-        for (int j = 0; j < k; ++j) {
-            BLAS_TRY(cublasSgemv(g_ctx.blas, CUBLAS_OP_T, n, n, &one, G32, ld, v, 1, &zero, t, 1));  // G^T v
-            BLAS_TRY(cublasSgemv(g_ctx.blas, CUBLAS_OP_N, n, n, &one, h32, ld, t, 1, &zero, w, 1));  // h (.)
-            BLAS_TRY(cublasSgemv(g_ctx.blas, CUBLAS_OP_N, n, n, &one, G32, ld, w, 1, &zero, t, 1));  // G (.)
-            lanczos_update_kernel<float><<<1, kLzBlock, 0, st>>>(v, vp, t, n, rec, k, j);
-            count_launch();
-        }
-    } else if (cs.oz) {
-        // explicit H~ rebuilt every step (ELHL_PREC_OZ64): one FP32 GEMV per Lanczos step on
-        // an FP32 copy in Hs (written by cheb_prepare afterwards); an FP64 DSYMV ran on the
-        // FP64 pipe at 87 us a step.  FP32 rounding (1e-7 of the width) is inside the guard.
-        float *v = reinterpret_cast<float *>(cs.lz), *vp = v + ld, *w = v + 2 * ld;
-        float *H32 = static_cast<float *>(cs.Hs);
-        to_fp32_kernel<<<dim3((n + 127) / 128, n), 128, 0, st>>>(cs.Ht, H32, n, ld);
-        count_launch();
-        lanczos_start<float><<<(n + 255) / 256, 256, 0, st>>>(v, n);
-        count_launch();
-        CU_TRY(cudaMemsetAsync(vp, 0, n * sizeof(float), st));
-        lanczos_normalize_kernel<float><<<1, kLzBlock, 0, st>>>(v, n);
-        count_launch();
-        const float one = 1.f, zero = 0.f;
-        for (int j = 0; j < k; ++j) {
-            BLAS_TRY(cublasSgemv(g_ctx.blas, CUBLAS_OP_N, n, n, &one, H32, ld, v, 1, &zero, w, 1));
-            lanczos_update_kernel<float><<<1, kLzBlock, 0, st>>>(v, vp, w, n, rec, k, j);
-            count_launch();
-        }
-    } else {
-        double *v = cs.lz, *vp = cs.lz + ld, *w = cs.lz + 2 * ld;
-        lanczos_start<double><<<(n + 255) / 256, 256, 0, st>>>(v, n);
-        count_launch();
-        CU_TRY(cudaMemsetAsync(vp, 0, n * sizeof(double), st));
-        lanczos_normalize_kernel<double><<<1, kLzBlock, 0, st>>>(v, n);
-        count_launch();
-        const double one = 1.0, zero = 0.0;
-        for (int j = 0; j < k; ++j) {
-            BLAS_TRY(cublasDsymv(g_ctx.blas, CUBLAS_FILL_MODE_LOWER, n, &one, cs.Ht, ld, v, 1, &zero, w, 1));
-            lanczos_update_kernel<double><<<1, kLzBlock, 0, st>>>(v, vp, w, n, rec, k, j);
-            count_launch();
-        }
-    }
-    CU_TRY(cudaGetLastError());
+    CU_TRY(cudaMemsetAsync(g_ctx.err, 0, sizeof(int), st));
+    CU_TRY(launch_lanczos64(n, ld, k, h ? h : cs.Ht, h ? cs.Ht : nullptr, Gt, cs.lz, cs.lz + 4 * ld, part, kLzPart,
+                            rec, g_ctx.bar, g_ctx.err, st));
+    int err = 0;
+    CU_TRY(copy_d2h(&err, g_ctx.err, sizeof(int)));
+    if (err) return err;
     std::vector<double> r(2 * k + 1);
     CU_TRY(copy_d2h(r.data(), rec, r.size() * sizeof(double)));
     const int used = r[2 * k] > 0.0 ? (int)r[2 * k] : k;
@@ -1168,19 +1046,22 @@ int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, do
     lower_only_kernel<<<dim3((ld + 127) / 128, n), 128, 0, st>>>(cs.Ht, n, ld);
     count_launch();
     CU_TRY(cudaGetLastError());
-    if (int rc = lanczos_bounds(cs, 40, h)) return rc;
-    if (int rc = cheb_prepare(cs, dt, tol, h)) return rc;
     dim3 grid((ld + 127) / 128, n);
-    if (cs.precision != ELHL_PREC_FP64) {  // FP64 L^T and G^T for the column transforms
+    // FP64 G^T: the bounds' G (.) products, then the column transforms (and the
+    // FP64 propagation); FP64 L^T for the transforms of the other precisions
+    if (cs.precision != ELHL_PREC_FP64) {
         if (!cs.Lt64)
             if (int rc = dev_alloc(&cs.Lt64, (size_t)ld * n)) return rc;
         if (!cs.Gt64)
             if (int rc = dev_alloc(&cs.Gt64, (size_t)ld * n)) return rc;
         convert_kernel<double><<<grid, 128, 0, st>>>(Lfac, cs.Lt64, n, ld, true);
         count_launch();
-        convert_kernel<double><<<grid, 128, 0, st>>>(cs.Ht, cs.Gt64, n, ld, true);
-        count_launch();
     }
+    convert_kernel<double><<<grid, 128, 0, st>>>(cs.Ht, const_cast<double *>(cs.gt64()), n, ld, true);
+    count_launch();
+    CU_TRY(cudaGetLastError());
+    if (int rc = lanczos_bounds(cs, 40, h, cs.gt64())) return rc;
+    if (int rc = cheb_prepare(cs, dt, tol, h)) return rc;
     if (cs.precision == ELHL_PREC_DF64) {  // G and G^T as (hi, lo) pairs; no device read-out matrices
         split_df_kernel<<<grid, 128, 0, st>>>(cs.Ht, (float2 *)cs.A, n, ld, 0.0, 1.0, false);
         count_launch();
@@ -1191,10 +1072,8 @@ int cheb_prepare_implicit(ChebState &cs, const double *Lfac, const double *h, do
         cs.readout_ready = false;  // read-out through the FP64 dense transforms
         return ELHL_OK;
     }
-    if (cs.precision == ELHL_PREC_FP64) {
+    if (cs.precision == ELHL_PREC_FP64) {  // G^T (cs.Gt) is in place already
         convert_kernel<double><<<grid, 128, 0, st>>>(cs.Ht, (double *)cs.A, n, ld, false);
-        count_launch();
-        convert_kernel<double><<<grid, 128, 0, st>>>(cs.Ht, (double *)cs.Gt, n, ld, true);
         count_launch();
         convert_kernel<double><<<grid, 128, 0, st>>>(Lfac, (double *)cs.B, n, ld, true);
         count_launch();
@@ -3138,6 +3017,8 @@ int elhl_traj_get_factor(elhl_traj *tr, double *L, double *G) {
 int elhl_traj_get_stats(elhl_traj *tr, elhl_traj_stats *st) {
     if (!tr || !st) return ELHL_ERR_BAD_ARG;
     *st = tr->stats;
+    st->emin = tr->cheb() ? tr->cs.emin : 0.0;
+    st->emax = tr->cheb() ? tr->cs.emax : 0.0;
     st->save_tau[0] = tr->save_tau[0];
     st->save_tau[1] = tr->save_tau[1];
     st->t = tr->t;

@@ -234,6 +234,16 @@ size_t ozgemm_smem_bytes();
 int leaf_rows();
 cudaError_t leaf_chol_inv64(double *A, double *G, int nb, int ld, int row0, int *info, cudaStream_t st);
 
+// Lanczos recursion of k steps for the spectral bounds, FP64, one cooperative
+// launch (lanczos.cu): explicit H (G == nullptr; both triangles stored) or
+// implicit G H G^T (G lower, Gt = G^T).  r: 4 x ld, t: 2 x ld, part: part_cap
+// doubles (at least two per SM), rec: alpha[k], beta[k], steps used (0 = all,
+// zeroed by the caller), bar: 2 barrier words, err: ELHL_ERR_TIMEOUT on a
+// barrier that gave up.
+cudaError_t launch_lanczos64(int n, int ld, int k, const double *H, const double *G, const double *Gt, double *r,
+                             double *t, double *part, int part_cap, double *rec, unsigned *bar, int *err,
+                             cudaStream_t st);
+
 int bessel_j_sequence(double beta, int kmax, double *J);
 int chebyshev_coefficients(double dt, double emin, double emax, double tol, int kcap, std::vector<double> &cre,
                            std::vector<double> &cim, int *K_out);

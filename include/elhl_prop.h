@@ -302,6 +302,8 @@ typedef struct {
     int cheb_retries;     /* Chebyshev steps redone on a widened spectral interval */
     double norm_drift;    /* Chebyshev: largest relative change of a column's squared norm in one step
                              (before renormalisation), over the call's accepted steps */
+    double emin, emax;    /* Chebyshev: spectral interval of the current operator (eV): FP64 Lanczos
+                             extremes with their residual bounds, widened by lanczos_guard */
 } elhl_traj_stats;
 int elhl_traj_get_stats(elhl_traj *tr, elhl_traj_stats *st);
 

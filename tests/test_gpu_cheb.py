@@ -270,3 +270,28 @@ def test_kernel_launch_counter(elhl, flake):
     n2 = elhl.kernel_launches()
     tr.close()
     assert n1 > n0 and n2 > n1
+
+
+@pytest.mark.parametrize("prec_name,moving", [("fp64", False), ("fp64", True), ("oz64", True), ("fp32", True),
+                                              ("fp32", False)])
+def test_spectral_interval_encloses_the_spectrum(elhl, prec_name, moving):
+    """The FP64 Lanczos bounds (one cooperative launch, lanczos.cu) of the explicit
+    H~ (fixed nuclei; OZ64 moving nuclei) and of the implicit G h G^T (moving
+    nuclei): [emin, emax] holds every generalised eigenvalue of (h, S) of the
+    current geometry and is no wider than the 1 % guards plus 3 % of the width."""
+    import scipy.linalg
+    prec = {"fp64": elhl.PREC_FP64, "fp32": elhl.PREC_FP32, "oz64": elhl.PREC_OZ64}[prec_name]
+    sysm = systems.cubic_cluster(n_atoms=150, seed=3)
+    coords = np.stack([systems.perturbed_coords(sysm.coords, i, seed=2) for i in range(3)])
+    tr = elhl.Trajectory(sysm, coords=coords[0] if moving else None, dt=2e-4, method=elhl.METHOD_CHEBYSHEV,
+                         precision=prec, ncols=4 if moving else 2, cheb_tol=1e-12)
+    homo = systems.fermi_state(sysm, sysm.fragment_atoms("E"))
+    tr.init_fmo(homo + 1, homo)
+    tr.step(coords[1:] if moving else None, nsteps=2)
+    st = tr.stats()
+    S, h, _ = tr.matrices()
+    tr.close()
+    lam = scipy.linalg.eigh(h, S, eigvals_only=True)
+    width = lam[-1] - lam[0]
+    assert st.emin <= lam[0] and st.emax >= lam[-1]
+    assert st.emin >= lam[0] - 0.04 * width and st.emax <= lam[-1] + 0.04 * width
