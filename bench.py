@@ -3,9 +3,14 @@
 
 Workload (default): the 1,200-atom disordered C/H/O cluster (60/30/10 %, 1.4 A
 jittered cubic lattice, N = 3,720 AO), moving nuclei (fresh N(0, 0.02 A^2)
-perturbation of every coordinate each step), dt = 0.5 fs, FP64 reference Taylor
-propagation of electron and hole (bra and ket), S, h and H' = S^-1 h rebuilt on
-the device every step.  One step = one nuclear step of both particles.
+perturbation of every coordinate each step), dt = 0.5 fs, Chebyshev propagation
+of electron and hole (bra and ket), S, h, the Cholesky factor of S and the
+propagation operator rebuilt on the device every step.  One step = one nuclear
+step of both particles.  Default precision OZ64: FP64 results, with every
+operator product computed exactly on the tensor cores from BF16 slices and
+rounded once to FP64; the same line carries the FP64-pipe run (fp64_variant)
+and the DF64 run (df64_variant) of the same workload.  `--method taylor` times
+the reference's adaptive-tau Taylor step instead.
 
 Synthetic, seeded data (no external dataset).  Lines:
   value  device-resident: all steps' coordinates uploaded before the timed
@@ -324,7 +329,7 @@ def run_ours(args, rank, world):
 def run_variant(args, precision_name: str):
     """The same workload and coordinates with another precision (device-resident
     steps, CUDA events on the library's stream, L2 flushed between steps): the
-    DF64 and OZ64 variants of the default FP64 run."""
+    FP64-pipe, DF64 and OZ64 variants of the default run."""
     import torch
     from dynemol_gb300 import api, systems
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
@@ -806,7 +811,7 @@ def main():
     ap.add_argument("--workload", default="ehrenfest", choices=sorted(WORKLOAD_DESC))
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--method", default="chebyshev", choices=["taylor", "chebyshev"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "bf16x3", "df64", "oz64"])
+    ap.add_argument("--precision", default="oz64", choices=["fp64", "fp32", "bf16x3", "df64", "oz64"])
     ap.add_argument("--mix", type=int, default=0, help="also run the batched-vs-drop-in comparison on a mix "
                     "of this many trajectories (0 = skip)")
     ap.add_argument("--served-mix", type=int, default=512, help="trajectories of the served mix (0 = skip)")
@@ -829,12 +834,13 @@ def main():
         import torch
         torch.distributed.init_process_group("nccl")
     line = run_ours(args, rank, world)
-    if rank == 0 and args.method == "chebyshev" and args.precision == "fp64" and args.workload != "flake":
-        # the same moving-nuclei workload with the operator in DF64 (FP32 pairs): FP64-level
-        # populations (tested to 1e-9 against the oracle) without the FP64 pipe
-        line["df64_variant"] = run_variant(args, "df64")
-        # and with every operator product exact on the tensor cores (FP64 results, 1e-10 tested)
-        line["oz64_variant"] = run_variant(args, "oz64")
+    if rank == 0 and args.method == "chebyshev" and args.precision in ("fp64", "oz64") and args.workload != "flake":
+        # the same moving-nuclei workload with the other FP64-level operators: OZ64 (every
+        # operator product exact on the tensor cores), FP64 on the FP64 pipe, DF64 (FP32
+        # pairs; populations tested to 1e-9 against the oracle)
+        for p in ("oz64", "fp64", "df64"):
+            if p != args.precision:
+                line[p + "_variant"] = run_variant(args, p)
     if rank == 0 and args.method == "chebyshev" and not args.no_dropin:
         line["dropin_taylor_fp64"] = run_dropin(args)
         line["dropin_host_fp64"] = run_dropin_host(args)
