@@ -263,6 +263,11 @@ def run_ours(args, rank, world):
         per_launch_orders = orders / max(1, K) / m
         bytes_per_launch = per_launch_orders * (bH * elems + vec * N * m)
         flops_per_launch = per_launch_orders * 4.0 * elems * m
+        if args.precision == "oz64" and not implicit:
+            # DRAM traffic per matrix element and order measured by ncu on the same kernel
+            # at N = 2790 (15.86 GB read + 0.59 GB written over 149 orders of N^2 elements:
+            # 14.19 B, the 14 B of slices plus the vectors); scaled to this launch
+            traffic_per_launch = 14.19 * elems * per_launch_orders
         if implicit and args.precision in ("fp64", "df64"):
             # DRAM traffic per matrix element and order measured by ncu on the same
             # kernel at N = 2790 (18.68 GB read + 0.11 GB written over 149 orders of

@@ -176,6 +176,15 @@ __device__ void rows_gemv(const T *M, int ld, const typename Vec2<T>::type *s_v,
     }
 }
 
+// (a + b) + c rounded once for |c| far below ulp(a + b): TwoSum gives a + b = t + e
+// exactly, then t + (e + c)
+__device__ __forceinline__ float two_sum_plus(float a, float b, float c) {
+    const float t = __fadd_rn(a, b);
+    const float z = __fsub_rn(t, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(t, z)), __fsub_rn(b, z));
+    return __fadd_rn(t, __fadd_rn(e, c));
+}
+
 // epilogue of one order: recurrence + FP64 accumulation of c_k v_k
 template <typename T, int MG>
 struct OrderEpi {
@@ -187,7 +196,38 @@ struct OrderEpi {
     double cre, cim;
     const T2 *vprev1;  // implicit operator: y -= shift v_{k-1}; nullptr for an explicit Hs
     T shift;
+    // explicit FP32 Hs: the part of its diagonal that FP32 rounding dropped, added
+    // back as y_i += dcorr_i v_{k-1,i} before v is rounded once (nullptr: none).
+    // FP32 only, error-free: with (t, e) = TwoSum(2 y, -v_{k-2}), v = t + (e + 2 dcorr v_{k-1})
+    // is 2 y + 2 dcorr v_{k-1} - v_{k-2} rounded once (the small terms are far below
+    // t's ulp, so their own roundings do not reach the result)
+    const float *dcorr;
+    const T2 *vdiag;   // v_{k-1}
     __device__ void operator()(int i, int c, T yr, T yi) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (dcorr) {
+                const T2 p = ldcg2(vdiag + (size_t)i * MG + c);
+                const float d = __ldg(dcorr + i);
+                const float dr = __fmul_rn(d, p.x), di = __fmul_rn(d, p.y);
+                T2 v;
+                if (k == 1) {
+                    v.x = __fadd_rn(yr, dr);
+                    v.y = __fadd_rn(yi, di);
+                } else {
+                    const T2 w2 = ldcg2(vprev2 + (size_t)i * MG + c);
+                    v.x = two_sum_plus(__fmul_rn(2.f, yr), -w2.x, __fmul_rn(2.f, dr));
+                    v.y = two_sum_plus(__fmul_rn(2.f, yi), -w2.y, __fmul_rn(2.f, di));
+                }
+                vout[(size_t)i * MG + c] = v;
+                const size_t ao = (size_t)i * m + g * MG + c;
+                double2 a = acc[ao];
+                const double vr = (double)v.x, vi = (double)v.y;
+                a.x += cre * vr - cim * vi;
+                a.y += cre * vi + cim * vr;
+                acc[ao] = a;
+                return;
+            }
+        }
         if (vprev1) {
             const T2 p = ldcg2(vprev1 + (size_t)i * MG + c);
             yr -= shift * p.x;
@@ -239,7 +279,7 @@ __device__ void order_rows(const ChebProblem &pb, const ChebSegment &sg, int k, 
     const T2 *vprev = vbuf + (size_t)((k + 2) % 3) * bstride + g * gstride;   // v_{k-1}
     OrderEpi<T, MG> epi{vbuf + (size_t)((k + 1) % 3) * bstride + g * gstride,
                         vbuf + (size_t)(k % 3) * bstride + g * gstride,
-                        pb.col[parity ^ 1], k, m, g, cre, cim, nullptr, T(0)};
+                        pb.col[parity ^ 1], k, m, g, cre, cim, nullptr, T(0), pb.dcorr, vprev};
     if (jwin == 0 || ld <= jwin) {  // the whole previous vector in shared memory
         __syncthreads();
         for (int q = tid; q < ld * MG; q += kBlock) s_v[q] = ldcg2(vprev + q);  // padding rows are zero
@@ -315,7 +355,7 @@ __device__ void implicit_phase(const ChebLaunch &L, const ChebProblem &pb, int s
         } else {
             OrderEpi<T, MG> epi{vbuf + (size_t)((k + 1) % 3) * bstride + g * gstride,
                                 vbuf + (size_t)(k % 3) * bstride + g * gstride,
-                                pb.col[L.parity ^ 1], k, m, g, cre, cim, vprev, (T)pb.shift};
+                                pb.col[L.parity ^ 1], k, m, g, cre, cim, vprev, (T)pb.shift, nullptr, nullptr};
             rows_gemv<T, MG, 2>(reinterpret_cast<const T *>(pb.Gt), ld, s_v, sg.row0, sg.row1, s_part, epi);
         }
     }

@@ -602,6 +602,22 @@ __global__ void scale_kernel(const double *__restrict__ Ht, T *__restrict__ Hs, 
     Hs[(size_t)j * ld + i] = (T)v;
 }
 
+// dcorr[i] = Hs_ii - (float) Hs_ii (rounded to FP32) for the FP32 Hs of
+// scale_kernel: the diagonal (the on-site energies, the largest entries of Hs)
+// is the part of the FP32 rounding that shifts every eigenvalue coherently, so
+// the row kernel adds it back before each order's single rounding (in numpy
+// replays with exact propagators over 200 steps of the trajectory mix, the FP32
+// Hs moved populations by up to 9.6e-7, the FP32 off-diagonal with the exact
+// diagonal by 6.7e-8 on the same member; on the GPU the served 512-member mix
+// went from 1.36e-6 to 7.9e-7 at most against FP64)
+__global__ void diag_corr_kernel(const double *__restrict__ Ht, float *__restrict__ dcorr, int n, int ld, double a,
+                                 double binv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double v = (Ht[(size_t)i * ld + i] - a) * binv;
+    dcorr[i] = (float)(v - (double)(float)v);
+}
+
 // pops[p*(nfrag+1) + f] = Re sum_{i in f} conj(psi_ip) bra_ip over column p of
 // [ld][m] arrays; one block per particle, fixed-order tree reduction.
 __global__ void populations_kernel(const double2 *__restrict__ psi, const double2 *__restrict__ bra, int n, int m,
@@ -774,6 +790,7 @@ struct ChebState {
     double emin = 0.0, emax = 0.0, a = 0.0, b = 1.0;
     double2 c0{1.0, 0.0};    // host copy of the order-0 coefficient
     double *lz = nullptr;    // Lanczos vectors [6][ld], partial sums [kLzPart], record [128]
+    float *dcorr = nullptr;  // explicit FP32 Hs: [ld] the rounding residual of its diagonal
     // implicit operator (geometry changing every step): Ht holds G = L^-1 in FP64,
     // Hs = h/b, A = G and Gt = G^T in the launch precision; no H~ is formed
     bool implicit = false;
@@ -839,6 +856,8 @@ struct ChebState {
         dev_free(gpops);
         dev_free(Ht); dev_free(phi); dev_free(acc); dev_free(coef); dev_free(lz); dev_free(scale);
         dev_free(drift); dev_free(saved); dev_free(ntot);
+        if (dcorr) cudaFree(dcorr);
+        dcorr = nullptr;
         if (Hs) cudaFree(Hs);
         if (vbuf) cudaFree(vbuf);
         if (A) cudaFree(A);
@@ -924,6 +943,11 @@ int cheb_prepare(ChebState &cs, double dt, double tol, const double *h = nullptr
     } else {
         scale_kernel<float><<<grid, 128, 0, st>>>(src, (float *)cs.Hs, cs.N, cs.ld, a, binv);
         count_launch();
+        if (!h) {  // explicit FP32 Hs: the FP64 correction of its diagonal
+            if (!cs.dcorr) CU_TRY(cudaMalloc(&cs.dcorr, (size_t)cs.ld * sizeof(float)));
+            diag_corr_kernel<<<(cs.N + 255) / 256, 256, 0, st>>>(src, cs.dcorr, cs.N, cs.ld, a, binv);
+            count_launch();
+        }
     }
     CU_TRY(cudaGetLastError());
     std::vector<double> cre, cim;
@@ -1426,6 +1450,8 @@ int cheb_plan(ChebPlan &pl, const std::vector<ChebState *> &states) {
             p.Gt = cs->Gt;
             p.wb = cs->wb;
             p.shift = cs->a / cs->b;
+        } else if (reduced_precision(cs->precision)) {
+            p.dcorr = cs->dcorr;
         }
         p.drift = pl.d_drift + pl.probs.size();
         pl.pops_per_step += (size_t)cs->P * (cs->nfrag + 1);

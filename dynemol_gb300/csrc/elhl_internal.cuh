@@ -119,6 +119,7 @@ struct ChebProblem {
     double *drift;          // largest relative change of a column's squared norm over a step (norm control)
     double *ntot;           // [P] total population of each particle after the step, in FP64 from the
                             // propagated columns (reduced precision: the renormalisation divides by it)
+    const float *dcorr;     // explicit FP32 Hs: [N] Hs_ii minus its FP32 value (in FP32), or nullptr
 };
 struct ChebSegment {
     int prob, row0, row1;   // rows [row0, row1) of problem `prob` owned by one CTA
