@@ -109,13 +109,15 @@ enum {
 };
 enum {
     ELHL_PREC_FP64 = 0,
-    ELHL_PREC_FP32 = 1,   /* Chebyshev: FP32 H~ and series vectors, FP64 coefficients, sums and norms;
-                             with >= 16 ket columns (one per particle) and N >= 2048, H~.Psi runs as
-                             FP32 GEMMs on the FP32 pipes (cuBLAS, FP32 sums along N) */
+    ELHL_PREC_FP32 = 1,   /* Chebyshev: FP32 H~ and series vectors (the FP32 rounding residual of H~'s
+                             diagonal added back in every order), FP64 coefficients, sums, norms,
+                             Cholesky factor with inverse and spectral bounds; with >= 16 ket columns
+                             (one per particle) and N >= 2048, H~.Psi runs as FP32 GEMMs on the FP32
+                             pipes (cuBLAS, FP32 sums along N) */
     ELHL_PREC_DF64 = 3,   /* Chebyshev, implicit operator: operator and series vectors as FP32 pairs
                              hi + lo (48-bit significands) with exact-product / TwoSum arithmetic on the
                              FP32 pipes, FP64 recurrence and sums: FP64-level accuracy (1e-10 populations)
-                             without the FP64 pipe; read-out through FP64 library products */
+                             without the FP64 pipe; FP64 factor, bounds and read-out */
     ELHL_PREC_BF16X3 = 2, /* Chebyshev: as FP32, but those GEMMs run on the tensor cores with each
                              FP32 operand split in three bf16 terms: a hand-written tcgen05/TMA kernel
                              for 16, 32 or 64 columns (cuBLAS emulation otherwise); outside the GEMM
@@ -123,8 +125,9 @@ enum {
     ELHL_PREC_OZ64 = 4    /* Chebyshev, trajectories with ncols <= 4: FP64 operator, vectors and
                              recurrence, with every operator product computed exactly on the tensor
                              cores from 7 bf16 slices of 8 bits per operand (Ozaki scheme I, products
-                             below 2^-64 of a row's scale dropped) and rounded once to FP64; set-up
-                             (factorisation, bounds, read-out) as ELHL_PREC_FP64 */
+                             below 2^-64 of a row's scale dropped) and rounded once to FP64; moving
+                             nuclei form H~ = G h G^T every step the same way, and the factorisation's
+                             products of 320 or more rows too; bounds and read-out in FP64 */
 };
 
 /* STO basis of one system (the STO_basis fields the path reads, types_EHT.f:135-165). */
