@@ -26,6 +26,7 @@ constexpr int kMaxL = 1;
 constexpr int kNT = kMaxN + 3 * kMaxL + 1;  // n index bound: na + la + 2 lb <= 6 -> 7 entries
 constexpr int kHR = kNT + 2;                // 1F1 rows (alpha up to namax + 1)
 constexpr int kHC = 2 * kNT + 2;            // 1F1 columns (gamma up to ngmax)
+constexpr int kMaxShell = 4;                // radial shells per atom handled per shell pair
 
 // Constant tables (UTIL_OVERLAP, overlap_D.f:1194-1231): 1/i (0 at i = 0), i!
 // and 1/i!.  Filled once per device by init_tables; FP64 division is slow on
@@ -53,27 +54,11 @@ __device__ __forceinline__ double rcp_int(int i) { return __ldg(&g_reali[i]); }
 __device__ __forceinline__ double dfact(int n) { return __ldg(&g_fact[n]); }
 __device__ __forceinline__ double dfacti(int n) { return __ldg(&g_facti[n]); }
 
-// <na la m | nb lb m>, m = 0..min(la, lb), lined-up frame.  Returns false on
-// quantum numbers outside the supported range.
-__device__ bool lined_up_overlap(int na, int la, double za, int nb, int lb, double zb, double R,
-                                 double *sol) {
-    if (na < 1 || nb < 1 || na > kMaxN || nb > kMaxN || la > kMaxL || lb > kMaxL) return false;
-    double h1f1[kHR][kHC];
-    double smat[kNT][kNT], saux_l[kNT][kNT], sbase[kNT][kNT];
-
-    const bool a_big = (za >= zb);
-    int nmin, nmax, npmin, npmax;
-    double z, zp;
-    if (a_big) {
-        nmin = na - la; nmax = na + la + 2 * lb; npmin = nb - lb; npmax = nb + lb + 2 * la;
-        z = za; zp = zb;
-    } else {
-        nmin = nb - lb; nmax = nb + lb + 2 * la; npmin = na - la; npmax = na + la + 2 * lb;
-        z = zb; zp = za;
-    }
-    const double expzR = exp(-z * R);
-    const int ngmax = nmax + npmax + 2;
-    const int namax = npmax + 1;
+// 1F1[i, j, arg] for i = 1..namax and j = 2..ngmax, arg = (z - zp) R, as SOLAP
+// builds it (overlap_D.f:766-819): column ngmax from the series pair at ia and
+// ia + 1 and the three-term recursion in i, then the columns j < ngmax by the
+// contiguous relations, downwards.  Entry [i][j] is filled for i <= min(namax, j - 1).
+__device__ void h1f1_table(double z, double zp, double R, int ngmax, int namax, double (&h1f1)[kHR][kHC]) {
     const double arg = (z - zp) * R;
     int ia = (ngmax - (int)z) / 2;
     if (ia < 1) ia = 1;
@@ -103,38 +88,45 @@ __device__ bool lined_up_overlap(int na, int la, double za, int nb, int lb, doub
         const int itop = min(namax - 1, j - 2);
         for (int i = 1; i <= itop; ++i) h1f1[i + 1][j] = aux * h1f1[i + 1][j + 1] + h1f1[i][j];
     }
+}
 
-    // basic integrals <N00|N'00>
-    {
-        const double pi4 = 12.566370614359172953850573533118012;
-        const double zzpR = (z + zp) * R;
-        const double zzpi = 1.0 / (z + zp);
-        double zzpin = 1.0;
-        for (int e = 0; e < nmin + npmin + 1; ++e) zzpin *= zzpi;
-        for (int n = nmin; n <= nmax; ++n) {
-            double zzpinp = zzpin;
-            for (int np = npmin; np <= npmax - n + nmin; ++np) {
-                double auxk = dfact(n + np) * zzpinp;
-                double sumk = 0.0;
-                for (int k = 0; k <= n + np; ++k) {
-                    double sumj = 0.0;
-                    for (int j = max(0, k - n); j <= min(k, np); ++j)
-                        sumj = sumj + h1f1[j + 1][k + 2] * dfacti(n + j - k) * dfacti(np - j);
-                    sumk = sumk + sumj * auxk;
-                    auxk = auxk * zzpR * rcp_int(n + np - k) * rcp_int(k + 2);
-                }
-                const double v = pi4 * expzR * dfact(n) * dfact(np) * sumk;
-                const int r0 = a_big ? n : np, r1 = a_big ? np : n;
-                smat[r0][r1] = v;
-                saux_l[r0][r1] = v;
-                sbase[r0][r1] = v;
-                zzpinp = zzpinp * zzpi;
-            }
-            zzpin = zzpin * zzpi;
-        }
+// basic integral <N00|N'00> for the index n of the larger exponent z and np of
+// the smaller zp (SOLAP's loop body, overlap_D.f:821-850); zpow[e] = (z + zp)^-e
+// by repeated products, the same sequence SOLAP's running products take
+__device__ double basic_integral(int n, int np, double z, double zp, double R, double expzR,
+                                 const double (&h1f1)[kHR][kHC], const double *zpow) {
+    const double pi4 = 12.566370614359172953850573533118012;
+    const double zzpR = (z + zp) * R;
+    double auxk = dfact(n + np) * zpow[n + np + 1];
+    double sumk = 0.0;
+    for (int k = 0; k <= n + np; ++k) {
+        double sumj = 0.0;
+        for (int j = max(0, k - n); j <= min(k, np); ++j)
+            sumj = sumj + h1f1[j + 1][k + 2] * dfacti(n + j - k) * dfacti(np - j);
+        sumk = sumk + sumj * auxk;
+        auxk = auxk * zzpR * rcp_int(n + np - k) * rcp_int(k + 2);
     }
+    return pi4 * expzR * dfact(n) * dfact(np) * sumk;
+}
 
-    nmin = na - la; nmax = na + la + 2 * lb; npmin = nb - lb; npmax = nb + lb + 2 * la;
+// index ranges of one lined-up overlap in the orientation of the basic integrals
+// (n: the atom with the larger exponent, np: the other)
+struct SolapRange {
+    int nmin, nmax, npmin, npmax;
+};
+__device__ __forceinline__ SolapRange solap_range(int na, int la, int nb, int lb, bool a_big) {
+    return a_big ? SolapRange{na - la, na + la + 2 * lb, nb - lb, nb + lb + 2 * la}
+                 : SolapRange{nb - lb, nb + lb + 2 * la, na - la, na + la + 2 * lb};
+}
+
+// the l, l' and m recurrences of SOLAP (overlap_D.f:852-962) from the basic
+// integrals base[n_a][n_b]: <na la m | nb lb m>, m = 0..min(la, lb)
+__device__ void lined_up_from_base(int na, int la, int nb, int lb, double R, const double (&base)[kNT][kNT],
+                                   double *sol) {
+    double smat[kNT][kNT], saux_l[kNT][kNT], sbase[kNT][kNT];
+    for (int i = 0; i < kNT; ++i)
+        for (int j = 0; j < kNT; ++j) smat[i][j] = saux_l[i][j] = sbase[i][j] = base[i][j];
+    int nmin = na - la, nmax = na + la + 2 * lb, npmin = nb - lb, npmax = nb + lb + 2 * la;
     const double Rinv = 1.0 / R, R2 = R * R, R4 = R2 * R2;
     double m0 = 0.5;
     const int mtop = min(la, lb);
@@ -164,7 +156,7 @@ __device__ bool lined_up_overlap(int na, int la, double za, int nb, int lb, doub
         sol[m] = smat[na][nb];
         if (m == mtop) break;
         nmin += 1; nmax -= 3; npmin += 1; npmax -= 3;
-        aux = m0 * 0.25 * (double)(m + m + 1) * (double)(m + m + 1) * Rinv * Rinv;
+        const double aux = m0 * 0.25 * (double)(m + m + 1) * (double)(m + m + 1) * Rinv * Rinv;
         for (int n = nmin; n <= nmax; ++n)
             for (int np = npmin; np <= npmax - n + nmin; ++np)
                 saux_l[n][np] = aux * (2.0 * (sbase[n + 1][np + 1] + R2 * (sbase[n + 1][np - 1] + sbase[n - 1][np + 1])) -
@@ -176,6 +168,75 @@ __device__ bool lined_up_overlap(int na, int la, double za, int nb, int lb, doub
             }
         m0 = 1.0;
     }
+}
+
+__device__ __forceinline__ bool supported(int n, int l) { return n >= 1 && n <= kMaxN && l >= 0 && l <= kMaxL; }
+
+// <na la m | nb lb m>, m = 0..min(la, lb), lined-up frame (SOLAP,
+// overlap_D.f:701-962).  Returns false on quantum numbers outside the supported range.
+__device__ bool lined_up_overlap(int na, int la, double za, int nb, int lb, double zb, double R,
+                                 double *sol) {
+    if (!supported(na, la) || !supported(nb, lb)) return false;
+    double h1f1[kHR][kHC];
+    double base[kNT][kNT] = {};
+    const bool a_big = (za >= zb);
+    const double z = a_big ? za : zb, zp = a_big ? zb : za;
+    const SolapRange r = solap_range(na, la, nb, lb, a_big);
+    h1f1_table(z, zp, R, r.nmax + r.npmax + 2, r.npmax + 1, h1f1);
+    const double expzR = exp(-z * R), zzpi = 1.0 / (z + zp);
+    double zpow[2 * kNT + 1];
+    zpow[0] = 1.0;
+    for (int e = 1; e <= 2 * kNT; ++e) zpow[e] = zpow[e - 1] * zzpi;
+    for (int n = r.nmin; n <= r.nmax; ++n)
+        for (int np = r.npmin; np <= r.npmax - n + r.nmin; ++np) {
+            const double v = basic_integral(n, np, z, zp, R, expzR, h1f1, zpow);
+            if (a_big) base[n][np] = v;
+            else base[np][n] = v;
+        }
+    lined_up_from_base(na, la, nb, lb, R, base, sol);
+    return true;
+}
+
+// Every shell pair of an atom pair whose shells all carry one exponent per atom
+// (za for A, zb for B; the H/C/O EHT basis): the lined-up overlaps sol[p][q][m]
+// from one 1F1 table, built at the largest (ngmax, namax) of the pairs, and one
+// basic integral per (n, n') cell that some pair reads; each pair then runs only
+// its own l, l' and m recurrences.  Per pair SOLAP rebuilds both (four times for
+// the s/p shells of two C atoms), and they are most of the build's FP64
+// instructions.  The shared table's columns below a pair's own ngmax come from
+// the same downward relations started higher up, so values differ from the
+// per-pair ones by rounding only.  Returns false on unsupported quantum numbers.
+__device__ bool shared_lined_up(const int *na, const int *la, int nsa, double za, const int *nb, const int *lb,
+                                int nsb, double zb, double R, double (*sol)[kMaxShell][kMaxL + 1]) {
+    const bool a_big = (za >= zb);
+    const double z = a_big ? za : zb, zp = a_big ? zb : za;
+    int ngmax = 0, namax = 0;
+    unsigned long long needl = 0;  // cells (n, np) of the basic integrals some pair reads: bit n * kNT + np
+    for (int p = 0; p < nsa; ++p)
+        for (int q = 0; q < nsb; ++q) {
+            if (!supported(na[p], la[p]) || !supported(nb[q], lb[q])) return false;
+            const SolapRange r = solap_range(na[p], la[p], nb[q], lb[q], a_big);
+            ngmax = max(ngmax, r.nmax + r.npmax + 2);
+            namax = max(namax, r.npmax + 1);
+            for (int n = r.nmin; n <= r.nmax; ++n)
+                for (int np = r.npmin; np <= r.npmax - n + r.nmin; ++np) needl |= 1ull << (n * kNT + np);
+        }
+    double h1f1[kHR][kHC];
+    h1f1_table(z, zp, R, ngmax, namax, h1f1);
+    const double expzR = exp(-z * R), zzpi = 1.0 / (z + zp);
+    double zpow[2 * kNT + 1];
+    zpow[0] = 1.0;
+    for (int e = 1; e <= 2 * kNT; ++e) zpow[e] = zpow[e - 1] * zzpi;
+    double base[kNT][kNT] = {};
+    for (int n = 0; n < kNT; ++n)
+        for (int np = 0; np < kNT; ++np) {
+            if (!((needl >> (n * kNT + np)) & 1ull)) continue;
+            const double v = basic_integral(n, np, z, zp, R, expzR, h1f1, zpow);
+            if (a_big) base[n][np] = v;
+            else base[np][n] = v;
+        }
+    for (int p = 0; p < nsa; ++p)
+        for (int q = 0; q < nsb; ++q) lined_up_from_base(na[p], la[p], nb[q], lb[q], R, base, sol[p][q]);
     return true;
 }
 
@@ -188,7 +249,7 @@ __device__ __forceinline__ double anor(double ea, double eb, int na, int nb, int
     v = v * (la * 2 + 1.0);
     v = v * (lb * 2 + 1.0);
     v = v * aux;
-    const double PI = 4.0 * atan(1.0);
+    const double PI = 3.141592653589793;  // 4 atan(1), the nearest double to pi (GET_ANOR's PI)
     return sqrt(v) / (4.0 * PI);
 }
 
@@ -205,7 +266,6 @@ __device__ __forceinline__ double x_ij(double ipi, double ipj, double vi, double
 // coefficients (the m components of one radial function).  The lined-up
 // overlaps depend on the shells only, so they are computed once per shell pair
 // and the rotation is applied per AO pair.
-constexpr int kMaxShell = 4;
 
 __device__ bool same_radial(const DevBasis &b, int x, int y) {
     return b.ao_n[x] == b.ao_n[y] && b.ao_l[x] == b.ao_l[y] && b.ao_nzeta[x] == b.ao_nzeta[y] &&
@@ -227,33 +287,49 @@ __device__ int atom_shells(const DevBasis &b, int ao0, int nao, int *first, int 
     return ns;
 }
 
-// normalised, contracted lined-up overlaps <aa|bb>_m, m = 0..min(la, lb)
-// (the SOLAP + GET_ANOR part of BUILD_OVERLAP_MATRIX, overlap_D.f:228-280)
-__device__ void contracted_overlap(const DevBasis &b, int aa, int bb, double R, double *solnorm) {
+// solnorm[m] += c_i c_j N_ij sol[m] for the zeta pair (i of aa, j of bb): the
+// normalisation and contraction of BUILD_OVERLAP_MATRIX (overlap_D.f:228-280)
+__device__ void add_normalised(const DevBasis &b, int aa, int bb, int i, int j, const double *sol, double *solnorm) {
     const int na = b.ao_n[aa], la = b.ao_l[aa];
     const int nb = b.ao_n[bb], lb = b.ao_l[bb];
     const double aux = 1.0 / (dfact(na + na) * dfact(nb + nb));
     const int msup = min(la, lb);
+    const double eb = b.ao_zeta[2 * bb + j], ea = b.ao_zeta[2 * aa + i];
+    double an = anor(ea, eb, na, nb, la, lb, aux);
+    double part[kMaxL + 1];
+    for (int m = 0; m <= msup - 1; ++m) {
+        part[m] = sol[m] * an;
+        an = an / sqrt((la + m + 1.0) * (la - m) * (lb + m + 1.0) * (lb - m));
+        if (m == 0) an = an + an;
+    }
+    part[msup] = sol[msup] * an;
+    const double cc = b.ao_coef[2 * aa + i] * b.ao_coef[2 * bb + j];
+    for (int k = 0; k <= msup; ++k) solnorm[k] = solnorm[k] + cc * part[k];
+}
+
+// normalised, contracted lined-up overlaps <aa|bb>_m, m = 0..min(la, lb)
+// (the SOLAP + GET_ANOR part of BUILD_OVERLAP_MATRIX, overlap_D.f:228-280)
+__device__ void contracted_overlap(const DevBasis &b, int aa, int bb, double R, double *solnorm) {
     solnorm[0] = solnorm[1] = 0.0;
     for (int j = 0; j < b.ao_nzeta[bb]; ++j) {
         for (int i = 0; i < b.ao_nzeta[aa]; ++i) {
-            const double eb = b.ao_zeta[2 * bb + j], ea = b.ao_zeta[2 * aa + i];
             double sol[kMaxL + 1];
-            if (!lined_up_overlap(na, la, ea, nb, lb, eb, R, sol)) {
+            if (!lined_up_overlap(b.ao_n[aa], b.ao_l[aa], b.ao_zeta[2 * aa + i], b.ao_n[bb], b.ao_l[bb],
+                                  b.ao_zeta[2 * bb + j], R, sol)) {
                 sol[0] = sol[1] = __longlong_as_double(0x7ff8000000000000ULL);  // NaN marks unsupported
             }
-            double an = anor(ea, eb, na, nb, la, lb, aux);
-            double part[kMaxL + 1];
-            for (int m = 0; m <= msup - 1; ++m) {
-                part[m] = sol[m] * an;
-                an = an / sqrt((la + m + 1.0) * (la - m) * (lb + m + 1.0) * (lb - m));
-                if (m == 0) an = an + an;
-            }
-            part[msup] = sol[msup] * an;
-            const double cc = b.ao_coef[2 * aa + i] * b.ao_coef[2 * bb + j];
-            for (int k = 0; k <= msup; ++k) solnorm[k] = solnorm[k] + cc * part[k];
+            add_normalised(b, aa, bb, i, j, sol, solnorm);
         }
     }
+}
+
+// the single exponent carried by every shell (first AOs first[0..ns)) of an atom, if there is one
+__device__ bool uniform_zeta(const DevBasis &b, const int *first, int ns, double *z) {
+    const double z0 = b.ao_zeta[2 * first[0]];
+    for (int s = 0; s < ns; ++s)
+        if (b.ao_nzeta[first[s]] != 1 || b.ao_zeta[2 * first[s]] != z0) return false;
+    *z = z0;
+    return true;
 }
 
 // S block of atoms ia != ib for B - A = (xab, yab, zab) (Angstrom): calls
@@ -303,9 +379,27 @@ __device__ void pair_overlap_block(const DevBasis &b, int ia, int ib, double xab
     const int nsb = (inside && nb_ao <= 16) ? atom_shells(b, b0, nb_ao, fb, shb) : -1;
     const bool shells = nsa > 0 && nsb > 0;
     double sn[kMaxShell][kMaxShell][kMaxL + 1];
-    if (shells)
-        for (int q = 0; q < nsb; ++q)
-            for (int p = 0; p < nsa; ++p) contracted_overlap(b, fa[p], fb[q], R, sn[p][q]);
+    if (shells) {
+        double za = 0.0, zb = 0.0;
+        bool done = false;
+        if (uniform_zeta(b, fa, nsa, &za) && uniform_zeta(b, fb, nsb, &zb)) {
+            int nas[kMaxShell], las[kMaxShell], nbs[kMaxShell], lbs[kMaxShell];
+            for (int p = 0; p < nsa; ++p) { nas[p] = b.ao_n[fa[p]]; las[p] = b.ao_l[fa[p]]; }
+            for (int q = 0; q < nsb; ++q) { nbs[q] = b.ao_n[fb[q]]; lbs[q] = b.ao_l[fb[q]]; }
+            double sol[kMaxShell][kMaxShell][kMaxL + 1];
+            if (shared_lined_up(nas, las, nsa, za, nbs, lbs, nsb, zb, R, sol)) {
+                for (int q = 0; q < nsb; ++q)
+                    for (int p = 0; p < nsa; ++p) {
+                        sn[p][q][0] = sn[p][q][1] = 0.0;
+                        add_normalised(b, fa[p], fb[q], 0, 0, sol[p][q], sn[p][q]);
+                    }
+                done = true;
+            }
+        }
+        if (!done)
+            for (int q = 0; q < nsb; ++q)
+                for (int p = 0; p < nsa; ++p) contracted_overlap(b, fa[p], fb[q], R, sn[p][q]);
+    }
 
     for (int jb = 0; jb < nb_ao; ++jb) {
         const int bb = b0 + jb;
