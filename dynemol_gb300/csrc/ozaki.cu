@@ -179,11 +179,20 @@ __device__ __forceinline__ bool grid_barrier_sub(unsigned *count, unsigned *gen,
 
 // ---- phase roles ----------------------------------------------------------------
 
-__device__ void produce(const Ctx &c, const OzLaunch &L, const CUtensorMap *map, Roles &r) {
+// The CTA's blocks of one order: its segments and their blocks in order, or (rev)
+// both backwards.  Odd orders run backwards: the operator's slices (14 N^2 bytes,
+// 194 MB at N = 3720) exceed the 129 MB L2, so a forward walk every order finds
+// none of them there, while turning back starts each order on the part the last
+// one read most recently.  The sums are exact, so the direction changes no bit.
+__device__ __forceinline__ int walk_seg(int s0, int s1, int i, bool rev) { return rev ? s1 - 1 - i : s0 + i; }
+__device__ __forceinline__ int walk_kb(const OzSeg &sg, int i, bool rev) { return rev ? sg.kb1 - 1 - i : sg.kb0 + i; }
+
+__device__ void produce(const Ctx &c, const OzLaunch &L, const CUtensorMap *map, Roles &r, bool rev) {
     const int s0 = L.seg_begin[blockIdx.x], s1 = L.seg_begin[blockIdx.x + 1];
-    for (int q = s0; q < s1; ++q) {
-        const OzSeg sg = L.segs[q];
-        for (int kb = sg.kb0; kb < sg.kb1; ++kb) {
+    for (int qi = 0; qi < s1 - s0; ++qi) {
+        const OzSeg sg = L.segs[walk_seg(s0, s1, qi, rev)];
+        for (int ki = 0; ki < sg.kb1 - sg.kb0; ++ki) {
+            const int kb = walk_kb(sg, ki, rev);
             for (int a = 0; a < kS; ++a) {
                 const unsigned s = r.acnt % kAStages;
                 if (r.acnt >= kAStages && !mbar_wait(&c.empty[s], ((r.acnt / kAStages) - 1) & 1, now_ns(), kWaitNs)) {
@@ -202,11 +211,11 @@ __device__ void produce(const Ctx &c, const OzLaunch &L, const CUtensorMap *map,
 
 // One block per accumulator buffer: over 64 K every weight's sum of slice
 // products stays below 2^23.2, exact in FP32.
-__device__ void issue_mma(const Ctx &c, const OzLaunch &L, Roles &r) {
+__device__ void issue_mma(const Ctx &c, const OzLaunch &L, Roles &r, bool rev) {
     const int s0 = L.seg_begin[blockIdx.x], s1 = L.seg_begin[blockIdx.x + 1];
-    for (int q = s0; q < s1; ++q) {
-        const OzSeg sg = L.segs[q];
-        for (int kb = sg.kb0; kb < sg.kb1; ++kb) {
+    for (int qi = 0; qi < s1 - s0; ++qi) {
+        const OzSeg sg = L.segs[walk_seg(s0, s1, qi, rev)];
+        for (int ki = 0; ki < sg.kb1 - sg.kb0; ++ki) {
             const unsigned tb = r.gcnt & 1;
             if (r.gcnt >= 2 && !mbar_wait(&c.accempty[tb], ((r.gcnt >> 1) - 1) & 1, now_ns(), kWaitNs)) {
                 set_abort(c, L.error);
@@ -246,12 +255,13 @@ __device__ void issue_mma(const Ctx &c, const OzLaunch &L, Roles &r) {
 }
 
 // vector operand of each block: the 9 KB tile the previous order wrote
-__device__ void load_vectors(const Ctx &c, const OzLaunch &L, const unsigned char *xs, Roles &r) {
+__device__ void load_vectors(const Ctx &c, const OzLaunch &L, const unsigned char *xs, Roles &r, bool rev) {
     fence_proxy_async_global();  // the tiles were written by generic stores before the grid barrier
     const int s0 = L.seg_begin[blockIdx.x], s1 = L.seg_begin[blockIdx.x + 1];
-    for (int q = s0; q < s1; ++q) {
-        const OzSeg sg = L.segs[q];
-        for (int kb = sg.kb0; kb < sg.kb1; ++kb) {
+    for (int qi = 0; qi < s1 - s0; ++qi) {
+        const OzSeg sg = L.segs[walk_seg(s0, s1, qi, rev)];
+        for (int ki = 0; ki < sg.kb1 - sg.kb0; ++ki) {
+            const int kb = walk_kb(sg, ki, rev);
             const unsigned sb = r.bcnt % kBStages;
             if (r.bcnt >= kBStages &&
                 !mbar_wait(&c.bempty[sb], ((r.bcnt / kBStages) - 1) & 1, now_ns(), kWaitNs)) {
@@ -470,7 +480,7 @@ __device__ void chunk_epilogue(const Ctx &c, const OzLaunch &L, const OrderIO &i
 // 64-row chunks this CTA is designated for (chunk h by CTA floor(h grid /
 // chunks): spread over the grid, at most one per CTA while chunks <= grid),
 // each once its row tile's segments are all counted.
-__device__ void flush_and_epilogue(const Ctx &c, const OzLaunch &L, const OrderIO &io, Roles &r) {
+__device__ void flush_and_epilogue(const Ctx &c, const OzLaunch &L, const OrderIO &io, Roles &r, bool rev) {
     const int t = threadIdx.x - 128;  // 0 .. 127: TMEM lane / row in the tile
     const int warp = threadIdx.x >> 5;
     const int s0 = L.seg_begin[blockIdx.x], s1 = L.seg_begin[blockIdx.x + 1];
@@ -479,12 +489,13 @@ __device__ void flush_and_epilogue(const Ctx &c, const OzLaunch &L, const OrderI
     int E[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) E[u] = __ldcg(io.emax_in + u);
-    for (int q = s0; q < s1; ++q) {
-        const OzSeg sg = L.segs[q];
+    for (int qi = 0; qi < s1 - s0; ++qi) {
+        const OzSeg sg = L.segs[walk_seg(s0, s1, qi, rev)];
         I128 A[8];
 #pragma unroll
         for (int u = 0; u < 8; ++u) A[u] = I128{0, 0ull};
-        for (int kb = sg.kb0; kb < sg.kb1; ++kb) {
+        for (int ki = 0; ki < sg.kb1 - sg.kb0; ++ki) {
+            const int kb = walk_kb(sg, ki, rev);
             const unsigned tb = r.gcnt & 1;
             // one thread waits and all 128 follow its outcome, so that none is left
             // alone at the named barriers
@@ -629,12 +640,12 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int k = 1; ok && k <= L.K; ++k) {
         const int bin = (k + 2) % 3, bout = k % 3;
         if (warp == 0) {
-            if ((threadIdx.x & 31) == 0) produce(c, L, &mH, r);
+            if ((threadIdx.x & 31) == 0) produce(c, L, &mH, r, k & 1);
             ok = !aborted(c) && *(volatile int *)L.error == 0;
             continue;
         }
         if (warp == 1) {
-            if ((threadIdx.x & 31) == 0) issue_mma(c, L, r);
+            if ((threadIdx.x & 31) == 0) issue_mma(c, L, r, k & 1);
             ok = !aborted(c) && *(volatile int *)L.error == 0;
             continue;
         }
@@ -642,7 +653,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             // buffer (k + 1) % 3 was written two orders ago and read in the last one
             if (blockIdx.x == 0 && threadIdx.x >= 96 && threadIdx.x < 104)
                 L.emax[(k + 1) % 3][threadIdx.x - 96] = kNoExp;
-            if (threadIdx.x == 64) load_vectors(c, L, L.xs[bin], r);
+            if (threadIdx.x == 64) load_vectors(c, L, L.xs[bin], r, k & 1);
         } else {
             OrderIO io{};
             const double2 ck = L.coef[k];
@@ -656,7 +667,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             io.xs_out = L.xs[bout];
             io.xe_out = L.xe[bout];
             io.emax_out = L.emax[bout];
-            flush_and_epilogue(c, L, io, r);
+            flush_and_epilogue(c, L, io, r, k & 1);
         }
         ok = grid_barrier_sub(L.bar_count, L.bar_gen, G, L.error, bar_ns) && !aborted(c);
         if (!ok && threadIdx.x == 64) atomicExch(c.abort_flag, 1);  // stops this CTA's producer and MMA issuer

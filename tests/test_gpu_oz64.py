@@ -97,3 +97,27 @@ def test_oz64_unsupported_forms(elhl, flake):
                         nparticles=8)
     with pytest.raises(elhl.ElhlError):
         elhl.Server(1e9, method=elhl.METHOD_CHEBYSHEV, precision=elhl.PREC_OZ64)
+
+
+def test_oz64_stalled_cta_is_reported(elhl, flake):
+    """A CTA that leaves the OZ64 propagation launch at once (the test hook) never
+    reaches the grid barrier, so the others' waits run out at the 0.2 s limit and
+    the call returns ELHL_ERR_TIMEOUT; a fresh launch on the same context then
+    succeeds."""
+    kw = dict(dt=1e-4, method=elhl.METHOD_CHEBYSHEV, precision=elhl.PREC_OZ64, ncols=2, cheb_tol=1e-14)
+    tr = elhl.Trajectory(flake, **kw)
+    tr.init_fmo(41, 40)
+    tr.step(None, nsteps=1)
+    elhl.debug_barrier(0.2, 0)
+    try:
+        with pytest.raises(elhl.ElhlError) as e:
+            tr.step(None, nsteps=1)
+    finally:
+        elhl.debug_barrier(0.0, -1)
+    tr.close()
+    assert e.value.status == elhl.ERR_TIMEOUT
+    tr = elhl.Trajectory(flake, **kw)
+    tr.init_fmo(41, 40)
+    pops = tr.step(None, nsteps=2)
+    tr.close()
+    assert np.isfinite(pops).all() and abs(pops[-1, 0, -1] - 1.0) < 1e-10
