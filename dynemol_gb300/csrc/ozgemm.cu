@@ -96,22 +96,25 @@ __device__ __forceinline__ void load_tile(const OperandView &v, int r0, int j0, 
 }
 
 // Slicing of both operands in two passes over pieces of 32 operand rows x
-// kChunk K (blockIdx.z: 0 = op(A), 1 = op(B)^T), tiles of 32 x 32 loaded along
+// chunk K (blockIdx.z: 0 = op(A), 1 = op(B)^T), tiles of 32 x 32 loaded along
 // X's contiguous index: oz_partmax_kernel writes each row's largest |element|
 // of the piece to pm[r][piece]; oz_slice_kernel reduces a row's pieces to its
 // scale 2^e_r (scale[r], written by the pieces at K = 0) and cuts every element
 // of its piece with slice7 into out[s][r][j] (row stride kp, zero for k <= j < kp).
-constexpr int kChunk = 256;
+// The piece is 256 K, or 128 / 64 for K up to 1024 / 512: a piece's tiles run one
+// after another, so short operands take more, shorter pieces (more CTAs, each
+// with fewer dependent tile loads).
+__host__ __device__ constexpr int slice_chunk(int kp) { return kp <= 512 ? 64 : kp <= 1024 ? 128 : 256; }
 
 __global__ void __launch_bounds__(256) oz_partmax_kernel(OperandView va, OperandView vb, double *pmA, double *pmB,
-                                                         int npiece) {
+                                                         int npiece, int chunk) {
     __shared__ double t[32][33];
     const bool isB = blockIdx.z == 1;
     const OperandView &v = isB ? vb : va;
-    const int r0 = blockIdx.y * 32, j00 = blockIdx.x * kChunk;
+    const int r0 = blockIdx.y * 32, j00 = blockIdx.x * chunk;
     if (r0 >= v.rows) return;
     double mx = 0.0;  // thread (x, y): row r0 + x over K columns y, y + 8, ... of each tile
-    for (int j0 = j00; j0 < min(v.k, j00 + kChunk); j0 += 32) {
+    for (int j0 = j00; j0 < min(v.k, j00 + chunk); j0 += 32) {
         __syncthreads();
         load_tile(v, r0, j0, t);
         __syncthreads();
@@ -129,14 +132,15 @@ __global__ void __launch_bounds__(256) oz_partmax_kernel(OperandView va, Operand
 
 __global__ void __launch_bounds__(256) oz_slice_kernel(OperandView va, OperandView vb, const double *pmA,
                                                        const double *pmB, int npiece, __nv_bfloat16 *outA,
-                                                       __nv_bfloat16 *outB, int kp, double *scA, double *scB) {
+                                                       __nv_bfloat16 *outB, int kp, double *scA, double *scB,
+                                                       int chunk) {
     __shared__ double t[32][33];
     __shared__ int s_e[32];
     const bool isB = blockIdx.z == 1;
     const OperandView &v = isB ? vb : va;
     const double *pm = isB ? pmB : pmA;
     __nv_bfloat16 *out = isB ? outB : outA;
-    const int r0 = blockIdx.y * 32, j00 = blockIdx.x * kChunk;
+    const int r0 = blockIdx.y * 32, j00 = blockIdx.x * chunk;
     if (r0 >= v.rows) return;
     if (threadIdx.y == 0) {
         const int r = r0 + threadIdx.x;
@@ -148,7 +152,7 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(OperandView va, OperandVi
         if (blockIdx.x == 0 && r < v.rows) (isB ? scB : scA)[r] = pow2(e);
     }
     const size_t sstride = (size_t)v.rows * kp;
-    for (int j0 = j00; j0 < min(kp, j00 + kChunk); j0 += 32) {
+    for (int j0 = j00; j0 < min(kp, j00 + chunk); j0 += 32) {
         __syncthreads();
         load_tile(v, r0, j0, t);
         __syncthreads();
@@ -458,13 +462,13 @@ cudaError_t ozgemm(int m, int n, int k, double alpha, const double *A, int lda, 
     const OperandView va{A, lda, transA, m, k, (tri & kTriA) ? 1 : (tri & kTriAt) ? 2 : 0};
     // op(B) columns: B(l, j) (K along B's columns) or B^T: B(j, l) (K along B's rows)
     const OperandView vb{B, ldb, !transB, n, k, (tri & kTriB) ? 2 : (tri & kTriBt) ? 1 : 0};
-    const int npiece = (kp + kChunk - 1) / kChunk;
+    const int chunk = slice_chunk(kp), npiece = (kp + chunk - 1) / chunk;
     if (cudaError_t e = ensure_pm(ln, (size_t)(m + n) * npiece)) return e;
     const dim3 grid(npiece, (std::max(m, n) + 31) / 32, 2), blk(32, 8);
-    oz_partmax_kernel<<<grid, blk, 0, st>>>(va, vb, ln.pm, ln.pm + (size_t)m * npiece, npiece);
+    oz_partmax_kernel<<<grid, blk, 0, st>>>(va, vb, ln.pm, ln.pm + (size_t)m * npiece, npiece, chunk);
     count_launch();
     oz_slice_kernel<<<grid, blk, 0, st>>>(va, vb, ln.pm, ln.pm + (size_t)m * npiece, npiece, slA, slB, kp, ln.sc,
-                                          ln.sc + m);
+                                          ln.sc + m, chunk);
     count_launch();
     CUtensorMap ma, mb;
     if (!make_map(&ma, slA, m, kp, kTM) || !make_map(&mb, slB, n, kp, kTN)) return cudaErrorInvalidValue;
