@@ -41,10 +41,39 @@ __device__ __forceinline__ void tri_elem(int e, int n, int &i, int &j) {
 template <int L>
 __host__ __device__ constexpr int tri_count() { return L * (L + 1) / 2; }
 
+// products of the doubling inverse: [L * L / 4] for one level at a time, or for
+// L = 64 the 8-, 16- and 32-row levels side by side (4 x 64 + 2 x 256 + 1024)
+template <int L>
+__host__ __device__ constexpr int leaf_wm() { return 7 * L * L / 16; }
+
 template <int L>
 constexpr size_t leaf_smem() {
-    return (size_t)(2 * L * (L + 1) + L * kPPitch + L * L / 4 + 2 * kDiag) * sizeof(double) +
+    return (size_t)(2 * L * (L + 1) + L * kPPitch + leaf_wm<L>() + 2 * kDiag) * sizeof(double) +
            (size_t)tri_count<L>() * sizeof(int);
+}
+
+// The doubling inverse of one s x s pair of diagonal blocks at o = 2 s blk
+// (pitch p): W = L21 G11 (G11 lower: t >= j) and G21 = -G22 W (G22 lower: t <= i).
+// W's rows of L21 come from `l21` (row i at l21 + i * lp: As, or the panel while
+// its copy into As is in flight).  Columns j0 .. j1 of W only; lanes along i for
+// W (equal trips s - j), along j for G21 (equal trips i + 1).
+__device__ void inv_w(const double *l21, int lp, const double *Gs, int p, double *W, int s, int o, int j0, int j1,
+                      int tid, int nthr) {
+    const int count = (j1 - j0) * s;
+    for (int e = tid; e < count; e += nthr) {
+        const int j = j0 + e / s, i = e % s;
+        double a = 0.0;
+        for (int t = j; t < s; ++t) a = fma(l21[i * lp + t], Gs[(o + t) * p + o + j], a);
+        W[i * s + j] = a;
+    }
+}
+__device__ void inv_g(double *Gs, int p, const double *W, int s, int o, int tid, int nthr) {
+    for (int e = tid; e < s * s; e += nthr) {
+        const int i = e / s, j = e % s;
+        double a = 0.0;
+        for (int t = 0; t <= i; ++t) a = fma(Gs[(o + s + i) * p + o + s + t], W[t * s + j], a);
+        Gs[(o + s + i) * p + o + j] = -a;
+    }
 }
 
 // Warp 0: factor and invert the 8 x 8 diagonal block at Ab / Gb (pitch p):
@@ -107,8 +136,8 @@ __global__ void __launch_bounds__(kThreads) leaf_chol_inv64_kernel(double *A, do
     double *As = smem;                 // [L][kP], row-major: A, then L
     double *Gs = As + L * kP;          // [L][kP]: G
     double *Pn = Gs + L * kP;          // [L][kPPitch]: panel of the current block
-    double *Wm = Pn + L * kPPitch;     // [L * L / 4]: L21 G11 of a doubling level
-    double *rb = Wm + L * L / 4, *sb = rb + kDiag;  // 1/L(k, k) and its square, warp 0's block
+    double *Wm = Pn + L * kPPitch;     // [leaf_wm<L>()]: L21 G11 of the doubling levels
+    double *rb = Wm + leaf_wm<L>(), *sb = rb + kDiag;  // 1/L(k, k) and its square, warp 0's block
     int *tab = reinterpret_cast<int *>(sb + kDiag);  // [tri_count<L>()]: (i << 8) | j, columns from the last
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
     const bool other = (warp & 3) != 0;
@@ -178,9 +207,36 @@ __global__ void __launch_bounds__(kThreads) leaf_chol_inv64_kernel(double *A, do
                 for (int t = 0; t < kDiag; ++t) a = fma(-Pn[i * kPPitch + t], Pn[j * kPPitch + t], a);
                 As[i * kP + j] = a;
             }
+            if constexpr (L == 64) {
+                // the doubling inverse's products whose blocks are final, in the time warp 0's
+                // pivot chain leaves these warps idle (b: this block; the pair (2q, 2q + 1) of
+                // 8 rows, the quad of 16, the halves of 32)
+                const int b = b0 / kDiag;
+                double *W8 = Wm, *W16 = Wm + 4 * 64, *W32 = Wm + 4 * 64 + 2 * 256;
+                if ((b & 1) == 0)  // W of pair b / 2: L21 rows are the panel's (its copy into As is in flight)
+                    inv_w(Pn + (size_t)r0 * kPPitch, kPPitch, Gs, kP, W8 + (b / 2) * 64, 8, 16 * (b / 2), 0, 8, ot,
+                          kOthers);
+                else  // G21 of pair (b - 1) / 2: its second diagonal block was factored in the last block
+                    inv_g(Gs, kP, W8 + (b / 2) * 64, 8, 16 * (b / 2), ot, kOthers);
+                if (b == 2 || b == 6)  // W of quad b / 4: pairs inverted, panels final
+                    inv_w(As + (size_t)(32 * (b / 4) + 16) * kP + 32 * (b / 4), kP, Gs, kP, W16 + (b / 4) * 256, 16,
+                          32 * (b / 4), 0, 16, ot, kOthers);
+                if (b == 4)  // G21 of quad 0
+                    inv_g(Gs, kP, W16, 16, 0, ot, kOthers);
+                if (b >= 5)  // W of the halves, columns 0-15 then 16-31: the first half is inverted
+                    inv_w(As + (size_t)32 * kP, kP, Gs, kP, W32, 32, 0, 16 * (b - 5), 16 * (b - 4), ot, kOthers);
+            }
         }
         __syncthreads();
     }
+    if constexpr (L == 64) {  // the doubling inverse's last products (their other halves ran in the loop)
+        inv_g(Gs, kP, Wm + 3 * 64, 8, 48, tid, kThreads);  // pair 3
+        __syncthreads();
+        inv_g(Gs, kP, Wm + 4 * 64 + 256, 16, 32, tid, kThreads);  // quad 1
+        __syncthreads();
+        inv_g(Gs, kP, Wm + 4 * 64 + 2 * 256, 32, 0, tid, kThreads);  // the halves
+        __syncthreads();
+    } else
     for (int s = kDiag; s < L; s *= 2) {  // inverse by doubling
         const int per = s * s, count = (L / (2 * s)) * per;
         // W = L21 G11 (G11 lower: t >= j), lanes along i: equal trips s - j
