@@ -40,10 +40,10 @@
 //              order's grid barrier;
 //   warps 4-7  fold each block from TMEM (one thread per row); at the end of a
 //              segment they store its partial (exact 128-bit integers); a CTA
-//              designated per row tile sums the tile's partials once all are
-//              counted (exact, in any order), applies the Chebyshev recurrence
-//              and the c_k v_k accumulation in FP64, and slices the 128 new
-//              rows of v_k for the next order.
+//              designated per half of a 64-row chunk (4 of the 8 columns) sums
+//              the tile's partials once all are counted (exact, in any order),
+//              applies the Chebyshev recurrence and the c_k v_k accumulation
+//              in FP64, and slices its rows of v_k for the next order.
 // Warps 2-7 meet the grid barrier of every order.  Every wait is bounded: on a
 // timeout the CTA sets ELHL_ERR_TIMEOUT, stops, waits for its own copies and
 // MMAs, and frees TMEM.
@@ -65,6 +65,7 @@ constexpr int kTileM = 128;           // rows per tile (MMA M)
 constexpr int kKB = 64;               // K per block: 64 BF16 = one 128-byte swizzled row
 constexpr int kAStages = 10;
 constexpr int kBStages = 4;
+constexpr int kXeCap = 2048;  // chunk exponents held in shared memory (N <= 16384; larger N reads them from L2)
 constexpr int kThreads = 256;
 constexpr int kATile = kTileM * kKB * 2;  // 16 KB
 // vector operand tile: 9 slots of 8 rows (one per real column) x 128 bytes:
@@ -122,8 +123,10 @@ struct SmemLayout {
     static constexpr size_t red_off = bar_off + n_bars * 8;        // [4][8] ints: column maxima of the warps
     static constexpr size_t out_off = (red_off + 4 * 8 * 4 + 1023) / 1024 * 1024;
     static constexpr size_t misc_off = out_off + (size_t)kBTile;  // one output tile
-    static constexpr size_t bytes = misc_off + 64;
+    static constexpr size_t xe_off = misc_off + 64;                // [kXeCap] the order's chunk exponents
+    static constexpr size_t bytes = xe_off + (size_t)kXeCap * 4;
 };
+static_assert(SmemLayout::bytes + 1024 <= 227 * 1024, "shared memory of one CTA");
 
 struct Roles {  // counters every role advances in the same order
     unsigned acnt = 0;   // A stages
@@ -135,6 +138,7 @@ struct Ctx {
     unsigned char *smem;
     uint64_t *full, *empty, *bfull, *bempty, *accfull, *accempty, *done;
     int *red;
+    int *xe;
     unsigned char *out;
     uint32_t tmem;
     int *abort_flag;
@@ -360,53 +364,56 @@ __device__ __forceinline__ double i128_to_double(I128 s) {
 }
 constexpr int kNoExp = (int)0x80808080;  // the column maximum before any chunk (bytes 0x80: a memset)
 
-// The epilogue of one 64-row chunk h of v_k (rows 64 h ...) runs on the 128
-// threads of warps 4-7 of the CTA designated for it: thread t handles row
-// 64 h + (t & 63) and the columns 4 (t >> 6) ... + 3.
+// The epilogue of one 64-row chunk h of v_k (rows 64 h ...) runs in two
+// halves of 4 columns, half c on the 128 threads of warps 4-7 of the CTA
+// designated for (h, c): thread t handles row 64 h + (t & 63) and the columns
+// 4 c + 2 (t >> 6) and the next (one complex column).  The halves share
+// nothing: every column has its own scale.
 struct EpiThread {
-    int t, r, half, row;  // thread, row in the chunk, column half, global row
+    int t, r, p, row, col;  // thread, row in the chunk, column pair, global row, first column
 };
-__device__ __forceinline__ EpiThread epi_thread(int h, int t) {
-    return EpiThread{t, t & 63, t >> 6, 64 * h + (t & 63)};
+__device__ __forceinline__ EpiThread epi_thread(int h, int c, int t) {
+    return EpiThread{t, t & 63, t >> 6, 64 * h + (t & 63), 4 * c + 2 * (t >> 6)};
 }
 
-// The chunk's 64 new rows (4 columns per thread, 0 past N) cut into slices on
-// one scale 2^e per column: tile h of xs, the exponents at xe[h], their maximum
-// over the chunks in emax (non-zero columns); slice b goes to slot b + 1, slots
-// 0 and 8 stay zero.  Digits formed in shared memory, copied out in 16-byte
-// stores.  Named barrier 1 (the 128 threads).
-__device__ void slice_chunk_out(const Ctx &c, int h, const EpiThread &et, const double (&y)[4], unsigned char *xs,
-                                int *xe, int *emax) {
-    const int w = et.t >> 5;  // warps 0, 1: columns 0-3; warps 2, 3: columns 4-7
+// The half's 64 new rows (2 columns per thread, 0 past N) cut into slices on
+// one scale 2^e per column: tile h of xs (this half's rows of it), the
+// exponents at xe[h], their maximum over the chunks in emax (non-zero
+// columns); slice b goes to slot b + 1, slots 0 and 8 stay zero.  Digits formed
+// in shared memory, copied out in 16-byte stores.  Named barrier 1 (the 128
+// threads).
+__device__ void slice_chunk_out(const Ctx &c, int h, int half, const EpiThread &et, const double (&y)[2],
+                                unsigned char *xs, int *xe, int *emax) {
+    const int w = et.t >> 5;  // warps 0, 1: the half's columns 0-1; warps 2, 3: columns 2-3
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {  // largest exponent field of the column over the warp's rows
+    for (int u = 0; u < 2; ++u) {  // largest exponent field of the column over the warp's rows
         const int m = __reduce_max_sync(0xffffffffu, exp_field(y[u]));
-        if ((et.t & 31) == 0) c.red[w * 4 + u] = m;
+        if ((et.t & 31) == 0) c.red[w * 2 + u] = m;
     }
     asm volatile("bar.sync 1, 128;" ::: "memory");
-    int e[4];
+    int e[2];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-        const int be = max(c.red[(2 * et.half) * 4 + u], c.red[(2 * et.half + 1) * 4 + u]);
+    for (int u = 0; u < 2; ++u) {
+        const int be = max(c.red[(2 * et.p) * 2 + u], c.red[(2 * et.p + 1) * 2 + u]);
         e[u] = be ? be - 1022 : 0;  // |column| < 2^e (0 for a zero column)
         if (et.r == 0) {
-            xe[h * 8 + 4 * et.half + u] = e[u];
-            if (be) atomicMax(emax + 4 * et.half + u, e[u]);
+            xe[h * 8 + et.col + u] = e[u];
+            if (be) atomicMax(emax + et.col + u, e[u]);
         }
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < 2; ++u) {
         int dig[kS];
         slice7(y[u], e[u], dig);
 #pragma unroll
         for (int b = 0; b < kS; ++b)
-            *reinterpret_cast<__nv_bfloat16 *>(c.out + swz_off(8 * (b + 1) + 4 * et.half + u, et.r)) =
+            *reinterpret_cast<__nv_bfloat16 *>(c.out + swz_off(8 * (b + 1) + et.col + u, et.r)) =
                 __float2bfloat16_rn((float)dig[b]);
     }
-    asm volatile("bar.sync 1, 128;" ::: "memory");  // the tile is complete; c.red is free again
-    constexpr int kChunks = kS * 8 * 128 / 16;  // slots 1-7: 7 KB
-    for (int q = et.t; q < kChunks; q += 128) {
-        const int o = 8 * 128 + q * 16;
+    asm volatile("bar.sync 1, 128;" ::: "memory");  // the rows are complete; c.red is free again
+    constexpr int kPieces = kS * 4 * 8;  // slots 1-7 x the half's 4 rows x 8 pieces of 16 bytes
+    for (int q = et.t; q < kPieces; q += 128) {
+        const int o = (8 * (1 + q / 32) + 4 * half + (q / 8) % 4) * 128 + (q % 8) * 16;
         *reinterpret_cast<uint4 *>(xs + (size_t)h * kBTile + o) = *reinterpret_cast<const uint4 *>(c.out + o);
     }
     fence_proxy_async_global();  // read by bulk copies after the next grid barrier
@@ -422,73 +429,109 @@ __device__ __forceinline__ bool wait_count(const unsigned *cnt, unsigned target)
     return true;
 }
 
-// Epilogue of chunk h once its row tile's np segments are written: the exact
-// sum of their partials, the row's product in FP64, the recurrence and
-// accumulation of order k, and the slices of the chunk's rows of v_k for the
-// next order.  The rows of a chunk are only ever touched by this CTA (order 0
-// included), so v and acc use plain (L1) loads.
-__device__ void chunk_epilogue(const Ctx &c, const OzLaunch &L, const OrderIO &io, int h, int np, const int (&E)[8],
-                               int t) {
-    const EpiThread et = epi_thread(h, t);
+// What a half-chunk epilogue reads besides the partials, loaded before it
+// waits for them: v_{k-2} and the accumulated sum of its rows.
+struct EpiPre {
+    double vm2[2];
+    double2 acc;
+};
+__device__ __forceinline__ EpiPre epi_prefetch(const OzLaunch &L, const OrderIO &io, const EpiThread &et) {
+    EpiPre q{{0.0, 0.0}, make_double2(0.0, 0.0)};
+    if (et.row < L.N) {
+        if (io.k > 1)
+#pragma unroll
+            for (int u = 0; u < 2; ++u) q.vm2[u] = io.vm2[(size_t)et.row * 8 + et.col + u];
+        if (et.col / 2 < L.m) q.acc = L.acc[(size_t)et.row * L.m + et.col / 2];
+    }
+    return q;
+}
+
+// Epilogue of half c of chunk h once its row tile's np segments are written:
+// the exact sum of their partials, the row's product in FP64, the recurrence
+// and accumulation of order k, and the slices of the half's rows of v_k for the
+// next order.  The rows and columns of a half are only ever touched by this
+// CTA (order 0 included), so v and acc use plain (L1) loads.
+__device__ void chunk_epilogue(const Ctx &c, const OzLaunch &L, const OrderIO &io, int h, int half, int np,
+                               const int (&E)[8], const EpiThread &et, const EpiPre &pre) {
     const int rt = h >> 1, trow = (h & 1) * 64 + et.r;  // row tile, row in it
-    I128 S[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) S[u] = I128{0, 0ull};
+    I128 S[2] = {I128{0, 0ull}, I128{0, 0ull}};
     const longlong2 *p0 = reinterpret_cast<const longlong2 *>(L.part) +
-                          ((size_t)L.part_base[rt] * kTileM + trow) * 8 + 4 * et.half;
-    for (int s0 = 0; s0 < np; s0 += 4) {  // up to 16 loads in flight
-        longlong2 v[4][4];
+                          ((size_t)L.part_base[rt] * kTileM + trow) * 8 + et.col;
+    for (int s0 = 0; s0 < np; s0 += 8) {  // up to 16 loads in flight
+        longlong2 v[8][2];
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < 8; ++j)
             if (s0 + j < np)
 #pragma unroll
-                for (int u = 0; u < 4; ++u) v[j][u] = __ldcg(p0 + (size_t)(s0 + j) * kTileM * 8 + u);
+                for (int u = 0; u < 2; ++u) v[j][u] = __ldcg(p0 + (size_t)(s0 + j) * kTileM * 8 + u);
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < 8; ++j)
             if (s0 + j < np)
 #pragma unroll
-                for (int u = 0; u < 4; ++u) add128(S[u], I128{v[j][u].x, (unsigned long long)v[j][u].y});
+                for (int u = 0; u < 2; ++u) add128(S[u], I128{v[j][u].x, (unsigned long long)v[j][u].y});
     }
     const double rs = L.rscale[et.row];
-    double y[4];
+    double y[2];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-        const int col = 4 * et.half + u;
+    for (int u = 0; u < 2; ++u) {
+        const int col = et.col + u;
         const double yv = i128_to_double(S[u]) * (pow2(max(E[col], -900) - 64) * rs);
         double v = 0.0;  // v_k = Hs v_{k-1} (k = 1), 2 Hs v_{k-1} - v_{k-2} after; rows past N stay zero
         if (et.row < L.N) {
-            v = io.k == 1 ? yv : 2.0 * yv - io.vm2[(size_t)et.row * 8 + col];
+            v = io.k == 1 ? yv : 2.0 * yv - pre.vm2[u];
             io.vk[(size_t)et.row * 8 + col] = v;
         }
         y[u] = v;
     }
-    if (et.row < L.N)
-        for (int cc = 0; cc < 2 && 2 * et.half + cc < L.m; ++cc) {  // acc += c_k v_k, complex column
-            double2 *ap = L.acc + (size_t)et.row * L.m + 2 * et.half + cc;
-            double2 a = *ap;
-            const double vr = y[2 * cc], vi = y[2 * cc + 1];
-            a.x += io.cre * vr - io.cim * vi;
-            a.y += io.cre * vi + io.cim * vr;
-            *ap = a;
-        }
-    slice_chunk_out(c, h, et, y, io.xs_out, io.xe_out, io.emax_out);
+    if (et.row < L.N && et.col / 2 < L.m) {  // acc += c_k v_k, the thread's complex column
+        double2 a = pre.acc;
+        a.x += io.cre * y[0] - io.cim * y[1];
+        a.y += io.cre * y[1] + io.cim * y[0];
+        L.acc[(size_t)et.row * L.m + et.col / 2] = a;
+    }
+    slice_chunk_out(c, h, half, et, y, io.xs_out, io.xe_out, io.emax_out);
+}
+
+// A row tile's partial (exact 128-bit integers, 8 columns per row) into its
+// slot.  It is counted at its row tile later (release_partials), once the next
+// segment's work has given the stores time to complete.
+__device__ __forceinline__ void store_partial(const OzLaunch &L, int slot, int t, const I128 (&A)[8]) {
+    longlong2 *part = reinterpret_cast<longlong2 *>(L.part) + ((size_t)slot * kTileM + t) * 8;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) part[u] = make_longlong2(A[u].hi, (long long)A[u].lo);
+}
+// the stored partial of row tile `tile` (if >= 0) made visible, then counted
+__device__ __forceinline__ void release_partial(const OzLaunch &L, int &tile, int t) {
+    if (tile < 0) return;
+    __threadfence();
+    asm volatile("bar.sync 1, 128;" ::: "memory");
+    if (t == 0) atomicAdd(&L.tile_cnt[tile], 1u);
+    tile = -1;
 }
 
 // The CTA's segments: each 64-K block's weight sums folded, with that chunk's
 // vector scale, into one exact 128-bit integer per row and column, stored as
-// the segment's partial and counted at its row tile.  Then the epilogues of the
-// 64-row chunks this CTA is designated for (chunk h by CTA floor(h grid /
-// chunks): spread over the grid, at most one per CTA while chunks <= grid),
-// each once its row tile's segments are all counted.
+// the segment's partial and counted at its row tile.  The chunk exponents of
+// the order's vector are read once into shared memory.  Then the epilogues of
+// the half-chunks this CTA is designated for (half-chunk q = 2 h + c by CTA
+// floor(q grid / halves): spread over the grid, at most one per CTA while
+// halves <= grid), each once its row tile's segments are all counted.
 __device__ void flush_and_epilogue(const Ctx &c, const OzLaunch &L, const OrderIO &io, Roles &r, bool rev) {
     const int t = threadIdx.x - 128;  // 0 .. 127: TMEM lane / row in the tile
     const int warp = threadIdx.x >> 5;
     const int s0 = L.seg_begin[blockIdx.x], s1 = L.seg_begin[blockIdx.x + 1];
+    const int nkb = (L.N + kKB - 1) / kKB, ntiles = (L.N + kTileM - 1) / kTileM;
     // every block of this order is added exactly in the frame 2^(E - 64) of its
     // column's largest chunk scale 2^E
     int E[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) E[u] = __ldcg(io.emax_in + u);
+    const bool xe_smem = nkb * 8 <= kXeCap;
+    if (xe_smem) {
+        for (int i = t; i < nkb * 8; i += 128) c.xe[i] = __ldcg(io.xe_in + i);
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+    }
+    int pend = -1;  // row tile of the stored, not yet counted partial
     for (int qi = 0; qi < s1 - s0; ++qi) {
         const OzSeg sg = L.segs[walk_seg(s0, s1, qi, rev)];
         I128 A[8];
@@ -516,23 +559,26 @@ __device__ void flush_and_epilogue(const Ctx &c, const OzLaunch &L, const OrderI
             }
             flush_block(c.tmem + ((uint32_t)((warp & 3) * 32) << 16) + tb * kAccCols, H, Lo);
             asm volatile("tcgen05.fence::before_thread_sync;");
-            mbar_arrive(&c.accempty[tb]);
+            __syncwarp();
+            if ((t & 31) == 0) mbar_arrive(&c.accempty[tb]);  // one arrival per warp: its loads are done
             ++r.gcnt;
-            const int *eg = io.xe_in + (size_t)kb * 8;  // the block's vector chunk exponents
 #pragma unroll
-            for (int u = 0; u < 8; ++u) add128(A[u], group_term(H[u], Lo[u], max(0, E[u] - __ldcg(eg + u))));
+            for (int u = 0; u < 8; ++u) {  // the block's vector chunk exponents
+                const int ec = xe_smem ? c.xe[kb * 8 + u] : __ldcg(io.xe_in + (size_t)kb * 8 + u);
+                add128(A[u], group_term(H[u], Lo[u], max(0, E[u] - ec)));
+            }
         }
-        longlong2 *part = reinterpret_cast<longlong2 *>(L.part) +
-                          ((size_t)(L.part_base[sg.rt] + sg.slot) * kTileM + t) * 8;
-#pragma unroll
-        for (int u = 0; u < 8; ++u) part[u] = make_longlong2(A[u].hi, (long long)A[u].lo);
-        __threadfence();
-        asm volatile("bar.sync 1, 128;" ::: "memory");
-        if (t == 0) atomicAdd(&L.tile_cnt[sg.rt], 1u);
+        release_partial(L, pend, t);
+        store_partial(L, L.part_base[sg.rt] + sg.slot, t, A);
+        pend = sg.rt;
     }
-    const int nch = 2 * ((L.N + kTileM - 1) / kTileM), G = gridDim.x;
-    const int h1 = (int)(((long long)(blockIdx.x + 1) * nch + G - 1) / G);
-    for (int h = (int)(((long long)blockIdx.x * nch + G - 1) / G); h < h1; ++h) {
+    release_partial(L, pend, t);
+    const int nhc = 4 * ntiles, G = gridDim.x;
+    const int q1 = (int)(((long long)(blockIdx.x + 1) * nhc + G - 1) / G);
+    for (int q = (int)(((long long)blockIdx.x * nhc + G - 1) / G); q < q1; ++q) {
+        const int h = q >> 1, half = q & 1;
+        const EpiThread et = epi_thread(h, half, t);
+        const EpiPre pre = epi_prefetch(L, io, et);
         const int np = L.part_count[h >> 1];
         // the count only grows (np per order, zero at the launch): order k waits for k np
         if (t == 0) *c.last_flag = wait_count(&L.tile_cnt[h >> 1], (unsigned)(np * io.k)) ? 1u : 0u;
@@ -544,36 +590,36 @@ __device__ void flush_and_epilogue(const Ctx &c, const OzLaunch &L, const OrderI
             return;
         }
         __threadfence();
-        chunk_epilogue(c, L, io, h, np, E, t);
+        chunk_epilogue(c, L, io, h, half, np, E, et, pre);
     }
 }
 
 // order 0: v_0 = s phi (s: pending renormalisation factor), acc = c_0 v_0, and
-// the slices of v_0, by warps 4-7 of the CTA designated for each 64-row chunk
+// the slices of v_0, by warps 4-7 of the CTA designated for each half-chunk
 __device__ void order_zero(const Ctx &c, const OzLaunch &L) {
     const int t = threadIdx.x - 128;
-    const int nch = 2 * ((L.N + kTileM - 1) / kTileM), G = gridDim.x;
+    const int nhc = 4 * ((L.N + kTileM - 1) / kTileM), G = gridDim.x;
     const double2 c0 = L.coef[0];
-    const int h1 = (int)(((long long)(blockIdx.x + 1) * nch + G - 1) / G);
-    for (int h = (int)(((long long)blockIdx.x * nch + G - 1) / G); h < h1; ++h) {
-        const EpiThread et = epi_thread(h, t);
-        double y[4] = {0.0, 0.0, 0.0, 0.0};
-        if (et.row < L.N)
-            for (int cc = 0; cc < 2 && 2 * et.half + cc < L.m; ++cc) {
-                const int col = 2 * et.half + cc;
-                double2 p = L.phi[(size_t)et.row * L.m + col];
-                if (L.scale) {
-                    const double sc = L.scale[col % L.P];
-                    p.x *= sc;
-                    p.y *= sc;
-                }
-                L.v[(size_t)et.row * 8 + 2 * col] = p.x;
-                L.v[(size_t)et.row * 8 + 2 * col + 1] = p.y;
-                L.acc[(size_t)et.row * L.m + col] = make_double2(c0.x * p.x - c0.y * p.y, c0.x * p.y + c0.y * p.x);
-                y[2 * cc] = p.x;
-                y[2 * cc + 1] = p.y;
+    const int q1 = (int)(((long long)(blockIdx.x + 1) * nhc + G - 1) / G);
+    for (int q = (int)(((long long)blockIdx.x * nhc + G - 1) / G); q < q1; ++q) {
+        const int h = q >> 1, half = q & 1;
+        const EpiThread et = epi_thread(h, half, t);
+        double y[2] = {0.0, 0.0};
+        const int cc = et.col / 2;  // the thread's complex column
+        if (et.row < L.N && cc < L.m) {
+            double2 p = L.phi[(size_t)et.row * L.m + cc];
+            if (L.scale) {
+                const double sc = L.scale[cc % L.P];
+                p.x *= sc;
+                p.y *= sc;
             }
-        slice_chunk_out(c, h, et, y, L.xs[0], L.xe[0], L.emax[0]);
+            L.v[(size_t)et.row * 8 + 2 * cc] = p.x;
+            L.v[(size_t)et.row * 8 + 2 * cc + 1] = p.y;
+            L.acc[(size_t)et.row * L.m + cc] = make_double2(c0.x * p.x - c0.y * p.y, c0.x * p.y + c0.y * p.x);
+            y[0] = p.x;
+            y[1] = p.y;
+        }
+        slice_chunk_out(c, h, half, et, y, L.xs[0], L.xe[0], L.emax[0]);
     }
 }
 
@@ -594,6 +640,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     c.done = c.accempty + 2;
     c.red = reinterpret_cast<int *>(c.smem + SmemLayout::red_off);
     c.out = c.smem + SmemLayout::out_off;
+    c.xe = reinterpret_cast<int *>(c.smem + SmemLayout::xe_off);
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(c.smem + SmemLayout::misc_off);
     c.abort_flag = reinterpret_cast<int *>(tmem_slot + 1);
     c.last_flag = reinterpret_cast<unsigned *>(tmem_slot + 2);
@@ -609,7 +656,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         for (int s = 0; s < 2; ++s) {
             mbar_init(&c.accfull[s], 1);
-            mbar_init(&c.accempty[s], 128);
+            mbar_init(&c.accempty[s], 4);  // one arrival per flush warp
         }
         mbar_init(c.done, 1);
         *c.abort_flag = 0;

@@ -69,10 +69,13 @@ def test_oz64_moving_nuclei_vs_taylor_oracle(elhl, oracle_mod):
     assert st.phases == 1
 
 
-def test_oz64_moving_nuclei_matches_fp64_n1860(elhl):
-    """N = 1860 (15 row tiles, several segments per tile, partial last tile and
-    block), two moving-nuclei steps: OZ64 against the FP64 pipe."""
-    sysm = systems.cubic_cluster(n_atoms=600, seed=11)
+@pytest.mark.parametrize("n_atoms", [600, 300])
+def test_oz64_moving_nuclei_matches_fp64(elhl, n_atoms):
+    """N = 1860 (15 row tiles, 68 rows in the last: several segments per tile,
+    partial last tile and block) and N = 930 (8 row tiles, 34 rows in the last:
+    its diagonal tile has one 64-K block and no second transposed half), two
+    moving-nuclei steps: OZ64 against the FP64 pipe."""
+    sysm = systems.cubic_cluster(n_atoms=n_atoms, seed=11)
     homo = systems.fermi_state(sysm, sysm.fragment_atoms("E"))
     coords = np.stack([systems.perturbed_coords(sysm.coords, i, seed=5) for i in range(3)])
     out = {}

@@ -5,7 +5,8 @@ dynemol_gb300/csrc/ozgemm.cu), checked on the CPU before any GPU run:
 * the block schedule (oz_schedule): every 128 x 64 block of the operator is
   given to exactly one CTA, CTAs differ by at most one block, a row tile's
   segments are numbered in K order and their partial slots fit the partial
-  buffer, and every row tile has one CTA designated for its epilogue;
+  buffer, and every half of a 64-row chunk (4 of its 8 columns) has one CTA
+  designated for its epilogue;
 * the arithmetic: operands cut into 7 slices of 8 bits on power-of-two scales
   exactly as the kernels do (slice7: one rounding to a 64-bit integer, then
   balanced base-256 digits; operator rows one scale each, vector columns one
@@ -75,8 +76,9 @@ def test_schedule_source_matches_replay():
 def test_schedule_covers_blocks_once(n):
     """Every 128 x 64 block of the operator (rows and K below n) goes to exactly
     one CTA, CTAs differ by at most one block, a row tile's segments are
-    numbered in K order, partial slots fit the buffer, and the epilogue of row
-    tile rt has one designated CTA, floor(rt grid / tiles)."""
+    numbered in K order, partial slots fit the buffer, and every half of a
+    64-row chunk (4 of its 8 columns) has one designated CTA, floor(q grid /
+    halves)."""
     segs, begin, base, count = schedule(n, GRID)
     nkb, ntiles = -(-n // KB), -(-n // TILE)
     seen = np.zeros((ntiles, nkb), dtype=int)
@@ -92,9 +94,11 @@ def test_schedule_covers_blocks_once(n):
         assert all(mine[i][2] == mine[i + 1][1] for i in range(len(mine) - 1))
         assert base[rt] + count[rt] <= len(segs)
     assert len(segs) <= GRID + ntiles
-    designated = [[rt for rt in range(-(-b * ntiles // GRID), -(-(b + 1) * ntiles // GRID))] for b in range(GRID)]
-    assert sorted(rt for d in designated for rt in d) == list(range(ntiles))
-    assert all(rt * GRID // ntiles == b for b, d in enumerate(designated) for rt in d)
+    nhc = 4 * ntiles  # half-chunks: 64 rows x 4 columns
+    designated = [list(range(-(-b * nhc // GRID), -(-(b + 1) * nhc // GRID))) for b in range(GRID)]
+    assert sorted(q for d in designated for q in d) == list(range(nhc))
+    assert all(q * GRID // nhc == b for b, d in enumerate(designated) for q in d)
+    assert "const int nhc = 4 * ntiles, G = gridDim.x;" in OZ
 
 
 def scale_exp(mx):
