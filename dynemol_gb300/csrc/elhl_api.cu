@@ -1656,7 +1656,6 @@ int oz_run(ChebPlan &pl) {
     L.part = oz.part;
     L.tile_cnt = oz.cnt;
     L.bar_count = g_ctx.bar;
-    L.bar_gen = g_ctx.bar + 1;
     L.error = g_ctx.err;
     L.barrier_ns = g_dbg_barrier_ns;
     L.exit_cta1 = g_dbg_exit_cta1;

@@ -192,7 +192,7 @@ struct OzLaunch {
     const int *part_count;       // [tiles] segments of a row tile
     double *part;                // partial tiles [slot][128][8] as 128-bit integers (16 bytes each)
     unsigned *tile_cnt;          // [tiles] segments written, over all orders of the launch
-    unsigned *bar_count, *bar_gen;
+    unsigned *bar_count;         // grid-barrier arrivals, over all orders of the launch (0 at the launch)
     int *error;
     unsigned long long barrier_ns;  // grid-barrier limit (0: default)
     int exit_cta1;                  // test hook: 1 + the CTA that leaves before its first barrier

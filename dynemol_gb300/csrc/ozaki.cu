@@ -151,31 +151,28 @@ __device__ __forceinline__ void set_abort(const Ctx &c, int *err) {
     atomicExch(err, (int)ELHL_ERR_TIMEOUT);
 }
 
-// The bounded grid barrier of grid_sync.cuh among the 192 threads of warps 2-7
-// (named barrier 2) instead of the whole CTA: thread 64 arrives for the CTA.
-__device__ __forceinline__ bool grid_barrier_sub(unsigned *count, unsigned *gen, unsigned nblocks, int *err,
+// Grid barrier among the 192 threads of warps 2-7 (named barrier 2): thread
+// 64 arrives for the CTA by a release add to a count that only grows (zero at
+// the launch) and waits, with acquire loads, until all nblocks CTAs have
+// arrived at this barrier (the count reaches `target` = nblocks x barriers so
+// far).  No reset and no generation word: the last arrival itself releases
+// the others.  Bounded: false (with ELHL_ERR_TIMEOUT) after limit_ns.
+__device__ __forceinline__ bool grid_barrier_sub(unsigned *count, unsigned target, int *err,
                                                  unsigned long long limit_ns) {
     asm volatile("bar.sync 2, 192;" ::: "memory");
     if (threadIdx.x == 64) {
-        volatile unsigned *vgen = gen;
-        const unsigned g = *vgen;
-        __threadfence();
-        const unsigned prev = atomicAdd(count, 1u);
-        if (prev == nblocks - 1) {
-            atomicExch(count, 0u);
-            __threadfence();
-            atomicAdd(gen, 1u);
-        } else {
-            const unsigned long long t0 = globaltimer_ns();
-            while (*vgen == g) {
-                if (globaltimer_ns() - t0 > limit_ns) {
-                    atomicExch(err, ELHL_ERR_TIMEOUT);
-                    break;
-                }
-                __nanosleep(40);
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(count) : "memory");
+        const unsigned long long t0 = globaltimer_ns();
+        while (true) {
+            unsigned v;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(count) : "memory");
+            if (v >= target) break;
+            if (globaltimer_ns() - t0 > limit_ns) {
+                atomicExch(err, ELHL_ERR_TIMEOUT);
+                break;
             }
+            __nanosleep(20);
         }
-        __threadfence();
     }
     asm volatile("bar.sync 2, 192;" ::: "memory");
     return *(volatile int *)err == 0;
@@ -682,7 +679,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // barrier.  So the next order's loads and MMAs overlap the barrier.  Warps
     // 2-7 meet every grid barrier on named barrier 2.
     bool ok = true;
-    if (warp >= 2) ok = grid_barrier_sub(L.bar_count, L.bar_gen, G, L.error, bar_ns);
+    if (warp >= 2) ok = grid_barrier_sub(L.bar_count, (unsigned)G, L.error, bar_ns);
     // the sliced vector v_k is in buffer k % 3
     for (int k = 1; ok && k <= L.K; ++k) {
         const int bin = (k + 2) % 3, bout = k % 3;
@@ -716,7 +713,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             io.emax_out = L.emax[bout];
             flush_and_epilogue(c, L, io, r, k & 1);
         }
-        ok = grid_barrier_sub(L.bar_count, L.bar_gen, G, L.error, bar_ns) && !aborted(c);
+        ok = grid_barrier_sub(L.bar_count, (unsigned)G * (unsigned)(k + 1), L.error, bar_ns) && !aborted(c);
         if (!ok && threadIdx.x == 64) atomicExch(c.abort_flag, 1);  // stops this CTA's producer and MMA issuer
     }
     // drain: copies issued into the A ring and every MMA complete before the CTA

@@ -455,16 +455,20 @@ cudaError_t ozgemm(int m, int n, int k, double alpha, const double *A, int lda, 
     if (lane < 0 || lane > 1 || k <= 0) return cudaErrorInvalidValue;
     Lane &ln = g_lane[lane];
     const int kp = round_up(k, 8);  // 16-byte row stride of the slices
-    const size_t sa = (size_t)kS * m * kp, sb = (size_t)kS * n * kp;
-    if (cudaError_t e = ensure(ln, sa + sb, (size_t)m + n)) return e;
-    __nv_bfloat16 *slA = ln.sl, *slB = ln.sl + sa;  // sa is a multiple of 8 elements: 16-byte aligned
     // op(A) rows: A(i, l) (K along A's rows) or A^T: A(l, i) (K along A's columns)
     const OperandView va{A, lda, transA, m, k, (tri & kTriA) ? 1 : (tri & kTriAt) ? 2 : 0};
     // op(B) columns: B(l, j) (K along B's columns) or B^T: B(j, l) (K along B's rows)
     const OperandView vb{B, ldb, !transB, n, k, (tri & kTriB) ? 2 : (tri & kTriBt) ? 1 : 0};
+    // op(B) = op(A)^T (the Schur update L21 L21^T): op(B)^T has op(A)'s rows, so
+    // one set of slices and scales serves both operands
+    const bool same = A == B && lda == ldb && va.kcontig == vb.kcontig && m == n && va.mask == vb.mask;
+    const size_t sa = (size_t)kS * m * kp, sb = same ? 0 : (size_t)kS * n * kp;
+    if (cudaError_t e = ensure(ln, sa + sb, (size_t)m + n)) return e;
+    __nv_bfloat16 *slA = ln.sl, *slB = same ? ln.sl : ln.sl + sa;  // sa is a multiple of 8 elements: 16-byte aligned
+    double *scB = same ? ln.sc : ln.sc + m;
     const int chunk = slice_chunk(kp), npiece = (kp + chunk - 1) / chunk;
     if (cudaError_t e = ensure_pm(ln, (size_t)(m + n) * npiece)) return e;
-    const dim3 grid(npiece, (std::max(m, n) + 31) / 32, 2), blk(32, 8);
+    const dim3 grid(npiece, (std::max(m, n) + 31) / 32, same ? 1 : 2), blk(32, 8);
     oz_partmax_kernel<<<grid, blk, 0, st>>>(va, vb, ln.pm, ln.pm + (size_t)m * npiece, npiece, chunk);
     count_launch();
     oz_slice_kernel<<<grid, blk, 0, st>>>(va, vb, ln.pm, ln.pm + (size_t)m * npiece, npiece, slA, slB, kp, ln.sc,
@@ -475,8 +479,7 @@ cudaError_t ozgemm(int m, int n, int k, double alpha, const double *A, int lda, 
     const size_t smem = ozgemm_smem_bytes();
     cudaError_t e = cudaFuncSetAttribute(ozgemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    OzGemmArgs g{m, n, k, alpha, beta, C, ldc, tri, (m + kTM - 1) / kTM, (n + kTN - 1) / kTN, ln.sc, ln.sc + m,
-                 ln.err};
+    OzGemmArgs g{m, n, k, alpha, beta, C, ldc, tri, (m + kTM - 1) / kTM, (n + kTN - 1) / kTN, ln.sc, scB, ln.err};
     ozgemm_kernel<<<g.gx * g.gy, kThreads, smem, st>>>(ma, mb, g);
     count_launch();
     return cudaGetLastError();
