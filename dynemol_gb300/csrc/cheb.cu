@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(kBlock, 1) cheb_kernel(ChebLaunch L) {
                     }
                 }
             }
-            if (!grid_barrier(L.bar_count, L.bar_gen, G, L.error, bar_ns)) return;
+            if (!grid_barrier(L.bar_count, G, L.error, bar_ns)) return;
         }
     }
 }
@@ -797,7 +797,7 @@ __global__ void __launch_bounds__(kBlock, 1) cheb_df_kernel(ChebLaunch L) {
                 for (int g = 0; g < pb.m / MG; ++g)
                     implicit_phase_df<MG>(L, pb, s0, s1, k, ph, g, s_v, s_part, cre, cim);
             }
-            if (!grid_barrier(L.bar_count, L.bar_gen, G, L.error, bar_ns)) return;
+            if (!grid_barrier(L.bar_count, G, L.error, bar_ns)) return;
         }
     }
 }

@@ -447,7 +447,6 @@ int run_taylor(const double *Hp, int N, int ld, TaylorBuffers &tb, int P, const 
     L.t_final = tb.tfinal;
     L.partials = g_ctx.partials;
     L.bar_count = g_ctx.bar;
-    L.bar_gen = g_ctx.bar + 1;
     L.error = g_ctx.err;
     CU_TRY(cudaEventRecord(g_ctx.ev[0], st));
     CU_TRY(launch_taylor(L, g_ctx.grid, kTaylorBlock, st));
@@ -1562,7 +1561,6 @@ ChebLaunch plan_launch(const ChebPlan &pl) {
     L.max_ld = pl.max_ld;
     L.grid = pl.grid;
     L.bar_count = g_ctx.bar;
-    L.bar_gen = g_ctx.bar + 1;
     L.error = g_ctx.err;
     L.prob_seg0 = pl.d_prob_seg0;
     L.parity = pl.parity;
@@ -1687,7 +1685,6 @@ int cheb_run(ChebPlan &pl) {
     L.max_ld = pl.max_ld;
     L.grid = pl.grid;
     L.bar_count = g_ctx.bar;
-    L.bar_gen = g_ctx.bar + 1;
     L.error = g_ctx.err;
     L.prob_seg0 = pl.d_prob_seg0;
     L.parity = pl.parity;

@@ -80,8 +80,7 @@ struct TaylorLaunch {
     // scratch
     double *partials;     // [2][nparticles][grid][4]
     double *pop_partials; // [grid][nparticles][kMaxFrag+1]
-    unsigned *bar_count;  // grid barrier
-    unsigned *bar_gen;
+    unsigned *bar_count;  // grid barrier: two words, one 64-bit count (8-byte aligned, zero at the launch)
     int *error;           // global error flag
 };
 constexpr int kSlots = 6;
@@ -130,7 +129,7 @@ struct ChebLaunch {
     const int *seg_begin;   // [grid + 1]: CTA c owns segs[seg_begin[c] .. seg_begin[c+1])
     const int *prob_seg0;   // [nprob + 1]: problem q owns segs[prob_seg0[q] .. prob_seg0[q+1])
     int kmax, max_ld, grid, parity;
-    unsigned *bar_count, *bar_gen;
+    unsigned *bar_count;    // grid barrier: two words, one 64-bit count (8-byte aligned, zero at the launch)
     int *error;
     double *seg_pops;       // [nseg][kMaxCols][kMaxFrag+1] read-out partials
     double *pops;           // this step's populations block, or nullptr

@@ -34,7 +34,7 @@ struct LzArgs {
     double *t;         // [2][ld] implicit intermediates G^T q, h G^T q
     double *part;      // [2][grid] per-CTA partial sums
     double *rec;       // alpha [k], beta [k], steps used [1]
-    unsigned *bar_count, *bar_gen;
+    unsigned *bar_count;  // grid barrier: two words, one 64-bit count (zero at the launch)
     int *err;
 };
 
@@ -152,7 +152,7 @@ __global__ void __launch_bounds__(kLzThreads) lanczos64_kernel(const LzArgs a) {
     }
     acc = block_sum(acc, red);
     if (threadIdx.x == 0) pb[blockIdx.x] = acc;
-    if (!grid_barrier(a.bar_count, a.bar_gen, g, a.err)) return;
+    if (!grid_barrier(a.bar_count, g, a.err)) return;
     double sq = 0.0;  // q_j = r[j & 3] * sq
     grid_sum(pb, g, true, red, &sq);
     double sp = 0.0, bprev = 0.0;              // q_{j-1} = r[(j + 3) & 3] * sp
@@ -165,13 +165,13 @@ __global__ void __launch_bounds__(kLzThreads) lanczos64_kernel(const LzArgs a) {
         } else {
             double *t1 = a.t, *t2 = a.t + ld;
             product(a.G, ld, n, 1, rq, t1, 1.0, nullptr, 0.0, xs, red);  // G^T r
-            if (!grid_barrier(a.bar_count, a.bar_gen, g, a.err)) return;
+            if (!grid_barrier(a.bar_count, g, a.err)) return;
             product(a.H, ld, n, 0, t1, t2, 1.0, nullptr, 0.0, xs, red);  // h (.)
-            if (!grid_barrier(a.bar_count, a.bar_gen, g, a.err)) return;
+            if (!grid_barrier(a.bar_count, g, a.err)) return;
             part = product(a.Gt, ld, n, 2, t2, rw, sq, rq, sq, xs, red);  // G (.) sq
         }
         if (threadIdx.x == 0) pa[blockIdx.x] = part;
-        if (!grid_barrier(a.bar_count, a.bar_gen, g, a.err)) return;
+        if (!grid_barrier(a.bar_count, g, a.err)) return;
         const double alpha = grid_sum(pa, g, false, red);
         // r_j = w - alpha q_j - beta_{j-1} q_{j-1}
         acc = 0.0;
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(kLzThreads) lanczos64_kernel(const LzArgs a) {
         }
         acc = block_sum(acc, red);
         if (threadIdx.x == 0) pb[blockIdx.x] = acc;
-        if (!grid_barrier(a.bar_count, a.bar_gen, g, a.err)) return;
+        if (!grid_barrier(a.bar_count, g, a.err)) return;
         double ibeta = 0.0;
         const double beta = grid_sum(pb, g, true, red, &ibeta);
         const bool stop = !(beta > 1e-10 * (fabs(alpha) + 1.0));  // invariant subspace found
@@ -219,7 +219,7 @@ cudaError_t launch_lanczos64(int n, int ld, int k, const double *H, const double
     }
     const size_t smem = (size_t)(std::min(n, kXsCap) + kRedSlots) * sizeof(double);
     if (grid > part_cap || k < 1 || n < 1 || (G && !Gt)) return cudaErrorInvalidValue;
-    LzArgs a{n, ld, k, H, G, Gt, r, t, part, rec, bar, bar + 1, err};
+    LzArgs a{n, ld, k, H, G, Gt, r, t, part, rec, bar, err};
     void *args[] = {&a};
     cudaError_t e = cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), st);
     if (e == cudaSuccess)

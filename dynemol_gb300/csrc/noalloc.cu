@@ -37,7 +37,7 @@ struct FixedScratch {
     double2 slots[kSlots * 2 * kFixedMaxN];  // one particle: 6 slots x (bra, ket)
     double partials[2 * 2 * kFixedMaxGrid * 16];
     TaylorParticle part[2];
-    unsigned bar[2];
+    alignas(8) unsigned bar[2];  // the grid barrier's 64-bit count
     int err;
 };
 
@@ -126,7 +126,6 @@ extern "C" int elhl_propagate_fixed_scratch(int n, const double *d_H, int ld, el
     L.t_final = nullptr;
     L.partials = fs->partials;
     L.bar_count = fs->bar;
-    L.bar_gen = fs->bar + 1;
     L.error = &fs->err;
     FX_TRY(launch_taylor(L, grid, kTaylorBlock, st));
     // Status first: the caller's Psi is overwritten only by a converged step,

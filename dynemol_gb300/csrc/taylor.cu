@@ -310,7 +310,7 @@ __global__ void __launch_bounds__(kTaylorBlock, 1) taylor_kernel(TaylorLaunch L)
             L.partials[(((size_t)parity * PMAX + p) * G + blockIdx.x) * PW + q] = cta_rec[p][q];
         }
 
-        if (!grid_barrier(L.bar_count, L.bar_gen, G, L.error)) break;
+        if (!grid_barrier(L.bar_count, G, L.error)) break;
 
         // ------------------------------------------------ phase B: reduce + advance
         // warp p reduces particle p's records in a fixed order (identical in every CTA)
@@ -435,7 +435,7 @@ __global__ void __launch_bounds__(kTaylorBlock, 1) taylor_kernel(TaylorLaunch L)
             const int p = tid / PW, q = tid % PW;
             L.partials[(((size_t)parity * PMAX + p) * G + blockIdx.x) * PW + q] = cta_rec[p][q];
         }
-        if (!grid_barrier(L.bar_count, L.bar_gen, G, L.error)) break;
+        if (!grid_barrier(L.bar_count, G, L.error)) break;
         if (warp < P) {
             const int p = warp;
             double v[kMaxFrag + 1];
