@@ -19,10 +19,10 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
 // `count` is two 32-bit words read as one 64-bit count (8-byte aligned, zero
 // at the launch).  Thread 0 arrives for its CTA by a release add, which
 // returns the arrivals before it: all nblocks arrivals of one barrier lie in
-// [nblocks e, nblocks (e + 1)), so the CTA waits, with acquire loads, until the
-// count reaches nblocks (e + 1).  The last arrival itself releases the others
-// (no reset, no generation word).  Returns false (and sets *err =
-// ELHL_ERR_TIMEOUT) if the other CTAs do not arrive within limit_ns
+// [nblocks e, nblocks (e + 1)), so the CTA polls (relaxed loads, then one
+// acquire fence) until the count reaches nblocks (e + 1).  The last arrival
+// itself releases the others (no reset, no generation word).  Returns false
+// (and sets *err = ELHL_ERR_TIMEOUT) if the other CTAs do not arrive within limit_ns
 // (kBarrierNs unless the launch sets a shorter limit), so a stuck launch ends
 // with an error instead of hanging.
 __device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned nblocks, int *err,
@@ -36,14 +36,15 @@ __device__ __forceinline__ bool grid_barrier(unsigned *count, unsigned nblocks, 
         const unsigned long long t0 = globaltimer_ns();
         while (true) {
             unsigned long long v;
-            asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(c) : "memory");
+            asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(c) : "memory");
             if (v >= target) break;
             if (globaltimer_ns() - t0 > limit_ns) {
                 atomicExch(err, ELHL_ERR_TIMEOUT);
                 break;
             }
-            __nanosleep(20);
+            __nanosleep(40);
         }
+        __threadfence();  // acquire: the other CTAs' writes before their arrivals
     }
     __syncthreads();
     return *(volatile int *)err == 0;

@@ -27,7 +27,7 @@ def test_barrier_sources_match_replay():
     gs = _src("grid_sync.cuh")
     assert "atom.add.release.gpu.global.u64 %0, [%1], 1;" in gs
     assert "const unsigned long long target = (prev / nblocks + 1) * nblocks;" in gs
-    assert "ld.acquire.gpu.global.u64" in gs
+    assert "ld.relaxed.gpu.global.u64" in gs and "__threadfence();  // acquire" in gs
     oz = _src("ozaki.cu")
     assert "red.release.gpu.global.add.u32 [%0], 1;" in oz
     assert "grid_barrier_sub(L.bar_count, (unsigned)G, L.error, bar_ns)" in oz
