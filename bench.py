@@ -263,11 +263,13 @@ def run_ours(args, rank, world):
         per_launch_orders = orders / max(1, K) / m
         bytes_per_launch = per_launch_orders * (bH * elems + vec * N * m)
         flops_per_launch = per_launch_orders * 4.0 * elems * m
-        if args.precision == "oz64" and not implicit:
+        if args.precision == "oz64" and not implicit and N == 3720:
             # DRAM traffic per matrix element and order measured by ncu on the same kernel
-            # at N = 2790 (15.86 GB read + 0.59 GB written over 149 orders of N^2 elements:
-            # 14.19 B, the 14 B of slices plus the vectors); scaled to this launch
-            traffic_per_launch = 14.19 * elems * per_launch_orders
+            # and workload (N = 3720: 18.77 GB read + 0.61 GB written in one launch of
+            # 143.4 orders of N^2 elements, 9.77 B: the backward walk serves about 31 % of
+            # the 14 B of slices from L2); scaled to this launch's orders.  At other sizes
+            # the L2's share differs (N = 2790 fits in it), so no figure is claimed there
+            traffic_per_launch = 9.77 * elems * per_launch_orders
         if implicit and args.precision in ("fp64", "df64"):
             # DRAM traffic per matrix element and order measured by ncu on the same
             # kernel at N = 2790 (18.68 GB read + 0.11 GB written over 149 orders of
