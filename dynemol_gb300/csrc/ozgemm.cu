@@ -73,7 +73,18 @@ struct OperandView {
     bool kcontig;  // the K index runs along X's columns (X[j + r ld]) instead of its rows (X[r + j ld])
     int rows, k;
     int mask;      // 0: all; 1: zero for j > r; 2: zero for j < r
+    int tile;      // rows of the operand per output tile of the product (kTM for op(A), kTN for op(B)^T)
 };
+
+// The K range [lo, hi) the product reads for the rows of the output tile that
+// holds row r: the triangular mask of the tile's rows cut out to whole 64-K
+// blocks, as ozgemm_kernel's k range does.  Slices outside it are never read,
+// so the slicing kernels skip them (they are zero there in any case).
+__device__ __forceinline__ void read_range(const OperandView &v, int r, int &lo, int &hi) {
+    const int t0 = r / v.tile * v.tile;
+    lo = v.mask == 2 ? t0 / kKB * kKB : 0;
+    hi = v.mask == 1 ? (min(v.k, t0 + v.tile) + kKB - 1) / kKB * kKB : 1 << 30;
+}
 
 // 32 x 32 tile of the operand rows [r0, r0+32) x K [j0, j0+32) in shared memory
 // (t[rr][jj]), loaded along X's contiguous index; masked and out-of-range entries 0
@@ -113,8 +124,11 @@ __global__ void __launch_bounds__(256) oz_partmax_kernel(OperandView va, Operand
     const OperandView &v = isB ? vb : va;
     const int r0 = blockIdx.y * 32, j00 = blockIdx.x * chunk;
     if (r0 >= v.rows) return;
+    int lo, hi;  // the same for the 32 rows: they lie in one output tile
+    read_range(v, r0, lo, hi);
     double mx = 0.0;  // thread (x, y): row r0 + x over K columns y, y + 8, ... of each tile
     for (int j0 = j00; j0 < min(v.k, j00 + chunk); j0 += 32) {
+        if (j0 >= hi || j0 + 32 <= lo) continue;  // masked out: zero (uniform over the block)
         __syncthreads();
         load_tile(v, r0, j0, t);
         __syncthreads();
@@ -152,7 +166,10 @@ __global__ void __launch_bounds__(256) oz_slice_kernel(OperandView va, OperandVi
         if (blockIdx.x == 0 && r < v.rows) (isB ? scB : scA)[r] = pow2(e);
     }
     const size_t sstride = (size_t)v.rows * kp;
+    int lo, hi;  // the same for the 32 rows: they lie in one output tile
+    read_range(v, r0, lo, hi);
     for (int j0 = j00; j0 < min(kp, j00 + chunk); j0 += 32) {
+        if (j0 >= hi || j0 + 32 <= lo) continue;  // never read by the product (uniform over the block)
         __syncthreads();
         load_tile(v, r0, j0, t);
         __syncthreads();
@@ -456,9 +473,9 @@ cudaError_t ozgemm(int m, int n, int k, double alpha, const double *A, int lda, 
     Lane &ln = g_lane[lane];
     const int kp = round_up(k, 8);  // 16-byte row stride of the slices
     // op(A) rows: A(i, l) (K along A's rows) or A^T: A(l, i) (K along A's columns)
-    const OperandView va{A, lda, transA, m, k, (tri & kTriA) ? 1 : (tri & kTriAt) ? 2 : 0};
+    const OperandView va{A, lda, transA, m, k, (tri & kTriA) ? 1 : (tri & kTriAt) ? 2 : 0, kTM};
     // op(B) columns: B(l, j) (K along B's columns) or B^T: B(j, l) (K along B's rows)
-    const OperandView vb{B, ldb, !transB, n, k, (tri & kTriB) ? 2 : (tri & kTriBt) ? 1 : 0};
+    const OperandView vb{B, ldb, !transB, n, k, (tri & kTriB) ? 2 : (tri & kTriBt) ? 1 : 0, kTN};
     // op(B) = op(A)^T (the Schur update L21 L21^T): op(B)^T has op(A)'s rows, so
     // one set of slices and scales serves both operands
     const bool same = A == B && lda == ldb && va.kcontig == vb.kcontig && m == n && va.mask == vb.mask;
