@@ -308,3 +308,56 @@ def test_partial_sums_round_to_fp64():
         assert abs(total) < 2 ** 116
         d = i128_to_double(total)
         assert abs(Fraction(d) - total) <= 2 * abs(Fraction(total)) * Fraction(1, 2 ** 53)
+
+
+def _gemm_kblocks(m, n, k, tri, bx, by):
+    """ozgemm_kernel's K blocks [kb0, kb1) for output tile (bx, by) (128 x 32)."""
+    TM, TN, KBK = 128, 32, 64
+    i0, j0 = bx * TM, by * TN
+    klo, khi = 0, k
+    if tri & 1:    # kTriA
+        khi = min(khi, i0 + TM)
+    if tri & 16:   # kTriAt
+        klo = max(klo, i0)
+    if tri & 2:    # kTriB
+        klo = max(klo, j0)
+    if tri & 4:    # kTriBt
+        khi = min(khi, j0 + TN)
+    kb0 = klo // KBK
+    kb1 = -(-khi // KBK) if khi > klo else kb0
+    return kb0, kb1
+
+
+def _read_range(mask, tile, k, r):
+    """The slicing kernels' read_range: the K range a row's output tile reads."""
+    t0 = r // tile * tile
+    lo = t0 // 64 * 64 if mask == 2 else 0
+    hi = -(-min(k, t0 + tile) // 64) * 64 if mask == 1 else 1 << 30
+    return lo, hi
+
+
+def test_slicing_covers_every_k_block_the_product_reads():
+    """The slicing kernels skip a triangular operand's 32-column tiles outside
+    read_range; every K block ozgemm_kernel loads for an output tile must lie
+    inside the range of every row of both operand tiles (op(A): 128 rows, op(B)^T:
+    32 rows), for each triangular flag and ragged sizes."""
+    src = OZG
+    assert "lo = v.mask == 2 ? t0 / kKB * kKB : 0;" in src
+    assert "hi = v.mask == 1 ? (min(v.k, t0 + v.tile) + kKB - 1) / kKB * kKB : 1 << 30;" in src
+    assert "if (g.tri & kTriA) khi = min(khi, i0 + kTM);" in src
+    assert "if (g.tri & kTriBt) khi = min(khi, j0 + kTN);" in src
+    masks = {0: (0, 0), 1: (1, 0), 16: (2, 0), 2: (0, 2), 4: (0, 1), 1 | 4: (1, 1), 16 | 2: (2, 2)}
+    for (m, n, k) in [(320, 320, 320), (448, 1000, 1920), (1800, 1920, 1920), (1000, 333, 777), (130, 97, 64)]:
+        for tri, (ma, mb) in masks.items():
+            for bx in range(-(-m // 128)):
+                for by in range(-(-n // 32)):
+                    kb0, kb1 = _gemm_kblocks(m, n, k, tri, bx, by)
+                    if kb1 <= kb0:
+                        continue
+                    K0, K1 = 64 * kb0, 64 * kb1
+                    for r in range(bx * 128, min(m, bx * 128 + 128), 32):
+                        lo, hi = _read_range(ma, 128, k, r)
+                        assert lo <= K0 and K1 <= hi, ("A", m, n, k, tri, bx, r)
+                    for r in range(by * 32, min(n, by * 32 + 32), 32):
+                        lo, hi = _read_range(mb, 32, k, r)
+                        assert lo <= K0 and K1 <= hi, ("B", m, n, k, tri, by, r)
