@@ -1,7 +1,8 @@
 """Build libelhlprop.so in-tree with nvcc for sm_103a (no cmake, no torch).
 
 Translation units compile in parallel, then one link step.  The library links
-the CUDA runtime and cuSOLVER (Cholesky of S) dynamically.
+the CUDA runtime, cuBLAS (the FP32 GEMM regime) and cuSOLVER (the generalised
+eigensolver of a trajectory's initial fragment state) dynamically.
 """
 from __future__ import annotations
 
