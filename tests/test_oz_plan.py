@@ -361,3 +361,30 @@ def test_slicing_covers_every_k_block_the_product_reads():
                     for r in range(by * 32, min(n, by * 32 + 32), 32):
                         lo, hi = _read_range(mb, 32, k, r)
                         assert lo <= K0 and K1 <= hi, ("B", m, n, k, tri, by, r)
+
+
+def test_half_chunk_epilogue_covers_the_chunk_once():
+    """The chunk epilogue runs in two halves of 4 columns on different CTAs:
+    thread t of half c owns row t & 63 and columns 4 c + 2 (t >> 6) + {0, 1}
+    (one complex column); together the halves own every (row, column) of the
+    64 x 8 chunk once, and their 16-byte copies of slots 1-7 cover the tile's
+    rows 8 (b + 1) + column without overlap and never touch the zero slots 0, 8."""
+    assert "return EpiThread{t, t & 63, t >> 6, 64 * h + (t & 63), 4 * c + 2 * (t >> 6)};" in OZ
+    assert "const int o = (8 * (1 + q / 32) + 4 * half + (q / 8) % 4) * 128 + (q % 8) * 16;" in OZ
+    assert "constexpr int kPieces = kS * 4 * 8;" in OZ
+    own = np.zeros((64, 8), dtype=int)
+    for c in range(2):
+        for t in range(128):
+            r, col = t & 63, 4 * c + 2 * (t >> 6)
+            own[r, col] += 1
+            own[r, col + 1] += 1
+            assert col // 2 == 2 * c + (t >> 6)  # the complex column the thread accumulates
+    assert np.all(own == 1)
+    tile = np.zeros(9 * 8 * 128, dtype=int)  # 9 slots x 8 rows x 128 bytes
+    for half in range(2):
+        for q in range(S * 4 * 8):
+            o = (8 * (1 + q // 32) + 4 * half + (q // 8) % 4) * 128 + (q % 8) * 16
+            tile[o:o + 16] += 1
+    rows = tile.reshape(9 * 8, 128)
+    assert np.all(rows[8:64] == 1)                   # slots 1-7: every byte copied once
+    assert np.all(rows[:8] == 0) and np.all(rows[64:] == 0)  # the zero slots are never written
