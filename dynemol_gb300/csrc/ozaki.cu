@@ -9,7 +9,7 @@
 //   a = 2^e  sum_{s<7} n_s 2^(-8(s+1)),   n_s integers, |n_0| <= 256, |n_s| <= 128,
 //
 // which represents a to 2^-57 relative to the scale.  An operator row has one
-// scale; a vector column has one per 128-row chunk.  Each n_s is exact in BF16,
+// scale; a vector column has one per 64-row chunk.  Each n_s is exact in BF16,
 // each product of two slices is an integer below 2^16, and a sum of 256 of them
 // an integer below 2^24: a BF16 tcgen05.mma with FP32 accumulation computes
 // slice products exactly as long as the sums stay below 2^24.  The products with s_a + s_b <= 6
